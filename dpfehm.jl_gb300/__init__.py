@@ -1,0 +1,412 @@
+"""GB300-native groundwater solve with DPFEHM.jl's interface.
+
+Host-side mirror of the reference's groundwater API (DPFEHM.jl
+src/groundwater.jl:75-109, src/utilities.jl:10-40, src/grid.jl) on top of the
+C ABI of libdpfehm_gpu.so. Every solve, assembly and gradient runs in the
+library's sm_103a kernels; this module only marshals arrays. Indices are 0-based
+(the reference is 1-based Julia).
+
+    h = groundwater_steadystate(Ks, neighbors, areasoverlengths, dirichletnodes, dirichleths, Qs)
+    h, pullback = rrule_groundwater_steadystate(Ks, neighbors, areasoverlengths, dirichletnodes, dirichleths, Qs)
+    _, dKs, _, _, _, ddirichleths, dQs = pullback(delta)
+
+Arrays may be numpy arrays (host) or torch CUDA tensors (used in place on the
+device); outputs follow the type of ``Ks`` / ``logK``.
+"""
+import ctypes
+import hashlib
+import warnings
+from collections import OrderedDict
+
+import numpy as np
+
+from . import _lib
+from . import fields, grid
+from ._lib import MEAN_GEOMETRIC, MEAN_HARMONIC, PREC_FP64, PREC_MIXED, default_options, load
+from .grid import addboundaryconditions, getfreenodes, load_uge, regulargrid1d, regulargrid2d, regulargrid3d
+
+__all__ = [
+    "groundwater_steadystate", "rrule_groundwater_steadystate", "logKs2Ks_neighbors", "GroundwaterProblem",
+    "GroundwaterBatch", "DPFError", "NoTangent", "getfreenodes", "addboundaryconditions", "regulargrid1d",
+    "regulargrid2d", "regulargrid3d", "load_uge", "fields", "grid", "load", "default_options", "MEAN_GEOMETRIC",
+    "MEAN_HARMONIC", "PREC_FP64", "PREC_MIXED",
+]
+
+
+class DPFError(RuntimeError):
+    """A non-OK dpf_status; ``code`` holds the status, the message dpf_last_error()."""
+
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (_lib.STATUS_NAMES.get(code, str(code)), msg))
+        self.code = code
+
+
+class _NoTangent:
+    def __repr__(self):
+        return "NoTangent()"
+
+
+NoTangent = _NoTangent()
+
+_MEANS = {"geometric": MEAN_GEOMETRIC, "harmonic": MEAN_HARMONIC, MEAN_GEOMETRIC: MEAN_GEOMETRIC,
+          MEAN_HARMONIC: MEAN_HARMONIC}
+_PRECS = {"fp64": PREC_FP64, "mixed": PREC_MIXED, PREC_FP64: PREC_FP64, PREC_MIXED: PREC_MIXED}
+
+
+def _is_torch(x):
+    return type(x).__module__.startswith("torch")
+
+
+class _Buf:
+    """A contiguous float64/int64 buffer (numpy host array or torch CUDA tensor) and its address."""
+
+    def __init__(self, x, dtype=np.float64, n=None):
+        if _is_torch(x):
+            import torch
+            tdt = torch.float64 if dtype == np.float64 else torch.int64
+            t = x.detach()
+            if t.dtype != tdt:
+                t = t.to(tdt)
+            t = t.contiguous()
+            self.obj, self.ptr, self.device = t, t.data_ptr(), t.is_cuda
+        else:
+            a = np.ascontiguousarray(x, dtype=dtype)
+            self.obj, self.ptr, self.device = a, a.ctypes.data, False
+        self.size = self.obj.numel() if _is_torch(self.obj) else self.obj.size
+        if n is not None and self.size != n:
+            raise ValueError("expected %d entries, got %d" % (n, self.size))
+
+
+def _out(like, n, dtype=np.float64):
+    """Output buffer on the same side (host/device) as `like`."""
+    if like is not None and _is_torch(like.obj) and like.device:
+        import torch
+        t = torch.empty(n, dtype=torch.float64, device=like.obj.device)
+        return t, t.data_ptr()
+    a = np.empty(n, dtype=dtype)
+    return a, a.ctypes.data
+
+
+def _check(lib, h, rc, allow_not_converged=True):
+    if rc == _lib.DPF_OK:
+        return
+    msg = lib.dpf_last_error(h)
+    msg = msg.decode() if msg else ""
+    if rc == _lib.DPF_NOT_CONVERGED and allow_not_converged:
+        warnings.warn("groundwater solve did not reach reltol: " + msg, RuntimeWarning, stacklevel=3)
+        return
+    raise DPFError(rc, msg)
+
+
+def _options(reltol=None, maxiter=None, precision=None, **kw):
+    o = default_options()
+    if reltol is not None:
+        o.reltol = float(reltol)
+    if maxiter is not None:
+        o.maxiter = int(maxiter)
+    if precision is not None:
+        o.precision = _PRECS[precision]
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise TypeError("unknown solver option %r" % k)
+        setattr(o, k, v)
+    return o
+
+
+class GroundwaterProblem:
+    """One groundwater topology on the GPU (faces, areas over lengths, Dirichlet set).
+
+    Construct from the reference's arrays (``neighbors`` as an (F, 2) 0-based
+    array) or with :meth:`regular3d`. Face lists produced by ``regulargrid3d``
+    are recognised and solved matrix-free on the structured path.
+    """
+
+    def __init__(self, neighbors=None, areasoverlengths=None, dirichletnodes=(), N=None, volumes=None, _handle=None,
+                 **options):
+        self._lib = load()
+        if _handle is not None:
+            self._h = _handle
+        else:
+            nb = np.ascontiguousarray(np.asarray(neighbors, dtype=np.int64).reshape(-1, 2))
+            F = nb.shape[0]
+            if N is None:
+                raise ValueError("N (number of cells) is required")
+            a = np.ascontiguousarray(nb[:, 0])
+            b = np.ascontiguousarray(nb[:, 1])
+            aol = np.ascontiguousarray(np.asarray(areasoverlengths, dtype=np.float64)[:F])
+            dn = np.ascontiguousarray(np.asarray(dirichletnodes, dtype=np.int64))
+            vol = None if volumes is None else np.ascontiguousarray(volumes, dtype=np.float64)
+            h = ctypes.c_void_p()
+            o = _options(**options)
+            rc = self._lib.dpf_create(int(N), F, a.ctypes.data, b.ctypes.data, aol.ctypes.data,
+                                      None if vol is None else vol.ctypes.data, dn.size, dn.ctypes.data,
+                                      ctypes.byref(o), ctypes.byref(h))
+            if rc != _lib.DPF_OK:
+                raise DPFError(rc, self._lib.dpf_last_error(None).decode())
+            self._h = h
+        self._info()
+
+    @classmethod
+    def regular3d(cls, mins, maxs, ns, dirichletnodes=(), **options):
+        lib = load()
+        mn = np.ascontiguousarray(mins, dtype=np.float64)
+        mx = np.ascontiguousarray(maxs, dtype=np.float64)
+        dn = np.ascontiguousarray(np.asarray(dirichletnodes, dtype=np.int64))
+        h = ctypes.c_void_p()
+        o = _options(**options)
+        rc = lib.dpf_create_regular3d(int(ns[0]), int(ns[1]), int(ns[2]), mn.ctypes.data, mx.ctypes.data, dn.size,
+                                      dn.ctypes.data, ctypes.byref(o), ctypes.byref(h))
+        if rc != _lib.DPF_OK:
+            raise DPFError(rc, lib.dpf_last_error(None).decode())
+        return cls(_handle=h)
+
+    def _info(self):
+        N, F, nf = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        st, lv = ctypes.c_int(), ctypes.c_int()
+        self._lib.dpf_info(self._h, ctypes.byref(N), ctypes.byref(F), ctypes.byref(nf), ctypes.byref(st),
+                           ctypes.byref(lv))
+        self.N, self.F, self.nfree = N.value, F.value, nf.value
+        self.structured, self.levels = bool(st.value), lv.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.dpf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stats(self):
+        it, ou, rr = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        self._lib.dpf_last_stats(self._h, ctypes.byref(it), ctypes.byref(ou), ctypes.byref(rr))
+        return {"iterations": it.value, "outer": ou.value, "relres": rr.value}
+
+    # ---- diagnostics
+    def profile(self, enable=True):
+        """Start/stop per-kernel CUDA-event timing on the handle's stream."""
+        self._lib.dpf_profile(self._h, 1 if enable else 0)
+
+    def profile_report(self):
+        """{kernel name: (launches, total ms, total scheduled cells)} since profile(True)."""
+        cap = 256
+        names = (ctypes.c_char_p * cap)()
+        cnt = (ctypes.c_longlong * cap)()
+        ms = (ctypes.c_double * cap)()
+        cells = (ctypes.c_longlong * cap)()
+        n = self._lib.dpf_profile_report(self._h, cap, names, cnt, ms, cells)
+        if n < 0:
+            raise DPFError(-n, self._lib.dpf_last_error(self._h).decode())
+        return {names[k].decode(): (cnt[k], ms[k], cells[k]) for k in range(min(n, cap))}
+
+    @property
+    def launch_count(self):
+        return int(self._lib.dpf_launch_count(self._h))
+
+    # ---- steady state
+    def forward(self, Ks, dirichleths, Qs):
+        K = _Buf(Ks, n=self.F)
+        d = _Buf(dirichleths, n=self.N)
+        q = _Buf(Qs, n=self.N)
+        h, hp = _out(K, self.N)
+        _check(self._lib, self._h, self._lib.dpf_steady_forward(self._h, K.ptr, d.ptr, q.ptr, hp))
+        return h
+
+    def adjoint(self, delta):
+        dl = _Buf(delta, n=self.N)
+        dK, dKp = _out(dl, self.F)
+        ddh, ddhp = _out(dl, self.N)
+        dQ, dQp = _out(dl, self.N)
+        _check(self._lib, self._h, self._lib.dpf_steady_adjoint(self._h, dl.ptr, dKp, ddhp, dQp))
+        return dK, ddh, dQ
+
+    def forward_logk(self, logK, dirichleths, Qs, mean="geometric"):
+        lk = _Buf(logK, n=self.N)
+        d = _Buf(dirichleths, n=self.N)
+        q = _Buf(Qs, n=self.N)
+        h, hp = _out(lk, self.N)
+        _check(self._lib, self._h, self._lib.dpf_steady_forward_logk(self._h, lk.ptr, _MEANS[mean], d.ptr, q.ptr, hp))
+        return h
+
+    def adjoint_logk(self, delta):
+        dl = _Buf(delta, n=self.N)
+        g, gp = _out(dl, self.N)
+        ddh, ddhp = _out(dl, self.N)
+        dQ, dQp = _out(dl, self.N)
+        _check(self._lib, self._h, self._lib.dpf_steady_adjoint_logk(self._h, dl.ptr, gp, ddhp, dQp))
+        return g, ddh, dQ
+
+    def solve_grad_logk(self, logK, dirichleths, Qs, obs, mean="geometric"):
+        """Forward solve, J = sum(h[obs]^2), adjoint; returns (h, dJ/dlogK)."""
+        lk = _Buf(logK, n=self.N)
+        d = _Buf(dirichleths, n=self.N)
+        q = _Buf(Qs, n=self.N)
+        ob = np.ascontiguousarray(obs, dtype=np.int64)
+        h, hp = _out(lk, self.N)
+        g, gp = _out(lk, self.N)
+        _check(self._lib, self._h, self._lib.dpf_solve_grad_logk(self._h, lk.ptr, _MEANS[mean], d.ptr, q.ptr, ob.size,
+                                                                 ob.ctypes.data, hp, gp))
+        return h, g
+
+    def logk_to_faces(self, logK, mean="geometric"):
+        lk = _Buf(logK, n=self.N)
+        K, Kp = _out(lk, self.F)
+        _check(self._lib, self._h, self._lib.dpf_logk_to_faces(self._h, lk.ptr, _MEANS[mean], Kp))
+        return K
+
+    def logk_to_faces_vjp(self, logK, dKs, mean="geometric"):
+        lk = _Buf(logK, n=self.N)
+        dk = _Buf(dKs, n=self.F)
+        g, gp = _out(lk, self.N)
+        _check(self._lib, self._h, self._lib.dpf_logk_to_faces_vjp(self._h, lk.ptr, _MEANS[mean], dk.ptr, gp))
+        return g
+
+    def apply(self, x):
+        xb = _Buf(x, n=self.N)
+        y, yp = _out(xb, self.N)
+        _check(self._lib, self._h, self._lib.dpf_apply_operator(self._h, xb.ptr, yp))
+        return y
+
+    # ---- transient
+    def transient_forward(self, Ks, dirichleths, Qs, specificstorage, dt, nsteps, h0, checkpoint_every=1,
+                          return_states=False):
+        K = _Buf(Ks, n=self.F)
+        d = _Buf(dirichleths, n=self.N)
+        q = _Buf(Qs, n=self.N)
+        s = _Buf(specificstorage, n=self.N)
+        h0b = _Buf(h0, n=self.N)
+        hT, hTp = _out(K, self.N)
+        states, sp = (None, None)
+        if return_states:
+            states, sp = _out(K, int(nsteps) * self.N)
+        _check(self._lib, self._h, self._lib.dpf_transient_forward(self._h, K.ptr, d.ptr, q.ptr, s.ptr, float(dt),
+                                                                   int(nsteps), h0b.ptr, int(checkpoint_every), sp,
+                                                                   hTp))
+        if return_states:
+            return hT, states.reshape(int(nsteps), self.N)
+        return hT
+
+    def transient_adjoint(self, obs, weights=None, gT=None):
+        ob = np.ascontiguousarray(obs, dtype=np.int64)
+        w = None if weights is None else _Buf(weights, n=ob.size)
+        g = None if gT is None else _Buf(gT, n=self.N)
+        like = w or g
+        dK, dKp = _out(like, self.F)
+        ddh, ddhp = _out(like, self.N)
+        dQ, dQp = _out(like, self.N)
+        dh0, dh0p = _out(like, self.N)
+        _check(self._lib, self._h, self._lib.dpf_transient_adjoint(self._h, ob.size, ob.ctypes.data,
+                                                                   None if w is None else w.ptr,
+                                                                   None if g is None else g.ptr, dKp, ddhp, dQp,
+                                                                   dh0p))
+        return dK, ddh, dQ, dh0
+
+
+class GroundwaterBatch(GroundwaterProblem):
+    """Many independent regular grids (uneven sizes allowed) solved in one set of launches."""
+
+    def __init__(self, dims, mins, maxs, dirichletnodes, **options):
+        lib = load()
+        dims = np.ascontiguousarray(np.asarray(dims, dtype=np.int32).reshape(-1, 3))
+        nprob = dims.shape[0]
+        mn = np.ascontiguousarray(np.asarray(mins, dtype=np.float64).reshape(nprob, 3))
+        mx = np.ascontiguousarray(np.asarray(maxs, dtype=np.float64).reshape(nprob, 3))
+        nd = np.ascontiguousarray([len(d) for d in dirichletnodes], dtype=np.int64)
+        dn = np.ascontiguousarray(np.concatenate([np.asarray(d, dtype=np.int64) for d in dirichletnodes])
+                                  if nd.sum() else np.zeros(0, np.int64))
+        h = ctypes.c_void_p()
+        o = _options(**options)
+        rc = lib.dpf_batch_create(nprob, dims.ctypes.data, mn.ctypes.data, mx.ctypes.data, nd.ctypes.data,
+                                  dn.ctypes.data, ctypes.byref(o), ctypes.byref(h))
+        if rc != _lib.DPF_OK:
+            raise DPFError(rc, lib.dpf_last_error(None).decode())
+        super().__init__(_handle=h)
+        self.nprob = nprob
+        co, fo = ctypes.c_int64(), ctypes.c_int64()
+        self.cell_offsets = np.zeros(nprob + 1, np.int64)
+        self.face_offsets = np.zeros(nprob + 1, np.int64)
+        for p in range(nprob + 1):
+            lib.dpf_batch_offsets(self._h, p, ctypes.byref(co), ctypes.byref(fo))
+            self.cell_offsets[p], self.face_offsets[p] = co.value, fo.value
+
+    def solve_grad_logk(self, logK, dirichleths, Qs, obs_per_problem, mean="geometric"):
+        lk = _Buf(logK, n=self.N)
+        d = _Buf(dirichleths, n=self.N)
+        q = _Buf(Qs, n=self.N)
+        offs = np.zeros(self.nprob + 1, np.int64)
+        offs[1:] = np.cumsum([len(o) for o in obs_per_problem])
+        ob = np.ascontiguousarray(np.concatenate([np.asarray(o, np.int64) for o in obs_per_problem])
+                                  if offs[-1] else np.zeros(0, np.int64))
+        h, hp = _out(lk, self.N)
+        g, gp = _out(lk, self.N)
+        _check(self._lib, self._h, self._lib.dpf_batch_solve_grad_logk(self._h, lk.ptr, _MEANS[mean], d.ptr, q.ptr,
+                                                                       offs.ctypes.data, ob.ctypes.data, hp, gp))
+        return h, g
+
+
+# ------------------------------------------------------ reference-shaped API
+_cache = OrderedDict()
+_CACHE_MAX = 8
+
+
+def _problem_for(neighbors, areasoverlengths, dirichletnodes, N, options):
+    nb = np.ascontiguousarray(np.asarray(neighbors, dtype=np.int64).reshape(-1, 2))
+    aol = np.ascontiguousarray(np.asarray(areasoverlengths, dtype=np.float64)[: nb.shape[0]])
+    dn = np.ascontiguousarray(np.asarray(dirichletnodes, dtype=np.int64))
+    hsh = hashlib.blake2b(digest_size=16)
+    for arr in (nb, aol, dn):
+        hsh.update(arr.tobytes())
+    key = (int(N), hsh.hexdigest(), tuple(sorted(options.items())))
+    P = _cache.get(key)
+    if P is None:
+        P = GroundwaterProblem(nb, aol, dn, N=N, **options)
+        _cache[key] = P
+        while len(_cache) > _CACHE_MAX:
+            _cache.popitem(last=False)
+    else:
+        _cache.move_to_end(key)
+    return P
+
+
+def groundwater_steadystate(Ks, neighbors, areasoverlengths, dirichletnodes, dirichleths, Qs, *, linear_solver=None,
+                            **kwargs):
+    """Steady-state heads over all cells (src/groundwater.jl:75-83).
+
+    ``linear_solver`` is accepted for signature compatibility and ignored: the
+    solve is always the GPU's AMG-preconditioned CG. ``kwargs`` are solver
+    options (reltol, maxiter, precision='fp64'|'mixed', ...).
+    """
+    N = len(Qs) if not _is_torch(Qs) else Qs.numel()
+    P = _problem_for(neighbors, areasoverlengths, dirichletnodes, N, kwargs)
+    return P.forward(Ks, dirichleths, Qs)
+
+
+def rrule_groundwater_steadystate(Ks, neighbors, areasoverlengths, dirichletnodes, dirichleths, Qs, **kwargs):
+    """(h, pullback) like ChainRulesCore.rrule (src/groundwater.jl:85-109).
+
+    pullback(delta) returns (NoTangent, dKs, NoTangent, NoTangent, NoTangent,
+    ddirichleths, dQs). The handle (and so the solved state and hierarchy)
+    lives as long as the pullback closure.
+    """
+    N = len(Qs) if not _is_torch(Qs) else Qs.numel()
+    P = GroundwaterProblem(neighbors, areasoverlengths, dirichletnodes, N=N, **kwargs)
+    h = P.forward(Ks, dirichleths, Qs)
+
+    def pullback(delta):
+        dKs, ddh, dQs = P.adjoint(delta)
+        return (NoTangent, dKs, NoTangent, NoTangent, NoTangent, ddh, dQs)
+
+    pullback.problem = P
+    return h, pullback
+
+
+def logKs2Ks_neighbors(logKs, neighbors, mean="geometric", N=None):
+    """Face conductances from cell log-conductivities on the GPU
+    (geometric: examples/gw_steadystate_3d/inputdeck.jl:51; harmonic: src/richards.jl:50-52)."""
+    N = N if N is not None else (logKs.numel() if _is_torch(logKs) else len(logKs))
+    nb = np.asarray(neighbors, dtype=np.int64).reshape(-1, 2)
+    P = _problem_for(nb, np.ones(nb.shape[0]), [], N, {})
+    return P.logk_to_faces(logKs, mean)

@@ -1,0 +1,72 @@
+// dpf_internal.h -- shared declarations of the GB300 groundwater library.
+//
+// Data layout in HBM (structured path). A batch of nprob regular grids is
+// stored level by level; at every multigrid level the cells of all problems
+// that have that level are concatenated (problem order), each grid in the
+// reference's order (z fastest, then y, then x; src/grid.jl:151). Per cell and
+// level the operator is four structure-of-arrays values:
+//   cx, cy, cz : conductance K*aol of the +x/+y/+z face (0 when the face does
+//                not exist or touches a Dirichlet cell)
+//   leak       : the part of the diagonal not carried by cx/cy/cz (faces to
+//                Dirichlet cells, storage/dt in transient runs); 1 for a
+//                Dirichlet cell, whose row is the identity.
+// The operator is applied in flux form, y_i = leak_i x_i + sum_f c_f (x_i - x_j),
+// which avoids the cancellation of diag*x - sum c*x for smooth x.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/dpfehm_gpu.h"
+
+namespace dpf {
+
+constexpr int kBlock = 256;        // threads per block of every cell-parallel kernel
+constexpr int kMaxCoarse = 64;     // largest dense coarsest level (cells)
+
+struct LevelDesc {                 // one problem at one level
+    int nx, ny, nz, pad;
+    long long n;                   // cells
+    long long off;                 // offset of the problem's cells in the level arrays
+};
+
+struct BlockMap {                  // launch map: block -> (problem, block within problem)
+    int2 *d_map = nullptr;         // [nblocks]
+    int2 *d_pinfo = nullptr;       // [nprob] {first block, number of blocks} (0,0 if absent)
+    int nblocks = 0;
+};
+
+// Per-problem CG state, device resident. Scalars are FP64 whatever the vector type.
+struct CgState {
+    double rz, rz_old, pq, rr, bb, tol2;
+    double alpha, beta;
+    double scale;                  // mixed precision: norm used to normalise the inner rhs
+    double ee, hh;                 // mixed precision: correction / solution norms of the last step
+    double orr, obb;               // mixed precision: outer (FP64) residual and rhs norms squared
+    int iters, active, status, outer;
+    int outer_active, total_iters, pad1, pad2;
+};
+
+// Reduction scratch: one double2 partial per block of the widest launch, one
+// ticket counter per problem; the last block of each problem sums the partials
+// in a fixed order (deterministic) and finalises that problem's scalars.
+struct ReduceScratch {
+    double2 *partials = nullptr;
+    unsigned *tickets = nullptr;
+    int capacity = 0;
+};
+
+struct ProbParam {                 // per-problem constants of a regular grid
+    double aol[3];                 // areas over lengths of +x, +y, +z faces
+    double vol;                    // cell volume (transient storage term)
+    long long face_off;            // offset of the problem's faces in concatenated face arrays
+    long long F;                   // faces of the problem
+};
+
+template <typename T>
+struct Coeffs {
+    const T *cx, *cy, *cz, *leak;
+};
+
+}  // namespace dpf

@@ -1,0 +1,1243 @@
+// dpf_struct.cu -- structured-grid groundwater solver for sm_103a.
+//
+// A StructBatch holds nprob regular grids (a single problem is a batch of one):
+// the multigrid hierarchy (2x2x2 aggregation, Galerkin 7-point coarse operators,
+// dense Cholesky coarsest level), the CG / iterative-refinement state, and the
+// kernels that solve and differentiate
+//   A h = b,   A = groundwater_h, b = -groundwater_residuals(0)   (src/groundwater.jl:75-83)
+//   A lambda = delta[free]                                        (src/groundwater.jl:93-107)
+// for every problem at once. Converged problems drop out of the launches (their
+// blocks exit at entry), so uneven batches cost what their unconverged members cost.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <set>
+#include <stdexcept>
+
+#include "dpf_struct.h"
+#include "dpf_struct_kernels.cuh"
+
+namespace dpf {
+
+// ================================================================ kernels
+#define DPF_BLOCK_PROLOGUE(DESC, BMAP, ST)                 \
+    int2 bm = (BMAP)[blockIdx.x];                          \
+    const int p = bm.x;                                    \
+    if ((ST) && !(ST)[p].active) return;                   \
+    const LevelDesc L = (DESC)[p];
+
+__device__ __forceinline__ void deactivate(CgState &s, int *count) {
+    if (s.active) {
+        s.active = 0;
+        atomicSub(count, 1);
+    }
+}
+
+template <typename T>
+__global__ void k_cheb_first(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+                             Coeffs<T> C, const T *__restrict__ b, T *__restrict__ x, T *__restrict__ d,
+                             T invtheta) {
+    DPF_BLOCK_PROLOGUE(desc, bmap, st)
+    Cell c;
+    if (!decode_cell(L, bm.y, c)) return;
+    T v = invtheta * b[c.i] / diag7(L, c, C);
+    x[c.i] = v;
+    d[c.i] = v;
+}
+
+// One Chebyshev step on D^-1 A: r = D^-1 (b - A xin); d = c1 d + c2 r; xout = xin + d.
+// With FUSE_RZ the kernel is the last of the level-0 V-cycle: it also reduces b . xout
+// (b is the CG residual, xout the preconditioned residual) and finalises beta.
+template <typename T, bool FUSE_RZ>
+__global__ void k_cheb_step(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+                            Coeffs<T> C, const T *__restrict__ b, const T *__restrict__ xin, T *__restrict__ xout,
+                            T *__restrict__ d, T c1, T c2, ReduceScratch rs, const int2 *__restrict__ pinfo) {
+    DPF_BLOCK_PROLOGUE(desc, bmap, st)
+    Cell c;
+    double part = 0.0;
+    if (decode_cell(L, bm.y, c)) {
+        T xi = xin[c.i], Ax, dg;
+        apply7(L, c, C, xi, [&](long long j, int, int, int) { return xin[j]; }, Ax, dg);
+        T bi = b[c.i];
+        T r = (bi - Ax) / dg;
+        T dn = c1 * d[c.i] + c2 * r;
+        T xo = xi + dn;
+        d[c.i] = dn;
+        xout[c.i] = xo;
+        if (FUSE_RZ) part = (double)bi * (double)xo;
+    }
+    if (FUSE_RZ) {
+        double2 tot;
+        if (reduce_last(part, 0.0, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+            CgState &s = st[p];
+            s.rz_old = s.rz;
+            s.rz = tot.x;
+            s.beta = (s.iters == 0 || s.rz_old == 0.0) ? 0.0 : s.rz / s.rz_old;
+        }
+    }
+}
+
+// Restriction of the residual: bc[I] = sum over the children i of I of (b_i - (A x)_i).
+template <typename T>
+__global__ void k_restrict(const LevelDesc *__restrict__ fdesc, const LevelDesc *__restrict__ cdesc,
+                           const int2 *__restrict__ bmap, CgState *st, Coeffs<T> C, const T *__restrict__ b,
+                           const T *__restrict__ x, T *__restrict__ bc) {
+    int2 bm = bmap[blockIdx.x];
+    const int p = bm.x;
+    if (st && !st[p].active) return;
+    const LevelDesc Lc = cdesc[p];
+    Cell cc;
+    if (!decode_cell(Lc, bm.y, cc)) return;
+    const LevelDesc L = fdesc[p];
+    const long long fsy = L.nz, fsx = (long long)L.ny * L.nz;
+    int x0 = 2 * cc.ix, y0 = 2 * cc.iy, z0 = 2 * cc.iz;
+    int x1 = min(x0 + 1, L.nx - 1), y1 = min(y0 + 1, L.ny - 1), z1 = min(z0 + 1, L.nz - 1);
+    T acc = 0;
+    for (int fx = x0; fx <= x1; fx++)
+        for (int fy = y0; fy <= y1; fy++)
+            for (int fz = z0; fz <= z1; fz++) {
+                Cell c;
+                c.ix = fx; c.iy = fy; c.iz = fz;
+                c.i = L.off + fx * fsx + fy * fsy + fz;
+                T xi = x[c.i], Ax, dg;
+                apply7(L, c, C, xi, [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
+                acc += b[c.i] - Ax;
+            }
+    bc[cc.i] = acc;
+}
+
+// Prolongation of the coarse correction fused with the first post-smoothing step:
+// x' = x + s * e[aggregate] (not at identity rows), r = D^-1 (b - A x'),
+// d = invtheta r, xout = x' + d.
+template <typename T, bool FUSE_RZ>
+__global__ void k_prolong_cheb(const LevelDesc *__restrict__ desc, const LevelDesc *__restrict__ cdesc,
+                               const int2 *__restrict__ bmap, CgState *st, Coeffs<T> C,
+                               const uint8_t *__restrict__ dir, const T *__restrict__ b, const T *__restrict__ x,
+                               const T *__restrict__ e, T *__restrict__ xout, T *__restrict__ d, T scale,
+                               T invtheta, ReduceScratch rs, const int2 *__restrict__ pinfo) {
+    DPF_BLOCK_PROLOGUE(desc, bmap, st)
+    const LevelDesc Lc = cdesc[p];
+    Cell c;
+    double part = 0.0;
+    if (decode_cell(L, bm.y, c)) {
+        auto xp = [&](long long j, int jx, int jy, int jz) -> T {
+            T v = x[j];
+            if (!dir[j]) v += scale * e[Lc.off + ((long long)(jx >> 1) * Lc.ny + (jy >> 1)) * Lc.nz + (jz >> 1)];
+            return v;
+        };
+        T xi = xp(c.i, c.ix, c.iy, c.iz), Ax, dg;
+        apply7(L, c, C, xi, xp, Ax, dg);
+        T bi = b[c.i];
+        T dn = invtheta * (bi - Ax) / dg;
+        T xo = xi + dn;
+        d[c.i] = dn;
+        xout[c.i] = xo;
+        if (FUSE_RZ) part = (double)bi * (double)xo;
+    }
+    if (FUSE_RZ) {
+        double2 tot;
+        if (reduce_last(part, 0.0, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+            CgState &s = st[p];
+            s.rz_old = s.rz;
+            s.rz = tot.x;
+            s.beta = (s.iters == 0 || s.rz_old == 0.0) ? 0.0 : s.rz / s.rz_old;
+        }
+    }
+}
+
+// Coarsest level: x = A^-1 b with the stored Cholesky factor, one warp per problem.
+// With FUSE_RZ (a problem whose finest level is its coarsest) it also sets rz and beta.
+template <typename T, bool FUSE_RZ>
+__global__ void k_coarse_solve(const LevelDesc *__restrict__ desc, const int *__restrict__ plist, CgState *st,
+                               const double *__restrict__ Lbuf, const T *__restrict__ b, T *__restrict__ x) {
+    const int p = plist[blockIdx.x];
+    if (st && !st[p].active) return;
+    const LevelDesc L = desc[p];
+    const int n = (int)L.n;
+    const double *Lp = Lbuf + (long long)p * kMaxCoarse * kMaxCoarse;
+    __shared__ double y[kMaxCoarse];
+    const int lane = threadIdx.x;
+    if (threadIdx.x >= 32) return;
+    for (int i = 0; i < n; i++) {
+        double s = 0.0;
+        for (int k = lane; k < i; k += 32) s += Lp[i * kMaxCoarse + k] * y[k];
+        s = warp_sum(s);
+        if (lane == 0) y[i] = ((double)b[L.off + i] - s) / Lp[i * kMaxCoarse + i];
+        __syncwarp();
+    }
+    for (int i = n - 1; i >= 0; i--) {
+        double s = 0.0;
+        for (int k = i + 1 + lane; k < n; k += 32) s += Lp[k * kMaxCoarse + i] * y[k];
+        s = warp_sum(s);
+        if (lane == 0) y[i] = (y[i] - s) / Lp[i * kMaxCoarse + i];
+        __syncwarp();
+    }
+    double rz = 0.0;
+    for (int i = lane; i < n; i += 32) {
+        x[L.off + i] = (T)y[i];
+        if (FUSE_RZ) rz += (double)b[L.off + i] * (double)(T)y[i];
+    }
+    if (FUSE_RZ) {
+        rz = warp_sum(rz);
+        if (lane == 0) {
+            CgState &s = st[p];
+            s.rz_old = s.rz;
+            s.rz = rz;
+            s.beta = (s.iters == 0 || s.rz_old == 0.0) ? 0.0 : s.rz / s.rz_old;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- CG kernels
+// r = b - A x; reduce (r.r, b.b); activate the problem unless already converged.
+template <typename T>
+__global__ void k_cg_start(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+                           int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, Coeffs<T> C,
+                           const T *__restrict__ b, const T *__restrict__ x, T *__restrict__ r, double tol2,
+                           int gated) {
+    int2 bm = bmap[blockIdx.x];
+    const int p = bm.x;
+    if (gated && !st[p].outer_active) return;
+    const LevelDesc L = desc[p];
+    Cell c;
+    double rr = 0.0, bb = 0.0;
+    if (decode_cell(L, bm.y, c)) {
+        T xi = x[c.i], Ax, dg;
+        apply7(L, c, C, xi, [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
+        T bi = b[c.i];
+        T ri = bi - Ax;
+        r[c.i] = ri;
+        rr = (double)ri * (double)ri;
+        bb = (double)bi * (double)bi;
+    }
+    double2 tot;
+    if (reduce_last(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+        CgState &s = st[p];
+        s.rr = tot.x;
+        s.bb = tot.y;
+        s.tol2 = tol2;
+        s.iters = 0;
+        s.rz = 0.0;
+        s.rz_old = 0.0;
+        s.beta = 0.0;
+        s.status = DPF_OK;
+        bool act = s.bb > 0.0 && s.rr > tol2 * s.bb;
+        if (!isfinite(s.rr)) { s.status = DPF_NAN; act = false; }
+        s.active = act ? 1 : 0;
+        if (act) atomicAdd(active_count, 1);
+    }
+}
+
+// q = A p; alpha = rz / (p . q)
+template <typename T>
+__global__ void k_spmv_pq(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+                          int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, Coeffs<T> C,
+                          const T *__restrict__ pv, T *__restrict__ q) {
+    DPF_BLOCK_PROLOGUE(desc, bmap, st)
+    Cell c;
+    double part = 0.0;
+    if (decode_cell(L, bm.y, c)) {
+        T pi = pv[c.i], Ax, dg;
+        apply7(L, c, C, pi, [&](long long j, int, int, int) { return pv[j]; }, Ax, dg);
+        q[c.i] = Ax;
+        part = (double)pi * (double)Ax;
+    }
+    double2 tot;
+    if (reduce_last(part, 0.0, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+        CgState &s = st[p];
+        s.pq = tot.x;
+        if (!isfinite(s.pq)) { s.alpha = 0.0; s.status = DPF_NAN; deactivate(s, active_count); }
+        else if (!(s.pq > 0.0)) { s.alpha = 0.0; deactivate(s, active_count); }   // p = 0: exact solution
+        else s.alpha = s.rz / s.pq;
+    }
+}
+
+// x += alpha p; r -= alpha q; convergence test on r . r.
+template <typename T>
+__global__ void k_update_xr(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+                            int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, T *__restrict__ x,
+                            T *__restrict__ r, const T *__restrict__ pv, const T *__restrict__ q, int maxiter) {
+    DPF_BLOCK_PROLOGUE(desc, bmap, st)
+    const double alpha = st[p].alpha;
+    Cell c;
+    double part = 0.0;
+    if (decode_cell(L, bm.y, c)) {
+        T a = (T)alpha;
+        x[c.i] += a * pv[c.i];
+        T ri = r[c.i] - a * q[c.i];
+        r[c.i] = ri;
+        part = (double)ri * (double)ri;
+    }
+    double2 tot;
+    if (reduce_last(part, 0.0, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+        CgState &s = st[p];
+        s.rr = tot.x;
+        s.iters++;
+        s.total_iters++;
+        if (!isfinite(s.rr)) { s.status = DPF_NAN; deactivate(s, active_count); }
+        else if (s.rr <= s.tol2 * s.bb) deactivate(s, active_count);
+        else if (s.iters >= maxiter) { s.status = DPF_NOT_CONVERGED; deactivate(s, active_count); }
+    }
+}
+
+// p = z + beta p
+template <typename T>
+__global__ void k_update_p(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+                           const T *__restrict__ z, T *__restrict__ pv) {
+    DPF_BLOCK_PROLOGUE(desc, bmap, st)
+    const T beta = (T)st[p].beta;
+    Cell c;
+    if (!decode_cell(L, bm.y, c)) return;
+    pv[c.i] = beta == (T)0 ? z[c.i] : z[c.i] + beta * pv[c.i];
+}
+
+// ------------------------------------------------ iterative refinement (FP64)
+// r64 = b - A h (FP64 flux form); decide whether another refinement step is needed.
+__global__ void k_ir_residual(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+                              int *outer_count, ReduceScratch rs, const int2 *__restrict__ pinfo, Coeffs<double> C,
+                              const double *__restrict__ b, const double *__restrict__ h, double *__restrict__ r,
+                              double tol2, int max_outer) {
+    int2 bm = bmap[blockIdx.x];
+    const int p = bm.x;
+    if (!st[p].outer_active) return;
+    const LevelDesc L = desc[p];
+    Cell c;
+    double rr = 0.0, bb = 0.0;
+    if (decode_cell(L, bm.y, c)) {
+        double xi = h[c.i], Ax, dg;
+        apply7(L, c, C, xi, [&](long long j, int, int, int) { return h[j]; }, Ax, dg);
+        double bi = b[c.i];
+        double ri = bi - Ax;
+        r[c.i] = ri;
+        rr = ri * ri;
+        bb = bi * bi;
+    }
+    double2 tot;
+    if (reduce_last(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+        CgState &s = st[p];
+        s.orr = tot.x;
+        if (s.outer == 0) s.obb = tot.y;
+        bool stop = false;
+        if (!isfinite(s.orr)) { s.status = DPF_NAN; stop = true; }
+        else if (s.obb == 0.0 || s.orr <= tol2 * s.obb) stop = true;
+        else if (s.outer > 0 && s.ee <= 1e-26 * s.hh) stop = true;       // correction below FP64 resolution
+        else if (s.outer >= max_outer) { s.status = DPF_NOT_CONVERGED; stop = true; }
+        if (stop) {
+            s.outer_active = 0;
+            atomicSub(outer_count, 1);
+        } else {
+            s.scale = sqrt(s.orr);
+            s.outer++;
+        }
+    }
+}
+
+// r32 = r64 / scale; e = 0
+__global__ void k_ir_cast(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+                          const double *__restrict__ r64, float *__restrict__ r32, float *__restrict__ e) {
+    int2 bm = bmap[blockIdx.x];
+    const int p = bm.x;
+    if (!st[p].outer_active) return;
+    const LevelDesc L = desc[p];
+    const double inv = 1.0 / st[p].scale;
+    Cell c;
+    if (!decode_cell(L, bm.y, c)) return;
+    r32[c.i] = (float)(r64[c.i] * inv);
+    e[c.i] = 0.0f;
+}
+
+// h += scale * e; reduce (|scale e|^2, |h|^2)
+__global__ void k_ir_update(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+                            ReduceScratch rs, const int2 *__restrict__ pinfo, double *__restrict__ h,
+                            const float *__restrict__ e) {
+    int2 bm = bmap[blockIdx.x];
+    const int p = bm.x;
+    if (!st[p].outer_active) return;
+    const LevelDesc L = desc[p];
+    const double sc = st[p].scale;
+    Cell c;
+    double ee = 0.0, hh = 0.0;
+    if (decode_cell(L, bm.y, c)) {
+        double de = sc * (double)e[c.i];
+        double hn = h[c.i] + de;
+        h[c.i] = hn;
+        ee = de * de;
+        hh = hn * hn;
+    }
+    double2 tot;
+    if (reduce_last(ee, hh, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+        st[p].ee = tot.x;
+        st[p].hh = tot.y;
+    }
+}
+
+// ------------------------------------------------------------ misc vector kernels
+__global__ void k_state_init(CgState *st, int nprob, int outer_active) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nprob) return;
+    CgState s;
+    memset(&s, 0, sizeof(s));
+    s.outer_active = outer_active;
+    st[p] = s;
+}
+
+// adjoint right-hand side: rhs = delta at free cells, 0 at Dirichlet cells; x = 0
+__global__ void k_adjoint_rhs(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+                              const uint8_t *__restrict__ dir, const double *__restrict__ delta,
+                              double *__restrict__ rhs, double *__restrict__ x) {
+    int2 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    Cell c;
+    if (!decode_cell(L, bm.y, c)) return;
+    rhs[c.i] = dir[c.i] ? 0.0 : delta[c.i];
+    x[c.i] = 0.0;
+}
+
+// delta = 2 h at observation cells (J = sum h[obs]^2), 0 elsewhere (delta zeroed before)
+__global__ void k_obs_delta(const long long *__restrict__ obs_global, long long nobs, const double *__restrict__ h,
+                            double *__restrict__ delta) {
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nobs) return;
+    long long i = obs_global[k];
+    atomicAdd(&delta[i], 2.0 * h[i]);
+}
+
+// storage shift S_i V_i / dt (transient)
+__global__ void k_shift(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+                        const ProbParam *__restrict__ prm, const double *__restrict__ Ss, double inv_dt,
+                        double *__restrict__ shift) {
+    int2 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    Cell c;
+    if (!decode_cell(L, bm.y, c)) return;
+    shift[c.i] = Ss[c.i] * prm[bm.x].vol * inv_dt;
+}
+
+// b_n = b0 + shift * h_prev (transient right-hand side); Dirichlet rows keep b0 = dirichleths
+__global__ void k_axpy_rhs(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+                           const uint8_t *__restrict__ dir, const double *__restrict__ b0,
+                           const double *__restrict__ shift, const double *__restrict__ hprev,
+                           double *__restrict__ b) {
+    int2 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    Cell c;
+    if (!decode_cell(L, bm.y, c)) return;
+    b[c.i] = dir[c.i] ? b0[c.i] : b0[c.i] + shift[c.i] * hprev[c.i];
+}
+
+// ------------------------------------------------------------- gradients
+// dKs_f = -aol_f (h_a - h_b)(lambda_a - lambda_b), in the reference face order; with
+// accumulate != 0 it adds to dKs (transient adjoint sums over steps).
+__global__ void k_grad_faces(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+                             const ProbParam *__restrict__ prm, const double *__restrict__ h,
+                             const double *__restrict__ lam, double *__restrict__ dKs, int accumulate) {
+    int2 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    Cell c;
+    if (!decode_cell(L, bm.y, c)) return;
+    const ProbParam P = prm[bm.x];
+    const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
+    const int co[3] = {c.ix, c.iy, c.iz};
+    const int nn[3] = {L.nx, L.ny, L.nz};
+    const double hi = h[c.i], li = lam[c.i];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        if (co[d] + 1 < nn[d]) {
+            long long j = c.i + st3[d];
+            double g = -P.aol[d] * (hi - h[j]) * (li - lam[j]);
+            long long f = P.face_off + regular_face_index(L.nx, L.ny, L.nz, c.ix, c.iy, c.iz, d);
+            if (accumulate) dKs[f] += g; else dKs[f] = g;
+        }
+    }
+}
+
+// dlogK_i = sum over the faces of i of dK_f/dlogK_i * dKs_f, with dKs_f formed on the fly
+// from h and lambda (geometric: dK/dlogK_i = K_f / 2; harmonic: K_f^2 / (2 K_i)).
+__global__ void k_grad_logk(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+                            const ProbParam *__restrict__ prm, const double *__restrict__ logK, int kind,
+                            const double *__restrict__ h, const double *__restrict__ lam, double *__restrict__ g) {
+    int2 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    Cell c;
+    if (!decode_cell(L, bm.y, c)) return;
+    const ProbParam P = prm[bm.x];
+    const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
+    const int co[3] = {c.ix, c.iy, c.iz};
+    const int nn[3] = {L.nx, L.ny, L.nz};
+    const double hi = h[c.i], li = lam[c.i], lki = logK[c.i];
+    double acc = 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+#pragma unroll
+        for (int s = -1; s <= 1; s += 2) {
+            bool ok = s > 0 ? co[d] + 1 < nn[d] : co[d] > 0;
+            if (!ok) continue;
+            long long j = c.i + s * st3[d];
+            double dK = -P.aol[d] * (hi - h[j]) * (li - lam[j]);
+            double K = face_mean(lki, logK[j], kind);
+            double w = kind == DPF_MEAN_GEOMETRIC ? 0.5 * K : K * K * 0.5 * exp(-lki);
+            acc += w * dK;
+        }
+    }
+    g[c.i] = acc;
+}
+
+// ddirichleths_k = delta_k + sum over free neighbours j of K_f aol_f lambda_j (Dirichlet k);
+// 0 at free cells. dQs = lambda (0 at Dirichlet cells). Either output may be null.
+__global__ void k_grad_dh_q(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+                            const ProbParam *__restrict__ prm, FaceK fk, const uint8_t *__restrict__ dir,
+                            const double *__restrict__ delta, const double *__restrict__ lam, double *ddh,
+                            double *dQs, int accumulate) {
+    int2 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    Cell c;
+    if (!decode_cell(L, bm.y, c)) return;
+    const ProbParam P = prm[bm.x];
+    const bool isd = dir[c.i];
+    if (dQs) {
+        double v = isd ? 0.0 : lam[c.i];
+        if (accumulate) dQs[c.i] += v; else dQs[c.i] = v;
+    }
+    if (!ddh) return;
+    double acc = 0.0;
+    if (isd) {
+        if (delta) acc = delta[c.i];
+        const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
+        const int co[3] = {c.ix, c.iy, c.iz};
+        const int nn[3] = {L.nx, L.ny, L.nz};
+        for (int d = 0; d < 3; d++)
+            for (int s = -1; s <= 1; s += 2) {
+                bool ok = s > 0 ? co[d] + 1 < nn[d] : co[d] > 0;
+                if (!ok) continue;
+                long long j = c.i + s * st3[d];
+                if (dir[j]) continue;
+                acc += fk(L, P, c, d, s, j) * P.aol[d] * lam[j];
+            }
+    }
+    if (accumulate) ddh[c.i] += acc; else ddh[c.i] = acc;
+}
+
+// Ks in the reference face order from logK
+__global__ void k_logk_to_faces(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+                                const ProbParam *__restrict__ prm, const double *__restrict__ logK, int kind,
+                                double *__restrict__ Ks) {
+    int2 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    Cell c;
+    if (!decode_cell(L, bm.y, c)) return;
+    const ProbParam P = prm[bm.x];
+    const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
+    const int co[3] = {c.ix, c.iy, c.iz};
+    const int nn[3] = {L.nx, L.ny, L.nz};
+    for (int d = 0; d < 3; d++)
+        if (co[d] + 1 < nn[d])
+            Ks[P.face_off + regular_face_index(L.nx, L.ny, L.nz, c.ix, c.iy, c.iz, d)] =
+                face_mean(logK[c.i], logK[c.i + st3[d]], kind);
+}
+
+// dlogK from dKs (gather over the six faces of each cell)
+__global__ void k_logk_vjp(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+                           const ProbParam *__restrict__ prm, const double *__restrict__ logK, int kind,
+                           const double *__restrict__ dKs, double *__restrict__ g) {
+    int2 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    Cell c;
+    if (!decode_cell(L, bm.y, c)) return;
+    const ProbParam P = prm[bm.x];
+    const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
+    const int co[3] = {c.ix, c.iy, c.iz};
+    const int nn[3] = {L.nx, L.ny, L.nz};
+    const double lki = logK[c.i];
+    double acc = 0.0;
+    for (int d = 0; d < 3; d++)
+        for (int s = -1; s <= 1; s += 2) {
+            bool ok = s > 0 ? co[d] + 1 < nn[d] : co[d] > 0;
+            if (!ok) continue;
+            long long j = c.i + s * st3[d];
+            int ax = c.ix, ay = c.iy, az = c.iz;
+            if (s < 0) { if (d == 0) ax--; else if (d == 1) ay--; else az--; }
+            long long f = P.face_off + regular_face_index(L.nx, L.ny, L.nz, ax, ay, az, d);
+            double K = face_mean(lki, logK[j], kind);
+            double w = kind == DPF_MEAN_GEOMETRIC ? 0.5 * K : K * K * 0.5 * exp(-lki);
+            acc += w * dKs[f];
+        }
+    g[c.i] = acc;
+}
+
+// y = A x (FP64 fine operator; Dirichlet rows identity)
+__global__ void k_apply(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, Coeffs<double> C,
+                        const double *__restrict__ x, double *__restrict__ y) {
+    int2 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    Cell c;
+    if (!decode_cell(L, bm.y, c)) return;
+    double Ax, dg;
+    apply7(L, c, C, x[c.i], [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
+    y[c.i] = Ax;
+}
+
+// ================================================================ host side
+static void ck(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e), e);
+}
+#define CK(x) ck((x), #x)
+#define LAUNCH_CHECK() ck(cudaGetLastError(), "kernel launch")
+
+template <typename T>
+static T *dalloc(size_t n, std::vector<void *> &owned) {
+    void *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw OomError(std::string("cudaMalloc of ") + std::to_string(n * sizeof(T)) + " bytes failed");
+    }
+    owned.push_back(p);
+    return (T *)p;
+}
+
+static BlockMap build_map(const std::vector<LevelDesc> &desc, const std::vector<int> &take, std::vector<void *> &own,
+                          int nprob) {
+    BlockMap m;
+    std::vector<int2> map, pinfo(nprob, make_int2(0, 0));
+    for (int p = 0; p < nprob; p++) {
+        if (!take[p]) continue;
+        int nb = (int)((desc[p].n + kBlock - 1) / kBlock);
+        pinfo[p] = make_int2((int)map.size(), nb);
+        for (int b = 0; b < nb; b++) map.push_back(make_int2(p, b));
+    }
+    m.nblocks = (int)map.size();
+    m.d_map = dalloc<int2>(map.size(), own);
+    m.d_pinfo = dalloc<int2>(nprob, own);
+    if (!map.empty()) CK(cudaMemcpy(m.d_map, map.data(), map.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(m.d_pinfo, pinfo.data(), nprob * sizeof(int2), cudaMemcpyHostToDevice));
+    return m;
+}
+
+StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<std::vector<int64_t>> &dnodes,
+                         const dpf_options &o, cudaStream_t s)
+    : opt(o), stream(s) {
+    nprob = (int)grids.size();
+    if (nprob <= 0) throw BadInput("empty batch");
+    if (opt.max_coarse < 1 || opt.max_coarse > kMaxCoarse) opt.max_coarse = kMaxCoarse;
+    if (opt.cheb_degree < 1) opt.cheb_degree = 1;
+    if (opt.cheb_degree > 8) opt.cheb_degree = 8;
+    mixed = opt.precision == DPF_PREC_MIXED;
+    // per-problem hierarchy shapes
+    nlev.resize(nprob);
+    std::vector<std::vector<std::array<int, 3>>> shapes(nprob);
+    nlev_max = 0;
+    for (int p = 0; p < nprob; p++) {
+        auto g = grids[p];
+        if (g.n[0] < 1 || g.n[1] < 1 || g.n[2] < 1) throw BadInput("grid dimensions must be >= 1");
+        long long n = (long long)g.n[0] * g.n[1] * g.n[2];
+        if (n >= (1LL << 31)) throw BadInput("a single grid must have fewer than 2^31 cells");
+        std::array<int, 3> d = {g.n[0], g.n[1], g.n[2]};
+        shapes[p].push_back(d);
+        while ((long long)d[0] * d[1] * d[2] > opt.max_coarse) {
+            d = {(d[0] + 1) / 2, (d[1] + 1) / 2, (d[2] + 1) / 2};
+            shapes[p].push_back(d);
+        }
+        nlev[p] = (int)shapes[p].size();
+        nlev_max = std::max(nlev_max, nlev[p]);
+    }
+    // level descriptors
+    lv.resize(nlev_max);
+    int maxblocks = 0;
+    for (int l = 0; l < nlev_max; l++) {
+        Level &L = lv[l];
+        L.h_desc.assign(nprob, LevelDesc{1, 1, 1, 0, 0, 0});
+        long long off = 0;
+        std::vector<int> has(nprob, 0), smooth(nprob, 0);
+        for (int p = 0; p < nprob; p++) {
+            if (l >= nlev[p]) continue;
+            auto d = shapes[p][l];
+            LevelDesc &D = L.h_desc[p];
+            D.nx = d[0]; D.ny = d[1]; D.nz = d[2];
+            D.n = (long long)d[0] * d[1] * d[2];
+            D.off = off;
+            off += D.n;
+            has[p] = 1;
+            smooth[p] = l < nlev[p] - 1;
+            if (l == nlev[p] - 1) L.coarse_list.push_back(p);
+        }
+        L.ntot = off;
+        L.d_desc = dalloc<LevelDesc>(nprob, owned);
+        CK(cudaMemcpy(L.d_desc, L.h_desc.data(), nprob * sizeof(LevelDesc), cudaMemcpyHostToDevice));
+        L.all = build_map(L.h_desc, has, owned, nprob);
+        L.smooth = build_map(L.h_desc, smooth, owned, nprob);
+        for (int p = 0; p < nprob; p++) {
+            if (has[p]) L.all_cells += L.h_desc[p].n;
+            if (smooth[p]) L.smooth_cells += L.h_desc[p].n;
+            if (has[p] && !smooth[p]) L.coarse_cells += L.h_desc[p].n;
+        }
+        maxblocks = std::max(maxblocks, L.all.nblocks);
+        L.d_coarse = dalloc<int>(L.coarse_list.size(), owned);
+        if (!L.coarse_list.empty())
+            CK(cudaMemcpy(L.d_coarse, L.coarse_list.data(), L.coarse_list.size() * sizeof(int),
+                          cudaMemcpyHostToDevice));
+        size_t n = (size_t)L.ntot;
+        L.dir = dalloc<uint8_t>(n, owned);
+        L.c64[0] = dalloc<double>(n, owned); L.c64[1] = dalloc<double>(n, owned);
+        L.c64[2] = dalloc<double>(n, owned); L.c64[3] = dalloc<double>(n, owned);
+        if (mixed) {
+            for (int k = 0; k < 4; k++) L.c32[k] = dalloc<float>(n, owned);
+        }
+        size_t vs = mixed ? sizeof(float) : sizeof(double);
+        for (int k = 0; k < 4; k++) L.work[k] = dalloc<char>(n * vs, owned);
+    }
+    N = lv[0].ntot;
+    // faces and parameters
+    prm.resize(nprob);
+    long long foff = 0;
+    cell_off.resize(nprob + 1);
+    face_off.resize(nprob + 1);
+    for (int p = 0; p < nprob; p++) {
+        auto g = grids[p];
+        int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+        double dxyz[3];
+        for (int k = 0; k < 3; k++) dxyz[k] = g.n[k] > 1 ? (g.maxs[k] - g.mins[k]) / (g.n[k] - 1) : 1.0;
+        ProbParam &P = prm[p];
+        P.aol[0] = dxyz[1] * dxyz[2] / dxyz[0];
+        P.aol[1] = dxyz[0] * dxyz[2] / dxyz[1];
+        P.aol[2] = dxyz[0] * dxyz[1] / dxyz[2];
+        if (g.aol_override) for (int k = 0; k < 3; k++) P.aol[k] = g.aol[k];
+        P.vol = g.vol_override ? g.vol : dxyz[0] * dxyz[1] * dxyz[2];
+        long long Fp = 3LL * nx * ny * nz - (long long)nx * ny - (long long)nx * nz - (long long)ny * nz;
+        P.face_off = foff;
+        P.F = Fp;
+        cell_off[p] = lv[0].h_desc[p].off;
+        face_off[p] = foff;
+        foff += Fp;
+    }
+    cell_off[nprob] = N;
+    face_off[nprob] = foff;
+    F = foff;
+    d_prm = dalloc<ProbParam>(nprob, owned);
+    CK(cudaMemcpy(d_prm, prm.data(), nprob * sizeof(ProbParam), cudaMemcpyHostToDevice));
+    // Dirichlet mask of the finest level
+    std::vector<uint8_t> dir(N, 0);
+    nfree_total = N;
+    ndir.assign(nprob, 0);
+    for (int p = 0; p < nprob; p++) {
+        for (int64_t k : dnodes[p]) {
+            if (k < 0 || k >= lv[0].h_desc[p].n) throw BadInput("Dirichlet node index out of range");
+            if (!dir[cell_off[p] + k]) { nfree_total--; ndir[p]++; }
+            dir[cell_off[p] + k] = 1;
+        }
+    }
+    CK(cudaMemcpy(lv[0].dir, dir.data(), N, cudaMemcpyHostToDevice));
+    // fine-level vectors
+    h = dalloc<double>(N, owned);
+    b64 = dalloc<double>(N, owned);
+    r64 = dalloc<double>(N, owned);
+    lam = dalloc<double>(N, owned);
+    delta = dalloc<double>(N, owned);
+    arhs = dalloc<double>(N, owned);
+    in_dh = dalloc<double>(N, owned);
+    in_Q = dalloc<double>(N, owned);
+    in_logK = dalloc<double>(N, owned);
+    in_Ks = dalloc<double>(F, owned);
+    size_t vs = mixed ? sizeof(float) : sizeof(double);
+    for (int k = 0; k < 5; k++) cgv[k] = dalloc<char>(N * vs, owned);
+    // state, reductions, coarse factors
+    d_state = dalloc<CgState>(nprob, owned);
+    d_count = dalloc<int>(2, owned);
+    d_factor_status = dalloc<int>(1, owned);
+    rs.partials = dalloc<double2>(std::max(maxblocks, 1), owned);
+    rs.tickets = dalloc<unsigned>(nprob, owned);
+    rs.capacity = maxblocks;
+    CK(cudaMemset(rs.tickets, 0, nprob * sizeof(unsigned)));
+    d_coarseL = dalloc<double>((size_t)nprob * kMaxCoarse * kMaxCoarse, owned);
+    CK(cudaMallocHost(&h_count, 2 * sizeof(int)));
+    CK(cudaMallocHost(&h_state_buf, nprob * sizeof(CgState)));
+    // Chebyshev coefficients on D^-1 A over [lo*2, 2] (Gershgorin: the spectrum of
+    // D^-1 A of a weakly diagonally dominant symmetric M-matrix lies in [0, 2]).
+    double lmax = 2.0, lmin = 2.0 * opt.cheb_lo;
+    double theta = 0.5 * (lmax + lmin), delt = 0.5 * (lmax - lmin);
+    double sigma = theta / delt, rho = 1.0 / sigma;
+    inv_theta = 1.0 / theta;
+    cheb_c1.assign(opt.cheb_degree, 0.0);
+    cheb_c2.assign(opt.cheb_degree, 0.0);
+    for (int k = 1; k < opt.cheb_degree; k++) {
+        double rn = 1.0 / (2.0 * sigma - rho);
+        cheb_c1[k] = rn * rho;
+        cheb_c2[k] = 2.0 * rn / delt;
+        rho = rn;
+    }
+    CK(cudaDeviceSynchronize());
+}
+
+// Stable names "kernel<f64|f32>/L<level>" for the per-kernel timing report.
+const char *kname(const char *base, int level, bool fp32) {
+    static std::set<std::string> names;
+    std::string n = std::string(base) + (fp32 ? "<f32>" : "<f64>") + "/L" + std::to_string(level);
+    return names.insert(n).first->c_str();
+}
+
+KTimer::KTimer(StructBatch *s, const char *name, long long cells) : S(s) {
+    S->launches++;
+    if (!S->prof_on || S->prof_recs.size() >= (1u << 20)) return;
+    int e = (int)(2 * S->prof_recs.size());
+    while ((int)S->ev_pool.size() < e + 2) {
+        cudaEvent_t ev;
+        if (cudaEventCreate(&ev) != cudaSuccess) { cudaGetLastError(); return; }
+        S->ev_pool.push_back(ev);
+    }
+    S->prof_recs.push_back(ProfRec{name, e, cells});
+    cudaEventRecord(S->ev_pool[e], S->stream);
+    slot = e;
+}
+
+KTimer::~KTimer() {
+    if (slot >= 0) cudaEventRecord(S->ev_pool[slot + 1], S->stream);
+}
+
+void StructBatch::profile(bool on) {
+    cudaStreamSynchronize(stream);
+    prof_recs.clear();
+    prof_on = on;
+}
+
+int StructBatch::profile_report(int cap, const char **names, long long *counts, double *ms, long long *cells) {
+    CK(cudaStreamSynchronize(stream));
+    std::vector<const char *> nm;
+    std::vector<long long> cnt, cl;
+    std::vector<double> tot;
+    for (auto &r : prof_recs) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, ev_pool[r.ev], ev_pool[r.ev + 1]) != cudaSuccess) { cudaGetLastError(); continue; }
+        size_t k = 0;
+        while (k < nm.size() && std::strcmp(nm[k], r.name) != 0) k++;
+        if (k == nm.size()) { nm.push_back(r.name); cnt.push_back(0); tot.push_back(0.0); cl.push_back(0); }
+        cnt[k]++;
+        tot[k] += t;
+        cl[k] += r.cells;
+    }
+    for (size_t k = 0; k < nm.size() && (int)k < cap; k++) {
+        if (names) names[k] = nm[k];
+        if (counts) counts[k] = cnt[k];
+        if (ms) ms[k] = tot[k];
+        if (cells) cells[k] = cl[k];
+    }
+    return (int)nm.size();
+}
+
+StructBatch::~StructBatch() {
+    for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    for (void *p : owned) cudaFree(p);
+    if (h_count) cudaFreeHost(h_count);
+    if (h_state_buf) cudaFreeHost(h_state_buf);
+}
+
+static inline unsigned nb_of(const BlockMap &m) { return (unsigned)m.nblocks; }
+
+// ---- assembly and hierarchy
+void StructBatch::assemble(const double *Ks, const double *logK, int kind, const double *shift, bool init_x) {
+    Level &L0 = lv[0];
+    FaceK fk{Ks, logK, kind};
+    if (nb_of(L0.all))
+        {
+            KTimer _kt(this, kname("k_assemble", 0, false), L0.all_cells);
+            k_assemble<<<nb_of(L0.all), kBlock, 0, stream>>>(
+                L0.d_desc, L0.all.d_map, d_prm, fk, in_dh, in_Q, shift, L0.dir, L0.c64[0], L0.c64[1], L0.c64[2],
+                L0.c64[3], mixed ? L0.c32[0] : nullptr, mixed ? L0.c32[1] : nullptr, mixed ? L0.c32[2] : nullptr,
+                mixed ? L0.c32[3] : nullptr, b64, h, init_x ? 1 : 0);
+        }
+    LAUNCH_CHECK();
+    for (int l = 0; l + 1 < nlev_max; l++) {
+        Level &F = lv[l], &C = lv[l + 1];
+        if (!nb_of(C.all)) continue;
+        {
+            KTimer _kt(this, kname("k_coarsen", l + 1, false), C.all_cells);
+            k_coarsen<<<nb_of(C.all), kBlock, 0, stream>>>(
+                F.d_desc, C.d_desc, C.all.d_map, F.c64[0], F.c64[1], F.c64[2], F.c64[3], F.dir, C.c64[0], C.c64[1],
+                C.c64[2], C.c64[3], C.dir, mixed ? C.c32[0] : nullptr, mixed ? C.c32[1] : nullptr,
+                mixed ? C.c32[2] : nullptr, mixed ? C.c32[3] : nullptr);
+        }
+        LAUNCH_CHECK();
+    }
+    CK(cudaMemsetAsync(d_factor_status, 0, sizeof(int), stream));
+    for (int l = 0; l < nlev_max; l++) {
+        Level &L = lv[l];
+        if (L.coarse_list.empty()) continue;
+        {
+            KTimer _kt(this, kname("k_coarse_factor", l, false), L.coarse_cells);
+            k_coarse_factor<<<(unsigned)L.coarse_list.size(), kBlock, 0, stream>>>(
+                L.d_desc, L.d_coarse, L.c64[0], L.c64[1], L.c64[2], L.c64[3], d_coarseL, d_factor_status);
+        }
+        LAUNCH_CHECK();
+    }
+    have_operator = true;
+}
+
+// ---- V-cycle: z = M r on the fine level (vector precision T)
+template <typename T>
+static Coeffs<T> coeffs_of(StructBatch::Level &L, bool mixed);
+template <>
+Coeffs<double> coeffs_of<double>(StructBatch::Level &L, bool) {
+    return Coeffs<double>{L.c64[0], L.c64[1], L.c64[2], L.c64[3]};
+}
+template <>
+Coeffs<float> coeffs_of<float>(StructBatch::Level &L, bool) {
+    return Coeffs<float>{L.c32[0], L.c32[1], L.c32[2], L.c32[3]};
+}
+
+template <typename T>
+void StructBatch::vcycle(const T *r, T *z) {
+    const int deg = opt.cheb_degree;
+    const T invth = (T)inv_theta, sc = (T)opt.coarse_scale;
+    std::vector<T *> pre(nlev_max, nullptr);
+    // descend
+    for (int l = 0; l < nlev_max; l++) {
+        Level &L = lv[l];
+        Coeffs<T> C = coeffs_of<T>(L, mixed);
+        const T *b = l == 0 ? r : (const T *)L.work[2];
+        T *xa = (T *)L.work[0], *xb = (T *)L.work[1], *d = (T *)L.work[3];
+        if (nb_of(L.smooth)) {
+            {
+                KTimer _kt(this, kname("k_cheb_first", l, sizeof(T) == 4), L.smooth_cells);
+                k_cheb_first<T><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, L.smooth.d_map, d_state, C, b, xa, d,
+                                                                        invth);
+            }
+            LAUNCH_CHECK();
+            T *cur = xa, *oth = xb;
+            for (int k = 1; k < deg; k++) {
+                {
+                    KTimer _kt(this, kname("k_cheb_step", l, sizeof(T) == 4), L.smooth_cells);
+                    k_cheb_step<T, false><<<nb_of(L.smooth), kBlock, 0, stream>>>(
+                        L.d_desc, L.smooth.d_map, d_state, C, b, cur, oth, d, (T)cheb_c1[k], (T)cheb_c2[k], rs,
+                        L.smooth.d_pinfo);
+                }
+                LAUNCH_CHECK();
+                std::swap(cur, oth);
+            }
+            pre[l] = cur;
+            Level &Cn = lv[l + 1];
+            {
+                KTimer _kt(this, kname("k_restrict", l + 1, sizeof(T) == 4), Cn.all_cells);
+                k_restrict<T><<<nb_of(Cn.all), kBlock, 0, stream>>>(L.d_desc, Cn.d_desc, Cn.all.d_map, d_state, C, b,
+                                                                   cur, (T *)Cn.work[2]);
+            }
+            LAUNCH_CHECK();
+        }
+        if (!L.coarse_list.empty()) {
+            // the coarse solution goes where the post-smoother of this level would
+            // leave its result: work[1] (always, see below), or z on the finest level
+            T *out = l == 0 ? z : xb;
+            if (l == 0)
+                {
+                    KTimer _kt(this, kname("k_coarse_solve", l, sizeof(T) == 4), L.coarse_cells);
+                    k_coarse_solve<T, true><<<(unsigned)L.coarse_list.size(), 32, 0, stream>>>(
+                        L.d_desc, L.d_coarse, d_state, d_coarseL, b, out);
+                }
+            else
+                {
+                    KTimer _kt(this, kname("k_coarse_solve", l, sizeof(T) == 4), L.coarse_cells);
+                    k_coarse_solve<T, false><<<(unsigned)L.coarse_list.size(), 32, 0, stream>>>(
+                        L.d_desc, L.d_coarse, d_state, d_coarseL, b, out);
+                }
+            LAUNCH_CHECK();
+        }
+    }
+    // ascend: deg post-smoothing kernels alternate buffers starting from pre[l];
+    // cheb_first + (deg-1) steps + prolong + (deg-1) steps = 2 deg kernels, so the
+    // final post-smoothed iterate always lands in work[1].
+    for (int l = nlev_max - 2; l >= 0; l--) {
+        Level &L = lv[l];
+        if (!nb_of(L.smooth)) continue;
+        Level &Cn = lv[l + 1];
+        Coeffs<T> C = coeffs_of<T>(L, mixed);
+        const T *b = l == 0 ? r : (const T *)L.work[2];
+        T *xa = (T *)L.work[0], *xb = (T *)L.work[1], *d = (T *)L.work[3];
+        T *cur = pre[l];
+        T *oth = cur == xa ? xb : xa;
+        const T *e = (const T *)Cn.work[1];
+        bool last_is_prolong = deg == 1;
+        T *out = (l == 0 && last_is_prolong) ? z : oth;
+        if (l == 0 && last_is_prolong)
+            {
+                KTimer _kt(this, kname("k_prolong_cheb", l, sizeof(T) == 4), L.smooth_cells);
+                k_prolong_cheb<T, true><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, Cn.d_desc, L.smooth.d_map,
+                                                                                d_state, C, L.dir, b, cur, e, out, d,
+                                                                                sc, invth, rs, L.smooth.d_pinfo);
+            }
+        else
+            {
+                KTimer _kt(this, kname("k_prolong_cheb", l, sizeof(T) == 4), L.smooth_cells);
+                k_prolong_cheb<T, false><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, Cn.d_desc, L.smooth.d_map,
+                                                                                 d_state, C, L.dir, b, cur, e, out, d,
+                                                                                 sc, invth, rs, L.smooth.d_pinfo);
+            }
+        LAUNCH_CHECK();
+        cur = out;
+        oth = cur == xa ? xb : xa;
+        for (int k = 1; k < deg; k++) {
+            bool last = k == deg - 1;
+            T *o = (l == 0 && last) ? z : oth;
+            if (l == 0 && last)
+                {
+                    KTimer _kt(this, kname("k_cheb_step", l, sizeof(T) == 4), L.smooth_cells);
+                    k_cheb_step<T, true><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, L.smooth.d_map, d_state, C,
+                                                                                 b, cur, o, d, (T)cheb_c1[k],
+                                                                                 (T)cheb_c2[k], rs, L.smooth.d_pinfo);
+                }
+            else
+                {
+                    KTimer _kt(this, kname("k_cheb_step", l, sizeof(T) == 4), L.smooth_cells);
+                    k_cheb_step<T, false><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, L.smooth.d_map, d_state, C,
+                                                                                  b, cur, o, d, (T)cheb_c1[k],
+                                                                                  (T)cheb_c2[k], rs, L.smooth.d_pinfo);
+                }
+            LAUNCH_CHECK();
+            cur = o;
+            oth = cur == xa ? xb : xa;
+        }
+    }
+}
+
+int StructBatch::read_count(int which) {
+    CK(cudaMemcpyAsync(h_count, d_count, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    return h_count[which];
+}
+
+// ---- preconditioned CG on all active problems: A x = b (vectors of type T)
+template <typename T>
+void StructBatch::pcg(const T *b, T *x, double tol2, bool gated) {
+    Level &L0 = lv[0];
+    Coeffs<T> C = coeffs_of<T>(L0, mixed);
+    T *r = (T *)cgv[0], *z = (T *)cgv[1], *pv = (T *)cgv[2], *q = (T *)cgv[3];
+    const unsigned nb = nb_of(L0.all);
+    CK(cudaMemsetAsync(d_count, 0, sizeof(int), stream));
+    {
+        KTimer _kt(this, kname("k_cg_start", 0, sizeof(T) == 4), L0.all_cells);
+        k_cg_start<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C, b, x,
+                                                 r, tol2, gated ? 1 : 0);
+    }
+    LAUNCH_CHECK();
+    if (read_count(0) == 0) return;
+    vcycle<T>(r, z);
+    {
+        KTimer _kt(this, kname("k_update_p", 0, sizeof(T) == 4), L0.all_cells);
+        k_update_p<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z, pv);
+    }
+    LAUNCH_CHECK();
+    const int check = std::max(1, opt.check_every);
+    for (int it = 1; it <= opt.maxiter; it++) {
+        {
+            KTimer _kt(this, kname("k_spmv_pq", 0, sizeof(T) == 4), L0.all_cells);
+            k_spmv_pq<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C,
+                                                    pv, q);
+        }
+        LAUNCH_CHECK();
+        {
+            KTimer _kt(this, kname("k_update_xr", 0, sizeof(T) == 4), L0.all_cells);
+            k_update_xr<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, x,
+                                                      r, pv, q, opt.maxiter);
+        }
+        LAUNCH_CHECK();
+        if (it % check == 0 && read_count(0) == 0) return;
+        vcycle<T>(r, z);
+        {
+            KTimer _kt(this, kname("k_update_p", 0, sizeof(T) == 4), L0.all_cells);
+            k_update_p<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z, pv);
+        }
+        LAUNCH_CHECK();
+    }
+    read_count(0);
+}
+
+// ---- full solve of A x = b for every problem (x holds the initial guess)
+void StructBatch::solve(const double *b, double *x, double reltol) {
+    const double tol2 = reltol * reltol;
+    Level &L0 = lv[0];
+    const unsigned nb = nb_of(L0.all);
+    {
+        KTimer _kt(this, kname("k_state_init", 0, false), 0);
+        k_state_init<<<(nprob + 127) / 128, 128, 0, stream>>>(d_state, nprob, 1);
+    }
+    LAUNCH_CHECK();
+    if (!mixed) {
+        pcg<double>(b, x, tol2, false);
+        stats_outer = 0;
+    } else {
+        float *r32 = (float *)cgv[4];
+        float *e = (float *)ir_e();
+        h_count[1] = nprob;
+        CK(cudaMemcpyAsync(d_count + 1, h_count + 1, sizeof(int), cudaMemcpyHostToDevice, stream));
+        int outer = 0;
+        for (;; outer++) {
+            {
+                KTimer _kt(this, kname("k_ir_residual", 0, false), L0.all_cells);
+                k_ir_residual<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count + 1, rs,
+                                                         L0.all.d_pinfo, coeffs_of<double>(L0, true), b, x, r64, tol2,
+                                                         opt.max_outer);
+            }
+            LAUNCH_CHECK();
+            if (read_count(1) == 0) break;
+            {
+                KTimer _kt(this, kname("k_ir_cast", 0, false), L0.all_cells);
+                k_ir_cast<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, r64, r32, e);
+            }
+            LAUNCH_CHECK();
+            pcg<float>(r32, e, opt.inner_tol * opt.inner_tol, true);
+            {
+                KTimer _kt(this, kname("k_ir_update", 0, false), L0.all_cells);
+                k_ir_update<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, rs, L0.all.d_pinfo, x, e);
+            }
+            LAUNCH_CHECK();
+        }
+        stats_outer = outer;
+    }
+    // statistics
+    CK(cudaMemcpyAsync(h_state_buf, d_state, nprob * sizeof(CgState), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    CgState *hs = (CgState *)h_state_buf;
+    last_status = DPF_OK;
+    stats_iters = 0;
+    stats_relres = 0.0;
+    for (int p = 0; p < nprob; p++) {
+        stats_iters = std::max(stats_iters, mixed ? hs[p].total_iters : hs[p].iters);
+        double rel = mixed ? (hs[p].obb > 0 ? std::sqrt(hs[p].orr / hs[p].obb) : 0.0)
+                           : (hs[p].bb > 0 ? std::sqrt(hs[p].rr / hs[p].bb) : 0.0);
+        stats_relres = std::max(stats_relres, rel);
+        if (hs[p].status != DPF_OK && last_status == DPF_OK) last_status = hs[p].status;
+    }
+    int fst = 0;
+    CK(cudaMemcpyAsync(&h_count[0], d_factor_status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    fst = h_count[0];
+    if (fst) {
+        last_status = DPF_BAD_INPUT;
+        last_message = "coarsest operator is not positive definite (does every problem have a Dirichlet cell?)";
+    }
+}
+
+void *StructBatch::ir_e() {
+    if (!ir_e_buf) ir_e_buf = dalloc<float>((size_t)N, owned);
+    return ir_e_buf;
+}
+
+// ---- public operations
+void StructBatch::forward(const double *Ks, const double *logK, int kind) {
+    for (int p = 0; p < nprob; p++)
+        if (ndir[p] == 0)
+            throw BadInput("problem " + std::to_string(p) +
+                           " has no Dirichlet cell: the steady-state operator is singular");
+    assemble(Ks, logK, kind, nullptr, true);
+    solve(b64, h, opt.reltol);
+    fwd_kind = logK ? 1 : 0;
+    mean_kind = kind;
+    have_forward = true;
+}
+
+void StructBatch::adjoint_solve() {
+    Level &L0 = lv[0];
+    {
+        KTimer _kt(this, kname("k_adjoint_rhs", 0, false), L0.all_cells);
+        k_adjoint_rhs<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, L0.dir, delta, arhs, lam);
+    }
+    LAUNCH_CHECK();
+    solve(arhs, lam, opt.reltol);
+}
+
+void StructBatch::obs_delta(const long long *d_obs, long long nobs) {
+    CK(cudaMemsetAsync(delta, 0, N * sizeof(double), stream));
+    if (nobs > 0) {
+        {
+            KTimer _kt(this, kname("k_obs_delta", 0, false), nobs);
+            k_obs_delta<<<(unsigned)((nobs + 255) / 256), 256, 0, stream>>>(d_obs, nobs, h, delta);
+        }
+        LAUNCH_CHECK();
+    }
+}
+
+void StructBatch::grad_faces(const double *hv, const double *lv_, double *dKs, bool accumulate) {
+    Level &L0 = lv[0];
+    {
+        KTimer _kt(this, kname("k_grad_faces", 0, false), L0.all_cells);
+        k_grad_faces<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_prm, hv, lv_, dKs,
+                                                           accumulate ? 1 : 0);
+    }
+    LAUNCH_CHECK();
+}
+
+void StructBatch::grad_logk(double *g) {
+    Level &L0 = lv[0];
+    {
+        KTimer _kt(this, kname("k_grad_logk", 0, false), L0.all_cells);
+        k_grad_logk<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_prm, in_logK, mean_kind, h, lam,
+                                                          g);
+    }
+    LAUNCH_CHECK();
+}
+
+void StructBatch::grad_dh_q(const double *lv_, double *ddh, double *dQs, bool with_delta, bool accumulate) {
+    Level &L0 = lv[0];
+    FaceK fk{fwd_kind ? nullptr : in_Ks, fwd_kind ? in_logK : nullptr, mean_kind};
+    {
+        KTimer _kt(this, kname("k_grad_dh_q", 0, false), L0.all_cells);
+        k_grad_dh_q<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_prm, fk, L0.dir,
+                                                          with_delta ? delta : nullptr, lv_, ddh, dQs,
+                                                          accumulate ? 1 : 0);
+    }
+    LAUNCH_CHECK();
+}
+
+void StructBatch::logk_to_faces(const double *logK, int kind, double *Ks) {
+    Level &L0 = lv[0];
+    {
+        KTimer _kt(this, kname("k_logk_to_faces", 0, false), L0.all_cells);
+        k_logk_to_faces<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_prm, logK, kind, Ks);
+    }
+    LAUNCH_CHECK();
+}
+
+void StructBatch::logk_vjp(const double *logK, int kind, const double *dKs, double *g) {
+    Level &L0 = lv[0];
+    {
+        KTimer _kt(this, kname("k_logk_vjp", 0, false), L0.all_cells);
+        k_logk_vjp<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_prm, logK, kind, dKs, g);
+    }
+    LAUNCH_CHECK();
+}
+
+void StructBatch::apply(const double *x, double *y) {
+    Level &L0 = lv[0];
+    {
+        KTimer _kt(this, kname("k_apply", 0, false), L0.all_cells);
+        k_apply<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, coeffs_of<double>(L0, true), x, y);
+    }
+    LAUNCH_CHECK();
+}
+
+// ---- transient backward Euler with checkpointed adjoint
+void StructBatch::set_shift(const double *Ss, double dt) {
+    if (!shift) shift = dalloc<double>(N, owned);
+    Level &L0 = lv[0];
+    {
+        KTimer _kt(this, kname("k_shift", 0, false), L0.all_cells);
+        k_shift<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_prm, Ss, 1.0 / dt, shift);
+    }
+    LAUNCH_CHECK();
+}
+
+void StructBatch::transient_step(const double *b0, const double *hprev) {
+    Level &L0 = lv[0];
+    {
+        KTimer _kt(this, kname("k_axpy_rhs", 0, false), L0.all_cells);
+        k_axpy_rhs<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, L0.dir, b0, shift, hprev, b64);
+    }
+    LAUNCH_CHECK();
+    solve(b64, h, opt.reltol);
+}
+
+template void StructBatch::vcycle<double>(const double *, double *);
+template void StructBatch::vcycle<float>(const float *, float *);
+template void StructBatch::pcg<double>(const double *, double *, double, bool);
+template void StructBatch::pcg<float>(const float *, float *, double, bool);
+
+}  // namespace dpf

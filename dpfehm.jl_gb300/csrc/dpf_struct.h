@@ -1,0 +1,149 @@
+// dpf_struct.h -- host-side class of the structured (regular-grid) batch solver.
+#pragma once
+#include <array>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "dpf_internal.h"
+
+namespace dpf {
+
+struct DpfError : std::runtime_error {
+    int code;
+    DpfError(const std::string &m, int c) : std::runtime_error(m), code(c) {}
+};
+struct BadInput : DpfError {
+    explicit BadInput(const std::string &m) : DpfError(m, DPF_BAD_INPUT) {}
+};
+struct OomError : DpfError {
+    explicit OomError(const std::string &m) : DpfError(m, DPF_OOM) {}
+};
+struct CudaError : DpfError {
+    CudaError(const std::string &m, cudaError_t) : DpfError(m, DPF_CUDA) {}
+};
+
+struct GridSpec {
+    int n[3];                 // nx, ny, nz
+    double mins[3], maxs[3];
+    bool aol_override = false;
+    double aol[3] = {0, 0, 0};
+    bool vol_override = false;
+    double vol = 0;
+};
+
+class StructBatch;
+
+// Counts every kernel launch and, while profiling is on, brackets it with a pair
+// of CUDA events on the launching stream (per-kernel device time).
+struct KTimer {
+    StructBatch *S;
+    int slot = -1;
+    KTimer(StructBatch *s, const char *name, long long cells);
+    ~KTimer();
+};
+
+struct ProfRec {
+    const char *name;
+    int ev;           // index of the first of two events in the pool
+    long long cells;  // cells the launch was scheduled over (all problems of its launch map)
+};
+
+const char *kname(const char *base, int level, bool fp32);
+
+class StructBatch {
+public:
+    struct Level {
+        long long ntot = 0;
+        long long all_cells = 0, smooth_cells = 0, coarse_cells = 0;
+        std::vector<LevelDesc> h_desc;
+        LevelDesc *d_desc = nullptr;
+        BlockMap all, smooth;          // every problem with this level / those for which it is not the coarsest
+        std::vector<int> coarse_list;  // problems whose coarsest level this is
+        int *d_coarse = nullptr;
+        uint8_t *dir = nullptr;        // identity (Dirichlet) rows
+        double *c64[4] = {nullptr, nullptr, nullptr, nullptr};  // cx, cy, cz, leak
+        float *c32[4] = {nullptr, nullptr, nullptr, nullptr};
+        void *work[4] = {nullptr, nullptr, nullptr, nullptr};   // xa, xb, b, d (V-cycle precision)
+    };
+
+    StructBatch(const std::vector<GridSpec> &grids, const std::vector<std::vector<int64_t>> &dnodes,
+                const dpf_options &opt, cudaStream_t stream);
+    ~StructBatch();
+    StructBatch(const StructBatch &) = delete;
+    StructBatch &operator=(const StructBatch &) = delete;
+
+    // operations (device pointers, all ordered on `stream`)
+    void assemble(const double *Ks, const double *logK, int kind, const double *shift, bool init_x);
+    void solve(const double *b, double *x, double reltol);
+    void forward(const double *Ks, const double *logK, int kind);
+    void adjoint_solve();  // lam = A^-1 delta (Dirichlet rows 0)
+    void obs_delta(const long long *d_obs, long long nobs);
+    void grad_faces(const double *hv, const double *lv_, double *dKs, bool accumulate);
+    void grad_logk(double *g);
+    void grad_dh_q(const double *lv_, double *ddh, double *dQs, bool with_delta, bool accumulate);
+    void logk_to_faces(const double *logK, int kind, double *Ks);
+    void logk_vjp(const double *logK, int kind, const double *dKs, double *g);
+    void apply(const double *x, double *y);
+    void set_shift(const double *Ss, double dt);
+    void transient_step(const double *b0, const double *hprev);
+
+    template <typename T>
+    void vcycle(const T *r, T *z);
+    template <typename T>
+    void pcg(const T *b, T *x, double tol2, bool gated);
+    int read_count(int which);
+    void *ir_e();
+
+    // configuration and sizes
+    dpf_options opt;
+    cudaStream_t stream;
+    bool mixed = false;
+    int nprob = 0, nlev_max = 0;
+    std::vector<int> nlev;
+    std::vector<long long> ndir;   // distinct Dirichlet cells per problem
+    std::vector<Level> lv;
+    long long N = 0, F = 0, nfree_total = 0;
+    std::vector<long long> cell_off, face_off;
+    std::vector<ProbParam> prm;
+    ProbParam *d_prm = nullptr;
+
+    // fine-level FP64 vectors
+    double *h = nullptr, *b64 = nullptr, *r64 = nullptr, *lam = nullptr, *delta = nullptr, *arhs = nullptr;
+    double *in_dh = nullptr, *in_Q = nullptr, *in_logK = nullptr, *in_Ks = nullptr, *shift = nullptr;
+    void *cgv[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // r, z, p, q, r32 (CG precision)
+    float *ir_e_buf = nullptr;
+
+    // device state
+    CgState *d_state = nullptr;
+    int *d_count = nullptr;       // [0] active CG problems, [1] problems still refining
+    int *d_factor_status = nullptr;
+    ReduceScratch rs;
+    double *d_coarseL = nullptr;
+    int *h_count = nullptr;
+    void *h_state_buf = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+
+    // Chebyshev
+    double inv_theta = 1.0;
+    std::vector<double> cheb_c1, cheb_c2;
+
+    // last-call bookkeeping
+    bool have_operator = false, have_forward = false;
+    int fwd_kind = 0, mean_kind = 0;
+    int last_status = DPF_OK, stats_iters = 0, stats_outer = 0;
+    double stats_relres = 0.0;
+    std::string last_message;
+
+    // launch counting / per-kernel timing
+    long long launches = 0;
+    bool prof_on = false;
+    std::vector<ProfRec> prof_recs;
+    std::vector<cudaEvent_t> ev_pool;
+    void profile(bool on);
+    int profile_report(int cap, const char **names, long long *counts, double *ms, long long *cells);
+
+    std::vector<void *> owned;
+};
+
+}  // namespace dpf

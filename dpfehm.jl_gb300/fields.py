@@ -1,0 +1,46 @@
+"""Seeded synthetic log-conductivity fields with Matern covariance.
+
+The reference samples log-conductivity with GaussianRandomFields' Karhunen-Loeve
+expansion (examples/gw_steadystate_3d/inputdeck.jl:30-36), a package absent here.
+This module draws a stationary Gaussian field with Matern covariance
+    C(r) = sigma^2 2^(1-nu)/Gamma(nu) (sqrt(2 nu) r / ell)^nu K_nu(sqrt(2 nu) r / ell)
+by spectral (circulant-embedding style) synthesis on a padded periodic grid: white
+noise is filtered by the square root of the Matern spectral density
+    S(k) proportional to (2 nu / ell^2 + |k|^2)^-(nu + d/2)
+normalised so each point has variance sigma^2. The GPU solve and the oracle both
+consume the same saved field, so parity does not depend on this sampler.
+"""
+import numpy as np
+
+
+def matern_field(ns, spacings, ell, sigma, mean, seed, nu=1.0):
+    """Return an array of shape ``ns`` (node-centred axes with the given spacings)."""
+    ns = tuple(int(n) for n in ns)
+    d = len(ns)
+    rng = np.random.default_rng(seed)
+    pads = []
+    for n, h in zip(ns, spacings):
+        p = int(n + np.ceil(1.5 * ell / h))
+        pads.append(p + (p % 2))
+    freqs = np.meshgrid(*[np.fft.fftfreq(p, h) for p, h in zip(pads, spacings)], indexing="ij", sparse=True)
+    k2 = sum((2.0 * np.pi * f) ** 2 for f in freqs)
+    spec = (2.0 * nu / ell ** 2 + k2) ** (-(nu + d / 2.0))
+    spec /= spec.mean()
+    w = rng.standard_normal(pads)
+    field = np.real(np.fft.ifftn(np.fft.fftn(w) * np.sqrt(spec)))
+    sl = tuple(slice(0, n) for n in ns)
+    return mean + sigma * np.ascontiguousarray(field[sl])
+
+
+def layered_logk(ns3, mins, maxs, ell, sigma, mean, seed):
+    """2-D field in (x, y) copied to every z layer; returned flat in cell order (z fastest)."""
+    n1, n2, n3 = ns3
+    sp = [(maxs[i] - mins[i]) / (ns3[i] - 1) for i in range(2)]
+    f2 = matern_field((n1, n2), sp, ell, sigma, mean, seed)
+    return np.repeat(f2[:, :, None], n3, axis=2).ravel()
+
+
+def volume_logk(ns3, mins, maxs, ell, sigma, mean, seed):
+    """Fully 3-D field; returned flat in cell order (z fastest)."""
+    sp = [(maxs[i] - mins[i]) / (ns3[i] - 1) for i in range(3)]
+    return matern_field(ns3, sp, ell, sigma, mean, seed).ravel()

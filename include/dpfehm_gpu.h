@@ -1,0 +1,208 @@
+/*
+ * dpfehm_gpu.h -- C ABI of the GB300 groundwater solve library (libdpfehm_gpu.so).
+ *
+ * Drop-in boundary for DPFEHM.jl's steady-state groundwater solve and its
+ * ChainRules rrule, plus the transient backward-Euler solve built from the same
+ * residual. Every entry point replaces a piece of the reference named beside it
+ * (paths relative to the DPFEHM.jl project):
+ *
+ *   dpf_create / dpf_create_regular3d   getfreenodes + problem topology
+ *                                       (src/utilities.jl:10-24, src/grid.jl:150-188)
+ *   dpf_steady_forward                  groundwater_steadystate (src/groundwater.jl:75-83)
+ *   dpf_steady_adjoint                  rrule pullback (src/groundwater.jl:85-107)
+ *   dpf_logk_to_faces(_vjp)             caller-side logKs2Ks_neighbors and its Zygote VJP
+ *                                       (examples/gw_steadystate_3d/inputdeck.jl:51;
+ *                                        harmonic mean: src/richards.jl:50-52)
+ *   dpf_transient_forward/_adjoint      backward-Euler stepping of -groundwater_residuals
+ *                                       (src/groundwater.jl:1-21 with specificstorage,
+ *                                        volumes; examples/gw_transient_3d/inputdeck.jl:60-92)
+ *   dpf_batch_*                         many independent problems in one set of launches
+ *                                       (replaces Distributed.pmap replicas,
+ *                                        examples/scott_example/ex.jl:10)
+ *
+ * Conventions
+ *   - Indices are 0-based (the Julia shim subtracts 1).
+ *   - Array arguments may be host or device pointers; the library detects which
+ *     with cudaPointerGetAttributes. Host arrays are copied with cudaMemcpyAsync
+ *     (page-locked host memory gives asynchronous DMA); device arrays are read
+ *     in place.
+ *   - Every call is ordered on the handle's CUDA stream and returns when its
+ *     outputs are complete.
+ *   - A handle is not thread-safe; distinct handles may be used from distinct
+ *     threads.
+ *   - Every function returns a dpf_status; dpf_last_error(h) describes the last
+ *     failure on h (or the last create failure when h is NULL).
+ *   - Nothing falls back to the CPU: without a usable CUDA device every call
+ *     fails with DPF_NO_DEVICE.
+ */
+#ifndef DPFEHM_GPU_H
+#define DPFEHM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    DPF_OK = 0,
+    DPF_BAD_INPUT = 1,      /* invalid sizes, indices or options */
+    DPF_NOT_CONVERGED = 2,  /* iteration cap reached; outputs hold the last iterate */
+    DPF_NAN = 3,            /* a residual became NaN/Inf */
+    DPF_OOM = 4,            /* device or pinned allocation failed */
+    DPF_CUDA = 5,           /* a CUDA runtime call failed */
+    DPF_NO_DEVICE = 6,      /* no CUDA device */
+    DPF_STATE = 7,          /* call out of order (e.g. adjoint before forward) */
+    DPF_UNSUPPORTED = 8     /* option not available for this problem kind */
+} dpf_status;
+
+typedef enum { DPF_MEAN_GEOMETRIC = 0, DPF_MEAN_HARMONIC = 1 } dpf_mean_kind;
+
+typedef enum {
+    DPF_PREC_FP64 = 0,  /* FP64 CG with an FP64 V-cycle */
+    DPF_PREC_MIXED = 1  /* FP64 outer residual / iterative refinement around an FP32 CG with an FP32 V-cycle */
+} dpf_precision;
+
+typedef struct dpf_options {
+    double reltol;       /* stop when ||b - A h|| <= reltol * ||b||            (default 1e-10) */
+    int maxiter;         /* CG iteration cap per solve                        (default 500)   */
+    int precision;       /* dpf_precision                                     (default FP64)  */
+    int cheb_degree;     /* Chebyshev smoother degree per pre/post sweep      (default 2)     */
+    double cheb_lo;      /* lower end of the Chebyshev interval / upper end   (default 0.2)   */
+    double coarse_scale; /* scaling of the coarse-grid correction              (default 2.0)   */
+    int max_coarse;      /* coarsen until a level has at most this many cells (default 64, <= 64) */
+    double inner_tol;    /* MIXED: relative tolerance of each inner FP32 solve (default 1e-4)  */
+    int max_outer;       /* MIXED: cap on refinement steps                    (default 12)    */
+    int use_graphs;      /* capture each solve's iteration in a CUDA graph    (default 1)     */
+    int check_every;     /* convergence is read back every this many iterations (default 1)   */
+} dpf_options;
+
+typedef struct dpf_problem dpf_problem;
+
+/* Fill *opts with the defaults listed above. */
+void dpf_default_options(dpf_options *opts);
+
+/* ---------------------------------------------------------------- topology */
+
+/* General topology from the reference's arrays (src/groundwater.jl:75 argument
+ * list): N cells, F faces (nbr_a[f], nbr_b[f], 0-based), areasoverlengths[F],
+ * nd Dirichlet cells. When the faces are exactly those of regulargrid3d
+ * (src/grid.jl:150-188) the matrix-free 7-point path is used, otherwise the CSR
+ * path. volumes may be NULL (unit volumes). opts may be NULL (defaults). */
+int dpf_create(int64_t N, int64_t F, const int64_t *nbr_a, const int64_t *nbr_b, const double *areasoverlengths,
+               const double *volumes, int64_t nd, const int64_t *dirichletnodes, const dpf_options *opts,
+               dpf_problem **out);
+
+/* Regular grid straight from regulargrid3d's arguments (mins, maxs: 3 each; ns = nx, ny, nz). */
+int dpf_create_regular3d(int nx, int ny, int nz, const double *mins, const double *maxs, int64_t nd,
+                         const int64_t *dirichletnodes, const dpf_options *opts, dpf_problem **out);
+
+/* Host-only check (no GPU needed): if the faces/areas are those of regulargrid3d
+ * for some (nx, ny, nz), write them to dims[3] and the three areas-over-lengths
+ * to aol3[3] and return 1; otherwise return 0. */
+int dpf_detect_regular3d(int64_t N, int64_t F, const int64_t *nbr_a, const int64_t *nbr_b,
+                         const double *areasoverlengths, int *dims, double *aol3);
+
+void dpf_destroy(dpf_problem *h);
+const char *dpf_last_error(const dpf_problem *h);
+
+/* Sizes: N, F, number of free cells, 1 if the structured path is in use, number of AMG levels. */
+int dpf_info(const dpf_problem *h, int64_t *N, int64_t *F, int64_t *nfree, int *structured, int *levels);
+
+/* Statistics of the last solve: iterations (CG, summed over refinement steps),
+ * refinement steps, final relative residual ||b - A h|| / ||b|| (FP64). */
+int dpf_last_stats(const dpf_problem *h, int *iterations, int *outer, double *relres);
+
+/* ---------------------------------------------------- steady state + rrule */
+
+/* groundwater_steadystate: Ks[F], dirichleths[N], Qs[N] -> h[N]
+ * (dirichleths copied to the Dirichlet cells). Keeps h on the device for the adjoint. */
+int dpf_steady_forward(dpf_problem *h, const double *Ks, const double *dirichleths, const double *Qs, double *h_out);
+
+/* rrule pullback for cotangent delta[N] of the last forward solve:
+ * dKs[F], ddirichleths[N], dQs[N] (any output may be NULL). The forward
+ * hierarchy is reused (the operator is symmetric). */
+int dpf_steady_adjoint(dpf_problem *h, const double *delta, double *dKs, double *ddirichleths, double *dQs);
+
+/* Face conductances from cell log-conductivities (structured or general). */
+int dpf_logk_to_faces(dpf_problem *h, const double *logK, int mean_kind, double *Ks);
+/* dlogK[N] = (dKs/dlogK)^T dKs */
+int dpf_logk_to_faces_vjp(dpf_problem *h, const double *logK, int mean_kind, const double *dKs, double *dlogK);
+
+/* Fused forward from logK (face means computed on the device, no Ks round trip). */
+int dpf_steady_forward_logk(dpf_problem *h, const double *logK, int mean_kind, const double *dirichleths,
+                            const double *Qs, double *h_out);
+/* Fused adjoint straight to dlogK[N] (and optionally ddirichleths, dQs). Requires
+ * the last forward to have been dpf_steady_forward_logk. */
+int dpf_steady_adjoint_logk(dpf_problem *h, const double *delta, double *dlogK, double *ddirichleths, double *dQs);
+
+/* --------------------------------------------------------------- transient */
+
+/* Fixed-step backward Euler of S_i V_i dh_i/dt = Q_i - sum_f K_f aol_f (h_i - h_nb)
+ * (the scaling of src/groundwater.jl:7,15,17): nsteps steps of dt from h0[N]
+ * (values at Dirichlet cells ignored). Writes h at the final step to hT[N] and,
+ * if states != NULL, every step to states[nsteps*N]. Heads of every
+ * checkpoint_every-th step are kept on the device for the adjoint, which
+ * recomputes the others segment by segment (checkpoint_every = 1 keeps all). */
+int dpf_transient_forward(dpf_problem *h, const double *Ks, const double *dirichleths, const double *Qs,
+                          const double *specificstorage, double dt, int nsteps, const double *h0,
+                          int checkpoint_every, double *states, double *hT);
+
+/* Adjoint of the last transient forward for
+ *   J = sum_{n=1..nsteps} sum_k w_k h^n[obs_k]^2  +  gT . h^nsteps
+ * (w may be NULL for unit weights, gT may be NULL). Outputs dKs[F],
+ * ddirichleths[N], dQs[N], dh0[N] (any may be NULL). */
+int dpf_transient_adjoint(dpf_problem *h, int64_t nobs, const int64_t *obs, const double *w, const double *gT,
+                          double *dKs, double *ddirichleths, double *dQs, double *dh0);
+
+/* ------------------------------------------------------------------- batch */
+
+/* nprob independent regular grids (dims[3*p..], mins/maxs[3*p..]) in one handle;
+ * nd[p] Dirichlet cells each, concatenated in dirichletnodes (indices local to
+ * each problem). Per-problem arrays passed to the batch calls are concatenated in
+ * problem order. */
+int dpf_batch_create(int nprob, const int *dims, const double *mins, const double *maxs, const int64_t *nd,
+                     const int64_t *dirichletnodes, const dpf_options *opts, dpf_problem **out);
+
+/* Offsets of problem p's cells / faces in concatenated arrays (p = nprob gives totals). */
+int dpf_batch_offsets(const dpf_problem *h, int p, int64_t *cell_offset, int64_t *face_offset);
+
+/* Forward + adjoint of every problem from concatenated logK; delta for the
+ * adjoint is J_p = sum_k h_p[obs]^2 over each problem's observation cells
+ * (obs_offsets[nprob+1] into obs, local indices). Outputs h[N_total] and
+ * dlogK[N_total] (either may be NULL). */
+int dpf_batch_solve_grad_logk(dpf_problem *h, const double *logK, int mean_kind, const double *dirichleths,
+                              const double *Qs, const int64_t *obs_offsets, const int64_t *obs, double *h_out,
+                              double *dlogK);
+
+/* Same as dpf_batch_solve_grad_logk for a single problem (nprob = 1 handles of
+ * any kind): forward, objective sum_k h[obs_k]^2, adjoint to dlogK. */
+int dpf_solve_grad_logk(dpf_problem *h, const double *logK, int mean_kind, const double *dirichleths,
+                        const double *Qs, int64_t nobs, const int64_t *obs, double *h_out, double *dlogK);
+
+/* ----------------------------------------------------------- diagnostics */
+
+/* Apply the assembled operator (last forward) to x[N]: y = A x, Dirichlet rows identity. */
+int dpf_apply_operator(dpf_problem *h, const double *x, double *y);
+
+/* ------------------------------------------------------------ diagnostics */
+
+/* Start (enable != 0) or stop per-kernel timing: while on, every kernel launch on
+ * the handle's stream is bracketed by CUDA events. Enabling clears earlier records. */
+int dpf_profile(dpf_problem *h, int enable);
+
+/* Per-kernel totals of the records since dpf_profile(h, 1): up to cap entries of
+ * kernel name ("kernel<f64|f32>/L<multigrid level>"), launches, summed device
+ * milliseconds and summed cells the launches were scheduled over (any output
+ * array may be NULL). Returns the number of distinct kernels (negative
+ * dpf_status on error). Names stay valid for the lifetime of the library. */
+int dpf_profile_report(dpf_problem *h, int cap, const char **names, long long *launches, double *ms,
+                       long long *cells);
+
+/* Kernel launches issued by the handle since it was created. */
+long long dpf_launch_count(const dpf_problem *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,117 @@
+"""The C-ABI library loads, exports every symbol declared in include/*.h, and its
+host-only pieces work without a GPU (no compute calls here)."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_symbols():
+    names = set()
+    for hdr in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(hdr).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"\b(dpf_[a-z0-9_]+)\s*\(", src))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib(pkg):
+    import __graft_entry__ as g
+    g._load_build_module().build()
+    return pkg.load()
+
+
+def test_header_declares_entry_points():
+    names = _declared_symbols()
+    for must in ["dpf_create", "dpf_steady_forward", "dpf_steady_adjoint", "dpf_logk_to_faces",
+                 "dpf_transient_forward", "dpf_transient_adjoint", "dpf_batch_create", "dpf_destroy",
+                 "dpf_last_error"]:
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in _declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_bindings_cover_header(pkg):
+    from importlib import import_module
+    _lib = import_module(pkg.__name__ + "._lib")
+    assert set(_declared_symbols()) <= set(_lib.SIGNATURES)
+
+
+def test_default_options(pkg, lib):
+    o = pkg.default_options()
+    assert o.reltol == 1e-10 and o.maxiter == 500 and o.precision == pkg.PREC_FP64
+    assert o.cheb_degree == 2 and o.max_coarse == 64
+
+
+@pytest.mark.parametrize("ns", [(4, 3, 2), (7, 1, 5), (1, 6, 3), (5, 4, 1), (9, 1, 1), (1, 1, 8), (3, 3, 3)])
+def test_detect_regular3d(pkg, lib, ns):
+    coords, nb, aol, vol = pkg.regulargrid3d((0, 0, 0), (1.5, 2.0, 3.0), [max(n, 1) for n in ns])
+    N = coords.shape[1]
+    a = np.ascontiguousarray(nb[:, 0])
+    b = np.ascontiguousarray(nb[:, 1])
+    dims = (ctypes.c_int * 3)()
+    a3 = (ctypes.c_double * 3)()
+    ok = lib.dpf_detect_regular3d(N, len(nb), a.ctypes.data, b.ctypes.data, aol.ctypes.data, dims, a3)
+    assert ok == 1
+    assert np.prod(list(dims)) == N
+    # the detected grid regenerates the same face list (a unit axis may be reported in another slot)
+    _, nb2, aol2, _ = pkg.regulargrid3d((0, 0, 0), (1, 1, 1), list(dims))
+    assert np.array_equal(nb2, nb)
+    d = np.array(list(dims))
+    for k in range(3):
+        if d[k] > 1:
+            sel = (nb2[:, 1] - nb2[:, 0]) == int(np.prod(d[k + 1:]))
+            assert np.allclose(aol[sel], a3[k])
+
+
+def test_detect_rejects_general_graph(pkg, lib):
+    coords, nb, aol, vol = pkg.regulargrid3d((0, 0, 0), (1, 1, 1), (4, 4, 4))
+    nb2 = nb.copy()
+    nb2[[3, 4]] = nb2[[4, 3]]  # reordered faces are no longer the regulargrid3d list
+    a, b = np.ascontiguousarray(nb2[:, 0]), np.ascontiguousarray(nb2[:, 1])
+    aol = np.ascontiguousarray(aol)
+    assert lib.dpf_detect_regular3d(64, len(nb2), a.ctypes.data, b.ctypes.data, aol.ctypes.data, None, None) == 0
+    aol2 = aol.copy()
+    aol2[5] *= 1.01  # non-uniform areas over lengths
+    a, b = np.ascontiguousarray(nb[:, 0]), np.ascontiguousarray(nb[:, 1])
+    assert lib.dpf_detect_regular3d(64, len(nb), a.ctypes.data, b.ctypes.data, aol2.ctypes.data, None, None) == 0
+
+
+def test_regulargrid2d_is_regular(pkg, lib):
+    coords, nb, aol, vol = pkg.regulargrid2d((-1, -1), (1, 1), (6, 5), 3.0)
+    a, b = np.ascontiguousarray(nb[:, 0]), np.ascontiguousarray(nb[:, 1])
+    dims = (ctypes.c_int * 3)()
+    a3 = (ctypes.c_double * 3)()
+    assert lib.dpf_detect_regular3d(30, len(nb), a.ctypes.data, b.ctypes.data, np.ascontiguousarray(aol).ctypes.data,
+                                    dims, a3) == 1
+    assert tuple(dims) == (6, 5, 1)
+
+
+def test_missing_library_fails_loudly(pkg, tmp_path):
+    from importlib import import_module
+    _lib = import_module(pkg.__name__ + "._lib")
+    with pytest.raises(OSError):
+        saved = _lib._lib
+        _lib._lib = None
+        try:
+            _lib.load(str(tmp_path / "nope.so"))
+        finally:
+            _lib._lib = saved
+
+
+def test_create_without_device_reports_no_device(pkg, lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    with pytest.raises(pkg.DPFError) as e:
+        pkg.GroundwaterProblem.regular3d((0, 0, 0), (1, 1, 1), (3, 3, 3), [26])
+    assert e.value.code == 6
