@@ -146,41 +146,35 @@ __global__ void k_prolong_cheb(const LevelDesc *__restrict__ desc, const LevelDe
     }
 }
 
-// Coarsest level: x = A^-1 b with the stored Cholesky factor, one warp per problem.
-// With FUSE_RZ (a problem whose finest level is its coarsest) it also sets rz and beta.
+// Coarsest level: x = A^-1 b with the stored dense inverse (symmetric), one block of
+// kMaxCoarse threads per problem. With FUSE_RZ (a problem whose finest level is its
+// coarsest) it also sets rz and beta.
 template <typename T, bool FUSE_RZ>
 __global__ void k_coarse_solve(const LevelDesc *__restrict__ desc, const int *__restrict__ plist, CgState *st,
-                               const double *__restrict__ Lbuf, const T *__restrict__ b, T *__restrict__ x) {
+                               const double *__restrict__ Inv, const T *__restrict__ b, T *__restrict__ x) {
     const int p = plist[blockIdx.x];
     if (st && !st[p].active) return;
     const LevelDesc L = desc[p];
     const int n = (int)L.n;
-    const double *Lp = Lbuf + (long long)p * kMaxCoarse * kMaxCoarse;
-    __shared__ double y[kMaxCoarse];
-    const int lane = threadIdx.x;
-    if (threadIdx.x >= 32) return;
-    for (int i = 0; i < n; i++) {
-        double s = 0.0;
-        for (int k = lane; k < i; k += 32) s += Lp[i * kMaxCoarse + k] * y[k];
-        s = warp_sum(s);
-        if (lane == 0) y[i] = ((double)b[L.off + i] - s) / Lp[i * kMaxCoarse + i];
-        __syncwarp();
-    }
-    for (int i = n - 1; i >= 0; i--) {
-        double s = 0.0;
-        for (int k = i + 1 + lane; k < n; k += 32) s += Lp[k * kMaxCoarse + i] * y[k];
-        s = warp_sum(s);
-        if (lane == 0) y[i] = (y[i] - s) / Lp[i * kMaxCoarse + i];
-        __syncwarp();
-    }
-    double rz = 0.0;
-    for (int i = lane; i < n; i += 32) {
-        x[L.off + i] = (T)y[i];
-        if (FUSE_RZ) rz += (double)b[L.off + i] * (double)(T)y[i];
-    }
+    const double *Ip = Inv + (long long)p * kMaxCoarse * kMaxCoarse;
+    __shared__ double bs[kMaxCoarse];
+    __shared__ double red[kMaxCoarse / 32];
+    const int i = threadIdx.x;
+    if (i < n) bs[i] = (double)b[L.off + i];
+    __syncthreads();
+    double xi = 0.0;
+    if (i < n)
+        for (int j = 0; j < n; j++) xi += Ip[j * kMaxCoarse + i] * bs[j];
+    T xo = (T)xi;
+    if (i < n) x[L.off + i] = xo;
     if (FUSE_RZ) {
-        rz = warp_sum(rz);
-        if (lane == 0) {
+        double v = i < n ? bs[i] * (double)xo : 0.0;
+        v = warp_sum(v);
+        if ((i & 31) == 0) red[i >> 5] = v;
+        __syncthreads();
+        if (i == 0) {
+            double rz = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) rz += red[w];
             CgState &s = st[p];
             s.rz_old = s.rz;
             s.rz = rz;
@@ -930,13 +924,13 @@ void StructBatch::vcycle(const T *r, T *z) {
             if (l == 0)
                 {
                     KTimer _kt(this, kname("k_coarse_solve", l, sizeof(T) == 4), L.coarse_cells);
-                    k_coarse_solve<T, true><<<(unsigned)L.coarse_list.size(), 32, 0, stream>>>(
+                    k_coarse_solve<T, true><<<(unsigned)L.coarse_list.size(), kMaxCoarse, 0, stream>>>(
                         L.d_desc, L.d_coarse, d_state, d_coarseL, b, out);
                 }
             else
                 {
                     KTimer _kt(this, kname("k_coarse_solve", l, sizeof(T) == 4), L.coarse_cells);
-                    k_coarse_solve<T, false><<<(unsigned)L.coarse_list.size(), 32, 0, stream>>>(
+                    k_coarse_solve<T, false><<<(unsigned)L.coarse_list.size(), kMaxCoarse, 0, stream>>>(
                         L.d_desc, L.d_coarse, d_state, d_coarseL, b, out);
                 }
             LAUNCH_CHECK();

@@ -240,13 +240,17 @@ __global__ void k_coarsen(const LevelDesc *__restrict__ fdesc, const LevelDesc *
 }
 
 // ------------------------------------------------------ coarsest level
-// Dense Cholesky of each listed problem's coarsest operator (n <= 64), one block
-// per problem, in shared memory. L is stored row-major with stride kMaxCoarse.
+// Dense inverse of each listed problem's coarsest operator (n <= 64), one block
+// per problem, by in-place Gauss-Jordan elimination in shared memory (no pivoting:
+// the operator is symmetric positive definite, so every pivot is a positive Schur
+// complement). The coarsest solve is then one small matrix-vector product.
+// The inverse is stored row-major with stride kMaxCoarse.
 __global__ void k_coarse_factor(const LevelDesc *__restrict__ desc, const int *__restrict__ plist,
                                 const double *__restrict__ cx, const double *__restrict__ cy,
-                                const double *__restrict__ cz, const double *__restrict__ leak, double *Lout,
+                                const double *__restrict__ cz, const double *__restrict__ leak, double *Inv,
                                 int *status) {
     __shared__ double A[kMaxCoarse][kMaxCoarse + 1];
+    __shared__ double col[kMaxCoarse];
     __shared__ int bad;
     int p = plist[blockIdx.x];
     LevelDesc L = desc[p];
@@ -268,26 +272,28 @@ __global__ void k_coarse_factor(const LevelDesc *__restrict__ desc, const int *_
         A[li][li] = d;
     }
     __syncthreads();
-    for (int j = 0; j < n; j++) {
-        if (threadIdx.x == 0) {
-            double v = A[j][j];
-            if (!(v > 0.0)) { bad = 1; v = 1.0; }
-            A[j][j] = sqrt(v);
-        }
+    for (int k = 0; k < n; k++) {
+        // pivot row k scaled by 1/A[k][k] (with the identity column folded in); save column k
+        double piv = A[k][k];
+        if (!(piv > 0.0)) { if (threadIdx.x == 0) bad = 1; piv = 1.0; }
+        double ip = 1.0 / piv;
         __syncthreads();
-        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) A[i][j] /= A[j][j];
+        for (int i = threadIdx.x; i < n; i += blockDim.x) col[i] = A[i][k];
         __syncthreads();
-        int m = n - j - 1;
-        for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
-            int i = j + 1 + t / m, k = j + 1 + t % m;
-            if (k <= i) A[i][k] -= A[i][j] * A[k][j];
+        for (int j = threadIdx.x; j < n; j += blockDim.x) A[k][j] = (j == k ? 1.0 : A[k][j]) * ip;
+        __syncthreads();
+        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+            int i = t / n, j = t % n;
+            if (i == k) continue;
+            double rk = A[k][j];
+            A[i][j] = (j == k ? 0.0 : A[i][j]) - col[i] * rk;
         }
         __syncthreads();
     }
-    double *Lp = Lout + (long long)p * kMaxCoarse * kMaxCoarse;
+    double *Ip = Inv + (long long)p * kMaxCoarse * kMaxCoarse;
     for (int k = threadIdx.x; k < kMaxCoarse * kMaxCoarse; k += blockDim.x) {
         int i = k / kMaxCoarse, j = k % kMaxCoarse;
-        Lp[k] = (i < n && j <= i) ? A[i][j] : 0.0;
+        Ip[k] = (i < n && j < n) ? A[i][j] : 0.0;
     }
     if (threadIdx.x == 0 && bad) atomicExch(status, 1);
 }

@@ -32,15 +32,19 @@ def matern_field(ns, spacings, ell, sigma, mean, seed, nu=1.0):
     return mean + sigma * np.ascontiguousarray(field[sl])
 
 
+def _spacing(lo, hi, n):
+    return (hi - lo) / (n - 1) if n > 1 and hi != lo else 1.0
+
+
 def layered_logk(ns3, mins, maxs, ell, sigma, mean, seed):
     """2-D field in (x, y) copied to every z layer; returned flat in cell order (z fastest)."""
     n1, n2, n3 = ns3
-    sp = [(maxs[i] - mins[i]) / (ns3[i] - 1) for i in range(2)]
+    sp = [_spacing(mins[i], maxs[i], ns3[i]) for i in range(2)]
     f2 = matern_field((n1, n2), sp, ell, sigma, mean, seed)
     return np.repeat(f2[:, :, None], n3, axis=2).ravel()
 
 
 def volume_logk(ns3, mins, maxs, ell, sigma, mean, seed):
     """Fully 3-D field; returned flat in cell order (z fastest)."""
-    sp = [(maxs[i] - mins[i]) / (ns3[i] - 1) for i in range(3)]
+    sp = [_spacing(mins[i], maxs[i], ns3[i]) for i in range(3)]
     return matern_field(ns3, sp, ell, sigma, mean, seed).ravel()
