@@ -29,7 +29,18 @@ struct LevelDesc {                 // one problem at one level
     int nx, ny, nz, pad;
     long long n;                   // cells
     long long off;                 // offset of the problem's cells in the level arrays
+    unsigned mag_nz, mag_ny;       // invariant-integer division by nz and ny (see fast_div)
+    int sh_nz, sh_ny;
 };
+
+// Division by an invariant integer d >= 1 for numerators n < 2^31 (Granlund and
+// Montgomery, "Division by invariant integers using multiplication", 1994):
+// l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1, q = (mulhi(n, m) + n) >> l.
+inline void fast_div_magic(unsigned d, unsigned &m, int &l) {
+    l = 0;
+    while ((1ull << l) < d) l++;
+    m = (unsigned)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+}
 
 struct BlockMap {                  // launch map: block -> (problem, block within problem)
     int2 *d_map = nullptr;         // [nblocks]
@@ -67,6 +78,7 @@ struct ProbParam {                 // per-problem constants of a regular grid
 template <typename T>
 struct Coeffs {
     const T *cx, *cy, *cz, *leak;
+    const T *idg;                  // inverse diagonal (FP64 levels), or null: computed on the fly
 };
 
 }  // namespace dpf

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <set>
 #include <stdexcept>
 
@@ -41,7 +42,9 @@ __global__ void k_cheb_first(const LevelDesc *__restrict__ desc, const int2 *__r
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     Cell c;
     if (!decode_cell(L, bm.y, c)) return;
-    T v = invtheta * b[c.i] / diag7(L, c, C);
+    T v;
+    if constexpr (sizeof(T) == 8) v = invtheta * b[c.i] * C.idg[c.i];
+    else v = invtheta * __fdividef(b[c.i], diag7(L, c, C));
     x[c.i] = v;
     d[c.i] = v;
 }
@@ -55,21 +58,21 @@ __global__ void k_cheb_step(const LevelDesc *__restrict__ desc, const int2 *__re
                             T *__restrict__ d, T c1, T c2, ReduceScratch rs, const int2 *__restrict__ pinfo) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     Cell c;
-    double part = 0.0;
+    Acc<T> part;
     if (decode_cell(L, bm.y, c)) {
         T xi = xin[c.i], Ax, dg;
         apply7(L, c, C, xi, [&](long long j, int, int, int) { return xin[j]; }, Ax, dg);
         T bi = b[c.i];
-        T r = (bi - Ax) / dg;
+        T r = dinv_times(C, c.i, bi - Ax, dg);
         T dn = c1 * d[c.i] + c2 * r;
         T xo = xi + dn;
         d[c.i] = dn;
         xout[c.i] = xo;
-        if (FUSE_RZ) part = (double)bi * (double)xo;
+        if (FUSE_RZ) part = Acc<T>::prod(bi, xo);
     }
     if (FUSE_RZ) {
         double2 tot;
-        if (reduce_last(part, 0.0, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+        if (reduce_last<T>(part, Acc<T>(), rs, pinfo[p], p, tot) && threadIdx.x == 0) {
             CgState &s = st[p];
             s.rz_old = s.rz;
             s.rz = tot.x;
@@ -119,7 +122,7 @@ __global__ void k_prolong_cheb(const LevelDesc *__restrict__ desc, const LevelDe
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     const LevelDesc Lc = cdesc[p];
     Cell c;
-    double part = 0.0;
+    Acc<T> part;
     if (decode_cell(L, bm.y, c)) {
         auto xp = [&](long long j, int jx, int jy, int jz) -> T {
             T v = x[j];
@@ -129,15 +132,15 @@ __global__ void k_prolong_cheb(const LevelDesc *__restrict__ desc, const LevelDe
         T xi = xp(c.i, c.ix, c.iy, c.iz), Ax, dg;
         apply7(L, c, C, xi, xp, Ax, dg);
         T bi = b[c.i];
-        T dn = invtheta * (bi - Ax) / dg;
+        T dn = invtheta * dinv_times(C, c.i, bi - Ax, dg);
         T xo = xi + dn;
         d[c.i] = dn;
         xout[c.i] = xo;
-        if (FUSE_RZ) part = (double)bi * (double)xo;
+        if (FUSE_RZ) part = Acc<T>::prod(bi, xo);
     }
     if (FUSE_RZ) {
         double2 tot;
-        if (reduce_last(part, 0.0, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+        if (reduce_last<T>(part, Acc<T>(), rs, pinfo[p], p, tot) && threadIdx.x == 0) {
             CgState &s = st[p];
             s.rz_old = s.rz;
             s.rz = tot.x;
@@ -195,18 +198,18 @@ __global__ void k_cg_start(const LevelDesc *__restrict__ desc, const int2 *__res
     if (gated && !st[p].outer_active) return;
     const LevelDesc L = desc[p];
     Cell c;
-    double rr = 0.0, bb = 0.0;
+    Acc<T> rr, bb;
     if (decode_cell(L, bm.y, c)) {
         T xi = x[c.i], Ax, dg;
         apply7(L, c, C, xi, [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
         T bi = b[c.i];
         T ri = bi - Ax;
         r[c.i] = ri;
-        rr = (double)ri * (double)ri;
-        bb = (double)bi * (double)bi;
+        rr = Acc<T>::prod(ri, ri);
+        bb = Acc<T>::prod(bi, bi);
     }
     double2 tot;
-    if (reduce_last(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+    if (reduce_last<T>(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
         CgState &s = st[p];
         s.rr = tot.x;
         s.bb = tot.y;
@@ -230,15 +233,15 @@ __global__ void k_spmv_pq(const LevelDesc *__restrict__ desc, const int2 *__rest
                           const T *__restrict__ pv, T *__restrict__ q) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     Cell c;
-    double part = 0.0;
+    Acc<T> part;
     if (decode_cell(L, bm.y, c)) {
         T pi = pv[c.i], Ax, dg;
         apply7(L, c, C, pi, [&](long long j, int, int, int) { return pv[j]; }, Ax, dg);
         q[c.i] = Ax;
-        part = (double)pi * (double)Ax;
+        part = Acc<T>::prod(pi, Ax);
     }
     double2 tot;
-    if (reduce_last(part, 0.0, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+    if (reduce_last<T>(part, Acc<T>(), rs, pinfo[p], p, tot) && threadIdx.x == 0) {
         CgState &s = st[p];
         s.pq = tot.x;
         if (!isfinite(s.pq)) { s.alpha = 0.0; s.status = DPF_NAN; deactivate(s, active_count); }
@@ -255,16 +258,16 @@ __global__ void k_update_xr(const LevelDesc *__restrict__ desc, const int2 *__re
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     const double alpha = st[p].alpha;
     Cell c;
-    double part = 0.0;
+    Acc<T> part;
     if (decode_cell(L, bm.y, c)) {
         T a = (T)alpha;
         x[c.i] += a * pv[c.i];
         T ri = r[c.i] - a * q[c.i];
         r[c.i] = ri;
-        part = (double)ri * (double)ri;
+        part = Acc<T>::prod(ri, ri);
     }
     double2 tot;
-    if (reduce_last(part, 0.0, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+    if (reduce_last<T>(part, Acc<T>(), rs, pinfo[p], p, tot) && threadIdx.x == 0) {
         CgState &s = st[p];
         s.rr = tot.x;
         s.iters++;
@@ -297,18 +300,18 @@ __global__ void k_ir_residual(const LevelDesc *__restrict__ desc, const int2 *__
     if (!st[p].outer_active) return;
     const LevelDesc L = desc[p];
     Cell c;
-    double rr = 0.0, bb = 0.0;
+    Acc<double> rr, bb;
     if (decode_cell(L, bm.y, c)) {
         double xi = h[c.i], Ax, dg;
         apply7(L, c, C, xi, [&](long long j, int, int, int) { return h[j]; }, Ax, dg);
         double bi = b[c.i];
         double ri = bi - Ax;
         r[c.i] = ri;
-        rr = ri * ri;
-        bb = bi * bi;
+        rr.v = ri * ri;
+        bb.v = bi * bi;
     }
     double2 tot;
-    if (reduce_last(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+    if (reduce_last<double>(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
         CgState &s = st[p];
         s.orr = tot.x;
         if (s.outer == 0) s.obb = tot.y;
@@ -351,16 +354,16 @@ __global__ void k_ir_update(const LevelDesc *__restrict__ desc, const int2 *__re
     const LevelDesc L = desc[p];
     const double sc = st[p].scale;
     Cell c;
-    double ee = 0.0, hh = 0.0;
+    Acc<double> ee, hh;
     if (decode_cell(L, bm.y, c)) {
         double de = sc * (double)e[c.i];
         double hn = h[c.i] + de;
         h[c.i] = hn;
-        ee = de * de;
-        hh = hn * hn;
+        ee.v = de * de;
+        hh.v = hn * hn;
     }
     double2 tot;
-    if (reduce_last(ee, hh, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+    if (reduce_last<double>(ee, hh, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
         st[p].ee = tot.x;
         st[p].hh = tot.y;
     }
@@ -447,9 +450,9 @@ __global__ void k_grad_faces(const LevelDesc *__restrict__ desc, const int2 *__r
 }
 
 // dlogK_i = sum over the faces of i of dK_f/dlogK_i * dKs_f, with dKs_f formed on the fly
-// from h and lambda (geometric: dK/dlogK_i = K_f / 2; harmonic: K_f^2 / (2 K_i)).
+// from h and lambda; K_f and its derivative come from the per-cell values kc.
 __global__ void k_grad_logk(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
-                            const ProbParam *__restrict__ prm, const double *__restrict__ logK, int kind,
+                            const ProbParam *__restrict__ prm, const double *__restrict__ kc, int kind,
                             const double *__restrict__ h, const double *__restrict__ lam, double *__restrict__ g) {
     int2 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
@@ -459,7 +462,7 @@ __global__ void k_grad_logk(const LevelDesc *__restrict__ desc, const int2 *__re
     const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
     const int co[3] = {c.ix, c.iy, c.iz};
     const int nn[3] = {L.nx, L.ny, L.nz};
-    const double hi = h[c.i], li = lam[c.i], lki = logK[c.i];
+    const double hi = h[c.i], li = lam[c.i], ki = kc[c.i];
     double acc = 0.0;
 #pragma unroll
     for (int d = 0; d < 3; d++) {
@@ -469,12 +472,32 @@ __global__ void k_grad_logk(const LevelDesc *__restrict__ desc, const int2 *__re
             if (!ok) continue;
             long long j = c.i + s * st3[d];
             double dK = -P.aol[d] * (hi - h[j]) * (li - lam[j]);
-            double K = face_mean(lki, logK[j], kind);
-            double w = kind == DPF_MEAN_GEOMETRIC ? 0.5 * K : K * K * 0.5 * exp(-lki);
-            acc += w * dK;
+            double K = face_mean_k(ki, kc[j], kind);
+            acc += face_mean_dlogk(K, ki, kind) * dK;
         }
     }
     g[c.i] = acc;
+}
+
+// per-cell values for the face means: exp(logK / 2) (geometric) or exp(logK) (harmonic)
+__global__ void k_cell_k(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+                         const double *__restrict__ logK, int kind, double *__restrict__ kc) {
+    int2 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    Cell c;
+    if (!decode_cell(L, bm.y, c)) return;
+    double v = logK[c.i];
+    kc[c.i] = exp(kind == DPF_MEAN_GEOMETRIC ? 0.5 * v : v);
+}
+
+// inverse diagonal of an FP64 level (the FP64 smoother multiplies instead of dividing)
+__global__ void k_invdiag(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, Coeffs<double> C,
+                          double *__restrict__ idg) {
+    int2 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    Cell c;
+    if (!decode_cell(L, bm.y, c)) return;
+    idg[c.i] = 1.0 / diag7(L, c, C);
 }
 
 // ddirichleths_k = delta_k + sum over free neighbours j of K_f aol_f lambda_j (Dirichlet k);
@@ -512,9 +535,9 @@ __global__ void k_grad_dh_q(const LevelDesc *__restrict__ desc, const int2 *__re
     if (accumulate) ddh[c.i] += acc; else ddh[c.i] = acc;
 }
 
-// Ks in the reference face order from logK
+// Ks in the reference face order from the per-cell values kc
 __global__ void k_logk_to_faces(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
-                                const ProbParam *__restrict__ prm, const double *__restrict__ logK, int kind,
+                                const ProbParam *__restrict__ prm, const double *__restrict__ kc, int kind,
                                 double *__restrict__ Ks) {
     int2 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
@@ -527,12 +550,12 @@ __global__ void k_logk_to_faces(const LevelDesc *__restrict__ desc, const int2 *
     for (int d = 0; d < 3; d++)
         if (co[d] + 1 < nn[d])
             Ks[P.face_off + regular_face_index(L.nx, L.ny, L.nz, c.ix, c.iy, c.iz, d)] =
-                face_mean(logK[c.i], logK[c.i + st3[d]], kind);
+                face_mean_k(kc[c.i], kc[c.i + st3[d]], kind);
 }
 
 // dlogK from dKs (gather over the six faces of each cell)
 __global__ void k_logk_vjp(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
-                           const ProbParam *__restrict__ prm, const double *__restrict__ logK, int kind,
+                           const ProbParam *__restrict__ prm, const double *__restrict__ kc, int kind,
                            const double *__restrict__ dKs, double *__restrict__ g) {
     int2 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
@@ -542,7 +565,7 @@ __global__ void k_logk_vjp(const LevelDesc *__restrict__ desc, const int2 *__res
     const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
     const int co[3] = {c.ix, c.iy, c.iz};
     const int nn[3] = {L.nx, L.ny, L.nz};
-    const double lki = logK[c.i];
+    const double ki = kc[c.i];
     double acc = 0.0;
     for (int d = 0; d < 3; d++)
         for (int s = -1; s <= 1; s += 2) {
@@ -552,9 +575,8 @@ __global__ void k_logk_vjp(const LevelDesc *__restrict__ desc, const int2 *__res
             int ax = c.ix, ay = c.iy, az = c.iz;
             if (s < 0) { if (d == 0) ax--; else if (d == 1) ay--; else az--; }
             long long f = P.face_off + regular_face_index(L.nx, L.ny, L.nz, ax, ay, az, d);
-            double K = face_mean(lki, logK[j], kind);
-            double w = kind == DPF_MEAN_GEOMETRIC ? 0.5 * K : K * K * 0.5 * exp(-lki);
-            acc += w * dKs[f];
+            double K = face_mean_k(ki, kc[j], kind);
+            acc += face_mean_dlogk(K, ki, kind) * dKs[f];
         }
     g[c.i] = acc;
 }
@@ -589,6 +611,16 @@ static T *dalloc(size_t n, std::vector<void *> &owned) {
     }
     owned.push_back(p);
     return (T *)p;
+}
+
+// host check of the invariant-integer division on the numerators a level can produce
+static void check_fast_div(unsigned d, unsigned m, int l, unsigned nmax) {
+    auto q = [&](unsigned n) { return (unsigned)(((unsigned long long)n * m >> 32) + n) >> l; };
+    unsigned probes[] = {0u, 1u, d - 1, d, d + 1, 2 * d - 1, nmax > 0 ? nmax - 1 : 0, nmax, nmax / 2, nmax / 3};
+    for (unsigned n : probes)
+        if (q(n) != n / d) throw DpfError("invariant-integer division self-check failed", DPF_CUDA);
+    for (unsigned n = 0; n < nmax && n < 4096; n++)
+        if (q(n) != n / d) throw DpfError("invariant-integer division self-check failed", DPF_CUDA);
 }
 
 static BlockMap build_map(const std::vector<LevelDesc> &desc, const std::vector<int> &take, std::vector<void *> &own,
@@ -641,7 +673,10 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
     int maxblocks = 0;
     for (int l = 0; l < nlev_max; l++) {
         Level &L = lv[l];
-        L.h_desc.assign(nprob, LevelDesc{1, 1, 1, 0, 0, 0});
+        LevelDesc unit{1, 1, 1, 0, 0, 0, 0, 0, 0, 0};
+        fast_div_magic(1u, unit.mag_nz, unit.sh_nz);
+        fast_div_magic(1u, unit.mag_ny, unit.sh_ny);
+        L.h_desc.assign(nprob, unit);
         long long off = 0;
         std::vector<int> has(nprob, 0), smooth(nprob, 0);
         for (int p = 0; p < nprob; p++) {
@@ -651,6 +686,10 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
             D.nx = d[0]; D.ny = d[1]; D.nz = d[2];
             D.n = (long long)d[0] * d[1] * d[2];
             D.off = off;
+            fast_div_magic((unsigned)d[2], D.mag_nz, D.sh_nz);
+            fast_div_magic((unsigned)d[1], D.mag_ny, D.sh_ny);
+            check_fast_div((unsigned)d[2], D.mag_nz, D.sh_nz, (unsigned)D.n);
+            check_fast_div((unsigned)d[1], D.mag_ny, D.sh_ny, (unsigned)(D.n / d[2]));
             off += D.n;
             has[p] = 1;
             smooth[p] = l < nlev[p] - 1;
@@ -677,6 +716,8 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         L.c64[2] = dalloc<double>(n, owned); L.c64[3] = dalloc<double>(n, owned);
         if (mixed) {
             for (int k = 0; k < 4; k++) L.c32[k] = dalloc<float>(n, owned);
+        } else {
+            L.idg64 = dalloc<double>(n, owned);
         }
         size_t vs = mixed ? sizeof(float) : sizeof(double);
         for (int k = 0; k < 4; k++) L.work[k] = dalloc<char>(n * vs, owned);
@@ -732,19 +773,21 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
     in_dh = dalloc<double>(N, owned);
     in_Q = dalloc<double>(N, owned);
     in_logK = dalloc<double>(N, owned);
+    in_kc = dalloc<double>(N, owned);
+    aux_kc = dalloc<double>(N, owned);
     in_Ks = dalloc<double>(F, owned);
     size_t vs = mixed ? sizeof(float) : sizeof(double);
     for (int k = 0; k < 5; k++) cgv[k] = dalloc<char>(N * vs, owned);
     // state, reductions, coarse factors
     d_state = dalloc<CgState>(nprob, owned);
-    d_count = dalloc<int>(2, owned);
+    d_count = dalloc<int>(4, owned);
     d_factor_status = dalloc<int>(1, owned);
     rs.partials = dalloc<double2>(std::max(maxblocks, 1), owned);
     rs.tickets = dalloc<unsigned>(nprob, owned);
     rs.capacity = maxblocks;
     CK(cudaMemset(rs.tickets, 0, nprob * sizeof(unsigned)));
     d_coarseL = dalloc<double>((size_t)nprob * kMaxCoarse * kMaxCoarse, owned);
-    CK(cudaMallocHost(&h_count, 2 * sizeof(int)));
+    CK(cudaMallocHost(&h_count, 4 * sizeof(int)));
     CK(cudaMallocHost(&h_state_buf, nprob * sizeof(CgState)));
     // Chebyshev coefficients on D^-1 A over [lo*2, 2] (Gershgorin: the spectrum of
     // D^-1 A of a weakly diagonally dominant symmetric M-matrix lies in [0, 2]).
@@ -820,7 +863,11 @@ int StructBatch::profile_report(int cap, const char **names, long long *counts, 
 
 StructBatch::~StructBatch() {
     for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
-    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    for (auto &kv : graphs) {
+        cudaGraphExecDestroy(kv.second.exec);
+        cudaGraphDestroy(kv.second.graph);
+    }
+    if (cap_stream) cudaStreamDestroy(cap_stream);
     for (void *p : owned) cudaFree(p);
     if (h_count) cudaFreeHost(h_count);
     if (h_state_buf) cudaFreeHost(h_state_buf);
@@ -829,9 +876,20 @@ StructBatch::~StructBatch() {
 static inline unsigned nb_of(const BlockMap &m) { return (unsigned)m.nblocks; }
 
 // ---- assembly and hierarchy
-void StructBatch::assemble(const double *Ks, const double *logK, int kind, const double *shift, bool init_x) {
+template <typename T>
+static Coeffs<T> coeffs_of(StructBatch::Level &L, bool mixed);
+template <>
+Coeffs<double> coeffs_of<double>(StructBatch::Level &L, bool) {
+    return Coeffs<double>{L.c64[0], L.c64[1], L.c64[2], L.c64[3], L.idg64};
+}
+template <>
+Coeffs<float> coeffs_of<float>(StructBatch::Level &L, bool) {
+    return Coeffs<float>{L.c32[0], L.c32[1], L.c32[2], L.c32[3], nullptr};
+}
+
+void StructBatch::assemble(const double *Ks, const double *kc, int kind, const double *shift, bool init_x) {
     Level &L0 = lv[0];
-    FaceK fk{Ks, logK, kind};
+    FaceK fk{Ks, kc, kind};
     if (nb_of(L0.all))
         {
             KTimer _kt(this, kname("k_assemble", 0, false), L0.all_cells);
@@ -864,21 +922,22 @@ void StructBatch::assemble(const double *Ks, const double *logK, int kind, const
         }
         LAUNCH_CHECK();
     }
+    if (!mixed) {
+        for (int l = 0; l < nlev_max; l++) {
+            Level &L = lv[l];
+            if (!nb_of(L.all)) continue;
+            {
+                KTimer _kt(this, kname("k_invdiag", l, false), L.all_cells);
+                k_invdiag<<<nb_of(L.all), kBlock, 0, stream>>>(L.d_desc, L.all.d_map, coeffs_of<double>(L, false),
+                                                               L.idg64);
+            }
+            LAUNCH_CHECK();
+        }
+    }
     have_operator = true;
 }
 
 // ---- V-cycle: z = M r on the fine level (vector precision T)
-template <typename T>
-static Coeffs<T> coeffs_of(StructBatch::Level &L, bool mixed);
-template <>
-Coeffs<double> coeffs_of<double>(StructBatch::Level &L, bool) {
-    return Coeffs<double>{L.c64[0], L.c64[1], L.c64[2], L.c64[3]};
-}
-template <>
-Coeffs<float> coeffs_of<float>(StructBatch::Level &L, bool) {
-    return Coeffs<float>{L.c32[0], L.c32[1], L.c32[2], L.c32[3]};
-}
-
 template <typename T>
 void StructBatch::vcycle(const T *r, T *z) {
     const int deg = opt.cheb_degree;
@@ -999,47 +1058,125 @@ int StructBatch::read_count(int which) {
 }
 
 // ---- preconditioned CG on all active problems: A x = b (vectors of type T)
+// One PCG iteration: q = A p, alpha; x, r update and convergence test; z = M r, beta; p update.
 template <typename T>
-void StructBatch::pcg(const T *b, T *x, double tol2, bool gated) {
+void StructBatch::pcg_iteration(T *x) {
     Level &L0 = lv[0];
     Coeffs<T> C = coeffs_of<T>(L0, mixed);
     T *r = (T *)cgv[0], *z = (T *)cgv[1], *pv = (T *)cgv[2], *q = (T *)cgv[3];
     const unsigned nb = nb_of(L0.all);
-    CK(cudaMemsetAsync(d_count, 0, sizeof(int), stream));
     {
-        KTimer _kt(this, kname("k_cg_start", 0, sizeof(T) == 4), L0.all_cells);
-        k_cg_start<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C, b, x,
-                                                 r, tol2, gated ? 1 : 0);
+        KTimer _kt(this, kname("k_spmv_pq", 0, sizeof(T) == 4), L0.all_cells);
+        k_spmv_pq<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C,
+                                                pv, q);
     }
     LAUNCH_CHECK();
-    if (read_count(0) == 0) return;
+    {
+        KTimer _kt(this, kname("k_update_xr", 0, sizeof(T) == 4), L0.all_cells);
+        k_update_xr<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, x, r,
+                                                  pv, q, opt.maxiter);
+    }
+    LAUNCH_CHECK();
     vcycle<T>(r, z);
     {
         KTimer _kt(this, kname("k_update_p", 0, sizeof(T) == 4), L0.all_cells);
         k_update_p<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z, pv);
     }
     LAUNCH_CHECK();
+}
+
+// Keeps iterating while any problem is active (bounded by maxiter + 2 passes).
+__global__ void k_loop_cond(cudaGraphConditionalHandle h, const int *count, int *iters, int maxiter) {
+    int it = ++(*iters);
+    cudaGraphSetConditional(h, (*count > 0 && it < maxiter + 2) ? 1u : 0u);
+}
+
+// The whole CG loop as one graph: a conditional WHILE node whose body is one PCG
+// iteration followed by k_loop_cond. Built once per (vector type, iterate buffer).
+template <typename T>
+cudaGraphExec_t StructBatch::loop_graph(T *x) {
+    auto key = std::make_pair((int)sizeof(T), (void *)x);
+    auto it = graphs.find(key);
+    if (it != graphs.end()) return it->second.exec;
+    if (!cap_stream) CK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+    cudaGraph_t g;
+    CK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle cond;
+    CK(cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaStream_t saved = stream;
+    long long l0 = launches;
+    stream = cap_stream;
+    cudaError_t ce = cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (ce != cudaSuccess) {
+        stream = saved;
+        cudaGraphDestroy(g);
+        ck(ce, "cudaStreamBeginCaptureToGraph");
+    }
+    try {
+        pcg_iteration<T>(x);
+        k_loop_cond<<<1, 1, 0, stream>>>(cond, d_count, d_count + 2, opt.maxiter);
+        launches++;
+        LAUNCH_CHECK();
+    } catch (...) {
+        cudaGraph_t junk;
+        cudaStreamEndCapture(stream, &junk);
+        stream = saved;
+        cudaGraphDestroy(g);
+        throw;
+    }
+    CK(cudaStreamEndCapture(stream, &body));
+    stream = saved;
+    GraphRec rec;
+    rec.graph = g;
+    rec.body_kernels = launches - l0;
+    launches = l0;
+    CK(cudaGraphInstantiate(&rec.exec, g, 0));
+    graphs[key] = rec;
+    return rec.exec;
+}
+
+// ---- preconditioned CG on all active problems: A x = b (vectors of type T)
+template <typename T>
+void StructBatch::pcg(const T *b, T *x, double tol2, bool gated) {
+    Level &L0 = lv[0];
+    Coeffs<T> C = coeffs_of<T>(L0, mixed);
+    T *r = (T *)cgv[0], *z = (T *)cgv[1], *pv = (T *)cgv[2];
+    const unsigned nb = nb_of(L0.all);
+    CK(cudaMemsetAsync(d_count, 0, sizeof(int), stream));       // active CG problems
+    CK(cudaMemsetAsync(d_count + 2, 0, sizeof(int), stream));   // loop passes ([1] belongs to the refinement)
+    {
+        KTimer _kt(this, kname("k_cg_start", 0, sizeof(T) == 4), L0.all_cells);
+        k_cg_start<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C, b, x,
+                                                 r, tol2, gated ? 1 : 0);
+    }
+    LAUNCH_CHECK();
+    vcycle<T>(r, z);
+    {
+        KTimer _kt(this, kname("k_update_p", 0, sizeof(T) == 4), L0.all_cells);
+        k_update_p<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z, pv);
+    }
+    LAUNCH_CHECK();
+    if (opt.use_graphs && !prof_on) {
+        cudaGraphExec_t ex = loop_graph<T>(x);
+        CK(cudaGraphLaunch(ex, stream));
+        // account the graph's kernel launches: body kernels times passes
+        CK(cudaMemcpyAsync(h_count + 2, d_count + 2, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        launches += graphs[std::make_pair((int)sizeof(T), (void *)x)].body_kernels * (long long)h_count[2];
+        return;
+    }
     const int check = std::max(1, opt.check_every);
-    for (int it = 1; it <= opt.maxiter; it++) {
-        {
-            KTimer _kt(this, kname("k_spmv_pq", 0, sizeof(T) == 4), L0.all_cells);
-            k_spmv_pq<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C,
-                                                    pv, q);
-        }
-        LAUNCH_CHECK();
-        {
-            KTimer _kt(this, kname("k_update_xr", 0, sizeof(T) == 4), L0.all_cells);
-            k_update_xr<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, x,
-                                                      r, pv, q, opt.maxiter);
-        }
-        LAUNCH_CHECK();
-        if (it % check == 0 && read_count(0) == 0) return;
-        vcycle<T>(r, z);
-        {
-            KTimer _kt(this, kname("k_update_p", 0, sizeof(T) == 4), L0.all_cells);
-            k_update_p<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z, pv);
-        }
-        LAUNCH_CHECK();
+    for (int it = 1; it <= opt.maxiter + 1; it++) {
+        pcg_iteration<T>(x);
+        if (it % check == 0 && read_count(0) <= 0) return;
     }
     read_count(0);
 }
@@ -1063,7 +1200,7 @@ void StructBatch::solve(const double *b, double *x, double reltol) {
         h_count[1] = nprob;
         CK(cudaMemcpyAsync(d_count + 1, h_count + 1, sizeof(int), cudaMemcpyHostToDevice, stream));
         int outer = 0;
-        for (;; outer++) {
+        for (; outer <= opt.max_outer + 1; outer++) {
             {
                 KTimer _kt(this, kname("k_ir_residual", 0, false), L0.all_cells);
                 k_ir_residual<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count + 1, rs,
@@ -1071,7 +1208,7 @@ void StructBatch::solve(const double *b, double *x, double reltol) {
                                                          opt.max_outer);
             }
             LAUNCH_CHECK();
-            if (read_count(1) == 0) break;
+            if (read_count(1) <= 0) break;
             {
                 KTimer _kt(this, kname("k_ir_cast", 0, false), L0.all_cells);
                 k_ir_cast<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, r64, r32, e);
@@ -1121,7 +1258,8 @@ void StructBatch::forward(const double *Ks, const double *logK, int kind) {
         if (ndir[p] == 0)
             throw BadInput("problem " + std::to_string(p) +
                            " has no Dirichlet cell: the steady-state operator is singular");
-    assemble(Ks, logK, kind, nullptr, true);
+    if (logK) cell_k(logK, kind, in_kc);
+    assemble(Ks, logK ? in_kc : nullptr, kind, nullptr, true);
     solve(b64, h, opt.reltol);
     fwd_kind = logK ? 1 : 0;
     mean_kind = kind;
@@ -1163,7 +1301,7 @@ void StructBatch::grad_logk(double *g) {
     Level &L0 = lv[0];
     {
         KTimer _kt(this, kname("k_grad_logk", 0, false), L0.all_cells);
-        k_grad_logk<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_prm, in_logK, mean_kind, h, lam,
+        k_grad_logk<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_prm, in_kc, mean_kind, h, lam,
                                                           g);
     }
     LAUNCH_CHECK();
@@ -1171,7 +1309,7 @@ void StructBatch::grad_logk(double *g) {
 
 void StructBatch::grad_dh_q(const double *lv_, double *ddh, double *dQs, bool with_delta, bool accumulate) {
     Level &L0 = lv[0];
-    FaceK fk{fwd_kind ? nullptr : in_Ks, fwd_kind ? in_logK : nullptr, mean_kind};
+    FaceK fk{fwd_kind ? nullptr : in_Ks, fwd_kind ? in_kc : nullptr, mean_kind};
     {
         KTimer _kt(this, kname("k_grad_dh_q", 0, false), L0.all_cells);
         k_grad_dh_q<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_prm, fk, L0.dir,
@@ -1181,20 +1319,31 @@ void StructBatch::grad_dh_q(const double *lv_, double *ddh, double *dQs, bool wi
     LAUNCH_CHECK();
 }
 
-void StructBatch::logk_to_faces(const double *logK, int kind, double *Ks) {
+void StructBatch::cell_k(const double *logK, int kind, double *kc) {
     Level &L0 = lv[0];
     {
+        KTimer _kt(this, kname("k_cell_k", 0, false), L0.all_cells);
+        k_cell_k<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, logK, kind, kc);
+    }
+    LAUNCH_CHECK();
+}
+
+void StructBatch::logk_to_faces(const double *logK, int kind, double *Ks) {
+    Level &L0 = lv[0];
+    cell_k(logK, kind, aux_kc);
+    {
         KTimer _kt(this, kname("k_logk_to_faces", 0, false), L0.all_cells);
-        k_logk_to_faces<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_prm, logK, kind, Ks);
+        k_logk_to_faces<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_prm, aux_kc, kind, Ks);
     }
     LAUNCH_CHECK();
 }
 
 void StructBatch::logk_vjp(const double *logK, int kind, const double *dKs, double *g) {
     Level &L0 = lv[0];
+    cell_k(logK, kind, aux_kc);
     {
         KTimer _kt(this, kname("k_logk_vjp", 0, false), L0.all_cells);
-        k_logk_vjp<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_prm, logK, kind, dKs, g);
+        k_logk_vjp<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_prm, aux_kc, kind, dKs, g);
     }
     LAUNCH_CHECK();
 }
@@ -1233,5 +1382,7 @@ template void StructBatch::vcycle<double>(const double *, double *);
 template void StructBatch::vcycle<float>(const float *, float *);
 template void StructBatch::pcg<double>(const double *, double *, double, bool);
 template void StructBatch::pcg<float>(const float *, float *, double, bool);
+template void StructBatch::pcg_iteration<double>(double *);
+template void StructBatch::pcg_iteration<float>(float *);
 
 }  // namespace dpf

@@ -1,6 +1,7 @@
 // dpf_struct.h -- host-side class of the structured (regular-grid) batch solver.
 #pragma once
 #include <array>
+#include <map>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -63,6 +64,7 @@ public:
         int *d_coarse = nullptr;
         uint8_t *dir = nullptr;        // identity (Dirichlet) rows
         double *c64[4] = {nullptr, nullptr, nullptr, nullptr};  // cx, cy, cz, leak
+        double *idg64 = nullptr;       // inverse diagonal (FP64 solves)
         float *c32[4] = {nullptr, nullptr, nullptr, nullptr};
         void *work[4] = {nullptr, nullptr, nullptr, nullptr};   // xa, xb, b, d (V-cycle precision)
     };
@@ -74,7 +76,8 @@ public:
     StructBatch &operator=(const StructBatch &) = delete;
 
     // operations (device pointers, all ordered on `stream`)
-    void assemble(const double *Ks, const double *logK, int kind, const double *shift, bool init_x);
+    void assemble(const double *Ks, const double *kc, int kind, const double *shift, bool init_x);
+    void cell_k(const double *logK, int kind, double *kc);
     void solve(const double *b, double *x, double reltol);
     void forward(const double *Ks, const double *logK, int kind);
     void adjoint_solve();  // lam = A^-1 delta (Dirichlet rows 0)
@@ -92,6 +95,10 @@ public:
     void vcycle(const T *r, T *z);
     template <typename T>
     void pcg(const T *b, T *x, double tol2, bool gated);
+    template <typename T>
+    void pcg_iteration(T *x);
+    template <typename T>
+    cudaGraphExec_t loop_graph(T *x);
     int read_count(int which);
     void *ir_e();
 
@@ -111,18 +118,25 @@ public:
     // fine-level FP64 vectors
     double *h = nullptr, *b64 = nullptr, *r64 = nullptr, *lam = nullptr, *delta = nullptr, *arhs = nullptr;
     double *in_dh = nullptr, *in_Q = nullptr, *in_logK = nullptr, *in_Ks = nullptr, *shift = nullptr;
+    double *in_kc = nullptr, *aux_kc = nullptr;  // per-cell face-mean values of the forward / standalone calls
     void *cgv[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // r, z, p, q, r32 (CG precision)
     float *ir_e_buf = nullptr;
 
     // device state
     CgState *d_state = nullptr;
-    int *d_count = nullptr;       // [0] active CG problems, [1] problems still refining
+    int *d_count = nullptr;       // [0] active CG problems, [1] problems still refining, [2] loop passes
     int *d_factor_status = nullptr;
     ReduceScratch rs;
     double *d_coarseL = nullptr;
     int *h_count = nullptr;
     void *h_state_buf = nullptr;
-    cudaGraphExec_t graph_exec = nullptr;
+    struct GraphRec {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        long long body_kernels = 0;
+    };
+    std::map<std::pair<int, void *>, GraphRec> graphs;  // CG loop graphs per (vector size, iterate)
+    cudaStream_t cap_stream = nullptr;                  // stream used only to capture graphs
 
     // Chebyshev
     double inv_theta = 1.0;

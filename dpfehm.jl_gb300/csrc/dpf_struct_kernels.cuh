@@ -16,13 +16,16 @@ struct Cell {
     int ix, iy, iz;
 };
 
+__device__ __forceinline__ unsigned fast_div(unsigned n, unsigned m, int l) { return (__umulhi(n, m) + n) >> l; }
+
 __device__ __forceinline__ bool decode_cell(const LevelDesc &L, int lb, Cell &c) {
-    int li = lb * kBlock + (int)threadIdx.x;
+    unsigned li = (unsigned)(lb * kBlock + (int)threadIdx.x);
     if ((long long)li >= L.n) return false;
-    int q = li / L.nz;
-    c.iz = li - q * L.nz;
-    c.iy = q % L.ny;
-    c.ix = q / L.ny;
+    unsigned q = fast_div(li, L.mag_nz, L.sh_nz);
+    c.iz = (int)(li - q * (unsigned)L.nz);
+    unsigned x = fast_div(q, L.mag_ny, L.sh_ny);
+    c.iy = (int)(q - x * (unsigned)L.ny);
+    c.ix = (int)x;
     c.i = L.off + li;
     return true;
 }
@@ -46,33 +49,87 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// Block-wide sum of two values; the result is valid in thread 0. Every thread of
-// the block must call it.
-__device__ __forceinline__ double2 block_sum2(double a, double b) {
-    __shared__ double2 sh[kBlock / 32];
+// Reduction accumulators. FP64 kernels sum in double. FP32 kernels avoid FP64
+// arithmetic per cell (GB300's FP64 rate is a small fraction of its FP32 rate):
+// each product is formed exactly as an unevaluated float pair (fmaf error term)
+// and pairs are added with Knuth's two-sum, giving about 48 significant bits;
+// only the per-block result is converted to double.
+struct DF {
+    float hi, lo;
+};
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    float s = a.hi + b.hi;
+    float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e += a.lo + b.lo;
+    float h = s + e;
+    return DF{h, e - (h - s)};
+}
+__device__ __forceinline__ DF df_shfl(DF a, int o) {
+    return DF{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+}
+
+template <typename T>
+struct Acc;
+template <>
+struct Acc<double> {
+    double v = 0.0;
+    __device__ __forceinline__ static Acc prod(double a, double b) { Acc r; r.v = a * b; return r; }
+    __device__ __forceinline__ Acc operator+(Acc o) const { Acc r; r.v = v + o.v; return r; }
+    __device__ __forceinline__ Acc shfl(int o) const { Acc r; r.v = __shfl_xor_sync(0xffffffffu, v, o); return r; }
+    __device__ __forceinline__ double to_double() const { return v; }
+};
+template <>
+struct Acc<float> {
+    DF v = DF{0.f, 0.f};
+    __device__ __forceinline__ static Acc prod(float a, float b) {
+        Acc r;
+        float p = a * b;
+        r.v = DF{p, fmaf(a, b, -p)};
+        return r;
+    }
+    __device__ __forceinline__ Acc operator+(Acc o) const { Acc r; r.v = df_add(v, o.v); return r; }
+    __device__ __forceinline__ Acc shfl(int o) const { Acc r; r.v = df_shfl(v, o); return r; }
+    __device__ __forceinline__ double to_double() const { return (double)v.hi + (double)v.lo; }
+};
+
+// Block-wide sum of two accumulators, converted to double; valid in thread 0.
+// Every thread of the block must call it.
+template <typename T>
+__device__ __forceinline__ double2 block_sum2(Acc<T> a, Acc<T> b) {
+    __shared__ Acc<T> sh[2][kBlock / 32];
     __syncthreads();
-    a = warp_sum(a);
-    b = warp_sum(b);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) { a = a + a.shfl(o); b = b + b.shfl(o); }
     int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) sh[w] = make_double2(a, b);
+    if (l == 0) { sh[0][w] = a; sh[1][w] = b; }
     __syncthreads();
     double2 r = make_double2(0.0, 0.0);
     if (w == 0) {
-        double2 t = l < (int)(blockDim.x >> 5) ? sh[l] : make_double2(0.0, 0.0);
-        t.x = warp_sum(t.x);
-        t.y = warp_sum(t.y);
-        r = t;
+        Acc<T> x, y;
+        if (l < (int)(blockDim.x >> 5)) { x = sh[0][l]; y = sh[1][l]; }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) { x = x + x.shfl(o); y = y + y.shfl(o); }
+        r = make_double2(x.to_double(), y.to_double());
     }
     return r;
+}
+
+__device__ __forceinline__ double2 block_sum2d(double a, double b) {
+    Acc<double> x, y;
+    x.v = a;
+    y.v = b;
+    return block_sum2<double>(x, y);
 }
 
 // Write this block's partial; return true (in every thread) in the last block of
 // problem p to arrive, with the problem total in `tot`. Deterministic: the total is
 // always summed over the partial slots in the same order.
-__device__ __forceinline__ bool reduce_last(double a, double b, ReduceScratch rs, int2 pinfo, int p, double2 &tot) {
+template <typename T>
+__device__ __forceinline__ bool reduce_last(Acc<T> a, Acc<T> b, ReduceScratch rs, int2 pinfo, int p, double2 &tot) {
     __shared__ int amlast;
     __shared__ double2 total;
-    double2 s = block_sum2(a, b);
+    double2 s = block_sum2<T>(a, b);
     if (threadIdx.x == 0) {
         rs.partials[blockIdx.x] = s;
         __threadfence();
@@ -88,7 +145,7 @@ __device__ __forceinline__ bool reduce_last(double a, double b, ReduceScratch rs
         ax += q.x;
         ay += q.y;
     }
-    double2 r = block_sum2(ax, ay);
+    double2 r = block_sum2d(ax, ay);
     if (threadIdx.x == 0) {
         total = r;
         rs.tickets[p] = 0u;
@@ -117,6 +174,18 @@ __device__ __forceinline__ void apply7(const LevelDesc &L, const Cell &c, const 
     diag = d;
 }
 
+// v / diag for the smoothers: FP64 levels multiply by the stored inverse diagonal
+// (a DP division per cell per sweep is expensive on GB300), FP32 levels use the fast
+// approximate division (about 2 ulp, ample for a smoother).
+template <typename T>
+__device__ __forceinline__ T dinv_times(const Coeffs<T> &C, long long i, T v, T dg) {
+    if constexpr (sizeof(T) == 8) {
+        return v * C.idg[i];
+    } else {
+        return __fdividef(v, dg);
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ T diag7(const LevelDesc &L, const Cell &c, const Coeffs<T> &C) {
     const long long i = c.i;
@@ -132,16 +201,25 @@ __device__ __forceinline__ T diag7(const LevelDesc &L, const Cell &c, const Coef
 }
 
 // -------------------------------------------------------------- assembly
-__device__ __forceinline__ double face_mean(double la, double lb, int kind) {
-    if (kind == DPF_MEAN_GEOMETRIC) return exp(0.5 * (la + lb));
-    return 2.0 / (exp(-la) + exp(-lb));
+// Face conductances from cell values kc, computed once per cell by k_cell_k
+// (GB300 has little FP64 throughput, so exp runs once per cell, not once per face):
+//   geometric  kc = exp(logK / 2):  K_f = exp((logK_a + logK_b)/2) = kc_a kc_b
+//   harmonic   kc = exp(logK):      K_f = 2 / (1/K_a + 1/K_b) = 2 kc_a kc_b / (kc_a + kc_b)
+__device__ __forceinline__ double face_mean_k(double ka, double kb, int kind) {
+    if (kind == DPF_MEAN_GEOMETRIC) return ka * kb;
+    return 2.0 * ka * kb / (ka + kb);
+}
+// dK_f / dlogK_a:  geometric K_f / 2;  harmonic K_f^2 / (2 K_a)
+__device__ __forceinline__ double face_mean_dlogk(double Kf, double ka, int kind) {
+    if (kind == DPF_MEAN_GEOMETRIC) return 0.5 * Kf;
+    return 0.5 * Kf * Kf / ka;
 }
 
-// Conductance of the face between cell c and its neighbour in direction d (0..2)
+// Conductance of the face between cell c and its neighbour j in direction d (0..2)
 // and side s (+1: neighbour at +, -1: neighbour at -).
 struct FaceK {
     const double *Ks;       // face list (reference order), or null
-    const double *logK;     // cell log-conductivities, or null
+    const double *kc;       // per-cell values of k_cell_k, or null
     int kind;
     __device__ __forceinline__ double operator()(const LevelDesc &L, const ProbParam &P, const Cell &c, int d, int s,
                                                 long long j) const {
@@ -150,12 +228,12 @@ struct FaceK {
             if (s < 0) { if (d == 0) ax--; else if (d == 1) ay--; else az--; }
             return Ks[P.face_off + regular_face_index(L.nx, L.ny, L.nz, ax, ay, az, d)];
         }
-        return face_mean(logK[c.i], logK[j], kind);
+        return face_mean_k(kc[c.i], kc[j], kind);
     }
 };
 
 // Fine-level operator, right-hand side and initial guess (src/groundwater.jl:4-20 with
-// S = V = 1; storage shift for transient). Writes FP64 coefficients and, when f32 != null,
+// S = V = 1; storage shift for transient). Writes FP64 coefficients and, when fx != null,
 // FP32 copies.
 __global__ void k_assemble(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
                            const ProbParam *__restrict__ prm, FaceK fk, const double *__restrict__ dh,
