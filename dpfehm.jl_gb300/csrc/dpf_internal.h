@@ -52,11 +52,11 @@ struct BlockMap {                  // launch map: block -> (problem, block withi
 struct CgState {
     double rz, rz_old, pq, rr, bb, tol2;
     double alpha, beta;
-    double scale;                  // mixed precision: norm used to normalise the inner rhs
-    double ee, hh;                 // mixed precision: correction / solution norms of the last step
-    double orr, obb;               // mixed precision: outer (FP64) residual and rhs norms squared
-    int iters, active, status, outer;
-    int outer_active, total_iters, pad1, pad2;
+    double scale;                  // mixed precision: normalisation of the FP32 residual
+    double ratio;                  // mixed precision: old scale / new scale at the last update
+    double orr, obb;               // mixed precision: true (FP64) residual and rhs norms squared
+    int iters, active, status, outer;  // outer: reliable updates so far
+    int ru_flag, total_iters, pad1, pad2;
 };
 
 // Reduction scratch: one double2 partial per block of the widest launch, one

@@ -191,11 +191,9 @@ __global__ void k_coarse_solve(const LevelDesc *__restrict__ desc, const int *__
 template <typename T>
 __global__ void k_cg_start(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
                            int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, Coeffs<T> C,
-                           const T *__restrict__ b, const T *__restrict__ x, T *__restrict__ r, double tol2,
-                           int gated) {
+                           const T *__restrict__ b, const T *__restrict__ x, T *__restrict__ r, double tol2) {
     int2 bm = bmap[blockIdx.x];
     const int p = bm.x;
-    if (gated && !st[p].outer_active) return;
     const LevelDesc L = desc[p];
     Cell c;
     Acc<T> rr, bb;
@@ -250,11 +248,14 @@ __global__ void k_spmv_pq(const LevelDesc *__restrict__ desc, const int2 *__rest
     }
 }
 
-// x += alpha p; r -= alpha q; convergence test on r . r.
-template <typename T>
+// x += alpha p; r -= alpha q; convergence test on r . r. With RU (mixed precision) the
+// residual is normalised: the problem is flagged for a reliable update instead of
+// being declared converged, which only the true FP64 residual can decide.
+template <typename T, bool RU>
 __global__ void k_update_xr(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
                             int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, T *__restrict__ x,
-                            T *__restrict__ r, const T *__restrict__ pv, const T *__restrict__ q, int maxiter) {
+                            T *__restrict__ r, const T *__restrict__ pv, const T *__restrict__ q, int maxiter,
+                            int *upd_count, double delta2) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     const double alpha = st[p].alpha;
     Cell c;
@@ -273,7 +274,12 @@ __global__ void k_update_xr(const LevelDesc *__restrict__ desc, const int2 *__re
         s.iters++;
         s.total_iters++;
         if (!isfinite(s.rr)) { s.status = DPF_NAN; deactivate(s, active_count); }
-        else if (s.rr <= s.tol2 * s.bb) deactivate(s, active_count);
+        else if (RU) {
+            if (s.rr <= delta2 || s.rr * s.scale * s.scale <= s.tol2 * s.obb || s.iters >= maxiter) {
+                s.ru_flag = 1;
+                atomicAdd(upd_count, 1);
+            }
+        } else if (s.rr <= s.tol2 * s.bb) deactivate(s, active_count);
         else if (s.iters >= maxiter) { s.status = DPF_NOT_CONVERGED; deactivate(s, active_count); }
     }
 }
@@ -289,93 +295,126 @@ __global__ void k_update_p(const LevelDesc *__restrict__ desc, const int2 *__res
     pv[c.i] = beta == (T)0 ? z[c.i] : z[c.i] + beta * pv[c.i];
 }
 
-// ------------------------------------------------ iterative refinement (FP64)
-// r64 = b - A h (FP64 flux form); decide whether another refinement step is needed.
-__global__ void k_ir_residual(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
-                              int *outer_count, ReduceScratch rs, const int2 *__restrict__ pinfo, Coeffs<double> C,
-                              const double *__restrict__ b, const double *__restrict__ h, double *__restrict__ r,
-                              double tol2, int max_outer) {
+// ------------------------------------- mixed precision: reliable-update CG
+// The CG recurrence runs in FP32 on a residual normalised by `scale`; the solution
+// is accumulated in FP64. When the recursive residual has dropped by a factor delta
+// (or looks converged, or the iteration cap is hit) the problem is flagged, and the
+// flagged problems replace their FP32 residual by the true FP64 residual b - A x
+// without restarting the Krylov recurrence (the search direction is rescaled to the
+// new normalisation). Convergence is decided on the true FP64 residual only.
+
+// x64 += scale * xs; xs = 0   (flagged problems)
+__global__ void k_ru_accum(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, const CgState *st,
+                           double *__restrict__ x64, float *__restrict__ xs) {
     int2 bm = bmap[blockIdx.x];
     const int p = bm.x;
-    if (!st[p].outer_active) return;
+    if (!st[p].ru_flag) return;
+    const LevelDesc L = desc[p];
+    const double sc = st[p].scale;
+    Cell c;
+    if (!decode_cell(L, bm.y, c)) return;
+    x64[c.i] += sc * (double)xs[c.i];
+    xs[c.i] = 0.0f;
+}
+
+// r64 = b - A x64 in FP64 flux form. START: every problem, sets up the state.
+// Otherwise flagged problems only: converged -> inactive, else new normalisation.
+template <bool START>
+__global__ void k_ru_residual(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+                              int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo,
+                              Coeffs<double> C, const double *__restrict__ b, const double *__restrict__ x,
+                              double *__restrict__ r, double tol2, int maxiter, int max_updates) {
+    int2 bm = bmap[blockIdx.x];
+    const int p = bm.x;
+    if (!START && !st[p].ru_flag) return;
     const LevelDesc L = desc[p];
     Cell c;
     Acc<double> rr, bb;
     if (decode_cell(L, bm.y, c)) {
-        double xi = h[c.i], Ax, dg;
-        apply7(L, c, C, xi, [&](long long j, int, int, int) { return h[j]; }, Ax, dg);
+        double xi = x[c.i], Ax, dg;
+        apply7(L, c, C, xi, [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
         double bi = b[c.i];
         double ri = bi - Ax;
         r[c.i] = ri;
         rr.v = ri * ri;
-        bb.v = bi * bi;
+        if (START) bb.v = bi * bi;
     }
     double2 tot;
     if (reduce_last<double>(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
         CgState &s = st[p];
         s.orr = tot.x;
-        if (s.outer == 0) s.obb = tot.y;
-        bool stop = false;
-        if (!isfinite(s.orr)) { s.status = DPF_NAN; stop = true; }
-        else if (s.obb == 0.0 || s.orr <= tol2 * s.obb) stop = true;
-        else if (s.outer > 0 && s.ee <= 1e-26 * s.hh) stop = true;       // correction below FP64 resolution
-        else if (s.outer >= max_outer) { s.status = DPF_NOT_CONVERGED; stop = true; }
-        if (stop) {
-            s.outer_active = 0;
-            atomicSub(outer_count, 1);
+        if (START) {
+            s.obb = tot.y;
+            s.tol2 = tol2;
+            s.status = DPF_OK;
+            s.iters = 0;
+            s.total_iters = 0;
+            s.outer = 0;
+            s.rz = 0.0;
+            s.rz_old = 0.0;
+            s.beta = 0.0;
+            s.ratio = 1.0;
+            bool act = s.obb > 0.0 && s.orr > tol2 * s.obb;
+            if (!isfinite(s.orr)) { s.status = DPF_NAN; act = false; }
+            s.active = act ? 1 : 0;
+            s.ru_flag = act ? 1 : 0;
+            if (act) {
+                s.scale = sqrt(s.orr);
+                atomicAdd(active_count, 1);
+            }
         } else {
-            s.scale = sqrt(s.orr);
             s.outer++;
+            if (!isfinite(s.orr)) { s.status = DPF_NAN; s.ru_flag = 0; deactivate(s, active_count); }
+            else if (s.orr <= tol2 * s.obb) { s.ru_flag = 0; deactivate(s, active_count); }
+            else if (s.iters >= maxiter || s.outer >= max_updates) {
+                s.status = DPF_NOT_CONVERGED;
+                s.ru_flag = 0;
+                deactivate(s, active_count);
+            } else {
+                double sn = sqrt(s.orr);
+                s.ratio = s.scale / sn;
+                s.scale = sn;
+                s.rz *= s.ratio * s.ratio;  // (r, z) of the next beta in the new normalisation
+            }
         }
     }
 }
 
-// r32 = r64 / scale; e = 0
-__global__ void k_ir_cast(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
-                          const double *__restrict__ r64, float *__restrict__ r32, float *__restrict__ e) {
+// r32 = r64 / scale; START: xs = 0; otherwise p *= ratio   (flagged problems)
+__global__ void k_ru_cast(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, const CgState *st,
+                          const double *__restrict__ r64, float *__restrict__ r32, float *__restrict__ pv,
+                          float *__restrict__ xs, int start) {
     int2 bm = bmap[blockIdx.x];
     const int p = bm.x;
-    if (!st[p].outer_active) return;
+    if (!st[p].ru_flag) return;
     const LevelDesc L = desc[p];
     const double inv = 1.0 / st[p].scale;
+    const float ratio = (float)st[p].ratio;
     Cell c;
     if (!decode_cell(L, bm.y, c)) return;
     r32[c.i] = (float)(r64[c.i] * inv);
-    e[c.i] = 0.0f;
+    if (start) xs[c.i] = 0.0f;
+    else pv[c.i] *= ratio;
 }
 
-// h += scale * e; reduce (|scale e|^2, |h|^2)
-__global__ void k_ir_update(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
-                            ReduceScratch rs, const int2 *__restrict__ pinfo, double *__restrict__ h,
-                            const float *__restrict__ e) {
-    int2 bm = bmap[blockIdx.x];
-    const int p = bm.x;
-    if (!st[p].outer_active) return;
-    const LevelDesc L = desc[p];
-    const double sc = st[p].scale;
-    Cell c;
-    Acc<double> ee, hh;
-    if (decode_cell(L, bm.y, c)) {
-        double de = sc * (double)e[c.i];
-        double hn = h[c.i] + de;
-        h[c.i] = hn;
-        ee.v = de * de;
-        hh.v = hn * hn;
-    }
-    double2 tot;
-    if (reduce_last<double>(ee, hh, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
-        st[p].ee = tot.x;
-        st[p].hh = tot.y;
-    }
+__global__ void k_ru_clear(CgState *st, int nprob, int *upd_count) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < nprob) st[p].ru_flag = 0;
+    if (p == 0) *upd_count = 0;
+}
+
+__global__ void k_if_cond(cudaGraphConditionalHandle h, const int *upd_count, int *taken) {
+    bool go = *upd_count > 0;
+    if (go) (*taken)++;
+    cudaGraphSetConditional(h, go ? 1u : 0u);
 }
 
 // ------------------------------------------------------------ misc vector kernels
-__global__ void k_state_init(CgState *st, int nprob, int outer_active) {
+__global__ void k_state_init(CgState *st, int nprob) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nprob) return;
     CgState s;
     memset(&s, 0, sizeof(s));
-    s.outer_active = outer_active;
     st[p] = s;
 }
 
@@ -868,6 +907,7 @@ StructBatch::~StructBatch() {
         cudaGraphDestroy(kv.second.graph);
     }
     if (cap_stream) cudaStreamDestroy(cap_stream);
+    if (cap_stream2) cudaStreamDestroy(cap_stream2);
     for (void *p : owned) cudaFree(p);
     if (h_count) cudaFreeHost(h_count);
     if (h_state_buf) cudaFreeHost(h_state_buf);
@@ -1058,13 +1098,17 @@ int StructBatch::read_count(int which) {
 }
 
 // ---- preconditioned CG on all active problems: A x = b (vectors of type T)
-// One PCG iteration: q = A p, alpha; x, r update and convergence test; z = M r, beta; p update.
+// One PCG iteration: q = A p, alpha; x, r update and convergence test; z = M r, beta; p
+// update. Mixed precision (ru): x is the FP32 partial solution and flagged problems get
+// a reliable update (FP64 true residual) between the x/r update and the V-cycle; inside
+// a graph that update sits in a conditional IF node taken only when a problem is flagged.
 template <typename T>
-void StructBatch::pcg_iteration(T *x) {
+void StructBatch::pcg_iteration(T *x, const double *b64, double *x64, bool capturing) {
     Level &L0 = lv[0];
     Coeffs<T> C = coeffs_of<T>(L0, mixed);
     T *r = (T *)cgv[0], *z = (T *)cgv[1], *pv = (T *)cgv[2], *q = (T *)cgv[3];
     const unsigned nb = nb_of(L0.all);
+    const bool ru = b64 != nullptr;
     {
         KTimer _kt(this, kname("k_spmv_pq", 0, sizeof(T) == 4), L0.all_cells);
         k_spmv_pq<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C,
@@ -1073,14 +1117,92 @@ void StructBatch::pcg_iteration(T *x) {
     LAUNCH_CHECK();
     {
         KTimer _kt(this, kname("k_update_xr", 0, sizeof(T) == 4), L0.all_cells);
-        k_update_xr<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, x, r,
-                                                  pv, q, opt.maxiter);
+        if (ru)
+            k_update_xr<T, true><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs,
+                                                            L0.all.d_pinfo, x, r, pv, q, opt.maxiter, d_count + 3,
+                                                            opt.inner_tol * opt.inner_tol);
+        else
+            k_update_xr<T, false><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs,
+                                                             L0.all.d_pinfo, x, r, pv, q, opt.maxiter, nullptr, 0.0);
     }
     LAUNCH_CHECK();
+    if (ru) {
+        if (!capturing) {
+            ru_update(b64, x64, false);
+        } else {
+            // conditional IF node: reliable update only when some problem is flagged
+            {
+                KTimer _kt(this, kname("k_if_cond", 0, false), 0);
+                k_if_cond<<<1, 1, 0, stream>>>(if_handle, d_count + 3, d_count + 1);
+            }
+            LAUNCH_CHECK();
+            cudaStreamCaptureStatus cs;
+            cudaGraph_t capg;
+            const cudaGraphNode_t *deps;
+            const cudaGraphEdgeData *edata;
+            size_t ndeps;
+            CK(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &capg, &deps, &edata, &ndeps));
+            cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+            cp.conditional.handle = if_handle;
+            cp.conditional.type = cudaGraphCondTypeIf;
+            cp.conditional.size = 1;
+            cudaGraphNode_t ifnode;
+            CK(cudaGraphAddNode(&ifnode, capg, deps, edata, ndeps, &cp));
+            CK(cudaStreamUpdateCaptureDependencies(stream, &ifnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+            cudaGraph_t ifbody = cp.conditional.phGraph_out[0];
+            if (!cap_stream2) CK(cudaStreamCreateWithFlags(&cap_stream2, cudaStreamNonBlocking));
+            cudaStream_t saved = stream;
+            stream = cap_stream2;
+            CK(cudaStreamBeginCaptureToGraph(stream, ifbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+            long long l0 = launches;
+            ru_update(b64, x64, false);
+            if_body_kernels = launches - l0;
+            launches = l0;
+            CK(cudaStreamEndCapture(stream, &ifbody));
+            stream = saved;
+        }
+    }
     vcycle<T>(r, z);
     {
         KTimer _kt(this, kname("k_update_p", 0, sizeof(T) == 4), L0.all_cells);
         k_update_p<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z, pv);
+    }
+    LAUNCH_CHECK();
+}
+
+// reliable update of the flagged problems (or, with start, the initial residual of all)
+void StructBatch::ru_update(const double *b64, double *x64, bool start) {
+    Level &L0 = lv[0];
+    const unsigned nb = nb_of(L0.all);
+    float *xs = (float *)ir_e(), *r32 = (float *)cgv[0], *pv = (float *)cgv[2];
+    const double tol2 = ru_tol2;
+    if (!start) {
+        {
+            KTimer _kt(this, kname("k_ru_accum", 0, false), L0.all_cells);
+            k_ru_accum<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, x64, xs);
+        }
+        LAUNCH_CHECK();
+        {
+            KTimer _kt(this, kname("k_ru_residual", 0, false), L0.all_cells);
+            k_ru_residual<false><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs,
+                                                            L0.all.d_pinfo, coeffs_of<double>(L0, true), b64, x64,
+                                                            r64, tol2, opt.maxiter, opt.max_outer);
+        }
+    } else {
+        KTimer _kt(this, kname("k_ru_residual", 0, false), L0.all_cells);
+        k_ru_residual<true><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs,
+                                                       L0.all.d_pinfo, coeffs_of<double>(L0, true), b64, x64, r64,
+                                                       tol2, opt.maxiter, opt.max_outer);
+    }
+    LAUNCH_CHECK();
+    {
+        KTimer _kt(this, kname("k_ru_cast", 0, false), L0.all_cells);
+        k_ru_cast<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, r64, r32, pv, xs, start ? 1 : 0);
+    }
+    LAUNCH_CHECK();
+    {
+        KTimer _kt(this, kname("k_ru_clear", 0, false), 0);
+        k_ru_clear<<<(nprob + 127) / 128, 128, 0, stream>>>(d_state, nprob, d_count + 3);
     }
     LAUNCH_CHECK();
 }
@@ -1092,10 +1214,10 @@ __global__ void k_loop_cond(cudaGraphConditionalHandle h, const int *count, int 
 }
 
 // The whole CG loop as one graph: a conditional WHILE node whose body is one PCG
-// iteration followed by k_loop_cond. Built once per (vector type, iterate buffer).
+// iteration followed by k_loop_cond. Built once per (vector type, buffers).
 template <typename T>
-cudaGraphExec_t StructBatch::loop_graph(T *x) {
-    auto key = std::make_pair((int)sizeof(T), (void *)x);
+cudaGraphExec_t StructBatch::loop_graph(T *x, const double *b64, double *x64) {
+    GraphKey key{(int)sizeof(T), (const void *)x, (const void *)b64, (const void *)x64};
     auto it = graphs.find(key);
     if (it != graphs.end()) return it->second.exec;
     if (!cap_stream) CK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
@@ -1104,15 +1226,16 @@ cudaGraphExec_t StructBatch::loop_graph(T *x) {
     cudaGraphConditionalHandle cond;
     CK(cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault));
     cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
-    cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = cond;
     cp.conditional.type = cudaGraphCondTypeWhile;
     cp.conditional.size = 1;
     cudaGraphNode_t node;
     CK(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if (b64) CK(cudaGraphConditionalHandleCreate(&if_handle, body, 0, 0));
     cudaStream_t saved = stream;
     long long l0 = launches;
+    if_body_kernels = 0;
     stream = cap_stream;
     cudaError_t ce = cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (ce != cudaSuccess) {
@@ -1121,13 +1244,13 @@ cudaGraphExec_t StructBatch::loop_graph(T *x) {
         ck(ce, "cudaStreamBeginCaptureToGraph");
     }
     try {
-        pcg_iteration<T>(x);
+        pcg_iteration<T>(x, b64, x64, true);
         k_loop_cond<<<1, 1, 0, stream>>>(cond, d_count, d_count + 2, opt.maxiter);
         launches++;
         LAUNCH_CHECK();
     } catch (...) {
         cudaGraph_t junk;
-        cudaStreamEndCapture(stream, &junk);
+        cudaStreamEndCapture(cap_stream, &junk);
         stream = saved;
         cudaGraphDestroy(g);
         throw;
@@ -1137,25 +1260,46 @@ cudaGraphExec_t StructBatch::loop_graph(T *x) {
     GraphRec rec;
     rec.graph = g;
     rec.body_kernels = launches - l0;
+    rec.if_kernels = if_body_kernels;
     launches = l0;
     CK(cudaGraphInstantiate(&rec.exec, g, 0));
     graphs[key] = rec;
     return rec.exec;
 }
 
-// ---- preconditioned CG on all active problems: A x = b (vectors of type T)
 template <typename T>
-void StructBatch::pcg(const T *b, T *x, double tol2, bool gated) {
+void StructBatch::run_loop(T *x, const double *b64, double *x64) {
+    if (opt.use_graphs && !prof_on) {
+        cudaGraphExec_t ex = loop_graph<T>(x, b64, x64);
+        CK(cudaGraphLaunch(ex, stream));
+        // account the graph's kernel launches: body kernels times passes, plus the
+        // reliable-update kernels each time the IF node was taken
+        CK(cudaMemcpyAsync(h_count, d_count, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        GraphKey key{(int)sizeof(T), (const void *)x, (const void *)b64, (const void *)x64};
+        launches += graphs[key].body_kernels * (long long)h_count[2] + graphs[key].if_kernels * (long long)h_count[1];
+        return;
+    }
+    const int check = std::max(1, opt.check_every);
+    for (int it = 1; it <= opt.maxiter + 1; it++) {
+        pcg_iteration<T>(x, b64, x64, false);
+        if (it % check == 0 && read_count(0) <= 0) return;
+    }
+    read_count(0);
+}
+
+// ---- preconditioned CG on all problems: A x = b (vectors of type T)
+template <typename T>
+void StructBatch::pcg(const T *b, T *x, double tol2) {
     Level &L0 = lv[0];
     Coeffs<T> C = coeffs_of<T>(L0, mixed);
     T *r = (T *)cgv[0], *z = (T *)cgv[1], *pv = (T *)cgv[2];
     const unsigned nb = nb_of(L0.all);
-    CK(cudaMemsetAsync(d_count, 0, sizeof(int), stream));       // active CG problems
-    CK(cudaMemsetAsync(d_count + 2, 0, sizeof(int), stream));   // loop passes ([1] belongs to the refinement)
+    CK(cudaMemsetAsync(d_count, 0, 4 * sizeof(int), stream));  // active problems, IF taken, loop passes, flagged
     {
         KTimer _kt(this, kname("k_cg_start", 0, sizeof(T) == 4), L0.all_cells);
         k_cg_start<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C, b, x,
-                                                 r, tol2, gated ? 1 : 0);
+                                                 r, tol2);
     }
     LAUNCH_CHECK();
     vcycle<T>(r, z);
@@ -1164,64 +1308,39 @@ void StructBatch::pcg(const T *b, T *x, double tol2, bool gated) {
         k_update_p<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z, pv);
     }
     LAUNCH_CHECK();
-    if (opt.use_graphs && !prof_on) {
-        cudaGraphExec_t ex = loop_graph<T>(x);
-        CK(cudaGraphLaunch(ex, stream));
-        // account the graph's kernel launches: body kernels times passes
-        CK(cudaMemcpyAsync(h_count + 2, d_count + 2, sizeof(int), cudaMemcpyDeviceToHost, stream));
-        CK(cudaStreamSynchronize(stream));
-        launches += graphs[std::make_pair((int)sizeof(T), (void *)x)].body_kernels * (long long)h_count[2];
-        return;
+    run_loop<T>(x, nullptr, nullptr);
+}
+
+// ---- mixed precision: reliable-update CG with FP32 vectors/V-cycle, FP64 solution x64
+void StructBatch::ru_pcg(const double *b64, double *x64, double tol2) {
+    Level &L0 = lv[0];
+    const unsigned nb = nb_of(L0.all);
+    float *xs = (float *)ir_e(), *r32 = (float *)cgv[0], *z = (float *)cgv[1], *pv = (float *)cgv[2];
+    ru_tol2 = tol2;
+    CK(cudaMemsetAsync(d_count, 0, 4 * sizeof(int), stream));
+    ru_update(b64, x64, true);
+    vcycle<float>(r32, z);
+    {
+        KTimer _kt(this, kname("k_update_p", 0, true), L0.all_cells);
+        k_update_p<float><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z, pv);
     }
-    const int check = std::max(1, opt.check_every);
-    for (int it = 1; it <= opt.maxiter + 1; it++) {
-        pcg_iteration<T>(x);
-        if (it % check == 0 && read_count(0) <= 0) return;
-    }
-    read_count(0);
+    LAUNCH_CHECK();
+    run_loop<float>(xs, b64, x64);
 }
 
 // ---- full solve of A x = b for every problem (x holds the initial guess)
 void StructBatch::solve(const double *b, double *x, double reltol) {
     const double tol2 = reltol * reltol;
-    Level &L0 = lv[0];
-    const unsigned nb = nb_of(L0.all);
     {
         KTimer _kt(this, kname("k_state_init", 0, false), 0);
-        k_state_init<<<(nprob + 127) / 128, 128, 0, stream>>>(d_state, nprob, 1);
+        k_state_init<<<(nprob + 127) / 128, 128, 0, stream>>>(d_state, nprob);
     }
     LAUNCH_CHECK();
     if (!mixed) {
-        pcg<double>(b, x, tol2, false);
+        pcg<double>(b, x, tol2);
         stats_outer = 0;
     } else {
-        float *r32 = (float *)cgv[4];
-        float *e = (float *)ir_e();
-        h_count[1] = nprob;
-        CK(cudaMemcpyAsync(d_count + 1, h_count + 1, sizeof(int), cudaMemcpyHostToDevice, stream));
-        int outer = 0;
-        for (; outer <= opt.max_outer + 1; outer++) {
-            {
-                KTimer _kt(this, kname("k_ir_residual", 0, false), L0.all_cells);
-                k_ir_residual<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count + 1, rs,
-                                                         L0.all.d_pinfo, coeffs_of<double>(L0, true), b, x, r64, tol2,
-                                                         opt.max_outer);
-            }
-            LAUNCH_CHECK();
-            if (read_count(1) <= 0) break;
-            {
-                KTimer _kt(this, kname("k_ir_cast", 0, false), L0.all_cells);
-                k_ir_cast<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, r64, r32, e);
-            }
-            LAUNCH_CHECK();
-            pcg<float>(r32, e, opt.inner_tol * opt.inner_tol, true);
-            {
-                KTimer _kt(this, kname("k_ir_update", 0, false), L0.all_cells);
-                k_ir_update<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, rs, L0.all.d_pinfo, x, e);
-            }
-            LAUNCH_CHECK();
-        }
-        stats_outer = outer;
+        ru_pcg(b, x, tol2);
     }
     // statistics
     CK(cudaMemcpyAsync(h_state_buf, d_state, nprob * sizeof(CgState), cudaMemcpyDeviceToHost, stream));
@@ -1230,7 +1349,9 @@ void StructBatch::solve(const double *b, double *x, double reltol) {
     last_status = DPF_OK;
     stats_iters = 0;
     stats_relres = 0.0;
+    if (mixed) stats_outer = 0;
     for (int p = 0; p < nprob; p++) {
+        if (mixed) stats_outer = std::max(stats_outer, hs[p].outer);
         stats_iters = std::max(stats_iters, mixed ? hs[p].total_iters : hs[p].iters);
         double rel = mixed ? (hs[p].obb > 0 ? std::sqrt(hs[p].orr / hs[p].obb) : 0.0)
                            : (hs[p].bb > 0 ? std::sqrt(hs[p].rr / hs[p].bb) : 0.0);
@@ -1380,9 +1501,7 @@ void StructBatch::transient_step(const double *b0, const double *hprev) {
 
 template void StructBatch::vcycle<double>(const double *, double *);
 template void StructBatch::vcycle<float>(const float *, float *);
-template void StructBatch::pcg<double>(const double *, double *, double, bool);
-template void StructBatch::pcg<float>(const float *, float *, double, bool);
-template void StructBatch::pcg_iteration<double>(double *);
-template void StructBatch::pcg_iteration<float>(float *);
+template void StructBatch::pcg<double>(const double *, double *, double);
+template void StructBatch::pcg<float>(const float *, float *, double);
 
 }  // namespace dpf

@@ -94,11 +94,15 @@ public:
     template <typename T>
     void vcycle(const T *r, T *z);
     template <typename T>
-    void pcg(const T *b, T *x, double tol2, bool gated);
+    void pcg(const T *b, T *x, double tol2);
+    void ru_pcg(const double *b64, double *x64, double tol2);
+    void ru_update(const double *b64, double *x64, bool start);
     template <typename T>
-    void pcg_iteration(T *x);
+    void pcg_iteration(T *x, const double *b64, double *x64, bool capturing);
     template <typename T>
-    cudaGraphExec_t loop_graph(T *x);
+    cudaGraphExec_t loop_graph(T *x, const double *b64, double *x64);
+    template <typename T>
+    void run_loop(T *x, const double *b64, double *x64);
     int read_count(int which);
     void *ir_e();
 
@@ -124,7 +128,7 @@ public:
 
     // device state
     CgState *d_state = nullptr;
-    int *d_count = nullptr;       // [0] active CG problems, [1] problems still refining, [2] loop passes
+    int *d_count = nullptr;       // [0] active CG problems, [1] reliable-update passes, [2] loop passes, [3] flagged
     int *d_factor_status = nullptr;
     ReduceScratch rs;
     double *d_coarseL = nullptr;
@@ -134,9 +138,24 @@ public:
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         long long body_kernels = 0;
+        long long if_kernels = 0;
     };
-    std::map<std::pair<int, void *>, GraphRec> graphs;  // CG loop graphs per (vector size, iterate)
-    cudaStream_t cap_stream = nullptr;                  // stream used only to capture graphs
+    struct GraphKey {
+        int vsize;
+        const void *x, *b64, *x64;
+        bool operator<(const GraphKey &o) const {
+            if (vsize != o.vsize) return vsize < o.vsize;
+            if (x != o.x) return x < o.x;
+            if (b64 != o.b64) return b64 < o.b64;
+            return x64 < o.x64;
+        }
+    };
+    std::map<GraphKey, GraphRec> graphs;  // CG loop graphs per (vector size, buffers)
+    cudaStream_t cap_stream = nullptr;    // streams used only to capture graphs
+    cudaStream_t cap_stream2 = nullptr;
+    cudaGraphConditionalHandle if_handle = 0;
+    long long if_body_kernels = 0;
+    double ru_tol2 = 0.0;
 
     // Chebyshev
     double inv_theta = 1.0;

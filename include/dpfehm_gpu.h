@@ -60,7 +60,8 @@ typedef enum { DPF_MEAN_GEOMETRIC = 0, DPF_MEAN_HARMONIC = 1 } dpf_mean_kind;
 
 typedef enum {
     DPF_PREC_FP64 = 0,  /* FP64 CG with an FP64 V-cycle */
-    DPF_PREC_MIXED = 1  /* FP64 outer residual / iterative refinement around an FP32 CG with an FP32 V-cycle */
+    DPF_PREC_MIXED = 1  /* FP32 CG recurrence and V-cycle; FP64 solution, FP64 true residual replaced into the
+                           recurrence every inner_tol of reduction (reliable updates); FP64 CG scalars */
 } dpf_precision;
 
 typedef struct dpf_options {
@@ -71,8 +72,8 @@ typedef struct dpf_options {
     double cheb_lo;      /* lower end of the Chebyshev interval / upper end   (default 0.2)   */
     double coarse_scale; /* scaling of the coarse-grid correction              (default 2.0)   */
     int max_coarse;      /* coarsen until a level has at most this many cells (default 64, <= 64) */
-    double inner_tol;    /* MIXED: relative tolerance of each inner FP32 solve (default 1e-4)  */
-    int max_outer;       /* MIXED: cap on refinement steps                    (default 12)    */
+    double inner_tol;    /* MIXED: residual reduction between FP64 residual replacements (default 1e-2) */
+    int max_outer;       /* MIXED: cap on FP64 residual replacements per solve (default 60)   */
     int use_graphs;      /* capture each solve's iteration in a CUDA graph    (default 1)     */
     int check_every;     /* convergence is read back every this many iterations (default 1)   */
 } dpf_options;

@@ -1,0 +1,93 @@
+"""Batched solves (uneven grids, one set of launches) against the oracle, and the
+CUDA-graph and host-driven CG loops against each other."""
+import numpy as np
+import pytest
+
+from helpers import rel
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(pkg, ns, seed):
+    mins = (0.0, 0.0, 0.0)
+    maxs = tuple(0.5 * (n - 1) for n in ns)
+    logK = pkg.fields.volume_logk(ns, mins, maxs, 0.5 * maxs[0] + 1.0, 1.0 + 0.5 * (seed % 3), -9.0, seed)
+    N = int(np.prod(ns))
+    rng = np.random.default_rng(seed)
+    Qs = np.zeros(N)
+    q = rng.choice(N, 1 + seed % 4, replace=False)
+    Qs[q] = rng.uniform(1e-5, 1e-3, len(q))
+    dn = np.sort(rng.choice(np.setdiff1d(np.arange(N), q), 1 + (seed + 1) % 4, replace=False))
+    dh = np.zeros(N)
+    obs = rng.choice(N, 10, replace=False)
+    return dict(ns=ns, mins=mins, maxs=maxs, logK=logK, N=N, Qs=Qs, dn=dn, dh=dh, obs=obs)
+
+
+def _oracle(orc, pkg, c):
+    _, nb, aol, _ = pkg.regulargrid3d(c["mins"], c["maxs"], c["ns"])
+    O = orc.Problem(c["N"], nb, aol, c["dn"])
+    h = O.steady(orc.logk_to_faces(nb, c["logK"]), c["dh"], c["Qs"], reltol=1e-14)
+    delta = np.zeros(c["N"])
+    np.add.at(delta, c["obs"], 2 * h[c["obs"]])
+    dKs, _, _ = O.adjoint(c["dh"], delta, reltol=1e-14)
+    return h, orc.logk_to_faces_vjp(nb, c["logK"], dKs)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_uneven_batch_vs_oracle(gpu_lib, orc, precision):
+    pkg = gpu_lib
+    shapes = [(20, 16, 5), (9, 9, 9), (40, 30, 6), (3, 4, 2), (25, 25, 4), (17, 5, 11)]
+    probs = [_problem(pkg, ns, 11 + k) for k, ns in enumerate(shapes)]
+    B = pkg.GroundwaterBatch([p["ns"] for p in probs], [p["mins"] for p in probs], [p["maxs"] for p in probs],
+                             [p["dn"] for p in probs], reltol=1e-11, precision=precision)
+    assert B.nprob == len(probs)
+    cat = lambda k: np.concatenate([p[k] for p in probs])
+    h, g = B.solve_grad_logk(cat("logK"), cat("dh"), cat("Qs"), [p["obs"] for p in probs])
+    for k, p in enumerate(probs):
+        a, b = B.cell_offsets[k], B.cell_offsets[k + 1]
+        h_or, g_or = _oracle(orc, pkg, p)
+        assert rel(h[a:b], h_or) < 1e-8, k
+        assert rel(g[a:b], g_or) < 1e-6, k
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_graph_and_host_loops_agree(gpu_lib, precision):
+    pkg = gpu_lib
+    c = _problem(pkg, (30, 24, 10), 5)
+    res = []
+    for graphs in (1, 0):
+        P = pkg.GroundwaterProblem.regular3d(c["mins"], c["maxs"], c["ns"], c["dn"], reltol=1e-11,
+                                              precision=precision, use_graphs=graphs, check_every=3)
+        res.append((P.solve_grad_logk(c["logK"], c["dh"], c["Qs"], c["obs"]), P.stats))
+    (h1, g1), s1 = res[0]
+    (h2, g2), s2 = res[1]
+    assert s1["iterations"] == s2["iterations"]
+    assert rel(h1, h2) < 1e-12 and rel(g1, g2) < 1e-10
+
+
+def test_batch_of_identical_problems_is_uniform(gpu_lib):
+    pkg = gpu_lib
+    c = _problem(pkg, (16, 16, 8), 3)
+    nb = 5
+    B = pkg.GroundwaterBatch([c["ns"]] * nb, [c["mins"]] * nb, [c["maxs"]] * nb, [c["dn"]] * nb, reltol=1e-11,
+                             precision="mixed")
+    h, g = B.solve_grad_logk(np.tile(c["logK"], nb), np.tile(c["dh"], nb), np.tile(c["Qs"], nb), [c["obs"]] * nb)
+    N = c["N"]
+    for k in range(1, nb):
+        assert np.array_equal(h[k * N:(k + 1) * N], h[:N])
+        assert np.array_equal(g[k * N:(k + 1) * N], g[:N])
+
+
+def test_profile_report_and_launch_count(gpu_lib):
+    pkg = gpu_lib
+    c = _problem(pkg, (20, 20, 6), 9)
+    P = pkg.GroundwaterProblem.regular3d(c["mins"], c["maxs"], c["ns"], c["dn"], precision="mixed")
+    n0 = P.launch_count
+    P.profile(True)
+    P.solve_grad_logk(c["logK"], c["dh"], c["Qs"], c["obs"])
+    rep = P.profile_report()
+    P.profile(False)
+    assert P.launch_count > n0
+    assert any(k.startswith("k_cheb_step<f32>/L0") for k in rep)
+    assert all(v[0] > 0 and v[1] >= 0 for v in rep.values())
+    assert sum(v[0] for v in rep.values()) == P.launch_count - n0
