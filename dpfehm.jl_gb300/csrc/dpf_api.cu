@@ -223,7 +223,7 @@ void dpf_default_options(dpf_options *o) {
     o->cheb_lo = 0.2;
     o->coarse_scale = 2.0;
     o->max_coarse = 64;
-    o->inner_tol = 1e-2;
+    o->inner_tol = 5e-2;
     o->max_outer = 60;
     o->use_graphs = 1;
     o->check_every = 1;

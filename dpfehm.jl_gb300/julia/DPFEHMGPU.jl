@@ -1,0 +1,121 @@
+"""
+    DPFEHMGPU
+
+Julia binding of libdpfehm_gpu.so (C ABI in include/dpfehm_gpu.h): drop-in
+versions of `DPFEHM.groundwater_steadystate` and its `ChainRulesCore.rrule`
+(DPFEHM src/groundwater.jl:75-109) that solve on a GB300 through `ccall`.
+
+Not exercised in this repository's tests (no Julia toolchain is available where
+they run); the same C entry points are exercised through ctypes.
+"""
+module DPFEHMGPU
+
+import ChainRulesCore
+
+const libdpf = get(ENV, "DPFEHM_GPU_LIB", joinpath(@__DIR__, "..", "_build", "libdpfehm_gpu.so"))
+
+const DPF_OK = Cint(0)
+const DPF_NOT_CONVERGED = Cint(2)
+
+mutable struct Options
+    reltol::Cdouble
+    maxiter::Cint
+    precision::Cint
+    cheb_degree::Cint
+    cheb_lo::Cdouble
+    coarse_scale::Cdouble
+    max_coarse::Cint
+    inner_tol::Cdouble
+    max_outer::Cint
+    use_graphs::Cint
+    check_every::Cint
+end
+
+function default_options(; reltol=nothing, maxiter=nothing, precision=nothing)
+    o = Options(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
+    ccall((:dpf_default_options, libdpf), Cvoid, (Ref{Options},), o)
+    reltol === nothing || (o.reltol = reltol)
+    maxiter === nothing || (o.maxiter = maxiter)
+    precision === nothing || (o.precision = precision == :mixed ? 1 : 0)
+    return o
+end
+
+lasterror(h) = unsafe_string(ccall((:dpf_last_error, libdpf), Cstring, (Ptr{Cvoid},), h))
+
+function check(h, rc)
+    rc == DPF_OK && return nothing
+    rc == DPF_NOT_CONVERGED && (@warn "groundwater solve did not reach reltol: $(lasterror(h))"; return nothing)
+    error("libdpfehm_gpu status $rc: $(lasterror(h))")
+end
+
+"""A problem handle: topology, multigrid hierarchy and the last forward state on the GPU."""
+mutable struct Problem
+    ptr::Ptr{Cvoid}
+    N::Int
+    F::Int
+end
+
+function Problem(neighbors, areasoverlengths, dirichletnodes, N; volumes=nothing, kwargs...)
+    F = length(neighbors)
+    a = Int64[p[1] - 1 for p in neighbors]          # 1-based pairs -> 0-based arrays
+    b = Int64[p[2] - 1 for p in neighbors]
+    aol = Vector{Float64}(areasoverlengths[1:F])
+    dn = Int64[d - 1 for d in dirichletnodes]
+    vol = volumes === nothing ? Ptr{Float64}(C_NULL) : Vector{Float64}(volumes)  # ccall roots a Vector argument
+    opts = default_options(; kwargs...)
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    rc = ccall((:dpf_create, libdpf), Cint,
+        (Int64, Int64, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Int64}, Ref{Options},
+         Ref{Ptr{Cvoid}}), N, F, a, b, aol, vol, length(dn), dn, opts, out)
+    rc == DPF_OK || error("dpf_create failed ($rc): $(lasterror(C_NULL))")
+    p = Problem(out[], N, F)
+    finalizer(p) do q
+        q.ptr == C_NULL || ccall((:dpf_destroy, libdpf), Cvoid, (Ptr{Cvoid},), q.ptr)
+        q.ptr = C_NULL
+    end
+    return p
+end
+
+function forward(p::Problem, Ks, dirichleths, Qs)
+    h = Vector{Float64}(undef, p.N)
+    K = Vector{Float64}(Ks); d = Vector{Float64}(dirichleths); q = Vector{Float64}(Qs)
+    rc = ccall((:dpf_steady_forward, libdpf), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+               Ptr{Float64}), p.ptr, K, d, q, h)
+    check(p.ptr, rc)
+    return h
+end
+
+function adjoint(p::Problem, delta)
+    dKs = Vector{Float64}(undef, p.F)
+    ddh = Vector{Float64}(undef, p.N)
+    dQs = Vector{Float64}(undef, p.N)
+    dl = Vector{Float64}(delta)
+    rc = ccall((:dpf_steady_adjoint, libdpf), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+               Ptr{Float64}), p.ptr, dl, dKs, ddh, dQs)
+    check(p.ptr, rc)
+    return dKs, ddh, dQs
+end
+
+"""Drop-in for `DPFEHM.groundwater_steadystate` (the `linear_solver` keyword is ignored)."""
+function groundwater_steadystate(Ks, neighbors, areasoverlengths, dirichletnodes, dirichleths, Qs;
+                                 linear_solver=nothing, kwargs...)
+    p = Problem(neighbors, areasoverlengths, dirichletnodes, length(Qs); kwargs...)
+    return forward(p, Ks, dirichleths, Qs)
+end
+
+function ChainRulesCore.rrule(::typeof(groundwater_steadystate), Ks, neighbors, areasoverlengths, dirichletnodes,
+                              dirichleths, Qs; kwargs...)
+    p = Problem(neighbors, areasoverlengths, dirichletnodes, length(Qs); kwargs...)
+    h = forward(p, Ks, dirichleths, Qs)
+    function pullback(delta)
+        dKs, ddh, dQs = adjoint(p, delta)     # the closure keeps the GPU handle alive
+        return (ChainRulesCore.NoTangent(),
+                ChainRulesCore.@thunk(dKs),
+                ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(),
+                ChainRulesCore.@thunk(ddh),
+                ChainRulesCore.@thunk(dQs))
+    end
+    return h, pullback
+end
+
+end # module

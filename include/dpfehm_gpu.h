@@ -72,7 +72,7 @@ typedef struct dpf_options {
     double cheb_lo;      /* lower end of the Chebyshev interval / upper end   (default 0.2)   */
     double coarse_scale; /* scaling of the coarse-grid correction              (default 2.0)   */
     int max_coarse;      /* coarsen until a level has at most this many cells (default 64, <= 64) */
-    double inner_tol;    /* MIXED: residual reduction between FP64 residual replacements (default 1e-2) */
+    double inner_tol;    /* MIXED: residual reduction between FP64 residual replacements (default 5e-2) */
     int max_outer;       /* MIXED: cap on FP64 residual replacements per solve (default 60)   */
     int use_graphs;      /* capture each solve's iteration in a CUDA graph    (default 1)     */
     int check_every;     /* convergence is read back every this many iterations (default 1)   */
