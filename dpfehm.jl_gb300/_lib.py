@@ -73,6 +73,8 @@ SIGNATURES = {
                                           ctypes.POINTER(ctypes.c_longlong), _f64p,
                                           ctypes.POINTER(ctypes.c_longlong)]),
     "dpf_launch_count": (ctypes.c_longlong, [_vp]),
+    "dpf_logk_to_faces_regular_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_int,
+                                                         _vp]),
 }
 
 _lib = None

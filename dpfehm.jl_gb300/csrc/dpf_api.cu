@@ -37,6 +37,11 @@ struct dpf_problem {
 
 static thread_local std::string g_create_error;
 
+namespace dpf {
+// message for dpf_last_error(NULL) from entry points that have no handle
+void set_global_error(const std::string &msg) { g_create_error = msg; }
+}  // namespace dpf
+
 namespace {
 
 struct DeviceGuard {

@@ -203,6 +203,21 @@ int dpf_profile_report(dpf_problem *h, int cap, const char **names, long long *l
 /* Kernel launches issued by the handle since it was created. */
 long long dpf_launch_count(const dpf_problem *h);
 
+/* ------------------------------------------------------ allocation-free path */
+
+/* No counterpart in the reference. The same face conductances as
+ * dpf_logk_to_faces on a regulargrid3d handle, for callers that must not have the
+ * library allocate device memory (an application that owns all device memory
+ * through its own pool): no handle, no cudaMalloc/cudaFree. logK[nx*ny*nz] and
+ * Ks[F] must be device pointers on the current device. The working memory is a
+ * fixed 16 MiB module array, so grids are limited to 2,097,152 cells (larger ones
+ * get DPF_BAD_INPUT). The first call on a device looks up that array's address;
+ * make it before any stream capture. All calls share the array: calls that
+ * overlap on the GPU race and must be serialized by the caller. Runs on the
+ * legacy default stream and returns when Ks is complete; errors are described by
+ * dpf_last_error(NULL). */
+int dpf_logk_to_faces_regular_noalloc(int nx, int ny, int nz, const double *logK, int mean_kind, double *Ks);
+
 #ifdef __cplusplus
 }
 #endif
