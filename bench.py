@@ -164,6 +164,9 @@ def run_ours(args, dist, rank, ws):
     d_Qs = torch.tensor(Qs, device=dev)
     flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float64, device=dev)
 
+    import warnings
+    warnings.simplefilter("error", RuntimeWarning)  # a solve that misses reltol must not be timed silently
+
     def step_dev():
         return batch.solve_grad_logk(d_logK, d_dh, d_Qs, obs)
 

@@ -31,6 +31,7 @@ class Options(ctypes.Structure):
         ("max_outer", ctypes.c_int),
         ("use_graphs", ctypes.c_int),
         ("check_every", ctypes.c_int),
+        ("blocks_per_sm", ctypes.c_int),
     ]
 
 

@@ -188,6 +188,7 @@ dpf_options fill_options(const dpf_options *o) {
     if (!(r.inner_tol > 0)) r.inner_tol = d.inner_tol;
     if (r.max_outer <= 0) r.max_outer = d.max_outer;
     if (r.check_every <= 0) r.check_every = d.check_every;
+    if (r.blocks_per_sm <= 0) r.blocks_per_sm = d.blocks_per_sm;
     return r;
 }
 
@@ -232,6 +233,7 @@ void dpf_default_options(dpf_options *o) {
     o->max_outer = 60;
     o->use_graphs = 1;
     o->check_every = 1;
+    o->blocks_per_sm = 16;
 }
 
 int dpf_detect_regular3d(int64_t N, int64_t F, const int64_t *a, const int64_t *b, const double *aol, int *dims,

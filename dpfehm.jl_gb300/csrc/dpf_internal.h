@@ -42,8 +42,8 @@ inline void fast_div_magic(unsigned d, unsigned &m, int &l) {
     m = (unsigned)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
 }
 
-struct BlockMap {                  // launch map: block -> (problem, block within problem)
-    int2 *d_map = nullptr;         // [nblocks]
+struct BlockMap {                  // launch map: block -> (problem, block within problem, blocks of problem)
+    int4 *d_map = nullptr;         // [nblocks]
     int2 *d_pinfo = nullptr;       // [nprob] {first block, number of blocks} (0,0 if absent)
     int nblocks = 0;
 };
@@ -55,6 +55,7 @@ struct CgState {
     double scale;                  // mixed precision: normalisation of the FP32 residual
     double ratio;                  // mixed precision: old scale / new scale at the last update
     double orr, obb;               // mixed precision: true (FP64) residual and rhs norms squared
+    double orr_prev;               // mixed precision: true residual norm squared at the previous replacement
     int iters, active, status, outer;  // outer: reliable updates so far
     int ru_flag, total_iters, pad1, pad2;
 };

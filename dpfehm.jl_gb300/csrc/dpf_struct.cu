@@ -23,7 +23,7 @@ namespace dpf {
 
 // ================================================================ kernels
 #define DPF_BLOCK_PROLOGUE(DESC, BMAP, ST)                 \
-    int2 bm = (BMAP)[blockIdx.x];                          \
+    int4 bm = (BMAP)[blockIdx.x];                          \
     const int p = bm.x;                                    \
     if ((ST) && !(ST)[p].active) return;                   \
     const LevelDesc L = (DESC)[p];
@@ -36,30 +36,33 @@ __device__ __forceinline__ void deactivate(CgState &s, int *count) {
 }
 
 template <typename T>
-__global__ void k_cheb_first(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+__global__ void k_cheb_first(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                              Coeffs<T> C, const T *__restrict__ b, T *__restrict__ x, T *__restrict__ d,
                              T invtheta) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
-    Cell c;
-    if (!decode_cell(L, bm.y, c)) return;
-    T v;
-    if constexpr (sizeof(T) == 8) v = invtheta * b[c.i] * C.idg[c.i];
-    else v = invtheta * __fdividef(b[c.i], diag7(L, c, C));
-    x[c.i] = v;
-    d[c.i] = v;
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        T v;
+        if constexpr (sizeof(T) == 8) v = invtheta * b[c.i] * C.idg[c.i];
+        else v = invtheta * __fdividef(b[c.i], diag7(L, c, C));
+        x[c.i] = v;
+        d[c.i] = v;
+    }
 }
 
 // One Chebyshev step on D^-1 A: r = D^-1 (b - A xin); d = c1 d + c2 r; xout = xin + d.
 // With FUSE_RZ the kernel is the last of the level-0 V-cycle: it also reduces b . xout
 // (b is the CG residual, xout the preconditioned residual) and finalises beta.
 template <typename T, bool FUSE_RZ>
-__global__ void k_cheb_step(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+__global__ void k_cheb_step(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                             Coeffs<T> C, const T *__restrict__ b, const T *__restrict__ xin, T *__restrict__ xout,
                             T *__restrict__ d, T c1, T c2, ReduceScratch rs, const int2 *__restrict__ pinfo) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
-    Cell c;
     Acc<T> part;
-    if (decode_cell(L, bm.y, c)) {
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
         T xi = xin[c.i], Ax, dg;
         apply7(L, c, C, xi, [&](long long j, int, int, int) { return xin[j]; }, Ax, dg);
         T bi = b[c.i];
@@ -68,7 +71,7 @@ __global__ void k_cheb_step(const LevelDesc *__restrict__ desc, const int2 *__re
         T xo = xi + dn;
         d[c.i] = dn;
         xout[c.i] = xo;
-        if (FUSE_RZ) part = Acc<T>::prod(bi, xo);
+        if (FUSE_RZ) part = part + Acc<T>::prod(bi, xo);
     }
     if (FUSE_RZ) {
         double2 tot;
@@ -84,30 +87,32 @@ __global__ void k_cheb_step(const LevelDesc *__restrict__ desc, const int2 *__re
 // Restriction of the residual: bc[I] = sum over the children i of I of (b_i - (A x)_i).
 template <typename T>
 __global__ void k_restrict(const LevelDesc *__restrict__ fdesc, const LevelDesc *__restrict__ cdesc,
-                           const int2 *__restrict__ bmap, CgState *st, Coeffs<T> C, const T *__restrict__ b,
+                           const int4 *__restrict__ bmap, CgState *st, Coeffs<T> C, const T *__restrict__ b,
                            const T *__restrict__ x, T *__restrict__ bc) {
-    int2 bm = bmap[blockIdx.x];
+    int4 bm = bmap[blockIdx.x];
     const int p = bm.x;
     if (st && !st[p].active) return;
     const LevelDesc Lc = cdesc[p];
-    Cell cc;
-    if (!decode_cell(Lc, bm.y, cc)) return;
-    const LevelDesc L = fdesc[p];
-    const long long fsy = L.nz, fsx = (long long)L.ny * L.nz;
-    int x0 = 2 * cc.ix, y0 = 2 * cc.iy, z0 = 2 * cc.iz;
-    int x1 = min(x0 + 1, L.nx - 1), y1 = min(y0 + 1, L.ny - 1), z1 = min(z0 + 1, L.nz - 1);
-    T acc = 0;
-    for (int fx = x0; fx <= x1; fx++)
-        for (int fy = y0; fy <= y1; fy++)
-            for (int fz = z0; fz <= z1; fz++) {
-                Cell c;
-                c.ix = fx; c.iy = fy; c.iz = fz;
-                c.i = L.off + fx * fsx + fy * fsy + fz;
-                T xi = x[c.i], Ax, dg;
-                apply7(L, c, C, xi, [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
-                acc += b[c.i] - Ax;
-            }
-    bc[cc.i] = acc;
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)Lc.n; li_ += bm.z * kBlock) {
+        Cell cc;
+        cell_at(Lc, li_, cc);
+        const LevelDesc L = fdesc[p];
+        const long long fsy = L.nz, fsx = (long long)L.ny * L.nz;
+        int x0 = 2 * cc.ix, y0 = 2 * cc.iy, z0 = 2 * cc.iz;
+        int x1 = min(x0 + 1, L.nx - 1), y1 = min(y0 + 1, L.ny - 1), z1 = min(z0 + 1, L.nz - 1);
+        T acc = 0;
+        for (int fx = x0; fx <= x1; fx++)
+            for (int fy = y0; fy <= y1; fy++)
+                for (int fz = z0; fz <= z1; fz++) {
+                    Cell c;
+                    c.ix = fx; c.iy = fy; c.iz = fz;
+                    c.i = L.off + fx * fsx + fy * fsy + fz;
+                    T xi = x[c.i], Ax, dg;
+                    apply7(L, c, C, xi, [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
+                    acc += b[c.i] - Ax;
+                }
+        bc[cc.i] = acc;
+    }
 }
 
 // Prolongation of the coarse correction fused with the first post-smoothing step:
@@ -115,28 +120,36 @@ __global__ void k_restrict(const LevelDesc *__restrict__ fdesc, const LevelDesc 
 // d = invtheta r, xout = x' + d.
 template <typename T, bool FUSE_RZ>
 __global__ void k_prolong_cheb(const LevelDesc *__restrict__ desc, const LevelDesc *__restrict__ cdesc,
-                               const int2 *__restrict__ bmap, CgState *st, Coeffs<T> C,
+                               const int4 *__restrict__ bmap, CgState *st, Coeffs<T> C,
                                const uint8_t *__restrict__ dir, const T *__restrict__ b, const T *__restrict__ x,
                                const T *__restrict__ e, T *__restrict__ xout, T *__restrict__ d, T scale,
                                T invtheta, ReduceScratch rs, const int2 *__restrict__ pinfo) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     const LevelDesc Lc = cdesc[p];
-    Cell c;
     Acc<T> part;
-    if (decode_cell(L, bm.y, c)) {
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        // aggregate of this cell; a neighbour's aggregate differs by at most one coarse
+        // cell in the direction of the neighbour
+        const int X = c.ix >> 1, Y = c.iy >> 1, Z = c.iz >> 1;
+        const long long csy = Lc.nz, csx = (long long)Lc.ny * Lc.nz;
+        const long long base = Lc.off + X * csx + Y * csy + Z;
+        // Dirichlet (identity) rows have no couplings, so only the centre needs the mask:
+        // a neighbour's value is multiplied by a zero coupling when the neighbour is one
         auto xp = [&](long long j, int jx, int jy, int jz) -> T {
-            T v = x[j];
-            if (!dir[j]) v += scale * e[Lc.off + ((long long)(jx >> 1) * Lc.ny + (jy >> 1)) * Lc.nz + (jz >> 1)];
-            return v;
+            return x[j] + scale * e[base + ((jx >> 1) - X) * csx + ((jy >> 1) - Y) * csy + ((jz >> 1) - Z)];
         };
-        T xi = xp(c.i, c.ix, c.iy, c.iz), Ax, dg;
+        T xi = x[c.i];
+        if (!dir[c.i]) xi += scale * e[base];
+        T Ax, dg;
         apply7(L, c, C, xi, xp, Ax, dg);
         T bi = b[c.i];
         T dn = invtheta * dinv_times(C, c.i, bi - Ax, dg);
         T xo = xi + dn;
         d[c.i] = dn;
         xout[c.i] = xo;
-        if (FUSE_RZ) part = Acc<T>::prod(bi, xo);
+        if (FUSE_RZ) part = part + Acc<T>::prod(bi, xo);
     }
     if (FUSE_RZ) {
         double2 tot;
@@ -189,25 +202,26 @@ __global__ void k_coarse_solve(const LevelDesc *__restrict__ desc, const int *__
 // ---------------------------------------------------------------- CG kernels
 // r = b - A x; reduce (r.r, b.b); activate the problem unless already converged.
 template <typename T>
-__global__ void k_cg_start(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+__global__ void k_cg_start(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                            int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, Coeffs<T> C,
                            const T *__restrict__ b, const T *__restrict__ x, T *__restrict__ r, double tol2) {
-    int2 bm = bmap[blockIdx.x];
+    int4 bm = bmap[blockIdx.x];
     const int p = bm.x;
     const LevelDesc L = desc[p];
-    Cell c;
     Acc<T> rr, bb;
-    if (decode_cell(L, bm.y, c)) {
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
         T xi = x[c.i], Ax, dg;
         apply7(L, c, C, xi, [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
         T bi = b[c.i];
         T ri = bi - Ax;
         r[c.i] = ri;
-        rr = Acc<T>::prod(ri, ri);
-        bb = Acc<T>::prod(bi, bi);
+        rr = rr + Acc<T>::prod(ri, ri);
+        bb = bb + Acc<T>::prod(bi, bi);
     }
     double2 tot;
-    if (reduce_last<T>(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+    if (reduce_last<T, 2>(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
         CgState &s = st[p];
         s.rr = tot.x;
         s.bb = tot.y;
@@ -226,17 +240,18 @@ __global__ void k_cg_start(const LevelDesc *__restrict__ desc, const int2 *__res
 
 // q = A p; alpha = rz / (p . q)
 template <typename T>
-__global__ void k_spmv_pq(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+__global__ void k_spmv_pq(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                           int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, Coeffs<T> C,
                           const T *__restrict__ pv, T *__restrict__ q) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
-    Cell c;
     Acc<T> part;
-    if (decode_cell(L, bm.y, c)) {
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
         T pi = pv[c.i], Ax, dg;
         apply7(L, c, C, pi, [&](long long j, int, int, int) { return pv[j]; }, Ax, dg);
         q[c.i] = Ax;
-        part = Acc<T>::prod(pi, Ax);
+        part = part + Acc<T>::prod(pi, Ax);
     }
     double2 tot;
     if (reduce_last<T>(part, Acc<T>(), rs, pinfo[p], p, tot) && threadIdx.x == 0) {
@@ -252,20 +267,21 @@ __global__ void k_spmv_pq(const LevelDesc *__restrict__ desc, const int2 *__rest
 // residual is normalised: the problem is flagged for a reliable update instead of
 // being declared converged, which only the true FP64 residual can decide.
 template <typename T, bool RU>
-__global__ void k_update_xr(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+__global__ void k_update_xr(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                             int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, T *__restrict__ x,
                             T *__restrict__ r, const T *__restrict__ pv, const T *__restrict__ q, int maxiter,
                             int *upd_count, double delta2) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     const double alpha = st[p].alpha;
-    Cell c;
     Acc<T> part;
-    if (decode_cell(L, bm.y, c)) {
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
         T a = (T)alpha;
         x[c.i] += a * pv[c.i];
         T ri = r[c.i] - a * q[c.i];
         r[c.i] = ri;
-        part = Acc<T>::prod(ri, ri);
+        part = part + Acc<T>::prod(ri, ri);
     }
     double2 tot;
     if (reduce_last<T>(part, Acc<T>(), rs, pinfo[p], p, tot) && threadIdx.x == 0) {
@@ -286,13 +302,15 @@ __global__ void k_update_xr(const LevelDesc *__restrict__ desc, const int2 *__re
 
 // p = z + beta p
 template <typename T>
-__global__ void k_update_p(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+__global__ void k_update_p(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                            const T *__restrict__ z, T *__restrict__ pv) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     const T beta = (T)st[p].beta;
-    Cell c;
-    if (!decode_cell(L, bm.y, c)) return;
-    pv[c.i] = beta == (T)0 ? z[c.i] : z[c.i] + beta * pv[c.i];
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        pv[c.i] = beta == (T)0 ? z[c.i] : z[c.i] + beta * pv[c.i];
+    }
 }
 
 // ------------------------------------- mixed precision: reliable-update CG
@@ -304,43 +322,46 @@ __global__ void k_update_p(const LevelDesc *__restrict__ desc, const int2 *__res
 // new normalisation). Convergence is decided on the true FP64 residual only.
 
 // x64 += scale * xs; xs = 0   (flagged problems)
-__global__ void k_ru_accum(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, const CgState *st,
+__global__ void k_ru_accum(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, const CgState *st,
                            double *__restrict__ x64, float *__restrict__ xs) {
-    int2 bm = bmap[blockIdx.x];
+    int4 bm = bmap[blockIdx.x];
     const int p = bm.x;
     if (!st[p].ru_flag) return;
     const LevelDesc L = desc[p];
     const double sc = st[p].scale;
-    Cell c;
-    if (!decode_cell(L, bm.y, c)) return;
-    x64[c.i] += sc * (double)xs[c.i];
-    xs[c.i] = 0.0f;
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        x64[c.i] += sc * (double)xs[c.i];
+        xs[c.i] = 0.0f;
+    }
 }
 
 // r64 = b - A x64 in FP64 flux form. START: every problem, sets up the state.
 // Otherwise flagged problems only: converged -> inactive, else new normalisation.
 template <bool START>
-__global__ void k_ru_residual(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, CgState *st,
+__global__ void k_ru_residual(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                               int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo,
                               Coeffs<double> C, const double *__restrict__ b, const double *__restrict__ x,
                               double *__restrict__ r, double tol2, int maxiter, int max_updates) {
-    int2 bm = bmap[blockIdx.x];
+    int4 bm = bmap[blockIdx.x];
     const int p = bm.x;
     if (!START && !st[p].ru_flag) return;
     const LevelDesc L = desc[p];
-    Cell c;
     Acc<double> rr, bb;
-    if (decode_cell(L, bm.y, c)) {
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
         double xi = x[c.i], Ax, dg;
         apply7(L, c, C, xi, [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
         double bi = b[c.i];
         double ri = bi - Ax;
         r[c.i] = ri;
-        rr.v = ri * ri;
-        if (START) bb.v = bi * bi;
+        rr.v += ri * ri;
+        if (START) bb.v += bi * bi;
     }
     double2 tot;
-    if (reduce_last<double>(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+    if (reduce_last<double, START ? 2 : 1>(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
         CgState &s = st[p];
         s.orr = tot.x;
         if (START) {
@@ -354,6 +375,7 @@ __global__ void k_ru_residual(const LevelDesc *__restrict__ desc, const int2 *__
             s.rz_old = 0.0;
             s.beta = 0.0;
             s.ratio = 1.0;
+            s.orr_prev = s.orr;
             bool act = s.obb > 0.0 && s.orr > tol2 * s.obb;
             if (!isfinite(s.orr)) { s.status = DPF_NAN; act = false; }
             s.active = act ? 1 : 0;
@@ -364,8 +386,14 @@ __global__ void k_ru_residual(const LevelDesc *__restrict__ desc, const int2 *__
             }
         } else {
             s.outer++;
+            // the recursion believed it had converged (estimate with the old scale) ...
+            const bool apparent = s.rr * s.scale * s.scale <= tol2 * s.obb;
+            // ... but the true residual did not even halve since the last replacement:
+            // it sits at the FP64 rounding floor of b - A x, so no further accuracy exists
+            const bool floor = apparent && s.orr > 0.25 * s.orr_prev;
+            s.orr_prev = s.orr;
             if (!isfinite(s.orr)) { s.status = DPF_NAN; s.ru_flag = 0; deactivate(s, active_count); }
-            else if (s.orr <= tol2 * s.obb) { s.ru_flag = 0; deactivate(s, active_count); }
+            else if (s.orr <= tol2 * s.obb || floor) { s.ru_flag = 0; deactivate(s, active_count); }
             else if (s.iters >= maxiter || s.outer >= max_updates) {
                 s.status = DPF_NOT_CONVERGED;
                 s.ru_flag = 0;
@@ -381,20 +409,22 @@ __global__ void k_ru_residual(const LevelDesc *__restrict__ desc, const int2 *__
 }
 
 // r32 = r64 / scale; START: xs = 0; otherwise p *= ratio   (flagged problems)
-__global__ void k_ru_cast(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, const CgState *st,
+__global__ void k_ru_cast(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, const CgState *st,
                           const double *__restrict__ r64, float *__restrict__ r32, float *__restrict__ pv,
                           float *__restrict__ xs, int start) {
-    int2 bm = bmap[blockIdx.x];
+    int4 bm = bmap[blockIdx.x];
     const int p = bm.x;
     if (!st[p].ru_flag) return;
     const LevelDesc L = desc[p];
     const double inv = 1.0 / st[p].scale;
     const float ratio = (float)st[p].ratio;
-    Cell c;
-    if (!decode_cell(L, bm.y, c)) return;
-    r32[c.i] = (float)(r64[c.i] * inv);
-    if (start) xs[c.i] = 0.0f;
-    else pv[c.i] *= ratio;
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        r32[c.i] = (float)(r64[c.i] * inv);
+        if (start) xs[c.i] = 0.0f;
+        else pv[c.i] *= ratio;
+    }
 }
 
 __global__ void k_ru_clear(CgState *st, int nprob, int *upd_count) {
@@ -419,15 +449,17 @@ __global__ void k_state_init(CgState *st, int nprob) {
 }
 
 // adjoint right-hand side: rhs = delta at free cells, 0 at Dirichlet cells; x = 0
-__global__ void k_adjoint_rhs(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+__global__ void k_adjoint_rhs(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                               const uint8_t *__restrict__ dir, const double *__restrict__ delta,
                               double *__restrict__ rhs, double *__restrict__ x) {
-    int2 bm = bmap[blockIdx.x];
+    int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
-    Cell c;
-    if (!decode_cell(L, bm.y, c)) return;
-    rhs[c.i] = dir[c.i] ? 0.0 : delta[c.i];
-    x[c.i] = 0.0;
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        rhs[c.i] = dir[c.i] ? 0.0 : delta[c.i];
+        x[c.i] = 0.0;
+    }
 }
 
 // delta = 2 h at observation cells (J = sum h[obs]^2), 0 elsewhere (delta zeroed before)
@@ -440,196 +472,216 @@ __global__ void k_obs_delta(const long long *__restrict__ obs_global, long long 
 }
 
 // storage shift S_i V_i / dt (transient)
-__global__ void k_shift(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+__global__ void k_shift(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                         const ProbParam *__restrict__ prm, const double *__restrict__ Ss, double inv_dt,
                         double *__restrict__ shift) {
-    int2 bm = bmap[blockIdx.x];
+    int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
-    Cell c;
-    if (!decode_cell(L, bm.y, c)) return;
-    shift[c.i] = Ss[c.i] * prm[bm.x].vol * inv_dt;
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        shift[c.i] = Ss[c.i] * prm[bm.x].vol * inv_dt;
+    }
 }
 
 // b_n = b0 + shift * h_prev (transient right-hand side); Dirichlet rows keep b0 = dirichleths
-__global__ void k_axpy_rhs(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+__global__ void k_axpy_rhs(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                            const uint8_t *__restrict__ dir, const double *__restrict__ b0,
                            const double *__restrict__ shift, const double *__restrict__ hprev,
                            double *__restrict__ b) {
-    int2 bm = bmap[blockIdx.x];
+    int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
-    Cell c;
-    if (!decode_cell(L, bm.y, c)) return;
-    b[c.i] = dir[c.i] ? b0[c.i] : b0[c.i] + shift[c.i] * hprev[c.i];
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        b[c.i] = dir[c.i] ? b0[c.i] : b0[c.i] + shift[c.i] * hprev[c.i];
+    }
 }
 
 // ------------------------------------------------------------- gradients
 // dKs_f = -aol_f (h_a - h_b)(lambda_a - lambda_b), in the reference face order; with
 // accumulate != 0 it adds to dKs (transient adjoint sums over steps).
-__global__ void k_grad_faces(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+__global__ void k_grad_faces(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                              const ProbParam *__restrict__ prm, const double *__restrict__ h,
                              const double *__restrict__ lam, double *__restrict__ dKs, int accumulate) {
-    int2 bm = bmap[blockIdx.x];
+    int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
-    Cell c;
-    if (!decode_cell(L, bm.y, c)) return;
-    const ProbParam P = prm[bm.x];
-    const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
-    const int co[3] = {c.ix, c.iy, c.iz};
-    const int nn[3] = {L.nx, L.ny, L.nz};
-    const double hi = h[c.i], li = lam[c.i];
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        if (co[d] + 1 < nn[d]) {
-            long long j = c.i + st3[d];
-            double g = -P.aol[d] * (hi - h[j]) * (li - lam[j]);
-            long long f = P.face_off + regular_face_index(L.nx, L.ny, L.nz, c.ix, c.iy, c.iz, d);
-            if (accumulate) dKs[f] += g; else dKs[f] = g;
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        const ProbParam P = prm[bm.x];
+        const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
+        const int co[3] = {c.ix, c.iy, c.iz};
+        const int nn[3] = {L.nx, L.ny, L.nz};
+        const double hi = h[c.i], li = lam[c.i];
+    #pragma unroll
+        for (int d = 0; d < 3; d++) {
+            if (co[d] + 1 < nn[d]) {
+                long long j = c.i + st3[d];
+                double g = -P.aol[d] * (hi - h[j]) * (li - lam[j]);
+                long long f = P.face_off + regular_face_index(L.nx, L.ny, L.nz, c.ix, c.iy, c.iz, d);
+                if (accumulate) dKs[f] += g; else dKs[f] = g;
+            }
         }
     }
 }
 
 // dlogK_i = sum over the faces of i of dK_f/dlogK_i * dKs_f, with dKs_f formed on the fly
 // from h and lambda; K_f and its derivative come from the per-cell values kc.
-__global__ void k_grad_logk(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+__global__ void k_grad_logk(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                             const ProbParam *__restrict__ prm, const double *__restrict__ kc, int kind,
                             const double *__restrict__ h, const double *__restrict__ lam, double *__restrict__ g) {
-    int2 bm = bmap[blockIdx.x];
+    int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
-    Cell c;
-    if (!decode_cell(L, bm.y, c)) return;
-    const ProbParam P = prm[bm.x];
-    const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
-    const int co[3] = {c.ix, c.iy, c.iz};
-    const int nn[3] = {L.nx, L.ny, L.nz};
-    const double hi = h[c.i], li = lam[c.i], ki = kc[c.i];
-    double acc = 0.0;
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-#pragma unroll
-        for (int s = -1; s <= 1; s += 2) {
-            bool ok = s > 0 ? co[d] + 1 < nn[d] : co[d] > 0;
-            if (!ok) continue;
-            long long j = c.i + s * st3[d];
-            double dK = -P.aol[d] * (hi - h[j]) * (li - lam[j]);
-            double K = face_mean_k(ki, kc[j], kind);
-            acc += face_mean_dlogk(K, ki, kind) * dK;
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        const ProbParam P = prm[bm.x];
+        const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
+        const int co[3] = {c.ix, c.iy, c.iz};
+        const int nn[3] = {L.nx, L.ny, L.nz};
+        const double hi = h[c.i], li = lam[c.i], ki = kc[c.i];
+        double acc = 0.0;
+    #pragma unroll
+        for (int d = 0; d < 3; d++) {
+    #pragma unroll
+            for (int s = -1; s <= 1; s += 2) {
+                bool ok = s > 0 ? co[d] + 1 < nn[d] : co[d] > 0;
+                if (!ok) continue;
+                long long j = c.i + s * st3[d];
+                double dK = -P.aol[d] * (hi - h[j]) * (li - lam[j]);
+                double K = face_mean_k(ki, kc[j], kind);
+                acc += face_mean_dlogk(K, ki, kind) * dK;
+            }
         }
+        g[c.i] = acc;
     }
-    g[c.i] = acc;
 }
 
 // per-cell values for the face means: exp(logK / 2) (geometric) or exp(logK) (harmonic)
-__global__ void k_cell_k(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+__global__ void k_cell_k(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                          const double *__restrict__ logK, int kind, double *__restrict__ kc) {
-    int2 bm = bmap[blockIdx.x];
+    int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
-    Cell c;
-    if (!decode_cell(L, bm.y, c)) return;
-    double v = logK[c.i];
-    kc[c.i] = exp(kind == DPF_MEAN_GEOMETRIC ? 0.5 * v : v);
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        double v = logK[c.i];
+        kc[c.i] = exp(kind == DPF_MEAN_GEOMETRIC ? 0.5 * v : v);
+    }
 }
 
 // inverse diagonal of an FP64 level (the FP64 smoother multiplies instead of dividing)
-__global__ void k_invdiag(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, Coeffs<double> C,
+__global__ void k_invdiag(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, Coeffs<double> C,
                           double *__restrict__ idg) {
-    int2 bm = bmap[blockIdx.x];
+    int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
-    Cell c;
-    if (!decode_cell(L, bm.y, c)) return;
-    idg[c.i] = 1.0 / diag7(L, c, C);
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        idg[c.i] = 1.0 / diag7(L, c, C);
+    }
 }
 
 // ddirichleths_k = delta_k + sum over free neighbours j of K_f aol_f lambda_j (Dirichlet k);
 // 0 at free cells. dQs = lambda (0 at Dirichlet cells). Either output may be null.
-__global__ void k_grad_dh_q(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+__global__ void k_grad_dh_q(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                             const ProbParam *__restrict__ prm, FaceK fk, const uint8_t *__restrict__ dir,
                             const double *__restrict__ delta, const double *__restrict__ lam, double *ddh,
                             double *dQs, int accumulate) {
-    int2 bm = bmap[blockIdx.x];
+    int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
-    Cell c;
-    if (!decode_cell(L, bm.y, c)) return;
-    const ProbParam P = prm[bm.x];
-    const bool isd = dir[c.i];
-    if (dQs) {
-        double v = isd ? 0.0 : lam[c.i];
-        if (accumulate) dQs[c.i] += v; else dQs[c.i] = v;
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        const ProbParam P = prm[bm.x];
+        const bool isd = dir[c.i];
+        if (dQs) {
+            double v = isd ? 0.0 : lam[c.i];
+            if (accumulate) dQs[c.i] += v; else dQs[c.i] = v;
+        }
+        if (!ddh) continue;
+        double acc = 0.0;
+        if (isd) {
+            if (delta) acc = delta[c.i];
+            const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
+            const int co[3] = {c.ix, c.iy, c.iz};
+            const int nn[3] = {L.nx, L.ny, L.nz};
+            for (int d = 0; d < 3; d++)
+                for (int s = -1; s <= 1; s += 2) {
+                    bool ok = s > 0 ? co[d] + 1 < nn[d] : co[d] > 0;
+                    if (!ok) continue;
+                    long long j = c.i + s * st3[d];
+                    if (dir[j]) continue;
+                    acc += fk(L, P, c, d, s, j) * P.aol[d] * lam[j];
+                }
+        }
+        if (accumulate) ddh[c.i] += acc; else ddh[c.i] = acc;
     }
-    if (!ddh) return;
-    double acc = 0.0;
-    if (isd) {
-        if (delta) acc = delta[c.i];
+}
+
+// Ks in the reference face order from the per-cell values kc
+__global__ void k_logk_to_faces(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
+                                const ProbParam *__restrict__ prm, const double *__restrict__ kc, int kind,
+                                double *__restrict__ Ks) {
+    int4 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        const ProbParam P = prm[bm.x];
         const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
         const int co[3] = {c.ix, c.iy, c.iz};
         const int nn[3] = {L.nx, L.ny, L.nz};
+        for (int d = 0; d < 3; d++)
+            if (co[d] + 1 < nn[d])
+                Ks[P.face_off + regular_face_index(L.nx, L.ny, L.nz, c.ix, c.iy, c.iz, d)] =
+                    face_mean_k(kc[c.i], kc[c.i + st3[d]], kind);
+    }
+}
+
+// dlogK from dKs (gather over the six faces of each cell)
+__global__ void k_logk_vjp(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
+                           const ProbParam *__restrict__ prm, const double *__restrict__ kc, int kind,
+                           const double *__restrict__ dKs, double *__restrict__ g) {
+    int4 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        const ProbParam P = prm[bm.x];
+        const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
+        const int co[3] = {c.ix, c.iy, c.iz};
+        const int nn[3] = {L.nx, L.ny, L.nz};
+        const double ki = kc[c.i];
+        double acc = 0.0;
         for (int d = 0; d < 3; d++)
             for (int s = -1; s <= 1; s += 2) {
                 bool ok = s > 0 ? co[d] + 1 < nn[d] : co[d] > 0;
                 if (!ok) continue;
                 long long j = c.i + s * st3[d];
-                if (dir[j]) continue;
-                acc += fk(L, P, c, d, s, j) * P.aol[d] * lam[j];
+                int ax = c.ix, ay = c.iy, az = c.iz;
+                if (s < 0) { if (d == 0) ax--; else if (d == 1) ay--; else az--; }
+                long long f = P.face_off + regular_face_index(L.nx, L.ny, L.nz, ax, ay, az, d);
+                double K = face_mean_k(ki, kc[j], kind);
+                acc += face_mean_dlogk(K, ki, kind) * dKs[f];
             }
+        g[c.i] = acc;
     }
-    if (accumulate) ddh[c.i] += acc; else ddh[c.i] = acc;
-}
-
-// Ks in the reference face order from the per-cell values kc
-__global__ void k_logk_to_faces(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
-                                const ProbParam *__restrict__ prm, const double *__restrict__ kc, int kind,
-                                double *__restrict__ Ks) {
-    int2 bm = bmap[blockIdx.x];
-    const LevelDesc L = desc[bm.x];
-    Cell c;
-    if (!decode_cell(L, bm.y, c)) return;
-    const ProbParam P = prm[bm.x];
-    const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
-    const int co[3] = {c.ix, c.iy, c.iz};
-    const int nn[3] = {L.nx, L.ny, L.nz};
-    for (int d = 0; d < 3; d++)
-        if (co[d] + 1 < nn[d])
-            Ks[P.face_off + regular_face_index(L.nx, L.ny, L.nz, c.ix, c.iy, c.iz, d)] =
-                face_mean_k(kc[c.i], kc[c.i + st3[d]], kind);
-}
-
-// dlogK from dKs (gather over the six faces of each cell)
-__global__ void k_logk_vjp(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
-                           const ProbParam *__restrict__ prm, const double *__restrict__ kc, int kind,
-                           const double *__restrict__ dKs, double *__restrict__ g) {
-    int2 bm = bmap[blockIdx.x];
-    const LevelDesc L = desc[bm.x];
-    Cell c;
-    if (!decode_cell(L, bm.y, c)) return;
-    const ProbParam P = prm[bm.x];
-    const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
-    const int co[3] = {c.ix, c.iy, c.iz};
-    const int nn[3] = {L.nx, L.ny, L.nz};
-    const double ki = kc[c.i];
-    double acc = 0.0;
-    for (int d = 0; d < 3; d++)
-        for (int s = -1; s <= 1; s += 2) {
-            bool ok = s > 0 ? co[d] + 1 < nn[d] : co[d] > 0;
-            if (!ok) continue;
-            long long j = c.i + s * st3[d];
-            int ax = c.ix, ay = c.iy, az = c.iz;
-            if (s < 0) { if (d == 0) ax--; else if (d == 1) ay--; else az--; }
-            long long f = P.face_off + regular_face_index(L.nx, L.ny, L.nz, ax, ay, az, d);
-            double K = face_mean_k(ki, kc[j], kind);
-            acc += face_mean_dlogk(K, ki, kind) * dKs[f];
-        }
-    g[c.i] = acc;
 }
 
 // y = A x (FP64 fine operator; Dirichlet rows identity)
-__global__ void k_apply(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap, Coeffs<double> C,
+__global__ void k_apply(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, Coeffs<double> C,
                         const double *__restrict__ x, double *__restrict__ y) {
-    int2 bm = bmap[blockIdx.x];
+    int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
-    Cell c;
-    if (!decode_cell(L, bm.y, c)) return;
-    double Ax, dg;
-    apply7(L, c, C, x[c.i], [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
-    y[c.i] = Ax;
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        double Ax, dg;
+        apply7(L, c, C, x[c.i], [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
+        y[c.i] = Ax;
+    }
 }
 
 // ================================================================ host side
@@ -662,20 +714,30 @@ static void check_fast_div(unsigned d, unsigned m, int l, unsigned nmax) {
         if (q(n) != n / d) throw DpfError("invariant-integer division self-check failed", DPF_CUDA);
 }
 
+// Launch map over the problems marked in `take`. Kernels loop over their cells with a
+// stride of (blocks of the problem) x kBlock, so a problem's block count is chosen to
+// fill the GPU once: about `target` blocks in total (SMs x resident blocks per SM),
+// split in proportion to the problems' cells, never more than one cell per thread.
 static BlockMap build_map(const std::vector<LevelDesc> &desc, const std::vector<int> &take, std::vector<void *> &own,
-                          int nprob) {
+                         int nprob, long long target) {
     BlockMap m;
-    std::vector<int2> map, pinfo(nprob, make_int2(0, 0));
+    long long total = 0;
+    for (int p = 0; p < nprob; p++)
+        if (take[p]) total += desc[p].n;
+    std::vector<int4> map;
+    std::vector<int2> pinfo(nprob, make_int2(0, 0));
     for (int p = 0; p < nprob; p++) {
         if (!take[p]) continue;
-        int nb = (int)((desc[p].n + kBlock - 1) / kBlock);
+        long long full = (desc[p].n + kBlock - 1) / kBlock;
+        long long share = total > 0 ? (long long)((double)target * (double)desc[p].n / (double)total + 0.5) : 1;
+        int nb = (int)std::max(1LL, std::min(full, share));
         pinfo[p] = make_int2((int)map.size(), nb);
-        for (int b = 0; b < nb; b++) map.push_back(make_int2(p, b));
+        for (int b = 0; b < nb; b++) map.push_back(make_int4(p, b, nb, 0));
     }
     m.nblocks = (int)map.size();
-    m.d_map = dalloc<int2>(map.size(), own);
+    m.d_map = dalloc<int4>(map.size(), own);
     m.d_pinfo = dalloc<int2>(nprob, own);
-    if (!map.empty()) CK(cudaMemcpy(m.d_map, map.data(), map.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    if (!map.empty()) CK(cudaMemcpy(m.d_map, map.data(), map.size() * sizeof(int4), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(m.d_pinfo, pinfo.data(), nprob * sizeof(int2), cudaMemcpyHostToDevice));
     return m;
 }
@@ -707,6 +769,11 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         nlev[p] = (int)shapes[p].size();
         nlev_max = std::max(nlev_max, nlev[p]);
     }
+    // launch shape: grids sized to the resident capacity of the device
+    int dev = 0, sms = 152;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const long long target_blocks = (long long)sms * std::max(1, opt.blocks_per_sm);
     // level descriptors
     lv.resize(nlev_max);
     int maxblocks = 0;
@@ -737,8 +804,8 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         L.ntot = off;
         L.d_desc = dalloc<LevelDesc>(nprob, owned);
         CK(cudaMemcpy(L.d_desc, L.h_desc.data(), nprob * sizeof(LevelDesc), cudaMemcpyHostToDevice));
-        L.all = build_map(L.h_desc, has, owned, nprob);
-        L.smooth = build_map(L.h_desc, smooth, owned, nprob);
+        L.all = build_map(L.h_desc, has, owned, nprob, target_blocks);
+        L.smooth = build_map(L.h_desc, smooth, owned, nprob, target_blocks);
         for (int p = 0; p < nprob; p++) {
             if (has[p]) L.all_cells += L.h_desc[p].n;
             if (smooth[p]) L.smooth_cells += L.h_desc[p].n;

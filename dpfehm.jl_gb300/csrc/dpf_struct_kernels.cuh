@@ -18,16 +18,15 @@ struct Cell {
 
 __device__ __forceinline__ unsigned fast_div(unsigned n, unsigned m, int l) { return (__umulhi(n, m) + n) >> l; }
 
-__device__ __forceinline__ bool decode_cell(const LevelDesc &L, int lb, Cell &c) {
-    unsigned li = (unsigned)(lb * kBlock + (int)threadIdx.x);
-    if ((long long)li >= L.n) return false;
-    unsigned q = fast_div(li, L.mag_nz, L.sh_nz);
-    c.iz = (int)(li - q * (unsigned)L.nz);
+// Coordinates of the li-th cell of a grid (li < n), without integer division.
+__device__ __forceinline__ void cell_at(const LevelDesc &L, int li, Cell &c) {
+    unsigned u = (unsigned)li;
+    unsigned q = fast_div(u, L.mag_nz, L.sh_nz);
+    c.iz = (int)(u - q * (unsigned)L.nz);
     unsigned x = fast_div(q, L.mag_ny, L.sh_ny);
     c.iy = (int)(q - x * (unsigned)L.ny);
     c.ix = (int)x;
     c.i = L.off + li;
-    return true;
 }
 
 // Face index of the reference face list (regulargrid3d, src/grid.jl:163-185) of the
@@ -93,43 +92,49 @@ struct Acc<float> {
     __device__ __forceinline__ double to_double() const { return (double)v.hi + (double)v.lo; }
 };
 
-// Block-wide sum of two accumulators, converted to double; valid in thread 0.
+// Block-wide sum of NV (1 or 2) accumulators, converted to double; valid in thread 0.
 // Every thread of the block must call it.
-template <typename T>
-__device__ __forceinline__ double2 block_sum2(Acc<T> a, Acc<T> b) {
-    __shared__ Acc<T> sh[2][kBlock / 32];
-    __syncthreads();
+template <typename T, int NV>
+__device__ __forceinline__ double2 block_sum(Acc<T> a, Acc<T> b) {
+    __shared__ Acc<T> sh[NV][kBlock / 32];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) { a = a + a.shfl(o); b = b + b.shfl(o); }
+    for (int o = 16; o > 0; o >>= 1) {
+        a = a + a.shfl(o);
+        if (NV == 2) b = b + b.shfl(o);
+    }
     int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) { sh[0][w] = a; sh[1][w] = b; }
+    if (l == 0) {
+        sh[0][w] = a;
+        if (NV == 2) sh[NV - 1][w] = b;
+    }
     __syncthreads();
     double2 r = make_double2(0.0, 0.0);
     if (w == 0) {
         Acc<T> x, y;
-        if (l < (int)(blockDim.x >> 5)) { x = sh[0][l]; y = sh[1][l]; }
+        if (l < (int)(blockDim.x >> 5)) {
+            x = sh[0][l];
+            if (NV == 2) y = sh[NV - 1][l];
+        }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) { x = x + x.shfl(o); y = y + y.shfl(o); }
-        r = make_double2(x.to_double(), y.to_double());
+        for (int o = 16; o > 0; o >>= 1) {
+            x = x + x.shfl(o);
+            if (NV == 2) y = y + y.shfl(o);
+        }
+        r = make_double2(x.to_double(), NV == 2 ? y.to_double() : 0.0);
     }
     return r;
 }
 
-__device__ __forceinline__ double2 block_sum2d(double a, double b) {
-    Acc<double> x, y;
-    x.v = a;
-    y.v = b;
-    return block_sum2<double>(x, y);
-}
-
 // Write this block's partial; return true (in every thread) in the last block of
 // problem p to arrive, with the problem total in `tot`. Deterministic: the total is
-// always summed over the partial slots in the same order.
-template <typename T>
+// always summed over the partial slots in the same order. Each block reduces once
+// per launch (kernels loop over their cells), so this runs about once per resident
+// block rather than once per 256 cells.
+template <typename T, int NV = 1>
 __device__ __forceinline__ bool reduce_last(Acc<T> a, Acc<T> b, ReduceScratch rs, int2 pinfo, int p, double2 &tot) {
     __shared__ int amlast;
     __shared__ double2 total;
-    double2 s = block_sum2<T>(a, b);
+    double2 s = block_sum<T, NV>(a, b);
     if (threadIdx.x == 0) {
         rs.partials[blockIdx.x] = s;
         __threadfence();
@@ -139,13 +144,13 @@ __device__ __forceinline__ bool reduce_last(Acc<T> a, Acc<T> b, ReduceScratch rs
     __syncthreads();
     if (!amlast) return false;
     __threadfence();
-    double ax = 0.0, ay = 0.0;
+    Acc<double> ax, ay;
     for (int k = threadIdx.x; k < pinfo.y; k += blockDim.x) {
         double2 q = __ldcg(&rs.partials[pinfo.x + k]);
-        ax += q.x;
-        ay += q.y;
+        ax.v += q.x;
+        if (NV == 2) ay.v += q.y;
     }
-    double2 r = block_sum2d(ax, ay);
+    double2 r = block_sum<double, 2>(ax, ay);
     if (threadIdx.x == 0) {
         total = r;
         rs.tickets[p] = 0u;
@@ -235,50 +240,52 @@ struct FaceK {
 // Fine-level operator, right-hand side and initial guess (src/groundwater.jl:4-20 with
 // S = V = 1; storage shift for transient). Writes FP64 coefficients and, when fx != null,
 // FP32 copies.
-__global__ void k_assemble(const LevelDesc *__restrict__ desc, const int2 *__restrict__ bmap,
+__global__ void k_assemble(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                            const ProbParam *__restrict__ prm, FaceK fk, const double *__restrict__ dh,
                            const double *__restrict__ Qs, const double *__restrict__ shift,
                            const uint8_t *__restrict__ dir, double *cx, double *cy, double *cz, double *leak,
                            float *fx, float *fy, float *fz, float *fleak, double *b, double *x, int init_x) {
-    int2 bm = bmap[blockIdx.x];
+    int4 bm = bmap[blockIdx.x];
     LevelDesc L = desc[bm.x];
-    Cell c;
-    if (!decode_cell(L, bm.y, c)) return;
-    const ProbParam P = prm[bm.x];
-    const long long i = c.i;
-    const long long st[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
-    const int co[3] = {c.ix, c.iy, c.iz};
-    const int nn[3] = {L.nx, L.ny, L.nz};
-    bool fi = !dir[i];
-    double lk = 0.0, rhs = fi ? Qs[i] : dh[i];
-    double cp[3] = {0.0, 0.0, 0.0};
-    if (fi) {
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-            if (co[d] + 1 < nn[d]) {
-                long long j = i + st[d];
-                double cf = fk(L, P, c, d, +1, j) * P.aol[d];
-                if (!dir[j]) cp[d] = cf;
-                else { lk += cf; rhs += cf * dh[j]; }
-            }
-            if (co[d] > 0) {
-                long long j = i - st[d];
-                if (dir[j]) {
-                    double cf = fk(L, P, c, d, -1, j) * P.aol[d];
-                    lk += cf;
-                    rhs += cf * dh[j];
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        const ProbParam P = prm[bm.x];
+        const long long i = c.i;
+        const long long st[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
+        const int co[3] = {c.ix, c.iy, c.iz};
+        const int nn[3] = {L.nx, L.ny, L.nz};
+        bool fi = !dir[i];
+        double lk = 0.0, rhs = fi ? Qs[i] : dh[i];
+        double cp[3] = {0.0, 0.0, 0.0};
+        if (fi) {
+    #pragma unroll
+            for (int d = 0; d < 3; d++) {
+                if (co[d] + 1 < nn[d]) {
+                    long long j = i + st[d];
+                    double cf = fk(L, P, c, d, +1, j) * P.aol[d];
+                    if (!dir[j]) cp[d] = cf;
+                    else { lk += cf; rhs += cf * dh[j]; }
+                }
+                if (co[d] > 0) {
+                    long long j = i - st[d];
+                    if (dir[j]) {
+                        double cf = fk(L, P, c, d, -1, j) * P.aol[d];
+                        lk += cf;
+                        rhs += cf * dh[j];
+                    }
                 }
             }
+            if (shift) lk += shift[i];
+        } else {
+            lk = 1.0;
         }
-        if (shift) lk += shift[i];
-    } else {
-        lk = 1.0;
+        cx[i] = cp[0]; cy[i] = cp[1]; cz[i] = cp[2]; leak[i] = lk;
+        if (fx) { fx[i] = (float)cp[0]; fy[i] = (float)cp[1]; fz[i] = (float)cp[2]; fleak[i] = (float)lk; }
+        b[i] = rhs;
+        if (init_x) x[i] = fi ? 0.0 : dh[i];
+        else if (!fi) x[i] = dh[i];
     }
-    cx[i] = cp[0]; cy[i] = cp[1]; cz[i] = cp[2]; leak[i] = lk;
-    if (fx) { fx[i] = (float)cp[0]; fy[i] = (float)cp[1]; fz[i] = (float)cp[2]; fleak[i] = (float)lk; }
-    b[i] = rhs;
-    if (init_x) x[i] = fi ? 0.0 : dh[i];
-    else if (!fi) x[i] = dh[i];
 }
 
 // ----------------------------------------------------------- coarsening
@@ -287,34 +294,36 @@ __global__ void k_assemble(const LevelDesc *__restrict__ desc, const int2 *__res
 // cross it, a coarse leak is the sum of the free children's leaks. An aggregate
 // with no free child becomes an identity row.
 __global__ void k_coarsen(const LevelDesc *__restrict__ fdesc, const LevelDesc *__restrict__ cdesc,
-                          const int2 *__restrict__ bmap, const double *__restrict__ fcx,
+                          const int4 *__restrict__ bmap, const double *__restrict__ fcx,
                           const double *__restrict__ fcy, const double *__restrict__ fcz,
                           const double *__restrict__ fleak, const uint8_t *__restrict__ fdir, double *ccx,
                           double *ccy, double *ccz, double *cleak, uint8_t *cdir, float *gx, float *gy, float *gz,
                           float *gleak) {
-    int2 bm = bmap[blockIdx.x];
+    int4 bm = bmap[blockIdx.x];
     LevelDesc Lc = cdesc[bm.x];
-    Cell c;
-    if (!decode_cell(Lc, bm.y, c)) return;
-    LevelDesc Lf = fdesc[bm.x];
-    const long long fsy = Lf.nz, fsx = (long long)Lf.ny * Lf.nz;
-    int x0 = 2 * c.ix, y0 = 2 * c.iy, z0 = 2 * c.iz;
-    int x1 = min(x0 + 1, Lf.nx - 1), y1 = min(y0 + 1, Lf.ny - 1), z1 = min(z0 + 1, Lf.nz - 1);
-    double lk = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
-    bool anyfree = false;
-    for (int fx = x0; fx <= x1; fx++)
-        for (int fy = y0; fy <= y1; fy++)
-            for (int fz = z0; fz <= z1; fz++) {
-                long long j = Lf.off + fx * fsx + fy * fsy + fz;
-                if (!fdir[j]) { anyfree = true; lk += fleak[j]; }
-                if (fx == x0 + 1 && c.ix + 1 < Lc.nx) sx += fcx[j];
-                if (fy == y0 + 1 && c.iy + 1 < Lc.ny) sy += fcy[j];
-                if (fz == z0 + 1 && c.iz + 1 < Lc.nz) sz += fcz[j];
-            }
-    if (!anyfree) { lk = 1.0; sx = sy = sz = 0.0; }
-    const long long i = c.i;
-    ccx[i] = sx; ccy[i] = sy; ccz[i] = sz; cleak[i] = lk; cdir[i] = anyfree ? 0 : 1;
-    if (gx) { gx[i] = (float)sx; gy[i] = (float)sy; gz[i] = (float)sz; gleak[i] = (float)lk; }
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)Lc.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(Lc, li_, c);
+        LevelDesc Lf = fdesc[bm.x];
+        const long long fsy = Lf.nz, fsx = (long long)Lf.ny * Lf.nz;
+        int x0 = 2 * c.ix, y0 = 2 * c.iy, z0 = 2 * c.iz;
+        int x1 = min(x0 + 1, Lf.nx - 1), y1 = min(y0 + 1, Lf.ny - 1), z1 = min(z0 + 1, Lf.nz - 1);
+        double lk = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
+        bool anyfree = false;
+        for (int fx = x0; fx <= x1; fx++)
+            for (int fy = y0; fy <= y1; fy++)
+                for (int fz = z0; fz <= z1; fz++) {
+                    long long j = Lf.off + fx * fsx + fy * fsy + fz;
+                    if (!fdir[j]) { anyfree = true; lk += fleak[j]; }
+                    if (fx == x0 + 1 && c.ix + 1 < Lc.nx) sx += fcx[j];
+                    if (fy == y0 + 1 && c.iy + 1 < Lc.ny) sy += fcy[j];
+                    if (fz == z0 + 1 && c.iz + 1 < Lc.nz) sz += fcz[j];
+                }
+        if (!anyfree) { lk = 1.0; sx = sy = sz = 0.0; }
+        const long long i = c.i;
+        ccx[i] = sx; ccy[i] = sy; ccz[i] = sz; cleak[i] = lk; cdir[i] = anyfree ? 0 : 1;
+        if (gx) { gx[i] = (float)sx; gy[i] = (float)sy; gz[i] = (float)sz; gleak[i] = (float)lk; }
+    }
 }
 
 // ------------------------------------------------------ coarsest level

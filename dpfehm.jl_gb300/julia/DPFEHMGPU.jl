@@ -29,10 +29,11 @@ mutable struct Options
     max_outer::Cint
     use_graphs::Cint
     check_every::Cint
+    blocks_per_sm::Cint
 end
 
 function default_options(; reltol=nothing, maxiter=nothing, precision=nothing)
-    o = Options(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
+    o = Options(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
     ccall((:dpf_default_options, libdpf), Cvoid, (Ref{Options},), o)
     reltol === nothing || (o.reltol = reltol)
     maxiter === nothing || (o.maxiter = maxiter)

@@ -76,6 +76,7 @@ typedef struct dpf_options {
     int max_outer;       /* MIXED: cap on FP64 residual replacements per solve (default 60)   */
     int use_graphs;      /* capture each solve's iteration in a CUDA graph    (default 1)     */
     int check_every;     /* convergence is read back every this many iterations (default 1)   */
+    int blocks_per_sm;   /* launch shape: grids hold SMs x this many 256-thread blocks (default 16) */
 } dpf_options;
 
 typedef struct dpf_problem dpf_problem;
