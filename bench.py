@@ -43,14 +43,15 @@ BYTES_PER_CELL = {
     "k_cheb_step": lambda T: 9 * T,            # xin, b, d, cx, cy, cz, leak in; xout, d out
     "k_prolong_cheb": lambda T: 8 * T + T / 8 + 1,  # x, b, cx, cy, cz, leak, e/8, dir in; xout, d out
     "k_cheb_first": lambda T: 7 * T,           # b, cx, cy, cz, leak in; x, d out
+    "k_cheb_first2": lambda T: 8 * T,          # b, idg, cx, cy, cz, leak in; xout, d out
     "k_restrict": lambda T: 49 * T,            # per coarse cell: 8 fine cells x (x, b, 4 coeffs) + bc out
     "k_spmv_pq": lambda T: 6 * T,              # p, 4 coeffs in; q out
     "k_update_xr": lambda T: 6 * T,            # x, p, r, q in; x, r out
     "k_update_p": lambda T: 3 * T,             # z, p in; p out
     "k_cg_start": lambda T: 7 * T,             # x, b, 4 coeffs in; r out
-    "k_ir_residual": lambda T: 56,             # h, b, 4 FP64 coeffs in; r out
-    "k_ir_cast": lambda T: 16,                 # r64 in; r32, e out
-    "k_ir_update": lambda T: 20,               # h, e in; h out
+    "k_ru_residual": lambda T: 56,             # x64, b64, 4 FP64 coeffs in; r64 out
+    "k_ru_cast": lambda T: 20,                 # r64, p in; r32, p out
+    "k_ru_accum": lambda T: 24,                # x64, xs in; x64, xs out
     "k_grad_logk": lambda T: 32,               # logK, h, lambda in; g out
 }
 

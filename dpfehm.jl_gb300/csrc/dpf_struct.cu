@@ -51,6 +51,29 @@ __global__ void k_cheb_first(const LevelDesc *__restrict__ desc, const int4 *__r
     }
 }
 
+// The first two Chebyshev steps from a zero initial guess in one pass: the first
+// iterate is x1 = d0 = invtheta D^-1 b pointwise, so its value at a neighbour is formed
+// on the fly from b and the stored inverse diagonal; then
+// r1 = D^-1 (b - A x1), d1 = c1 d0 + c2 r1, xout = x1 + d1.
+template <typename T>
+__global__ void k_cheb_first2(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
+                              Coeffs<T> C, const T *__restrict__ b, T *__restrict__ xout, T *__restrict__ d,
+                              T invtheta, T c1, T c2) {
+    DPF_BLOCK_PROLOGUE(desc, bmap, st)
+    const T *__restrict__ g = C.idg;
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        const T bi = b[c.i], gi = g[c.i];
+        const T x1 = invtheta * bi * gi;
+        T Ax, dg;
+        apply7(L, c, C, x1, [&](long long j, int, int, int) { return invtheta * b[j] * g[j]; }, Ax, dg);
+        const T dn = c1 * x1 + c2 * (bi - Ax) * gi;
+        d[c.i] = dn;
+        xout[c.i] = x1 + dn;
+    }
+}
+
 // One Chebyshev step on D^-1 A: r = D^-1 (b - A xin); d = c1 d + c2 r; xout = xin + d.
 // With FUSE_RZ the kernel is the last of the level-0 V-cycle: it also reduces b . xout
 // (b is the CG residual, xout the preconditioned residual) and finalises beta.
@@ -388,9 +411,10 @@ __global__ void k_ru_residual(const LevelDesc *__restrict__ desc, const int4 *__
             s.outer++;
             // the recursion believed it had converged (estimate with the old scale) ...
             const bool apparent = s.rr * s.scale * s.scale <= tol2 * s.obb;
-            // ... but the true residual did not even halve since the last replacement:
-            // it sits at the FP64 rounding floor of b - A x, so no further accuracy exists
-            const bool floor = apparent && s.orr > 0.25 * s.orr_prev;
+            // ... after claiming at least a tenfold reduction since the last replacement,
+            // but the true residual did not even halve: it sits at the FP64 rounding
+            // floor of b - A x, so no further accuracy exists
+            const bool floor = apparent && s.rr <= 1e-2 && s.orr > 0.25 * s.orr_prev;
             s.orr_prev = s.orr;
             if (!isfinite(s.orr)) { s.status = DPF_NAN; s.ru_flag = 0; deactivate(s, active_count); }
             else if (s.orr <= tol2 * s.obb || floor) { s.ru_flag = 0; deactivate(s, active_count); }
@@ -571,15 +595,18 @@ __global__ void k_cell_k(const LevelDesc *__restrict__ desc, const int4 *__restr
     }
 }
 
-// inverse diagonal of an FP64 level (the FP64 smoother multiplies instead of dividing)
+// inverse diagonal of a level from its FP64 coefficients (the smoothers multiply
+// instead of dividing); written in FP64 and/or FP32
 __global__ void k_invdiag(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, Coeffs<double> C,
-                          double *__restrict__ idg) {
+                          double *__restrict__ idg, float *__restrict__ idg32) {
     int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
         Cell c;
         cell_at(L, li_, c);
-        idg[c.i] = 1.0 / diag7(L, c, C);
+        double v = 1.0 / diag7(L, c, C);
+        if (idg) idg[c.i] = v;
+        if (idg32) idg32[c.i] = (float)v;
     }
 }
 
@@ -822,6 +849,7 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         L.c64[2] = dalloc<double>(n, owned); L.c64[3] = dalloc<double>(n, owned);
         if (mixed) {
             for (int k = 0; k < 4; k++) L.c32[k] = dalloc<float>(n, owned);
+            L.idg32 = dalloc<float>(n, owned);
         } else {
             L.idg64 = dalloc<double>(n, owned);
         }
@@ -991,7 +1019,7 @@ Coeffs<double> coeffs_of<double>(StructBatch::Level &L, bool) {
 }
 template <>
 Coeffs<float> coeffs_of<float>(StructBatch::Level &L, bool) {
-    return Coeffs<float>{L.c32[0], L.c32[1], L.c32[2], L.c32[3], nullptr};
+    return Coeffs<float>{L.c32[0], L.c32[1], L.c32[2], L.c32[3], L.idg32};
 }
 
 void StructBatch::assemble(const double *Ks, const double *kc, int kind, const double *shift, bool init_x) {
@@ -1029,17 +1057,15 @@ void StructBatch::assemble(const double *Ks, const double *kc, int kind, const d
         }
         LAUNCH_CHECK();
     }
-    if (!mixed) {
-        for (int l = 0; l < nlev_max; l++) {
-            Level &L = lv[l];
-            if (!nb_of(L.all)) continue;
-            {
-                KTimer _kt(this, kname("k_invdiag", l, false), L.all_cells);
-                k_invdiag<<<nb_of(L.all), kBlock, 0, stream>>>(L.d_desc, L.all.d_map, coeffs_of<double>(L, false),
-                                                               L.idg64);
-            }
-            LAUNCH_CHECK();
+    for (int l = 0; l < nlev_max; l++) {
+        Level &L = lv[l];
+        if (!nb_of(L.all)) continue;
+        {
+            KTimer _kt(this, kname("k_invdiag", l, false), L.all_cells);
+            k_invdiag<<<nb_of(L.all), kBlock, 0, stream>>>(L.d_desc, L.all.d_map, coeffs_of<double>(L, false),
+                                                           mixed ? nullptr : L.idg64, mixed ? L.idg32 : nullptr);
         }
+        LAUNCH_CHECK();
     }
     have_operator = true;
 }
@@ -1057,14 +1083,29 @@ void StructBatch::vcycle(const T *r, T *z) {
         const T *b = l == 0 ? r : (const T *)L.work[2];
         T *xa = (T *)L.work[0], *xb = (T *)L.work[1], *d = (T *)L.work[3];
         if (nb_of(L.smooth)) {
-            {
-                KTimer _kt(this, kname("k_cheb_first", l, sizeof(T) == 4), L.smooth_cells);
-                k_cheb_first<T><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, L.smooth.d_map, d_state, C, b, xa, d,
-                                                                        invth);
-            }
-            LAUNCH_CHECK();
             T *cur = xa, *oth = xb;
-            for (int k = 1; k < deg; k++) {
+            int k0 = 1;
+            if (deg >= 2) {
+                // steps 0 and 1 fused; the iterate lands where step 1 would leave it (xb)
+                {
+                    KTimer _kt(this, kname("k_cheb_first2", l, sizeof(T) == 4), L.smooth_cells);
+                    k_cheb_first2<T><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, L.smooth.d_map, d_state, C, b,
+                                                                             xb, d, invth, (T)cheb_c1[1],
+                                                                             (T)cheb_c2[1]);
+                }
+                LAUNCH_CHECK();
+                cur = xb;
+                oth = xa;
+                k0 = 2;
+            } else {
+                {
+                    KTimer _kt(this, kname("k_cheb_first", l, sizeof(T) == 4), L.smooth_cells);
+                    k_cheb_first<T><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, L.smooth.d_map, d_state, C, b,
+                                                                            xa, d, invth);
+                }
+                LAUNCH_CHECK();
+            }
+            for (int k = k0; k < deg; k++) {
                 {
                     KTimer _kt(this, kname("k_cheb_step", l, sizeof(T) == 4), L.smooth_cells);
                     k_cheb_step<T, false><<<nb_of(L.smooth), kBlock, 0, stream>>>(

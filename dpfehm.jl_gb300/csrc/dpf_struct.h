@@ -66,6 +66,7 @@ public:
         double *c64[4] = {nullptr, nullptr, nullptr, nullptr};  // cx, cy, cz, leak
         double *idg64 = nullptr;       // inverse diagonal (FP64 solves)
         float *c32[4] = {nullptr, nullptr, nullptr, nullptr};
+        float *idg32 = nullptr;        // inverse diagonal (FP32 V-cycle)
         void *work[4] = {nullptr, nullptr, nullptr, nullptr};   // xa, xb, b, d (V-cycle precision)
     };
 
