@@ -27,7 +27,6 @@ class Options(ctypes.Structure):
         ("cheb_lo", ctypes.c_double),
         ("coarse_scale", ctypes.c_double),
         ("max_coarse", ctypes.c_int),
-        ("inner_tol", ctypes.c_double),
         ("max_outer", ctypes.c_int),
         ("use_graphs", ctypes.c_int),
         ("check_every", ctypes.c_int),

@@ -185,7 +185,6 @@ dpf_options fill_options(const dpf_options *o) {
     if (!(r.cheb_lo > 0 && r.cheb_lo < 1)) r.cheb_lo = d.cheb_lo;
     if (!(r.coarse_scale > 0)) r.coarse_scale = d.coarse_scale;
     if (r.max_coarse <= 0) r.max_coarse = d.max_coarse;
-    if (!(r.inner_tol > 0)) r.inner_tol = d.inner_tol;
     if (r.max_outer <= 0) r.max_outer = d.max_outer;
     if (r.check_every <= 0) r.check_every = d.check_every;
     if (r.blocks_per_sm <= 0) r.blocks_per_sm = d.blocks_per_sm;
@@ -229,8 +228,7 @@ void dpf_default_options(dpf_options *o) {
     o->cheb_lo = 0.2;
     o->coarse_scale = 2.0;
     o->max_coarse = 64;
-    o->inner_tol = 5e-2;
-    o->max_outer = 60;
+    o->max_outer = 6;
     o->use_graphs = 1;
     o->check_every = 1;
     o->blocks_per_sm = 16;

@@ -57,7 +57,7 @@ struct CgState {
     double orr, obb;               // mixed precision: true (FP64) residual and rhs norms squared
     double orr_prev;               // mixed precision: true residual norm squared at the previous replacement
     int iters, active, status, outer;  // outer: reliable updates so far
-    int ru_flag, total_iters, pad1, pad2;
+    int ru_flag, total_iters, stall, pad2;  // stall: consecutive replacements without progress
 };
 
 // Reduction scratch: one double2 partial per block of the widest launch, one

@@ -286,14 +286,11 @@ __global__ void k_spmv_pq(const LevelDesc *__restrict__ desc, const int4 *__rest
     }
 }
 
-// x += alpha p; r -= alpha q; convergence test on r . r. With RU (mixed precision) the
-// residual is normalised: the problem is flagged for a reliable update instead of
-// being declared converged, which only the true FP64 residual can decide.
-template <typename T, bool RU>
+// x += alpha p; r -= alpha q; convergence test on r . r.
+template <typename T>
 __global__ void k_update_xr(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                             int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, T *__restrict__ x,
-                            T *__restrict__ r, const T *__restrict__ pv, const T *__restrict__ q, int maxiter,
-                            int *upd_count, double delta2) {
+                            T *__restrict__ r, const T *__restrict__ pv, const T *__restrict__ q, int maxiter) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     const double alpha = st[p].alpha;
     Acc<T> part;
@@ -313,12 +310,7 @@ __global__ void k_update_xr(const LevelDesc *__restrict__ desc, const int4 *__re
         s.iters++;
         s.total_iters++;
         if (!isfinite(s.rr)) { s.status = DPF_NAN; deactivate(s, active_count); }
-        else if (RU) {
-            if (s.rr <= delta2 || s.rr * s.scale * s.scale <= s.tol2 * s.obb || s.iters >= maxiter) {
-                s.ru_flag = 1;
-                atomicAdd(upd_count, 1);
-            }
-        } else if (s.rr <= s.tol2 * s.bb) deactivate(s, active_count);
+        else if (s.rr <= s.tol2 * s.bb) deactivate(s, active_count);
         else if (s.iters >= maxiter) { s.status = DPF_NOT_CONVERGED; deactivate(s, active_count); }
     }
 }
@@ -336,40 +328,140 @@ __global__ void k_update_p(const LevelDesc *__restrict__ desc, const int4 *__res
     }
 }
 
-// ------------------------------------- mixed precision: reliable-update CG
-// The CG recurrence runs in FP32 on a residual normalised by `scale`; the solution
-// is accumulated in FP64. When the recursive residual has dropped by a factor delta
-// (or looks converged, or the iteration cap is hit) the problem is flagged, and the
-// flagged problems replace their FP32 residual by the true FP64 residual b - A x
-// without restarting the Krylov recurrence (the search direction is rescaled to the
-// new normalisation). Convergence is decided on the true FP64 residual only.
+// ----------------------------------- mixed precision: double-float CG recurrence
+// The CG recurrence (iterate, residual, search direction, SpMV with the finest-level
+// operator) runs on double-float numbers: an unevaluated sum hi + lo of two floats
+// (about 48 significant bits) handled with FP32 arithmetic only (GB300's FP32 rate is
+// many times its FP64 rate). The V-cycle preconditioner runs in plain FP32 on the
+// rounded residual. FP32 storage alone is not enough here: with few Dirichlet cells
+// the operator is nearly singular and the search directions are dominated by a
+// smooth near-null mode whose small variations FP32 cannot resolve, so an FP32
+// recurrence stagnates; 48 bits resolve them like FP64 does.
+// Each solve round starts from the true FP64 residual (normalised by its norm) and
+// ends by adding the correction to the FP64 solution; convergence is then confirmed
+// on the true FP64 residual, and another round runs if it is not met.
 
-// x64 += scale * xs; xs = 0   (flagged problems)
-__global__ void k_ru_accum(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, const CgState *st,
-                           double *__restrict__ x64, float *__restrict__ xs) {
-    int4 bm = bmap[blockIdx.x];
-    const int p = bm.x;
-    if (!st[p].ru_flag) return;
-    const LevelDesc L = desc[p];
-    const double sc = st[p].scale;
+__device__ __forceinline__ float2 df_two_sum(float a, float b) {
+    float s = a + b;
+    float bb = s - a;
+    return make_float2(s, (a - (s - bb)) + (b - bb));
+}
+__device__ __forceinline__ float2 df_quick(float a, float b) {
+    float s = a + b;
+    return make_float2(s, b - (s - a));
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    float2 s = df_two_sum(a.x, b.x);
+    s.y += a.y + b.y;
+    return df_quick(s.x, s.y);
+}
+__device__ __forceinline__ float2 df_sub(float2 a, float2 b) { return df_add(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+    float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    return df_quick(p, e);
+}
+__device__ __forceinline__ float2 df_from_double(double v) {
+    float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+}
+__device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + (double)a.y; }
+
+struct CoeffsDF {
+    const float2 *cx, *cy, *cz, *leak;
+};
+
+// q = A p in double-float (flux form); alpha = rz / (p . q) (hi parts: q is accurate, so
+// its leading float is too)
+__global__ void k_df_spmv_pq(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
+                             int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, CoeffsDF C,
+                             const float2 *__restrict__ pv, float2 *__restrict__ q) {
+    DPF_BLOCK_PROLOGUE(desc, bmap, st)
+    Acc<float> part;
+    const long long sy = L.nz, sx = (long long)L.ny * L.nz;
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
         Cell c;
         cell_at(L, li_, c);
-        x64[c.i] += sc * (double)xs[c.i];
-        xs[c.i] = 0.0f;
+        const long long i = c.i;
+        const float2 pi = pv[i];
+        float2 a = df_mul(C.leak[i], pi);
+        if (c.iz + 1 < L.nz) a = df_add(a, df_mul(C.cz[i], df_sub(pi, pv[i + 1])));
+        if (c.iz > 0) a = df_add(a, df_mul(C.cz[i - 1], df_sub(pi, pv[i - 1])));
+        if (c.iy + 1 < L.ny) a = df_add(a, df_mul(C.cy[i], df_sub(pi, pv[i + sy])));
+        if (c.iy > 0) a = df_add(a, df_mul(C.cy[i - sy], df_sub(pi, pv[i - sy])));
+        if (c.ix + 1 < L.nx) a = df_add(a, df_mul(C.cx[i], df_sub(pi, pv[i + sx])));
+        if (c.ix > 0) a = df_add(a, df_mul(C.cx[i - sx], df_sub(pi, pv[i - sx])));
+        q[i] = a;
+        part = part + Acc<float>::prod(pi.x, a.x);
+    }
+    double2 tot;
+    if (reduce_last<float>(part, Acc<float>(), rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+        CgState &s = st[p];
+        s.pq = tot.x;
+        if (!isfinite(s.pq)) { s.alpha = 0.0; s.status = DPF_NAN; deactivate(s, active_count); }
+        else if (!(s.pq > 0.0)) { s.alpha = 0.0; deactivate(s, active_count); }
+        else s.alpha = s.rz / s.pq;
     }
 }
 
-// r64 = b - A x64 in FP64 flux form. START: every problem, sets up the state.
-// Otherwise flagged problems only: converged -> inactive, else new normalisation.
-template <bool START>
-__global__ void k_ru_residual(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
+// x += alpha p; r -= alpha q (double-float); r32 = leading float of r for the V-cycle;
+// convergence test on the recursive residual (r is normalised by `scale`)
+__global__ void k_df_update_xr(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
+                               int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo,
+                               float2 *__restrict__ x, float2 *__restrict__ r, float *__restrict__ r32,
+                               const float2 *__restrict__ pv, const float2 *__restrict__ q, int maxiter) {
+    DPF_BLOCK_PROLOGUE(desc, bmap, st)
+    const float2 a = df_from_double(st[p].alpha);
+    Acc<float> part;
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        const long long i = c.i;
+        x[i] = df_add(x[i], df_mul(a, pv[i]));
+        const float2 ri = df_sub(r[i], df_mul(a, q[i]));
+        r[i] = ri;
+        r32[i] = ri.x;
+        part = part + Acc<float>::prod(ri.x, ri.x);
+    }
+    double2 tot;
+    if (reduce_last<float>(part, Acc<float>(), rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+        CgState &s = st[p];
+        s.rr = tot.x;
+        s.iters++;
+        s.total_iters++;
+        if (!isfinite(s.rr)) { s.status = DPF_NAN; deactivate(s, active_count); }
+        else if (s.rr * s.scale * s.scale <= s.tol2 * s.obb) deactivate(s, active_count);
+        else if (s.total_iters >= maxiter) { s.status = DPF_NOT_CONVERGED; deactivate(s, active_count); }
+    }
+}
+
+// p = z + beta p (double-float; z is the FP32 preconditioned residual)
+__global__ void k_df_update_p(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
+                              const float *__restrict__ z, float2 *__restrict__ pv) {
+    DPF_BLOCK_PROLOGUE(desc, bmap, st)
+    const double beta = st[p].beta;
+    const float2 b = df_from_double(beta);
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        const long long i = c.i;
+        const float2 zi = make_float2(z[i], 0.0f);
+        pv[i] = beta == 0.0 ? zi : df_add(zi, df_mul(b, pv[i]));
+    }
+}
+
+// True residual r64 = b - A x64 in FP64 flux form; decides whether a (further) round is
+// needed. FIRST: the start of a solve.
+template <bool FIRST>
+__global__ void k_df_residual(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                               int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo,
                               Coeffs<double> C, const double *__restrict__ b, const double *__restrict__ x,
-                              double *__restrict__ r, double tol2, int maxiter, int max_updates) {
+                              double *__restrict__ r, double tol2, int maxiter, int max_rounds) {
     int4 bm = bmap[blockIdx.x];
     const int p = bm.x;
-    if (!START && !st[p].ru_flag) return;
+    if (!FIRST && st[p].ru_flag == 0) return;  // finished in an earlier round
     const LevelDesc L = desc[p];
     Acc<double> rr, bb;
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -381,86 +473,90 @@ __global__ void k_ru_residual(const LevelDesc *__restrict__ desc, const int4 *__
         double ri = bi - Ax;
         r[c.i] = ri;
         rr.v += ri * ri;
-        if (START) bb.v += bi * bi;
+        if (FIRST) bb.v += bi * bi;
     }
     double2 tot;
-    if (reduce_last<double, START ? 2 : 1>(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+    if (reduce_last<double, FIRST ? 2 : 1>(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
         CgState &s = st[p];
         s.orr = tot.x;
-        if (START) {
+        bool go;
+        if (FIRST) {
             s.obb = tot.y;
             s.tol2 = tol2;
             s.status = DPF_OK;
-            s.iters = 0;
             s.total_iters = 0;
             s.outer = 0;
-            s.rz = 0.0;
-            s.rz_old = 0.0;
-            s.beta = 0.0;
-            s.ratio = 1.0;
-            s.orr_prev = s.orr;
-            bool act = s.obb > 0.0 && s.orr > tol2 * s.obb;
-            if (!isfinite(s.orr)) { s.status = DPF_NAN; act = false; }
-            s.active = act ? 1 : 0;
-            s.ru_flag = act ? 1 : 0;
-            if (act) {
-                s.scale = sqrt(s.orr);
-                atomicAdd(active_count, 1);
-            }
+            s.stall = 0;
+            go = s.obb > 0.0 && s.orr > tol2 * s.obb;
+            if (!isfinite(s.orr)) { s.status = DPF_NAN; go = false; }
         } else {
             s.outer++;
-            // the recursion believed it had converged (estimate with the old scale) ...
-            const bool apparent = s.rr * s.scale * s.scale <= tol2 * s.obb;
-            // ... after claiming at least a tenfold reduction since the last replacement,
-            // but the true residual did not even halve: it sits at the FP64 rounding
-            // floor of b - A x, so no further accuracy exists
-            const bool floor = apparent && s.rr <= 1e-2 && s.orr > 0.25 * s.orr_prev;
-            s.orr_prev = s.orr;
-            if (!isfinite(s.orr)) { s.status = DPF_NAN; s.ru_flag = 0; deactivate(s, active_count); }
-            else if (s.orr <= tol2 * s.obb || floor) { s.ru_flag = 0; deactivate(s, active_count); }
-            else if (s.iters >= maxiter || s.outer >= max_updates) {
-                s.status = DPF_NOT_CONVERGED;
-                s.ru_flag = 0;
-                deactivate(s, active_count);
-            } else {
-                double sn = sqrt(s.orr);
-                s.ratio = s.scale / sn;
-                s.scale = sn;
-                s.rz *= s.ratio * s.ratio;  // (r, z) of the next beta in the new normalisation
-            }
+            // a round that did not even halve the true residual means it sits at the FP64
+            // rounding floor of b - A x (no further accuracy exists): accept it
+            const bool stalled = s.orr > 0.25 * s.orr_prev;
+            go = true;
+            if (!isfinite(s.orr)) { s.status = DPF_NAN; go = false; }
+            else if (s.orr <= tol2 * s.obb || stalled) go = false;
+            else if (s.total_iters >= maxiter || s.outer >= max_rounds) { s.status = DPF_NOT_CONVERGED; go = false; }
+        }
+        s.orr_prev = s.orr;
+        s.ru_flag = go ? 1 : 0;  // problem takes part in the next round
+        s.active = go ? 1 : 0;
+        s.iters = 0;
+        s.rz = 0.0;
+        s.rz_old = 0.0;
+        s.beta = 0.0;
+        if (go) {
+            s.scale = sqrt(s.orr);
+            atomicAdd(active_count, 1);
         }
     }
 }
 
-// r32 = r64 / scale; START: xs = 0; otherwise p *= ratio   (flagged problems)
-__global__ void k_ru_cast(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, const CgState *st,
-                          const double *__restrict__ r64, float *__restrict__ r32, float *__restrict__ pv,
-                          float *__restrict__ xs, int start) {
+// start of a round: r = r64 / scale (double-float and its leading float), x = 0
+__global__ void k_df_begin(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, const CgState *st,
+                           const double *__restrict__ r64, float2 *__restrict__ r, float *__restrict__ r32,
+                           float2 *__restrict__ x) {
     int4 bm = bmap[blockIdx.x];
     const int p = bm.x;
     if (!st[p].ru_flag) return;
     const LevelDesc L = desc[p];
     const double inv = 1.0 / st[p].scale;
-    const float ratio = (float)st[p].ratio;
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
-        Cell c;
-        cell_at(L, li_, c);
-        r32[c.i] = (float)(r64[c.i] * inv);
-        if (start) xs[c.i] = 0.0f;
-        else pv[c.i] *= ratio;
+        const long long i = L.off + li_;
+        const float2 v = df_from_double(r64[i] * inv);
+        r[i] = v;
+        r32[i] = v.x;
+        x[i] = make_float2(0.0f, 0.0f);
     }
 }
 
-__global__ void k_ru_clear(CgState *st, int nprob, int *upd_count) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < nprob) st[p].ru_flag = 0;
-    if (p == 0) *upd_count = 0;
+// end of a round: x64 += scale * x
+__global__ void k_df_end(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, const CgState *st,
+                         const float2 *__restrict__ x, double *__restrict__ x64) {
+    int4 bm = bmap[blockIdx.x];
+    const int p = bm.x;
+    if (!st[p].ru_flag) return;
+    const LevelDesc L = desc[p];
+    const double sc = st[p].scale;
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        const long long i = L.off + li_;
+        x64[i] += sc * df_to_double(x[i]);
+    }
 }
 
-__global__ void k_if_cond(cudaGraphConditionalHandle h, const int *upd_count, int *taken) {
-    bool go = *upd_count > 0;
-    if (go) (*taken)++;
-    cudaGraphSetConditional(h, go ? 1u : 0u);
+// double-float copy of the finest FP64 operator
+__global__ void k_df_coeffs(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, Coeffs<double> C,
+                            float2 *cx, float2 *cy, float2 *cz, float2 *leak) {
+    int4 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        const long long i = L.off + li_;
+        cx[i] = df_from_double(C.cx[i]);
+        cy[i] = df_from_double(C.cy[i]);
+        cz[i] = df_from_double(C.cz[i]);
+        leak[i] = df_from_double(C.leak[i]);
+    }
 }
 
 // ------------------------------------------------------------ misc vector kernels
@@ -910,8 +1006,13 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
     in_kc = dalloc<double>(N, owned);
     aux_kc = dalloc<double>(N, owned);
     in_Ks = dalloc<double>(F, owned);
-    size_t vs = mixed ? sizeof(float) : sizeof(double);
-    for (int k = 0; k < 5; k++) cgv[k] = dalloc<char>(N * vs, owned);
+    if (!mixed) {
+        for (int k = 0; k < 4; k++) cgv[k] = dalloc<double>(N, owned);  // r, z, p, q
+    } else {
+        for (int k = 0; k < 2; k++) cgv[k] = dalloc<float>(N, owned);   // r32, z32
+        for (int k = 0; k < 4; k++) dfv[k] = dalloc<float2>(N, owned);  // x, r, p, q (double-float)
+        for (int k = 0; k < 4; k++) cdf[k] = dalloc<float2>(N, owned);  // finest operator (double-float)
+    }
     // state, reductions, coarse factors
     d_state = dalloc<CgState>(nprob, owned);
     d_count = dalloc<int>(4, owned);
@@ -1002,7 +1103,6 @@ StructBatch::~StructBatch() {
         cudaGraphDestroy(kv.second.graph);
     }
     if (cap_stream) cudaStreamDestroy(cap_stream);
-    if (cap_stream2) cudaStreamDestroy(cap_stream2);
     for (void *p : owned) cudaFree(p);
     if (h_count) cudaFreeHost(h_count);
     if (h_state_buf) cudaFreeHost(h_state_buf);
@@ -1064,6 +1164,14 @@ void StructBatch::assemble(const double *Ks, const double *kc, int kind, const d
             KTimer _kt(this, kname("k_invdiag", l, false), L.all_cells);
             k_invdiag<<<nb_of(L.all), kBlock, 0, stream>>>(L.d_desc, L.all.d_map, coeffs_of<double>(L, false),
                                                            mixed ? nullptr : L.idg64, mixed ? L.idg32 : nullptr);
+        }
+        LAUNCH_CHECK();
+    }
+    if (mixed) {
+        {
+            KTimer _kt(this, kname("k_df_coeffs", 0, false), L0.all_cells);
+            k_df_coeffs<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, coeffs_of<double>(L0, true),
+                                                             cdf[0], cdf[1], cdf[2], cdf[3]);
         }
         LAUNCH_CHECK();
     }
@@ -1205,18 +1313,14 @@ int StructBatch::read_count(int which) {
     return h_count[which];
 }
 
-// ---- preconditioned CG on all active problems: A x = b (vectors of type T)
-// One PCG iteration: q = A p, alpha; x, r update and convergence test; z = M r, beta; p
-// update. Mixed precision (ru): x is the FP32 partial solution and flagged problems get
-// a reliable update (FP64 true residual) between the x/r update and the V-cycle; inside
-// a graph that update sits in a conditional IF node taken only when a problem is flagged.
+// One PCG iteration (FP64 mode): q = A p, alpha; x, r update and convergence test;
+// z = M r, beta; p update.
 template <typename T>
-void StructBatch::pcg_iteration(T *x, const double *b64, double *x64, bool capturing) {
+void StructBatch::pcg_iteration(T *x) {
     Level &L0 = lv[0];
     Coeffs<T> C = coeffs_of<T>(L0, mixed);
     T *r = (T *)cgv[0], *z = (T *)cgv[1], *pv = (T *)cgv[2], *q = (T *)cgv[3];
     const unsigned nb = nb_of(L0.all);
-    const bool ru = b64 != nullptr;
     {
         KTimer _kt(this, kname("k_spmv_pq", 0, sizeof(T) == 4), L0.all_cells);
         k_spmv_pq<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C,
@@ -1225,51 +1329,10 @@ void StructBatch::pcg_iteration(T *x, const double *b64, double *x64, bool captu
     LAUNCH_CHECK();
     {
         KTimer _kt(this, kname("k_update_xr", 0, sizeof(T) == 4), L0.all_cells);
-        if (ru)
-            k_update_xr<T, true><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs,
-                                                            L0.all.d_pinfo, x, r, pv, q, opt.maxiter, d_count + 3,
-                                                            opt.inner_tol * opt.inner_tol);
-        else
-            k_update_xr<T, false><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs,
-                                                             L0.all.d_pinfo, x, r, pv, q, opt.maxiter, nullptr, 0.0);
+        k_update_xr<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, x, r,
+                                                  pv, q, opt.maxiter);
     }
     LAUNCH_CHECK();
-    if (ru) {
-        if (!capturing) {
-            ru_update(b64, x64, false);
-        } else {
-            // conditional IF node: reliable update only when some problem is flagged
-            {
-                KTimer _kt(this, kname("k_if_cond", 0, false), 0);
-                k_if_cond<<<1, 1, 0, stream>>>(if_handle, d_count + 3, d_count + 1);
-            }
-            LAUNCH_CHECK();
-            cudaStreamCaptureStatus cs;
-            cudaGraph_t capg;
-            const cudaGraphNode_t *deps;
-            const cudaGraphEdgeData *edata;
-            size_t ndeps;
-            CK(cudaStreamGetCaptureInfo(stream, &cs, nullptr, &capg, &deps, &edata, &ndeps));
-            cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
-            cp.conditional.handle = if_handle;
-            cp.conditional.type = cudaGraphCondTypeIf;
-            cp.conditional.size = 1;
-            cudaGraphNode_t ifnode;
-            CK(cudaGraphAddNode(&ifnode, capg, deps, edata, ndeps, &cp));
-            CK(cudaStreamUpdateCaptureDependencies(stream, &ifnode, nullptr, 1, cudaStreamSetCaptureDependencies));
-            cudaGraph_t ifbody = cp.conditional.phGraph_out[0];
-            if (!cap_stream2) CK(cudaStreamCreateWithFlags(&cap_stream2, cudaStreamNonBlocking));
-            cudaStream_t saved = stream;
-            stream = cap_stream2;
-            CK(cudaStreamBeginCaptureToGraph(stream, ifbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-            long long l0 = launches;
-            ru_update(b64, x64, false);
-            if_body_kernels = launches - l0;
-            launches = l0;
-            CK(cudaStreamEndCapture(stream, &ifbody));
-            stream = saved;
-        }
-    }
     vcycle<T>(r, z);
     {
         KTimer _kt(this, kname("k_update_p", 0, sizeof(T) == 4), L0.all_cells);
@@ -1278,39 +1341,29 @@ void StructBatch::pcg_iteration(T *x, const double *b64, double *x64, bool captu
     LAUNCH_CHECK();
 }
 
-// reliable update of the flagged problems (or, with start, the initial residual of all)
-void StructBatch::ru_update(const double *b64, double *x64, bool start) {
+// One iteration of the mixed-precision CG: double-float q = A p, alpha, x/r update,
+// FP32 V-cycle on the rounded residual, double-float p update.
+void StructBatch::df_iteration() {
     Level &L0 = lv[0];
     const unsigned nb = nb_of(L0.all);
-    float *xs = (float *)ir_e(), *r32 = (float *)cgv[0], *pv = (float *)cgv[2];
-    const double tol2 = ru_tol2;
-    if (!start) {
-        {
-            KTimer _kt(this, kname("k_ru_accum", 0, false), L0.all_cells);
-            k_ru_accum<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, x64, xs);
-        }
-        LAUNCH_CHECK();
-        {
-            KTimer _kt(this, kname("k_ru_residual", 0, false), L0.all_cells);
-            k_ru_residual<false><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs,
-                                                            L0.all.d_pinfo, coeffs_of<double>(L0, true), b64, x64,
-                                                            r64, tol2, opt.maxiter, opt.max_outer);
-        }
-    } else {
-        KTimer _kt(this, kname("k_ru_residual", 0, false), L0.all_cells);
-        k_ru_residual<true><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs,
-                                                       L0.all.d_pinfo, coeffs_of<double>(L0, true), b64, x64, r64,
-                                                       tol2, opt.maxiter, opt.max_outer);
+    float *r32 = (float *)cgv[0], *z32 = (float *)cgv[1];
+    CoeffsDF C{cdf[0], cdf[1], cdf[2], cdf[3]};
+    {
+        KTimer _kt(this, kname("k_df_spmv_pq", 0, true), L0.all_cells);
+        k_df_spmv_pq<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C,
+                                                dfv[2], dfv[3]);
     }
     LAUNCH_CHECK();
     {
-        KTimer _kt(this, kname("k_ru_cast", 0, false), L0.all_cells);
-        k_ru_cast<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, r64, r32, pv, xs, start ? 1 : 0);
+        KTimer _kt(this, kname("k_df_update_xr", 0, true), L0.all_cells);
+        k_df_update_xr<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo,
+                                                  dfv[0], dfv[1], r32, dfv[2], dfv[3], opt.maxiter);
     }
     LAUNCH_CHECK();
+    vcycle<float>(r32, z32);
     {
-        KTimer _kt(this, kname("k_ru_clear", 0, false), 0);
-        k_ru_clear<<<(nprob + 127) / 128, 128, 0, stream>>>(d_state, nprob, d_count + 3);
+        KTimer _kt(this, kname("k_df_update_p", 0, true), L0.all_cells);
+        k_df_update_p<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z32, dfv[2]);
     }
     LAUNCH_CHECK();
 }
@@ -1321,11 +1374,10 @@ __global__ void k_loop_cond(cudaGraphConditionalHandle h, const int *count, int 
     cudaGraphSetConditional(h, (*count > 0 && it < maxiter + 2) ? 1u : 0u);
 }
 
-// The whole CG loop as one graph: a conditional WHILE node whose body is one PCG
-// iteration followed by k_loop_cond. Built once per (vector type, buffers).
-template <typename T>
-cudaGraphExec_t StructBatch::loop_graph(T *x, const double *b64, double *x64) {
-    GraphKey key{(int)sizeof(T), (const void *)x, (const void *)b64, (const void *)x64};
+// The CG loop as one graph: a conditional WHILE node whose body is one iteration followed
+// by k_loop_cond. Built once per (kind, iterate buffer); kind 0: FP64 CG, 1: mixed.
+cudaGraphExec_t StructBatch::loop_graph(int kind, void *x) {
+    GraphKey key{kind, x};
     auto it = graphs.find(key);
     if (it != graphs.end()) return it->second.exec;
     if (!cap_stream) CK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
@@ -1340,10 +1392,8 @@ cudaGraphExec_t StructBatch::loop_graph(T *x, const double *b64, double *x64) {
     cudaGraphNode_t node;
     CK(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
-    if (b64) CK(cudaGraphConditionalHandleCreate(&if_handle, body, 0, 0));
     cudaStream_t saved = stream;
     long long l0 = launches;
-    if_body_kernels = 0;
     stream = cap_stream;
     cudaError_t ce = cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (ce != cudaSuccess) {
@@ -1352,7 +1402,8 @@ cudaGraphExec_t StructBatch::loop_graph(T *x, const double *b64, double *x64) {
         ck(ce, "cudaStreamBeginCaptureToGraph");
     }
     try {
-        pcg_iteration<T>(x, b64, x64, true);
+        if (kind == 0) pcg_iteration<double>((double *)x);
+        else df_iteration();
         k_loop_cond<<<1, 1, 0, stream>>>(cond, d_count, d_count + 2, opt.maxiter);
         launches++;
         LAUNCH_CHECK();
@@ -1368,42 +1419,39 @@ cudaGraphExec_t StructBatch::loop_graph(T *x, const double *b64, double *x64) {
     GraphRec rec;
     rec.graph = g;
     rec.body_kernels = launches - l0;
-    rec.if_kernels = if_body_kernels;
     launches = l0;
     CK(cudaGraphInstantiate(&rec.exec, g, 0));
     graphs[key] = rec;
     return rec.exec;
 }
 
-template <typename T>
-void StructBatch::run_loop(T *x, const double *b64, double *x64) {
+void StructBatch::run_loop(int kind, void *x) {
     if (opt.use_graphs && !prof_on) {
-        cudaGraphExec_t ex = loop_graph<T>(x, b64, x64);
+        cudaGraphExec_t ex = loop_graph(kind, x);
         CK(cudaGraphLaunch(ex, stream));
-        // account the graph's kernel launches: body kernels times passes, plus the
-        // reliable-update kernels each time the IF node was taken
+        // account the graph's kernel launches: body kernels times passes
         CK(cudaMemcpyAsync(h_count, d_count, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));
-        GraphKey key{(int)sizeof(T), (const void *)x, (const void *)b64, (const void *)x64};
-        launches += graphs[key].body_kernels * (long long)h_count[2] + graphs[key].if_kernels * (long long)h_count[1];
+        launches += graphs[GraphKey{kind, x}].body_kernels * (long long)h_count[2];
         return;
     }
     const int check = std::max(1, opt.check_every);
     for (int it = 1; it <= opt.maxiter + 1; it++) {
-        pcg_iteration<T>(x, b64, x64, false);
+        if (kind == 0) pcg_iteration<double>((double *)x);
+        else df_iteration();
         if (it % check == 0 && read_count(0) <= 0) return;
     }
     read_count(0);
 }
 
-// ---- preconditioned CG on all problems: A x = b (vectors of type T)
+// ---- FP64 preconditioned CG on all problems: A x = b
 template <typename T>
 void StructBatch::pcg(const T *b, T *x, double tol2) {
     Level &L0 = lv[0];
     Coeffs<T> C = coeffs_of<T>(L0, mixed);
     T *r = (T *)cgv[0], *z = (T *)cgv[1], *pv = (T *)cgv[2];
     const unsigned nb = nb_of(L0.all);
-    CK(cudaMemsetAsync(d_count, 0, 4 * sizeof(int), stream));  // active problems, IF taken, loop passes, flagged
+    CK(cudaMemsetAsync(d_count, 0, 4 * sizeof(int), stream));  // active problems, -, loop passes, -
     {
         KTimer _kt(this, kname("k_cg_start", 0, sizeof(T) == 4), L0.all_cells);
         k_cg_start<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C, b, x,
@@ -1416,24 +1464,50 @@ void StructBatch::pcg(const T *b, T *x, double tol2) {
         k_update_p<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z, pv);
     }
     LAUNCH_CHECK();
-    run_loop<T>(x, nullptr, nullptr);
+    run_loop(0, (void *)x);
 }
 
-// ---- mixed precision: reliable-update CG with FP32 vectors/V-cycle, FP64 solution x64
-void StructBatch::ru_pcg(const double *b64, double *x64, double tol2) {
+// ---- mixed precision: rounds of double-float CG with the FP32 V-cycle, each started
+// from and checked against the true FP64 residual b64 - A x64
+void StructBatch::df_pcg(const double *b64, double *x64, double tol2) {
     Level &L0 = lv[0];
     const unsigned nb = nb_of(L0.all);
-    float *xs = (float *)ir_e(), *r32 = (float *)cgv[0], *z = (float *)cgv[1], *pv = (float *)cgv[2];
-    ru_tol2 = tol2;
+    float *r32 = (float *)cgv[0], *z32 = (float *)cgv[1];
     CK(cudaMemsetAsync(d_count, 0, 4 * sizeof(int), stream));
-    ru_update(b64, x64, true);
-    vcycle<float>(r32, z);
     {
-        KTimer _kt(this, kname("k_update_p", 0, true), L0.all_cells);
-        k_update_p<float><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z, pv);
+        KTimer _kt(this, kname("k_df_residual", 0, false), L0.all_cells);
+        k_df_residual<true><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo,
+                                                       coeffs_of<double>(L0, true), b64, x64, r64, tol2,
+                                                       opt.maxiter, opt.max_outer);
     }
     LAUNCH_CHECK();
-    run_loop<float>(xs, b64, x64);
+    for (int round = 0; round < opt.max_outer && read_count(0) > 0; round++) {
+        {
+            KTimer _kt(this, kname("k_df_begin", 0, false), L0.all_cells);
+            k_df_begin<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, r64, dfv[1], r32, dfv[0]);
+        }
+        LAUNCH_CHECK();
+        vcycle<float>(r32, z32);
+        {
+            KTimer _kt(this, kname("k_df_update_p", 0, true), L0.all_cells);
+            k_df_update_p<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z32, dfv[2]);
+        }
+        LAUNCH_CHECK();
+        run_loop(1, nullptr);
+        {
+            KTimer _kt(this, kname("k_df_end", 0, false), L0.all_cells);
+            k_df_end<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, dfv[0], x64);
+        }
+        LAUNCH_CHECK();
+        CK(cudaMemsetAsync(d_count, 0, sizeof(int), stream));
+        {
+            KTimer _kt(this, kname("k_df_residual", 0, false), L0.all_cells);
+            k_df_residual<false><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs,
+                                                            L0.all.d_pinfo, coeffs_of<double>(L0, true), b64, x64,
+                                                            r64, tol2, opt.maxiter, opt.max_outer);
+        }
+        LAUNCH_CHECK();
+    }
 }
 
 // ---- full solve of A x = b for every problem (x holds the initial guess)
@@ -1448,7 +1522,7 @@ void StructBatch::solve(const double *b, double *x, double reltol) {
         pcg<double>(b, x, tol2);
         stats_outer = 0;
     } else {
-        ru_pcg(b, x, tol2);
+        df_pcg(b, x, tol2);
     }
     // statistics
     CK(cudaMemcpyAsync(h_state_buf, d_state, nprob * sizeof(CgState), cudaMemcpyDeviceToHost, stream));
@@ -1476,10 +1550,6 @@ void StructBatch::solve(const double *b, double *x, double reltol) {
     }
 }
 
-void *StructBatch::ir_e() {
-    if (!ir_e_buf) ir_e_buf = dalloc<float>((size_t)N, owned);
-    return ir_e_buf;
-}
 
 // ---- public operations
 void StructBatch::forward(const double *Ks, const double *logK, int kind) {
@@ -1610,6 +1680,5 @@ void StructBatch::transient_step(const double *b0, const double *hprev) {
 template void StructBatch::vcycle<double>(const double *, double *);
 template void StructBatch::vcycle<float>(const float *, float *);
 template void StructBatch::pcg<double>(const double *, double *, double);
-template void StructBatch::pcg<float>(const float *, float *, double);
 
 }  // namespace dpf

@@ -96,16 +96,13 @@ public:
     void vcycle(const T *r, T *z);
     template <typename T>
     void pcg(const T *b, T *x, double tol2);
-    void ru_pcg(const double *b64, double *x64, double tol2);
-    void ru_update(const double *b64, double *x64, bool start);
+    void df_pcg(const double *b64, double *x64, double tol2);
     template <typename T>
-    void pcg_iteration(T *x, const double *b64, double *x64, bool capturing);
-    template <typename T>
-    cudaGraphExec_t loop_graph(T *x, const double *b64, double *x64);
-    template <typename T>
-    void run_loop(T *x, const double *b64, double *x64);
+    void pcg_iteration(T *x);
+    void df_iteration();
+    cudaGraphExec_t loop_graph(int kind, void *x);
+    void run_loop(int kind, void *x);
     int read_count(int which);
-    void *ir_e();
 
     // configuration and sizes
     dpf_options opt;
@@ -124,12 +121,13 @@ public:
     double *h = nullptr, *b64 = nullptr, *r64 = nullptr, *lam = nullptr, *delta = nullptr, *arhs = nullptr;
     double *in_dh = nullptr, *in_Q = nullptr, *in_logK = nullptr, *in_Ks = nullptr, *shift = nullptr;
     double *in_kc = nullptr, *aux_kc = nullptr;  // per-cell face-mean values of the forward / standalone calls
-    void *cgv[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // r, z, p, q, r32 (CG precision)
-    float *ir_e_buf = nullptr;
+    void *cgv[4] = {nullptr, nullptr, nullptr, nullptr};  // FP64: r, z, p, q; mixed: r32, z32
+    float2 *dfv[4] = {nullptr, nullptr, nullptr, nullptr};  // mixed: x, r, p, q in double-float
+    float2 *cdf[4] = {nullptr, nullptr, nullptr, nullptr};  // mixed: finest cx, cy, cz, leak in double-float
 
     // device state
     CgState *d_state = nullptr;
-    int *d_count = nullptr;       // [0] active CG problems, [1] reliable-update passes, [2] loop passes, [3] flagged
+    int *d_count = nullptr;       // [0] active CG problems, [2] loop passes
     int *d_factor_status = nullptr;
     ReduceScratch rs;
     double *d_coarseL = nullptr;
@@ -139,24 +137,14 @@ public:
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         long long body_kernels = 0;
-        long long if_kernels = 0;
     };
     struct GraphKey {
-        int vsize;
-        const void *x, *b64, *x64;
-        bool operator<(const GraphKey &o) const {
-            if (vsize != o.vsize) return vsize < o.vsize;
-            if (x != o.x) return x < o.x;
-            if (b64 != o.b64) return b64 < o.b64;
-            return x64 < o.x64;
-        }
+        int kind;
+        void *x;
+        bool operator<(const GraphKey &o) const { return kind != o.kind ? kind < o.kind : x < o.x; }
     };
     std::map<GraphKey, GraphRec> graphs;  // CG loop graphs per (vector size, buffers)
     cudaStream_t cap_stream = nullptr;    // streams used only to capture graphs
-    cudaStream_t cap_stream2 = nullptr;
-    cudaGraphConditionalHandle if_handle = 0;
-    long long if_body_kernels = 0;
-    double ru_tol2 = 0.0;
 
     // Chebyshev
     double inv_theta = 1.0;

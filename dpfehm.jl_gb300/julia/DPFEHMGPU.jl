@@ -25,7 +25,6 @@ mutable struct Options
     cheb_lo::Cdouble
     coarse_scale::Cdouble
     max_coarse::Cint
-    inner_tol::Cdouble
     max_outer::Cint
     use_graphs::Cint
     check_every::Cint
@@ -33,7 +32,7 @@ mutable struct Options
 end
 
 function default_options(; reltol=nothing, maxiter=nothing, precision=nothing)
-    o = Options(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
+    o = Options(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
     ccall((:dpf_default_options, libdpf), Cvoid, (Ref{Options},), o)
     reltol === nothing || (o.reltol = reltol)
     maxiter === nothing || (o.maxiter = maxiter)

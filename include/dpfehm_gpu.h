@@ -60,8 +60,9 @@ typedef enum { DPF_MEAN_GEOMETRIC = 0, DPF_MEAN_HARMONIC = 1 } dpf_mean_kind;
 
 typedef enum {
     DPF_PREC_FP64 = 0,  /* FP64 CG with an FP64 V-cycle */
-    DPF_PREC_MIXED = 1  /* FP32 CG recurrence and V-cycle; FP64 solution, FP64 true residual replaced into the
-                           recurrence every inner_tol of reduction (reliable updates); FP64 CG scalars */
+    DPF_PREC_MIXED = 1  /* FP32 V-cycle; CG recurrence and finest-level SpMV in double-float (pairs of
+                           floats, FP32 arithmetic); FP64 solution, FP64 true residual check per round,
+                           FP64 CG scalars */
 } dpf_precision;
 
 typedef struct dpf_options {
@@ -72,8 +73,7 @@ typedef struct dpf_options {
     double cheb_lo;      /* lower end of the Chebyshev interval / upper end   (default 0.2)   */
     double coarse_scale; /* scaling of the coarse-grid correction              (default 2.0)   */
     int max_coarse;      /* coarsen until a level has at most this many cells (default 64, <= 64) */
-    double inner_tol;    /* MIXED: residual reduction between FP64 residual replacements (default 5e-2) */
-    int max_outer;       /* MIXED: cap on FP64 residual replacements per solve (default 60)   */
+    int max_outer;       /* MIXED: cap on rounds, each restarted from the true FP64 residual (default 6) */
     int use_graphs;      /* capture each solve's iteration in a CUDA graph    (default 1)     */
     int check_every;     /* convergence is read back every this many iterations (default 1)   */
     int blocks_per_sm;   /* launch shape: grids hold SMs x this many 256-thread blocks (default 16) */
