@@ -24,6 +24,7 @@ namespace dpf {
 
 constexpr int kBlock = 256;        // threads per block of every cell-parallel kernel
 constexpr int kMaxCoarse = 64;     // largest dense coarsest level (cells)
+constexpr int kMinBlocks = 6;      // resident blocks per SM the CG stencils are compiled for
 
 struct LevelDesc {                 // one problem at one level
     int nx, ny, nz, pad;

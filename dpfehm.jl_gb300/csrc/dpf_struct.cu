@@ -56,7 +56,7 @@ __global__ void k_cheb_first(const LevelDesc *__restrict__ desc, const int4 *__r
 // on the fly from b and the stored inverse diagonal; then
 // r1 = D^-1 (b - A x1), d1 = c1 d0 + c2 r1, xout = x1 + d1.
 template <typename T>
-__global__ void k_cheb_first2(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
+__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 8 : 5) k_cheb_first2(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                               Coeffs<T> C, const T *__restrict__ b, T *__restrict__ xout, T *__restrict__ d,
                               T invtheta, T c1, T c2) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
@@ -75,12 +75,14 @@ __global__ void k_cheb_first2(const LevelDesc *__restrict__ desc, const int4 *__
 }
 
 // One Chebyshev step on D^-1 A: r = D^-1 (b - A xin); d = c1 d + c2 r; xout = xin + d.
+// FIRST: the first step from a nonzero iterate, d = c2 r (d is not read).
 // With FUSE_RZ the kernel is the last of the level-0 V-cycle: it also reduces b . xout
 // (b is the CG residual, xout the preconditioned residual) and finalises beta.
-template <typename T, bool FUSE_RZ>
-__global__ void k_cheb_step(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
-                            Coeffs<T> C, const T *__restrict__ b, const T *__restrict__ xin, T *__restrict__ xout,
-                            T *__restrict__ d, T c1, T c2, ReduceScratch rs, const int2 *__restrict__ pinfo) {
+template <typename T, bool FUSE_RZ, bool FIRST = false>
+__global__ void __launch_bounds__(kBlock, (sizeof(T) == 4 && !FUSE_RZ) ? 8 : 6)
+k_cheb_step(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st, Coeffs<T> C,
+            const T *__restrict__ b, const T *__restrict__ xin, T *__restrict__ xout, T *__restrict__ d, T c1, T c2,
+            ReduceScratch rs, const int2 *__restrict__ pinfo) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     Acc<T> part;
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -90,7 +92,7 @@ __global__ void k_cheb_step(const LevelDesc *__restrict__ desc, const int4 *__re
         apply7(L, c, C, xi, [&](long long j, int, int, int) { return xin[j]; }, Ax, dg);
         T bi = b[c.i];
         T r = dinv_times(C, c.i, bi - Ax, dg);
-        T dn = c1 * d[c.i] + c2 * r;
+        T dn = FIRST ? c2 * r : c1 * d[c.i] + c2 * r;
         T xo = xi + dn;
         d[c.i] = dn;
         xout[c.i] = xo;
@@ -109,7 +111,7 @@ __global__ void k_cheb_step(const LevelDesc *__restrict__ desc, const int4 *__re
 
 // Restriction of the residual: bc[I] = sum over the children i of I of (b_i - (A x)_i).
 template <typename T>
-__global__ void k_restrict(const LevelDesc *__restrict__ fdesc, const LevelDesc *__restrict__ cdesc,
+__global__ void __launch_bounds__(kBlock, 5) k_restrict(const LevelDesc *__restrict__ fdesc, const LevelDesc *__restrict__ cdesc,
                            const int4 *__restrict__ bmap, CgState *st, Coeffs<T> C, const T *__restrict__ b,
                            const T *__restrict__ x, T *__restrict__ bc) {
     int4 bm = bmap[blockIdx.x];
@@ -138,50 +140,20 @@ __global__ void k_restrict(const LevelDesc *__restrict__ fdesc, const LevelDesc 
     }
 }
 
-// Prolongation of the coarse correction fused with the first post-smoothing step:
-// x' = x + s * e[aggregate] (not at identity rows), r = D^-1 (b - A x'),
-// d = invtheta r, xout = x' + d.
-template <typename T, bool FUSE_RZ>
-__global__ void k_prolong_cheb(const LevelDesc *__restrict__ desc, const LevelDesc *__restrict__ cdesc,
-                               const int4 *__restrict__ bmap, CgState *st, Coeffs<T> C,
-                               const uint8_t *__restrict__ dir, const T *__restrict__ b, const T *__restrict__ x,
-                               const T *__restrict__ e, T *__restrict__ xout, T *__restrict__ d, T scale,
-                               T invtheta, ReduceScratch rs, const int2 *__restrict__ pinfo) {
+// Prolongation of the coarse correction, in place: x += s * e[aggregate] (not at
+// identity rows). Pointwise, so it streams at bandwidth; the first post-smoothing step
+// then runs as a plain Chebyshev step on the corrected iterate.
+template <typename T>
+__global__ void k_prolong_add(const LevelDesc *__restrict__ desc, const LevelDesc *__restrict__ cdesc,
+              const int4 *__restrict__ bmap, CgState *st, const uint8_t *__restrict__ dir, T *__restrict__ x,
+              const T *__restrict__ e, T scale) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     const LevelDesc Lc = cdesc[p];
-    Acc<T> part;
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
         Cell c;
         cell_at(L, li_, c);
-        // aggregate of this cell; a neighbour's aggregate differs by at most one coarse
-        // cell in the direction of the neighbour
-        const int X = c.ix >> 1, Y = c.iy >> 1, Z = c.iz >> 1;
-        const long long csy = Lc.nz, csx = (long long)Lc.ny * Lc.nz;
-        const long long base = Lc.off + X * csx + Y * csy + Z;
-        // Dirichlet (identity) rows have no couplings, so only the centre needs the mask:
-        // a neighbour's value is multiplied by a zero coupling when the neighbour is one
-        auto xp = [&](long long j, int jx, int jy, int jz) -> T {
-            return x[j] + scale * e[base + ((jx >> 1) - X) * csx + ((jy >> 1) - Y) * csy + ((jz >> 1) - Z)];
-        };
-        T xi = x[c.i];
-        if (!dir[c.i]) xi += scale * e[base];
-        T Ax, dg;
-        apply7(L, c, C, xi, xp, Ax, dg);
-        T bi = b[c.i];
-        T dn = invtheta * dinv_times(C, c.i, bi - Ax, dg);
-        T xo = xi + dn;
-        d[c.i] = dn;
-        xout[c.i] = xo;
-        if (FUSE_RZ) part = part + Acc<T>::prod(bi, xo);
-    }
-    if (FUSE_RZ) {
-        double2 tot;
-        if (reduce_last<T>(part, Acc<T>(), rs, pinfo[p], p, tot) && threadIdx.x == 0) {
-            CgState &s = st[p];
-            s.rz_old = s.rz;
-            s.rz = tot.x;
-            s.beta = (s.iters == 0 || s.rz_old == 0.0) ? 0.0 : s.rz / s.rz_old;
-        }
+        if (dir[c.i]) continue;
+        x[c.i] += scale * e[Lc.off + ((long long)(c.ix >> 1) * Lc.ny + (c.iy >> 1)) * Lc.nz + (c.iz >> 1)];
     }
 }
 
@@ -263,7 +235,7 @@ __global__ void k_cg_start(const LevelDesc *__restrict__ desc, const int4 *__res
 
 // q = A p; alpha = rz / (p . q)
 template <typename T>
-__global__ void k_spmv_pq(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_spmv_pq(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                           int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, Coeffs<T> C,
                           const T *__restrict__ pv, T *__restrict__ q) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
@@ -375,7 +347,7 @@ struct CoeffsDF {
 
 // q = A p in double-float (flux form); alpha = rz / (p . q) (hi parts: q is accurate, so
 // its leading float is too)
-__global__ void k_df_spmv_pq(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_df_spmv_pq(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                              int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, CoeffsDF C,
                              const float2 *__restrict__ pv, float2 *__restrict__ q) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
@@ -1251,9 +1223,10 @@ void StructBatch::vcycle(const T *r, T *z) {
             LAUNCH_CHECK();
         }
     }
-    // ascend: deg post-smoothing kernels alternate buffers starting from pre[l];
-    // cheb_first + (deg-1) steps + prolong + (deg-1) steps = 2 deg kernels, so the
-    // final post-smoothed iterate always lands in work[1].
+    // ascend: the coarse correction is added in place to the pre-smoothed iterate, then
+    // deg Chebyshev steps alternate buffers. Pre-smoothing wrote deg iterates starting in
+    // work[0] and post-smoothing writes deg more, so the final iterate always lands in
+    // work[1] (or z on the finest level).
     for (int l = nlev_max - 2; l >= 0; l--) {
         Level &L = lv[l];
         if (!nb_of(L.smooth)) continue;
@@ -1262,47 +1235,37 @@ void StructBatch::vcycle(const T *r, T *z) {
         const T *b = l == 0 ? r : (const T *)L.work[2];
         T *xa = (T *)L.work[0], *xb = (T *)L.work[1], *d = (T *)L.work[3];
         T *cur = pre[l];
-        T *oth = cur == xa ? xb : xa;
         const T *e = (const T *)Cn.work[1];
-        bool last_is_prolong = deg == 1;
-        T *out = (l == 0 && last_is_prolong) ? z : oth;
-        if (l == 0 && last_is_prolong)
-            {
-                KTimer _kt(this, kname("k_prolong_cheb", l, sizeof(T) == 4), L.smooth_cells);
-                k_prolong_cheb<T, true><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, Cn.d_desc, L.smooth.d_map,
-                                                                                d_state, C, L.dir, b, cur, e, out, d,
-                                                                                sc, invth, rs, L.smooth.d_pinfo);
-            }
-        else
-            {
-                KTimer _kt(this, kname("k_prolong_cheb", l, sizeof(T) == 4), L.smooth_cells);
-                k_prolong_cheb<T, false><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, Cn.d_desc, L.smooth.d_map,
-                                                                                 d_state, C, L.dir, b, cur, e, out, d,
-                                                                                 sc, invth, rs, L.smooth.d_pinfo);
-            }
+        {
+            KTimer _kt(this, kname("k_prolong_add", l, sizeof(T) == 4), L.smooth_cells);
+            k_prolong_add<T><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, Cn.d_desc, L.smooth.d_map, d_state,
+                                                                     L.dir, cur, e, sc);
+        }
         LAUNCH_CHECK();
-        cur = out;
-        oth = cur == xa ? xb : xa;
-        for (int k = 1; k < deg; k++) {
-            bool last = k == deg - 1;
-            T *o = (l == 0 && last) ? z : oth;
-            if (l == 0 && last)
-                {
-                    KTimer _kt(this, kname("k_cheb_step", l, sizeof(T) == 4), L.smooth_cells);
-                    k_cheb_step<T, true><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, L.smooth.d_map, d_state, C,
-                                                                                 b, cur, o, d, (T)cheb_c1[k],
-                                                                                 (T)cheb_c2[k], rs, L.smooth.d_pinfo);
+        for (int k = 0; k < deg; k++) {
+            const bool last = k == deg - 1;
+            T *o = (l == 0 && last) ? z : (cur == xa ? xb : xa);
+            const T c1 = (T)cheb_c1[k], c2 = k == 0 ? invth : (T)cheb_c2[k];
+            {
+                KTimer _kt(this, kname("k_cheb_step", l, sizeof(T) == 4), L.smooth_cells);
+                if (l == 0 && last) {
+                    if (k == 0)
+                        k_cheb_step<T, true, true><<<nb_of(L.smooth), kBlock, 0, stream>>>(
+                            L.d_desc, L.smooth.d_map, d_state, C, b, cur, o, d, c1, c2, rs, L.smooth.d_pinfo);
+                    else
+                        k_cheb_step<T, true, false><<<nb_of(L.smooth), kBlock, 0, stream>>>(
+                            L.d_desc, L.smooth.d_map, d_state, C, b, cur, o, d, c1, c2, rs, L.smooth.d_pinfo);
+                } else {
+                    if (k == 0)
+                        k_cheb_step<T, false, true><<<nb_of(L.smooth), kBlock, 0, stream>>>(
+                            L.d_desc, L.smooth.d_map, d_state, C, b, cur, o, d, c1, c2, rs, L.smooth.d_pinfo);
+                    else
+                        k_cheb_step<T, false, false><<<nb_of(L.smooth), kBlock, 0, stream>>>(
+                            L.d_desc, L.smooth.d_map, d_state, C, b, cur, o, d, c1, c2, rs, L.smooth.d_pinfo);
                 }
-            else
-                {
-                    KTimer _kt(this, kname("k_cheb_step", l, sizeof(T) == 4), L.smooth_cells);
-                    k_cheb_step<T, false><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, L.smooth.d_map, d_state, C,
-                                                                                  b, cur, o, d, (T)cheb_c1[k],
-                                                                                  (T)cheb_c2[k], rs, L.smooth.d_pinfo);
-                }
+            }
             LAUNCH_CHECK();
             cur = o;
-            oth = cur == xa ? xb : xa;
         }
     }
 }
