@@ -139,6 +139,11 @@ int guarded(dpf_problem *P, F &&f) {
     }
 }
 
+int gs_status(dpf_problem *P, int rc) {
+    if (rc != DPF_OK) P->err = P->gs->last_message.empty() ? "general-topology solve failed" : P->gs->last_message;
+    return rc;
+}
+
 int solver_status(dpf_problem *P, StructBatch &S) {
     if (S.last_status != DPF_OK) {
         P->err = S.last_message.empty() ? (S.last_status == DPF_NOT_CONVERGED ? "CG did not converge within maxiter"
@@ -422,7 +427,7 @@ int dpf_last_stats(const dpf_problem *P, int *iterations, int *outer, double *re
 int dpf_steady_forward(dpf_problem *P, const double *Ks, const double *dh, const double *Qs, double *h_out) {
     return guarded(P, [&]() -> int {
         if (!Ks || !dh || !Qs) throw BadInput("Ks, dirichleths and Qs are required");
-        if (P->gs) return P->gs->forward(Ks, nullptr, 0, dh, Qs, h_out);
+        if (P->gs) return gs_status(P, P->gs->forward(Ks, nullptr, 0, dh, Qs, h_out));
         StructBatch &S = *P->sb;
         stage_in(P, Ks, S.F, S.in_Ks);
         stage_in(P, dh, S.N, S.in_dh);
@@ -438,7 +443,7 @@ int dpf_steady_forward_logk(dpf_problem *P, const double *logK, int kind, const 
     return guarded(P, [&]() -> int {
         if (!logK || !dh || !Qs) throw BadInput("logK, dirichleths and Qs are required");
         if (kind != DPF_MEAN_GEOMETRIC && kind != DPF_MEAN_HARMONIC) throw BadInput("unknown mean kind");
-        if (P->gs) return P->gs->forward(nullptr, logK, kind, dh, Qs, h_out);
+        if (P->gs) return gs_status(P, P->gs->forward(nullptr, logK, kind, dh, Qs, h_out));
         StructBatch &S = *P->sb;
         stage_in(P, logK, S.N, S.in_logK);
         stage_in(P, dh, S.N, S.in_dh);
@@ -452,7 +457,7 @@ int dpf_steady_forward_logk(dpf_problem *P, const double *logK, int kind, const 
 int dpf_steady_adjoint(dpf_problem *P, const double *delta, double *dKs, double *ddh, double *dQs) {
     return guarded(P, [&]() -> int {
         if (!delta) throw BadInput("delta is required");
-        if (P->gs) return P->gs->adjoint(delta, dKs, nullptr, ddh, dQs);
+        if (P->gs) return gs_status(P, P->gs->adjoint(delta, dKs, nullptr, ddh, dQs));
         StructBatch &S = *P->sb;
         if (!S.have_forward) { P->err = "adjoint called before a forward solve"; return DPF_STATE; }
         stage_in(P, delta, S.N, S.delta);
@@ -480,7 +485,7 @@ int dpf_steady_adjoint(dpf_problem *P, const double *delta, double *dKs, double 
 int dpf_steady_adjoint_logk(dpf_problem *P, const double *delta, double *dlogK, double *ddh, double *dQs) {
     return guarded(P, [&]() -> int {
         if (!delta) throw BadInput("delta is required");
-        if (P->gs) return P->gs->adjoint(delta, nullptr, dlogK, ddh, dQs);
+        if (P->gs) return gs_status(P, P->gs->adjoint(delta, nullptr, dlogK, ddh, dQs));
         StructBatch &S = *P->sb;
         if (!S.have_forward || S.fwd_kind != 1) {
             P->err = "dpf_steady_adjoint_logk needs a preceding dpf_steady_forward_logk";
@@ -512,7 +517,7 @@ int dpf_logk_to_faces(dpf_problem *P, const double *logK, int kind, double *Ks) 
     return guarded(P, [&]() -> int {
         if (!logK || !Ks) throw BadInput("logK and Ks are required");
         if (kind != DPF_MEAN_GEOMETRIC && kind != DPF_MEAN_HARMONIC) throw BadInput("unknown mean kind");
-        if (P->gs) return P->gs->logk_to_faces(logK, kind, Ks);
+        if (P->gs) return gs_status(P, P->gs->logk_to_faces(logK, kind, Ks));
         StructBatch &S = *P->sb;
         stage_in(P, logK, S.N, S.in_logK);
         double *tmp = is_device_ptr(Ks) ? Ks : S.in_Ks;
@@ -526,7 +531,7 @@ int dpf_logk_to_faces_vjp(dpf_problem *P, const double *logK, int kind, const do
     return guarded(P, [&]() -> int {
         if (!logK || !dKs || !dlogK) throw BadInput("logK, dKs and dlogK are required");
         if (kind != DPF_MEAN_GEOMETRIC && kind != DPF_MEAN_HARMONIC) throw BadInput("unknown mean kind");
-        if (P->gs) return P->gs->logk_vjp(logK, kind, dKs, dlogK);
+        if (P->gs) return gs_status(P, P->gs->logk_vjp(logK, kind, dKs, dlogK));
         StructBatch &S = *P->sb;
         stage_in(P, logK, S.N, S.in_logK);
         double *dk = scratch<double>(P, S.F);
@@ -574,7 +579,7 @@ int dpf_solve_grad_logk(dpf_problem *P, const double *logK, int kind, const doub
     return guarded(P, [&]() -> int {
         if (!logK || !dh || !Qs || nobs < 0 || (nobs > 0 && !obs)) throw BadInput("invalid arguments");
         if (kind != DPF_MEAN_GEOMETRIC && kind != DPF_MEAN_HARMONIC) throw BadInput("unknown mean kind");
-        if (P->gs) return P->gs->solve_grad_logk(logK, kind, dh, Qs, nobs, obs, h_out, dlogK);
+        if (P->gs) return gs_status(P, P->gs->solve_grad_logk(logK, kind, dh, Qs, nobs, obs, h_out, dlogK));
         StructBatch &S = *P->sb;
         if (S.nprob != 1) throw BadInput("use dpf_batch_solve_grad_logk for a batch");
         std::vector<long long> og(nobs);
@@ -622,7 +627,7 @@ int dpf_batch_solve_grad_logk(dpf_problem *P, const double *logK, int kind, cons
 int dpf_apply_operator(dpf_problem *P, const double *x, double *y) {
     return guarded(P, [&]() -> int {
         if (!x || !y) throw BadInput("x and y are required");
-        if (P->gs) return P->gs->apply(x, y);
+        if (P->gs) return gs_status(P, P->gs->apply(x, y));
         StructBatch &S = *P->sb;
         if (!S.have_operator) { P->err = "no operator assembled yet"; return DPF_STATE; }
         stage_in(P, x, S.N, S.r64);
@@ -638,7 +643,7 @@ int dpf_transient_forward(dpf_problem *P, const double *Ks, const double *dh, co
                           double *hT) {
     return guarded(P, [&]() -> int {
         if (!Ks || !dh || !Qs || !Ss || !h0 || nsteps <= 0 || !(dt > 0)) throw BadInput("invalid arguments");
-        if (P->gs) return P->gs->transient_forward(Ks, dh, Qs, Ss, dt, nsteps, h0, states, hT);
+        if (P->gs) return gs_status(P, P->gs->transient_forward(Ks, dh, Qs, Ss, dt, nsteps, h0, states, hT));
         StructBatch &S = *P->sb;
         int ck_every = checkpoint_every <= 0 ? 1 : std::min(checkpoint_every, nsteps);
         int nck = nsteps / ck_every + 1;
@@ -714,7 +719,7 @@ int dpf_transient_adjoint(dpf_problem *P, int64_t nobs, const int64_t *obs, cons
                           double *dKs, double *ddh, double *dQs, double *dh0) {
     return guarded(P, [&]() -> int {
         if (nobs < 0 || (nobs > 0 && !obs)) throw BadInput("invalid arguments");
-        if (P->gs) return P->gs->transient_adjoint(nobs, obs, w, gT, dKs, ddh, dQs, dh0);
+        if (P->gs) return gs_status(P, P->gs->transient_adjoint(nobs, obs, w, gT, dKs, ddh, dQs, dh0));
         StructBatch &S = *P->sb;
         if (P->tr_nsteps <= 0) { P->err = "transient adjoint needs a preceding transient forward"; return DPF_STATE; }
         const long long N = S.N;

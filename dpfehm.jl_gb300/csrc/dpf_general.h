@@ -1,4 +1,12 @@
 // dpf_general.h -- CSR (general topology) groundwater solver.
+//
+// For face lists that are not a regulargrid3d (unstructured meshes read by
+// load_uge, graphs with extra or duplicated faces). Same formulation as the
+// structured path: all N cells, Dirichlet cells as identity rows with decoupled
+// faces, operator applied in flux form y_i = leak_i x_i + sum_e c_e (x_i - x_j)
+// over the CSR couplings of row i. Multigrid by greedy graph aggregation (set up
+// once per topology on the host; the numeric Galerkin rebuild each forward is a
+// deterministic gather on the device).
 #pragma once
 #include <vector>
 
@@ -6,12 +14,29 @@
 
 namespace dpf {
 
+struct GLevel {
+    int n = 0, nnz = 0;
+    int *rp = nullptr, *ci = nullptr;        // couplings (no diagonal)
+    double *v64 = nullptr, *leak64 = nullptr, *idg64 = nullptr;
+    float *v32 = nullptr, *leak32 = nullptr, *idg32 = nullptr;
+    uint8_t *dir = nullptr;                   // identity rows
+    // transfer to the next coarser level
+    int *agg = nullptr;                       // fine cell -> aggregate (-1: none)
+    int *mrp = nullptr, *mci = nullptr;       // aggregate -> member cells (next level's row order)
+    int *crp = nullptr, *cci = nullptr;       // coarse coupling -> contributing fine couplings
+    void *work[4] = {nullptr, nullptr, nullptr, nullptr};  // xa, xb, b, d
+    bool dense = false;                       // coarsest level solved by its dense inverse
+};
+
 class GeneralSolver {
 public:
     GeneralSolver(long long N, long long F, const int64_t *a, const int64_t *b, const double *aol,
                   const double *volumes, long long nd, const int64_t *dn, const dpf_options &opt,
                   cudaStream_t stream);
     ~GeneralSolver();
+    GeneralSolver(const GeneralSolver &) = delete;
+    GeneralSolver &operator=(const GeneralSolver &) = delete;
+
     int forward(const double *Ks, const double *logK, int kind, const double *dh, const double *Qs, double *h_out);
     int adjoint(const double *delta, double *dKs, double *dlogK, double *ddh, double *dQs);
     int logk_to_faces(const double *logK, int kind, double *Ks);
@@ -23,12 +48,73 @@ public:
                           int nsteps, const double *h0, double *states, double *hT);
     int transient_adjoint(long long nobs, const int64_t *obs, const double *w, const double *gT, double *dKs,
                           double *ddh, double *dQs, double *dh0);
-    int nlevels() const;
+    int nlevels() const { return (int)lv.size(); }
 
     long long N = 0, F = 0, nfree = 0;
     int stats_iters = 0, stats_outer = 0;
-    long long launches = 0;
     double stats_relres = 0.0;
+    long long launches = 0;
+    std::string last_message;
+
+private:
+    void setup_topology(const int64_t *a, const int64_t *b, const double *aol, const double *volumes, long long nd,
+                        const int64_t *dn);
+    void build_hierarchy();
+    void assemble(const double *Ks, const double *kc, int kind, const double *shift, bool init_x);
+    void solve(const double *b, double *x);
+    template <typename T>
+    void vcycle(const T *r, T *z);
+    template <typename T>
+    void pcg(const T *b, T *x, double tol2);
+    void df_pcg(const double *b64, double *x64, double tol2);
+    void adjoint_solve(const double *delta_dev);
+    int finish_status();
+    int read_active();
+    template <typename T>
+    T *dev(size_t n);
+    void to_dev(void *dst, const void *src, size_t bytes);
+    void from_dev(void *dst, const void *src, size_t bytes);
+    const double *stage(const double *src, size_t n, double *dst);
+
+    dpf_options opt;
+    cudaStream_t stream;
+    bool mixed = false;
+    int nblocks = 0;                         // grid of every cell- or entry-parallel launch
+    std::vector<GLevel> lv;
+    std::vector<void *> owned;
+
+    // topology (device)
+    int *fa = nullptr, *fb = nullptr;        // face ends
+    double *faol = nullptr;                  // areas over lengths
+    int *e_face = nullptr;                   // fine coupling -> face
+    int *irp = nullptr, *ifc = nullptr;      // cell -> incident faces
+    double *vol = nullptr;                   // cell volumes
+    // vectors
+    double *h = nullptr, *b64 = nullptr, *r64 = nullptr, *lam = nullptr, *delta = nullptr, *arhs = nullptr;
+    double *in_Ks = nullptr, *in_kc = nullptr, *aux_kc = nullptr, *in_dh = nullptr, *in_Q = nullptr;
+    double *shift = nullptr, *tmpN = nullptr, *tmpF = nullptr;
+    void *cgv[4] = {nullptr, nullptr, nullptr, nullptr};
+    float2 *dfv[4] = {nullptr, nullptr, nullptr, nullptr};
+    float2 *vdf = nullptr, *leakdf = nullptr;
+    double *dense_inv = nullptr;
+    // CG state
+    CgState *d_state = nullptr;
+    int *d_count = nullptr;
+    int *d_status = nullptr;
+    int *h_count = nullptr;
+    CgState *h_state = nullptr;
+    ReduceScratch rs;
+    int2 *d_pinfo = nullptr;
+    double inv_theta = 1.0;
+    std::vector<double> cheb_c1, cheb_c2;
+    std::vector<double> cheb8_c1, cheb8_c2;  // degree-8 sweep standing in for a coarsest solve
+    std::vector<int> hrp_, hci_;             // finest couplings on the host (hierarchy set-up)
+    // bookkeeping
+    bool have_forward = false;
+    int fwd_kind = 0, mean_kind = 0;
+    int tr_nsteps = 0;
+    double *tr_b0 = nullptr, *tr_states = nullptr;
+    std::vector<int> h_dir;
 };
 
 }  // namespace dpf

@@ -206,6 +206,43 @@ __device__ __forceinline__ T diag7(const LevelDesc &L, const Cell &c, const Coef
 }
 
 // -------------------------------------------------------------- assembly
+// ---------------------------------------------------------- shared helpers
+__device__ __forceinline__ void deactivate(CgState &s, int *count) {
+    if (s.active) {
+        s.active = 0;
+        atomicSub(count, 1);
+    }
+}
+
+// double-float arithmetic: unevaluated sums hi + lo of two floats (about 48 bits)
+__device__ __forceinline__ float2 df_two_sum(float a, float b) {
+    float s = a + b;
+    float bb = s - a;
+    return make_float2(s, (a - (s - bb)) + (b - bb));
+}
+__device__ __forceinline__ float2 df_quick(float a, float b) {
+    float s = a + b;
+    return make_float2(s, b - (s - a));
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    float2 s = df_two_sum(a.x, b.x);
+    s.y += a.y + b.y;
+    return df_quick(s.x, s.y);
+}
+__device__ __forceinline__ float2 df_sub(float2 a, float2 b) { return df_add(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+    float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    return df_quick(p, e);
+}
+__device__ __forceinline__ float2 df_from_double(double v) {
+    float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+}
+__device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + (double)a.y; }
+
 // Face conductances from cell values kc, computed once per cell by k_cell_k
 // (GB300 has little FP64 throughput, so exp runs once per cell, not once per face):
 //   geometric  kc = exp(logK / 2):  K_f = exp((logK_a + logK_b)/2) = kc_a kc_b
@@ -218,171 +255,6 @@ __device__ __forceinline__ double face_mean_k(double ka, double kb, int kind) {
 __device__ __forceinline__ double face_mean_dlogk(double Kf, double ka, int kind) {
     if (kind == DPF_MEAN_GEOMETRIC) return 0.5 * Kf;
     return 0.5 * Kf * Kf / ka;
-}
-
-// Conductance of the face between cell c and its neighbour j in direction d (0..2)
-// and side s (+1: neighbour at +, -1: neighbour at -).
-struct FaceK {
-    const double *Ks;       // face list (reference order), or null
-    const double *kc;       // per-cell values of k_cell_k, or null
-    int kind;
-    __device__ __forceinline__ double operator()(const LevelDesc &L, const ProbParam &P, const Cell &c, int d, int s,
-                                                long long j) const {
-        if (Ks) {
-            int ax = c.ix, ay = c.iy, az = c.iz;  // face is owned by the lower cell
-            if (s < 0) { if (d == 0) ax--; else if (d == 1) ay--; else az--; }
-            return Ks[P.face_off + regular_face_index(L.nx, L.ny, L.nz, ax, ay, az, d)];
-        }
-        return face_mean_k(kc[c.i], kc[j], kind);
-    }
-};
-
-// Fine-level operator, right-hand side and initial guess (src/groundwater.jl:4-20 with
-// S = V = 1; storage shift for transient). Writes FP64 coefficients and, when fx != null,
-// FP32 copies.
-__global__ void k_assemble(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
-                           const ProbParam *__restrict__ prm, FaceK fk, const double *__restrict__ dh,
-                           const double *__restrict__ Qs, const double *__restrict__ shift,
-                           const uint8_t *__restrict__ dir, double *cx, double *cy, double *cz, double *leak,
-                           float *fx, float *fy, float *fz, float *fleak, double *b, double *x, int init_x) {
-    int4 bm = bmap[blockIdx.x];
-    LevelDesc L = desc[bm.x];
-    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
-        Cell c;
-        cell_at(L, li_, c);
-        const ProbParam P = prm[bm.x];
-        const long long i = c.i;
-        const long long st[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
-        const int co[3] = {c.ix, c.iy, c.iz};
-        const int nn[3] = {L.nx, L.ny, L.nz};
-        bool fi = !dir[i];
-        double lk = 0.0, rhs = fi ? Qs[i] : dh[i];
-        double cp[3] = {0.0, 0.0, 0.0};
-        if (fi) {
-    #pragma unroll
-            for (int d = 0; d < 3; d++) {
-                if (co[d] + 1 < nn[d]) {
-                    long long j = i + st[d];
-                    double cf = fk(L, P, c, d, +1, j) * P.aol[d];
-                    if (!dir[j]) cp[d] = cf;
-                    else { lk += cf; rhs += cf * dh[j]; }
-                }
-                if (co[d] > 0) {
-                    long long j = i - st[d];
-                    if (dir[j]) {
-                        double cf = fk(L, P, c, d, -1, j) * P.aol[d];
-                        lk += cf;
-                        rhs += cf * dh[j];
-                    }
-                }
-            }
-            if (shift) lk += shift[i];
-        } else {
-            lk = 1.0;
-        }
-        cx[i] = cp[0]; cy[i] = cp[1]; cz[i] = cp[2]; leak[i] = lk;
-        if (fx) { fx[i] = (float)cp[0]; fy[i] = (float)cp[1]; fz[i] = (float)cp[2]; fleak[i] = (float)lk; }
-        b[i] = rhs;
-        if (init_x) x[i] = fi ? 0.0 : dh[i];
-        else if (!fi) x[i] = dh[i];
-    }
-}
-
-// ----------------------------------------------------------- coarsening
-// Galerkin coarse operator of piecewise-constant 2x2x2 aggregation that leaves out
-// Dirichlet (identity) cells: a coarse face carries the sum of the fine faces that
-// cross it, a coarse leak is the sum of the free children's leaks. An aggregate
-// with no free child becomes an identity row.
-__global__ void k_coarsen(const LevelDesc *__restrict__ fdesc, const LevelDesc *__restrict__ cdesc,
-                          const int4 *__restrict__ bmap, const double *__restrict__ fcx,
-                          const double *__restrict__ fcy, const double *__restrict__ fcz,
-                          const double *__restrict__ fleak, const uint8_t *__restrict__ fdir, double *ccx,
-                          double *ccy, double *ccz, double *cleak, uint8_t *cdir, float *gx, float *gy, float *gz,
-                          float *gleak) {
-    int4 bm = bmap[blockIdx.x];
-    LevelDesc Lc = cdesc[bm.x];
-    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)Lc.n; li_ += bm.z * kBlock) {
-        Cell c;
-        cell_at(Lc, li_, c);
-        LevelDesc Lf = fdesc[bm.x];
-        const long long fsy = Lf.nz, fsx = (long long)Lf.ny * Lf.nz;
-        int x0 = 2 * c.ix, y0 = 2 * c.iy, z0 = 2 * c.iz;
-        int x1 = min(x0 + 1, Lf.nx - 1), y1 = min(y0 + 1, Lf.ny - 1), z1 = min(z0 + 1, Lf.nz - 1);
-        double lk = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
-        bool anyfree = false;
-        for (int fx = x0; fx <= x1; fx++)
-            for (int fy = y0; fy <= y1; fy++)
-                for (int fz = z0; fz <= z1; fz++) {
-                    long long j = Lf.off + fx * fsx + fy * fsy + fz;
-                    if (!fdir[j]) { anyfree = true; lk += fleak[j]; }
-                    if (fx == x0 + 1 && c.ix + 1 < Lc.nx) sx += fcx[j];
-                    if (fy == y0 + 1 && c.iy + 1 < Lc.ny) sy += fcy[j];
-                    if (fz == z0 + 1 && c.iz + 1 < Lc.nz) sz += fcz[j];
-                }
-        if (!anyfree) { lk = 1.0; sx = sy = sz = 0.0; }
-        const long long i = c.i;
-        ccx[i] = sx; ccy[i] = sy; ccz[i] = sz; cleak[i] = lk; cdir[i] = anyfree ? 0 : 1;
-        if (gx) { gx[i] = (float)sx; gy[i] = (float)sy; gz[i] = (float)sz; gleak[i] = (float)lk; }
-    }
-}
-
-// ------------------------------------------------------ coarsest level
-// Dense inverse of each listed problem's coarsest operator (n <= 64), one block
-// per problem, by in-place Gauss-Jordan elimination in shared memory (no pivoting:
-// the operator is symmetric positive definite, so every pivot is a positive Schur
-// complement). The coarsest solve is then one small matrix-vector product.
-// The inverse is stored row-major with stride kMaxCoarse.
-__global__ void k_coarse_factor(const LevelDesc *__restrict__ desc, const int *__restrict__ plist,
-                                const double *__restrict__ cx, const double *__restrict__ cy,
-                                const double *__restrict__ cz, const double *__restrict__ leak, double *Inv,
-                                int *status) {
-    __shared__ double A[kMaxCoarse][kMaxCoarse + 1];
-    __shared__ double col[kMaxCoarse];
-    __shared__ int bad;
-    int p = plist[blockIdx.x];
-    LevelDesc L = desc[p];
-    int n = (int)L.n;
-    const int sy = L.nz, sx = L.ny * L.nz;
-    for (int k = threadIdx.x; k < kMaxCoarse * kMaxCoarse; k += blockDim.x) A[k / kMaxCoarse][k % kMaxCoarse] = 0.0;
-    if (threadIdx.x == 0) bad = 0;
-    __syncthreads();
-    for (int li = threadIdx.x; li < n; li += blockDim.x) {
-        int q = li / L.nz, iz = li - q * L.nz, iy = q % L.ny, ix = q / L.ny;
-        long long i = L.off + li;
-        double d = leak[i];
-        if (iz + 1 < L.nz) { double w = cz[i];      d += w; A[li][li + 1] = -w; }
-        if (iz > 0)        { double w = cz[i - 1];  d += w; A[li][li - 1] = -w; }
-        if (iy + 1 < L.ny) { double w = cy[i];      d += w; A[li][li + sy] = -w; }
-        if (iy > 0)        { double w = cy[i - sy]; d += w; A[li][li - sy] = -w; }
-        if (ix + 1 < L.nx) { double w = cx[i];      d += w; A[li][li + sx] = -w; }
-        if (ix > 0)        { double w = cx[i - sx]; d += w; A[li][li - sx] = -w; }
-        A[li][li] = d;
-    }
-    __syncthreads();
-    for (int k = 0; k < n; k++) {
-        // pivot row k scaled by 1/A[k][k] (with the identity column folded in); save column k
-        double piv = A[k][k];
-        if (!(piv > 0.0)) { if (threadIdx.x == 0) bad = 1; piv = 1.0; }
-        double ip = 1.0 / piv;
-        __syncthreads();
-        for (int i = threadIdx.x; i < n; i += blockDim.x) col[i] = A[i][k];
-        __syncthreads();
-        for (int j = threadIdx.x; j < n; j += blockDim.x) A[k][j] = (j == k ? 1.0 : A[k][j]) * ip;
-        __syncthreads();
-        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
-            int i = t / n, j = t % n;
-            if (i == k) continue;
-            double rk = A[k][j];
-            A[i][j] = (j == k ? 0.0 : A[i][j]) - col[i] * rk;
-        }
-        __syncthreads();
-    }
-    double *Ip = Inv + (long long)p * kMaxCoarse * kMaxCoarse;
-    for (int k = threadIdx.x; k < kMaxCoarse * kMaxCoarse; k += blockDim.x) {
-        int i = k / kMaxCoarse, j = k % kMaxCoarse;
-        Ip[k] = (i < n && j < n) ? A[i][j] : 0.0;
-    }
-    if (threadIdx.x == 0 && bad) atomicExch(status, 1);
 }
 
 }  // namespace dpf
