@@ -40,7 +40,8 @@ METRIC = "forward+adjoint solves/sec at 1M cells vs plain FP64 GPU, at 1e-8 rel 
 # algorithmic bytes per cell of each kernel (vector/coefficient element size T):
 # reads and writes of every array the kernel touches once per cell
 BYTES_PER_CELL = {
-    "k_cheb_step": lambda T: 9 * T,            # xin, b, d, cx, cy, cz, leak in; xout, d out (first step: 8T)
+    "k_cheb_step": lambda T: 9 * T,            # xin, b, d, cx, cy, cz, leak in; xout, d out
+    "k_cheb_step0": lambda T: 8 * T,           # first step after prolongation: d is not read
     "k_prolong_add": lambda T: 2 * T + T / 8 + 1,   # x, e/8, dir in; x out
     "k_cheb_first": lambda T: 7 * T,           # b, cx, cy, cz, leak in; x, d out
     "k_cheb_first2": lambda T: 8 * T,          # b, idg, cx, cy, cz, leak in; xout, d out

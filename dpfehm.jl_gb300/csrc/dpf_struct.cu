@@ -1378,7 +1378,7 @@ void StructBatch::vcycle(const T *r, T *z) {
             T *o = (l == 0 && last) ? z : (cur == xa ? xb : xa);
             const T c1 = (T)cheb_c1[k], c2 = k == 0 ? invth : (T)cheb_c2[k];
             {
-                KTimer _kt(this, kname("k_cheb_step", l, sizeof(T) == 4), L.smooth_cells);
+                KTimer _kt(this, kname(k == 0 ? "k_cheb_step0" : "k_cheb_step", l, sizeof(T) == 4), L.smooth_cells);
                 if (l == 0 && last) {
                     if (k == 0)
                         k_cheb_step<T, true, true><<<nb_of(L.smooth), kBlock, 0, stream>>>(
