@@ -85,7 +85,7 @@ def load(path=None):
     global _lib
     if _lib is not None:
         return _lib
-    path = path or LIB_PATH
+    path = path or os.environ.get("DPFEHM_GPU_LIB") or LIB_PATH
     if not os.path.exists(path):
         raise OSError("libdpfehm_gpu.so not found at %s: build it first (dpfehm.jl_gb300/build.py or "
                       "__graft_entry__.build()); there is no CPU fallback" % path)

@@ -28,16 +28,20 @@ def _deps():
     return max(os.path.getmtime(f) for f in files)
 
 
-def build(force=False, verbose=False):
-    """Compile (if sources changed) and return the library path."""
-    os.makedirs(OUT, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps():
-        return LIB
+def build(force=False, verbose=False, out_dir=None, defines=()):
+    """Compile (if sources changed) and return the library path. `out_dir` and
+    `defines` (extra -D flags) build a variant elsewhere, e.g. for tuning runs."""
+    out = out_dir or OUT
+    lib = os.path.join(out, "libdpfehm_gpu.so")
+    os.makedirs(out, exist_ok=True)
+    if not force and os.path.exists(lib) and os.path.getmtime(lib) >= _deps():
+        return lib
     nvcc = _nvcc()
+    extra = ["-D" + d for d in defines]
 
     def compile_one(src):
-        obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
-        cmd = [nvcc] + ARCH + NVCC_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+        obj = os.path.join(out, os.path.splitext(src)[0] + ".o")
+        cmd = [nvcc] + ARCH + NVCC_FLAGS + extra + ["-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd))
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -47,13 +51,13 @@ def build(force=False, verbose=False):
 
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
-    tmp = LIB + ".tmp%d" % os.getpid()
+    tmp = lib + ".tmp%d" % os.getpid()
     cmd = [nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s" % r.stderr)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 8 : 5) k_cheb_first2(
 // With FUSE_RZ the kernel is the last of the level-0 V-cycle: it also reduces b . xout
 // (b is the CG residual, xout the preconditioned residual) and finalises beta.
 template <typename T, bool FUSE_RZ, bool FIRST = false>
-__global__ void __launch_bounds__(kBlock, (sizeof(T) == 4 && !FUSE_RZ) ? 8 : 6)
+__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 8 : 6)
 k_cheb_step(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st, Coeffs<T> C,
             const T *__restrict__ b, const T *__restrict__ xin, T *__restrict__ xout, T *__restrict__ d, T c1, T c2,
             ReduceScratch rs, const int2 *__restrict__ pinfo) {
@@ -270,7 +270,7 @@ k_cheb_step(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, C
 
 // Restriction of the residual: bc[I] = sum over the children i of I of (b_i - (A x)_i).
 template <typename T>
-__global__ void __launch_bounds__(kBlock, 5) k_restrict(const LevelDesc *__restrict__ fdesc, const LevelDesc *__restrict__ cdesc,
+__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 8 : 5) k_restrict(const LevelDesc *__restrict__ fdesc, const LevelDesc *__restrict__ cdesc,
                            const int4 *__restrict__ bmap, CgState *st, Coeffs<T> C, const T *__restrict__ b,
                            const T *__restrict__ x, T *__restrict__ bc) {
     int4 bm = bmap[blockIdx.x];
@@ -478,7 +478,7 @@ struct CoeffsDF {
 
 // q = A p in double-float (flux form); alpha = rz / (p . q) (hi parts: q is accurate, so
 // its leading float is too)
-__global__ void __launch_bounds__(kBlock, kMinBlocks) k_df_spmv_pq(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
+__global__ void __launch_bounds__(kBlock, 8) k_df_spmv_pq(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                              int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, CoeffsDF C,
                              const float2 *__restrict__ pv, float2 *__restrict__ q) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
