@@ -51,12 +51,16 @@ BYTES_PER_CELL = {
     "k_update_p": lambda T: 3 * T,             # z, p in; p out
     "k_cg_start": lambda T: 7 * T,             # x, b, 4 coeffs in; r out
     "k_df_spmv_pq": lambda T: 48,              # p (2 floats), 4 double-float coeffs in; q out
-    "k_df_update_xr": lambda T: 52,            # x, p, r, q (2 floats each) in; x, r, r32 out
+    "k_df_update_xr": lambda T: 52,            # x (f64), p, r, q (2 floats each) in; x, r, r32 out
     "k_df_update_p": lambda T: 20,             # z, p in; p out
     "k_df_residual": lambda T: 56,             # x64, b64, 4 FP64 coeffs in; r64 out
-    "k_df_begin": lambda T: 28,                # r64 in; r (2 floats), r32, x out
-    "k_df_end": lambda T: 24,                  # x (2 floats), x64 in; x64 out
+    "k_df_begin": lambda T: 20,                # r64 in; r (2 floats), r32 out
     "k_grad_logk": lambda T: 32,               # logK, h, lambda in; g out
+    # plane-marching smoothers (Chebyshev degree 2): each value is read from HBM once
+    "k_pm_first2": lambda T: 7 * T,            # b, idg, cx, cy, cz, leak in; x out (no direction)
+    "k_pm_step": lambda T: 8 * T,              # x, b, d, cx, cy, cz, leak in; x out (last step)
+    "k_pm_prolong_step": lambda T: 8 * T + T / 8 + 1,  # x, e/8, dir, b, 4 coeffs in; x, d out
+    "k_df_residual0": lambda T: 17,            # b, dir in; r out
 }
 
 

@@ -31,6 +31,8 @@ class Options(ctypes.Structure):
         ("use_graphs", ctypes.c_int),
         ("check_every", ctypes.c_int),
         ("blocks_per_sm", ctypes.c_int),
+        ("tail_cells", ctypes.c_int),
+        ("plane", ctypes.c_int),
     ]
 
 

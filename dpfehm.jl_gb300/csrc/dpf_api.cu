@@ -193,6 +193,8 @@ dpf_options fill_options(const dpf_options *o) {
     if (r.max_outer <= 0) r.max_outer = d.max_outer;
     if (r.check_every <= 0) r.check_every = d.check_every;
     if (r.blocks_per_sm <= 0) r.blocks_per_sm = d.blocks_per_sm;
+    if (r.tail_cells == 0) r.tail_cells = d.tail_cells;
+    if (r.plane == 0) r.plane = d.plane;
     return r;
 }
 
@@ -237,6 +239,8 @@ void dpf_default_options(dpf_options *o) {
     o->use_graphs = 1;
     o->check_every = 1;
     o->blocks_per_sm = 16;
+    o->tail_cells = 4096;
+    o->plane = 1;
 }
 
 int dpf_detect_regular3d(int64_t N, int64_t F, const int64_t *a, const int64_t *b, const double *aol, int *dims,

@@ -421,14 +421,17 @@ __global__ void kg_df_spmv_pq(int n, CgState *st, int *active_count, ReduceScrat
     }
 }
 
-__global__ void kg_df_update_xr(int n, CgState *st, int *active_count, ReduceScratch rs, float2 *__restrict__ x,
+// x64 += (alpha scale) p in FP64 (the solution keeps all 53 bits); r -= alpha q (double-float)
+__global__ void kg_df_update_xr(int n, CgState *st, int *active_count, ReduceScratch rs, double *__restrict__ x64,
                                 float2 *__restrict__ r, float *__restrict__ r32, const float2 *__restrict__ pv,
                                 const float2 *__restrict__ q, int maxiter) {
     if (!st[0].active) return;
     const float2 a = df_from_double(st[0].alpha);
+    const double as = st[0].alpha * st[0].scale;
     Acc<float> part;
     GSTRIDE(i, n) {
-        x[i] = df_add(x[i], df_mul(a, pv[i]));
+        const float2 pi = pv[i];
+        x64[i] = fma(as, (double)pi.x + (double)pi.y, x64[i]);
         const float2 ri = df_sub(r[i], df_mul(a, q[i]));
         r[i] = ri;
         r32[i] = ri.x;
@@ -462,20 +465,27 @@ __global__ void kg_df_residual(int n, CgState *st, int *active_count, ReduceScra
                                const double *__restrict__ b, const double *__restrict__ x, double *__restrict__ r,
                                double tol2, int maxiter, int max_rounds) {
     if (!FIRST && !st[0].ru_flag) return;
-    Acc<double> rr, bb;
+    Acc<double> rr, bb;  // FIRST: |r|^2, |b|^2; otherwise |r|^2 and the FP64 rounding floor
     GSTRIDE(i, n) {
         double dg;
-        double ri = b[i] - g_apply<double>(i, A.rp, A.ci, A.v, A.leak, x[i], [&](int j) { return x[j]; }, dg);
+        const double xi = x[i];
+        double ri = b[i] - g_apply<double>(i, A.rp, A.ci, A.v, A.leak, xi, [&](int j) { return x[j]; }, dg);
         r[i] = ri;
         rr.v += ri * ri;
-        if (FIRST) bb.v += b[i] * b[i];
+        if (FIRST) {
+            bb.v += b[i] * b[i];
+        } else {
+            const double f = 0x1p-53 * fma(2.0 * dg, fabs(xi), fabs(b[i]));
+            bb.v += f * f;
+        }
     }
     double2 tot;
-    if (reduce_last<double, FIRST ? 2 : 1>(rr, bb, rs, make_int2(0, gridDim.x), 0, tot) && threadIdx.x == 0) {
+    if (reduce_last<double, 2>(rr, bb, rs, make_int2(0, gridDim.x), 0, tot) && threadIdx.x == 0) {
         CgState &s = st[0];
         s.orr = tot.x;
         bool go;
         if (FIRST) {
+            s.floor2 = 0.0;
             s.obb = tot.y;
             s.tol2 = tol2;
             s.status = DPF_OK;
@@ -485,10 +495,12 @@ __global__ void kg_df_residual(int n, CgState *st, int *active_count, ReduceScra
             if (!isfinite(s.orr)) { s.status = DPF_NAN; go = false; }
         } else {
             s.outer++;
-            const bool stalled = s.orr > 0.25 * s.orr_prev;
+            s.floor2 = tot.y;
+            // at the FP64 rounding floor of b - A x: accept (no further accuracy exists)
+            const bool at_floor = s.orr <= s.floor2 || s.orr > 0.25 * s.orr_prev;
             go = true;
             if (!isfinite(s.orr)) { s.status = DPF_NAN; go = false; }
-            else if (s.orr <= tol2 * s.obb || stalled) go = false;
+            else if (s.orr <= tol2 * s.obb || at_floor) go = false;
             else if (s.total_iters >= maxiter || s.outer >= max_rounds) { s.status = DPF_NOT_CONVERGED; go = false; }
         }
         s.orr_prev = s.orr;
@@ -504,21 +516,14 @@ __global__ void kg_df_residual(int n, CgState *st, int *active_count, ReduceScra
 }
 
 __global__ void kg_df_begin(int n, const CgState *st, const double *__restrict__ r64, float2 *__restrict__ r,
-                            float *__restrict__ r32, float2 *__restrict__ x) {
+                            float *__restrict__ r32) {
     if (!st[0].ru_flag) return;
     const double inv = 1.0 / st[0].scale;
     GSTRIDE(i, n) {
         const float2 v = df_from_double(r64[i] * inv);
         r[i] = v;
         r32[i] = v.x;
-        x[i] = make_float2(0.0f, 0.0f);
     }
-}
-
-__global__ void kg_df_end(int n, const CgState *st, const float2 *__restrict__ x, double *__restrict__ x64) {
-    if (!st[0].ru_flag) return;
-    const double sc = st[0].scale;
-    GSTRIDE(i, n) x64[i] += sc * df_to_double(x[i]);
 }
 
 // ------------------------------------------------------------ misc and gradients
@@ -719,7 +724,7 @@ GeneralSolver::GeneralSolver(long long N_, long long F_, const int64_t *a, const
         for (int k = 0; k < 4; k++) cgv[k] = dev<double>(N);
     } else {
         for (int k = 0; k < 2; k++) cgv[k] = dev<float>(N);
-        for (int k = 0; k < 4; k++) dfv[k] = dev<float2>(N);
+        for (int k = 1; k < 4; k++) dfv[k] = dev<float2>(N);  // r, p, q (double-float)
         vdf = dev<float2>(lv[0].nnz);
         leakdf = dev<float2>(N);
     }
@@ -1115,7 +1120,7 @@ void GeneralSolver::df_pcg(const double *b, double *x, double tol2) {
     GLAUNCH();
     const int check = std::max(1, opt.check_every);
     for (int round = 0; round < opt.max_outer && read_active() > 0; round++) {
-        kg_df_begin<<<nblocks, kBlock, 0, stream>>>(n, d_state, r64, dfv[1], r32, dfv[0]);
+        kg_df_begin<<<nblocks, kBlock, 0, stream>>>(n, d_state, r64, dfv[1], r32);
         GLAUNCH();
         vcycle<float>(r32, z32);
         kg_df_update_p<<<nblocks, kBlock, 0, stream>>>(n, d_state, z32, dfv[2]);
@@ -1124,7 +1129,7 @@ void GeneralSolver::df_pcg(const double *b, double *x, double tol2) {
             kg_df_spmv_pq<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, L0.rp, L0.ci, vdf, leakdf, dfv[2],
                                                           dfv[3]);
             GLAUNCH();
-            kg_df_update_xr<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, dfv[0], dfv[1], r32, dfv[2],
+            kg_df_update_xr<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, x, dfv[1], r32, dfv[2],
                                                             dfv[3], opt.maxiter);
             GLAUNCH();
             if (it % check == 0 && read_active() <= 0) break;
@@ -1132,8 +1137,6 @@ void GeneralSolver::df_pcg(const double *b, double *x, double tol2) {
             kg_df_update_p<<<nblocks, kBlock, 0, stream>>>(n, d_state, z32, dfv[2]);
             GLAUNCH();
         }
-        kg_df_end<<<nblocks, kBlock, 0, stream>>>(n, d_state, dfv[0], x);
-        GLAUNCH();
         GCK(cudaMemsetAsync(d_count, 0, sizeof(int), stream));
         kg_df_residual<false><<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, A, b, x, r64, tol2,
                                                               opt.maxiter, opt.max_outer);

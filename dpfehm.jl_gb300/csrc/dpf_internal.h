@@ -53,12 +53,12 @@ struct BlockMap {                  // launch map: block -> (problem, block withi
 struct CgState {
     double rz, rz_old, pq, rr, bb, tol2;
     double alpha, beta;
-    double scale;                  // mixed precision: normalisation of the FP32 residual
-    double ratio;                  // mixed precision: old scale / new scale at the last update
+    double scale;                  // mixed precision: normalisation of the double-float residual
+    double floor2;                 // mixed precision: FP64 rounding floor of |b - A x|^2 at the last check
     double orr, obb;               // mixed precision: true (FP64) residual and rhs norms squared
-    double orr_prev;               // mixed precision: true residual norm squared at the previous replacement
-    int iters, active, status, outer;  // outer: reliable updates so far
-    int ru_flag, total_iters, stall, pad2;  // stall: consecutive replacements without progress
+    double orr_prev;               // mixed precision: true residual norm squared after the previous round
+    int iters, active, status, outer;  // outer: rounds so far
+    int ru_flag, total_iters, stall, pad2;  // ru_flag: problem takes part in the current round
 };
 
 // Reduction scratch: one double2 partial per block of the widest launch, one

@@ -1,0 +1,363 @@
+// dpf_plane.cuh -- plane-marching Chebyshev kernels for the structured multigrid levels.
+//
+// A block owns a slab of `rows` consecutive y-rows of a problem's grid (all nz cells of
+// each row, so the slab is one contiguous range of each array per x-plane) and marches
+// along x over a chunk of planes. Every array the step reads is streamed plane by plane
+// into a ring of shared-memory stages with 1-D bulk asynchronous copies
+// (cp.async.bulk, completion on an mbarrier); the x-plane of the iterate is staged with one
+// halo row on each side, so all six neighbours of a cell come from shared memory and each
+// value is read from HBM once. A producer warp issues the copies, so the copies in flight
+// do not occupy registers and the ring keeps planes ahead in flight per block.
+//
+// The arithmetic is that of the per-cell bodies in dpf_struct.cu in the same order
+// (apply7: z+, z-, y+, y-, x+, x-), so results are bitwise identical to the grid-stride
+// kernels. Every mbarrier wait is bounded; on expiry the kernel records an error in *err,
+// and the producer drains its copies (bounded) before the block returns.
+#pragma once
+#include <cstdint>
+
+#include "dpf_struct_kernels.cuh"
+
+namespace dpf {
+
+constexpr int kPlaneThreads = 256;
+#ifndef DPF_PLANE_STAGES
+#define DPF_PLANE_STAGES 4
+#endif
+constexpr int kPlaneStages = DPF_PLANE_STAGES;  // planes x-1, x, x+1 resident, the rest in flight
+#ifndef DPF_PLANE_CPT
+#define DPF_PLANE_CPT 3
+#endif
+constexpr int kPlaneCells = kPlaneThreads * DPF_PLANE_CPT;  // slab cells per plane (whole rows)
+constexpr uint32_t kWaitTries = 1u << 20;  // bounded mbarrier polling (well under a second)
+
+enum : int { PM_FIRST2 = 1, PM_FIRST = 2, PM_PROLONG = 4, PM_NOD = 8, PM_RZ = 16 };
+
+// byte offsets of the per-stream regions in one stage, and the stage size (host computed)
+struct PlaneLayout {
+    int slot_bytes;
+    int oX, oB, oD, oCX, oCY, oCZ, oLK, oG, oDIR, oE;
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred P;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, P;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait for the phase with the given parity; false (and *err set) on expiry
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
+    for (uint32_t k = 0; k < kWaitTries; k++)
+        if (mbar_try_wait(bar, parity)) return true;
+    if (err) atomicExch(err, 1);
+    return false;
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+// order this thread's generic-proxy shared-memory accesses before later async-proxy ones
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbarrier_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// One staged range: global elements [a0, a1) of `base` land in the stage region at
+// element position delta + (a0 - l0), where l0 is the logical start of the region and
+// delta = (l0 * es mod 16) / es puts source and destination on the same 16-byte phase.
+// Both ends are widened to 16-byte boundaries (allocations carry 64 bytes of padding).
+struct BulkRange {
+    const char *src;
+    char *dst;
+    uint32_t bytes;
+};
+
+__device__ __forceinline__ int stage_delta(long long l0, int es) { return (int)(((l0 * es) & 15) / es); }
+
+__device__ __forceinline__ BulkRange make_range(const void *base, int es, long long l0, long long a0, long long a1,
+                                                char *region) {
+    BulkRange r;
+    const uintptr_t s0 = (uintptr_t)base + (uintptr_t)(a0 * es);
+    const uintptr_t res = s0 & 15u;
+    const uintptr_t s1 = (uintptr_t)base + (uintptr_t)(a1 * es);
+    r.src = (const char *)(s0 - res);
+    r.dst = region + (stage_delta(l0, es) + (a0 - l0)) * es - res;
+    r.bytes = (uint32_t)(((s1 - (s0 - res)) + 15u) & ~(uintptr_t)15u);
+    return r;
+}
+
+// Fast division of k (< 2^31) by nz with the level's invariant-integer constants.
+__device__ __forceinline__ int div_nz(const LevelDesc &L, int k) { return (int)fast_div((unsigned)k, L.mag_nz, L.sh_nz); }
+
+// Chebyshev step family on the plane ring. MODE bits:
+//   PM_FIRST2  the first two steps from a zero guess (reads b and the inverse diagonal
+//              with halos instead of an iterate)
+//   PM_FIRST   d = c2 r (d not read)
+//   PM_PROLONG the iterate is corrected on arrival: x += scale * e[aggregate] (not at
+//              identity rows), i.e. the prolongation fused into the first post-step
+//   PM_NOD     d not written (last step of a sweep)
+//   PM_RZ      reduce b . xout per problem and finalise beta (last step of the cycle)
+//
+// Warp-specialised pipeline: warp kPlaneThreads/32 is the producer (its lane 0 stages
+// plane after plane as ring slots free up), warps 0..7 consume. Per slot three mbarriers:
+// full (copies landed), empty (all consumer warps are done with the plane), ready (with
+// PM_PROLONG: every consumer thread has applied its share of the correction).
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
+    const LevelDesc *__restrict__ desc, const LevelDesc *__restrict__ cdesc, const int4 *__restrict__ items,
+    CgState *st, Coeffs<T> C, const T *__restrict__ b, const T *__restrict__ xin, T *__restrict__ xout,
+    T *__restrict__ d, const uint8_t *__restrict__ dir, const T *__restrict__ e, T c1, T c2, T invtheta, T scale,
+    PlaneLayout lay, ReduceScratch rs, const int2 *__restrict__ pinfo, int *err) {
+    constexpr bool F2 = (MODE & PM_FIRST2) != 0, FIRST = (MODE & PM_FIRST) != 0,
+                   PROL = (MODE & PM_PROLONG) != 0, NOD = (MODE & PM_NOD) != 0, RZ = (MODE & PM_RZ) != 0;
+    constexpr int R = kPlaneStages;
+    constexpr int es = (int)sizeof(T);
+    constexpr int kConsumerWarps = kPlaneThreads / 32;
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ uint64_t full[R], empty[R], ready[R];
+
+    const int4 it = items[blockIdx.x];
+    const int p = it.x, y0 = it.y, xa = it.z, xe = it.w;
+    if (st && !st[p].active) return;
+    const LevelDesc L = desc[p];
+    const int nz = L.nz, ny = L.ny, nx = L.nx;
+    const long long sx = (long long)ny * nz;
+    const int Ty = max(1, min(ny, kPlaneCells / nz));
+    const int rows = min(Ty, ny - y0);
+    const int ncell = rows * nz;
+    const int t = threadIdx.x;
+    const int warp = t >> 5, lane = t & 31;
+    const int pl_lo = max(xa - 1, 0), pl_hi = min(xe, nx - 1);
+    const int h0 = max(y0 - 1, 0), h1 = min(y0 + rows + 1, ny);
+    LevelDesc Lc{};
+    if (PROL) Lc = cdesc[p];
+    const long long csx = PROL ? (long long)Lc.ny * Lc.nz : 0;
+    const int cr_lo = (y0 - 1) >> 1;  // logical first coarse row of the halo (may be -1)
+    auto slot_of = [&](int q) { return (char *)sm + ((q - pl_lo) % R) * lay.slot_bytes; };
+
+    if (t == 0) {
+        for (int s = 0; s < R; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kConsumerWarps);
+            mbar_init(&ready[s], kPlaneThreads);
+        }
+        fence_mbarrier_init();
+    }
+    __syncthreads();
+    Acc<T> part;
+
+    if (warp == kConsumerWarps) {
+        // ---------------- producer
+        if (lane == 0) {
+            int issued_hi = pl_lo - 1;
+            for (int q = pl_lo; q <= pl_hi; q++) {
+                const int u = q - pl_lo, s = u % R;
+                if (u >= R && !mbar_wait(&empty[s], (uint32_t)((u / R - 1) & 1), err)) break;
+                fence_proxy_async_smem();
+                char *slot = (char *)sm + s * lay.slot_bytes;
+                const long long pb = L.off + (long long)q * sx;
+                const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
+                const long long hA = pb + (long long)h0 * nz, hB = pb + (long long)h1 * nz, pE = lp + ncell;
+                // each copy is announced on the barrier right before it is issued; the one
+                // pending arrival keeps the phase open until every copy has been announced
+                uint64_t *bar = &full[s];
+                auto stage = [&](const void *base, int esz, long long l0, long long a0, long long a1, int off) {
+                    const BulkRange r = make_range(base, esz, l0, a0, a1, slot + off);
+                    mbar_expect_tx(bar, r.bytes);
+                    bulk_copy_g2s(r.dst, r.src, r.bytes, bar);
+                };
+                if (F2) {
+                    stage(b, es, lh, hA, hB, lay.oB);
+                    stage(C.idg, es, lh, hA, hB, lay.oG);
+                } else {
+                    stage(xin, es, lh, hA, hB, lay.oX);
+                    stage(b, es, lp, lp, pE, lay.oB);
+                    if (!FIRST) stage(d, es, lp, lp, pE, lay.oD);
+                }
+                stage(C.cx, es, lp, lp, pE, lay.oCX);
+                stage(C.cy, es, lh, hA, pE, lay.oCY);
+                stage(C.cz, es, lp, lp, pE, lay.oCZ);
+                stage(C.leak, es, lp, lp, pE, lay.oLK);
+                if (PROL) {
+                    stage(dir, 1, lh, hA, hB, lay.oDIR);
+                    const long long cb = Lc.off + (long long)(q >> 1) * csx;
+                    const int c0 = max(cr_lo, 0), c1r = min((y0 + rows) >> 1, Lc.ny - 1) + 1;
+                    stage(e, es, cb + (long long)cr_lo * Lc.nz, cb + (long long)c0 * Lc.nz,
+                          cb + (long long)c1r * Lc.nz, lay.oE);
+                }
+                mbar_arrive(bar);
+                issued_hi = q;
+            }
+            // the block must not end with copies in flight into its shared memory: wait
+            // (bounded) for the last phase of every slot that was filled
+            for (int q = max(pl_lo, issued_hi - R + 1); q <= issued_hi; q++) {
+                const int u = q - pl_lo;
+                mbar_wait(&full[u % R], (uint32_t)((u / R) & 1), nullptr);
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---------------- consumers
+        int waited = pl_lo - 1;
+        bool ok = true;
+        for (int x = xa; x < xe && ok; x++) {
+            const int need = min(x + 1, pl_hi);
+            const int first_new = waited + 1;
+            while (waited < need) {
+                const int q = waited + 1, u = q - pl_lo;
+                if (!mbar_wait(&full[u % R], (uint32_t)((u / R) & 1), err)) {
+                    ok = false;
+                    break;
+                }
+                waited = q;
+                if (PROL) {
+                    // prolongation on arrival: this thread's share of the slab and its halo rows
+                    char *sl = slot_of(q);
+                    const long long pb = L.off + (long long)q * sx;
+                    const long long lh = pb + (long long)(y0 - 1) * nz;
+                    T *X = (T *)(sl + lay.oX) + stage_delta(lh, es);
+                    const uint8_t *DR = (const uint8_t *)(sl + lay.oDIR) + stage_delta(lh, 1);
+                    const long long cb = Lc.off + (long long)(q >> 1) * csx;
+                    const T *E = (const T *)(sl + lay.oE) + stage_delta(cb + (long long)cr_lo * Lc.nz, es);
+                    const int nh = (rows + 2) * nz;
+                    for (int k = t; k < nh; k += kPlaneThreads) {
+                        const int rr = div_nz(L, k);
+                        const int row = y0 - 1 + rr;
+                        if (row < 0 || row >= ny || DR[k]) continue;
+                        const int zz = k - rr * nz;
+                        X[k] += scale * E[((row >> 1) - cr_lo) * Lc.nz + (zz >> 1)];
+                    }
+                    mbar_arrive(&ready[u % R]);
+                }
+            }
+            if (!ok) break;
+            if (PROL) {
+                for (int q = first_new; q <= waited; q++) {
+                    const int u = q - pl_lo;
+                    if (!mbar_wait(&ready[u % R], (uint32_t)((u / R) & 1), err)) {
+                        ok = false;
+                        break;
+                    }
+                }
+                if (!ok) break;
+            }
+            for (int tc = t; tc < ncell; tc += kPlaneThreads) {
+                const int ty = div_nz(L, tc);
+                const int z = tc - ty * nz;
+                const int y = y0 + ty;
+                const long long pb = L.off + (long long)x * sx;
+                const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
+                const int dh = stage_delta(lh, es), dp = stage_delta(lp, es);
+                char *sc = slot_of(x);
+                const T *CX = (const T *)(sc + lay.oCX) + dp;
+                const T *CY = (const T *)(sc + lay.oCY) + dh;  // logical row 0 = y0 - 1
+                const T *CZ = (const T *)(sc + lay.oCZ) + dp;
+                const T *LK = (const T *)(sc + lay.oLK) + dp;
+                const long long i = lp + tc;
+                const int c = nz + tc;  // own cell in halo coordinates
+                if (F2) {
+                    // x1 = invtheta b g at a cell; neighbours from the staged b and g halos
+                    const T *B = (const T *)(sc + lay.oB) + dh;
+                    const T *G = (const T *)(sc + lay.oG) + dh;
+                    const T bi = B[c], gi = G[c];
+                    const T x1 = invtheta * bi * gi;
+                    const T lk = LK[tc];
+                    T a = lk * x1;
+                    if (z + 1 < nz) a += CZ[tc] * (x1 - invtheta * B[c + 1] * G[c + 1]);
+                    if (z > 0)      a += CZ[tc - 1] * (x1 - invtheta * B[c - 1] * G[c - 1]);
+                    if (y + 1 < ny) a += CY[c] * (x1 - invtheta * B[c + nz] * G[c + nz]);
+                    if (y > 0)      a += CY[tc] * (x1 - invtheta * B[c - nz] * G[c - nz]);
+                    if (x + 1 < nx) {
+                        char *sn = slot_of(x + 1);
+                        const int dn_ = stage_delta(lh + sx, es);
+                        const T *Bn = (const T *)(sn + lay.oB) + dn_;
+                        const T *Gn = (const T *)(sn + lay.oG) + dn_;
+                        a += CX[tc] * (x1 - invtheta * Bn[c] * Gn[c]);
+                    }
+                    if (x > 0) {
+                        char *sq = slot_of(x - 1);
+                        const int dq = stage_delta(lh - sx, es);
+                        const T *Bq = (const T *)(sq + lay.oB) + dq;
+                        const T *Gq = (const T *)(sq + lay.oG) + dq;
+                        const T *CXq = (const T *)(sq + lay.oCX) + stage_delta(lp - sx, es);
+                        a += CXq[tc] * (x1 - invtheta * Bq[c] * Gq[c]);
+                    }
+                    const T dn = c1 * x1 + c2 * (bi - a) * gi;
+                    if (!NOD) d[i] = dn;
+                    xout[i] = x1 + dn;
+                } else {
+                    const T *X = (const T *)(sc + lay.oX) + dh;
+                    const T *B = (const T *)(sc + lay.oB) + dp;
+                    const T xi = X[c];
+                    const T lk = LK[tc];
+                    T a = lk * xi, dg = lk;
+                    if (z + 1 < nz) { T w = CZ[tc];     a += w * (xi - X[c + 1]);  dg += w; }
+                    if (z > 0)      { T w = CZ[tc - 1]; a += w * (xi - X[c - 1]);  dg += w; }
+                    if (y + 1 < ny) { T w = CY[c];     a += w * (xi - X[c + nz]); dg += w; }
+                    if (y > 0)      { T w = CY[tc];     a += w * (xi - X[c - nz]); dg += w; }
+                    if (x + 1 < nx) {
+                        const T *Xn = (const T *)(slot_of(x + 1) + lay.oX) + stage_delta(lh + sx, es);
+                        T w = CX[tc];
+                        a += w * (xi - Xn[c]);
+                        dg += w;
+                    }
+                    if (x > 0) {
+                        char *sq = slot_of(x - 1);
+                        const T *Xq = (const T *)(sq + lay.oX) + stage_delta(lh - sx, es);
+                        const T *CXq = (const T *)(sq + lay.oCX) + stage_delta(lp - sx, es);
+                        T w = CXq[tc];
+                        a += w * (xi - Xq[c]);
+                        dg += w;
+                    }
+                    const T bi = B[tc];
+                    T r;
+                    if constexpr (sizeof(T) == 8) r = (bi - a) * C.idg[i];
+                    else r = __fdividef(bi - a, dg);
+                    T dn;
+                    if (FIRST) dn = c2 * r;
+                    else dn = c1 * ((const T *)(sc + lay.oD) + dp)[tc] + c2 * r;
+                    const T xo = xi + dn;
+                    if (!NOD) d[i] = dn;
+                    xout[i] = xo;
+                    if (RZ) part = part + Acc<T>::prod(bi, xo);
+                }
+            }
+            // this warp is done with plane x-1
+            __syncwarp();
+            if (lane == 0 && x - 1 >= pl_lo) mbar_arrive(&empty[(x - 1 - pl_lo) % R]);
+        }
+    }
+    if (RZ) {
+        double2 tot;
+        if (reduce_last<T>(part, Acc<T>(), rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+            CgState &s = st[p];
+            s.rz_old = s.rz;
+            s.rz = tot.x;
+            s.beta = (s.iters == 0 || s.rz_old == 0.0) ? 0.0 : s.rz / s.rz_old;
+        }
+    }
+}
+
+}  // namespace dpf

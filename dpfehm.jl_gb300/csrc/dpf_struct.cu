@@ -2,7 +2,7 @@
 //
 // A StructBatch holds nprob regular grids (a single problem is a batch of one):
 // the multigrid hierarchy (2x2x2 aggregation, Galerkin 7-point coarse operators,
-// dense Cholesky coarsest level), the CG / iterative-refinement state, and the
+// dense inverse of the coarsest level), the CG / iterative-refinement state, and the
 // kernels that solve and differentiate
 //   A h = b,   A = groundwater_h, b = -groundwater_residuals(0)   (src/groundwater.jl:75-83)
 //   A lambda = delta[free]                                        (src/groundwater.jl:93-107)
@@ -18,6 +18,7 @@
 
 #include "dpf_struct.h"
 #include "dpf_struct_kernels.cuh"
+#include "dpf_plane.cuh"
 
 namespace dpf {
 
@@ -46,7 +47,8 @@ __global__ void k_assemble(const LevelDesc *__restrict__ desc, const int4 *__res
                            const ProbParam *__restrict__ prm, FaceK fk, const double *__restrict__ dh,
                            const double *__restrict__ Qs, const double *__restrict__ shift,
                            const uint8_t *__restrict__ dir, double *cx, double *cy, double *cz, double *leak,
-                           float *fx, float *fy, float *fz, float *fleak, double *b, double *x, int init_x) {
+                           float *fx, float *fy, float *fz, float *fleak, float2 *dfx, float2 *dfy, float2 *dfz,
+                           float2 *dfleak, double *b, double *x, int init_x) {
     int4 bm = bmap[blockIdx.x];
     LevelDesc L = desc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -84,6 +86,10 @@ __global__ void k_assemble(const LevelDesc *__restrict__ desc, const int4 *__res
         }
         cx[i] = cp[0]; cy[i] = cp[1]; cz[i] = cp[2]; leak[i] = lk;
         if (fx) { fx[i] = (float)cp[0]; fy[i] = (float)cp[1]; fz[i] = (float)cp[2]; fleak[i] = (float)lk; }
+        if (dfx) {
+            dfx[i] = df_from_double(cp[0]); dfy[i] = df_from_double(cp[1]);
+            dfz[i] = df_from_double(cp[2]); dfleak[i] = df_from_double(lk);
+        }
         b[i] = rhs;
         if (init_x) x[i] = fi ? 0.0 : dh[i];
         else if (!fi) x[i] = dh[i];
@@ -187,6 +193,73 @@ __global__ void k_coarse_factor(const LevelDesc *__restrict__ desc, const int *_
     if (threadIdx.x == 0 && bad) atomicExch(status, 1);
 }
 
+// ---- per-cell bodies of the V-cycle steps, shared by the per-level kernels (one launch
+// per level, all problems) and the fused tail kernel (all small levels of one problem)
+
+// first Chebyshev step from a zero guess: x = d = invtheta D^-1 b
+template <typename T>
+__device__ __forceinline__ void cell_cheb_first(const LevelDesc &L, const Cell &c, const Coeffs<T> &C,
+                                                const T *__restrict__ b, T *__restrict__ x, T *__restrict__ d,
+                                                T invtheta) {
+    T v;
+    if constexpr (sizeof(T) == 8) v = invtheta * b[c.i] * C.idg[c.i];
+    else v = invtheta * __fdividef(b[c.i], diag7(L, c, C));
+    x[c.i] = v;
+    d[c.i] = v;
+}
+
+// the first two Chebyshev steps from a zero guess (see k_cheb_first2)
+template <typename T>
+__device__ __forceinline__ void cell_cheb_first2(const LevelDesc &L, const Cell &c, const Coeffs<T> &C,
+                                                 const T *__restrict__ b, T *__restrict__ xout, T *__restrict__ d,
+                                                 T invtheta, T c1, T c2) {
+    const T *__restrict__ g = C.idg;
+    const T bi = b[c.i], gi = g[c.i];
+    const T x1 = invtheta * bi * gi;
+    T Ax, dg;
+    apply7(L, c, C, x1, [&](long long j, int, int, int) { return invtheta * b[j] * g[j]; }, Ax, dg);
+    const T dn = c1 * x1 + c2 * (bi - Ax) * gi;
+    d[c.i] = dn;
+    xout[c.i] = x1 + dn;
+}
+
+// one Chebyshev step (see k_cheb_step); returns the new iterate
+template <typename T, bool FIRST>
+__device__ __forceinline__ T cell_cheb_step(const LevelDesc &L, const Cell &c, const Coeffs<T> &C,
+                                            const T *__restrict__ b, const T *__restrict__ xin,
+                                            T *__restrict__ xout, T *__restrict__ d, T c1, T c2, T &bi) {
+    T xi = xin[c.i], Ax, dg;
+    apply7(L, c, C, xi, [&](long long j, int, int, int) { return xin[j]; }, Ax, dg);
+    bi = b[c.i];
+    T r = dinv_times(C, c.i, bi - Ax, dg);
+    T dn = FIRST ? c2 * r : c1 * d[c.i] + c2 * r;
+    T xo = xi + dn;
+    d[c.i] = dn;
+    xout[c.i] = xo;
+    return xo;
+}
+
+// restricted residual of coarse cell cc: sum over its children i of b_i - (A x)_i
+template <typename T>
+__device__ __forceinline__ T cell_restrict(const LevelDesc &L, const Cell &cc, const Coeffs<T> &C,
+                                           const T *__restrict__ b, const T *__restrict__ x) {
+    const long long fsy = L.nz, fsx = (long long)L.ny * L.nz;
+    int x0 = 2 * cc.ix, y0 = 2 * cc.iy, z0 = 2 * cc.iz;
+    int x1 = min(x0 + 1, L.nx - 1), y1 = min(y0 + 1, L.ny - 1), z1 = min(z0 + 1, L.nz - 1);
+    T acc = 0;
+    for (int fx = x0; fx <= x1; fx++)
+        for (int fy = y0; fy <= y1; fy++)
+            for (int fz = z0; fz <= z1; fz++) {
+                Cell c;
+                c.ix = fx; c.iy = fy; c.iz = fz;
+                c.i = L.off + fx * fsx + fy * fsy + fz;
+                T xi = x[c.i], Ax, dg;
+                apply7(L, c, C, xi, [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
+                acc += b[c.i] - Ax;
+            }
+    return acc;
+}
+
 #define DPF_BLOCK_PROLOGUE(DESC, BMAP, ST)                 \
     int4 bm = (BMAP)[blockIdx.x];                          \
     const int p = bm.x;                                    \
@@ -202,11 +275,7 @@ __global__ void k_cheb_first(const LevelDesc *__restrict__ desc, const int4 *__r
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
         Cell c;
         cell_at(L, li_, c);
-        T v;
-        if constexpr (sizeof(T) == 8) v = invtheta * b[c.i] * C.idg[c.i];
-        else v = invtheta * __fdividef(b[c.i], diag7(L, c, C));
-        x[c.i] = v;
-        d[c.i] = v;
+        cell_cheb_first(L, c, C, b, x, d, invtheta);
     }
 }
 
@@ -219,17 +288,10 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 8 : 5) k_cheb_first2(
                               Coeffs<T> C, const T *__restrict__ b, T *__restrict__ xout, T *__restrict__ d,
                               T invtheta, T c1, T c2) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
-    const T *__restrict__ g = C.idg;
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
         Cell c;
         cell_at(L, li_, c);
-        const T bi = b[c.i], gi = g[c.i];
-        const T x1 = invtheta * bi * gi;
-        T Ax, dg;
-        apply7(L, c, C, x1, [&](long long j, int, int, int) { return invtheta * b[j] * g[j]; }, Ax, dg);
-        const T dn = c1 * x1 + c2 * (bi - Ax) * gi;
-        d[c.i] = dn;
-        xout[c.i] = x1 + dn;
+        cell_cheb_first2(L, c, C, b, xout, d, invtheta, c1, c2);
     }
 }
 
@@ -247,14 +309,8 @@ k_cheb_step(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, C
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
         Cell c;
         cell_at(L, li_, c);
-        T xi = xin[c.i], Ax, dg;
-        apply7(L, c, C, xi, [&](long long j, int, int, int) { return xin[j]; }, Ax, dg);
-        T bi = b[c.i];
-        T r = dinv_times(C, c.i, bi - Ax, dg);
-        T dn = FIRST ? c2 * r : c1 * d[c.i] + c2 * r;
-        T xo = xi + dn;
-        d[c.i] = dn;
-        xout[c.i] = xo;
+        T bi;
+        const T xo = cell_cheb_step<T, FIRST>(L, c, C, b, xin, xout, d, c1, c2, bi);
         if (FUSE_RZ) part = part + Acc<T>::prod(bi, xo);
     }
     if (FUSE_RZ) {
@@ -281,21 +337,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 8 : 5) k_restrict(con
         Cell cc;
         cell_at(Lc, li_, cc);
         const LevelDesc L = fdesc[p];
-        const long long fsy = L.nz, fsx = (long long)L.ny * L.nz;
-        int x0 = 2 * cc.ix, y0 = 2 * cc.iy, z0 = 2 * cc.iz;
-        int x1 = min(x0 + 1, L.nx - 1), y1 = min(y0 + 1, L.ny - 1), z1 = min(z0 + 1, L.nz - 1);
-        T acc = 0;
-        for (int fx = x0; fx <= x1; fx++)
-            for (int fy = y0; fy <= y1; fy++)
-                for (int fz = z0; fz <= z1; fz++) {
-                    Cell c;
-                    c.ix = fx; c.iy = fy; c.iz = fz;
-                    c.i = L.off + fx * fsx + fy * fsy + fz;
-                    T xi = x[c.i], Ax, dg;
-                    apply7(L, c, C, xi, [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
-                    acc += b[c.i] - Ax;
-                }
-        bc[cc.i] = acc;
+        bc[cc.i] = cell_restrict(L, cc, C, b, x);
     }
 }
 
@@ -349,6 +391,124 @@ __global__ void k_coarse_solve(const LevelDesc *__restrict__ desc, const int *__
             s.rz_old = s.rz;
             s.rz = rz;
             s.beta = (s.iters == 0 || s.rz_old == 0.0) ? 0.0 : s.rz / s.rz_old;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- fused tail
+// The small levels of one problem (from level `lt`, where the problem first has at most
+// tail_cells cells, down to its coarsest) run as one block: pre-smoothing, restriction,
+// the dense coarsest solve, prolongation and post-smoothing, with block barriers between
+// steps instead of kernel boundaries (on a 1M-cell grid this replaces about a dozen
+// launches of a few thousand cells each per V-cycle). Same arithmetic, same buffers
+// and the same result as the per-level kernels: the corrected iterate of level lt
+// lands in its xb buffer.
+template <typename T>
+struct TailLevel {
+    const LevelDesc *desc;
+    Coeffs<T> C;
+    T *xa, *xb, *b, *d;
+    const uint8_t *dir;
+};
+
+template <typename T>
+struct TailParams {
+    T c1[8], c2[8];  // Chebyshev recurrence coefficients, steps 0..deg-1
+    T invtheta, coarse_scale;
+    int deg;
+};
+
+constexpr int kTailThreads = 1024;
+
+template <typename T>
+__global__ void __launch_bounds__(kTailThreads) k_tail_cycle(const TailLevel<T> *__restrict__ tl,
+                                                             const int4 *__restrict__ tails, const CgState *st,
+                                                             const double *__restrict__ Inv, TailParams<T> tp) {
+    const int4 t = tails[blockIdx.x];  // problem, first tail level, coarsest level
+    const int p = t.x, lt = t.y, lc = t.z;
+    if (st && !st[p].active) return;
+    const int deg = tp.deg;
+    // descend
+    for (int l = lt; l < lc; l++) {
+        const TailLevel<T> V = tl[l];
+        const LevelDesc L = V.desc[p];
+        T *cur = V.xa, *oth = V.xb;
+        int k0 = 1;
+        if (deg >= 2) {
+            for (int li = threadIdx.x; li < (int)L.n; li += blockDim.x) {
+                Cell c;
+                cell_at(L, li, c);
+                cell_cheb_first2(L, c, V.C, V.b, V.xb, V.d, tp.invtheta, tp.c1[1], tp.c2[1]);
+            }
+            cur = V.xb;
+            oth = V.xa;
+            k0 = 2;
+        } else {
+            for (int li = threadIdx.x; li < (int)L.n; li += blockDim.x) {
+                Cell c;
+                cell_at(L, li, c);
+                cell_cheb_first(L, c, V.C, V.b, V.xa, V.d, tp.invtheta);
+            }
+        }
+        __syncthreads();
+        for (int k = k0; k < deg; k++) {
+            for (int li = threadIdx.x; li < (int)L.n; li += blockDim.x) {
+                Cell c;
+                cell_at(L, li, c);
+                T bi;
+                cell_cheb_step<T, false>(L, c, V.C, V.b, cur, oth, V.d, tp.c1[k], tp.c2[k], bi);
+            }
+            __syncthreads();
+            T *tmp = cur; cur = oth; oth = tmp;
+        }
+        const TailLevel<T> W = tl[l + 1];
+        const LevelDesc Lc = W.desc[p];
+        for (int li = threadIdx.x; li < (int)Lc.n; li += blockDim.x) {
+            Cell cc;
+            cell_at(Lc, li, cc);
+            W.b[cc.i] = cell_restrict(L, cc, V.C, V.b, cur);
+        }
+        __syncthreads();
+    }
+    // coarsest: x = A^-1 b with the stored dense inverse
+    {
+        const TailLevel<T> V = tl[lc];
+        const LevelDesc L = V.desc[p];
+        const double *Ip = Inv + (long long)p * kMaxCoarse * kMaxCoarse;
+        const int i = threadIdx.x;
+        if (i < (int)L.n) {
+            double xi = 0.0;
+            for (int j = 0; j < (int)L.n; j++) xi += Ip[j * kMaxCoarse + i] * (double)V.b[L.off + j];
+            V.xb[L.off + i] = (T)xi;
+        }
+        __syncthreads();
+    }
+    // ascend: prolongation in place into the pre-smoothed iterate, then deg steps
+    for (int l = lc - 1; l >= lt; l--) {
+        const TailLevel<T> V = tl[l];
+        const LevelDesc L = V.desc[p];
+        const TailLevel<T> W = tl[l + 1];
+        const LevelDesc Lc = W.desc[p];
+        T *cur = (deg % 2 == 0) ? V.xb : V.xa;  // where pre-smoothing left its iterate
+        for (int li = threadIdx.x; li < (int)L.n; li += blockDim.x) {
+            Cell c;
+            cell_at(L, li, c);
+            if (V.dir[c.i]) continue;
+            cur[c.i] += tp.coarse_scale *
+                        W.xb[Lc.off + ((long long)(c.ix >> 1) * Lc.ny + (c.iy >> 1)) * Lc.nz + (c.iz >> 1)];
+        }
+        __syncthreads();
+        for (int k = 0; k < deg; k++) {
+            T *o = cur == V.xa ? V.xb : V.xa;
+            for (int li = threadIdx.x; li < (int)L.n; li += blockDim.x) {
+                Cell c;
+                cell_at(L, li, c);
+                T bi;
+                if (k == 0) cell_cheb_step<T, true>(L, c, V.C, V.b, cur, o, V.d, tp.c1[0], tp.invtheta, bi);
+                else cell_cheb_step<T, false>(L, c, V.C, V.b, cur, o, V.d, tp.c1[k], tp.c2[k], bi);
+            }
+            __syncthreads();
+            cur = o;
         }
     }
 }
@@ -509,20 +669,24 @@ __global__ void __launch_bounds__(kBlock, 8) k_df_spmv_pq(const LevelDesc *__res
     }
 }
 
-// x += alpha p; r -= alpha q (double-float); r32 = leading float of r for the V-cycle;
-// convergence test on the recursive residual (r is normalised by `scale`)
+// x64 += (alpha scale) p in FP64 (the solution keeps all 53 bits: a 48-bit double-float
+// solution would put the FP64 check's floor 32x higher and cost extra rounds);
+// r -= alpha q (double-float); r32 = leading float of r for the V-cycle; convergence test
+// on the recursive residual (r is normalised by `scale`)
 __global__ void k_df_update_xr(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                                int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo,
-                               float2 *__restrict__ x, float2 *__restrict__ r, float *__restrict__ r32,
+                               double *__restrict__ x64, float2 *__restrict__ r, float *__restrict__ r32,
                                const float2 *__restrict__ pv, const float2 *__restrict__ q, int maxiter) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     const float2 a = df_from_double(st[p].alpha);
+    const double as = st[p].alpha * st[p].scale;
     Acc<float> part;
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
         Cell c;
         cell_at(L, li_, c);
         const long long i = c.i;
-        x[i] = df_add(x[i], df_mul(a, pv[i]));
+        const float2 pi = pv[i];
+        x64[i] = fma(as, (double)pi.x + (double)pi.y, x64[i]);
         const float2 ri = df_sub(r[i], df_mul(a, q[i]));
         r[i] = ri;
         r32[i] = ri.x;
@@ -556,34 +720,53 @@ __global__ void k_df_update_p(const LevelDesc *__restrict__ desc, const int4 *__
 }
 
 // True residual r64 = b - A x64 in FP64 flux form; decides whether a (further) round is
-// needed. FIRST: the start of a solve.
-template <bool FIRST>
+// needed. FIRST: the start of a solve. ZERO (with FIRST): the initial guess is zero on
+// free cells and the Dirichlet value on identity rows, so r = b on free rows and 0 on
+// identity rows (free rows have no coupling to identity rows) and no product is formed.
+template <bool FIRST, bool ZERO = false>
 __global__ void k_df_residual(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                               int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo,
-                              Coeffs<double> C, const double *__restrict__ b, const double *__restrict__ x,
-                              double *__restrict__ r, double tol2, int maxiter, int max_rounds) {
+                              Coeffs<double> C, const uint8_t *__restrict__ dir, const double *__restrict__ b,
+                              const double *__restrict__ x, double *__restrict__ r, double tol2, int maxiter,
+                              int max_rounds) {
     int4 bm = bmap[blockIdx.x];
     const int p = bm.x;
     if (!FIRST && st[p].ru_flag == 0) return;  // finished in an earlier round
     const LevelDesc L = desc[p];
-    Acc<double> rr, bb;
+    Acc<double> rr, bb;  // FIRST: |r|^2, |b|^2; otherwise |r|^2 and the rounding floor
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
         Cell c;
-        cell_at(L, li_, c);
-        double xi = x[c.i], Ax, dg;
-        apply7(L, c, C, xi, [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
-        double bi = b[c.i];
-        double ri = bi - Ax;
+        double ri, bi, xi = 0.0, dg = 0.0;
+        if (ZERO) {
+            c.i = L.off + li_;
+            bi = b[c.i];
+            ri = dir[c.i] ? 0.0 : bi;
+        } else {
+            cell_at(L, li_, c);
+            xi = x[c.i];
+            double Ax;
+            apply7(L, c, C, xi, [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
+            bi = b[c.i];
+            ri = bi - Ax;
+        }
         r[c.i] = ri;
         rr.v += ri * ri;
-        if (FIRST) bb.v += bi * bi;
+        if (FIRST) {
+            bb.v += bi * bi;
+        } else {
+            // rounding bound of b_i - (A x)_i in FP64, and of storing x itself:
+            // u (|b_i| + 2 diag_i |x_i|), u = 2^-53 (neighbours of x_i taken as |x_i|)
+            const double f = 0x1p-53 * fma(2.0 * dg, fabs(xi), fabs(bi));
+            bb.v += f * f;
+        }
     }
     double2 tot;
-    if (reduce_last<double, FIRST ? 2 : 1>(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
+    if (reduce_last<double, 2>(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
         CgState &s = st[p];
         s.orr = tot.x;
         bool go;
         if (FIRST) {
+            s.floor2 = 0.0;
             s.obb = tot.y;
             s.tol2 = tol2;
             s.status = DPF_OK;
@@ -594,12 +777,14 @@ __global__ void k_df_residual(const LevelDesc *__restrict__ desc, const int4 *__
             if (!isfinite(s.orr)) { s.status = DPF_NAN; go = false; }
         } else {
             s.outer++;
-            // a round that did not even halve the true residual means it sits at the FP64
-            // rounding floor of b - A x (no further accuracy exists): accept it
-            const bool stalled = s.orr > 0.25 * s.orr_prev;
+            s.floor2 = tot.y;
+            // the true residual is at the FP64 rounding floor of b - A x when it is within the
+            // floor's bound, or when a whole round did not even halve it: no further accuracy
+            // exists in FP64, so the solve is accepted there
+            const bool at_floor = s.orr <= s.floor2 || s.orr > 0.25 * s.orr_prev;
             go = true;
             if (!isfinite(s.orr)) { s.status = DPF_NAN; go = false; }
-            else if (s.orr <= tol2 * s.obb || stalled) go = false;
+            else if (s.orr <= tol2 * s.obb || at_floor) go = false;
             else if (s.total_iters >= maxiter || s.outer >= max_rounds) { s.status = DPF_NOT_CONVERGED; go = false; }
         }
         s.orr_prev = s.orr;
@@ -616,10 +801,9 @@ __global__ void k_df_residual(const LevelDesc *__restrict__ desc, const int4 *__
     }
 }
 
-// start of a round: r = r64 / scale (double-float and its leading float), x = 0
+// start of a round: r = r64 / scale (double-float and its leading float)
 __global__ void k_df_begin(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, const CgState *st,
-                           const double *__restrict__ r64, float2 *__restrict__ r, float *__restrict__ r32,
-                           float2 *__restrict__ x) {
+                           const double *__restrict__ r64, float2 *__restrict__ r, float *__restrict__ r32) {
     int4 bm = bmap[blockIdx.x];
     const int p = bm.x;
     if (!st[p].ru_flag) return;
@@ -630,35 +814,6 @@ __global__ void k_df_begin(const LevelDesc *__restrict__ desc, const int4 *__res
         const float2 v = df_from_double(r64[i] * inv);
         r[i] = v;
         r32[i] = v.x;
-        x[i] = make_float2(0.0f, 0.0f);
-    }
-}
-
-// end of a round: x64 += scale * x
-__global__ void k_df_end(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, const CgState *st,
-                         const float2 *__restrict__ x, double *__restrict__ x64) {
-    int4 bm = bmap[blockIdx.x];
-    const int p = bm.x;
-    if (!st[p].ru_flag) return;
-    const LevelDesc L = desc[p];
-    const double sc = st[p].scale;
-    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
-        const long long i = L.off + li_;
-        x64[i] += sc * df_to_double(x[i]);
-    }
-}
-
-// double-float copy of the finest FP64 operator
-__global__ void k_df_coeffs(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, Coeffs<double> C,
-                            float2 *cx, float2 *cy, float2 *cz, float2 *leak) {
-    int4 bm = bmap[blockIdx.x];
-    const LevelDesc L = desc[bm.x];
-    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
-        const long long i = L.off + li_;
-        cx[i] = df_from_double(C.cx[i]);
-        cy[i] = df_from_double(C.cy[i]);
-        cz[i] = df_from_double(C.cz[i]);
-        leak[i] = df_from_double(C.leak[i]);
     }
 }
 
@@ -765,6 +920,25 @@ __global__ void k_grad_logk(const LevelDesc *__restrict__ desc, const int4 *__re
         const int nn[3] = {L.nx, L.ny, L.nz};
         const double hi = h[c.i], li = lam[c.i], ki = kc[c.i];
         double acc = 0.0;
+        if (kind == DPF_MEAN_GEOMETRIC) {
+            // dK_f/dlogK_i = K_f / 2 = kc_i kc_j / 2: per direction sum kc_j (h_i-h_j)(l_i-l_j),
+            // then scale by -aol kc_i / 2 (4 FP64 operations per face)
+    #pragma unroll
+            for (int d = 0; d < 3; d++) {
+                double sd = 0.0;
+                if (co[d] + 1 < nn[d]) {
+                    const long long j = c.i + st3[d];
+                    sd = fma(kc[j], (hi - h[j]) * (li - lam[j]), sd);
+                }
+                if (co[d] > 0) {
+                    const long long j = c.i - st3[d];
+                    sd = fma(kc[j], (hi - h[j]) * (li - lam[j]), sd);
+                }
+                acc = fma(-0.5 * P.aol[d] * ki, sd, acc);
+            }
+            g[c.i] = acc;
+            continue;
+        }
     #pragma unroll
         for (int d = 0; d < 3; d++) {
     #pragma unroll
@@ -803,9 +977,13 @@ __global__ void k_invdiag(const LevelDesc *__restrict__ desc, const int4 *__rest
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
         Cell c;
         cell_at(L, li_, c);
-        double v = 1.0 / diag7(L, c, C);
-        if (idg) idg[c.i] = v;
-        if (idg32) idg32[c.i] = (float)v;
+        if (idg) {
+            const double v = 1.0 / diag7(L, c, C);
+            idg[c.i] = v;
+            if (idg32) idg32[c.i] = (float)v;
+        } else {
+            idg32[c.i] = 1.0f / (float)diag7(L, c, C);  // smoother only: FP32 division suffices
+        }
     }
 }
 
@@ -921,7 +1099,8 @@ template <typename T>
 static T *dalloc(size_t n, std::vector<void *> &owned) {
     void *p = nullptr;
     if (n == 0) n = 1;
-    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+    // 64 bytes of padding: bulk copies widen their ranges to 16-byte boundaries
+    cudaError_t e = cudaMalloc(&p, n * sizeof(T) + 64);
     if (e != cudaSuccess) {
         cudaGetLastError();
         throw OomError(std::string("cudaMalloc of ") + std::to_string(n * sizeof(T)) + " bytes failed");
@@ -968,6 +1147,58 @@ static BlockMap build_map(const std::vector<LevelDesc> &desc, const std::vector<
     return m;
 }
 
+// Plane-marching work items of a level: per smoothed problem, slabs of Ty = 256 / nz rows
+// (whole rows, so a slab is contiguous in every array) times chunks of x-planes, with the
+// chunk length chosen so that all items fill the device about once.
+void StructBatch::build_plane_items(Level &L, const std::vector<int> &smooth, int sms,
+                                    const std::vector<std::vector<std::array<int, 3>>> *shapes, int l) {
+    L.pm_ok = false;
+    // FP32 V-cycles only: with 8-byte values the stages of a 768-cell slab allow one block
+    // per SM, and the FP64 smoothers are faster as grid-stride kernels
+    if (opt.plane <= 0 || !mixed) return;
+    long long total = 0;
+    for (int p = 0; p < nprob; p++) {
+        if (!smooth[p]) continue;
+        const LevelDesc &D = L.h_desc[p];
+        if (D.nz > kPlaneCells) return;  // a row must fit a slab
+        total += D.n;
+    }
+    if (total == 0) return;
+#ifndef DPF_PLANE_BPSM
+#define DPF_PLANE_BPSM 2
+#endif
+    const long long target = (long long)sms * DPF_PLANE_BPSM;
+    std::vector<int4> items;
+    std::vector<int2> pinfo(nprob, make_int2(0, 0));
+    for (int p = 0; p < nprob; p++) {
+        if (!smooth[p]) continue;
+        const LevelDesc &D = L.h_desc[p];
+        const int Ty = std::max(1, std::min(D.ny, kPlaneCells / D.nz));
+        const int ytiles = (D.ny + Ty - 1) / Ty;
+        long long chunks = (long long)((double)target * (double)D.n / (double)total / ytiles);
+        chunks = std::max(1LL, std::min(chunks, (long long)D.nx));
+        int xc = (int)((D.nx + chunks - 1) / chunks);
+        xc = std::max(xc, std::min(2, D.nx));
+        pinfo[p].x = (int)items.size();
+        for (int y0 = 0; y0 < D.ny; y0 += Ty)
+            for (int x0 = 0; x0 < D.nx; x0 += xc) items.push_back(make_int4(p, y0, x0, std::min(x0 + xc, D.nx)));
+        pinfo[p].y = (int)items.size() - pinfo[p].x;
+        L.pm_halo = std::max(L.pm_halo, (Ty + 2) * D.nz);
+        L.pm_cy = std::max(L.pm_cy, (Ty + 1) * D.nz);
+        L.pm_slab = std::max(L.pm_slab, Ty * D.nz);
+        if (shapes) {
+            const int cnz = (*shapes)[p][l + 1][2];
+            L.pm_coarse = std::max(L.pm_coarse, ((Ty + 2) / 2 + 2) * cnz);
+        }
+    }
+    L.pm_nitems = (int)items.size();
+    L.pm_items = dalloc<int4>(items.size(), owned);
+    L.pm_pinfo = dalloc<int2>(nprob, owned);
+    CK(cudaMemcpy(L.pm_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(L.pm_pinfo, pinfo.data(), nprob * sizeof(int2), cudaMemcpyHostToDevice));
+    L.pm_ok = true;
+}
+
 StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<std::vector<int64_t>> &dnodes,
                          const dpf_options &o, cudaStream_t s)
     : opt(o), stream(s) {
@@ -1000,6 +1231,17 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const long long target_blocks = (long long)sms * std::max(1, opt.blocks_per_sm);
+    // fused tail: from the first level (>= 1) at which a problem has at most tail_cells cells
+    std::vector<int> tail_at(nprob);
+    for (int p = 0; p < nprob; p++) {
+        tail_at[p] = nlev[p];  // none
+        if (opt.tail_cells <= 0 || nlev[p] < 2) continue;
+        for (int l = 1; l < nlev[p]; l++) {
+            auto d = shapes[p][l];
+            if ((long long)d[0] * d[1] * d[2] <= opt.tail_cells) { tail_at[p] = l; break; }
+        }
+        if (tail_at[p] < nlev[p]) tails.push_back(make_int4(p, tail_at[p], nlev[p] - 1, 0));
+    }
     // level descriptors
     lv.resize(nlev_max);
     int maxblocks = 0;
@@ -1010,7 +1252,7 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         fast_div_magic(1u, unit.mag_ny, unit.sh_ny);
         L.h_desc.assign(nprob, unit);
         long long off = 0;
-        std::vector<int> has(nprob, 0), smooth(nprob, 0);
+        std::vector<int> has(nprob, 0), smooth(nprob, 0), restr(nprob, 0);
         for (int p = 0; p < nprob; p++) {
             if (l >= nlev[p]) continue;
             auto d = shapes[p][l];
@@ -1024,23 +1266,38 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
             check_fast_div((unsigned)d[1], D.mag_ny, D.sh_ny, (unsigned)(D.n / d[2]));
             off += D.n;
             has[p] = 1;
-            smooth[p] = l < nlev[p] - 1;
-            if (l == nlev[p] - 1) L.coarse_list.push_back(p);
+            smooth[p] = l < nlev[p] - 1 && l < tail_at[p];
+            restr[p] = l >= 1 && l <= tail_at[p];
+            if (l == nlev[p] - 1) {
+                L.coarse_list.push_back(p);
+                if (tail_at[p] == nlev[p]) {
+                    L.csolve_list.push_back(p);
+                    L.csolve_cells += D.n;
+                }
+            }
+            if (l == tail_at[p]) tail_cells_total += D.n;
         }
         L.ntot = off;
         L.d_desc = dalloc<LevelDesc>(nprob, owned);
         CK(cudaMemcpy(L.d_desc, L.h_desc.data(), nprob * sizeof(LevelDesc), cudaMemcpyHostToDevice));
         L.all = build_map(L.h_desc, has, owned, nprob, target_blocks);
         L.smooth = build_map(L.h_desc, smooth, owned, nprob, target_blocks);
+        L.restr = build_map(L.h_desc, restr, owned, nprob, target_blocks);
+        build_plane_items(L, smooth, sms, (l + 1 < nlev_max) ? &shapes : nullptr, l);
         for (int p = 0; p < nprob; p++) {
             if (has[p]) L.all_cells += L.h_desc[p].n;
             if (smooth[p]) L.smooth_cells += L.h_desc[p].n;
-            if (has[p] && !smooth[p]) L.coarse_cells += L.h_desc[p].n;
+            if (restr[p]) L.restr_cells += L.h_desc[p].n;
+            if (has[p] && l == nlev[p] - 1) L.coarse_cells += L.h_desc[p].n;
         }
-        maxblocks = std::max(maxblocks, L.all.nblocks);
+        maxblocks = std::max(maxblocks, std::max(L.all.nblocks, L.pm_nitems));
         L.d_coarse = dalloc<int>(L.coarse_list.size(), owned);
         if (!L.coarse_list.empty())
             CK(cudaMemcpy(L.d_coarse, L.coarse_list.data(), L.coarse_list.size() * sizeof(int),
+                          cudaMemcpyHostToDevice));
+        L.d_csolve = dalloc<int>(L.csolve_list.size(), owned);
+        if (!L.csolve_list.empty())
+            CK(cudaMemcpy(L.d_csolve, L.csolve_list.data(), L.csolve_list.size() * sizeof(int),
                           cudaMemcpyHostToDevice));
         size_t n = (size_t)L.ntot;
         L.dir = dalloc<uint8_t>(n, owned);
@@ -1113,18 +1370,25 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         for (int k = 0; k < 4; k++) cgv[k] = dalloc<double>(N, owned);  // r, z, p, q
     } else {
         for (int k = 0; k < 2; k++) cgv[k] = dalloc<float>(N, owned);   // r32, z32
-        for (int k = 0; k < 4; k++) dfv[k] = dalloc<float2>(N, owned);  // x, r, p, q (double-float)
+        for (int k = 1; k < 4; k++) dfv[k] = dalloc<float2>(N, owned);  // r, p, q (double-float)
         for (int k = 0; k < 4; k++) cdf[k] = dalloc<float2>(N, owned);  // finest operator (double-float)
     }
     // state, reductions, coarse factors
     d_state = dalloc<CgState>(nprob, owned);
     d_count = dalloc<int>(4, owned);
-    d_factor_status = dalloc<int>(1, owned);
+    d_factor_status = dalloc<int>(2, owned);
+    CK(cudaMemset(d_factor_status, 0, 2 * sizeof(int)));
     rs.partials = dalloc<double2>(std::max(maxblocks, 1), owned);
     rs.tickets = dalloc<unsigned>(nprob, owned);
     rs.capacity = maxblocks;
     CK(cudaMemset(rs.tickets, 0, nprob * sizeof(unsigned)));
     d_coarseL = dalloc<double>((size_t)nprob * kMaxCoarse * kMaxCoarse, owned);
+    if (!tails.empty()) {
+        d_tails = dalloc<int4>(tails.size(), owned);
+        CK(cudaMemcpy(d_tails, tails.data(), tails.size() * sizeof(int4), cudaMemcpyHostToDevice));
+        tail_first_level = nlev_max;
+        for (auto &t : tails) tail_first_level = std::min(tail_first_level, t.y);
+    }
     CK(cudaMallocHost(&h_count, 4 * sizeof(int)));
     CK(cudaMallocHost(&h_state_buf, nprob * sizeof(CgState)));
     // Chebyshev coefficients on D^-1 A over [lo*2, 2] (Gershgorin: the spectrum of
@@ -1234,7 +1498,8 @@ void StructBatch::assemble(const double *Ks, const double *kc, int kind, const d
             k_assemble<<<nb_of(L0.all), kBlock, 0, stream>>>(
                 L0.d_desc, L0.all.d_map, d_prm, fk, in_dh, in_Q, shift, L0.dir, L0.c64[0], L0.c64[1], L0.c64[2],
                 L0.c64[3], mixed ? L0.c32[0] : nullptr, mixed ? L0.c32[1] : nullptr, mixed ? L0.c32[2] : nullptr,
-                mixed ? L0.c32[3] : nullptr, b64, h, init_x ? 1 : 0);
+                mixed ? L0.c32[3] : nullptr, mixed ? cdf[0] : nullptr, mixed ? cdf[1] : nullptr,
+                mixed ? cdf[2] : nullptr, mixed ? cdf[3] : nullptr, b64, h, init_x ? 1 : 0);
         }
     LAUNCH_CHECK();
     for (int l = 0; l + 1 < nlev_max; l++) {
@@ -1270,18 +1535,73 @@ void StructBatch::assemble(const double *Ks, const double *kc, int kind, const d
         }
         LAUNCH_CHECK();
     }
-    if (mixed) {
-        {
-            KTimer _kt(this, kname("k_df_coeffs", 0, false), L0.all_cells);
-            k_df_coeffs<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, coeffs_of<double>(L0, true),
-                                                             cdf[0], cdf[1], cdf[2], cdf[3]);
-        }
-        LAUNCH_CHECK();
-    }
     have_operator = true;
 }
 
 // ---- V-cycle: z = M r on the fine level (vector precision T)
+// ---- plane-marching launches
+static int pm_region(int count, int es) { return ((count * es + 32) + 15) & ~15; }
+
+template <typename T, int MODE>
+static void pm_kernel(unsigned nblocks, size_t smem, cudaStream_t stream, const LevelDesc *desc,
+                      const LevelDesc *cdesc, const int4 *items, CgState *st, Coeffs<T> C, const T *b,
+                      const T *xin, T *xout, T *d, const uint8_t *dir, const T *e, T c1, T c2, T invth, T sc,
+                      PlaneLayout lay, ReduceScratch rs, const int2 *pinfo, int *err) {
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        CK(cudaFuncSetAttribute(k_pm_cheb<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = smem;
+    }
+    k_pm_cheb<T, MODE><<<nblocks, kPlaneThreads + 32, smem, stream>>>(desc, cdesc, items, st, C, b, xin, xout, d, dir, e,
+                                                                  c1, c2, invth, sc, lay, rs, pinfo, err);
+}
+
+// One plane-marching Chebyshev launch over the smoothed problems of level l (mode: PM_* bits).
+template <typename T>
+void StructBatch::pm_launch(int mode, int l, const T *b, const T *xin, T *xout, T *d, const T *e, T c1, T c2,
+                            T invth, T sc) {
+    Level &L = lv[l];
+    const int es = (int)sizeof(T);
+    PlaneLayout lay{};
+    int off = 0;
+    auto take = [&](int bytes) { int o = off; off += bytes; return o; };
+    const bool f2 = mode & PM_FIRST2, first = mode & PM_FIRST, prol = mode & PM_PROLONG;
+    lay.oX = f2 ? -1 : take(pm_region(L.pm_halo, es));
+    lay.oB = take(pm_region(f2 ? L.pm_halo : L.pm_slab, es));
+    lay.oD = (f2 || first) ? -1 : take(pm_region(L.pm_slab, es));
+    lay.oG = f2 ? take(pm_region(L.pm_halo, es)) : -1;
+    lay.oCX = take(pm_region(L.pm_slab, es));
+    lay.oCY = take(pm_region(L.pm_cy, es));
+    lay.oCZ = take(pm_region(L.pm_slab, es));
+    lay.oLK = take(pm_region(L.pm_slab, es));
+    lay.oDIR = prol ? take(pm_region(L.pm_halo, 1)) : -1;
+    lay.oE = prol ? take(pm_region(L.pm_coarse, es)) : -1;
+    lay.slot_bytes = (off + 127) & ~127;
+    const size_t smem = (size_t)kPlaneStages * lay.slot_bytes;
+    Coeffs<T> C = coeffs_of<T>(L, mixed);
+    const LevelDesc *cd = l + 1 < nlev_max ? lv[l + 1].d_desc : nullptr;
+    const unsigned nb = (unsigned)L.pm_nitems;
+    int *err = d_factor_status + 1;
+#define DPF_PM_CASE(M)                                                                                           \
+    case M:                                                                                                      \
+        pm_kernel<T, M>(nb, smem, stream, L.d_desc, cd, L.pm_items, d_state, C, b, xin, xout, d, L.dir, e, c1, c2, \
+                        invth, sc, lay, rs, L.pm_pinfo, err);                                                     \
+        break;
+    switch (mode) {
+        DPF_PM_CASE(PM_FIRST2)
+        DPF_PM_CASE(PM_FIRST2 | PM_NOD)
+        DPF_PM_CASE(0)
+        DPF_PM_CASE(PM_NOD)
+        DPF_PM_CASE(PM_PROLONG | PM_FIRST)
+        DPF_PM_CASE(PM_PROLONG | PM_FIRST | PM_NOD)
+        DPF_PM_CASE(PM_PROLONG | PM_FIRST | PM_NOD | PM_RZ)
+        DPF_PM_CASE(PM_NOD | PM_RZ)
+        default:
+            throw std::logic_error("unsupported plane kernel mode");
+    }
+#undef DPF_PM_CASE
+}
+
 template <typename T>
 void StructBatch::vcycle(const T *r, T *z) {
     const int deg = opt.cheb_degree;
@@ -1293,7 +1613,33 @@ void StructBatch::vcycle(const T *r, T *z) {
         Coeffs<T> C = coeffs_of<T>(L, mixed);
         const T *b = l == 0 ? r : (const T *)L.work[2];
         T *xa = (T *)L.work[0], *xb = (T *)L.work[1], *d = (T *)L.work[3];
-        if (nb_of(L.smooth)) {
+        if (nb_of(L.smooth) && L.pm_ok && deg >= 2) {
+            // plane-marching pre-smoothing: two fused first steps, then the rest
+            {
+                KTimer _kt(this, kname("k_pm_first2", l, sizeof(T) == 4), L.smooth_cells);
+                pm_launch<T>(deg == 2 ? (PM_FIRST2 | PM_NOD) : PM_FIRST2, l, b, nullptr, xb, d, nullptr,
+                             (T)cheb_c1[1], (T)cheb_c2[1], invth, sc);
+            }
+            LAUNCH_CHECK();
+            T *cur = xb, *oth = xa;
+            for (int k = 2; k < deg; k++) {
+                {
+                    KTimer _kt(this, kname("k_pm_step", l, sizeof(T) == 4), L.smooth_cells);
+                    pm_launch<T>(k == deg - 1 ? PM_NOD : 0, l, b, cur, oth, d, nullptr, (T)cheb_c1[k],
+                                 (T)cheb_c2[k], invth, sc);
+                }
+                LAUNCH_CHECK();
+                std::swap(cur, oth);
+            }
+            pre[l] = cur;
+            Level &Cn = lv[l + 1];
+            {
+                KTimer _kt(this, kname("k_restrict", l + 1, sizeof(T) == 4), Cn.restr_cells);
+                k_restrict<T><<<nb_of(Cn.restr), kBlock, 0, stream>>>(L.d_desc, Cn.d_desc, Cn.restr.d_map, d_state, C, b,
+                                                                     cur, (T *)Cn.work[2]);
+            }
+            LAUNCH_CHECK();
+        } else if (nb_of(L.smooth)) {
             T *cur = xa, *oth = xb;
             int k0 = 1;
             if (deg >= 2) {
@@ -1329,30 +1675,57 @@ void StructBatch::vcycle(const T *r, T *z) {
             pre[l] = cur;
             Level &Cn = lv[l + 1];
             {
-                KTimer _kt(this, kname("k_restrict", l + 1, sizeof(T) == 4), Cn.all_cells);
-                k_restrict<T><<<nb_of(Cn.all), kBlock, 0, stream>>>(L.d_desc, Cn.d_desc, Cn.all.d_map, d_state, C, b,
+                KTimer _kt(this, kname("k_restrict", l + 1, sizeof(T) == 4), Cn.restr_cells);
+                k_restrict<T><<<nb_of(Cn.restr), kBlock, 0, stream>>>(L.d_desc, Cn.d_desc, Cn.restr.d_map, d_state, C, b,
                                                                    cur, (T *)Cn.work[2]);
             }
             LAUNCH_CHECK();
         }
-        if (!L.coarse_list.empty()) {
+        if (!L.csolve_list.empty()) {
             // the coarse solution goes where the post-smoother of this level would
             // leave its result: work[1] (always, see below), or z on the finest level
             T *out = l == 0 ? z : xb;
             if (l == 0)
                 {
-                    KTimer _kt(this, kname("k_coarse_solve", l, sizeof(T) == 4), L.coarse_cells);
-                    k_coarse_solve<T, true><<<(unsigned)L.coarse_list.size(), kMaxCoarse, 0, stream>>>(
-                        L.d_desc, L.d_coarse, d_state, d_coarseL, b, out);
+                    KTimer _kt(this, kname("k_coarse_solve", l, sizeof(T) == 4), L.csolve_cells);
+                    k_coarse_solve<T, true><<<(unsigned)L.csolve_list.size(), kMaxCoarse, 0, stream>>>(
+                        L.d_desc, L.d_csolve, d_state, d_coarseL, b, out);
                 }
             else
                 {
-                    KTimer _kt(this, kname("k_coarse_solve", l, sizeof(T) == 4), L.coarse_cells);
-                    k_coarse_solve<T, false><<<(unsigned)L.coarse_list.size(), kMaxCoarse, 0, stream>>>(
-                        L.d_desc, L.d_coarse, d_state, d_coarseL, b, out);
+                    KTimer _kt(this, kname("k_coarse_solve", l, sizeof(T) == 4), L.csolve_cells);
+                    k_coarse_solve<T, false><<<(unsigned)L.csolve_list.size(), kMaxCoarse, 0, stream>>>(
+                        L.d_desc, L.d_csolve, d_state, d_coarseL, b, out);
                 }
             LAUNCH_CHECK();
         }
+    }
+    // the small levels: one fused block per problem
+    if (!tails.empty()) {
+        if (!d_tail_lv) {
+            std::vector<TailLevel<T>> tab(nlev_max);
+            for (int l = 0; l < nlev_max; l++) {
+                Level &L = lv[l];
+                tab[l] = TailLevel<T>{L.d_desc, coeffs_of<T>(L, mixed), (T *)L.work[0], (T *)L.work[1],
+                                      (T *)L.work[2], (T *)L.work[3], L.dir};
+            }
+            d_tail_lv = dalloc<TailLevel<T>>(nlev_max, owned);
+            CK(cudaMemcpy(d_tail_lv, tab.data(), nlev_max * sizeof(TailLevel<T>), cudaMemcpyHostToDevice));
+        }
+        TailParams<T> tp{};
+        for (int k = 0; k < deg && k < 8; k++) {
+            tp.c1[k] = (T)cheb_c1[k];
+            tp.c2[k] = (T)cheb_c2[k];
+        }
+        tp.invtheta = invth;
+        tp.coarse_scale = sc;
+        tp.deg = deg;
+        {
+            KTimer _kt(this, kname("k_tail_cycle", tail_first_level, sizeof(T) == 4), tail_cells_total);
+            k_tail_cycle<T><<<(unsigned)tails.size(), kTailThreads, 0, stream>>>(
+                (const TailLevel<T> *)d_tail_lv, d_tails, d_state, d_coarseL, tp);
+        }
+        LAUNCH_CHECK();
     }
     // ascend: the coarse correction is added in place to the pre-smoothed iterate, then
     // deg Chebyshev steps alternate buffers. Pre-smoothing wrote deg iterates starting in
@@ -1367,6 +1740,25 @@ void StructBatch::vcycle(const T *r, T *z) {
         T *xa = (T *)L.work[0], *xb = (T *)L.work[1], *d = (T *)L.work[3];
         T *cur = pre[l];
         const T *e = (const T *)Cn.work[1];
+        if (L.pm_ok && deg >= 2) {
+            // plane-marching post-smoothing: prolongation fused into the first step; the
+            // last step writes no direction (and on the finest level also forms r . z)
+            for (int k = 0; k < deg; k++) {
+                const bool last = k == deg - 1;
+                T *o = (l == 0 && last) ? z : (cur == xa ? xb : xa);
+                int mode = k == 0 ? (PM_PROLONG | PM_FIRST) : 0;
+                if (last) mode |= PM_NOD;
+                if (last && l == 0) mode |= PM_RZ;
+                {
+                    KTimer _kt(this, kname(k == 0 ? "k_pm_prolong_step" : "k_pm_step", l, sizeof(T) == 4),
+                               L.smooth_cells);
+                    pm_launch<T>(mode, l, b, cur, o, d, e, (T)cheb_c1[k], k == 0 ? invth : (T)cheb_c2[k], invth, sc);
+                }
+                LAUNCH_CHECK();
+                cur = o;
+            }
+            continue;
+        }
         {
             KTimer _kt(this, kname("k_prolong_add", l, sizeof(T) == 4), L.smooth_cells);
             k_prolong_add<T><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, Cn.d_desc, L.smooth.d_map, d_state,
@@ -1437,7 +1829,7 @@ void StructBatch::pcg_iteration(T *x) {
 
 // One iteration of the mixed-precision CG: double-float q = A p, alpha, x/r update,
 // FP32 V-cycle on the rounded residual, double-float p update.
-void StructBatch::df_iteration() {
+void StructBatch::df_iteration(double *x64) {
     Level &L0 = lv[0];
     const unsigned nb = nb_of(L0.all);
     float *r32 = (float *)cgv[0], *z32 = (float *)cgv[1];
@@ -1451,7 +1843,7 @@ void StructBatch::df_iteration() {
     {
         KTimer _kt(this, kname("k_df_update_xr", 0, true), L0.all_cells);
         k_df_update_xr<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo,
-                                                  dfv[0], dfv[1], r32, dfv[2], dfv[3], opt.maxiter);
+                                                  x64, dfv[1], r32, dfv[2], dfv[3], opt.maxiter);
     }
     LAUNCH_CHECK();
     vcycle<float>(r32, z32);
@@ -1497,7 +1889,7 @@ cudaGraphExec_t StructBatch::loop_graph(int kind, void *x) {
     }
     try {
         if (kind == 0) pcg_iteration<double>((double *)x);
-        else df_iteration();
+        else df_iteration((double *)x);
         k_loop_cond<<<1, 1, 0, stream>>>(cond, d_count, d_count + 2, opt.maxiter);
         launches++;
         LAUNCH_CHECK();
@@ -1532,7 +1924,7 @@ void StructBatch::run_loop(int kind, void *x) {
     const int check = std::max(1, opt.check_every);
     for (int it = 1; it <= opt.maxiter + 1; it++) {
         if (kind == 0) pcg_iteration<double>((double *)x);
-        else df_iteration();
+        else df_iteration((double *)x);
         if (it % check == 0 && read_count(0) <= 0) return;
     }
     read_count(0);
@@ -1569,16 +1961,21 @@ void StructBatch::df_pcg(const double *b64, double *x64, double tol2) {
     float *r32 = (float *)cgv[0], *z32 = (float *)cgv[1];
     CK(cudaMemsetAsync(d_count, 0, 4 * sizeof(int), stream));
     {
-        KTimer _kt(this, kname("k_df_residual", 0, false), L0.all_cells);
-        k_df_residual<true><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo,
-                                                       coeffs_of<double>(L0, true), b64, x64, r64, tol2,
-                                                       opt.maxiter, opt.max_outer);
+        KTimer _kt(this, kname(zero_guess ? "k_df_residual0" : "k_df_residual", 0, false), L0.all_cells);
+        if (zero_guess)
+            k_df_residual<true, true><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs,
+                                                                 L0.all.d_pinfo, coeffs_of<double>(L0, true), L0.dir,
+                                                                 b64, x64, r64, tol2, opt.maxiter, opt.max_outer);
+        else
+            k_df_residual<true><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs,
+                                                           L0.all.d_pinfo, coeffs_of<double>(L0, true), L0.dir, b64,
+                                                           x64, r64, tol2, opt.maxiter, opt.max_outer);
     }
     LAUNCH_CHECK();
     for (int round = 0; round < opt.max_outer && read_count(0) > 0; round++) {
         {
             KTimer _kt(this, kname("k_df_begin", 0, false), L0.all_cells);
-            k_df_begin<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, r64, dfv[1], r32, dfv[0]);
+            k_df_begin<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, r64, dfv[1], r32);
         }
         LAUNCH_CHECK();
         vcycle<float>(r32, z32);
@@ -1587,18 +1984,13 @@ void StructBatch::df_pcg(const double *b64, double *x64, double tol2) {
             k_df_update_p<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z32, dfv[2]);
         }
         LAUNCH_CHECK();
-        run_loop(1, nullptr);
-        {
-            KTimer _kt(this, kname("k_df_end", 0, false), L0.all_cells);
-            k_df_end<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, dfv[0], x64);
-        }
-        LAUNCH_CHECK();
+        run_loop(1, x64);
         CK(cudaMemsetAsync(d_count, 0, sizeof(int), stream));
         {
             KTimer _kt(this, kname("k_df_residual", 0, false), L0.all_cells);
             k_df_residual<false><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs,
-                                                            L0.all.d_pinfo, coeffs_of<double>(L0, true), b64, x64,
-                                                            r64, tol2, opt.maxiter, opt.max_outer);
+                                                            L0.all.d_pinfo, coeffs_of<double>(L0, true), L0.dir, b64,
+                                                            x64, r64, tol2, opt.maxiter, opt.max_outer);
         }
         LAUNCH_CHECK();
     }
@@ -1607,6 +1999,10 @@ void StructBatch::df_pcg(const double *b64, double *x64, double tol2) {
 // ---- full solve of A x = b for every problem (x holds the initial guess)
 void StructBatch::solve(const double *b, double *x, double reltol) {
     const double tol2 = reltol * reltol;
+    struct ZeroGuessReset {
+        bool &f;
+        ~ZeroGuessReset() { f = false; }
+    } zg{zero_guess};
     {
         KTimer _kt(this, kname("k_state_init", 0, false), 0);
         k_state_init<<<(nprob + 127) / 128, 128, 0, stream>>>(d_state, nprob);
@@ -1634,13 +2030,15 @@ void StructBatch::solve(const double *b, double *x, double reltol) {
         stats_relres = std::max(stats_relres, rel);
         if (hs[p].status != DPF_OK && last_status == DPF_OK) last_status = hs[p].status;
     }
-    int fst = 0;
-    CK(cudaMemcpyAsync(&h_count[0], d_factor_status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(&h_count[0], d_factor_status, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
-    fst = h_count[0];
-    if (fst) {
+    if (h_count[0]) {
         last_status = DPF_BAD_INPUT;
         last_message = "coarsest operator is not positive definite (does every problem have a Dirichlet cell?)";
+    }
+    if (h_count[1]) {
+        last_status = DPF_CUDA;
+        last_message = "a shared-memory staging wait of a smoother kernel expired";
     }
 }
 
@@ -1653,6 +2051,7 @@ void StructBatch::forward(const double *Ks, const double *logK, int kind) {
                            " has no Dirichlet cell: the steady-state operator is singular");
     if (logK) cell_k(logK, kind, in_kc);
     assemble(Ks, logK ? in_kc : nullptr, kind, nullptr, true);
+    zero_guess = true;
     solve(b64, h, opt.reltol);
     fwd_kind = logK ? 1 : 0;
     mean_kind = kind;
@@ -1666,6 +2065,7 @@ void StructBatch::adjoint_solve() {
         k_adjoint_rhs<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, L0.dir, delta, arhs, lam);
     }
     LAUNCH_CHECK();
+    zero_guess = true;
     solve(arhs, lam, opt.reltol);
 }
 

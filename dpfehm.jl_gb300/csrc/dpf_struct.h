@@ -59,9 +59,21 @@ public:
         long long all_cells = 0, smooth_cells = 0, coarse_cells = 0;
         std::vector<LevelDesc> h_desc;
         LevelDesc *d_desc = nullptr;
-        BlockMap all, smooth;          // every problem with this level / those for which it is not the coarsest
+        BlockMap all, smooth;          // every problem with this level / those smoothed by per-level kernels
+        BlockMap restr;                // problems whose residual is restricted into this level by a per-level kernel
+        long long restr_cells = 0;
         std::vector<int> coarse_list;  // problems whose coarsest level this is
         int *d_coarse = nullptr;
+        // plane-marching launches over the smoothed problems: items {p, y0, x0, x1} (slab of
+        // rows y0.. of planes x0..x1-1), per-problem item ranges, and the largest stage regions
+        int4 *pm_items = nullptr;
+        int2 *pm_pinfo = nullptr;
+        int pm_nitems = 0;
+        bool pm_ok = false;
+        int pm_halo = 0, pm_cy = 0, pm_slab = 0, pm_coarse = 0;  // elements
+        std::vector<int> csolve_list;  // ... of those, the ones solved by a per-level launch (no fused tail)
+        int *d_csolve = nullptr;
+        long long csolve_cells = 0;
         uint8_t *dir = nullptr;        // identity (Dirichlet) rows
         double *c64[4] = {nullptr, nullptr, nullptr, nullptr};  // cx, cy, cz, leak
         double *idg64 = nullptr;       // inverse diagonal (FP64 solves)
@@ -94,12 +106,16 @@ public:
 
     template <typename T>
     void vcycle(const T *r, T *z);
+    void build_plane_items(Level &L, const std::vector<int> &smooth, int sms,
+                           const std::vector<std::vector<std::array<int, 3>>> *shapes, int l);
+    template <typename T>
+    void pm_launch(int mode, int l, const T *b, const T *xin, T *xout, T *d, const T *e, T c1, T c2, T invth, T sc);
     template <typename T>
     void pcg(const T *b, T *x, double tol2);
     void df_pcg(const double *b64, double *x64, double tol2);
     template <typename T>
     void pcg_iteration(T *x);
-    void df_iteration();
+    void df_iteration(double *x64);
     cudaGraphExec_t loop_graph(int kind, void *x);
     void run_loop(int kind, void *x);
     int read_count(int which);
@@ -122,15 +138,22 @@ public:
     double *in_dh = nullptr, *in_Q = nullptr, *in_logK = nullptr, *in_Ks = nullptr, *shift = nullptr;
     double *in_kc = nullptr, *aux_kc = nullptr;  // per-cell face-mean values of the forward / standalone calls
     void *cgv[4] = {nullptr, nullptr, nullptr, nullptr};  // FP64: r, z, p, q; mixed: r32, z32
-    float2 *dfv[4] = {nullptr, nullptr, nullptr, nullptr};  // mixed: x, r, p, q in double-float
+    float2 *dfv[4] = {nullptr, nullptr, nullptr, nullptr};  // mixed: -, r, p, q in double-float
     float2 *cdf[4] = {nullptr, nullptr, nullptr, nullptr};  // mixed: finest cx, cy, cz, leak in double-float
 
     // device state
     CgState *d_state = nullptr;
     int *d_count = nullptr;       // [0] active CG problems, [2] loop passes
-    int *d_factor_status = nullptr;
+    int *d_factor_status = nullptr;  // [0] coarsest factorisation failed, [1] an async-copy wait expired
     ReduceScratch rs;
     double *d_coarseL = nullptr;
+    // fused tail: per problem {p, first tail level, coarsest level, 0}; level table built on first use
+    bool zero_guess = false;  // the next solve starts from 0 (Dirichlet values on identity rows)
+    std::vector<int4> tails;
+    int4 *d_tails = nullptr;
+    void *d_tail_lv = nullptr;
+    long long tail_cells_total = 0;
+    int tail_first_level = 0;
     int *h_count = nullptr;
     void *h_state_buf = nullptr;
     struct GraphRec {

@@ -96,7 +96,7 @@ struct Acc<float> {
 // Every thread of the block must call it.
 template <typename T, int NV>
 __device__ __forceinline__ double2 block_sum(Acc<T> a, Acc<T> b) {
-    __shared__ Acc<T> sh[NV][kBlock / 32];
+    __shared__ Acc<T> sh[NV][32];  // one slot per warp of any block size
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         a = a + a.shfl(o);

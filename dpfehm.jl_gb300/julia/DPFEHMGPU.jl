@@ -29,10 +29,12 @@ mutable struct Options
     use_graphs::Cint
     check_every::Cint
     blocks_per_sm::Cint
+    tail_cells::Cint
+    plane::Cint
 end
 
 function default_options(; reltol=nothing, maxiter=nothing, precision=nothing)
-    o = Options(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
+    o = Options(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
     ccall((:dpf_default_options, libdpf), Cvoid, (Ref{Options},), o)
     reltol === nothing || (o.reltol = reltol)
     maxiter === nothing || (o.maxiter = maxiter)

@@ -77,6 +77,10 @@ typedef struct dpf_options {
     int use_graphs;      /* capture each solve's iteration in a CUDA graph    (default 1)     */
     int check_every;     /* convergence is read back every this many iterations (default 1)   */
     int blocks_per_sm;   /* launch shape: grids hold SMs x this many 256-thread blocks (default 16) */
+    int tail_cells;      /* regular grids: the multigrid levels of a problem with at most this many cells
+                            run as one fused kernel per problem (default 4096; negative: off) */
+    int plane;           /* regular grids, MIXED: plane-marching smoother kernels with shared-memory
+                            staging (default 1; negative: grid-stride kernels) */
 } dpf_options;
 
 typedef struct dpf_problem dpf_problem;
