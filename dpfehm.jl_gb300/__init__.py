@@ -87,6 +87,17 @@ def _out(like, n, dtype=np.float64):
     return a, a.ctypes.data
 
 
+def _out_into(given, like, n):
+    """`given` (a caller's float64 buffer of n entries: numpy array or torch tensor, e.g. in
+    page-locked host memory) as an output buffer, or a new one on the side of `like`."""
+    if given is None:
+        return _out(like, n)
+    b = _Buf(given, n=n)
+    if b.obj is not given and not (_is_torch(given) and b.obj.data_ptr() == given.data_ptr()):
+        raise ValueError("output buffers must be contiguous float64")
+    return given, b.ptr
+
+
 def _check(lib, h, rc, allow_not_converged=True):
     if rc == _lib.DPF_OK:
         return
@@ -239,14 +250,15 @@ class GroundwaterProblem:
         _check(self._lib, self._h, self._lib.dpf_steady_adjoint_logk(self._h, dl.ptr, gp, ddhp, dQp))
         return g, ddh, dQ
 
-    def solve_grad_logk(self, logK, dirichleths, Qs, obs, mean="geometric"):
-        """Forward solve, J = sum(h[obs]^2), adjoint; returns (h, dJ/dlogK)."""
+    def solve_grad_logk(self, logK, dirichleths, Qs, obs, mean="geometric", out=None):
+        """Forward solve, J = sum(h[obs]^2), adjoint; returns (h, dJ/dlogK). `out` = (h, g)
+        writes into the caller's buffers (e.g. page-locked host arrays)."""
         lk = _Buf(logK, n=self.N)
         d = _Buf(dirichleths, n=self.N)
         q = _Buf(Qs, n=self.N)
         ob = np.ascontiguousarray(obs, dtype=np.int64)
-        h, hp = _out(lk, self.N)
-        g, gp = _out(lk, self.N)
+        h, hp = _out_into(out[0] if out else None, lk, self.N)
+        g, gp = _out_into(out[1] if out else None, lk, self.N)
         _check(self._lib, self._h, self._lib.dpf_solve_grad_logk(self._h, lk.ptr, _MEANS[mean], d.ptr, q.ptr, ob.size,
                                                                  ob.ctypes.data, hp, gp))
         return h, g
@@ -332,7 +344,9 @@ class GroundwaterBatch(GroundwaterProblem):
             lib.dpf_batch_offsets(self._h, p, ctypes.byref(co), ctypes.byref(fo))
             self.cell_offsets[p], self.face_offsets[p] = co.value, fo.value
 
-    def solve_grad_logk(self, logK, dirichleths, Qs, obs_per_problem, mean="geometric"):
+    def solve_grad_logk(self, logK, dirichleths, Qs, obs_per_problem, mean="geometric", out=None):
+        """Forward solves, J_p = sum(h_p[obs_p]^2), adjoints for every problem; returns the
+        concatenated (h, dJ/dlogK). `out` = (h, g) writes into the caller's buffers."""
         lk = _Buf(logK, n=self.N)
         d = _Buf(dirichleths, n=self.N)
         q = _Buf(Qs, n=self.N)
@@ -340,8 +354,8 @@ class GroundwaterBatch(GroundwaterProblem):
         offs[1:] = np.cumsum([len(o) for o in obs_per_problem])
         ob = np.ascontiguousarray(np.concatenate([np.asarray(o, np.int64) for o in obs_per_problem])
                                   if offs[-1] else np.zeros(0, np.int64))
-        h, hp = _out(lk, self.N)
-        g, gp = _out(lk, self.N)
+        h, hp = _out_into(out[0] if out else None, lk, self.N)
+        g, gp = _out_into(out[1] if out else None, lk, self.N)
         _check(self._lib, self._h, self._lib.dpf_batch_solve_grad_logk(self._h, lk.ptr, _MEANS[mean], d.ptr, q.ptr,
                                                                        offs.ctypes.data, ob.ctypes.data, hp, gp))
         return h, g

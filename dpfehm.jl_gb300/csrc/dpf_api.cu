@@ -559,7 +559,7 @@ static int solve_grad_common(dpf_problem *P, const double *logK, int kind, const
     S.forward(nullptr, S.in_logK, kind);
     int rc = solver_status(P, S);
     if (rc != DPF_OK && rc != DPF_NOT_CONVERGED) return rc;
-    long long *d_obs = scratch<long long>(P, obs_global.size());
+    long long *d_obs = S.obs_buffer(obs_global.size());
     if (!obs_global.empty())
         ck(cudaMemcpyAsync(d_obs, obs_global.data(), obs_global.size() * sizeof(long long), cudaMemcpyHostToDevice,
                            P->stream),
@@ -574,7 +574,6 @@ static int solve_grad_common(dpf_problem *P, const double *logK, int kind, const
         if (tmp != dlogK) stage_out(P, dlogK, tmp, S.N);
     }
     ck(cudaStreamSynchronize(P->stream), "sync");
-    release(P, d_obs);
     return rc != DPF_OK ? rc : rc2;
 }
 

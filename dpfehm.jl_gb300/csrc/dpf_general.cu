@@ -530,6 +530,7 @@ __global__ void kg_df_begin(int n, const CgState *st, const double *__restrict__
 __global__ void kg_state_init(CgState *st) {
     CgState s;
     memset(&s, 0, sizeof(s));
+    s.cont = 1.0;
     st[0] = s;
 }
 

@@ -55,6 +55,7 @@ struct CgState {
     double alpha, beta;
     double scale;                  // mixed precision: normalisation of the double-float residual
     double floor2;                 // mixed precision: FP64 rounding floor of |b - A x|^2 at the last check
+    double cont;                   // mixed precision: factor of the next beta after a residual replacement
     double orr, obb;               // mixed precision: true (FP64) residual and rhs norms squared
     double orr_prev;               // mixed precision: true residual norm squared after the previous round
     int iters, active, status, outer;  // outer: rounds so far

@@ -28,7 +28,7 @@ constexpr int kPlaneStages = DPF_PLANE_STAGES;  // planes x-1, x, x+1 resident, 
 #ifndef DPF_PLANE_CPT
 #define DPF_PLANE_CPT 3
 #endif
-constexpr int kPlaneCells = kPlaneThreads * DPF_PLANE_CPT;  // slab cells per plane (whole rows)
+constexpr int kPlaneCells = kPlaneThreads * DPF_PLANE_CPT;  // slab capacity (whole rows)
 constexpr uint32_t kWaitTries = 1u << 20;  // bounded mbarrier polling (well under a second)
 
 enum : int { PM_FIRST2 = 1, PM_FIRST = 2, PM_PROLONG = 4, PM_NOD = 8, PM_RZ = 16 };
@@ -111,6 +111,30 @@ __device__ __forceinline__ BulkRange make_range(const void *base, int es, long l
 // Fast division of k (< 2^31) by nz with the level's invariant-integer constants.
 __device__ __forceinline__ int div_nz(const LevelDesc &L, int k) { return (int)fast_div((unsigned)k, L.mag_nz, L.sh_nz); }
 
+// Producer loop, run by lane 0 of the producer warp: stages planes pl_lo..pl_hi into the
+// ring of R slots as the consumer warps release them. stage_plane(q, slot, bar) announces
+// (mbarrier expect_tx) and issues the copies of plane q; the one pending arrival made here
+// afterwards keeps the phase open until every copy has been announced. Before the block
+// may end, the last phase of every filled slot is waited for (bounded), so no copy is
+// still in flight into the block's shared memory.
+template <int R, typename F>
+__device__ __forceinline__ void pm_produce(int pl_lo, int pl_hi, uint64_t *full, uint64_t *empty, unsigned char *sm,
+                                           int slot_bytes, int *err, F stage_plane) {
+    int issued_hi = pl_lo - 1;
+    for (int q = pl_lo; q <= pl_hi; q++) {
+        const int u = q - pl_lo, s = u % R;
+        if (u >= R && !mbar_wait(&empty[s], (uint32_t)((u / R - 1) & 1), err)) break;
+        fence_proxy_async_smem();
+        stage_plane(q, (char *)sm + s * slot_bytes, &full[s]);
+        mbar_arrive(&full[s]);
+        issued_hi = q;
+    }
+    for (int q = max(pl_lo, issued_hi - R + 1); q <= issued_hi; q++) {
+        const int u = q - pl_lo;
+        mbar_wait(&full[u % R], (uint32_t)((u / R) & 1), nullptr);
+    }
+}
+
 // Chebyshev step family on the plane ring. MODE bits:
 //   PM_FIRST2  the first two steps from a zero guess (reads b and the inverse diagonal
 //              with halos instead of an iterate)
@@ -171,18 +195,10 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
     if (warp == kConsumerWarps) {
         // ---------------- producer
         if (lane == 0) {
-            int issued_hi = pl_lo - 1;
-            for (int q = pl_lo; q <= pl_hi; q++) {
-                const int u = q - pl_lo, s = u % R;
-                if (u >= R && !mbar_wait(&empty[s], (uint32_t)((u / R - 1) & 1), err)) break;
-                fence_proxy_async_smem();
-                char *slot = (char *)sm + s * lay.slot_bytes;
+            pm_produce<R>(pl_lo, pl_hi, full, empty, sm, lay.slot_bytes, err, [&](int q, char *slot, uint64_t *bar) {
                 const long long pb = L.off + (long long)q * sx;
                 const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
                 const long long hA = pb + (long long)h0 * nz, hB = pb + (long long)h1 * nz, pE = lp + ncell;
-                // each copy is announced on the barrier right before it is issued; the one
-                // pending arrival keeps the phase open until every copy has been announced
-                uint64_t *bar = &full[s];
                 auto stage = [&](const void *base, int esz, long long l0, long long a0, long long a1, int off) {
                     const BulkRange r = make_range(base, esz, l0, a0, a1, slot + off);
                     mbar_expect_tx(bar, r.bytes);
@@ -207,15 +223,7 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
                     stage(e, es, cb + (long long)cr_lo * Lc.nz, cb + (long long)c0 * Lc.nz,
                           cb + (long long)c1r * Lc.nz, lay.oE);
                 }
-                mbar_arrive(bar);
-                issued_hi = q;
-            }
-            // the block must not end with copies in flight into its shared memory: wait
-            // (bounded) for the last phase of every slot that was filled
-            for (int q = max(pl_lo, issued_hi - R + 1); q <= issued_hi; q++) {
-                const int u = q - pl_lo;
-                mbar_wait(&full[u % R], (uint32_t)((u / R) & 1), nullptr);
-            }
+            });
         }
         __syncwarp();
     } else {
@@ -355,9 +363,21 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
             CgState &s = st[p];
             s.rz_old = s.rz;
             s.rz = tot.x;
-            s.beta = (s.iters == 0 || s.rz_old == 0.0) ? 0.0 : s.rz / s.rz_old;
+            s.beta = (s.iters == 0 || s.rz_old == 0.0) ? 0.0 : s.rz / s.rz_old * s.cont;
+            s.cont = 1.0;
         }
     }
+}
+
+struct CoeffsDF {
+    const float2 *cx, *cy, *cz, *leak;
+};
+
+__device__ __forceinline__ void finish_pq(CgState &s, double pq, int *active_count) {
+    s.pq = pq;
+    if (!isfinite(s.pq)) { s.alpha = 0.0; s.status = DPF_NAN; deactivate(s, active_count); }
+    else if (!(s.pq > 0.0)) { s.alpha = 0.0; deactivate(s, active_count); }
+    else s.alpha = s.rz / s.pq;
 }
 
 }  // namespace dpf

@@ -84,12 +84,17 @@ __global__ void k_assemble(const LevelDesc *__restrict__ desc, const int4 *__res
         } else {
             lk = 1.0;
         }
+        if (dfx) {
+            // mixed precision: the FP64 operator is the exact value of its double-float copy
+            // (48 of 53 bits), so the double-float CG and the FP64 residual check see the
+            // same operator (a relative change of at most 2^-49 in every coefficient)
+            const float2 qx = df_from_double(cp[0]), qy = df_from_double(cp[1]);
+            const float2 qz = df_from_double(cp[2]), ql = df_from_double(lk);
+            dfx[i] = qx; dfy[i] = qy; dfz[i] = qz; dfleak[i] = ql;
+            cp[0] = df_to_double(qx); cp[1] = df_to_double(qy); cp[2] = df_to_double(qz); lk = df_to_double(ql);
+        }
         cx[i] = cp[0]; cy[i] = cp[1]; cz[i] = cp[2]; leak[i] = lk;
         if (fx) { fx[i] = (float)cp[0]; fy[i] = (float)cp[1]; fz[i] = (float)cp[2]; fleak[i] = (float)lk; }
-        if (dfx) {
-            dfx[i] = df_from_double(cp[0]); dfy[i] = df_from_double(cp[1]);
-            dfz[i] = df_from_double(cp[2]); dfleak[i] = df_from_double(lk);
-        }
         b[i] = rhs;
         if (init_x) x[i] = fi ? 0.0 : dh[i];
         else if (!fi) x[i] = dh[i];
@@ -319,7 +324,8 @@ k_cheb_step(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, C
             CgState &s = st[p];
             s.rz_old = s.rz;
             s.rz = tot.x;
-            s.beta = (s.iters == 0 || s.rz_old == 0.0) ? 0.0 : s.rz / s.rz_old;
+            s.beta = (s.iters == 0 || s.rz_old == 0.0) ? 0.0 : s.rz / s.rz_old * s.cont;
+            s.cont = 1.0;
         }
     }
 }
@@ -390,7 +396,8 @@ __global__ void k_coarse_solve(const LevelDesc *__restrict__ desc, const int *__
             CgState &s = st[p];
             s.rz_old = s.rz;
             s.rz = rz;
-            s.beta = (s.iters == 0 || s.rz_old == 0.0) ? 0.0 : s.rz / s.rz_old;
+            s.beta = (s.iters == 0 || s.rz_old == 0.0) ? 0.0 : s.rz / s.rz_old * s.cont;
+            s.cont = 1.0;
         }
     }
 }
@@ -632,13 +639,13 @@ __global__ void k_update_p(const LevelDesc *__restrict__ desc, const int4 *__res
 // ends by adding the correction to the FP64 solution; convergence is then confirmed
 // on the true FP64 residual, and another round runs if it is not met.
 
-struct CoeffsDF {
-    const float2 *cx, *cy, *cz, *leak;
-};
 
 // q = A p in double-float (flux form); alpha = rz / (p . q) (hi parts: q is accurate, so
 // its leading float is too)
-__global__ void __launch_bounds__(kBlock, 8) k_df_spmv_pq(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
+#ifndef DPF_DF_SPMV_MINB
+#define DPF_DF_SPMV_MINB 8
+#endif
+__global__ void __launch_bounds__(kBlock, DPF_DF_SPMV_MINB) k_df_spmv_pq(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                              int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, CoeffsDF C,
                              const float2 *__restrict__ pv, float2 *__restrict__ q) {
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
@@ -660,13 +667,8 @@ __global__ void __launch_bounds__(kBlock, 8) k_df_spmv_pq(const LevelDesc *__res
         part = part + Acc<float>::prod(pi.x, a.x);
     }
     double2 tot;
-    if (reduce_last<float>(part, Acc<float>(), rs, pinfo[p], p, tot) && threadIdx.x == 0) {
-        CgState &s = st[p];
-        s.pq = tot.x;
-        if (!isfinite(s.pq)) { s.alpha = 0.0; s.status = DPF_NAN; deactivate(s, active_count); }
-        else if (!(s.pq > 0.0)) { s.alpha = 0.0; deactivate(s, active_count); }
-        else s.alpha = s.rz / s.pq;
-    }
+    if (reduce_last<float>(part, Acc<float>(), rs, pinfo[p], p, tot) && threadIdx.x == 0)
+        finish_pq(st[p], tot.x, active_count);
 }
 
 // x64 += (alpha scale) p in FP64 (the solution keeps all 53 bits: a 48-bit double-float
@@ -790,12 +792,20 @@ __global__ void k_df_residual(const LevelDesc *__restrict__ desc, const int4 *__
         s.orr_prev = s.orr;
         s.ru_flag = go ? 1 : 0;  // problem takes part in the next round
         s.active = go ? 1 : 0;
-        s.iters = 0;
-        s.rz = 0.0;
-        s.rz_old = 0.0;
-        s.beta = 0.0;
+        if (FIRST) {
+            s.iters = 0;
+            s.rz = 0.0;
+            s.rz_old = 0.0;
+            s.beta = 0.0;
+            s.cont = 1.0;
+        }
         if (go) {
-            s.scale = sqrt(s.orr);
+            // a further round continues the Krylov process on the true residual (residual
+            // replacement): the direction is kept, and the next beta is rescaled by the change
+            // of normalisation new/old so that p = z + beta p holds in the new units
+            const double sc = sqrt(s.orr);
+            if (!FIRST) s.cont = sc / s.scale;
+            s.scale = sc;
             atomicAdd(active_count, 1);
         }
     }
@@ -823,6 +833,7 @@ __global__ void k_state_init(CgState *st, int nprob) {
     if (p >= nprob) return;
     CgState s;
     memset(&s, 0, sizeof(s));
+    s.cont = 1.0;
     st[p] = s;
 }
 
@@ -1150,17 +1161,18 @@ static BlockMap build_map(const std::vector<LevelDesc> &desc, const std::vector<
 // Plane-marching work items of a level: per smoothed problem, slabs of Ty = 256 / nz rows
 // (whole rows, so a slab is contiguous in every array) times chunks of x-planes, with the
 // chunk length chosen so that all items fill the device about once.
-void StructBatch::build_plane_items(Level &L, const std::vector<int> &smooth, int sms,
-                                    const std::vector<std::vector<std::array<int, 3>>> *shapes, int l) {
-    L.pm_ok = false;
+void StructBatch::build_plane_items(PlaneItems &P, const Level &L, const std::vector<int> &take, int sms,
+                                    int cells, const std::vector<std::vector<std::array<int, 3>>> *shapes, int l) {
+    P.ok = false;
+    P.cells = cells;
     // FP32 V-cycles only: with 8-byte values the stages of a 768-cell slab allow one block
     // per SM, and the FP64 smoothers are faster as grid-stride kernels
     if (opt.plane <= 0 || !mixed) return;
     long long total = 0;
     for (int p = 0; p < nprob; p++) {
-        if (!smooth[p]) continue;
+        if (!take[p]) continue;
         const LevelDesc &D = L.h_desc[p];
-        if (D.nz > kPlaneCells) return;  // a row must fit a slab
+        if (D.nz > cells) return;  // a row must fit a slab
         total += D.n;
     }
     if (total == 0) return;
@@ -1171,9 +1183,9 @@ void StructBatch::build_plane_items(Level &L, const std::vector<int> &smooth, in
     std::vector<int4> items;
     std::vector<int2> pinfo(nprob, make_int2(0, 0));
     for (int p = 0; p < nprob; p++) {
-        if (!smooth[p]) continue;
+        if (!take[p]) continue;
         const LevelDesc &D = L.h_desc[p];
-        const int Ty = std::max(1, std::min(D.ny, kPlaneCells / D.nz));
+        const int Ty = std::max(1, std::min(D.ny, cells / D.nz));
         const int ytiles = (D.ny + Ty - 1) / Ty;
         long long chunks = (long long)((double)target * (double)D.n / (double)total / ytiles);
         chunks = std::max(1LL, std::min(chunks, (long long)D.nx));
@@ -1183,20 +1195,20 @@ void StructBatch::build_plane_items(Level &L, const std::vector<int> &smooth, in
         for (int y0 = 0; y0 < D.ny; y0 += Ty)
             for (int x0 = 0; x0 < D.nx; x0 += xc) items.push_back(make_int4(p, y0, x0, std::min(x0 + xc, D.nx)));
         pinfo[p].y = (int)items.size() - pinfo[p].x;
-        L.pm_halo = std::max(L.pm_halo, (Ty + 2) * D.nz);
-        L.pm_cy = std::max(L.pm_cy, (Ty + 1) * D.nz);
-        L.pm_slab = std::max(L.pm_slab, Ty * D.nz);
-        if (shapes) {
+        P.halo = std::max(P.halo, (Ty + 2) * D.nz);
+        P.cy = std::max(P.cy, (Ty + 1) * D.nz);
+        P.slab = std::max(P.slab, Ty * D.nz);
+        if (shapes && l + 1 < (int)(*shapes)[p].size()) {
             const int cnz = (*shapes)[p][l + 1][2];
-            L.pm_coarse = std::max(L.pm_coarse, ((Ty + 2) / 2 + 2) * cnz);
+            P.coarse = std::max(P.coarse, ((Ty + 2) / 2 + 2) * cnz);
         }
     }
-    L.pm_nitems = (int)items.size();
-    L.pm_items = dalloc<int4>(items.size(), owned);
-    L.pm_pinfo = dalloc<int2>(nprob, owned);
-    CK(cudaMemcpy(L.pm_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(L.pm_pinfo, pinfo.data(), nprob * sizeof(int2), cudaMemcpyHostToDevice));
-    L.pm_ok = true;
+    P.n = (int)items.size();
+    P.items = dalloc<int4>(items.size(), owned);
+    P.pinfo = dalloc<int2>(nprob, owned);
+    CK(cudaMemcpy(P.items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.pinfo, pinfo.data(), nprob * sizeof(int2), cudaMemcpyHostToDevice));
+    P.ok = true;
 }
 
 StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<std::vector<int64_t>> &dnodes,
@@ -1283,14 +1295,14 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         L.all = build_map(L.h_desc, has, owned, nprob, target_blocks);
         L.smooth = build_map(L.h_desc, smooth, owned, nprob, target_blocks);
         L.restr = build_map(L.h_desc, restr, owned, nprob, target_blocks);
-        build_plane_items(L, smooth, sms, (l + 1 < nlev_max) ? &shapes : nullptr, l);
+        build_plane_items(L.pm, L, smooth, sms, kPlaneCells, &shapes, l);
         for (int p = 0; p < nprob; p++) {
             if (has[p]) L.all_cells += L.h_desc[p].n;
             if (smooth[p]) L.smooth_cells += L.h_desc[p].n;
             if (restr[p]) L.restr_cells += L.h_desc[p].n;
             if (has[p] && l == nlev[p] - 1) L.coarse_cells += L.h_desc[p].n;
         }
-        maxblocks = std::max(maxblocks, std::max(L.all.nblocks, L.pm_nitems));
+        maxblocks = std::max(maxblocks, std::max(L.all.nblocks, L.pm.n));
         L.d_coarse = dalloc<int>(L.coarse_list.size(), owned);
         if (!L.coarse_list.empty())
             CK(cudaMemcpy(L.d_coarse, L.coarse_list.data(), L.coarse_list.size() * sizeof(int),
@@ -1566,26 +1578,26 @@ void StructBatch::pm_launch(int mode, int l, const T *b, const T *xin, T *xout, 
     int off = 0;
     auto take = [&](int bytes) { int o = off; off += bytes; return o; };
     const bool f2 = mode & PM_FIRST2, first = mode & PM_FIRST, prol = mode & PM_PROLONG;
-    lay.oX = f2 ? -1 : take(pm_region(L.pm_halo, es));
-    lay.oB = take(pm_region(f2 ? L.pm_halo : L.pm_slab, es));
-    lay.oD = (f2 || first) ? -1 : take(pm_region(L.pm_slab, es));
-    lay.oG = f2 ? take(pm_region(L.pm_halo, es)) : -1;
-    lay.oCX = take(pm_region(L.pm_slab, es));
-    lay.oCY = take(pm_region(L.pm_cy, es));
-    lay.oCZ = take(pm_region(L.pm_slab, es));
-    lay.oLK = take(pm_region(L.pm_slab, es));
-    lay.oDIR = prol ? take(pm_region(L.pm_halo, 1)) : -1;
-    lay.oE = prol ? take(pm_region(L.pm_coarse, es)) : -1;
+    lay.oX = f2 ? -1 : take(pm_region(L.pm.halo, es));
+    lay.oB = take(pm_region(f2 ? L.pm.halo : L.pm.slab, es));
+    lay.oD = (f2 || first) ? -1 : take(pm_region(L.pm.slab, es));
+    lay.oG = f2 ? take(pm_region(L.pm.halo, es)) : -1;
+    lay.oCX = take(pm_region(L.pm.slab, es));
+    lay.oCY = take(pm_region(L.pm.cy, es));
+    lay.oCZ = take(pm_region(L.pm.slab, es));
+    lay.oLK = take(pm_region(L.pm.slab, es));
+    lay.oDIR = prol ? take(pm_region(L.pm.halo, 1)) : -1;
+    lay.oE = prol ? take(pm_region(L.pm.coarse, es)) : -1;
     lay.slot_bytes = (off + 127) & ~127;
     const size_t smem = (size_t)kPlaneStages * lay.slot_bytes;
     Coeffs<T> C = coeffs_of<T>(L, mixed);
     const LevelDesc *cd = l + 1 < nlev_max ? lv[l + 1].d_desc : nullptr;
-    const unsigned nb = (unsigned)L.pm_nitems;
+    const unsigned nb = (unsigned)L.pm.n;
     int *err = d_factor_status + 1;
 #define DPF_PM_CASE(M)                                                                                           \
     case M:                                                                                                      \
-        pm_kernel<T, M>(nb, smem, stream, L.d_desc, cd, L.pm_items, d_state, C, b, xin, xout, d, L.dir, e, c1, c2, \
-                        invth, sc, lay, rs, L.pm_pinfo, err);                                                     \
+        pm_kernel<T, M>(nb, smem, stream, L.d_desc, cd, L.pm.items, d_state, C, b, xin, xout, d, L.dir, e, c1, c2, \
+                        invth, sc, lay, rs, L.pm.pinfo, err);                                                     \
         break;
     switch (mode) {
         DPF_PM_CASE(PM_FIRST2)
@@ -1613,7 +1625,7 @@ void StructBatch::vcycle(const T *r, T *z) {
         Coeffs<T> C = coeffs_of<T>(L, mixed);
         const T *b = l == 0 ? r : (const T *)L.work[2];
         T *xa = (T *)L.work[0], *xb = (T *)L.work[1], *d = (T *)L.work[3];
-        if (nb_of(L.smooth) && L.pm_ok && deg >= 2) {
+        if (nb_of(L.smooth) && L.pm.ok && deg >= 2) {
             // plane-marching pre-smoothing: two fused first steps, then the rest
             {
                 KTimer _kt(this, kname("k_pm_first2", l, sizeof(T) == 4), L.smooth_cells);
@@ -1740,7 +1752,7 @@ void StructBatch::vcycle(const T *r, T *z) {
         T *xa = (T *)L.work[0], *xb = (T *)L.work[1], *d = (T *)L.work[3];
         T *cur = pre[l];
         const T *e = (const T *)Cn.work[1];
-        if (L.pm_ok && deg >= 2) {
+        if (L.pm.ok && deg >= 2) {
             // plane-marching post-smoothing: prolongation fused into the first step; the
             // last step writes no direction (and on the finest level also forms r . z)
             for (int k = 0; k < deg; k++) {
@@ -2067,6 +2079,15 @@ void StructBatch::adjoint_solve() {
     LAUNCH_CHECK();
     zero_guess = true;
     solve(arhs, lam, opt.reltol);
+}
+
+long long *StructBatch::obs_buffer(size_t n) {
+    if (n > obs_cap || !d_obs_buf) {
+        const size_t cap = std::max<size_t>(n, 1024);
+        d_obs_buf = dalloc<long long>(cap, owned);  // the previous buffer stays owned until destruction
+        obs_cap = cap;
+    }
+    return d_obs_buf;
 }
 
 void StructBatch::obs_delta(const long long *d_obs, long long nobs) {

@@ -54,6 +54,16 @@ const char *kname(const char *base, int level, bool fp32);
 
 class StructBatch {
 public:
+    // Plane-marching work items {p, y0, x0, x1} (slab of rows y0.. of planes x0..x1-1),
+    // per-problem item ranges, and the largest stage regions (elements)
+    struct PlaneItems {
+        int4 *items = nullptr;
+        int2 *pinfo = nullptr;
+        int n = 0;
+        bool ok = false;
+        int cells = 0;  // slab capacity: Ty = cells / nz whole rows
+        int halo = 0, cy = 0, slab = 0, coarse = 0;
+    };
     struct Level {
         long long ntot = 0;
         long long all_cells = 0, smooth_cells = 0, coarse_cells = 0;
@@ -64,13 +74,7 @@ public:
         long long restr_cells = 0;
         std::vector<int> coarse_list;  // problems whose coarsest level this is
         int *d_coarse = nullptr;
-        // plane-marching launches over the smoothed problems: items {p, y0, x0, x1} (slab of
-        // rows y0.. of planes x0..x1-1), per-problem item ranges, and the largest stage regions
-        int4 *pm_items = nullptr;
-        int2 *pm_pinfo = nullptr;
-        int pm_nitems = 0;
-        bool pm_ok = false;
-        int pm_halo = 0, pm_cy = 0, pm_slab = 0, pm_coarse = 0;  // elements
+        PlaneItems pm;  // plane-marching launches over the smoothed problems
         std::vector<int> csolve_list;  // ... of those, the ones solved by a per-level launch (no fused tail)
         int *d_csolve = nullptr;
         long long csolve_cells = 0;
@@ -106,7 +110,7 @@ public:
 
     template <typename T>
     void vcycle(const T *r, T *z);
-    void build_plane_items(Level &L, const std::vector<int> &smooth, int sms,
+    void build_plane_items(PlaneItems &P, const Level &L, const std::vector<int> &take, int sms, int cells,
                            const std::vector<std::vector<std::array<int, 3>>> *shapes, int l);
     template <typename T>
     void pm_launch(int mode, int l, const T *b, const T *xin, T *xout, T *d, const T *e, T c1, T c2, T invth, T sc);
@@ -149,6 +153,10 @@ public:
     double *d_coarseL = nullptr;
     // fused tail: per problem {p, first tail level, coarsest level, 0}; level table built on first use
     bool zero_guess = false;  // the next solve starts from 0 (Dirichlet values on identity rows)
+    // device buffer for observation indices, kept between calls (no allocation per call)
+    long long *obs_buffer(size_t n);
+    long long *d_obs_buf = nullptr;
+    size_t obs_cap = 0;
     std::vector<int4> tails;
     int4 *d_tails = nullptr;
     void *d_tail_lv = nullptr;

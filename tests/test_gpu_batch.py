@@ -112,3 +112,17 @@ def test_plane_and_grid_stride_smoothers_agree(gpu_lib, precision):
     for key, (h, g) in out.items():
         assert rel(h, h0) < 1e-11, key
         assert rel(g, g0) < 1e-9, key
+
+
+def test_caller_output_buffers(gpu_lib):
+    """solve_grad_logk(out=(h, g)) fills the caller's host buffers with the same values."""
+    pkg = gpu_lib
+    c = _problem(pkg, (14, 12, 5), 21)
+    B = pkg.GroundwaterBatch([c["ns"]], [c["mins"]], [c["maxs"]], [c["dn"]], reltol=1e-11, precision="mixed")
+    h0, g0 = B.solve_grad_logk(c["logK"], c["dh"], c["Qs"], [c["obs"]])
+    hb, gb = np.full(c["N"], np.nan), np.full(c["N"], np.nan)
+    h1, g1 = B.solve_grad_logk(c["logK"], c["dh"], c["Qs"], [c["obs"]], out=(hb, gb))
+    assert h1 is hb and g1 is gb
+    assert np.array_equal(hb, h0) and np.array_equal(gb, g0)
+    with pytest.raises(ValueError):
+        B.solve_grad_logk(c["logK"], c["dh"], c["Qs"], [c["obs"]], out=(np.zeros(c["N"], np.float32), gb))
