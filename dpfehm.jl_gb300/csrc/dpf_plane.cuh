@@ -20,15 +20,21 @@
 
 namespace dpf {
 
-constexpr int kPlaneThreads = 256;
+#ifndef DPF_PLANE_THREADS
+#define DPF_PLANE_THREADS 256
+#endif
+constexpr int kPlaneThreads = DPF_PLANE_THREADS;  // consumer threads per block (plus one producer warp)
 #ifndef DPF_PLANE_STAGES
 #define DPF_PLANE_STAGES 4
 #endif
 constexpr int kPlaneStages = DPF_PLANE_STAGES;  // planes x-1, x, x+1 resident, the rest in flight
 #ifndef DPF_PLANE_CPT
-#define DPF_PLANE_CPT 3
+#define DPF_PLANE_CPT 4
 #endif
 constexpr int kPlaneCells = kPlaneThreads * DPF_PLANE_CPT;  // slab capacity (whole rows)
+constexpr int kCellsPerThread = DPF_PLANE_CPT;
+// per-cell flags: inside the slab, and which of the z+/z-/y+/y- neighbours exist
+constexpr unsigned CF_VALID = 1u, CF_ZP = 2u, CF_ZM = 4u, CF_YP = 8u, CF_YM = 16u;
 constexpr uint32_t kWaitTries = 1u << 20;  // bounded mbarrier polling (well under a second)
 
 enum : int { PM_FIRST2 = 1, PM_FIRST = 2, PM_PROLONG = 4, PM_NOD = 8, PM_RZ = 16 };
@@ -179,7 +185,7 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
     if (PROL) Lc = cdesc[p];
     const long long csx = PROL ? (long long)Lc.ny * Lc.nz : 0;
     const int cr_lo = (y0 - 1) >> 1;  // logical first coarse row of the halo (may be -1)
-    auto slot_of = [&](int q) { return (char *)sm + ((q - pl_lo) % R) * lay.slot_bytes; };
+    auto slot_of = [&](int q) { return (char *)sm + ((unsigned)(q - pl_lo) % (unsigned)R) * lay.slot_bytes; };
 
     if (t == 0) {
         for (int s = 0; s < R; s++) {
@@ -228,6 +234,19 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
         __syncwarp();
     } else {
         // ---------------- consumers
+        // this thread's cells of the slab (the same in every plane) and their y/z neighbours
+        unsigned cfl[kCellsPerThread];
+#pragma unroll
+        for (int k = 0; k < kCellsPerThread; k++) {
+            const int tc = t + k * kPlaneThreads;
+            unsigned f = 0;
+            if (tc < ncell) {
+                const int ty = div_nz(L, tc), z = tc - ty * nz, y = y0 + ty;
+                f = CF_VALID | (z + 1 < nz ? CF_ZP : 0u) | (z > 0 ? CF_ZM : 0u) | (y + 1 < ny ? CF_YP : 0u) |
+                    (y > 0 ? CF_YM : 0u);
+            }
+            cfl[k] = f;
+        }
         int waited = pl_lo - 1;
         bool ok = true;
         for (int x = xa; x < xe && ok; x++) {
@@ -271,85 +290,87 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
                 }
                 if (!ok) break;
             }
-            for (int tc = t; tc < ncell; tc += kPlaneThreads) {
-                const int ty = div_nz(L, tc);
-                const int z = tc - ty * nz;
-                const int y = y0 + ty;
+            {
+                // per-plane addresses, shared by this thread's cells
                 const long long pb = L.off + (long long)x * sx;
                 const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
                 const int dh = stage_delta(lh, es), dp = stage_delta(lp, es);
                 char *sc = slot_of(x);
+                const bool xp = x + 1 < nx, xm = x > 0;
+                char *sn = xp ? slot_of(x + 1) : sc;
+                char *sq = xm ? slot_of(x - 1) : sc;
+                const int dn_ = xp ? stage_delta(lh + sx, es) : dh;
+                const int dq = xm ? stage_delta(lh - sx, es) : dh;
+                const int dqp = xm ? stage_delta(lp - sx, es) : dp;
                 const T *CX = (const T *)(sc + lay.oCX) + dp;
+                const T *CXq = (const T *)(sq + lay.oCX) + dqp;
                 const T *CY = (const T *)(sc + lay.oCY) + dh;  // logical row 0 = y0 - 1
                 const T *CZ = (const T *)(sc + lay.oCZ) + dp;
                 const T *LK = (const T *)(sc + lay.oLK) + dp;
-                const long long i = lp + tc;
-                const int c = nz + tc;  // own cell in halo coordinates
-                if (F2) {
-                    // x1 = invtheta b g at a cell; neighbours from the staged b and g halos
-                    const T *B = (const T *)(sc + lay.oB) + dh;
-                    const T *G = (const T *)(sc + lay.oG) + dh;
-                    const T bi = B[c], gi = G[c];
-                    const T x1 = invtheta * bi * gi;
-                    const T lk = LK[tc];
-                    T a = lk * x1;
-                    if (z + 1 < nz) a += CZ[tc] * (x1 - invtheta * B[c + 1] * G[c + 1]);
-                    if (z > 0)      a += CZ[tc - 1] * (x1 - invtheta * B[c - 1] * G[c - 1]);
-                    if (y + 1 < ny) a += CY[c] * (x1 - invtheta * B[c + nz] * G[c + nz]);
-                    if (y > 0)      a += CY[tc] * (x1 - invtheta * B[c - nz] * G[c - nz]);
-                    if (x + 1 < nx) {
-                        char *sn = slot_of(x + 1);
-                        const int dn_ = stage_delta(lh + sx, es);
-                        const T *Bn = (const T *)(sn + lay.oB) + dn_;
-                        const T *Gn = (const T *)(sn + lay.oG) + dn_;
-                        a += CX[tc] * (x1 - invtheta * Bn[c] * Gn[c]);
+#pragma unroll
+                for (int k = 0; k < kCellsPerThread; k++) {
+                    const unsigned f = cfl[k];
+                    if (!(f & CF_VALID)) continue;
+                    const int tc = t + k * kPlaneThreads;
+                    const long long i = lp + tc;
+                    const int c = nz + tc;  // own cell in halo coordinates
+                    if (F2) {
+                        // x1 = invtheta b g at a cell; neighbours from the staged b and g halos
+                        const T *B = (const T *)(sc + lay.oB) + dh;
+                        const T *G = (const T *)(sc + lay.oG) + dh;
+                        const T bi = B[c], gi = G[c];
+                        const T x1 = invtheta * bi * gi;
+                        T a = LK[tc] * x1;
+                        if (f & CF_ZP) a += CZ[tc] * (x1 - invtheta * B[c + 1] * G[c + 1]);
+                        if (f & CF_ZM) a += CZ[tc - 1] * (x1 - invtheta * B[c - 1] * G[c - 1]);
+                        if (f & CF_YP) a += CY[c] * (x1 - invtheta * B[c + nz] * G[c + nz]);
+                        if (f & CF_YM) a += CY[tc] * (x1 - invtheta * B[c - nz] * G[c - nz]);
+                        if (xp) {
+                            const T *Bn = (const T *)(sn + lay.oB) + dn_;
+                            const T *Gn = (const T *)(sn + lay.oG) + dn_;
+                            a += CX[tc] * (x1 - invtheta * Bn[c] * Gn[c]);
+                        }
+                        if (xm) {
+                            const T *Bq = (const T *)(sq + lay.oB) + dq;
+                            const T *Gq = (const T *)(sq + lay.oG) + dq;
+                            a += CXq[tc] * (x1 - invtheta * Bq[c] * Gq[c]);
+                        }
+                        const T dn = c1 * x1 + c2 * (bi - a) * gi;
+                        if (!NOD) d[i] = dn;
+                        xout[i] = x1 + dn;
+                    } else {
+                        const T *X = (const T *)(sc + lay.oX) + dh;
+                        const T xi = X[c];
+                        const T lk = LK[tc];
+                        T a = lk * xi, dg = lk;
+                        if (f & CF_ZP) { T w = CZ[tc];     a += w * (xi - X[c + 1]);  dg += w; }
+                        if (f & CF_ZM) { T w = CZ[tc - 1]; a += w * (xi - X[c - 1]);  dg += w; }
+                        if (f & CF_YP) { T w = CY[c];      a += w * (xi - X[c + nz]); dg += w; }
+                        if (f & CF_YM) { T w = CY[tc];     a += w * (xi - X[c - nz]); dg += w; }
+                        if (xp) {
+                            const T *Xn = (const T *)(sn + lay.oX) + dn_;
+                            T w = CX[tc];
+                            a += w * (xi - Xn[c]);
+                            dg += w;
+                        }
+                        if (xm) {
+                            const T *Xq = (const T *)(sq + lay.oX) + dq;
+                            T w = CXq[tc];
+                            a += w * (xi - Xq[c]);
+                            dg += w;
+                        }
+                        const T bi = ((const T *)(sc + lay.oB) + dp)[tc];
+                        T r;
+                        if constexpr (sizeof(T) == 8) r = (bi - a) * C.idg[i];
+                        else r = __fdividef(bi - a, dg);
+                        T dn;
+                        if (FIRST) dn = c2 * r;
+                        else dn = c1 * ((const T *)(sc + lay.oD) + dp)[tc] + c2 * r;
+                        const T xo = xi + dn;
+                        if (!NOD) d[i] = dn;
+                        xout[i] = xo;
+                        if (RZ) part = part + Acc<T>::prod(bi, xo);
                     }
-                    if (x > 0) {
-                        char *sq = slot_of(x - 1);
-                        const int dq = stage_delta(lh - sx, es);
-                        const T *Bq = (const T *)(sq + lay.oB) + dq;
-                        const T *Gq = (const T *)(sq + lay.oG) + dq;
-                        const T *CXq = (const T *)(sq + lay.oCX) + stage_delta(lp - sx, es);
-                        a += CXq[tc] * (x1 - invtheta * Bq[c] * Gq[c]);
-                    }
-                    const T dn = c1 * x1 + c2 * (bi - a) * gi;
-                    if (!NOD) d[i] = dn;
-                    xout[i] = x1 + dn;
-                } else {
-                    const T *X = (const T *)(sc + lay.oX) + dh;
-                    const T *B = (const T *)(sc + lay.oB) + dp;
-                    const T xi = X[c];
-                    const T lk = LK[tc];
-                    T a = lk * xi, dg = lk;
-                    if (z + 1 < nz) { T w = CZ[tc];     a += w * (xi - X[c + 1]);  dg += w; }
-                    if (z > 0)      { T w = CZ[tc - 1]; a += w * (xi - X[c - 1]);  dg += w; }
-                    if (y + 1 < ny) { T w = CY[c];     a += w * (xi - X[c + nz]); dg += w; }
-                    if (y > 0)      { T w = CY[tc];     a += w * (xi - X[c - nz]); dg += w; }
-                    if (x + 1 < nx) {
-                        const T *Xn = (const T *)(slot_of(x + 1) + lay.oX) + stage_delta(lh + sx, es);
-                        T w = CX[tc];
-                        a += w * (xi - Xn[c]);
-                        dg += w;
-                    }
-                    if (x > 0) {
-                        char *sq = slot_of(x - 1);
-                        const T *Xq = (const T *)(sq + lay.oX) + stage_delta(lh - sx, es);
-                        const T *CXq = (const T *)(sq + lay.oCX) + stage_delta(lp - sx, es);
-                        T w = CXq[tc];
-                        a += w * (xi - Xq[c]);
-                        dg += w;
-                    }
-                    const T bi = B[tc];
-                    T r;
-                    if constexpr (sizeof(T) == 8) r = (bi - a) * C.idg[i];
-                    else r = __fdividef(bi - a, dg);
-                    T dn;
-                    if (FIRST) dn = c2 * r;
-                    else dn = c1 * ((const T *)(sc + lay.oD) + dp)[tc] + c2 * r;
-                    const T xo = xi + dn;
-                    if (!NOD) d[i] = dn;
-                    xout[i] = xo;
-                    if (RZ) part = part + Acc<T>::prod(bi, xo);
                 }
             }
             // this warp is done with plane x-1
