@@ -33,6 +33,16 @@ constexpr int kPlaneStages = DPF_PLANE_STAGES;  // planes x-1, x, x+1 resident, 
 #endif
 constexpr int kPlaneCells = kPlaneThreads * DPF_PLANE_CPT;  // slab capacity (whole rows)
 constexpr int kCellsPerThread = DPF_PLANE_CPT;
+// Rows per slab: as many whole rows as fit `cells`, even (so that slabs align with the
+// 2x2x2 aggregates of the next level) unless one slab holds the whole plane. Host and
+// device both use it, so the work items and the kernels agree.
+__host__ __device__ __forceinline__ int plane_rows(int ny, int nz, int cells) {
+    int t = cells / nz;
+    if (t >= 2) t &= ~1;
+    if (t < 1) t = 1;
+    return t < ny ? t : ny;
+}
+
 // per-cell flags: inside the slab, and which of the z+/z-/y+/y- neighbours exist
 constexpr unsigned CF_VALID = 1u, CF_ZP = 2u, CF_ZM = 4u, CF_YP = 8u, CF_YM = 16u;
 constexpr uint32_t kWaitTries = 1u << 20;  // bounded mbarrier polling (well under a second)
@@ -71,6 +81,21 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *e
         if (mbar_try_wait(bar, parity)) return true;
     if (err) atomicExch(err, 1);
     return false;
+}
+// barrier 1 over the `count` consumer threads only (the producer warp does not take part),
+// returning the OR of `pred` over them: a shared error flag makes every consumer leave
+// together, so no consumer is left waiting at the barrier
+__device__ __forceinline__ bool consumer_sync_or(bool pred, int count) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "barrier.red.or.pred q, 1, %2, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)pred), "r"(count)
+        : "memory");
+    return r != 0;
 }
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
@@ -174,7 +199,7 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
     const LevelDesc L = desc[p];
     const int nz = L.nz, ny = L.ny, nx = L.nx;
     const long long sx = (long long)ny * nz;
-    const int Ty = max(1, min(ny, kPlaneCells / nz));
+    const int Ty = plane_rows(ny, nz, kPlaneCells);
     const int rows = min(Ty, ny - y0);
     const int ncell = rows * nz;
     const int t = threadIdx.x;
@@ -399,6 +424,163 @@ __device__ __forceinline__ void finish_pq(CgState &s, double pq, int *active_cou
     if (!isfinite(s.pq)) { s.alpha = 0.0; s.status = DPF_NAN; deactivate(s, active_count); }
     else if (!(s.pq > 0.0)) { s.alpha = 0.0; deactivate(s, active_count); }
     else s.alpha = s.rz / s.pq;
+}
+
+// Restriction on the plane ring: residuals b - A x of each fine plane of the slab go to a
+// shared buffer (two planes), and after every odd plane (or the grid's last) the coarse
+// cells of the slab sum their children in the order of cell_restrict (x, then y, then z),
+// so the coarse right-hand side is bitwise that of k_restrict. Slabs start on even rows and
+// chunks on even planes. Streams per plane: x with halo rows, b, cx, cy (+ row below), cz, leak.
+template <typename T>
+__global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
+    const LevelDesc *__restrict__ desc, const LevelDesc *__restrict__ cdesc, const int4 *__restrict__ items,
+    const CgState *st, Coeffs<T> C, const T *__restrict__ b, const T *__restrict__ xin, T *__restrict__ bc,
+    PlaneLayout lay, int *err) {
+    constexpr int R = kPlaneStages;
+    constexpr int es = (int)sizeof(T);
+    constexpr int kConsumerWarps = kPlaneThreads / 32;
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ uint64_t full[R], empty[R];
+    __shared__ T res[2][kPlaneCells];
+
+    const int4 it = items[blockIdx.x];
+    const int p = it.x, y0 = it.y, xa = it.z, xe = it.w;
+    if (st && !st[p].active) return;
+    const LevelDesc L = desc[p];
+    const LevelDesc Lc = cdesc[p];
+    const int nz = L.nz, ny = L.ny, nx = L.nx;
+    const long long sx = (long long)ny * nz;
+    const int Ty = plane_rows(ny, nz, kPlaneCells);
+    const int rows = min(Ty, ny - y0);
+    const int ncell = rows * nz;
+    const int t = threadIdx.x;
+    const int warp = t >> 5, lane = t & 31;
+    const int pl_lo = max(xa - 1, 0), pl_hi = min(xe, nx - 1);
+    const int h0 = max(y0 - 1, 0), h1 = min(y0 + rows + 1, ny);
+    auto slot_of = [&](int q) { return (char *)sm + ((unsigned)(q - pl_lo) % (unsigned)R) * lay.slot_bytes; };
+    // coarse cells of the slab: rows y0/2 .. (y0+rows-1)/2, all coarse z
+    const int cy0 = y0 >> 1, crows = ((y0 + rows - 1) >> 1) - cy0 + 1;
+    const int ncc = crows * Lc.nz;
+
+    if (t == 0) {
+        for (int s = 0; s < R; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kConsumerWarps);
+        }
+        fence_mbarrier_init();
+    }
+    __syncthreads();
+
+    if (warp == kConsumerWarps) {
+        if (lane == 0) {
+            pm_produce<R>(pl_lo, pl_hi, full, empty, sm, lay.slot_bytes, err, [&](int q, char *slot, uint64_t *bar) {
+                const long long pb = L.off + (long long)q * sx;
+                const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
+                const long long hA = pb + (long long)h0 * nz, hB = pb + (long long)h1 * nz, pE = lp + ncell;
+                auto stage = [&](const void *base, long long l0, long long a0, long long a1, int off) {
+                    const BulkRange r = make_range(base, es, l0, a0, a1, slot + off);
+                    mbar_expect_tx(bar, r.bytes);
+                    bulk_copy_g2s(r.dst, r.src, r.bytes, bar);
+                };
+                stage(xin, lh, hA, hB, lay.oX);
+                stage(b, lp, lp, pE, lay.oB);
+                stage(C.cx, lp, lp, pE, lay.oCX);
+                stage(C.cy, lh, hA, pE, lay.oCY);
+                stage(C.cz, lp, lp, pE, lay.oCZ);
+                stage(C.leak, lp, lp, pE, lay.oLK);
+            });
+        }
+        __syncwarp();
+        return;
+    }
+    // ---------------- consumers
+    unsigned cfl[kCellsPerThread];
+#pragma unroll
+    for (int k = 0; k < kCellsPerThread; k++) {
+        const int tc = t + k * kPlaneThreads;
+        unsigned f = 0;
+        if (tc < ncell) {
+            const int ty = div_nz(L, tc), z = tc - ty * nz, y = y0 + ty;
+            f = CF_VALID | (z + 1 < nz ? CF_ZP : 0u) | (z > 0 ? CF_ZM : 0u) | (y + 1 < ny ? CF_YP : 0u) |
+                (y > 0 ? CF_YM : 0u);
+        }
+        cfl[k] = f;
+    }
+    int waited = pl_lo - 1;
+    bool bad = false;
+    for (int x = xa; x < xe; x++) {
+        const int need = min(x + 1, pl_hi);
+        while (!bad && waited < need) {
+            const int u = waited + 1 - pl_lo;
+            if (!mbar_wait(&full[u % R], (uint32_t)((u / R) & 1), err)) bad = true;
+            else waited++;
+        }
+        if (!bad) {
+            const long long pb = L.off + (long long)x * sx;
+            const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
+            const int dh = stage_delta(lh, es), dp = stage_delta(lp, es);
+            char *sc = slot_of(x);
+            const bool xp = x + 1 < nx, xm = x > 0;
+            char *sn = xp ? slot_of(x + 1) : sc;
+            char *sq = xm ? slot_of(x - 1) : sc;
+            const int dn_ = xp ? stage_delta(lh + sx, es) : dh;
+            const int dq = xm ? stage_delta(lh - sx, es) : dh;
+            const int dqp = xm ? stage_delta(lp - sx, es) : dp;
+            const T *X = (const T *)(sc + lay.oX) + dh;
+            const T *B = (const T *)(sc + lay.oB) + dp;
+            const T *CX = (const T *)(sc + lay.oCX) + dp;
+            const T *CXq = (const T *)(sq + lay.oCX) + dqp;
+            const T *CY = (const T *)(sc + lay.oCY) + dh;
+            const T *CZ = (const T *)(sc + lay.oCZ) + dp;
+            const T *LK = (const T *)(sc + lay.oLK) + dp;
+            const T *Xn = (const T *)(sn + lay.oX) + dn_;
+            const T *Xq = (const T *)(sq + lay.oX) + dq;
+            T *rs = res[x & 1];
+#pragma unroll
+            for (int k = 0; k < kCellsPerThread; k++) {
+                const unsigned f = cfl[k];
+                if (!(f & CF_VALID)) continue;
+                const int tc = t + k * kPlaneThreads;
+                const int c = nz + tc;
+                const T xi = X[c];
+                T a = LK[tc] * xi;
+                if (f & CF_ZP) a += CZ[tc] * (xi - X[c + 1]);
+                if (f & CF_ZM) a += CZ[tc - 1] * (xi - X[c - 1]);
+                if (f & CF_YP) a += CY[c] * (xi - X[c + nz]);
+                if (f & CF_YM) a += CY[tc] * (xi - X[c - nz]);
+                if (xp) a += CX[tc] * (xi - Xn[c]);
+                if (xm) a += CXq[tc] * (xi - Xq[c]);
+                rs[tc] = B[tc] - a;
+            }
+        }
+        // planes x-1 is no longer needed by this warp
+        __syncwarp();
+        if (lane == 0 && x - 1 >= pl_lo) mbar_arrive(&empty[(x - 1 - pl_lo) % R]);
+        const bool pair_done = (x & 1) || x + 1 == nx;
+        if (!pair_done) continue;
+        if (consumer_sync_or(bad, kPlaneThreads)) break;  // residuals of the pair are in res[]
+        const int X0 = x & ~1;
+        const int cx = X0 >> 1;
+        const bool two = X0 + 1 < nx;
+        const long long cb = Lc.off + (long long)cx * Lc.ny * Lc.nz + (long long)cy0 * Lc.nz;
+        for (int tcc = t; tcc < ncc; tcc += kPlaneThreads) {
+            const int cr = div_nz(Lc, tcc), czz = tcc - cr * Lc.nz;
+            const int fy0 = 2 * (cy0 + cr) - y0, fz0 = 2 * czz;
+            const bool y2 = 2 * (cy0 + cr) + 1 < ny, z2 = fz0 + 1 < nz;
+            T acc = 0;
+            for (int ix = 0; ix < (two ? 2 : 1); ix++) {
+                const T *r = res[(X0 + ix) & 1];
+                acc += r[fy0 * nz + fz0];
+                if (z2) acc += r[fy0 * nz + fz0 + 1];
+                if (y2) {
+                    acc += r[(fy0 + 1) * nz + fz0];
+                    if (z2) acc += r[(fy0 + 1) * nz + fz0 + 1];
+                }
+            }
+            bc[cb + tcc] = acc;
+        }
+        if (consumer_sync_or(bad, kPlaneThreads)) break;  // res[] may be overwritten
+    }
 }
 
 }  // namespace dpf

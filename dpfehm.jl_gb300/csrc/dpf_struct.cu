@@ -1185,12 +1185,13 @@ void StructBatch::build_plane_items(PlaneItems &P, const Level &L, const std::ve
     for (int p = 0; p < nprob; p++) {
         if (!take[p]) continue;
         const LevelDesc &D = L.h_desc[p];
-        const int Ty = std::max(1, std::min(D.ny, cells / D.nz));
+        const int Ty = plane_rows(D.ny, D.nz, cells);
         const int ytiles = (D.ny + Ty - 1) / Ty;
         long long chunks = (long long)((double)target * (double)D.n / (double)total / ytiles);
         chunks = std::max(1LL, std::min(chunks, (long long)D.nx));
         int xc = (int)((D.nx + chunks - 1) / chunks);
         xc = std::max(xc, std::min(2, D.nx));
+        xc += xc & 1;  // chunks start on even planes (restriction pairs planes)
         pinfo[p].x = (int)items.size();
         for (int y0 = 0; y0 < D.ny; y0 += Ty)
             for (int x0 = 0; x0 < D.nx; x0 += xc) items.push_back(make_int4(p, y0, x0, std::min(x0 + xc, D.nx)));
@@ -1614,6 +1615,32 @@ void StructBatch::pm_launch(int mode, int l, const T *b, const T *xin, T *xout, 
 #undef DPF_PM_CASE
 }
 
+// Plane-marching restriction of level l's residual into level l+1 (the smoothed problems).
+template <typename T>
+void StructBatch::pm_restrict(int l, const T *b, const T *x, T *bc) {
+    Level &L = lv[l];
+    const int es = (int)sizeof(T);
+    PlaneLayout lay{};
+    int off = 0;
+    auto take = [&](int bytes) { int o = off; off += bytes; return o; };
+    lay.oX = take(pm_region(L.pm.halo, es));
+    lay.oB = take(pm_region(L.pm.slab, es));
+    lay.oCX = take(pm_region(L.pm.slab, es));
+    lay.oCY = take(pm_region(L.pm.cy, es));
+    lay.oCZ = take(pm_region(L.pm.slab, es));
+    lay.oLK = take(pm_region(L.pm.slab, es));
+    lay.oD = lay.oG = lay.oDIR = lay.oE = -1;
+    lay.slot_bytes = (off + 127) & ~127;
+    const size_t smem = (size_t)kPlaneStages * lay.slot_bytes;
+    static size_t configured = 0;
+    if (smem > 48 * 1024 - 2 * kPlaneCells * sizeof(T) && smem > configured) {
+        CK(cudaFuncSetAttribute(k_pm_restrict<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = smem;
+    }
+    k_pm_restrict<T><<<(unsigned)L.pm.n, kPlaneThreads + 32, smem, stream>>>(
+        L.d_desc, lv[l + 1].d_desc, L.pm.items, d_state, coeffs_of<T>(L, mixed), b, x, bc, lay, d_factor_status + 1);
+}
+
 template <typename T>
 void StructBatch::vcycle(const T *r, T *z) {
     const int deg = opt.cheb_degree;
@@ -1646,9 +1673,8 @@ void StructBatch::vcycle(const T *r, T *z) {
             pre[l] = cur;
             Level &Cn = lv[l + 1];
             {
-                KTimer _kt(this, kname("k_restrict", l + 1, sizeof(T) == 4), Cn.restr_cells);
-                k_restrict<T><<<nb_of(Cn.restr), kBlock, 0, stream>>>(L.d_desc, Cn.d_desc, Cn.restr.d_map, d_state, C, b,
-                                                                     cur, (T *)Cn.work[2]);
+                KTimer _kt(this, kname("k_pm_restrict", l + 1, sizeof(T) == 4), Cn.restr_cells);
+                pm_restrict<T>(l, b, cur, (T *)Cn.work[2]);
             }
             LAUNCH_CHECK();
         } else if (nb_of(L.smooth)) {

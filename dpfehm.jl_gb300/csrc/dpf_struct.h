@@ -113,6 +113,8 @@ public:
     void build_plane_items(PlaneItems &P, const Level &L, const std::vector<int> &take, int sms, int cells,
                            const std::vector<std::vector<std::array<int, 3>>> *shapes, int l);
     template <typename T>
+    void pm_restrict(int l, const T *b, const T *x, T *bc);
+    template <typename T>
     void pm_launch(int mode, int l, const T *b, const T *xin, T *xout, T *d, const T *e, T c1, T c2, T invth, T sc);
     template <typename T>
     void pcg(const T *b, T *x, double tol2);
