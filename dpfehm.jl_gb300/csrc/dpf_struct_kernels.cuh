@@ -53,16 +53,43 @@ __device__ __forceinline__ double warp_sum(double v) {
 // each product is formed exactly as an unevaluated float pair (fmaf error term)
 // and pairs are added with Knuth's two-sum, giving about 48 significant bits;
 // only the per-block result is converted to double.
+// Double-float (hi + lo) arithmetic. Additions and products inside an error-free
+// transformation use the _rn intrinsics, which the compiler never contracts into a fused
+// multiply-add (a contraction would make the captured rounding errors inexact).
+#ifndef DPF_DF_STRICT_ACC
+#define DPF_DF_STRICT_ACC 1
+#endif
+#ifndef DPF_DF_STRICT_VEC
+#define DPF_DF_STRICT_VEC 1
+#endif
+#if DPF_DF_STRICT_ACC
+#define DPF_ACC_ADD(a, b) __fadd_rn(a, b)
+#define DPF_ACC_SUB(a, b) __fsub_rn(a, b)
+#define DPF_ACC_MUL(a, b) __fmul_rn(a, b)
+#else
+#define DPF_ACC_ADD(a, b) ((a) + (b))
+#define DPF_ACC_SUB(a, b) ((a) - (b))
+#define DPF_ACC_MUL(a, b) ((a) * (b))
+#endif
+#if DPF_DF_STRICT_VEC
+#define DPF_VEC_ADD(a, b) __fadd_rn(a, b)
+#define DPF_VEC_SUB(a, b) __fsub_rn(a, b)
+#define DPF_VEC_MUL(a, b) __fmul_rn(a, b)
+#else
+#define DPF_VEC_ADD(a, b) ((a) + (b))
+#define DPF_VEC_SUB(a, b) ((a) - (b))
+#define DPF_VEC_MUL(a, b) ((a) * (b))
+#endif
 struct DF {
     float hi, lo;
 };
 __device__ __forceinline__ DF df_add(DF a, DF b) {
-    float s = a.hi + b.hi;
-    float bb = s - a.hi;
-    float e = (a.hi - (s - bb)) + (b.hi - bb);
-    e += a.lo + b.lo;
-    float h = s + e;
-    return DF{h, e - (h - s)};
+    const float s = DPF_ACC_ADD(a.hi, b.hi);
+    const float bb = DPF_ACC_SUB(s, a.hi);
+    float e = DPF_ACC_ADD(DPF_ACC_SUB(a.hi, DPF_ACC_SUB(s, bb)), DPF_ACC_SUB(b.hi, bb));
+    e = DPF_ACC_ADD(e, DPF_ACC_ADD(a.lo, b.lo));
+    const float h = DPF_ACC_ADD(s, e);
+    return DF{h, DPF_ACC_SUB(e, DPF_ACC_SUB(h, s))};
 }
 __device__ __forceinline__ DF df_shfl(DF a, int o) {
     return DF{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
@@ -83,7 +110,7 @@ struct Acc<float> {
     DF v = DF{0.f, 0.f};
     __device__ __forceinline__ static Acc prod(float a, float b) {
         Acc r;
-        float p = a * b;
+        const float p = DPF_ACC_MUL(a, b);
         r.v = DF{p, fmaf(a, b, -p)};
         return r;
     }
@@ -216,22 +243,22 @@ __device__ __forceinline__ void deactivate(CgState &s, int *count) {
 
 // double-float arithmetic: unevaluated sums hi + lo of two floats (about 48 bits)
 __device__ __forceinline__ float2 df_two_sum(float a, float b) {
-    float s = a + b;
-    float bb = s - a;
-    return make_float2(s, (a - (s - bb)) + (b - bb));
+    const float s = DPF_VEC_ADD(a, b);
+    const float bb = DPF_VEC_SUB(s, a);
+    return make_float2(s, DPF_VEC_ADD(DPF_VEC_SUB(a, DPF_VEC_SUB(s, bb)), DPF_VEC_SUB(b, bb)));
 }
 __device__ __forceinline__ float2 df_quick(float a, float b) {
-    float s = a + b;
-    return make_float2(s, b - (s - a));
+    const float s = DPF_VEC_ADD(a, b);
+    return make_float2(s, DPF_VEC_SUB(b, DPF_VEC_SUB(s, a)));
 }
 __device__ __forceinline__ float2 df_add(float2 a, float2 b) {
     float2 s = df_two_sum(a.x, b.x);
-    s.y += a.y + b.y;
+    s.y = DPF_VEC_ADD(s.y, DPF_VEC_ADD(a.y, b.y));
     return df_quick(s.x, s.y);
 }
 __device__ __forceinline__ float2 df_sub(float2 a, float2 b) { return df_add(a, make_float2(-b.x, -b.y)); }
 __device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
-    float p = a.x * b.x;
+    const float p = DPF_VEC_MUL(a.x, b.x);
     float e = fmaf(a.x, b.x, -p);
     e = fmaf(a.x, b.y, e);
     e = fmaf(a.y, b.x, e);
