@@ -438,11 +438,19 @@ def main():
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch the CG loop from the host (ncu cannot profile kernels inside conditional graphs)")
     ap.add_argument("--main-only", action="store_true", help="only the timed region (for profiling runs)")
+    ap.add_argument("--workload", default="steady_1m", choices=["steady_1m", "steady_100k", "uneven_batch", "transient"],
+                    help="steady_1m is the headline; the others are the remaining configurations (bench_workloads.py)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     dist, rank, ws = _dist()
-    out = run_reference(args, dist, rank, ws) if args.impl == "reference" else run_ours(args, dist, rank, ws)
+    if args.workload != "steady_1m" and args.impl == "ours":
+        import bench_workloads
+        if args.batch == 8:
+            args.batch = 0  # the workload's own default batch
+        out = bench_workloads.run(args.workload, args, dist, rank, ws)
+    else:
+        out = run_reference(args, dist, rank, ws) if args.impl == "reference" else run_ours(args, dist, rank, ws)
     if rank == 0 and out is not None:
         print(json.dumps(out), flush=True)
     if dist is not None:

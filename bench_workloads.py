@@ -1,0 +1,238 @@
+"""Secondary benchmark workloads: the other configurations of the groundwater path, timed
+with the same harness as bench.py's headline (CUDA events on the solver stream, W warm-up
+steps, L2 flushed between steps, a plain FP64 GPU run of the same workload beside it).
+
+    python bench.py --workload steady_100k     # 100x100x10, layered Matern (l=50, s=1), J at 100 cells
+    python bench.py --workload uneven_batch    # 256 realizations of 4 grid sizes (~73M cells), random
+                                               # l, sigma, 1-4 injection and 1-4 Dirichlet cells
+    python bench.py --workload transient       # 200x200x20, 100 backward-Euler steps of 3600 s,
+                                               # Dirichlet x = max face, J = sum_t sum_50obs h^2
+
+All inputs are seeded synthetic data. One "solve" is a forward + adjoint (for the transient
+workload: the whole 100-step forward run and its adjoint).
+"""
+import os
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+
+
+def _events(torch, fn, steps, warmup, flush):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for k in range(steps):
+        flush.add_(1.0)
+        ev[k][0].record()
+        fn()
+        ev[k][1].record()
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev) / 1e3
+
+
+def _rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+# ---------------------------------------------------------------- steady, 100k cells
+def steady_100k(pkg, torch, dev, args):
+    grid, mins, maxs = (100, 100, 10), (0.0, 0.0, 0.0), (50.0, 50.0, 5.0)
+    N = 100 * 100 * 10
+    B = args.batch if args.batch else 64
+    logK = np.concatenate([pkg.fields.layered_logk(grid, mins, maxs, 50.0, 1.0, -9.0, 5000 + p) for p in range(B)])
+    Qs = np.zeros(B * N)
+    Qs[np.arange(B) * N] = 1e-4
+    dh = np.zeros(B * N)
+    rng = np.random.default_rng(17)
+    obs = [rng.choice(N, 100, replace=False) for _ in range(B)]
+
+    def make(prec, tol):
+        return pkg.GroundwaterBatch([grid] * B, [mins] * B, [maxs] * B, [[N - 1]] * B, reltol=tol, precision=prec)
+
+    d = [torch.tensor(x, device=dev) for x in (logK, dh, Qs)]
+    res = {"workload": "gw_steady_fwd_adj_100x100x10_layered_l50_s1", "cells": N, "batch_per_gpu": B,
+           "problems": B}
+    return res, make, d, obs, B, [(grid, mins, maxs, [N - 1], slice(0, N))]
+
+
+# ---------------------------------------------------------------- uneven batch
+def uneven_batch(pkg, torch, dev, args):
+    sizes = [(50, 50, 5), (100, 100, 10), (150, 150, 10), (200, 200, 20)]
+    B = args.batch if args.batch else 256
+    rng = np.random.default_rng(33)
+    grids, mins, maxs, dns, Q, lks, obs = [], [], [], [], [], [], []
+    for p in range(B):
+        g = sizes[rng.integers(4)]
+        mx = tuple(0.5 * (n - 1) for n in g)
+        N = int(np.prod(g))
+        ell = rng.uniform(0.5, 2.0) * mx[0]
+        sig = rng.uniform(0.5, 2.0)
+        lks.append(pkg.fields.volume_logk_torch(g, (0, 0, 0), mx, ell, sig, -9.0, 9000 + p, device=dev))
+        cells = rng.choice(N, 8, replace=False)
+        ninj, ndir = 1 + rng.integers(4), 1 + rng.integers(4)
+        q = np.zeros(N)
+        q[cells[:ninj]] = rng.uniform(1e-5, 1e-3, ninj)
+        grids.append(g), mins.append((0.0, 0.0, 0.0)), maxs.append(mx)
+        dns.append(np.sort(cells[4:4 + ndir]))
+        Q.append(q)
+        obs.append(rng.choice(N, 100, replace=False))
+    logK = torch.cat(lks)
+    Qs = torch.tensor(np.concatenate(Q), device=dev)
+    dh = torch.zeros_like(Qs)
+
+    def make(prec, tol):
+        return pkg.GroundwaterBatch(grids, mins, maxs, dns, reltol=tol, precision=prec)
+
+    cells = int(sum(np.prod(g) for g in grids))
+    res = {"workload": "gw_steady_fwd_adj_uneven_batch_256", "cells": cells, "batch_per_gpu": B, "problems": B,
+           "sizes": "uniform over 50x50x5, 100x100x10, 150x150x10, 200x200x20 (0.5 m spacing)"}
+    off = np.concatenate([[0], np.cumsum([np.prod(g) for g in grids])]).astype(np.int64)
+    check = [(grids[p], mins[p], maxs[p], dns[p], slice(off[p], off[p + 1])) for p in range(min(B, 4))]
+    return res, make, [logK, dh, Qs], obs, B, check
+
+
+def run_steady(name, args, dist, rank, ws, METRIC_NAME):
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    ge._load_build_module().build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    cfg, make, d, obs, B, check = (steady_100k if name == "steady_100k" else uneven_batch)(pkg, torch, dev, args)
+    flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float64, device=dev)
+    import warnings
+    warnings.simplefilter("error", RuntimeWarning)
+    mixed = make(args.precision, 1e-10)
+    t = _events(torch, lambda: mixed.solve_grad_logk(*d, obs), args.steps, args.warmup, flush)
+    h, g = mixed.solve_grad_logk(*d, obs)
+    # e2e: page-locked host buffers in and out
+    hosts = [x.cpu().pin_memory() for x in d]
+    hh = torch.empty(mixed.N, dtype=torch.float64).pin_memory()
+    hg = torch.empty(mixed.N, dtype=torch.float64).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        mixed.solve_grad_logk(*[x.numpy() for x in hosts], obs, out=(hh.numpy(), hg.numpy()))
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    # plain FP64 GPU and accuracy against an FP64 solve at 1e-13
+    plain = make("fp64", 1e-10)
+    t64 = _events(torch, lambda: plain.solve_grad_logk(*d, obs), max(1, args.steps // 2), 1, flush)
+    ref = make("fp64", 1e-13)
+    warnings.simplefilter("ignore", RuntimeWarning)
+    h64, g64 = ref.solve_grad_logk(*d, obs)
+    h, g, h64, g64 = (x.cpu().numpy() for x in (h, g, h64, g64))
+    errs = [(_rel(h[s], h64[s]), _rel(g[s], g64[s])) for (_, _, _, _, s) in check]
+    solves = B * args.steps
+    out = {
+        "metric": METRIC_NAME, "value": round(solves / t, 3), "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * t / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 V-cycle + double-float CG (f32 ops), f64 residual",
+        "data": "synthetic (seeded Matern logK fields)", "config": dict(cfg, precision=args.precision, reltol=1e-10,
+                                                                      l2="flushed between timed steps"),
+        "e2e": {"value": round(solves / t_e2e, 3), "unit": "solves/s",
+                "h2d_bytes_per_step": int(3 * 8 * mixed.N), "d2h_bytes_per_step": int(2 * 8 * mixed.N)},
+        "plain_fp64_gpu": {"value": round(B * max(1, args.steps // 2) / t64, 3), "unit": "solves/s"},
+        "accuracy": {"max_rel_head_err_vs_fp64_1e-13": max(e[0] for e in errs),
+                     "max_rel_grad_err_vs_fp64_1e-13": max(e[1] for e in errs), "problems_checked": len(errs)},
+        "iterations_last_adjoint": mixed.stats["iterations"],
+    }
+    out["speedup_vs_plain_fp64"] = round(out["value"] / out["plain_fp64_gpu"]["value"], 3)
+    if name == "steady_100k" and not args.no_cpu_baseline:
+        # the oracle on realization 0: parity and the CPU rate at this size
+        import sys
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+        orc.build()
+        orc.set_threads(os.cpu_count() or 1)
+        grid, mn, mx, dn, s = check[0]
+        _, nb, aol, _ = pkg.regulargrid3d(mn, mx, grid)
+        lk = d[0][s].cpu().numpy()
+        t0 = time.perf_counter()
+        O = orc.Problem(s.stop - s.start, nb, aol, np.asarray(dn, np.int64))
+        ho = O.steady(orc.logk_to_faces(nb, lk), np.zeros(s.stop - s.start), d[2][s].cpu().numpy(), reltol=1e-14)
+        delta = np.zeros(s.stop - s.start)
+        np.add.at(delta, obs[0], 2 * ho[obs[0]])
+        dKs, _, _ = O.adjoint(np.zeros(s.stop - s.start), delta, reltol=1e-14)
+        go = orc.logk_to_faces_vjp(nb, lk, dKs)
+        tc = time.perf_counter() - t0
+        out["accuracy"]["rel_head_err_vs_oracle"] = _rel(h[s], ho)
+        out["accuracy"]["rel_grad_err_vs_oracle"] = _rel(g[s], go)
+        out["cpu_baseline"] = {"value": round(1.0 / tc, 4), "unit": "solves/s", "cores": os.cpu_count() or 1,
+                               "kind": "port", "sample": "one forward+adjoint of realization 0 (oracle, reltol 1e-14)"}
+    return out
+
+
+# ---------------------------------------------------------------- transient
+def run_transient(args, dist, rank, ws, METRIC_NAME):
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    ge._load_build_module().build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    grid, mins, maxs = (200, 200, 20), (0.0, 0.0, 0.0), (100.0, 100.0, 10.0)
+    nx, ny, nz = grid
+    N = nx * ny * nz
+    lk = pkg.fields.volume_logk(grid, mins, maxs, 30.0, 1.5, -9.0, 777)
+    rng = np.random.default_rng(55)
+    dn = np.arange((nx - 1) * ny * nz, N)  # the x = max face
+    free = np.arange(0, (nx - 1) * ny * nz)
+    Qs = np.zeros(N)
+    Qs[rng.choice(free, 4, replace=False)] = 1e-3
+    obs = rng.choice(free, 50, replace=False)
+    Ss = np.full(N, 1e-5)
+    dt, nsteps, ck = 3600.0, 100, 10
+    flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float64, device=dev)
+    import warnings
+    warnings.simplefilter("error", RuntimeWarning)
+
+    def make(prec, tol):
+        return pkg.GroundwaterProblem.regular3d(mins, maxs, grid, dn, reltol=tol, precision=prec)
+
+    d_lk = torch.tensor(lk, device=dev)
+    d = {k: torch.tensor(v, device=dev) for k, v in (("dh", np.zeros(N)), ("Q", Qs), ("S", Ss), ("h0", np.zeros(N)))}
+    w = torch.ones(50, dtype=torch.float64, device=dev)
+
+    def run(P):
+        Ks = P.logk_to_faces(d_lk)
+        P.transient_forward(Ks, d["dh"], d["Q"], d["S"], dt, nsteps, d["h0"], checkpoint_every=ck)
+        return P.transient_adjoint(obs, weights=w)
+
+    mixed = make(args.precision, 1e-10)
+    steps = max(1, args.steps // 2)
+    t = _events(torch, lambda: run(mixed), steps, max(1, args.warmup - 1), flush)
+    dK = run(mixed)[0]
+    plain = make("fp64", 1e-10)
+    t64 = _events(torch, lambda: run(plain), 1, 1, flush)
+    warnings.simplefilter("ignore", RuntimeWarning)
+    dK64 = run(make("fp64", 1e-13))[0]
+    return {
+        "metric": METRIC_NAME, "value": round(steps / t, 4), "unit": "runs/s", "n_gpus": ws, "steps": steps,
+        "warmup": max(1, args.warmup - 1), "ms_per_step": round(1e3 * t / steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 V-cycle + double-float CG (f32 ops), f64 residual",
+        "data": "synthetic (seeded Matern logK field)",
+        "config": {"workload": "gw_transient_fwd_adj_200x200x20_100steps_ckpt10", "cells": N, "steps": nsteps,
+                   "dt": dt, "checkpoint_every": ck, "dirichlet": "x = max face (4000 cells)", "obs": 50,
+                   "precision": args.precision, "reltol": 1e-10},
+        "plain_fp64_gpu": {"value": round(1.0 / t64, 4), "unit": "runs/s"},
+        "speedup_vs_plain_fp64": round(t64 / (t / steps), 3),
+        "accuracy": {"rel_dKs_err_vs_fp64_1e-13": _rel(dK.cpu().numpy(), dK64.cpu().numpy())},
+    }
+
+
+def run(name, args, dist, rank, ws):
+    if rank != 0:
+        return None
+    if name == "transient":
+        return run_transient(args, dist, rank, ws, "transient forward+adjoint runs/sec, 800k cells x 100 BE steps")
+    metric = ("forward+adjoint solves/sec at 100k cells" if name == "steady_100k"
+              else "forward+adjoint solves/sec, uneven batch of 256 grids")
+    return run_steady(name, args, dist, rank, ws, metric)

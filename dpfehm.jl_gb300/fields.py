@@ -48,3 +48,27 @@ def volume_logk(ns3, mins, maxs, ell, sigma, mean, seed):
     """Fully 3-D field; returned flat in cell order (z fastest)."""
     sp = [_spacing(mins[i], maxs[i], ns3[i]) for i in range(3)]
     return matern_field(ns3, sp, ell, sigma, mean, seed).ravel()
+
+
+def volume_logk_torch(ns3, mins, maxs, ell, sigma, mean, seed, device="cuda"):
+    """The spectral synthesis of matern_field (nu = 1) on a torch device (FFT by torch), for
+    large batches of synthetic inputs; white noise from torch's generator, so the draws
+    differ from the numpy sampler's for the same seed, and the periodic padding is capped
+    at 2n per axis. Returns a flat float64 tensor (z fastest)."""
+    import torch
+    ns = tuple(int(n) for n in ns3)
+    sp = [_spacing(mins[i], maxs[i], ns[i]) for i in range(3)]
+    pads = []
+    for n, h in zip(ns, sp):
+        p = int(n + min(np.ceil(1.5 * ell / h), 2 * n))  # padding capped at 2n for long correlation lengths
+        pads.append(p + (p % 2))
+    f = [torch.fft.fftfreq(p, h, dtype=torch.float64, device=device) for p, h in zip(pads, sp)]
+    k2 = ((2 * np.pi * f[0])[:, None, None] ** 2 + (2 * np.pi * f[1])[None, :, None] ** 2 +
+          (2 * np.pi * f[2])[None, None, :] ** 2)
+    spec = (2.0 / ell ** 2 + k2) ** (-(1.0 + 1.5))
+    spec = spec / spec.mean()
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    w = torch.randn(pads, dtype=torch.float64, device=device, generator=g)
+    field = torch.fft.ifftn(torch.fft.fftn(w) * torch.sqrt(spec)).real
+    return (mean + sigma * field[: ns[0], : ns[1], : ns[2]]).contiguous().reshape(-1)
