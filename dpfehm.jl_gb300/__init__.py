@@ -361,6 +361,39 @@ class GroundwaterBatch(GroundwaterProblem):
         return h, g
 
 
+_TUNED = ("cheb_degree", "plane_cells", "plane_blocks_per_sm", "tail_cells", "blocks_per_sm")
+
+
+def autotune_batch(dims, mins, maxs, dirichletnodes, logK, dirichleths, Qs, obs_per_problem, mean="geometric",
+                   repeats=2, **options):
+    """Choose the smoother degree and launch shapes for a batch by timing forward + adjoint
+    solves of these inputs (the library's dpf_batch_autotune). Returns ({option: value}
+    for the tuned options, ms per solve call); pass the dict to GroundwaterBatch."""
+    lib = load()
+    dims = np.ascontiguousarray(np.asarray(dims, dtype=np.int32).reshape(-1, 3))
+    nprob = dims.shape[0]
+    mn = np.ascontiguousarray(np.asarray(mins, dtype=np.float64).reshape(nprob, 3))
+    mx = np.ascontiguousarray(np.asarray(maxs, dtype=np.float64).reshape(nprob, 3))
+    nd = np.ascontiguousarray([len(d) for d in dirichletnodes], dtype=np.int64)
+    dn = np.ascontiguousarray(np.concatenate([np.asarray(d, dtype=np.int64) for d in dirichletnodes])
+                              if nd.sum() else np.zeros(0, np.int64))
+    N = int(np.prod(dims, axis=1).sum())
+    lk, d, q = _Buf(logK, n=N), _Buf(dirichleths, n=N), _Buf(Qs, n=N)
+    offs = np.zeros(nprob + 1, np.int64)
+    offs[1:] = np.cumsum([len(o) for o in obs_per_problem])
+    ob = np.ascontiguousarray(np.concatenate([np.asarray(o, np.int64) for o in obs_per_problem])
+                              if offs[-1] else np.zeros(0, np.int64))
+    base = _options(**options)
+    best = _lib.Options()
+    ms = ctypes.c_double()
+    rc = lib.dpf_batch_autotune(nprob, dims.ctypes.data, mn.ctypes.data, mx.ctypes.data, nd.ctypes.data,
+                                dn.ctypes.data, ctypes.byref(base), lk.ptr, _MEANS[mean], d.ptr, q.ptr,
+                                offs.ctypes.data, ob.ctypes.data, int(repeats), ctypes.byref(best), ctypes.byref(ms))
+    if rc != _lib.DPF_OK:
+        raise DPFError(rc, "autotuning failed (the starting options do not give a converged solve)")
+    return {k: getattr(best, k) for k in _TUNED}, ms.value
+
+
 # ------------------------------------------------------ reference-shaped API
 _cache = OrderedDict()
 _CACHE_MAX = 8

@@ -33,6 +33,8 @@ class Options(ctypes.Structure):
         ("blocks_per_sm", ctypes.c_int),
         ("tail_cells", ctypes.c_int),
         ("plane", ctypes.c_int),
+        ("plane_cells", ctypes.c_int),
+        ("plane_blocks_per_sm", ctypes.c_int),
     ]
 
 
@@ -64,6 +66,9 @@ SIGNATURES = {
     "dpf_transient_forward": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int, _vp,
                                              ctypes.c_int, _vp, _vp]),
     "dpf_transient_adjoint": (ctypes.c_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "dpf_batch_autotune": (ctypes.c_int, [ctypes.c_int, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(Options), _vp,
+                                           ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.POINTER(Options),
+                                           ctypes.POINTER(ctypes.c_double)]),
     "dpf_batch_create": (ctypes.c_int, [ctypes.c_int, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(Options),
                                         ctypes.POINTER(_vp)]),
     "dpf_batch_offsets": (ctypes.c_int, [_vp, ctypes.c_int, _i64p, _i64p]),

@@ -195,6 +195,9 @@ dpf_options fill_options(const dpf_options *o) {
     if (r.blocks_per_sm <= 0) r.blocks_per_sm = d.blocks_per_sm;
     if (r.tail_cells == 0) r.tail_cells = d.tail_cells;
     if (r.plane == 0) r.plane = d.plane;
+    if (r.plane_cells <= 0) r.plane_cells = d.plane_cells;
+    r.plane_cells = std::min(4, std::max(1, (r.plane_cells + 255) / 256)) * 256;
+    if (r.plane_blocks_per_sm <= 0) r.plane_blocks_per_sm = d.plane_blocks_per_sm;
     return r;
 }
 
@@ -241,6 +244,8 @@ void dpf_default_options(dpf_options *o) {
     o->blocks_per_sm = 16;
     o->tail_cells = 4096;
     o->plane = 1;
+    o->plane_cells = 1024;
+    o->plane_blocks_per_sm = 2;
 }
 
 int dpf_detect_regular3d(int64_t N, int64_t F, const int64_t *a, const int64_t *b, const double *aol, int *dims,

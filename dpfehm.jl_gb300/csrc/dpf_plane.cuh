@@ -28,11 +28,7 @@ constexpr int kPlaneThreads = DPF_PLANE_THREADS;  // consumer threads per block 
 #define DPF_PLANE_STAGES 4
 #endif
 constexpr int kPlaneStages = DPF_PLANE_STAGES;  // planes x-1, x, x+1 resident, the rest in flight
-#ifndef DPF_PLANE_CPT
-#define DPF_PLANE_CPT 4
-#endif
-constexpr int kPlaneCells = kPlaneThreads * DPF_PLANE_CPT;  // slab capacity (whole rows)
-constexpr int kCellsPerThread = DPF_PLANE_CPT;
+constexpr int kMaxCellsPerThread = 4;  // slab capacity CPT x kPlaneThreads cells, CPT = 1..4 (a template parameter)
 // Rows per slab: as many whole rows as fit `cells`, even (so that slabs align with the
 // 2x2x2 aggregates of the next level) unless one slab holds the whole plane. Host and
 // device both use it, so the work items and the kernels agree.
@@ -179,7 +175,7 @@ __device__ __forceinline__ void pm_produce(int pl_lo, int pl_hi, uint64_t *full,
 // plane after plane as ring slots free up), warps 0..7 consume. Per slot three mbarriers:
 // full (copies landed), empty (all consumer warps are done with the plane), ready (with
 // PM_PROLONG: every consumer thread has applied its share of the correction).
-template <typename T, int MODE>
+template <typename T, int MODE, int CPT>
 __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
     const LevelDesc *__restrict__ desc, const LevelDesc *__restrict__ cdesc, const int4 *__restrict__ items,
     CgState *st, Coeffs<T> C, const T *__restrict__ b, const T *__restrict__ xin, T *__restrict__ xout,
@@ -199,7 +195,7 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
     const LevelDesc L = desc[p];
     const int nz = L.nz, ny = L.ny, nx = L.nx;
     const long long sx = (long long)ny * nz;
-    const int Ty = plane_rows(ny, nz, kPlaneCells);
+    const int Ty = plane_rows(ny, nz, CPT * kPlaneThreads);
     const int rows = min(Ty, ny - y0);
     const int ncell = rows * nz;
     const int t = threadIdx.x;
@@ -260,9 +256,9 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
     } else {
         // ---------------- consumers
         // this thread's cells of the slab (the same in every plane) and their y/z neighbours
-        unsigned cfl[kCellsPerThread];
+        unsigned cfl[CPT];
 #pragma unroll
-        for (int k = 0; k < kCellsPerThread; k++) {
+        for (int k = 0; k < CPT; k++) {
             const int tc = t + k * kPlaneThreads;
             unsigned f = 0;
             if (tc < ncell) {
@@ -333,7 +329,7 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
                 const T *CZ = (const T *)(sc + lay.oCZ) + dp;
                 const T *LK = (const T *)(sc + lay.oLK) + dp;
 #pragma unroll
-                for (int k = 0; k < kCellsPerThread; k++) {
+                for (int k = 0; k < CPT; k++) {
                     const unsigned f = cfl[k];
                     if (!(f & CF_VALID)) continue;
                     const int tc = t + k * kPlaneThreads;
@@ -431,7 +427,7 @@ __device__ __forceinline__ void finish_pq(CgState &s, double pq, int *active_cou
 // cells of the slab sum their children in the order of cell_restrict (x, then y, then z),
 // so the coarse right-hand side is bitwise that of k_restrict. Slabs start on even rows and
 // chunks on even planes. Streams per plane: x with halo rows, b, cx, cy (+ row below), cz, leak.
-template <typename T>
+template <typename T, int CPT>
 __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
     const LevelDesc *__restrict__ desc, const LevelDesc *__restrict__ cdesc, const int4 *__restrict__ items,
     const CgState *st, Coeffs<T> C, const T *__restrict__ b, const T *__restrict__ xin, T *__restrict__ bc,
@@ -441,7 +437,7 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
     constexpr int kConsumerWarps = kPlaneThreads / 32;
     extern __shared__ __align__(128) unsigned char sm[];
     __shared__ uint64_t full[R], empty[R];
-    __shared__ T res[2][kPlaneCells];
+    __shared__ T res[2][CPT * kPlaneThreads];
 
     const int4 it = items[blockIdx.x];
     const int p = it.x, y0 = it.y, xa = it.z, xe = it.w;
@@ -450,7 +446,7 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
     const LevelDesc Lc = cdesc[p];
     const int nz = L.nz, ny = L.ny, nx = L.nx;
     const long long sx = (long long)ny * nz;
-    const int Ty = plane_rows(ny, nz, kPlaneCells);
+    const int Ty = plane_rows(ny, nz, CPT * kPlaneThreads);
     const int rows = min(Ty, ny - y0);
     const int ncell = rows * nz;
     const int t = threadIdx.x;
@@ -494,9 +490,9 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
         return;
     }
     // ---------------- consumers
-    unsigned cfl[kCellsPerThread];
+    unsigned cfl[CPT];
 #pragma unroll
-    for (int k = 0; k < kCellsPerThread; k++) {
+    for (int k = 0; k < CPT; k++) {
         const int tc = t + k * kPlaneThreads;
         unsigned f = 0;
         if (tc < ncell) {
@@ -537,7 +533,7 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
             const T *Xq = (const T *)(sq + lay.oX) + dq;
             T *rs = res[x & 1];
 #pragma unroll
-            for (int k = 0; k < kCellsPerThread; k++) {
+            for (int k = 0; k < CPT; k++) {
                 const unsigned f = cfl[k];
                 if (!(f & CF_VALID)) continue;
                 const int tc = t + k * kPlaneThreads;

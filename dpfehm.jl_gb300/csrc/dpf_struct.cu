@@ -1176,10 +1176,7 @@ void StructBatch::build_plane_items(PlaneItems &P, const Level &L, const std::ve
         total += D.n;
     }
     if (total == 0) return;
-#ifndef DPF_PLANE_BPSM
-#define DPF_PLANE_BPSM 2
-#endif
-    const long long target = (long long)sms * DPF_PLANE_BPSM;
+    const long long target = (long long)sms * std::max(1, opt.plane_blocks_per_sm);
     std::vector<int4> items;
     std::vector<int2> pinfo(nprob, make_int2(0, 0));
     for (int p = 0; p < nprob; p++) {
@@ -1296,7 +1293,7 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         L.all = build_map(L.h_desc, has, owned, nprob, target_blocks);
         L.smooth = build_map(L.h_desc, smooth, owned, nprob, target_blocks);
         L.restr = build_map(L.h_desc, restr, owned, nprob, target_blocks);
-        build_plane_items(L.pm, L, smooth, sms, kPlaneCells, &shapes, l);
+        build_plane_items(L.pm, L, smooth, sms, opt.plane_cells, &shapes, l);
         for (int p = 0; p < nprob; p++) {
             if (has[p]) L.all_cells += L.h_desc[p].n;
             if (smooth[p]) L.smooth_cells += L.h_desc[p].n;
@@ -1555,25 +1552,50 @@ void StructBatch::assemble(const double *Ks, const double *kc, int kind, const d
 // ---- plane-marching launches
 static int pm_region(int count, int es) { return ((count * es + 32) + 15) & ~15; }
 
-template <typename T, int MODE>
+template <typename T, int MODE, int CPT>
 static void pm_kernel(unsigned nblocks, size_t smem, cudaStream_t stream, const LevelDesc *desc,
                       const LevelDesc *cdesc, const int4 *items, CgState *st, Coeffs<T> C, const T *b,
                       const T *xin, T *xout, T *d, const uint8_t *dir, const T *e, T c1, T c2, T invth, T sc,
                       PlaneLayout lay, ReduceScratch rs, const int2 *pinfo, int *err) {
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
-        CK(cudaFuncSetAttribute(k_pm_cheb<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CK(cudaFuncSetAttribute(k_pm_cheb<T, MODE, CPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = smem;
     }
-    k_pm_cheb<T, MODE><<<nblocks, kPlaneThreads + 32, smem, stream>>>(desc, cdesc, items, st, C, b, xin, xout, d, dir, e,
-                                                                  c1, c2, invth, sc, lay, rs, pinfo, err);
+    k_pm_cheb<T, MODE, CPT><<<nblocks, kPlaneThreads + 32, smem, stream>>>(desc, cdesc, items, st, C, b, xin, xout, d,
+                                                                       dir, e, c1, c2, invth, sc, lay, rs, pinfo, err);
+}
+
+template <typename T, int MODE>
+static void pm_kernel_cpt(int cpt, unsigned nblocks, size_t smem, cudaStream_t stream, const LevelDesc *desc,
+                          const LevelDesc *cdesc, const int4 *items, CgState *st, Coeffs<T> C, const T *b,
+                          const T *xin, T *xout, T *d, const uint8_t *dir, const T *e, T c1, T c2, T invth, T sc,
+                          PlaneLayout lay, ReduceScratch rs, const int2 *pinfo, int *err) {
+#define DPF_PM_CPT(N)                                                                                              \
+    case N:                                                                                                        \
+        pm_kernel<T, MODE, N>(nblocks, smem, stream, desc, cdesc, items, st, C, b, xin, xout, d, dir, e, c1, c2, invth, \
+                              sc, lay, rs, pinfo, err);                                                            \
+        break;
+    switch (cpt) {
+        DPF_PM_CPT(1)
+        DPF_PM_CPT(2)
+        DPF_PM_CPT(3)
+        DPF_PM_CPT(4)
+        default:
+            throw std::logic_error("plane slab must hold 1..4 cells per thread");
+    }
+#undef DPF_PM_CPT
 }
 
 // One plane-marching Chebyshev launch over the smoothed problems of level l (mode: PM_* bits).
 template <typename T>
 void StructBatch::pm_launch(int mode, int l, const T *b, const T *xin, T *xout, T *d, const T *e, T c1, T c2,
                             T invth, T sc) {
+    if constexpr (sizeof(T) != 4) {
+        throw std::logic_error("plane-marching kernels run FP32 V-cycles only");
+    } else {
     Level &L = lv[l];
+    const int cpt = L.pm.cells / kPlaneThreads;
     const int es = (int)sizeof(T);
     PlaneLayout lay{};
     int off = 0;
@@ -1597,8 +1619,8 @@ void StructBatch::pm_launch(int mode, int l, const T *b, const T *xin, T *xout, 
     int *err = d_factor_status + 1;
 #define DPF_PM_CASE(M)                                                                                           \
     case M:                                                                                                      \
-        pm_kernel<T, M>(nb, smem, stream, L.d_desc, cd, L.pm.items, d_state, C, b, xin, xout, d, L.dir, e, c1, c2, \
-                        invth, sc, lay, rs, L.pm.pinfo, err);                                                     \
+        pm_kernel_cpt<T, M>(cpt, nb, smem, stream, L.d_desc, cd, L.pm.items, d_state, C, b, xin, xout, d, L.dir, e, \
+                            c1, c2, invth, sc, lay, rs, L.pm.pinfo, err);                                         \
         break;
     switch (mode) {
         DPF_PM_CASE(PM_FIRST2)
@@ -1613,11 +1635,27 @@ void StructBatch::pm_launch(int mode, int l, const T *b, const T *xin, T *xout, 
             throw std::logic_error("unsupported plane kernel mode");
     }
 #undef DPF_PM_CASE
+    }
 }
 
 // Plane-marching restriction of level l's residual into level l+1 (the smoothed problems).
+template <typename T, int CPT>
+static void pm_restrict_kernel(unsigned nblocks, size_t smem, cudaStream_t stream, const LevelDesc *desc,
+                               const LevelDesc *cdesc, const int4 *items, const CgState *st, Coeffs<T> C, const T *b,
+                               const T *x, T *bc, PlaneLayout lay, int *err) {
+    static size_t configured = 0;
+    if (smem > 48 * 1024 - 2 * CPT * kPlaneThreads * sizeof(T) && smem > configured) {
+        CK(cudaFuncSetAttribute(k_pm_restrict<T, CPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = smem;
+    }
+    k_pm_restrict<T, CPT><<<nblocks, kPlaneThreads + 32, smem, stream>>>(desc, cdesc, items, st, C, b, x, bc, lay, err);
+}
+
 template <typename T>
 void StructBatch::pm_restrict(int l, const T *b, const T *x, T *bc) {
+    if constexpr (sizeof(T) != 4) {
+        throw std::logic_error("plane-marching kernels run FP32 V-cycles only");
+    } else {
     Level &L = lv[l];
     const int es = (int)sizeof(T);
     PlaneLayout lay{};
@@ -1632,13 +1670,16 @@ void StructBatch::pm_restrict(int l, const T *b, const T *x, T *bc) {
     lay.oD = lay.oG = lay.oDIR = lay.oE = -1;
     lay.slot_bytes = (off + 127) & ~127;
     const size_t smem = (size_t)kPlaneStages * lay.slot_bytes;
-    static size_t configured = 0;
-    if (smem > 48 * 1024 - 2 * kPlaneCells * sizeof(T) && smem > configured) {
-        CK(cudaFuncSetAttribute(k_pm_restrict<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = smem;
+    const unsigned nb = (unsigned)L.pm.n;
+    const Coeffs<T> C = coeffs_of<T>(L, mixed);
+    switch (L.pm.cells / kPlaneThreads) {
+        case 1: pm_restrict_kernel<T, 1>(nb, smem, stream, L.d_desc, lv[l + 1].d_desc, L.pm.items, d_state, C, b, x, bc, lay, d_factor_status + 1); break;
+        case 2: pm_restrict_kernel<T, 2>(nb, smem, stream, L.d_desc, lv[l + 1].d_desc, L.pm.items, d_state, C, b, x, bc, lay, d_factor_status + 1); break;
+        case 3: pm_restrict_kernel<T, 3>(nb, smem, stream, L.d_desc, lv[l + 1].d_desc, L.pm.items, d_state, C, b, x, bc, lay, d_factor_status + 1); break;
+        case 4: pm_restrict_kernel<T, 4>(nb, smem, stream, L.d_desc, lv[l + 1].d_desc, L.pm.items, d_state, C, b, x, bc, lay, d_factor_status + 1); break;
+        default: throw std::logic_error("plane slab must hold 1..4 cells per thread");
     }
-    k_pm_restrict<T><<<(unsigned)L.pm.n, kPlaneThreads + 32, smem, stream>>>(
-        L.d_desc, lv[l + 1].d_desc, L.pm.items, d_state, coeffs_of<T>(L, mixed), b, x, bc, lay, d_factor_status + 1);
+    }
 }
 
 template <typename T>

@@ -1,0 +1,134 @@
+// dpf_tune.cu -- autotuner for the batched steady solve: chooses the Chebyshev degree, the
+// plane-marching slab size and blocks per SM, the fused-tail threshold and the grid-stride
+// blocks per SM for a given batch by timing real forward + adjoint solves.
+//
+// Coordinate descent from the caller's options: each parameter in turn is set to each of
+// its candidate values with the others held at the best so far; a candidate is adopted
+// when its solve converges and is at least 2 % faster. Every evaluation creates the batch
+// through the public API, runs one untimed solve (graph capture, warm caches) and then
+// `repeats` timed solves with CUDA events on the library's stream (the legacy default
+// stream). Only the public C ABI is used, so what is timed is what a caller runs.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "dpfehm_gpu.h"
+
+namespace {
+
+struct DevCopy {
+    const double *ptr = nullptr;
+    double *owned = nullptr;
+    ~DevCopy() {
+        if (owned) cudaFree(owned);
+    }
+};
+
+bool on_device(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int to_device(const double *src, size_t n, DevCopy &out) {
+    if (on_device(src)) {
+        out.ptr = src;
+        return DPF_OK;
+    }
+    if (cudaMalloc(&out.owned, n * sizeof(double)) != cudaSuccess) return DPF_OOM;
+    if (cudaMemcpy(out.owned, src, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) return DPF_CUDA;
+    out.ptr = out.owned;
+    return DPF_OK;
+}
+
+}  // namespace
+
+extern "C" int dpf_batch_autotune(int nprob, const int *dims, const double *mins, const double *maxs, const int64_t *nd,
+                                  const int64_t *dn, const dpf_options *base, const double *logK, int kind,
+                                  const double *dh, const double *Qs, const int64_t *obs_offsets, const int64_t *obs,
+                                  int repeats, dpf_options *best, double *best_ms) {
+    if (nprob <= 0 || !dims || !mins || !maxs || !nd || !logK || !dh || !Qs || !obs_offsets || !best)
+        return DPF_BAD_INPUT;
+    if (repeats < 1) repeats = 1;
+    size_t N = 0;
+    for (int p = 0; p < nprob; p++) N += (size_t)dims[3 * p] * dims[3 * p + 1] * dims[3 * p + 2];
+    dpf_options cur;
+    dpf_default_options(&cur);
+    if (base) cur = *base;
+    DevCopy dlk, ddh, dq;
+    int rc;
+    if ((rc = to_device(logK, N, dlk)) || (rc = to_device(dh, N, ddh)) || (rc = to_device(Qs, N, dq))) return rc;
+    double *hout = nullptr, *gout = nullptr;
+    if (cudaMalloc(&hout, N * sizeof(double)) != cudaSuccess || cudaMalloc(&gout, N * sizeof(double)) != cudaSuccess) {
+        cudaFree(hout);
+        return DPF_OOM;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+
+    // one evaluation: create, warm up, time `repeats` solves; DPF_OK and the mean ms per solve
+    auto evaluate = [&](const dpf_options &o, double &ms) -> int {
+        dpf_problem *h = nullptr;
+        int r = dpf_batch_create(nprob, dims, mins, maxs, nd, dn, &o, &h);
+        if (r != DPF_OK) return r;
+        r = dpf_batch_solve_grad_logk(h, dlk.ptr, kind, ddh.ptr, dq.ptr, obs_offsets, obs, hout, gout);
+        if (r == DPF_OK) {
+            cudaEventRecord(e0, 0);
+            for (int k = 0; k < repeats && r == DPF_OK; k++)
+                r = dpf_batch_solve_grad_logk(h, dlk.ptr, kind, ddh.ptr, dq.ptr, obs_offsets, obs, hout, gout);
+            cudaEventRecord(e1, 0);
+            cudaEventSynchronize(e1);
+            float t = 0.f;
+            cudaEventElapsedTime(&t, e0, e1);
+            ms = (double)t / repeats;
+        }
+        dpf_destroy(h);
+        return r;
+    };
+
+    double cur_ms = 0.0;
+    rc = evaluate(cur, cur_ms);
+    if (rc == DPF_OK) {
+        const bool mixed = cur.precision == DPF_PREC_MIXED && cur.plane > 0;
+        struct Knob {
+            int *field;
+            std::vector<int> values;
+            bool active;
+        };
+        const Knob knobs[] = {
+            {&cur.cheb_degree, {1, 2, 3}, true},
+            {&cur.plane_cells, {512, 768, 1024}, mixed},
+            {&cur.plane_blocks_per_sm, {1, 2, 3}, mixed},
+            {&cur.tail_cells, {-1, 1024, 4096, 16384}, true},
+            {&cur.blocks_per_sm, {8, 16, 24}, true},
+        };
+        for (const Knob &k : knobs) {
+            if (!k.active) continue;
+            const int keep = *k.field;
+            int pick = keep;
+            for (int v : k.values) {
+                if (v == keep) continue;
+                *k.field = v;
+                double ms = 0.0;
+                if (evaluate(cur, ms) == DPF_OK && ms < 0.98 * cur_ms) {
+                    cur_ms = ms;
+                    pick = v;
+                }
+            }
+            *k.field = pick;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(hout);
+    cudaFree(gout);
+    *best = cur;
+    if (best_ms) *best_ms = cur_ms;
+    return rc;
+}

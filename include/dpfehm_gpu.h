@@ -81,6 +81,8 @@ typedef struct dpf_options {
                             run as one fused kernel per problem (default 4096; negative: off) */
     int plane;           /* regular grids, MIXED: plane-marching smoother kernels with shared-memory
                             staging (default 1; negative: grid-stride kernels) */
+    int plane_cells;     /* plane-marching slab capacity in cells: 256, 512, 768 or 1024 (default 1024) */
+    int plane_blocks_per_sm; /* plane-marching work items per SM (default 2) */
 } dpf_options;
 
 typedef struct dpf_problem dpf_problem;
@@ -180,6 +182,18 @@ int dpf_batch_offsets(const dpf_problem *h, int p, int64_t *cell_offset, int64_t
 int dpf_batch_solve_grad_logk(dpf_problem *h, const double *logK, int mean_kind, const double *dirichleths,
                               const double *Qs, const int64_t *obs_offsets, const int64_t *obs, double *h_out,
                               double *dlogK);
+
+/* Autotuner for a batch (same arguments as dpf_batch_create and dpf_batch_solve_grad_logk):
+ * coordinate descent over the Chebyshev degree, plane_cells, plane_blocks_per_sm,
+ * tail_cells and blocks_per_sm, starting from *base (NULL: defaults), each candidate timed
+ * over `repeats` forward + adjoint solves of the given inputs (host or device buffers)
+ * after one untimed solve; a candidate is kept if it converges and is >= 2 % faster.
+ * Writes the chosen options to *best and their time per solve call to *best_ms.
+ * Launch shapes and smoother degree are this library's own; no reference counterpart. */
+int dpf_batch_autotune(int nprob, const int *dims, const double *mins, const double *maxs, const int64_t *nd,
+                       const int64_t *dn, const dpf_options *base, const double *logK, int kind, const double *dh,
+                       const double *Qs, const int64_t *obs_offsets, const int64_t *obs, int repeats,
+                       dpf_options *best, double *best_ms);
 
 /* Same as dpf_batch_solve_grad_logk for a single problem (nprob = 1 handles of
  * any kind): forward, objective sum_k h[obs_k]^2, adjoint to dlogK. */

@@ -126,3 +126,24 @@ def test_caller_output_buffers(gpu_lib):
     assert np.array_equal(hb, h0) and np.array_equal(gb, g0)
     with pytest.raises(ValueError):
         B.solve_grad_logk(c["logK"], c["dh"], c["Qs"], [c["obs"]], out=(np.zeros(c["N"], np.float32), gb))
+
+
+def test_autotune_batch(gpu_lib):
+    """The autotuner returns options from its candidate sets that give the same solution."""
+    pkg = gpu_lib
+    shapes = [(20, 16, 5), (9, 9, 9), (40, 30, 6)]
+    probs = [_problem(pkg, ns, 41 + k) for k, ns in enumerate(shapes)]
+    cat = lambda k: np.concatenate([p[k] for p in probs])
+    args = ([p["ns"] for p in probs], [p["mins"] for p in probs], [p["maxs"] for p in probs],
+            [p["dn"] for p in probs])
+    tuned, ms = pkg.autotune_batch(*args, cat("logK"), cat("dh"), cat("Qs"), [p["obs"] for p in probs],
+                                   repeats=1, reltol=1e-11, precision="mixed")
+    assert ms > 0
+    assert tuned["cheb_degree"] in (1, 2, 3) and tuned["plane_cells"] in (512, 768, 1024)
+    assert tuned["plane_blocks_per_sm"] in (1, 2, 3) and tuned["tail_cells"] in (-1, 1024, 4096, 16384)
+    assert tuned["blocks_per_sm"] in (8, 16, 24)
+    B0 = pkg.GroundwaterBatch(*args, reltol=1e-11, precision="mixed")
+    B1 = pkg.GroundwaterBatch(*args, reltol=1e-11, precision="mixed", **tuned)
+    h0, g0 = B0.solve_grad_logk(cat("logK"), cat("dh"), cat("Qs"), [p["obs"] for p in probs])
+    h1, g1 = B1.solve_grad_logk(cat("logK"), cat("dh"), cat("Qs"), [p["obs"] for p in probs])
+    assert rel(h1, h0) < 1e-9 and rel(g1, g0) < 1e-7
