@@ -361,7 +361,7 @@ class GroundwaterBatch(GroundwaterProblem):
         return h, g
 
 
-_TUNED = ("cheb_degree", "plane_cells", "plane_blocks_per_sm", "tail_cells", "blocks_per_sm")
+_TUNED = ("cheb_degree", "plane_cells", "plane_blocks_per_sm", "tail_cells", "blocks_per_sm", "df_plane_cells")
 
 
 def autotune_batch(dims, mins, maxs, dirichletnodes, logK, dirichleths, Qs, obs_per_problem, mean="geometric",

@@ -35,6 +35,8 @@ class Options(ctypes.Structure):
         ("plane", ctypes.c_int),
         ("plane_cells", ctypes.c_int),
         ("plane_blocks_per_sm", ctypes.c_int),
+        ("df_plane_cells", ctypes.c_int),
+        ("df_plane_blocks_per_sm", ctypes.c_int),
     ]
 
 

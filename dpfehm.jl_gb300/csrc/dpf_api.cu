@@ -198,6 +198,9 @@ dpf_options fill_options(const dpf_options *o) {
     if (r.plane_cells <= 0) r.plane_cells = d.plane_cells;
     r.plane_cells = std::min(4, std::max(1, (r.plane_cells + 255) / 256)) * 256;
     if (r.plane_blocks_per_sm <= 0) r.plane_blocks_per_sm = d.plane_blocks_per_sm;
+    if (r.df_plane_cells == 0) r.df_plane_cells = d.df_plane_cells;
+    if (r.df_plane_cells > 0) r.df_plane_cells = std::min(4, std::max(1, (r.df_plane_cells + 255) / 256)) * 256;
+    if (r.df_plane_blocks_per_sm <= 0) r.df_plane_blocks_per_sm = d.df_plane_blocks_per_sm;
     return r;
 }
 
@@ -246,6 +249,8 @@ void dpf_default_options(dpf_options *o) {
     o->plane = 1;
     o->plane_cells = 1024;
     o->plane_blocks_per_sm = 2;
+    o->df_plane_cells = -1;
+    o->df_plane_blocks_per_sm = 4;
 }
 
 int dpf_detect_regular3d(int64_t N, int64_t F, const int64_t *a, const int64_t *b, const double *aol, int *dims,

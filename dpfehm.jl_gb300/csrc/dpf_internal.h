@@ -62,6 +62,11 @@ struct CgState {
     int ru_flag, total_iters, stall, pad2;  // ru_flag: problem takes part in the current round
 };
 
+// Double-float copies of the finest operator's coefficients (hi, lo per entry).
+struct CoeffsDF {
+    const float2 *cx, *cy, *cz, *leak;
+};
+
 // Reduction scratch: one double2 partial per block of the widest launch, one
 // ticket counter per problem; the last block of each problem sums the partials
 // in a fixed order (deterministic) and finalises that problem's scalars.

@@ -411,10 +411,6 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
     }
 }
 
-struct CoeffsDF {
-    const float2 *cx, *cy, *cz, *leak;
-};
-
 __device__ __forceinline__ void finish_pq(CgState &s, double pq, int *active_count) {
     s.pq = pq;
     if (!isfinite(s.pq)) { s.alpha = 0.0; s.status = DPF_NAN; deactivate(s, active_count); }
@@ -577,6 +573,132 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
         }
         if (consumer_sync_or(bad, kPlaneThreads)) break;  // res[] may be overwritten
     }
+}
+
+// Double-float CG product q = A p (flux form, double-float coefficients) and the problem's
+// p . q (leading floats) on the plane ring; the arithmetic and its order are those of the
+// grid-stride k_df_spmv_pq. Streams per plane: p with halo rows, cx, cy (+ the row
+// below), cz, leak, all 8-byte double-float values.
+template <int CPT>
+__global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_df_spmv(
+    const LevelDesc *__restrict__ desc, const int4 *__restrict__ items, CgState *st, int *active_count,
+    ReduceScratch rs, const int2 *__restrict__ pinfo, CoeffsDF C, const float2 *__restrict__ pv,
+    float2 *__restrict__ qv, PlaneLayout lay, int *err) {
+    constexpr int R = kPlaneStages;
+    constexpr int es = 8;
+    constexpr int kConsumerWarps = kPlaneThreads / 32;
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ uint64_t full[R], empty[R];
+
+    const int4 it = items[blockIdx.x];
+    const int p = it.x, y0 = it.y, xa = it.z, xe = it.w;
+    if (!st[p].active) return;
+    const LevelDesc L = desc[p];
+    const int nz = L.nz, ny = L.ny, nx = L.nx;
+    const long long sx = (long long)ny * nz;
+    const int Ty = plane_rows(ny, nz, CPT * kPlaneThreads);
+    const int rows = min(Ty, ny - y0);
+    const int ncell = rows * nz;
+    const int t = threadIdx.x;
+    const int warp = t >> 5, lane = t & 31;
+    const int pl_lo = max(xa - 1, 0), pl_hi = min(xe, nx - 1);
+    const int h0 = max(y0 - 1, 0), h1 = min(y0 + rows + 1, ny);
+    auto slot_of = [&](int q) { return (char *)sm + ((unsigned)(q - pl_lo) % (unsigned)R) * lay.slot_bytes; };
+
+    if (t == 0) {
+        for (int s = 0; s < R; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kConsumerWarps);
+        }
+        fence_mbarrier_init();
+    }
+    __syncthreads();
+    Acc<float> part;
+
+    if (warp == kConsumerWarps) {
+        if (lane == 0) {
+            pm_produce<R>(pl_lo, pl_hi, full, empty, sm, lay.slot_bytes, err, [&](int q, char *slot, uint64_t *bar) {
+                const long long pb = L.off + (long long)q * sx;
+                const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
+                const long long hA = pb + (long long)h0 * nz, hB = pb + (long long)h1 * nz, pE = lp + ncell;
+                auto stage = [&](const void *base, long long l0, long long a0, long long a1, int off) {
+                    const BulkRange r = make_range(base, es, l0, a0, a1, slot + off);
+                    mbar_expect_tx(bar, r.bytes);
+                    bulk_copy_g2s(r.dst, r.src, r.bytes, bar);
+                };
+                stage(pv, lh, hA, hB, lay.oX);
+                stage(C.cx, lp, lp, pE, lay.oCX);
+                stage(C.cy, lh, hA, pE, lay.oCY);
+                stage(C.cz, lp, lp, pE, lay.oCZ);
+                stage(C.leak, lp, lp, pE, lay.oLK);
+            });
+        }
+        __syncwarp();
+    } else {
+        unsigned cfl[CPT];
+#pragma unroll
+        for (int k = 0; k < CPT; k++) {
+            const int tc = t + k * kPlaneThreads;
+            unsigned f = 0;
+            if (tc < ncell) {
+                const int ty = div_nz(L, tc), z = tc - ty * nz, y = y0 + ty;
+                f = CF_VALID | (z + 1 < nz ? CF_ZP : 0u) | (z > 0 ? CF_ZM : 0u) | (y + 1 < ny ? CF_YP : 0u) |
+                    (y > 0 ? CF_YM : 0u);
+            }
+            cfl[k] = f;
+        }
+        int waited = pl_lo - 1;
+        bool ok = true;
+        for (int x = xa; x < xe && ok; x++) {
+            const int need = min(x + 1, pl_hi);
+            while (waited < need) {
+                const int u = waited + 1 - pl_lo;
+                if (!mbar_wait(&full[u % R], (uint32_t)((u / R) & 1), err)) {
+                    ok = false;
+                    break;
+                }
+                waited++;
+            }
+            if (!ok) break;
+            const long long pb = L.off + (long long)x * sx;
+            const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
+            const int dh = stage_delta(lh, es), dp = stage_delta(lp, es);
+            char *sc = slot_of(x);
+            const bool xp = x + 1 < nx, xm = x > 0;
+            char *sn = xp ? slot_of(x + 1) : sc;
+            char *sq = xm ? slot_of(x - 1) : sc;
+            const float2 *P = (const float2 *)(sc + lay.oX) + dh;
+            const float2 *CX = (const float2 *)(sc + lay.oCX) + dp;
+            const float2 *CY = (const float2 *)(sc + lay.oCY) + dh;
+            const float2 *CZ = (const float2 *)(sc + lay.oCZ) + dp;
+            const float2 *LK = (const float2 *)(sc + lay.oLK) + dp;
+            const float2 *Pn = (const float2 *)(sn + lay.oX) + (xp ? stage_delta(lh + sx, es) : dh);
+            const float2 *Pq = (const float2 *)(sq + lay.oX) + (xm ? stage_delta(lh - sx, es) : dh);
+            const float2 *CXq = (const float2 *)(sq + lay.oCX) + (xm ? stage_delta(lp - sx, es) : dp);
+#pragma unroll
+            for (int k = 0; k < CPT; k++) {
+                const unsigned f = cfl[k];
+                if (!(f & CF_VALID)) continue;
+                const int tc = t + k * kPlaneThreads;
+                const int c = nz + tc;
+                const float2 pi = P[c];
+                float2 a = df_mul(LK[tc], pi);
+                if (f & CF_ZP) a = df_add(a, df_mul(CZ[tc], df_sub(pi, P[c + 1])));
+                if (f & CF_ZM) a = df_add(a, df_mul(CZ[tc - 1], df_sub(pi, P[c - 1])));
+                if (f & CF_YP) a = df_add(a, df_mul(CY[c], df_sub(pi, P[c + nz])));
+                if (f & CF_YM) a = df_add(a, df_mul(CY[tc], df_sub(pi, P[c - nz])));
+                if (xp) a = df_add(a, df_mul(CX[tc], df_sub(pi, Pn[c])));
+                if (xm) a = df_add(a, df_mul(CXq[tc], df_sub(pi, Pq[c])));
+                qv[lp + tc] = a;
+                part = part + Acc<float>::prod(pi.x, a.x);
+            }
+            __syncwarp();
+            if (lane == 0 && x - 1 >= pl_lo) mbar_arrive(&empty[(x - 1 - pl_lo) % R]);
+        }
+    }
+    double2 tot;
+    if (reduce_last<float>(part, Acc<float>(), rs, pinfo[p], p, tot) && threadIdx.x == 0)
+        finish_pq(st[p], tot.x, active_count);
 }
 
 }  // namespace dpf

@@ -684,9 +684,7 @@ __global__ void k_df_update_xr(const LevelDesc *__restrict__ desc, const int4 *_
     const double as = st[p].alpha * st[p].scale;
     Acc<float> part;
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
-        Cell c;
-        cell_at(L, li_, c);
-        const long long i = c.i;
+        const long long i = L.off + li_;  // pointwise: no cell decode
         const float2 pi = pv[i];
         x64[i] = fma(as, (double)pi.x + (double)pi.y, x64[i]);
         const float2 ri = df_sub(r[i], df_mul(a, q[i]));
@@ -713,9 +711,7 @@ __global__ void k_df_update_p(const LevelDesc *__restrict__ desc, const int4 *__
     const double beta = st[p].beta;
     const float2 b = df_from_double(beta);
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
-        Cell c;
-        cell_at(L, li_, c);
-        const long long i = c.i;
+        const long long i = L.off + li_;  // pointwise: no cell decode
         const float2 zi = make_float2(z[i], 0.0f);
         pv[i] = beta == 0.0 ? zi : df_add(zi, df_mul(b, pv[i]));
     }
@@ -1162,12 +1158,13 @@ static BlockMap build_map(const std::vector<LevelDesc> &desc, const std::vector<
 // (whole rows, so a slab is contiguous in every array) times chunks of x-planes, with the
 // chunk length chosen so that all items fill the device about once.
 void StructBatch::build_plane_items(PlaneItems &P, const Level &L, const std::vector<int> &take, int sms,
-                                    int cells, const std::vector<std::vector<std::array<int, 3>>> *shapes, int l) {
+                                    int cells, int blocks_per_sm,
+                                    const std::vector<std::vector<std::array<int, 3>>> *shapes, int l) {
     P.ok = false;
     P.cells = cells;
     // FP32 V-cycles only: with 8-byte values the stages of a 768-cell slab allow one block
     // per SM, and the FP64 smoothers are faster as grid-stride kernels
-    if (opt.plane <= 0 || !mixed) return;
+    if (cells <= 0 || !mixed) return;
     long long total = 0;
     for (int p = 0; p < nprob; p++) {
         if (!take[p]) continue;
@@ -1176,7 +1173,7 @@ void StructBatch::build_plane_items(PlaneItems &P, const Level &L, const std::ve
         total += D.n;
     }
     if (total == 0) return;
-    const long long target = (long long)sms * std::max(1, opt.plane_blocks_per_sm);
+    const long long target = (long long)sms * std::max(1, blocks_per_sm);
     std::vector<int4> items;
     std::vector<int2> pinfo(nprob, make_int2(0, 0));
     for (int p = 0; p < nprob; p++) {
@@ -1293,14 +1290,16 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         L.all = build_map(L.h_desc, has, owned, nprob, target_blocks);
         L.smooth = build_map(L.h_desc, smooth, owned, nprob, target_blocks);
         L.restr = build_map(L.h_desc, restr, owned, nprob, target_blocks);
-        build_plane_items(L.pm, L, smooth, sms, opt.plane_cells, &shapes, l);
+        build_plane_items(L.pm, L, smooth, sms, opt.plane > 0 ? opt.plane_cells : 0, opt.plane_blocks_per_sm, &shapes,
+                          l);
+        if (l == 0) build_plane_items(L.pa, L, has, sms, opt.df_plane_cells, opt.df_plane_blocks_per_sm, nullptr, l);
         for (int p = 0; p < nprob; p++) {
             if (has[p]) L.all_cells += L.h_desc[p].n;
             if (smooth[p]) L.smooth_cells += L.h_desc[p].n;
             if (restr[p]) L.restr_cells += L.h_desc[p].n;
             if (has[p] && l == nlev[p] - 1) L.coarse_cells += L.h_desc[p].n;
         }
-        maxblocks = std::max(maxblocks, std::max(L.all.nblocks, L.pm.n));
+        maxblocks = std::max(maxblocks, std::max(L.all.nblocks, std::max(L.pm.n, L.pa.n)));
         L.d_coarse = dalloc<int>(L.coarse_list.size(), owned);
         if (!L.coarse_list.empty())
             CK(cudaMemcpy(L.d_coarse, L.coarse_list.data(), L.coarse_list.size() * sizeof(int),
@@ -1908,12 +1907,52 @@ void StructBatch::pcg_iteration(T *x) {
 
 // One iteration of the mixed-precision CG: double-float q = A p, alpha, x/r update,
 // FP32 V-cycle on the rounded residual, double-float p update.
+// Plane-marching double-float CG product over all problems of the finest level.
+template <int CPT>
+static void pm_df_kernel(unsigned nblocks, size_t smem, cudaStream_t stream, const LevelDesc *desc, const int4 *items,
+                         CgState *st, int *count, ReduceScratch rs, const int2 *pinfo, CoeffsDF C, const float2 *pv,
+                         float2 *q, PlaneLayout lay, int *err) {
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        CK(cudaFuncSetAttribute(k_pm_df_spmv<CPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = smem;
+    }
+    k_pm_df_spmv<CPT><<<nblocks, kPlaneThreads + 32, smem, stream>>>(desc, items, st, count, rs, pinfo, C, pv, q, lay,
+                                                                     err);
+}
+
+void StructBatch::pm_df_spmv(const CoeffsDF &C) {
+    Level &L0 = lv[0];
+    PlaneLayout lay{};
+    int off = 0;
+    auto take = [&](int bytes) { int o = off; off += bytes; return o; };
+    lay.oX = take(pm_region(L0.pa.halo, 8));
+    lay.oCX = take(pm_region(L0.pa.slab, 8));
+    lay.oCY = take(pm_region(L0.pa.cy, 8));
+    lay.oCZ = take(pm_region(L0.pa.slab, 8));
+    lay.oLK = take(pm_region(L0.pa.slab, 8));
+    lay.oB = lay.oD = lay.oG = lay.oDIR = lay.oE = -1;
+    lay.slot_bytes = (off + 127) & ~127;
+    const size_t smem = (size_t)kPlaneStages * lay.slot_bytes;
+    const unsigned nb = (unsigned)L0.pa.n;
+    switch (L0.pa.cells / kPlaneThreads) {
+        case 1: pm_df_kernel<1>(nb, smem, stream, L0.d_desc, L0.pa.items, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2], dfv[3], lay, d_factor_status + 1); break;
+        case 2: pm_df_kernel<2>(nb, smem, stream, L0.d_desc, L0.pa.items, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2], dfv[3], lay, d_factor_status + 1); break;
+        case 3: pm_df_kernel<3>(nb, smem, stream, L0.d_desc, L0.pa.items, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2], dfv[3], lay, d_factor_status + 1); break;
+        case 4: pm_df_kernel<4>(nb, smem, stream, L0.d_desc, L0.pa.items, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2], dfv[3], lay, d_factor_status + 1); break;
+        default: throw std::logic_error("plane slab must hold 1..4 cells per thread");
+    }
+}
+
 void StructBatch::df_iteration(double *x64) {
     Level &L0 = lv[0];
     const unsigned nb = nb_of(L0.all);
     float *r32 = (float *)cgv[0], *z32 = (float *)cgv[1];
     CoeffsDF C{cdf[0], cdf[1], cdf[2], cdf[3]};
-    {
+    if (L0.pa.ok) {
+        KTimer _kt(this, kname("k_pm_df_spmv", 0, true), L0.all_cells);
+        pm_df_spmv(C);
+    } else {
         KTimer _kt(this, kname("k_df_spmv_pq", 0, true), L0.all_cells);
         k_df_spmv_pq<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C,
                                                 dfv[2], dfv[3]);

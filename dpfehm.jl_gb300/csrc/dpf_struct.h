@@ -75,6 +75,7 @@ public:
         std::vector<int> coarse_list;  // problems whose coarsest level this is
         int *d_coarse = nullptr;
         PlaneItems pm;  // plane-marching launches over the smoothed problems
+        PlaneItems pa;  // finest level: plane-marching CG product over all problems
         std::vector<int> csolve_list;  // ... of those, the ones solved by a per-level launch (no fused tail)
         int *d_csolve = nullptr;
         long long csolve_cells = 0;
@@ -111,9 +112,10 @@ public:
     template <typename T>
     void vcycle(const T *r, T *z);
     void build_plane_items(PlaneItems &P, const Level &L, const std::vector<int> &take, int sms, int cells,
-                           const std::vector<std::vector<std::array<int, 3>>> *shapes, int l);
+                           int blocks_per_sm, const std::vector<std::vector<std::array<int, 3>>> *shapes, int l);
     template <typename T>
     void pm_restrict(int l, const T *b, const T *x, T *bc);
+    void pm_df_spmv(const CoeffsDF &C);
     template <typename T>
     void pm_launch(int mode, int l, const T *b, const T *xin, T *xout, T *d, const T *e, T c1, T c2, T invth, T sc);
     template <typename T>

@@ -1,6 +1,7 @@
 // dpf_tune.cu -- autotuner for the batched steady solve: chooses the Chebyshev degree, the
-// plane-marching slab size and blocks per SM, the fused-tail threshold and the grid-stride
-// blocks per SM for a given batch by timing real forward + adjoint solves.
+// plane-marching slab size and blocks per SM, the fused-tail threshold, the grid-stride
+// blocks per SM and the form of the double-float CG product for a given batch by timing
+// real forward + adjoint solves.
 //
 // Coordinate descent from the caller's options: each parameter in turn is set to each of
 // its candidate values with the others held at the best so far; a candidate is adopted
@@ -107,6 +108,7 @@ extern "C" int dpf_batch_autotune(int nprob, const int *dims, const double *mins
             {&cur.plane_blocks_per_sm, {1, 2, 3}, mixed},
             {&cur.tail_cells, {-1, 1024, 4096, 16384}, true},
             {&cur.blocks_per_sm, {8, 16, 24}, true},
+            {&cur.df_plane_cells, {-1, 512}, mixed},
         };
         for (const Knob &k : knobs) {
             if (!k.active) continue;
