@@ -361,7 +361,8 @@ class GroundwaterBatch(GroundwaterProblem):
         return h, g
 
 
-_TUNED = ("cheb_degree", "plane_cells", "plane_blocks_per_sm", "tail_cells", "blocks_per_sm", "df_plane_cells")
+_TUNED = ("cheb_degree", "plane_cells", "plane_blocks_per_sm", "tail_cells", "blocks_per_sm", "df_plane_cells",
+          "tail_cluster")
 
 
 def autotune_batch(dims, mins, maxs, dirichletnodes, logK, dirichleths, Qs, obs_per_problem, mean="geometric",

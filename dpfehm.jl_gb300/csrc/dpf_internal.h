@@ -89,4 +89,23 @@ struct Coeffs {
     const T *idg;                  // inverse diagonal (FP64 levels), or null: computed on the fly
 };
 
+// Per-level pointers and the Chebyshev parameters of the fused small-level tail kernel.
+template <typename T>
+struct TailLevel {
+    const LevelDesc *desc;
+    Coeffs<T> C;
+    T *xa, *xb, *b, *d;
+    const uint8_t *dir;
+};
+
+template <typename T>
+struct TailParams {
+    T c1[8], c2[8];  // Chebyshev recurrence coefficients, steps 0..deg-1
+    T invtheta, coarse_scale;
+    int deg;
+};
+
+constexpr int kTailThreads = 1024;
+
+
 }  // namespace dpf

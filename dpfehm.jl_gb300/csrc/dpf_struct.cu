@@ -16,11 +16,14 @@
 #include <set>
 #include <stdexcept>
 
+#include <cooperative_groups.h>
+
 #include "dpf_struct.h"
 #include "dpf_struct_kernels.cuh"
 #include "dpf_plane.cuh"
 
 namespace dpf {
+namespace cg = cooperative_groups;
 
 // ================================================================ kernels
 // Conductance of the face between cell c and its neighbour j in direction d (0..2)
@@ -199,45 +202,52 @@ __global__ void k_coarse_factor(const LevelDesc *__restrict__ desc, const int *_
 }
 
 // ---- per-cell bodies of the V-cycle steps, shared by the per-level kernels (one launch
-// per level, all problems) and the fused tail kernel (all small levels of one problem)
+// per level, all problems) and the fused tail kernel (all small levels of one problem).
+// CG: vectors written earlier in the same kernel by other blocks of a cluster are read
+// through L2 (ld.global.cg), so no block sees a stale L1 line.
+template <bool CG, typename T>
+__device__ __forceinline__ T ldv(const T *p, long long i) {
+    if constexpr (CG) return __ldcg(p + i);
+    else return p[i];
+}
 
 // first Chebyshev step from a zero guess: x = d = invtheta D^-1 b
-template <typename T>
+template <typename T, bool CG = false>
 __device__ __forceinline__ void cell_cheb_first(const LevelDesc &L, const Cell &c, const Coeffs<T> &C,
                                                 const T *__restrict__ b, T *__restrict__ x, T *__restrict__ d,
                                                 T invtheta) {
     T v;
-    if constexpr (sizeof(T) == 8) v = invtheta * b[c.i] * C.idg[c.i];
-    else v = invtheta * __fdividef(b[c.i], diag7(L, c, C));
+    if constexpr (sizeof(T) == 8) v = invtheta * ldv<CG>(b, c.i) * C.idg[c.i];
+    else v = invtheta * __fdividef(ldv<CG>(b, c.i), diag7(L, c, C));
     x[c.i] = v;
     d[c.i] = v;
 }
 
 // the first two Chebyshev steps from a zero guess (see k_cheb_first2)
-template <typename T>
+template <typename T, bool CG = false>
 __device__ __forceinline__ void cell_cheb_first2(const LevelDesc &L, const Cell &c, const Coeffs<T> &C,
                                                  const T *__restrict__ b, T *__restrict__ xout, T *__restrict__ d,
                                                  T invtheta, T c1, T c2) {
     const T *__restrict__ g = C.idg;
-    const T bi = b[c.i], gi = g[c.i];
+    const T bi = ldv<CG>(b, c.i), gi = g[c.i];
     const T x1 = invtheta * bi * gi;
     T Ax, dg;
-    apply7(L, c, C, x1, [&](long long j, int, int, int) { return invtheta * b[j] * g[j]; }, Ax, dg);
+    apply7(L, c, C, x1, [&](long long j, int, int, int) { return invtheta * ldv<CG>(b, j) * g[j]; }, Ax, dg);
     const T dn = c1 * x1 + c2 * (bi - Ax) * gi;
     d[c.i] = dn;
     xout[c.i] = x1 + dn;
 }
 
 // one Chebyshev step (see k_cheb_step); returns the new iterate
-template <typename T, bool FIRST>
+template <typename T, bool FIRST, bool CG = false>
 __device__ __forceinline__ T cell_cheb_step(const LevelDesc &L, const Cell &c, const Coeffs<T> &C,
                                             const T *__restrict__ b, const T *__restrict__ xin,
                                             T *__restrict__ xout, T *__restrict__ d, T c1, T c2, T &bi) {
-    T xi = xin[c.i], Ax, dg;
-    apply7(L, c, C, xi, [&](long long j, int, int, int) { return xin[j]; }, Ax, dg);
-    bi = b[c.i];
+    T xi = ldv<CG>(xin, c.i), Ax, dg;
+    apply7(L, c, C, xi, [&](long long j, int, int, int) { return ldv<CG>(xin, j); }, Ax, dg);
+    bi = ldv<CG>(b, c.i);
     T r = dinv_times(C, c.i, bi - Ax, dg);
-    T dn = FIRST ? c2 * r : c1 * d[c.i] + c2 * r;
+    T dn = FIRST ? c2 * r : c1 * ldv<CG>((const T *)d, c.i) + c2 * r;
     T xo = xi + dn;
     d[c.i] = dn;
     xout[c.i] = xo;
@@ -245,7 +255,7 @@ __device__ __forceinline__ T cell_cheb_step(const LevelDesc &L, const Cell &c, c
 }
 
 // restricted residual of coarse cell cc: sum over its children i of b_i - (A x)_i
-template <typename T>
+template <typename T, bool CG = false>
 __device__ __forceinline__ T cell_restrict(const LevelDesc &L, const Cell &cc, const Coeffs<T> &C,
                                            const T *__restrict__ b, const T *__restrict__ x) {
     const long long fsy = L.nz, fsx = (long long)L.ny * L.nz;
@@ -258,9 +268,9 @@ __device__ __forceinline__ T cell_restrict(const LevelDesc &L, const Cell &cc, c
                 Cell c;
                 c.ix = fx; c.iy = fy; c.iz = fz;
                 c.i = L.off + fx * fsx + fy * fsy + fz;
-                T xi = x[c.i], Ax, dg;
-                apply7(L, c, C, xi, [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
-                acc += b[c.i] - Ax;
+                T xi = ldv<CG>(x, c.i), Ax, dg;
+                apply7(L, c, C, xi, [&](long long j, int, int, int) { return ldv<CG>(x, j); }, Ax, dg);
+                acc += ldv<CG>(b, c.i) - Ax;
             }
     return acc;
 }
@@ -410,30 +420,27 @@ __global__ void k_coarse_solve(const LevelDesc *__restrict__ desc, const int *__
 // launches of a few thousand cells each per V-cycle). Same arithmetic, same buffers
 // and the same result as the per-level kernels: the corrected iterate of level lt
 // lands in its xb buffer.
-template <typename T>
-struct TailLevel {
-    const LevelDesc *desc;
-    Coeffs<T> C;
-    T *xa, *xb, *b, *d;
-    const uint8_t *dir;
-};
 
-template <typename T>
-struct TailParams {
-    T c1[8], c2[8];  // Chebyshev recurrence coefficients, steps 0..deg-1
-    T invtheta, coarse_scale;
-    int deg;
-};
-
-constexpr int kTailThreads = 1024;
-
-template <typename T>
+template <typename T, bool CLUSTER>
 __global__ void __launch_bounds__(kTailThreads) k_tail_cycle(const TailLevel<T> *__restrict__ tl,
                                                              const int4 *__restrict__ tails, const CgState *st,
                                                              const double *__restrict__ Inv, TailParams<T> tp) {
-    const int4 t = tails[blockIdx.x];  // problem, first tail level, coarsest level
+    // one problem per block, or (CLUSTER) per thread-block cluster: its blocks share every
+    // step's cells and meet at hardware cluster barriers
+    unsigned rank = 0, nranks = 1;
+    if constexpr (CLUSTER) {
+        rank = cg::this_cluster().block_rank();
+        nranks = cg::this_cluster().num_blocks();
+    }
+    const int4 t = tails[blockIdx.x / nranks];  // problem, first tail level, coarsest level
     const int p = t.x, lt = t.y, lc = t.z;
-    if (st && !st[p].active) return;
+    if (st && !st[p].active) return;  // uniform over the problem's blocks
+    auto sync = [&]() {
+        if constexpr (CLUSTER) cg::this_cluster().sync();
+        else __syncthreads();
+    };
+    const int first = (int)(rank * blockDim.x + threadIdx.x);
+    const int stride = (int)(nranks * blockDim.x);
     const int deg = tp.deg;
     // descend
     for (int l = lt; l < lc; l++) {
@@ -442,53 +449,53 @@ __global__ void __launch_bounds__(kTailThreads) k_tail_cycle(const TailLevel<T> 
         T *cur = V.xa, *oth = V.xb;
         int k0 = 1;
         if (deg >= 2) {
-            for (int li = threadIdx.x; li < (int)L.n; li += blockDim.x) {
+            for (int li = first; li < (int)L.n; li += stride) {
                 Cell c;
                 cell_at(L, li, c);
-                cell_cheb_first2(L, c, V.C, V.b, V.xb, V.d, tp.invtheta, tp.c1[1], tp.c2[1]);
+                cell_cheb_first2<T, CLUSTER>(L, c, V.C, V.b, V.xb, V.d, tp.invtheta, tp.c1[1], tp.c2[1]);
             }
             cur = V.xb;
             oth = V.xa;
             k0 = 2;
         } else {
-            for (int li = threadIdx.x; li < (int)L.n; li += blockDim.x) {
+            for (int li = first; li < (int)L.n; li += stride) {
                 Cell c;
                 cell_at(L, li, c);
-                cell_cheb_first(L, c, V.C, V.b, V.xa, V.d, tp.invtheta);
+                cell_cheb_first<T, CLUSTER>(L, c, V.C, V.b, V.xa, V.d, tp.invtheta);
             }
         }
-        __syncthreads();
+        sync();
         for (int k = k0; k < deg; k++) {
-            for (int li = threadIdx.x; li < (int)L.n; li += blockDim.x) {
+            for (int li = first; li < (int)L.n; li += stride) {
                 Cell c;
                 cell_at(L, li, c);
                 T bi;
-                cell_cheb_step<T, false>(L, c, V.C, V.b, cur, oth, V.d, tp.c1[k], tp.c2[k], bi);
+                cell_cheb_step<T, false, CLUSTER>(L, c, V.C, V.b, cur, oth, V.d, tp.c1[k], tp.c2[k], bi);
             }
-            __syncthreads();
+            sync();
             T *tmp = cur; cur = oth; oth = tmp;
         }
         const TailLevel<T> W = tl[l + 1];
         const LevelDesc Lc = W.desc[p];
-        for (int li = threadIdx.x; li < (int)Lc.n; li += blockDim.x) {
+        for (int li = first; li < (int)Lc.n; li += stride) {
             Cell cc;
             cell_at(Lc, li, cc);
-            W.b[cc.i] = cell_restrict(L, cc, V.C, V.b, cur);
+            W.b[cc.i] = cell_restrict<T, CLUSTER>(L, cc, V.C, V.b, cur);
         }
-        __syncthreads();
+        sync();
     }
-    // coarsest: x = A^-1 b with the stored dense inverse
+    // coarsest: x = A^-1 b with the stored dense inverse (first block of the problem)
     {
         const TailLevel<T> V = tl[lc];
         const LevelDesc L = V.desc[p];
         const double *Ip = Inv + (long long)p * kMaxCoarse * kMaxCoarse;
         const int i = threadIdx.x;
-        if (i < (int)L.n) {
+        if (rank == 0 && i < (int)L.n) {
             double xi = 0.0;
-            for (int j = 0; j < (int)L.n; j++) xi += Ip[j * kMaxCoarse + i] * (double)V.b[L.off + j];
+            for (int j = 0; j < (int)L.n; j++) xi += Ip[j * kMaxCoarse + i] * (double)ldv<CLUSTER>(V.b, L.off + j);
             V.xb[L.off + i] = (T)xi;
         }
-        __syncthreads();
+        sync();
     }
     // ascend: prolongation in place into the pre-smoothed iterate, then deg steps
     for (int l = lc - 1; l >= lt; l--) {
@@ -497,24 +504,24 @@ __global__ void __launch_bounds__(kTailThreads) k_tail_cycle(const TailLevel<T> 
         const TailLevel<T> W = tl[l + 1];
         const LevelDesc Lc = W.desc[p];
         T *cur = (deg % 2 == 0) ? V.xb : V.xa;  // where pre-smoothing left its iterate
-        for (int li = threadIdx.x; li < (int)L.n; li += blockDim.x) {
+        for (int li = first; li < (int)L.n; li += stride) {
             Cell c;
             cell_at(L, li, c);
             if (V.dir[c.i]) continue;
             cur[c.i] += tp.coarse_scale *
-                        W.xb[Lc.off + ((long long)(c.ix >> 1) * Lc.ny + (c.iy >> 1)) * Lc.nz + (c.iz >> 1)];
+                        ldv<CLUSTER>(W.xb, Lc.off + ((long long)(c.ix >> 1) * Lc.ny + (c.iy >> 1)) * Lc.nz + (c.iz >> 1));
         }
-        __syncthreads();
+        sync();
         for (int k = 0; k < deg; k++) {
             T *o = cur == V.xa ? V.xb : V.xa;
-            for (int li = threadIdx.x; li < (int)L.n; li += blockDim.x) {
+            for (int li = first; li < (int)L.n; li += stride) {
                 Cell c;
                 cell_at(L, li, c);
                 T bi;
-                if (k == 0) cell_cheb_step<T, true>(L, c, V.C, V.b, cur, o, V.d, tp.c1[0], tp.invtheta, bi);
-                else cell_cheb_step<T, false>(L, c, V.C, V.b, cur, o, V.d, tp.c1[k], tp.c2[k], bi);
+                if (k == 0) cell_cheb_step<T, true, CLUSTER>(L, c, V.C, V.b, cur, o, V.d, tp.c1[0], tp.invtheta, bi);
+                else cell_cheb_step<T, false, CLUSTER>(L, c, V.C, V.b, cur, o, V.d, tp.c1[k], tp.c2[k], bi);
             }
-            __syncthreads();
+            sync();
             cur = o;
         }
     }
@@ -1681,6 +1688,55 @@ void StructBatch::pm_restrict(int l, const T *b, const T *x, T *bc) {
     }
 }
 
+// The fused tail: one block per problem, or a cluster of tail_cs blocks per problem when
+// the device can co-schedule that many 1024-thread blocks (halved until it can).
+template <typename T>
+void StructBatch::launch_tail(const TailParams<T> &tp) {
+    const unsigned nt = (unsigned)tails.size();
+    if (tail_cs == 0) {
+        int cs = std::max(1, std::min(16, opt.tail_cluster));
+        while (cs > 1) {
+            if (cs > 8)
+                CK(cudaFuncSetAttribute(k_tail_cycle<T, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(nt * cs);
+            cfg.blockDim = dim3(kTailThreads);
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = cs;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            int nclusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&nclusters, k_tail_cycle<T, true>, &cfg) == cudaSuccess && nclusters > 0)
+                break;
+            cudaGetLastError();
+            cs /= 2;
+        }
+        tail_cs = cs;
+    }
+    if (tail_cs <= 1) {
+        k_tail_cycle<T, false><<<nt, kTailThreads, 0, stream>>>((const TailLevel<T> *)d_tail_lv, d_tails, d_state,
+                                                               d_coarseL, tp);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nt * tail_cs);
+    cfg.blockDim = dim3(kTailThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = tail_cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    CK(cudaLaunchKernelEx(&cfg, k_tail_cycle<T, true>, (const TailLevel<T> *)d_tail_lv, (const int4 *)d_tails,
+                          (const CgState *)d_state, (const double *)d_coarseL, tp));
+}
+
 template <typename T>
 void StructBatch::vcycle(const T *r, T *z) {
     const int deg = opt.cheb_degree;
@@ -1800,8 +1856,7 @@ void StructBatch::vcycle(const T *r, T *z) {
         tp.deg = deg;
         {
             KTimer _kt(this, kname("k_tail_cycle", tail_first_level, sizeof(T) == 4), tail_cells_total);
-            k_tail_cycle<T><<<(unsigned)tails.size(), kTailThreads, 0, stream>>>(
-                (const TailLevel<T> *)d_tail_lv, d_tails, d_state, d_coarseL, tp);
+            launch_tail<T>(tp);
         }
         LAUNCH_CHECK();
     }

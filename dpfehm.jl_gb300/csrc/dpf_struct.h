@@ -114,6 +114,8 @@ public:
     void build_plane_items(PlaneItems &P, const Level &L, const std::vector<int> &take, int sms, int cells,
                            int blocks_per_sm, const std::vector<std::vector<std::array<int, 3>>> *shapes, int l);
     template <typename T>
+    void launch_tail(const TailParams<T> &tp);
+    template <typename T>
     void pm_restrict(int l, const T *b, const T *x, T *bc);
     void pm_df_spmv(const CoeffsDF &C);
     template <typename T>
@@ -165,6 +167,7 @@ public:
     int4 *d_tails = nullptr;
     void *d_tail_lv = nullptr;
     long long tail_cells_total = 0;
+    int tail_cs = 0;  // cluster size actually used for the tail (0: not yet chosen)
     int tail_first_level = 0;
     int *h_count = nullptr;
     void *h_state_buf = nullptr;

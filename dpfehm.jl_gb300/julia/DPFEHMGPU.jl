@@ -35,10 +35,11 @@ mutable struct Options
     plane_blocks_per_sm::Cint
     df_plane_cells::Cint
     df_plane_blocks_per_sm::Cint
+    tail_cluster::Cint
 end
 
 function default_options(; reltol=nothing, maxiter=nothing, precision=nothing)
-    o = Options(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
+    o = Options(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
     ccall((:dpf_default_options, libdpf), Cvoid, (Ref{Options},), o)
     reltol === nothing || (o.reltol = reltol)
     maxiter === nothing || (o.maxiter = maxiter)

@@ -86,6 +86,8 @@ typedef struct dpf_options {
     int df_plane_cells;  /* MIXED: slab capacity of a plane-marching double-float CG product, 256..1024
                             (default -1: the grid-stride product, as fast on GB300; an autotuner choice) */
     int df_plane_blocks_per_sm; /* its work items per SM (default 4) */
+    int tail_cluster;    /* blocks (a thread-block cluster, 2..16) per problem for the fused tail
+                            (default 1: one block) */
 } dpf_options;
 
 typedef struct dpf_problem dpf_problem;
@@ -188,7 +190,7 @@ int dpf_batch_solve_grad_logk(dpf_problem *h, const double *logK, int mean_kind,
 
 /* Autotuner for a batch (same arguments as dpf_batch_create and dpf_batch_solve_grad_logk):
  * coordinate descent over the Chebyshev degree, plane_cells, plane_blocks_per_sm,
- * tail_cells, blocks_per_sm and df_plane_cells, starting from *base (NULL: defaults), each candidate timed
+ * tail_cells, blocks_per_sm, df_plane_cells and tail_cluster, starting from *base (NULL: defaults), each candidate timed
  * over `repeats` forward + adjoint solves of the given inputs (host or device buffers)
  * after one untimed solve; a candidate is kept if it converges and is >= 2 % faster.
  * Writes the chosen options to *best and their time per solve call to *best_ms.

@@ -143,8 +143,27 @@ def test_autotune_batch(gpu_lib):
     assert tuned["cheb_degree"] in (1, 2, 3) and tuned["plane_cells"] in (512, 768, 1024)
     assert tuned["plane_blocks_per_sm"] in (1, 2, 3) and tuned["tail_cells"] in (-1, 1024, 4096, 16384)
     assert tuned["blocks_per_sm"] in (8, 16, 24) and tuned["df_plane_cells"] in (-1, 512)
+    assert tuned["tail_cluster"] in (1, 8)
     B0 = pkg.GroundwaterBatch(*args, reltol=1e-11, precision="mixed")
     B1 = pkg.GroundwaterBatch(*args, reltol=1e-11, precision="mixed", **tuned)
     h0, g0 = B0.solve_grad_logk(cat("logK"), cat("dh"), cat("Qs"), [p["obs"] for p in probs])
     h1, g1 = B1.solve_grad_logk(cat("logK"), cat("dh"), cat("Qs"), [p["obs"] for p in probs])
     assert rel(h1, h0) < 1e-9 and rel(g1, g0) < 1e-7
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cluster_tail_agrees(gpu_lib, precision):
+    """The fused small-level tail run by a thread-block cluster per problem (levels from 1
+    down) gives the per-level kernels' solution."""
+    pkg = gpu_lib
+    shapes = [(20, 16, 5), (9, 9, 9), (40, 30, 6), (3, 4, 2), (17, 5, 11)]
+    probs = [_problem(pkg, ns, 61 + k) for k, ns in enumerate(shapes)]
+    cat = lambda k: np.concatenate([p[k] for p in probs])
+    res = []
+    for tail, cl in ((-1, 1), (20000, 8), (20000, 1), (4096, 16)):
+        B = pkg.GroundwaterBatch([p["ns"] for p in probs], [p["mins"] for p in probs], [p["maxs"] for p in probs],
+                                 [p["dn"] for p in probs], reltol=1e-12, precision=precision, tail_cells=tail,
+                                 tail_cluster=cl)
+        res.append(B.solve_grad_logk(cat("logK"), cat("dh"), cat("Qs"), [p["obs"] for p in probs]))
+    for h, g in res[1:]:
+        assert rel(h, res[0][0]) < 1e-11 and rel(g, res[0][1]) < 1e-9
