@@ -449,7 +449,7 @@ def main():
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch the CG loop from the host (ncu cannot profile kernels inside conditional graphs)")
     ap.add_argument("--main-only", action="store_true", help="only the timed region (for profiling runs)")
-    ap.add_argument("--workload", default="steady_1m", choices=["steady_1m", "steady_100k", "uneven_batch", "transient"],
+    ap.add_argument("--workload", default="steady_1m", choices=["steady_1m", "steady_100k", "uneven_batch", "transient", "general_1m"],
                     help="steady_1m is the headline; the others are the remaining configurations (bench_workloads.py)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

@@ -186,9 +186,9 @@ dpf_options fill_options(const dpf_options *o) {
     dpf_options r = *o;
     if (!(r.reltol > 0)) r.reltol = d.reltol;
     if (r.maxiter <= 0) r.maxiter = d.maxiter;
-    if (r.cheb_degree <= 0) r.cheb_degree = d.cheb_degree;
+    if (r.cheb_degree < 0) r.cheb_degree = d.cheb_degree;  // 0: the path's own default
     if (!(r.cheb_lo > 0 && r.cheb_lo < 1)) r.cheb_lo = d.cheb_lo;
-    if (!(r.coarse_scale > 0)) r.coarse_scale = d.coarse_scale;
+    if (!(r.coarse_scale >= 0)) r.coarse_scale = d.coarse_scale;  // 0: the path's own default
     if (r.max_coarse <= 0) r.max_coarse = d.max_coarse;
     if (r.max_outer <= 0) r.max_outer = d.max_outer;
     if (r.check_every <= 0) r.check_every = d.check_every;
@@ -239,9 +239,9 @@ void dpf_default_options(dpf_options *o) {
     o->reltol = 1e-10;
     o->maxiter = 500;
     o->precision = DPF_PREC_FP64;
-    o->cheb_degree = 2;
+    o->cheb_degree = 0;
     o->cheb_lo = 0.2;
-    o->coarse_scale = 2.0;
+    o->coarse_scale = 0.0;
     o->max_coarse = 64;
     o->max_outer = 6;
     o->use_graphs = 1;

@@ -706,6 +706,11 @@ GeneralSolver::GeneralSolver(long long N_, long long F_, const int64_t *a, const
     F = F_;
     if (N >= (1LL << 31) || F >= (1LL << 31)) throw BadInput("general topologies are limited to 2^31 cells and faces");
     if (opt.max_coarse < 1 || opt.max_coarse > kMaxCoarse) opt.max_coarse = kMaxCoarse;
+    // defaults of the general path: graph aggregates are larger and less regular than
+    // 2x2x2 cubes, and a stronger smoother with a larger over-correction pays (on a 1M-cell
+    // 7-point graph with a sigma = 2 field: 32 CG iterations instead of 74 with 2 / 2.0)
+    if (opt.cheb_degree == 0) opt.cheb_degree = 3;
+    if (!(opt.coarse_scale > 0)) opt.coarse_scale = 3.5;
     if (opt.cheb_degree < 1) opt.cheb_degree = 1;
     if (opt.cheb_degree > 8) opt.cheb_degree = 8;
     mixed = opt.precision == DPF_PREC_MIXED;

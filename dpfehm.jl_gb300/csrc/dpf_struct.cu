@@ -1219,6 +1219,8 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
     nprob = (int)grids.size();
     if (nprob <= 0) throw BadInput("empty batch");
     if (opt.max_coarse < 1 || opt.max_coarse > kMaxCoarse) opt.max_coarse = kMaxCoarse;
+    if (opt.cheb_degree == 0) opt.cheb_degree = 2;  // regular grids' defaults (2x2x2 aggregates)
+    if (!(opt.coarse_scale > 0)) opt.coarse_scale = 2.0;
     if (opt.cheb_degree < 1) opt.cheb_degree = 1;
     if (opt.cheb_degree > 8) opt.cheb_degree = 8;
     mixed = opt.precision == DPF_PREC_MIXED;

@@ -61,6 +61,9 @@ extern "C" int dpf_batch_autotune(int nprob, const int *dims, const double *mins
     dpf_options cur;
     dpf_default_options(&cur);
     if (base) cur = *base;
+    // batches are regular grids: resolve the "path default" values to the regular-grid ones
+    if (cur.cheb_degree == 0) cur.cheb_degree = 2;
+    if (!(cur.coarse_scale > 0)) cur.coarse_scale = 2.0;
     DevCopy dlk, ddh, dq;
     int rc;
     if ((rc = to_device(logK, N, dlk)) || (rc = to_device(dh, N, ddh)) || (rc = to_device(Qs, N, dq))) return rc;

@@ -69,9 +69,11 @@ typedef struct dpf_options {
     double reltol;       /* stop when ||b - A h|| <= reltol * ||b||            (default 1e-10) */
     int maxiter;         /* CG iteration cap per solve                        (default 500)   */
     int precision;       /* dpf_precision                                     (default FP64)  */
-    int cheb_degree;     /* Chebyshev smoother degree per pre/post sweep      (default 2)     */
+    int cheb_degree;     /* Chebyshev smoother degree per pre/post sweep (default 0: 2 on regular
+                            grids, 3 on the general path) */
     double cheb_lo;      /* lower end of the Chebyshev interval / upper end   (default 0.2)   */
-    double coarse_scale; /* scaling of the coarse-grid correction              (default 2.0)   */
+    double coarse_scale; /* scaling of the coarse-grid correction (default 0: 2.0 on regular grids,
+                            3.5 on the general path, whose graph aggregates are larger) */
     int max_coarse;      /* coarsen until a level has at most this many cells (default 64, <= 64) */
     int max_outer;       /* MIXED: cap on rounds, each restarted from the true FP64 residual (default 6) */
     int use_graphs;      /* capture each solve's iteration in a CUDA graph    (default 1)     */
