@@ -29,7 +29,8 @@ __all__ = [
     "groundwater_steadystate", "rrule_groundwater_steadystate", "logKs2Ks_neighbors", "GroundwaterProblem",
     "GroundwaterBatch", "DPFError", "NoTangent", "getfreenodes", "addboundaryconditions", "regulargrid1d",
     "regulargrid2d", "regulargrid3d", "load_uge", "fields", "grid", "load", "default_options", "MEAN_GEOMETRIC",
-    "MEAN_HARMONIC", "PREC_FP64", "PREC_MIXED",
+    "MEAN_HARMONIC", "PREC_FP64", "PREC_MIXED", "solvepressure", "rrule_solvepressure", "amg_solver",
+    "cholesky_solver", "autotune_batch",
 ]
 
 
@@ -419,20 +420,46 @@ def _problem_for(neighbors, areasoverlengths, dirichletnodes, N, options):
     return P
 
 
+def amg_solver(*_a, **_k):
+    """Selector for ``linear_solver=`` (src/groundwater.jl:45-49): the GPU's AMG-preconditioned
+    CG to ``reltol`` (the default)."""
+    raise TypeError("amg_solver selects the solver; pass it as linear_solver=amg_solver")
+
+
+def cholesky_solver(*_a, **_k):
+    """Selector for ``linear_solver=`` (src/groundwater.jl:56-60): a solve to direct-solve
+    accuracy. On the GPU this is the AMG-preconditioned CG run to the FP64 rounding floor of
+    the system (the mixed solver with reltol 0 stops there), not a sparse factorisation."""
+    raise TypeError("cholesky_solver selects the solver; pass it as linear_solver=cholesky_solver")
+
+
+def _solver_options(linear_solver, kwargs):
+    if linear_solver is None or linear_solver is amg_solver or linear_solver == "amg":
+        return kwargs
+    if linear_solver is cholesky_solver or linear_solver == "cholesky":
+        o = dict(kwargs)
+        o.setdefault("precision", "mixed")
+        o["reltol"] = 1e-30  # below any FP64 floor: the solve ends at the floor (status OK)
+        o.setdefault("max_outer", 12)
+        return o
+    raise ValueError("linear_solver must be amg_solver or cholesky_solver")
+
+
 def groundwater_steadystate(Ks, neighbors, areasoverlengths, dirichletnodes, dirichleths, Qs, *, linear_solver=None,
                             **kwargs):
     """Steady-state heads over all cells (src/groundwater.jl:75-83).
 
-    ``linear_solver`` is accepted for signature compatibility and ignored: the
-    solve is always the GPU's AMG-preconditioned CG. ``kwargs`` are solver
-    options (reltol, maxiter, precision='fp64'|'mixed', ...).
+    ``linear_solver``: ``amg_solver`` (default; CG + AMG to ``reltol``) or ``cholesky_solver``
+    (the same solver run to the FP64 rounding floor, i.e. direct-solve accuracy). ``kwargs``
+    are solver options (reltol, maxiter, precision='fp64'|'mixed', ...).
     """
     N = len(Qs) if not _is_torch(Qs) else Qs.numel()
-    P = _problem_for(neighbors, areasoverlengths, dirichletnodes, N, kwargs)
+    P = _problem_for(neighbors, areasoverlengths, dirichletnodes, N, _solver_options(linear_solver, kwargs))
     return P.forward(Ks, dirichleths, Qs)
 
 
-def rrule_groundwater_steadystate(Ks, neighbors, areasoverlengths, dirichletnodes, dirichleths, Qs, **kwargs):
+def rrule_groundwater_steadystate(Ks, neighbors, areasoverlengths, dirichletnodes, dirichleths, Qs, *,
+                                  linear_solver=None, **kwargs):
     """(h, pullback) like ChainRulesCore.rrule (src/groundwater.jl:85-109).
 
     pullback(delta) returns (NoTangent, dKs, NoTangent, NoTangent, NoTangent,
@@ -440,7 +467,8 @@ def rrule_groundwater_steadystate(Ks, neighbors, areasoverlengths, dirichletnode
     lives as long as the pullback closure.
     """
     N = len(Qs) if not _is_torch(Qs) else Qs.numel()
-    P = GroundwaterProblem(neighbors, areasoverlengths, dirichletnodes, N=N, **kwargs)
+    P = GroundwaterProblem(neighbors, areasoverlengths, dirichletnodes, N=N,
+                           **_solver_options(linear_solver, kwargs))
     h = P.forward(Ks, dirichleths, Qs)
 
     def pullback(delta):
@@ -448,6 +476,37 @@ def rrule_groundwater_steadystate(Ks, neighbors, areasoverlengths, dirichletnode
         return (NoTangent, dKs, NoTangent, NoTangent, NoTangent, ddh, dQs)
 
     pullback.problem = P
+    return h, pullback
+
+
+def _scaled(x, c):
+    return x * c
+
+
+def solvepressure(Ks_neighbors, neighbors, areasoverlengths, dirichletnodes, dirichleths, Qs, **kwargs):
+    """Two-phase pressure solve (src/twophase.jl:48-56): the steady system of
+    groundwater_steadystate with transmissibility 2 aol K (src/twophase.jl:25), i.e. the
+    steady solve with conductances 2 K. Solved to reltol 1e-14 unless given, like the
+    reference's cg_solver (src/twophase.jl:9-13); at the FP64 floor the solve is accepted."""
+    kwargs.setdefault("reltol", 1e-14)
+    kwargs.setdefault("precision", "mixed")
+    return groundwater_steadystate(_scaled(Ks_neighbors, 2.0), neighbors, areasoverlengths, dirichletnodes,
+                                   dirichleths, Qs, **kwargs)
+
+
+def rrule_solvepressure(Ks_neighbors, neighbors, areasoverlengths, dirichletnodes, dirichleths, Qs, **kwargs):
+    """(h, pullback) of solvepressure (src/twophase.jl:59-82): the tangents of the steady
+    rrule at conductances 2 K, with dKs scaled by 2 (d(2K)/dK)."""
+    kwargs.setdefault("reltol", 1e-14)
+    kwargs.setdefault("precision", "mixed")
+    h, pb = rrule_groundwater_steadystate(_scaled(Ks_neighbors, 2.0), neighbors, areasoverlengths, dirichletnodes,
+                                          dirichleths, Qs, **kwargs)
+
+    def pullback(delta):
+        t = pb(delta)
+        return (t[0], _scaled(t[1], 2.0)) + tuple(t[2:])
+
+    pullback.problem = pb.problem
     return h, pullback
 
 

@@ -103,11 +103,34 @@ function adjoint(p::Problem, delta)
     return dKs, ddh, dQs
 end
 
-"""Drop-in for `DPFEHM.groundwater_steadystate` (the `linear_solver` keyword is ignored)."""
+"""Selectors for the `linear_solver` keyword: `amg_solver` (CG + AMG to reltol, the default)
+and `cholesky_solver` (the same GPU solver run to the FP64 rounding floor of the system)."""
+function amg_solver end
+function cholesky_solver end
+
+solver_kwargs(ls, kwargs) = ls === cholesky_solver ? merge((; precision=:mixed, max_outer=12), kwargs, (; reltol=1e-30)) : kwargs
+
+"""Drop-in for `DPFEHM.groundwater_steadystate`."""
 function groundwater_steadystate(Ks, neighbors, areasoverlengths, dirichletnodes, dirichleths, Qs;
-                                 linear_solver=nothing, kwargs...)
-    p = Problem(neighbors, areasoverlengths, dirichletnodes, length(Qs); kwargs...)
+                                 linear_solver=amg_solver, kwargs...)
+    p = Problem(neighbors, areasoverlengths, dirichletnodes, length(Qs); solver_kwargs(linear_solver, values(kwargs))...)
     return forward(p, Ks, dirichleths, Qs)
+end
+
+"""Drop-in for `DPFEHM.solvepressure` (src/twophase.jl:48): the steady system with
+transmissibility 2 aol K, i.e. the steady solve at conductances 2K."""
+solvepressure(Ks, neighbors, areasoverlengths, dirichletnodes, dirichleths, Qs; kwargs...) =
+    groundwater_steadystate(2 .* Ks, neighbors, areasoverlengths, dirichletnodes, dirichleths, Qs; kwargs...)
+
+function ChainRulesCore.rrule(::typeof(solvepressure), Ks, neighbors, areasoverlengths, dirichletnodes,
+                              dirichleths, Qs; kwargs...)
+    h, pb = ChainRulesCore.rrule(groundwater_steadystate, 2 .* Ks, neighbors, areasoverlengths, dirichletnodes,
+                                 dirichleths, Qs; kwargs...)
+    function pullback(delta)
+        t = pb(delta)
+        return (t[1], ChainRulesCore.@thunk(2 .* ChainRulesCore.unthunk(t[2])), t[3:end]...)
+    end
+    return h, pullback
 end
 
 function ChainRulesCore.rrule(::typeof(groundwater_steadystate), Ks, neighbors, areasoverlengths, dirichletnodes,

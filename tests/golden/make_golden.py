@@ -6,7 +6,8 @@ explicit loops over the face list exactly as written in src/groundwater.jl:1-21
 (residual, and its derivatives with respect to h, Ks, dirichleths and Qs, as the
 NonlinearEquations macro would form them), solved by scipy's direct sparse
 solver, and the rrule formulas of src/groundwater.jl:93-107 applied literally
-(-(gw_Ks' * lambda) etc.). The C oracle and the GPU library are both checked
+(-(gw_Ks' * lambda) etc.); likewise the two-phase pressure solve of
+src/twophase.jl:22-82. The C oracle and the GPU library are both checked
 against these files.
 
 Run: python tests/golden/make_golden.py   (writes next to this script)
@@ -80,6 +81,50 @@ def steady_and_rrule(Ks, nb, aol, dn, dh, Qs, delta):
     ddh = -(Jdh.T @ lam) + delta * (~isfree)
     dQs = -(JQ.T @ lam)
     return h, dKs, ddh, dQs
+
+
+def pressure_and_rrule(Ks, nb, aol, dn, dh, Qs, delta):
+    """Two-phase pressure solve and its rrule, src/twophase.jl:22-82 restated literally:
+    residual -Q_i + sum over the faces of a free cell of (h_1 - h_2) * (tx K) with tx = 2 aol
+    (the Dirichlet value for h_2 at Dirichlet neighbours), its Jacobians by explicit loops, a
+    direct solve, and the pullback -(trans_Ks' lambda), -(trans_dirichleths' lambda) + delta at
+    Dirichlet cells, -(trans_Qs' lambda)."""
+    N, F = len(Qs), len(nb)
+    isfree, n2f, f2n = getfreenodes(N, dn)
+    m = len(f2n)
+    tx = 2.0 * aol
+
+    def terms(h):
+        R = np.zeros(m); Jh = np.zeros((m, m)); JK = np.zeros((m, F)); Jdh = np.zeros((m, N)); JQ = np.zeros((m, N))
+        for i in range(N):
+            if isfree[i]:
+                R[n2f[i]] += -Qs[i]
+                JQ[n2f[i], i] += -1.0
+        for f in range(F):
+            a, b = nb[f]
+            for n1, n2 in ((a, b), (b, a)):
+                if not isfree[n1]:
+                    continue
+                j1 = n2f[n1]
+                if isfree[n2]:
+                    j2 = n2f[n2]
+                    R[j1] += (h[j1] - h[j2]) * (tx[f] * Ks[f])
+                    Jh[j1, j1] += tx[f] * Ks[f]
+                    Jh[j1, j2] -= tx[f] * Ks[f]
+                    JK[j1, f] += (h[j1] - h[j2]) * tx[f]
+                else:
+                    R[j1] += (h[j1] - dh[n2]) * (tx[f] * Ks[f])
+                    Jh[j1, j1] += tx[f] * Ks[f]
+                    JK[j1, f] += (h[j1] - dh[n2]) * tx[f]
+                    Jdh[j1, n2] += -tx[f] * Ks[f]
+        return R, Jh, JK, Jdh, JQ
+
+    R0, A, _, _, _ = terms(np.zeros(m))
+    hfree = spl.spsolve(sp.csc_matrix(A), -R0)
+    h = np.where(isfree, hfree[np.maximum(n2f, 0)], dh)
+    _, _, JK, Jdh, JQ = terms(hfree)
+    lam = spl.spsolve(sp.csc_matrix(A.T), delta[isfree])
+    return h, -(JK.T @ lam), -(Jdh.T @ lam) + delta * (~isfree), -(JQ.T @ lam)
 
 
 def transient_and_adjoint(Ks, nb, aol, dn, dh, Qs, Ss, V, dt, nsteps, h0free, obs):
@@ -188,6 +233,17 @@ def main():
     np.savez(os.path.join(HERE, "transient_regular3d.npz"), ns=np.array(ns), nb=nb, aol=aol, Ks=Ks, Qs=Qs, dn=dn,
              dh=dh, Ss=Ss, V=V, dt=np.array(dt), nsteps=np.array(nsteps), h0=h0, obs=obs, states=states, dKs=dK,
              ddh=ddh, dQs=dQ, dh0=dh0)
+    # case E: two-phase pressure solve (transmissibility 2 aol K) and its rrule
+    ns = (6, 4, 3)
+    nb, aol, vol = grid3d(ns, (0, 0, 0), (3.0, 2.0, 1.0))
+    N = int(np.prod(ns))
+    Ks = np.exp(-8.0 + rng.standard_normal(len(nb)))
+    Qs = np.zeros(N); Qs[[1, 40]] = [3e-4, -1e-4]
+    dn = np.array([0, N - 1]); dh = np.zeros(N); dh[dn] = [2.0, -1.0]
+    delta = rng.standard_normal(N)
+    h, dKs, ddh, dQs = pressure_and_rrule(Ks, nb, aol, dn, dh, Qs, delta)
+    np.savez(os.path.join(HERE, "twophase_pressure.npz"), ns=np.array(ns), nb=nb, aol=aol, Ks=Ks, Qs=Qs, dn=dn,
+             dh=dh, delta=delta, h=h, dKs=dKs, ddh=ddh, dQs=dQs)
 
 
 if __name__ == "__main__":

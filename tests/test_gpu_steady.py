@@ -42,6 +42,35 @@ def test_golden_steady(gpu_lib, name):
     assert h.shape == (N,)
 
 
+def test_golden_twophase_pressure(gpu_lib):
+    """solvepressure and its rrule (src/twophase.jl:48-82) against the literal restatement."""
+    pkg = gpu_lib
+    g = dict(np.load(os.path.join(GOLD, "twophase_pressure.npz")))
+    h0 = pkg.solvepressure(g["Ks"], g["nb"], g["aol"], g["dn"], g["dh"], g["Qs"])
+    assert rel(h0, g["h"]) < HEAD_TOL
+    h, back = pkg.rrule_solvepressure(g["Ks"], g["nb"], g["aol"], g["dn"], g["dh"], g["Qs"])
+    assert rel(h, g["h"]) < HEAD_TOL
+    assert np.array_equal(h[g["dn"]], g["dh"][g["dn"]])
+    _, dKs, _, _, _, ddh, dQs = back(g["delta"])
+    assert rel(dKs, g["dKs"]) < GRAD_TOL
+    assert rel(ddh, g["ddh"]) < GRAD_TOL
+    assert rel(dQs, g["dQs"]) < GRAD_TOL
+
+
+def test_cholesky_solver_selector(gpu_lib):
+    """linear_solver=cholesky_solver solves to the FP64 rounding floor (direct-solve accuracy)."""
+    pkg = gpu_lib
+    g = dict(np.load(os.path.join(GOLD, "steady_harmonic_multidir.npz")))
+    h = pkg.groundwater_steadystate(g["Ks"], g["nb"], g["aol"], g["dn"], g["dh"], g["Qs"],
+                                    linear_solver=pkg.cholesky_solver)
+    assert rel(h, g["h"]) < 1e-12
+    h2 = pkg.groundwater_steadystate(g["Ks"], g["nb"], g["aol"], g["dn"], g["dh"], g["Qs"],
+                                     linear_solver=pkg.amg_solver, reltol=1e-10)
+    assert rel(h2, g["h"]) < HEAD_TOL
+    with pytest.raises(ValueError):
+        pkg.groundwater_steadystate(g["Ks"], g["nb"], g["aol"], g["dn"], g["dh"], g["Qs"], linear_solver="lu")
+
+
 @pytest.mark.parametrize("ns", [(12, 10, 6), (9, 7, 5), (16, 1, 9), (33, 17, 1), (5, 5, 5), (3, 2, 2), (64, 3, 2)])
 def test_steady_shapes_vs_oracle(gpu_lib, orc, ns):
     c = steady_case(gpu_lib, ns, sigma=1.5, seed=sum(ns), ndir=2, nq=3)

@@ -28,6 +28,20 @@ def test_oracle_matches_golden_steady(orc, name):
     assert rel(dQs, g["dQs"]) < 1e-10
 
 
+def test_oracle_matches_golden_twophase_pressure(orc):
+    """The two-phase pressure system (transmissibility 2 aol K, src/twophase.jl:25) is the steady
+    groundwater system with areas-over-lengths doubled; the oracle reproduces its golden case."""
+    g = _load("twophase_pressure.npz")
+    N = int(np.prod(g["ns"]))
+    P = orc.Problem(N, g["nb"], 2.0 * g["aol"], g["dn"])
+    h = P.steady(g["Ks"], g["dh"], g["Qs"], reltol=1e-15)
+    assert rel(h, g["h"]) < 1e-12
+    dKs, ddh, dQs = P.adjoint(g["dh"], g["delta"], reltol=1e-15)
+    assert rel(dKs, g["dKs"]) < 1e-10
+    assert rel(ddh, g["ddh"]) < 1e-10
+    assert rel(dQs, g["dQs"]) < 1e-10
+
+
 def test_oracle_matches_golden_transient(orc):
     g = _load("transient_regular3d.npz")
     N = int(np.prod(g["ns"]))
