@@ -38,12 +38,18 @@ mutable struct Options
     tail_cluster::Cint
 end
 
-function default_options(; reltol=nothing, maxiter=nothing, precision=nothing)
+"""The library defaults with any `dpf_options` field overridden by keyword (`precision` as
+`:fp64` or `:mixed`)."""
+function default_options(; kwargs...)
     o = Options(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
     ccall((:dpf_default_options, libdpf), Cvoid, (Ref{Options},), o)
-    reltol === nothing || (o.reltol = reltol)
-    maxiter === nothing || (o.maxiter = maxiter)
-    precision === nothing || (o.precision = precision == :mixed ? 1 : 0)
+    for (k, v) in pairs(kwargs)
+        if k === :precision
+            o.precision = v == :mixed ? 1 : 0
+        else
+            setfield!(o, k, convert(fieldtype(Options, k), v))
+        end
+    end
     return o
 end
 
