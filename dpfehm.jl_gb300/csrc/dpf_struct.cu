@@ -1408,6 +1408,7 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         for (auto &t : tails) tail_first_level = std::min(tail_first_level, t.y);
     }
     CK(cudaMallocHost(&h_count, 4 * sizeof(int)));
+    CK(cudaMallocHost(&h_misc, 4 * sizeof(int)));
     CK(cudaMallocHost(&h_state_buf, nprob * sizeof(CgState)));
     // Chebyshev coefficients on D^-1 A over [lo*2, 2] (Gershgorin: the spectrum of
     // D^-1 A of a weakly diagonally dominant symmetric M-matrix lies in [0, 2]).
@@ -1490,6 +1491,7 @@ StructBatch::~StructBatch() {
     if (cap_stream) cudaStreamDestroy(cap_stream);
     for (void *p : owned) cudaFree(p);
     if (h_count) cudaFreeHost(h_count);
+    if (h_misc) cudaFreeHost(h_misc);
     if (h_state_buf) cudaFreeHost(h_state_buf);
 }
 
@@ -2090,10 +2092,9 @@ void StructBatch::run_loop(int kind, void *x) {
     if (opt.use_graphs && !prof_on) {
         cudaGraphExec_t ex = loop_graph(kind, x);
         CK(cudaGraphLaunch(ex, stream));
-        // account the graph's kernel launches: body kernels times passes
-        CK(cudaMemcpyAsync(h_count, d_count, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
-        CK(cudaStreamSynchronize(stream));
-        launches += graphs[GraphKey{kind, x}].body_kernels * (long long)h_count[2];
+        // the graph's kernel launches (body kernels times passes) are counted when the solve
+        // reads its statistics, with no synchronisation here
+        graph_body_kernels = graphs[GraphKey{kind, x}].body_kernels;
         return;
     }
     const int check = std::max(1, opt.check_every);
@@ -2183,15 +2184,19 @@ void StructBatch::solve(const double *b, double *x, double reltol) {
         k_state_init<<<(nprob + 127) / 128, 128, 0, stream>>>(d_state, nprob);
     }
     LAUNCH_CHECK();
+    graph_body_kernels = 0;
     if (!mixed) {
         pcg<double>(b, x, tol2);
         stats_outer = 0;
     } else {
         df_pcg(b, x, tol2);
     }
-    // statistics
+    // statistics, the error words and the graph passes in one synchronisation
     CK(cudaMemcpyAsync(h_state_buf, d_state, nprob * sizeof(CgState), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(h_misc, d_factor_status, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(h_misc + 2, d_count + 2, sizeof(int), cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
+    if (graph_body_kernels) launches += graph_body_kernels * (long long)h_misc[2];
     CgState *hs = (CgState *)h_state_buf;
     last_status = DPF_OK;
     stats_iters = 0;
@@ -2205,13 +2210,11 @@ void StructBatch::solve(const double *b, double *x, double reltol) {
         stats_relres = std::max(stats_relres, rel);
         if (hs[p].status != DPF_OK && last_status == DPF_OK) last_status = hs[p].status;
     }
-    CK(cudaMemcpyAsync(&h_count[0], d_factor_status, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
-    CK(cudaStreamSynchronize(stream));
-    if (h_count[0]) {
+    if (h_misc[0]) {
         last_status = DPF_BAD_INPUT;
         last_message = "coarsest operator is not positive definite (does every problem have a Dirichlet cell?)";
     }
-    if (h_count[1]) {
+    if (h_misc[1]) {
         last_status = DPF_CUDA;
         last_message = "a shared-memory staging wait of a smoother kernel expired";
     }

@@ -168,6 +168,8 @@ public:
     void *d_tail_lv = nullptr;
     long long tail_cells_total = 0;
     int tail_cs = 0;  // cluster size actually used for the tail (0: not yet chosen)
+    int *h_misc = nullptr;           // pinned: error words and graph passes read with the statistics
+    long long graph_body_kernels = 0;  // kernels per pass of the loop graph used by the current solve
     int tail_first_level = 0;
     int *h_count = nullptr;
     void *h_state_buf = nullptr;
