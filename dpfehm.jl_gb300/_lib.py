@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libdpfehm_gpu.so")
 DPF_OK, DPF_BAD_INPUT, DPF_NOT_CONVERGED, DPF_NAN, DPF_OOM, DPF_CUDA, DPF_NO_DEVICE, DPF_STATE, DPF_UNSUPPORTED = range(9)
 STATUS_NAMES = {
     0: "DPF_OK", 1: "DPF_BAD_INPUT", 2: "DPF_NOT_CONVERGED", 3: "DPF_NAN", 4: "DPF_OOM", 5: "DPF_CUDA",
-    6: "DPF_NO_DEVICE", 7: "DPF_STATE", 8: "DPF_UNSUPPORTED",
+    6: "DPF_NO_DEVICE", 7: "DPF_STATE", 8: "DPF_UNSUPPORTED", 9: "DPF_TIMEOUT",
 }
 MEAN_GEOMETRIC, MEAN_HARMONIC = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
@@ -85,6 +85,9 @@ SIGNATURES = {
     "dpf_launch_count": (ctypes.c_longlong, [_vp]),
     "dpf_logk_to_faces_regular_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_int,
                                                          _vp]),
+    "dpf_debug_fail_alloc": (None, [ctypes.c_int64]),
+    "dpf_debug_alloc_stats": (None, [ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
+    "dpf_debug_expired_wait": (ctypes.c_int, [_f64p]),
 }
 
 _lib = None

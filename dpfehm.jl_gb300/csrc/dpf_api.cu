@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -31,7 +32,7 @@ struct dpf_problem {
     double tr_dt = 0;
     std::vector<void *> scratch;       // device scratch owned by the handle
     ~dpf_problem() {
-        for (void *p : scratch) cudaFree(p);
+        for (void *p : scratch) dev_free(p);
     }
 };
 
@@ -40,7 +41,52 @@ static thread_local std::string g_create_error;
 namespace dpf {
 // message for dpf_last_error(NULL) from entry points that have no handle
 void set_global_error(const std::string &msg) { g_create_error = msg; }
+
+// allocation accounting and the one-shot injected failure (k-th following allocation)
+static std::atomic<long long> g_fail_in{-1}, g_made{0}, g_live{0};
+
+static bool injected_failure() {
+    long long k = g_fail_in.load();
+    while (k >= 0)
+        if (g_fail_in.compare_exchange_weak(k, k - 1)) return k == 0;
+    return false;
+}
+
+cudaError_t dev_malloc(void **p, size_t bytes) {
+    *p = nullptr;
+    if (injected_failure()) return cudaErrorMemoryAllocation;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) { g_made++; g_live++; }
+    return e;
+}
+
+cudaError_t host_malloc(void **p, size_t bytes) {
+    *p = nullptr;
+    if (injected_failure()) return cudaErrorMemoryAllocation;
+    cudaError_t e = cudaMallocHost(p, bytes);
+    if (e == cudaSuccess) { g_made++; g_live++; }
+    return e;
+}
+
+void dev_free(void *p) {
+    if (!p) return;
+    cudaFree(p);
+    g_live--;
+}
+
+void host_free(void *p) {
+    if (!p) return;
+    cudaFreeHost(p);
+    g_live--;
+}
 }  // namespace dpf
+
+extern "C" void dpf_debug_fail_alloc(int64_t k) { dpf::g_fail_in.store(k < 0 ? -1 : (long long)k); }
+
+extern "C" void dpf_debug_alloc_stats(int64_t *made, int64_t *live) {
+    if (made) *made = dpf::g_made.load();
+    if (live) *live = dpf::g_live.load();
+}
 
 namespace {
 
@@ -97,7 +143,7 @@ void stage_out(dpf_problem *P, T *dst, const T *src, size_t n) {
 template <typename T>
 T *scratch(dpf_problem *P, size_t n) {
     void *p = nullptr;
-    if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) {
+    if (dev_malloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) {
         cudaGetLastError();
         throw OomError("device allocation failed");
     }
@@ -108,7 +154,7 @@ T *scratch(dpf_problem *P, size_t n) {
 void release(dpf_problem *P, void *p) {
     auto it = std::find(P->scratch.begin(), P->scratch.end(), p);
     if (it != P->scratch.end()) {
-        cudaFree(p);
+        dev_free(p);
         P->scratch.erase(it);
     }
 }
@@ -123,8 +169,9 @@ int check_device() {
 }
 
 template <typename F>
-int guarded(dpf_problem *P, F &&f) {
+int guarded(dpf_problem *P, const char *name, F &&f) {
     if (!P) return DPF_BAD_INPUT;
+    NvtxRange range(name);
     DeviceGuard g(P->device);
     try {
         int rc = f();
@@ -212,6 +259,7 @@ int make_struct(const std::vector<GridSpec> &grids, const std::vector<std::vecto
     *out = nullptr;
     int rc = check_device();
     if (rc) { g_create_error = "no CUDA device"; return rc; }
+    NvtxRange range("dpf_create (regular grids)");
     auto P = new dpf_problem();
     try {
         ck(cudaGetDevice(&P->device), "cudaGetDevice");
@@ -342,6 +390,7 @@ int dpf_create(int64_t N, int64_t F, const int64_t *nbr_a, const int64_t *nbr_b,
     *out = nullptr;
     int rc = check_device();
     if (rc) { g_create_error = "no CUDA device"; return rc; }
+    NvtxRange range("dpf_create (face list)");
     auto P = new dpf_problem();
     try {
         ck(cudaGetDevice(&P->device), "cudaGetDevice");
@@ -442,7 +491,7 @@ int dpf_last_stats(const dpf_problem *P, int *iterations, int *outer, double *re
 
 // ------------------------------------------------------------- steady state
 int dpf_steady_forward(dpf_problem *P, const double *Ks, const double *dh, const double *Qs, double *h_out) {
-    return guarded(P, [&]() -> int {
+    return guarded(P, __func__, [&]() -> int {
         if (!Ks || !dh || !Qs) throw BadInput("Ks, dirichleths and Qs are required");
         if (P->gs) return gs_status(P, P->gs->forward(Ks, nullptr, 0, dh, Qs, h_out));
         StructBatch &S = *P->sb;
@@ -457,7 +506,7 @@ int dpf_steady_forward(dpf_problem *P, const double *Ks, const double *dh, const
 
 int dpf_steady_forward_logk(dpf_problem *P, const double *logK, int kind, const double *dh, const double *Qs,
                             double *h_out) {
-    return guarded(P, [&]() -> int {
+    return guarded(P, __func__, [&]() -> int {
         if (!logK || !dh || !Qs) throw BadInput("logK, dirichleths and Qs are required");
         if (kind != DPF_MEAN_GEOMETRIC && kind != DPF_MEAN_HARMONIC) throw BadInput("unknown mean kind");
         if (P->gs) return gs_status(P, P->gs->forward(nullptr, logK, kind, dh, Qs, h_out));
@@ -472,7 +521,7 @@ int dpf_steady_forward_logk(dpf_problem *P, const double *logK, int kind, const 
 }
 
 int dpf_steady_adjoint(dpf_problem *P, const double *delta, double *dKs, double *ddh, double *dQs) {
-    return guarded(P, [&]() -> int {
+    return guarded(P, __func__, [&]() -> int {
         if (!delta) throw BadInput("delta is required");
         if (P->gs) return gs_status(P, P->gs->adjoint(delta, dKs, nullptr, ddh, dQs));
         StructBatch &S = *P->sb;
@@ -500,7 +549,7 @@ int dpf_steady_adjoint(dpf_problem *P, const double *delta, double *dKs, double 
 }
 
 int dpf_steady_adjoint_logk(dpf_problem *P, const double *delta, double *dlogK, double *ddh, double *dQs) {
-    return guarded(P, [&]() -> int {
+    return guarded(P, __func__, [&]() -> int {
         if (!delta) throw BadInput("delta is required");
         if (P->gs) return gs_status(P, P->gs->adjoint(delta, nullptr, dlogK, ddh, dQs));
         StructBatch &S = *P->sb;
@@ -531,7 +580,7 @@ int dpf_steady_adjoint_logk(dpf_problem *P, const double *delta, double *dlogK, 
 }
 
 int dpf_logk_to_faces(dpf_problem *P, const double *logK, int kind, double *Ks) {
-    return guarded(P, [&]() -> int {
+    return guarded(P, __func__, [&]() -> int {
         if (!logK || !Ks) throw BadInput("logK and Ks are required");
         if (kind != DPF_MEAN_GEOMETRIC && kind != DPF_MEAN_HARMONIC) throw BadInput("unknown mean kind");
         if (P->gs) return gs_status(P, P->gs->logk_to_faces(logK, kind, Ks));
@@ -545,7 +594,7 @@ int dpf_logk_to_faces(dpf_problem *P, const double *logK, int kind, double *Ks) 
 }
 
 int dpf_logk_to_faces_vjp(dpf_problem *P, const double *logK, int kind, const double *dKs, double *dlogK) {
-    return guarded(P, [&]() -> int {
+    return guarded(P, __func__, [&]() -> int {
         if (!logK || !dKs || !dlogK) throw BadInput("logK, dKs and dlogK are required");
         if (kind != DPF_MEAN_GEOMETRIC && kind != DPF_MEAN_HARMONIC) throw BadInput("unknown mean kind");
         if (P->gs) return gs_status(P, P->gs->logk_vjp(logK, kind, dKs, dlogK));
@@ -592,7 +641,7 @@ static int solve_grad_common(dpf_problem *P, const double *logK, int kind, const
 
 int dpf_solve_grad_logk(dpf_problem *P, const double *logK, int kind, const double *dh, const double *Qs,
                         int64_t nobs, const int64_t *obs, double *h_out, double *dlogK) {
-    return guarded(P, [&]() -> int {
+    return guarded(P, __func__, [&]() -> int {
         if (!logK || !dh || !Qs || nobs < 0 || (nobs > 0 && !obs)) throw BadInput("invalid arguments");
         if (kind != DPF_MEAN_GEOMETRIC && kind != DPF_MEAN_HARMONIC) throw BadInput("unknown mean kind");
         if (P->gs) return gs_status(P, P->gs->solve_grad_logk(logK, kind, dh, Qs, nobs, obs, h_out, dlogK));
@@ -621,7 +670,7 @@ int dpf_batch_offsets(const dpf_problem *P, int p, int64_t *cell_offset, int64_t
 
 int dpf_batch_solve_grad_logk(dpf_problem *P, const double *logK, int kind, const double *dh, const double *Qs,
                               const int64_t *obs_offsets, const int64_t *obs, double *h_out, double *dlogK) {
-    return guarded(P, [&]() -> int {
+    return guarded(P, __func__, [&]() -> int {
         if (!P->sb) throw BadInput("not a batch handle");
         if (!logK || !dh || !Qs || !obs_offsets) throw BadInput("invalid arguments");
         if (kind != DPF_MEAN_GEOMETRIC && kind != DPF_MEAN_HARMONIC) throw BadInput("unknown mean kind");
@@ -641,7 +690,7 @@ int dpf_batch_solve_grad_logk(dpf_problem *P, const double *logK, int kind, cons
 }
 
 int dpf_apply_operator(dpf_problem *P, const double *x, double *y) {
-    return guarded(P, [&]() -> int {
+    return guarded(P, __func__, [&]() -> int {
         if (!x || !y) throw BadInput("x and y are required");
         if (P->gs) return gs_status(P, P->gs->apply(x, y));
         StructBatch &S = *P->sb;
@@ -657,7 +706,7 @@ int dpf_apply_operator(dpf_problem *P, const double *x, double *y) {
 int dpf_transient_forward(dpf_problem *P, const double *Ks, const double *dh, const double *Qs, const double *Ss,
                           double dt, int nsteps, const double *h0, int checkpoint_every, double *states,
                           double *hT) {
-    return guarded(P, [&]() -> int {
+    return guarded(P, __func__, [&]() -> int {
         if (!Ks || !dh || !Qs || !Ss || !h0 || nsteps <= 0 || !(dt > 0)) throw BadInput("invalid arguments");
         if (P->gs) return gs_status(P, P->gs->transient_forward(Ks, dh, Qs, Ss, dt, nsteps, h0, states, hT));
         StructBatch &S = *P->sb;
@@ -733,7 +782,7 @@ __global__ void k_dh0(long long N, const uint8_t *__restrict__ dir, const double
 
 int dpf_transient_adjoint(dpf_problem *P, int64_t nobs, const int64_t *obs, const double *w, const double *gT,
                           double *dKs, double *ddh, double *dQs, double *dh0) {
-    return guarded(P, [&]() -> int {
+    return guarded(P, __func__, [&]() -> int {
         if (nobs < 0 || (nobs > 0 && !obs)) throw BadInput("invalid arguments");
         if (P->gs) return gs_status(P, P->gs->transient_adjoint(nobs, obs, w, gT, dKs, ddh, dQs, dh0));
         StructBatch &S = *P->sb;

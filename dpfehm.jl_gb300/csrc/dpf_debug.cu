@@ -1,0 +1,69 @@
+// dpf_debug.cu -- test hook for the bounded waits of the staging kernels.
+//
+// dpf_debug_expired_wait runs one block whose threads wait on a shared-memory mbarrier
+// that nothing arrives on, through the same bounded wait (mbar_wait) that every staging
+// kernel uses, so that a test sees that wait end by its bound, the error word set and the
+// device still usable, without any kernel of a solve being made to fail.
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "dpf_plane.cuh"
+
+namespace dpf {
+
+void set_global_error(const std::string &msg);
+
+__global__ void k_expired_wait(int *err, unsigned long long *waited_ns) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);  // one arrival completes phase 0; none is made
+    __syncthreads();
+    const uint64_t t0 = global_ns();
+    const bool done = mbar_wait(&bar, 0, err);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        waited_ns[0] = global_ns() - t0;
+        if (done) atomicExch(err, 2);  // the phase cannot complete: a defect of the wait
+    }
+}
+
+}  // namespace dpf
+
+extern "C" int dpf_debug_expired_wait(double *waited_ms) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        dpf::set_global_error("no CUDA device");
+        return DPF_NO_DEVICE;
+    }
+    void *buf = nullptr;
+    if (dpf::dev_malloc(&buf, 16) != cudaSuccess) {
+        cudaGetLastError();
+        dpf::set_global_error("device allocation failed");
+        return DPF_OOM;
+    }
+    int *d_err = (int *)buf;
+    unsigned long long *d_ns = (unsigned long long *)((char *)buf + 8);
+    int h_err = -1;
+    unsigned long long h_ns = 0;
+    cudaError_t e = cudaMemset(buf, 0, 16);
+    if (e == cudaSuccess) {
+        dpf::k_expired_wait<<<1, 32>>>(d_err, d_ns);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&h_ns, d_ns, sizeof(h_ns), cudaMemcpyDeviceToHost);
+    dpf::dev_free(buf);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        dpf::set_global_error(std::string("expired-wait probe: ") + cudaGetErrorString(e));
+        return DPF_CUDA;
+    }
+    if (waited_ms) *waited_ms = 1e-6 * (double)h_ns;
+    if (h_err != 1) {
+        dpf::set_global_error("the bounded wait did not report its expiry");
+        return DPF_STATE;
+    }
+    dpf::set_global_error("a bounded staging wait expired after " + std::to_string(1e-6 * (double)h_ns) + " ms");
+    return DPF_TIMEOUT;
+}

@@ -659,12 +659,21 @@ static void gck(cudaError_t e, const char *what) {
 template <typename T>
 T *GeneralSolver::dev(size_t n) {
     void *p = nullptr;
-    if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) {
+    if (dev_malloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) {
         cudaGetLastError();
         throw OomError("cudaMalloc of " + std::to_string(n * sizeof(T)) + " bytes failed");
     }
     owned.push_back(p);
     return (T *)p;
+}
+
+void GeneralSolver::drop(void *p) {
+    if (!p) return;
+    auto it = std::find(owned.begin(), owned.end(), p);
+    if (it != owned.end()) {
+        dev_free(p);
+        owned.erase(it);
+    }
 }
 
 void GeneralSolver::to_dev(void *dst, const void *src, size_t bytes) {
@@ -742,8 +751,9 @@ GeneralSolver::GeneralSolver(long long N_, long long F_, const int64_t *a, const
     rs.capacity = nblocks;
     GCK(cudaMemset(rs.tickets, 0, sizeof(unsigned)));
     dense_inv = dev<double>(kMaxCoarse * kMaxCoarse);
-    GCK(cudaMallocHost(&h_count, 4 * sizeof(int)));
-    GCK(cudaMallocHost(&h_state, sizeof(CgState)));
+    h_count = (int *)pinned.alloc(4 * sizeof(int));
+    h_state = (CgState *)pinned.alloc(sizeof(CgState));
+    if (!h_count || !h_state) throw OomError("pinned host allocation failed");
     // Chebyshev coefficients over [2 cheb_lo, 2] (Gershgorin bound 2 for these M-matrices)
     double lmax = 2.0, lmin = 2.0 * opt.cheb_lo;
     double theta = 0.5 * (lmax + lmin), delt = 0.5 * (lmax - lmin);
@@ -767,10 +777,7 @@ GeneralSolver::GeneralSolver(long long N_, long long F_, const int64_t *a, const
 }
 
 GeneralSolver::~GeneralSolver() {
-    cudaStreamSynchronize(stream);
-    for (void *p : owned) cudaFree(p);
-    if (h_count) cudaFreeHost(h_count);
-    if (h_state) cudaFreeHost(h_state);
+    cudaStreamSynchronize(stream);  // then `owned` and `pinned` free the buffers
 }
 
 // Host-side topology: the Dirichlet mask, the cell -> face incidence, the CSR of the
@@ -867,6 +874,7 @@ static int aggregate(int n, const std::vector<int> &rp, const std::vector<int> &
 }
 
 void GeneralSolver::build_hierarchy() {
+    NvtxRange range("build hierarchy (CSR)");
     std::vector<int> rp = hrp_, ci = hci_, dir = h_dir;
     int n = (int)N;
     while (n > opt.max_coarse) {
@@ -1151,6 +1159,7 @@ void GeneralSolver::df_pcg(const double *b, double *x, double tol2) {
 }
 
 void GeneralSolver::solve(const double *b, double *x) {
+    NvtxRange range("CG + AMG solve (CSR)");
     kg_state_init<<<1, 1, 0, stream>>>(d_state);
     GLAUNCH();
     const double tol2 = opt.reltol * opt.reltol;
@@ -1289,8 +1298,7 @@ int GeneralSolver::solve_grad_logk(const double *logK, int kind, const double *d
     }
     int rc2 = adjoint(delta, nullptr, dlogK, nullptr, nullptr);
     GCK(cudaStreamSynchronize(stream));
-    cudaFree(d_obs);
-    owned.pop_back();
+    drop(d_obs);
     return rc != DPF_OK ? rc : rc2;
 }
 
@@ -1398,11 +1406,7 @@ int GeneralSolver::transient_adjoint(long long nobs, const int64_t *obs, const d
     copy_out(ddh, adh, N, stream);
     copy_out(dQs, aQ, N, stream);
     GCK(cudaStreamSynchronize(stream));
-    for (void *p : {(void *)d_obs, (void *)d_w, (void *)d_gT, (void *)aK, (void *)adh, (void *)aQ}) {
-        if (!p) continue;
-        auto it = std::find(owned.begin(), owned.end(), p);
-        if (it != owned.end()) { cudaFree(p); owned.erase(it); }
-    }
+    for (void *p : {(void *)d_obs, (void *)d_w, (void *)d_gT, (void *)aK, (void *)adh, (void *)aQ}) drop(p);
     return worst;
 }
 

@@ -72,6 +72,7 @@ private:
     int read_active();
     template <typename T>
     T *dev(size_t n);
+    void drop(void *p);            // free an allocation made by dev() (nullptr: nothing)
     void to_dev(void *dst, const void *src, size_t bytes);
     void from_dev(void *dst, const void *src, size_t bytes);
     const double *stage(const double *src, size_t n, double *dst);
@@ -81,7 +82,8 @@ private:
     bool mixed = false;
     int nblocks = 0;                         // grid of every cell- or entry-parallel launch
     std::vector<GLevel> lv;
-    std::vector<void *> owned;
+    DevList owned;                 // every device allocation of the solver
+    HostList pinned;               // h_count, h_state
 
     // topology (device)
     int *fa = nullptr, *fb = nullptr;        // face ends

@@ -14,6 +14,7 @@
 // which avoids the cancellation of diag*x - sum c*x for smooth x.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 #include <string>
 #include <vector>
@@ -107,5 +108,50 @@ struct TailParams {
 
 constexpr int kTailThreads = 1024;
 
+// Every device and pinned-host allocation of the library goes through these calls: they keep
+// the process-wide counts that dpf_debug_alloc_stats reports and fail the allocation that
+// dpf_debug_fail_alloc selects (cudaErrorMemoryAllocation, nothing allocated). The frees
+// accept nullptr.
+cudaError_t dev_malloc(void **p, size_t bytes);
+cudaError_t host_malloc(void **p, size_t bytes);
+void dev_free(void *p);
+void host_free(void *p);
+
+// An NVTX range over a scope (entry points and solver phases) for profilers that record
+// NVTX; without one attached the push and pop return at once.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
+// The device (DevList) and pinned-host (HostList) allocations a solver object owns. As
+// members they free what they hold when the object is destroyed, and also when its
+// constructor throws part-way through (members already built are destroyed then; the
+// object's own destructor is not run).
+struct DevList : std::vector<void *> {
+    DevList() = default;
+    DevList(const DevList &) = delete;
+    DevList &operator=(const DevList &) = delete;
+    ~DevList() {
+        for (void *p : *this) dev_free(p);
+    }
+};
+struct HostList : std::vector<void *> {
+    HostList() = default;
+    HostList(const HostList &) = delete;
+    HostList &operator=(const HostList &) = delete;
+    // a pinned buffer of the given size that the list owns; nullptr on failure
+    void *alloc(size_t bytes) {
+        void *p = nullptr;
+        if (host_malloc(&p, bytes) != cudaSuccess) return nullptr;
+        push_back(p);
+        return p;
+    }
+    ~HostList() {
+        for (void *p : *this) host_free(p);
+    }
+};
 
 }  // namespace dpf

@@ -41,7 +41,8 @@ __host__ __device__ __forceinline__ int plane_rows(int ny, int nz, int cells) {
 
 // per-cell flags: inside the slab, and which of the z+/z-/y+/y- neighbours exist
 constexpr unsigned CF_VALID = 1u, CF_ZP = 2u, CF_ZM = 4u, CF_YP = 8u, CF_YM = 16u;
-constexpr uint32_t kWaitTries = 1u << 20;  // bounded mbarrier polling (well under a second)
+constexpr uint32_t kWaitTries = 1u << 20;         // bounded mbarrier polling ...
+constexpr uint64_t kWaitNs = 1000000000ull;       // ... and at most one second of it
 
 enum : int { PM_FIRST2 = 1, PM_FIRST = 2, PM_PROLONG = 4, PM_NOD = 8, PM_RZ = 16 };
 
@@ -71,10 +72,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// bounded wait for the phase with the given parity; false (and *err set) on expiry
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// bounded wait for the phase with the given parity (kWaitTries polls or kWaitNs, whichever
+// ends first); false (and *err set) on expiry
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
-    for (uint32_t k = 0; k < kWaitTries; k++)
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (uint32_t k = 0; k < kWaitTries; k++) {
         if (mbar_try_wait(bar, parity)) return true;
+        if ((k & 63) == 63 && global_ns() - t0 > kWaitNs) break;
+    }
     if (err) atomicExch(err, 1);
     return false;
 }

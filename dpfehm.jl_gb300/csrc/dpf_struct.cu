@@ -1110,11 +1110,11 @@ static void ck(cudaError_t e, const char *what) {
 #define LAUNCH_CHECK() ck(cudaGetLastError(), "kernel launch")
 
 template <typename T>
-static T *dalloc(size_t n, std::vector<void *> &owned) {
+static T *dalloc(size_t n, DevList &owned) {
     void *p = nullptr;
     if (n == 0) n = 1;
     // 64 bytes of padding: bulk copies widen their ranges to 16-byte boundaries
-    cudaError_t e = cudaMalloc(&p, n * sizeof(T) + 64);
+    cudaError_t e = dev_malloc(&p, n * sizeof(T) + 64);
     if (e != cudaSuccess) {
         cudaGetLastError();
         throw OomError(std::string("cudaMalloc of ") + std::to_string(n * sizeof(T)) + " bytes failed");
@@ -1137,7 +1137,7 @@ static void check_fast_div(unsigned d, unsigned m, int l, unsigned nmax) {
 // stride of (blocks of the problem) x kBlock, so a problem's block count is chosen to
 // fill the GPU once: about `target` blocks in total (SMs x resident blocks per SM),
 // split in proportion to the problems' cells, never more than one cell per thread.
-static BlockMap build_map(const std::vector<LevelDesc> &desc, const std::vector<int> &take, std::vector<void *> &own,
+static BlockMap build_map(const std::vector<LevelDesc> &desc, const std::vector<int> &take, DevList &own,
                          int nprob, long long target) {
     BlockMap m;
     long long total = 0;
@@ -1407,9 +1407,10 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         tail_first_level = nlev_max;
         for (auto &t : tails) tail_first_level = std::min(tail_first_level, t.y);
     }
-    CK(cudaMallocHost(&h_count, 4 * sizeof(int)));
-    CK(cudaMallocHost(&h_misc, 4 * sizeof(int)));
-    CK(cudaMallocHost(&h_state_buf, nprob * sizeof(CgState)));
+    h_count = (int *)pinned.alloc(4 * sizeof(int));
+    h_misc = (int *)pinned.alloc(4 * sizeof(int));
+    h_state_buf = pinned.alloc(nprob * sizeof(CgState));
+    if (!h_count || !h_misc || !h_state_buf) throw OomError("pinned host allocation failed");
     // Chebyshev coefficients on D^-1 A over [lo*2, 2] (Gershgorin: the spectrum of
     // D^-1 A of a weakly diagonally dominant symmetric M-matrix lies in [0, 2]).
     double lmax = 2.0, lmin = 2.0 * opt.cheb_lo;
@@ -1489,10 +1490,7 @@ StructBatch::~StructBatch() {
         cudaGraphDestroy(kv.second.graph);
     }
     if (cap_stream) cudaStreamDestroy(cap_stream);
-    for (void *p : owned) cudaFree(p);
-    if (h_count) cudaFreeHost(h_count);
-    if (h_misc) cudaFreeHost(h_misc);
-    if (h_state_buf) cudaFreeHost(h_state_buf);
+    cudaStreamSynchronize(stream);  // then `owned` and `pinned` free the buffers
 }
 
 static inline unsigned nb_of(const BlockMap &m) { return (unsigned)m.nblocks; }
@@ -1510,6 +1508,7 @@ Coeffs<float> coeffs_of<float>(StructBatch::Level &L, bool) {
 }
 
 void StructBatch::assemble(const double *Ks, const double *kc, int kind, const double *shift, bool init_x) {
+    NvtxRange range("assemble operator and hierarchy");
     Level &L0 = lv[0];
     FaceK fk{Ks, kc, kind};
     if (nb_of(L0.all))
@@ -2174,6 +2173,7 @@ void StructBatch::df_pcg(const double *b64, double *x64, double tol2) {
 
 // ---- full solve of A x = b for every problem (x holds the initial guess)
 void StructBatch::solve(const double *b, double *x, double reltol) {
+    NvtxRange range("CG + AMG solve");
     const double tol2 = reltol * reltol;
     struct ZeroGuessReset {
         bool &f;
@@ -2184,6 +2184,7 @@ void StructBatch::solve(const double *b, double *x, double reltol) {
         k_state_init<<<(nprob + 127) / 128, 128, 0, stream>>>(d_state, nprob);
     }
     LAUNCH_CHECK();
+    CK(cudaMemsetAsync(d_factor_status + 1, 0, sizeof(int), stream));  // expired-wait word of this solve
     graph_body_kernels = 0;
     if (!mixed) {
         pcg<double>(b, x, tol2);
@@ -2215,7 +2216,7 @@ void StructBatch::solve(const double *b, double *x, double reltol) {
         last_message = "coarsest operator is not positive definite (does every problem have a Dirichlet cell?)";
     }
     if (h_misc[1]) {
-        last_status = DPF_CUDA;
+        last_status = DPF_TIMEOUT;
         last_message = "a shared-memory staging wait of a smoother kernel expired";
     }
 }
@@ -2237,6 +2238,7 @@ void StructBatch::forward(const double *Ks, const double *logK, int kind) {
 }
 
 void StructBatch::adjoint_solve() {
+    NvtxRange range("adjoint solve");
     Level &L0 = lv[0];
     {
         KTimer _kt(this, kname("k_adjoint_rhs", 0, false), L0.all_cells);
@@ -2268,6 +2270,7 @@ void StructBatch::obs_delta(const long long *d_obs, long long nobs) {
 }
 
 void StructBatch::grad_faces(const double *hv, const double *lv_, double *dKs, bool accumulate) {
+    NvtxRange range("face gradient");
     Level &L0 = lv[0];
     {
         KTimer _kt(this, kname("k_grad_faces", 0, false), L0.all_cells);

@@ -205,7 +205,8 @@ public:
     void profile(bool on);
     int profile_report(int cap, const char **names, long long *counts, double *ms, long long *cells);
 
-    std::vector<void *> owned;
+    DevList owned;                   // every device allocation of the batch
+    HostList pinned;                 // h_count, h_misc, h_state_buf
 };
 
 }  // namespace dpf

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "dpfehm_gpu.h"
+#include "dpf_internal.h"
 
 namespace {
 
@@ -23,7 +24,7 @@ struct DevCopy {
     const double *ptr = nullptr;
     double *owned = nullptr;
     ~DevCopy() {
-        if (owned) cudaFree(owned);
+        dpf::dev_free(owned);
     }
 };
 
@@ -41,7 +42,7 @@ int to_device(const double *src, size_t n, DevCopy &out) {
         out.ptr = src;
         return DPF_OK;
     }
-    if (cudaMalloc(&out.owned, n * sizeof(double)) != cudaSuccess) return DPF_OOM;
+    if (dpf::dev_malloc((void **)&out.owned, n * sizeof(double)) != cudaSuccess) return DPF_OOM;
     if (cudaMemcpy(out.owned, src, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) return DPF_CUDA;
     out.ptr = out.owned;
     return DPF_OK;
@@ -68,8 +69,9 @@ extern "C" int dpf_batch_autotune(int nprob, const int *dims, const double *mins
     int rc;
     if ((rc = to_device(logK, N, dlk)) || (rc = to_device(dh, N, ddh)) || (rc = to_device(Qs, N, dq))) return rc;
     double *hout = nullptr, *gout = nullptr;
-    if (cudaMalloc(&hout, N * sizeof(double)) != cudaSuccess || cudaMalloc(&gout, N * sizeof(double)) != cudaSuccess) {
-        cudaFree(hout);
+    if (dpf::dev_malloc((void **)&hout, N * sizeof(double)) != cudaSuccess ||
+        dpf::dev_malloc((void **)&gout, N * sizeof(double)) != cudaSuccess) {
+        dpf::dev_free(hout);
         return DPF_OOM;
     }
     cudaEvent_t e0, e1;
@@ -132,8 +134,8 @@ extern "C" int dpf_batch_autotune(int nprob, const int *dims, const double *mins
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    cudaFree(hout);
-    cudaFree(gout);
+    dpf::dev_free(hout);
+    dpf::dev_free(gout);
     *best = cur;
     if (best_ms) *best_ms = cur_ms;
     return rc;

@@ -53,7 +53,8 @@ typedef enum {
     DPF_CUDA = 5,           /* a CUDA runtime call failed */
     DPF_NO_DEVICE = 6,      /* no CUDA device */
     DPF_STATE = 7,          /* call out of order (e.g. adjoint before forward) */
-    DPF_UNSUPPORTED = 8     /* option not available for this problem kind */
+    DPF_UNSUPPORTED = 8,    /* option not available for this problem kind */
+    DPF_TIMEOUT = 9         /* a bounded device-side wait expired; the handle stays usable */
 } dpf_status;
 
 typedef enum { DPF_MEAN_GEOMETRIC = 0, DPF_MEAN_HARMONIC = 1 } dpf_mean_kind;
@@ -243,6 +244,24 @@ long long dpf_launch_count(const dpf_problem *h);
  * legacy default stream and returns when Ks is complete; errors are described by
  * dpf_last_error(NULL). */
 int dpf_logk_to_faces_regular_noalloc(int nx, int ny, int nz, const double *logK, int mean_kind, double *Ks);
+
+/* ------------------------------------------------------------ test hooks */
+
+/* No counterpart in the reference. Every device and pinned-host allocation of the
+ * library is counted; dpf_debug_fail_alloc(k) makes the k-th following one fail
+ * as if the device were out of memory (k = 0: the next one; k < 0: none), once,
+ * so that a test can walk each allocation's error path on a healthy device.
+ * dpf_debug_alloc_stats reports the allocations made since the library was
+ * loaded and those still live (either pointer may be NULL). Process-wide. */
+void dpf_debug_fail_alloc(int64_t k);
+void dpf_debug_alloc_stats(int64_t *made, int64_t *live);
+
+/* No counterpart in the reference. Runs one block whose threads wait on a
+ * shared-memory barrier that nothing arrives on, through the bounded wait every
+ * staging kernel uses (at most 2^20 polls or one second). Returns DPF_TIMEOUT when
+ * the bound ended the wait as designed, with the milliseconds it took in
+ * *waited_ms (may be NULL); any other status is a defect. The device stays usable. */
+int dpf_debug_expired_wait(double *waited_ms);
 
 #ifdef __cplusplus
 }
