@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "dpf_check.cuh"
 #include "dpf_general.h"
 #include "dpf_struct.h"
 
@@ -80,6 +81,42 @@ void host_free(void *p) {
     g_live--;
 }
 }  // namespace dpf
+
+namespace dpf {
+static std::vector<CheckReader> &check_readers() {
+    static std::vector<CheckReader> r;
+    return r;
+}
+void register_check_reader(CheckReader f) { check_readers().push_back(f); }
+}  // namespace dpf
+
+extern "C" int dpf_debug_check_report(int64_t *violations, int64_t *first) {
+#if DPF_CHECKED
+    long long total = 0, f0[3] = {0, 0, 0};
+    bool have = false;
+    for (dpf::CheckReader rd : dpf::check_readers()) {
+        long long c = 0, f[3] = {0, 0, 0};
+        if (rd(&c, f) != 0) {
+            dpf::set_global_error("reading the check words failed");
+            return DPF_CUDA;
+        }
+        if (c > 0 && !have) {
+            have = true;
+            for (int k = 0; k < 3; k++) f0[k] = f[k];
+        }
+        total += c;
+    }
+    if (violations) *violations = total;
+    if (first)
+        for (int k = 0; k < 3; k++) first[k] = f0[k];
+    return DPF_OK;
+#else
+    (void)violations;
+    (void)first;
+    dpf::set_global_error("the library was built without DPF_CHECK");
+    return DPF_UNSUPPORTED;
+#endif
+}
 
 extern "C" void dpf_debug_fail_alloc(int64_t k) { dpf::g_fail_in.store(k < 0 ? -1 : (long long)k); }
 

@@ -20,26 +20,28 @@ namespace dpf {
 #define GSTRIDE(i, n) for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
 
 // ------------------------------------------------------------ operator
+template <typename T>
+struct GOp {
+    const int *rp, *ci;
+    const T *v, *leak, *idg;
+    int n;                         // rows (= columns)
+};
+
 // flux form y_i = leak_i x_i + sum_e c_e (x_i - x_j); also returns the diagonal
 template <typename T, typename XAt>
-__device__ __forceinline__ T g_apply(int i, const int *__restrict__ rp, const int *__restrict__ ci,
-                                     const T *__restrict__ v, const T *__restrict__ leak, T xi, XAt xat, T &diag) {
-    T lk = leak[i];
+__device__ __forceinline__ T g_apply(int i, const GOp<T> &A, T xi, XAt xat, T &diag) {
+    T lk = A.leak[i];
     T a = lk * xi, d = lk;
-    for (int e = rp[i]; e < rp[i + 1]; e++) {
-        T w = v[e];
-        a += w * (xi - xat(ci[e]));
+    for (int e = A.rp[i]; e < A.rp[i + 1]; e++) {
+        const int j = A.ci[e];
+        if (!DPF_INSIDE(CK_CSR_COL, j, 0, A.n)) continue;
+        T w = A.v[e];
+        a += w * (xi - xat(j));
         d += w;
     }
     diag = d;
     return a;
 }
-
-template <typename T>
-struct GOp {
-    const int *rp, *ci;
-    const T *v, *leak, *idg;
-};
 
 __device__ __forceinline__ int other_end(const int *fa, const int *fb, int f, int i) {
     return fa[f] == i ? fb[f] : fa[f];
@@ -217,7 +219,7 @@ __global__ void kg_cheb_first2(int n, const CgState *st, GOp<T> A, const T *__re
         const T bi = b[i], gi = A.idg[i];
         const T x1 = invtheta * bi * gi;
         T dg;
-        T Ax = g_apply<T>(i, A.rp, A.ci, A.v, A.leak, x1, [&](int j) { return invtheta * b[j] * A.idg[j]; }, dg);
+        T Ax = g_apply<T>(i, A, x1, [&](int j) { return invtheta * b[j] * A.idg[j]; }, dg);
         const T dn = c1 * x1 + c2 * (bi - Ax) * gi;
         d[i] = dn;
         xout[i] = x1 + dn;
@@ -242,7 +244,7 @@ __global__ void kg_cheb_step(int n, CgState *st, GOp<T> A, const T *__restrict__
     Acc<T> part;
     GSTRIDE(i, n) {
         T xi = xin[i], dg;
-        T Ax = g_apply<T>(i, A.rp, A.ci, A.v, A.leak, xi, [&](int j) { return xin[j]; }, dg);
+        T Ax = g_apply<T>(i, A, xi, [&](int j) { return xin[j]; }, dg);
         T bi = b[i];
         T r = g_dinv(A, i, bi - Ax, dg);
         T dn = FIRST ? c2 * r : c1 * d[i] + c2 * r;
@@ -273,7 +275,7 @@ __global__ void kg_restrict(int nc, const CgState *st, GOp<T> A, const int *__re
         for (int k = mrp[I]; k < mrp[I + 1]; k++) {
             int i = mci[k];
             T dg;
-            acc += b[i] - g_apply<T>(i, A.rp, A.ci, A.v, A.leak, x[i], [&](int j) { return x[j]; }, dg);
+            acc += b[i] - g_apply<T>(i, A, x[i], [&](int j) { return x[j]; }, dg);
         }
         bc[I] = acc;
     }
@@ -326,7 +328,7 @@ __global__ void kg_cg_start(int n, CgState *st, int *active_count, ReduceScratch
     Acc<double> rr, bb;
     GSTRIDE(i, n) {
         double dg;
-        double ri = b[i] - g_apply<double>(i, A.rp, A.ci, A.v, A.leak, x[i], [&](int j) { return x[j]; }, dg);
+        double ri = b[i] - g_apply<double>(i, A, x[i], [&](int j) { return x[j]; }, dg);
         r[i] = ri;
         rr.v += ri * ri;
         bb.v += b[i] * b[i];
@@ -354,7 +356,7 @@ __global__ void kg_spmv_pq(int n, CgState *st, int *active_count, ReduceScratch 
     Acc<double> part;
     GSTRIDE(i, n) {
         double dg;
-        double a = g_apply<double>(i, A.rp, A.ci, A.v, A.leak, pv[i], [&](int j) { return pv[j]; }, dg);
+        double a = g_apply<double>(i, A, pv[i], [&](int j) { return pv[j]; }, dg);
         q[i] = a;
         part.v += pv[i] * a;
     }
@@ -407,7 +409,10 @@ __global__ void kg_df_spmv_pq(int n, CgState *st, int *active_count, ReduceScrat
     GSTRIDE(i, n) {
         const float2 pi = pv[i];
         float2 a = df_mul(leak[i], pi);
-        for (int e = rp[i]; e < rp[i + 1]; e++) a = df_add(a, df_mul(v[e], df_sub(pi, pv[ci[e]])));
+        for (int e = rp[i]; e < rp[i + 1]; e++) {
+            if (!DPF_INSIDE(CK_CSR_COL, ci[e], 0, n)) continue;
+            a = df_add(a, df_mul(v[e], df_sub(pi, pv[ci[e]])));
+        }
         q[i] = a;
         part = part + Acc<float>::prod(pi.x, a.x);
     }
@@ -469,7 +474,7 @@ __global__ void kg_df_residual(int n, CgState *st, int *active_count, ReduceScra
     GSTRIDE(i, n) {
         double dg;
         const double xi = x[i];
-        double ri = b[i] - g_apply<double>(i, A.rp, A.ci, A.v, A.leak, xi, [&](int j) { return x[j]; }, dg);
+        double ri = b[i] - g_apply<double>(i, A, xi, [&](int j) { return x[j]; }, dg);
         r[i] = ri;
         rr.v += ri * ri;
         if (FIRST) {
@@ -537,7 +542,7 @@ __global__ void kg_state_init(CgState *st) {
 __global__ void kg_apply(int n, GOp<double> A, const double *__restrict__ x, double *__restrict__ y) {
     GSTRIDE(i, n) {
         double dg;
-        y[i] = g_apply<double>(i, A.rp, A.ci, A.v, A.leak, x[i], [&](int j) { return x[j]; }, dg);
+        y[i] = g_apply<double>(i, A, x[i], [&](int j) { return x[j]; }, dg);
     }
 }
 
@@ -1004,9 +1009,9 @@ void GeneralSolver::assemble(const double *Ks, const double *kc, int kind, const
 template <typename T>
 static GOp<T> gop(GLevel &L);
 template <>
-GOp<double> gop<double>(GLevel &L) { return GOp<double>{L.rp, L.ci, L.v64, L.leak64, L.idg64}; }
+GOp<double> gop<double>(GLevel &L) { return GOp<double>{L.rp, L.ci, L.v64, L.leak64, L.idg64, (int)L.n}; }
 template <>
-GOp<float> gop<float>(GLevel &L) { return GOp<float>{L.rp, L.ci, L.v32, L.leak32, L.idg32}; }
+GOp<float> gop<float>(GLevel &L) { return GOp<float>{L.rp, L.ci, L.v32, L.leak32, L.idg32, (int)L.n}; }
 
 // V-cycle: z = M r on the finest level
 template <typename T>

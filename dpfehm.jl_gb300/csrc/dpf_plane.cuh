@@ -16,6 +16,7 @@
 #pragma once
 #include <cstdint>
 
+#include "dpf_check.cuh"
 #include "dpf_struct_kernels.cuh"
 
 namespace dpf {
@@ -146,6 +147,31 @@ __device__ __forceinline__ BulkRange make_range(const void *base, int es, long l
     return r;
 }
 
+// Announces (expect_tx) and issues the bulk copy of elements [a0, a1) of `base` into the
+// stage region `region` (see make_range). In a checked build the range must lie in the array
+// section [lo, hi), the copy inside its slot [slot, slot + slot_bytes) and on 16-byte
+// boundaries; a violation is recorded and the copy is not issued (the phase then completes
+// without it).
+__device__ __forceinline__ void stage_range(uint64_t *bar, const void *base, int es, long long l0, long long a0,
+                                            long long a1, char *region, long long lo, long long hi, const char *slot,
+                                            int slot_bytes) {
+    const BulkRange r = make_range(base, es, l0, a0, a1, region);
+#if DPF_CHECKED
+    if (a1 > a0 && !(DPF_INSIDE(CK_STAGE_SRC, a0, lo, hi) && DPF_INSIDE(CK_STAGE_SRC, a1 - 1, lo, hi))) return;
+    if (!DPF_INSIDE(CK_STAGE_DST, r.dst - slot, 0, slot_bytes) ||
+        !DPF_INSIDE(CK_STAGE_DST, r.dst + r.bytes - slot, 0, slot_bytes + 1))
+        return;
+    if (!DPF_INSIDE(CK_STAGE_ALIGN, (long long)(((uintptr_t)r.src | smem_addr(r.dst) | r.bytes) & 15u), 0, 1)) return;
+#else
+    (void)lo;
+    (void)hi;
+    (void)slot;
+    (void)slot_bytes;
+#endif
+    mbar_expect_tx(bar, r.bytes);
+    bulk_copy_g2s(r.dst, r.src, r.bytes, bar);
+}
+
 // Fast division of k (< 2^31) by nz with the level's invariant-integer constants.
 __device__ __forceinline__ int div_nz(const LevelDesc &L, int k) { return (int)fast_div((unsigned)k, L.mag_nz, L.sh_nz); }
 
@@ -238,9 +264,7 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
                 const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
                 const long long hA = pb + (long long)h0 * nz, hB = pb + (long long)h1 * nz, pE = lp + ncell;
                 auto stage = [&](const void *base, int esz, long long l0, long long a0, long long a1, int off) {
-                    const BulkRange r = make_range(base, esz, l0, a0, a1, slot + off);
-                    mbar_expect_tx(bar, r.bytes);
-                    bulk_copy_g2s(r.dst, r.src, r.bytes, bar);
+                    stage_range(bar, base, esz, l0, a0, a1, slot + off, L.off, L.off + L.n, slot, lay.slot_bytes);
                 };
                 if (F2) {
                     stage(b, es, lh, hA, hB, lay.oB);
@@ -258,8 +282,9 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
                     stage(dir, 1, lh, hA, hB, lay.oDIR);
                     const long long cb = Lc.off + (long long)(q >> 1) * csx;
                     const int c0 = max(cr_lo, 0), c1r = min((y0 + rows) >> 1, Lc.ny - 1) + 1;
-                    stage(e, es, cb + (long long)cr_lo * Lc.nz, cb + (long long)c0 * Lc.nz,
-                          cb + (long long)c1r * Lc.nz, lay.oE);
+                    stage_range(bar, e, es, cb + (long long)cr_lo * Lc.nz, cb + (long long)c0 * Lc.nz,
+                                cb + (long long)c1r * Lc.nz, slot + lay.oE, Lc.off, Lc.off + Lc.n, slot,
+                                lay.slot_bytes);
                 }
             });
         }
@@ -481,9 +506,7 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
                 const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
                 const long long hA = pb + (long long)h0 * nz, hB = pb + (long long)h1 * nz, pE = lp + ncell;
                 auto stage = [&](const void *base, long long l0, long long a0, long long a1, int off) {
-                    const BulkRange r = make_range(base, es, l0, a0, a1, slot + off);
-                    mbar_expect_tx(bar, r.bytes);
-                    bulk_copy_g2s(r.dst, r.src, r.bytes, bar);
+                    stage_range(bar, base, es, l0, a0, a1, slot + off, L.off, L.off + L.n, slot, lay.slot_bytes);
                 };
                 stage(xin, lh, hA, hB, lay.oX);
                 stage(b, lp, lp, pE, lay.oB);
@@ -633,9 +656,7 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_df_spmv(
                 const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
                 const long long hA = pb + (long long)h0 * nz, hB = pb + (long long)h1 * nz, pE = lp + ncell;
                 auto stage = [&](const void *base, long long l0, long long a0, long long a1, int off) {
-                    const BulkRange r = make_range(base, es, l0, a0, a1, slot + off);
-                    mbar_expect_tx(bar, r.bytes);
-                    bulk_copy_g2s(r.dst, r.src, r.bytes, bar);
+                    stage_range(bar, base, es, l0, a0, a1, slot + off, L.off, L.off + L.n, slot, lay.slot_bytes);
                 };
                 stage(pv, lh, hA, hB, lay.oX);
                 stage(C.cx, lp, lp, pE, lay.oCX);

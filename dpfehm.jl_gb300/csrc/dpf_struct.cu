@@ -370,7 +370,7 @@ __global__ void k_prolong_add(const LevelDesc *__restrict__ desc, const LevelDes
         Cell c;
         cell_at(L, li_, c);
         if (dir[c.i]) continue;
-        x[c.i] += scale * e[Lc.off + ((long long)(c.ix >> 1) * Lc.ny + (c.iy >> 1)) * Lc.nz + (c.iz >> 1)];
+        x[c.i] += scale * e[agg_index(Lc, c)];
     }
 }
 
@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(kTailThreads) k_tail_cycle(const TailLevel<T> 
             cell_at(L, li, c);
             if (V.dir[c.i]) continue;
             cur[c.i] += tp.coarse_scale *
-                        ldv<CLUSTER>(W.xb, Lc.off + ((long long)(c.ix >> 1) * Lc.ny + (c.iy >> 1)) * Lc.nz + (c.iz >> 1));
+                        ldv<CLUSTER>(W.xb, agg_index(Lc, c));
         }
         sync();
         for (int k = 0; k < deg; k++) {

@@ -6,6 +6,7 @@
 // warp shuffles, and a deterministic "last block finalises" reduction that puts
 // CG scalars on the device (no host round trip per reduction).
 #pragma once
+#include "dpf_check.cuh"
 #include "dpf_internal.h"
 
 namespace dpf {
@@ -27,6 +28,24 @@ __device__ __forceinline__ void cell_at(const LevelDesc &L, int li, Cell &c) {
     c.iy = (int)(q - x * (unsigned)L.ny);
     c.ix = (int)x;
     c.i = L.off + li;
+#if DPF_CHECKED
+    if (!DPF_INSIDE(CK_CELL, li, 0, L.n) || !DPF_INSIDE(CK_CELL, c.ix, 0, L.nx) || !DPF_INSIDE(CK_CELL, c.iy, 0, L.ny) ||
+        !DPF_INSIDE(CK_CELL, ((long long)c.ix * L.ny + c.iy) * L.nz + c.iz, li, (long long)li + 1)) {
+        c.ix = c.iy = c.iz = 0;  // the problem's first cell: no access outside it
+        c.i = L.off;
+    }
+#endif
+}
+
+// Index in the coarse level arrays of the 2x2x2 aggregate that holds fine cell c.
+__device__ __forceinline__ long long agg_index(const LevelDesc &Lc, const Cell &c) {
+    const int ax = c.ix >> 1, ay = c.iy >> 1, az = c.iz >> 1;
+#if DPF_CHECKED
+    if (!DPF_INSIDE(CK_AGGREGATE, ax, 0, Lc.nx) || !DPF_INSIDE(CK_AGGREGATE, ay, 0, Lc.ny) ||
+        !DPF_INSIDE(CK_AGGREGATE, az, 0, Lc.nz))
+        return Lc.off;
+#endif
+    return Lc.off + ((long long)ax * Lc.ny + ay) * Lc.nz + az;
 }
 
 // Face index of the reference face list (regulargrid3d, src/grid.jl:163-185) of the
@@ -196,6 +215,19 @@ __device__ __forceinline__ void apply7(const LevelDesc &L, const Cell &c, const 
     const long long sy = L.nz, sx = (long long)L.ny * L.nz;
     T lk = C.leak[i];
     T a = lk * xi, d = lk;
+#if DPF_CHECKED
+    // every neighbour the flags below admit lies inside the problem's cells
+    if (!(DPF_INSIDE(CK_NEIGHBOUR, c.iz + 1 < L.nz ? i + 1 : i, L.off, L.off + L.n) &&
+          DPF_INSIDE(CK_NEIGHBOUR, c.iz > 0 ? i - 1 : i, L.off, L.off + L.n) &&
+          DPF_INSIDE(CK_NEIGHBOUR, c.iy + 1 < L.ny ? i + sy : i, L.off, L.off + L.n) &&
+          DPF_INSIDE(CK_NEIGHBOUR, c.iy > 0 ? i - sy : i, L.off, L.off + L.n) &&
+          DPF_INSIDE(CK_NEIGHBOUR, c.ix + 1 < L.nx ? i + sx : i, L.off, L.off + L.n) &&
+          DPF_INSIDE(CK_NEIGHBOUR, c.ix > 0 ? i - sx : i, L.off, L.off + L.n))) {
+        Ax = a;
+        diag = d;
+        return;
+    }
+#endif
     if (c.iz + 1 < L.nz) { T w = C.cz[i];      a += w * (xi - xat(i + 1, c.ix, c.iy, c.iz + 1));   d += w; }
     if (c.iz > 0)        { T w = C.cz[i - 1];  a += w * (xi - xat(i - 1, c.ix, c.iy, c.iz - 1));   d += w; }
     if (c.iy + 1 < L.ny) { T w = C.cy[i];      a += w * (xi - xat(i + sy, c.ix, c.iy + 1, c.iz));  d += w; }

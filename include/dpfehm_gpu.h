@@ -263,6 +263,14 @@ void dpf_debug_alloc_stats(int64_t *made, int64_t *live);
  * *waited_ms (may be NULL); any other status is a defect. The device stays usable. */
 int dpf_debug_expired_wait(double *waited_ms);
 
+/* No counterpart in the reference. In a library built with DPF_CHECK defined
+ * (device-side bounds and alignment checks on cell decodes, stencil neighbours,
+ * aggregates, staged copies and CSR columns; a violating access is clamped or
+ * skipped, never trapped): the violations recorded since the last call, which are
+ * then cleared, and the first one's {site code, index, bound} in first[3] (either
+ * pointer may be NULL). Returns DPF_UNSUPPORTED in a library built without them. */
+int dpf_debug_check_report(int64_t *violations, int64_t *first);
+
 #ifdef __cplusplus
 }
 #endif

@@ -104,9 +104,8 @@ def test_general_path_allocation_failure(gpu_lib, lib):
     of the first forward solve."""
     pkg = gpu_lib
     _, nb, aol, _ = pkg.regulargrid3d((0.0, 0.0, 0.0), (9.0, 7.0, 3.0), (10, 8, 4))
-    keep = np.ones(len(nb), bool)
-    keep[::7] = False                            # drop faces: no longer a regular grid
-    nb, aol = nb[keep], aol[keep]
+    nb = np.concatenate([nb, nb[::5]])           # duplicated faces: no longer a regular grid
+    aol = np.concatenate([aol, 0.5 * aol[::5]])
     N = 320
     dn = [N - 1]
     Ks = np.exp(np.random.default_rng(5).normal(-9, 0.5, len(nb)))
