@@ -39,14 +39,21 @@ METRIC = "forward+adjoint solves/sec at 1M cells vs plain FP64 GPU, at 1e-8 rel 
 
 # algorithmic bytes per cell of each kernel (vector/coefficient element size T):
 # reads and writes of every array the kernel touches once per cell
+def _coef(T):
+    """Bytes of one stored operator coefficient: FP64 levels keep FP64, the FP32 V-cycle bf16."""
+    return 2 if T == 4 else 8
+
+
 BYTES_PER_CELL = {
-    "k_cheb_step": lambda T: 9 * T,            # xin, b, d, cx, cy, cz, leak in; xout, d out
-    "k_cheb_step0": lambda T: 8 * T,           # first step after prolongation: d is not read
-    "k_prolong_add": lambda T: 2 * T + T / 8 + 1,   # x, e/8, dir in; x out
-    "k_cheb_first": lambda T: 7 * T,           # b, cx, cy, cz, leak in; x, d out
-    "k_cheb_first2": lambda T: 8 * T,          # b, idg, cx, cy, cz, leak in; xout, d out
-    "k_restrict": lambda T: 49 * T,            # per coarse cell: 8 fine cells x (x, b, 4 coeffs) + bc out
-    "k_spmv_pq": lambda T: 6 * T,              # p, 4 coeffs in; q out
+    "k_cheb_step": lambda T: 5 * T + 4 * _coef(T),    # xin, b, d, cx, cy, cz, leak in; xout, d out
+    "k_cheb_step0": lambda T: 4 * T + 4 * _coef(T),   # first step after prolongation: d is not read
+    "k_prolong_add": lambda T: 2 * T + T / 8 + 1,     # x, e/8, dir in; x out
+    "k_cheb_first": lambda T: 3 * T + 4 * _coef(T),   # b, cx, cy, cz, leak in; x, d out
+    "k_cheb_first2": lambda T: 4 * T + 4 * _coef(T),  # b, idg, cx, cy, cz, leak in; xout, d out
+    # per coarse cell: 8 fine cells x (x, b, 4 coeffs) + bc out
+    "k_restrict": lambda T: 17 * T + 32 * _coef(T),
+    "k_pm_restrict": lambda T: 17 * T + 32 * _coef(T),
+    "k_spmv_pq": lambda T: 6 * T,              # p, 4 coeffs in; q out (FP64 CG)
     "k_update_xr": lambda T: 6 * T,            # x, p, r, q in; x, r out
     "k_update_p": lambda T: 3 * T,             # z, p in; p out
     "k_cg_start": lambda T: 7 * T,             # x, b, 4 coeffs in; r out
@@ -57,9 +64,9 @@ BYTES_PER_CELL = {
     "k_df_begin": lambda T: 20,                # r64 in; r (2 floats), r32 out
     "k_grad_logk": lambda T: 32,               # logK, h, lambda in; g out
     # plane-marching smoothers (Chebyshev degree 2): each value is read from HBM once
-    "k_pm_first2": lambda T: 7 * T,            # b, idg, cx, cy, cz, leak in; x out (no direction)
-    "k_pm_step": lambda T: 8 * T,              # x, b, d, cx, cy, cz, leak in; x out (last step)
-    "k_pm_prolong_step": lambda T: 8 * T + T / 8 + 1,  # x, e/8, dir, b, 4 coeffs in; x, d out
+    "k_pm_first2": lambda T: 3 * T + 4 * _coef(T),   # b, idg, cx, cy, cz, leak in; x out (no direction)
+    "k_pm_step": lambda T: 4 * T + 4 * _coef(T),     # x, b, d, cx, cy, cz, leak in; x out (last step)
+    "k_pm_prolong_step": lambda T: 4 * T + T / 8 + 1 + 4 * _coef(T),  # x, e/8, dir, b, 4 coeffs in; x, d out
     "k_df_residual0": lambda T: 17,            # b, dir in; r out
 }
 

@@ -13,6 +13,7 @@
 // The operator is applied in flux form, y_i = leak_i x_i + sum_f c_f (x_i - x_j),
 // which avoids the cancellation of diag*x - sum c*x for smooth x.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
@@ -84,10 +85,26 @@ struct ProbParam {                 // per-problem constants of a regular grid
     long long F;                   // faces of the problem
 };
 
+// Storage type of the operator coefficients of a level whose vectors are T. FP64 levels
+// keep FP64. The FP32 V-cycle (a preconditioner: CG's own operator products are FP64 or
+// double-float) reads bf16 coefficients, 8 significant bits with FP32's exponent range,
+// which halves its coefficient traffic; its diagonals are formed from the same rounded
+// values, so every smoother step and the Galerkin levels see one consistent operator.
+template <typename T>
+struct CoefStore {
+    using type = T;
+};
+template <>
+struct CoefStore<float> {
+    using type = __nv_bfloat16;
+};
+template <typename T>
+using coef_t = typename CoefStore<T>::type;
+
 template <typename T>
 struct Coeffs {
-    const T *cx, *cy, *cz, *leak;
-    const T *idg;                  // inverse diagonal (FP64 levels), or null: computed on the fly
+    const coef_t<T> *cx, *cy, *cz, *leak;
+    const T *idg;                  // inverse diagonal
 };
 
 // Per-level pointers and the Chebyshev parameters of the fused small-level tail kernel.

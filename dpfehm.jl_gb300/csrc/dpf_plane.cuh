@@ -222,6 +222,8 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
                    PROL = (MODE & PM_PROLONG) != 0, NOD = (MODE & PM_NOD) != 0, RZ = (MODE & PM_RZ) != 0;
     constexpr int R = kPlaneStages;
     constexpr int es = (int)sizeof(T);
+    using CT = coef_t<T>;
+    constexpr int ec = (int)sizeof(CT);  // coefficient streams
     constexpr int kConsumerWarps = kPlaneThreads / 32;
     extern __shared__ __align__(128) unsigned char sm[];
     __shared__ uint64_t full[R], empty[R], ready[R];
@@ -274,10 +276,10 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
                     stage(b, es, lp, lp, pE, lay.oB);
                     if (!FIRST) stage(d, es, lp, lp, pE, lay.oD);
                 }
-                stage(C.cx, es, lp, lp, pE, lay.oCX);
-                stage(C.cy, es, lh, hA, pE, lay.oCY);
-                stage(C.cz, es, lp, lp, pE, lay.oCZ);
-                stage(C.leak, es, lp, lp, pE, lay.oLK);
+                stage(C.cx, ec, lp, lp, pE, lay.oCX);
+                stage(C.cy, ec, lh, hA, pE, lay.oCY);
+                stage(C.cz, ec, lp, lp, pE, lay.oCZ);
+                stage(C.leak, ec, lp, lp, pE, lay.oLK);
                 if (PROL) {
                     stage(dir, 1, lh, hA, hB, lay.oDIR);
                     const long long cb = Lc.off + (long long)(q >> 1) * csx;
@@ -358,12 +360,13 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
                 char *sq = xm ? slot_of(x - 1) : sc;
                 const int dn_ = xp ? stage_delta(lh + sx, es) : dh;
                 const int dq = xm ? stage_delta(lh - sx, es) : dh;
-                const int dqp = xm ? stage_delta(lp - sx, es) : dp;
-                const T *CX = (const T *)(sc + lay.oCX) + dp;
-                const T *CXq = (const T *)(sq + lay.oCX) + dqp;
-                const T *CY = (const T *)(sc + lay.oCY) + dh;  // logical row 0 = y0 - 1
-                const T *CZ = (const T *)(sc + lay.oCZ) + dp;
-                const T *LK = (const T *)(sc + lay.oLK) + dp;
+                const int ch = stage_delta(lh, ec), cp = stage_delta(lp, ec);
+                const int cqp = xm ? stage_delta(lp - sx, ec) : cp;
+                const CT *CX = (const CT *)(sc + lay.oCX) + cp;
+                const CT *CXq = (const CT *)(sq + lay.oCX) + cqp;
+                const CT *CY = (const CT *)(sc + lay.oCY) + ch;  // logical row 0 = y0 - 1
+                const CT *CZ = (const CT *)(sc + lay.oCZ) + cp;
+                const CT *LK = (const CT *)(sc + lay.oLK) + cp;
 #pragma unroll
                 for (int k = 0; k < CPT; k++) {
                     const unsigned f = cfl[k];
@@ -377,20 +380,20 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
                         const T *G = (const T *)(sc + lay.oG) + dh;
                         const T bi = B[c], gi = G[c];
                         const T x1 = invtheta * bi * gi;
-                        T a = LK[tc] * x1;
-                        if (f & CF_ZP) a += CZ[tc] * (x1 - invtheta * B[c + 1] * G[c + 1]);
-                        if (f & CF_ZM) a += CZ[tc - 1] * (x1 - invtheta * B[c - 1] * G[c - 1]);
-                        if (f & CF_YP) a += CY[c] * (x1 - invtheta * B[c + nz] * G[c + nz]);
-                        if (f & CF_YM) a += CY[tc] * (x1 - invtheta * B[c - nz] * G[c - nz]);
+                        T a = cf(LK[tc]) * x1;
+                        if (f & CF_ZP) a += cf(CZ[tc]) * (x1 - invtheta * B[c + 1] * G[c + 1]);
+                        if (f & CF_ZM) a += cf(CZ[tc - 1]) * (x1 - invtheta * B[c - 1] * G[c - 1]);
+                        if (f & CF_YP) a += cf(CY[c]) * (x1 - invtheta * B[c + nz] * G[c + nz]);
+                        if (f & CF_YM) a += cf(CY[tc]) * (x1 - invtheta * B[c - nz] * G[c - nz]);
                         if (xp) {
                             const T *Bn = (const T *)(sn + lay.oB) + dn_;
                             const T *Gn = (const T *)(sn + lay.oG) + dn_;
-                            a += CX[tc] * (x1 - invtheta * Bn[c] * Gn[c]);
+                            a += cf(CX[tc]) * (x1 - invtheta * Bn[c] * Gn[c]);
                         }
                         if (xm) {
                             const T *Bq = (const T *)(sq + lay.oB) + dq;
                             const T *Gq = (const T *)(sq + lay.oG) + dq;
-                            a += CXq[tc] * (x1 - invtheta * Bq[c] * Gq[c]);
+                            a += cf(CXq[tc]) * (x1 - invtheta * Bq[c] * Gq[c]);
                         }
                         const T dn = c1 * x1 + c2 * (bi - a) * gi;
                         if (!NOD) d[i] = dn;
@@ -398,21 +401,21 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
                     } else {
                         const T *X = (const T *)(sc + lay.oX) + dh;
                         const T xi = X[c];
-                        const T lk = LK[tc];
+                        const T lk = cf(LK[tc]);
                         T a = lk * xi, dg = lk;
-                        if (f & CF_ZP) { T w = CZ[tc];     a += w * (xi - X[c + 1]);  dg += w; }
-                        if (f & CF_ZM) { T w = CZ[tc - 1]; a += w * (xi - X[c - 1]);  dg += w; }
-                        if (f & CF_YP) { T w = CY[c];      a += w * (xi - X[c + nz]); dg += w; }
-                        if (f & CF_YM) { T w = CY[tc];     a += w * (xi - X[c - nz]); dg += w; }
+                        if (f & CF_ZP) { T w = cf(CZ[tc]);     a += w * (xi - X[c + 1]);  dg += w; }
+                        if (f & CF_ZM) { T w = cf(CZ[tc - 1]); a += w * (xi - X[c - 1]);  dg += w; }
+                        if (f & CF_YP) { T w = cf(CY[c]);      a += w * (xi - X[c + nz]); dg += w; }
+                        if (f & CF_YM) { T w = cf(CY[tc]);     a += w * (xi - X[c - nz]); dg += w; }
                         if (xp) {
                             const T *Xn = (const T *)(sn + lay.oX) + dn_;
-                            T w = CX[tc];
+                            T w = cf(CX[tc]);
                             a += w * (xi - Xn[c]);
                             dg += w;
                         }
                         if (xm) {
                             const T *Xq = (const T *)(sq + lay.oX) + dq;
-                            T w = CXq[tc];
+                            T w = cf(CXq[tc]);
                             a += w * (xi - Xq[c]);
                             dg += w;
                         }
@@ -466,6 +469,8 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
     PlaneLayout lay, int *err) {
     constexpr int R = kPlaneStages;
     constexpr int es = (int)sizeof(T);
+    using CT = coef_t<T>;
+    constexpr int ec = (int)sizeof(CT);  // coefficient streams
     constexpr int kConsumerWarps = kPlaneThreads / 32;
     extern __shared__ __align__(128) unsigned char sm[];
     __shared__ uint64_t full[R], empty[R];
@@ -505,15 +510,15 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
                 const long long pb = L.off + (long long)q * sx;
                 const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
                 const long long hA = pb + (long long)h0 * nz, hB = pb + (long long)h1 * nz, pE = lp + ncell;
-                auto stage = [&](const void *base, long long l0, long long a0, long long a1, int off) {
-                    stage_range(bar, base, es, l0, a0, a1, slot + off, L.off, L.off + L.n, slot, lay.slot_bytes);
+                auto stage = [&](const void *base, int esz, long long l0, long long a0, long long a1, int off) {
+                    stage_range(bar, base, esz, l0, a0, a1, slot + off, L.off, L.off + L.n, slot, lay.slot_bytes);
                 };
-                stage(xin, lh, hA, hB, lay.oX);
-                stage(b, lp, lp, pE, lay.oB);
-                stage(C.cx, lp, lp, pE, lay.oCX);
-                stage(C.cy, lh, hA, pE, lay.oCY);
-                stage(C.cz, lp, lp, pE, lay.oCZ);
-                stage(C.leak, lp, lp, pE, lay.oLK);
+                stage(xin, es, lh, hA, hB, lay.oX);
+                stage(b, es, lp, lp, pE, lay.oB);
+                stage(C.cx, ec, lp, lp, pE, lay.oCX);
+                stage(C.cy, ec, lh, hA, pE, lay.oCY);
+                stage(C.cz, ec, lp, lp, pE, lay.oCZ);
+                stage(C.leak, ec, lp, lp, pE, lay.oLK);
             });
         }
         __syncwarp();
@@ -554,11 +559,13 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
             const int dqp = xm ? stage_delta(lp - sx, es) : dp;
             const T *X = (const T *)(sc + lay.oX) + dh;
             const T *B = (const T *)(sc + lay.oB) + dp;
-            const T *CX = (const T *)(sc + lay.oCX) + dp;
-            const T *CXq = (const T *)(sq + lay.oCX) + dqp;
-            const T *CY = (const T *)(sc + lay.oCY) + dh;
-            const T *CZ = (const T *)(sc + lay.oCZ) + dp;
-            const T *LK = (const T *)(sc + lay.oLK) + dp;
+            const int ch = stage_delta(lh, ec), cp = stage_delta(lp, ec);
+            const int cqp = xm ? stage_delta(lp - sx, ec) : cp;
+            const CT *CX = (const CT *)(sc + lay.oCX) + cp;
+            const CT *CXq = (const CT *)(sq + lay.oCX) + cqp;
+            const CT *CY = (const CT *)(sc + lay.oCY) + ch;
+            const CT *CZ = (const CT *)(sc + lay.oCZ) + cp;
+            const CT *LK = (const CT *)(sc + lay.oLK) + cp;
             const T *Xn = (const T *)(sn + lay.oX) + dn_;
             const T *Xq = (const T *)(sq + lay.oX) + dq;
             T *rs = res[x & 1];
@@ -569,13 +576,13 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
                 const int tc = t + k * kPlaneThreads;
                 const int c = nz + tc;
                 const T xi = X[c];
-                T a = LK[tc] * xi;
-                if (f & CF_ZP) a += CZ[tc] * (xi - X[c + 1]);
-                if (f & CF_ZM) a += CZ[tc - 1] * (xi - X[c - 1]);
-                if (f & CF_YP) a += CY[c] * (xi - X[c + nz]);
-                if (f & CF_YM) a += CY[tc] * (xi - X[c - nz]);
-                if (xp) a += CX[tc] * (xi - Xn[c]);
-                if (xm) a += CXq[tc] * (xi - Xq[c]);
+                T a = cf(LK[tc]) * xi;
+                if (f & CF_ZP) a += cf(CZ[tc]) * (xi - X[c + 1]);
+                if (f & CF_ZM) a += cf(CZ[tc - 1]) * (xi - X[c - 1]);
+                if (f & CF_YP) a += cf(CY[c]) * (xi - X[c + nz]);
+                if (f & CF_YM) a += cf(CY[tc]) * (xi - X[c - nz]);
+                if (xp) a += cf(CX[tc]) * (xi - Xn[c]);
+                if (xm) a += cf(CXq[tc]) * (xi - Xq[c]);
                 rs[tc] = B[tc] - a;
             }
         }

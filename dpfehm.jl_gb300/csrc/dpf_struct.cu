@@ -45,12 +45,13 @@ struct FaceK {
 
 // Fine-level operator, right-hand side and initial guess (src/groundwater.jl:4-20 with
 // S = V = 1; storage shift for transient). Writes FP64 coefficients and, when fx != null,
-// FP32 copies.
+// the bf16 copies of the FP32 V-cycle.
 __global__ void k_assemble(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                            const ProbParam *__restrict__ prm, FaceK fk, const double *__restrict__ dh,
                            const double *__restrict__ Qs, const double *__restrict__ shift,
                            const uint8_t *__restrict__ dir, double *cx, double *cy, double *cz, double *leak,
-                           float *fx, float *fy, float *fz, float *fleak, float2 *dfx, float2 *dfy, float2 *dfz,
+                           __nv_bfloat16 *fx, __nv_bfloat16 *fy, __nv_bfloat16 *fz, __nv_bfloat16 *fleak,
+                           float2 *dfx, float2 *dfy, float2 *dfz,
                            float2 *dfleak, double *b, double *x, int init_x) {
     int4 bm = bmap[blockIdx.x];
     LevelDesc L = desc[bm.x];
@@ -97,7 +98,10 @@ __global__ void k_assemble(const LevelDesc *__restrict__ desc, const int4 *__res
             cp[0] = df_to_double(qx); cp[1] = df_to_double(qy); cp[2] = df_to_double(qz); lk = df_to_double(ql);
         }
         cx[i] = cp[0]; cy[i] = cp[1]; cz[i] = cp[2]; leak[i] = lk;
-        if (fx) { fx[i] = (float)cp[0]; fy[i] = (float)cp[1]; fz[i] = (float)cp[2]; fleak[i] = (float)lk; }
+        if (fx) {
+            fx[i] = __double2bfloat16(cp[0]); fy[i] = __double2bfloat16(cp[1]);
+            fz[i] = __double2bfloat16(cp[2]); fleak[i] = __double2bfloat16(lk);
+        }
         b[i] = rhs;
         if (init_x) x[i] = fi ? 0.0 : dh[i];
         else if (!fi) x[i] = dh[i];
@@ -113,8 +117,8 @@ __global__ void k_coarsen(const LevelDesc *__restrict__ fdesc, const LevelDesc *
                           const int4 *__restrict__ bmap, const double *__restrict__ fcx,
                           const double *__restrict__ fcy, const double *__restrict__ fcz,
                           const double *__restrict__ fleak, const uint8_t *__restrict__ fdir, double *ccx,
-                          double *ccy, double *ccz, double *cleak, uint8_t *cdir, float *gx, float *gy, float *gz,
-                          float *gleak) {
+                          double *ccy, double *ccz, double *cleak, uint8_t *cdir, __nv_bfloat16 *gx,
+                          __nv_bfloat16 *gy, __nv_bfloat16 *gz, __nv_bfloat16 *gleak) {
     int4 bm = bmap[blockIdx.x];
     LevelDesc Lc = cdesc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)Lc.n; li_ += bm.z * kBlock) {
@@ -138,7 +142,10 @@ __global__ void k_coarsen(const LevelDesc *__restrict__ fdesc, const LevelDesc *
         if (!anyfree) { lk = 1.0; sx = sy = sz = 0.0; }
         const long long i = c.i;
         ccx[i] = sx; ccy[i] = sy; ccz[i] = sz; cleak[i] = lk; cdir[i] = anyfree ? 0 : 1;
-        if (gx) { gx[i] = (float)sx; gy[i] = (float)sy; gz[i] = (float)sz; gleak[i] = (float)lk; }
+        if (gx) {
+            gx[i] = __double2bfloat16(sx); gy[i] = __double2bfloat16(sy);
+            gz[i] = __double2bfloat16(sz); gleak[i] = __double2bfloat16(lk);
+        }
     }
 }
 
@@ -985,7 +992,7 @@ __global__ void k_cell_k(const LevelDesc *__restrict__ desc, const int4 *__restr
 // inverse diagonal of a level from its FP64 coefficients (the smoothers multiply
 // instead of dividing); written in FP64 and/or FP32
 __global__ void k_invdiag(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, Coeffs<double> C,
-                          double *__restrict__ idg, float *__restrict__ idg32) {
+                          Coeffs<float> C16, double *__restrict__ idg, float *__restrict__ idg32) {
     int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -996,7 +1003,8 @@ __global__ void k_invdiag(const LevelDesc *__restrict__ desc, const int4 *__rest
             idg[c.i] = v;
             if (idg32) idg32[c.i] = (float)v;
         } else {
-            idg32[c.i] = 1.0f / (float)diag7(L, c, C);  // smoother only: FP32 division suffices
+            // the FP32 V-cycle: the diagonal its kernels form from the bf16 coefficients
+            idg32[c.i] = 1.0f / diag7(L, c, C16);
         }
     }
 }
@@ -1322,7 +1330,7 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         L.c64[0] = dalloc<double>(n, owned); L.c64[1] = dalloc<double>(n, owned);
         L.c64[2] = dalloc<double>(n, owned); L.c64[3] = dalloc<double>(n, owned);
         if (mixed) {
-            for (int k = 0; k < 4; k++) L.c32[k] = dalloc<float>(n, owned);
+            for (int k = 0; k < 4; k++) L.c16[k] = dalloc<__nv_bfloat16>(n, owned);
             L.idg32 = dalloc<float>(n, owned);
         } else {
             L.idg64 = dalloc<double>(n, owned);
@@ -1504,7 +1512,7 @@ Coeffs<double> coeffs_of<double>(StructBatch::Level &L, bool) {
 }
 template <>
 Coeffs<float> coeffs_of<float>(StructBatch::Level &L, bool) {
-    return Coeffs<float>{L.c32[0], L.c32[1], L.c32[2], L.c32[3], L.idg32};
+    return Coeffs<float>{L.c16[0], L.c16[1], L.c16[2], L.c16[3], L.idg32};
 }
 
 void StructBatch::assemble(const double *Ks, const double *kc, int kind, const double *shift, bool init_x) {
@@ -1516,8 +1524,8 @@ void StructBatch::assemble(const double *Ks, const double *kc, int kind, const d
             KTimer _kt(this, kname("k_assemble", 0, false), L0.all_cells);
             k_assemble<<<nb_of(L0.all), kBlock, 0, stream>>>(
                 L0.d_desc, L0.all.d_map, d_prm, fk, in_dh, in_Q, shift, L0.dir, L0.c64[0], L0.c64[1], L0.c64[2],
-                L0.c64[3], mixed ? L0.c32[0] : nullptr, mixed ? L0.c32[1] : nullptr, mixed ? L0.c32[2] : nullptr,
-                mixed ? L0.c32[3] : nullptr, mixed ? cdf[0] : nullptr, mixed ? cdf[1] : nullptr,
+                L0.c64[3], mixed ? L0.c16[0] : nullptr, mixed ? L0.c16[1] : nullptr, mixed ? L0.c16[2] : nullptr,
+                mixed ? L0.c16[3] : nullptr, mixed ? cdf[0] : nullptr, mixed ? cdf[1] : nullptr,
                 mixed ? cdf[2] : nullptr, mixed ? cdf[3] : nullptr, b64, h, init_x ? 1 : 0);
         }
     LAUNCH_CHECK();
@@ -1528,8 +1536,8 @@ void StructBatch::assemble(const double *Ks, const double *kc, int kind, const d
             KTimer _kt(this, kname("k_coarsen", l + 1, false), C.all_cells);
             k_coarsen<<<nb_of(C.all), kBlock, 0, stream>>>(
                 F.d_desc, C.d_desc, C.all.d_map, F.c64[0], F.c64[1], F.c64[2], F.c64[3], F.dir, C.c64[0], C.c64[1],
-                C.c64[2], C.c64[3], C.dir, mixed ? C.c32[0] : nullptr, mixed ? C.c32[1] : nullptr,
-                mixed ? C.c32[2] : nullptr, mixed ? C.c32[3] : nullptr);
+                C.c64[2], C.c64[3], C.dir, mixed ? C.c16[0] : nullptr, mixed ? C.c16[1] : nullptr,
+                mixed ? C.c16[2] : nullptr, mixed ? C.c16[3] : nullptr);
         }
         LAUNCH_CHECK();
     }
@@ -1550,6 +1558,7 @@ void StructBatch::assemble(const double *Ks, const double *kc, int kind, const d
         {
             KTimer _kt(this, kname("k_invdiag", l, false), L.all_cells);
             k_invdiag<<<nb_of(L.all), kBlock, 0, stream>>>(L.d_desc, L.all.d_map, coeffs_of<double>(L, false),
+                                                           mixed ? coeffs_of<float>(L, true) : Coeffs<float>{},
                                                            mixed ? nullptr : L.idg64, mixed ? L.idg32 : nullptr);
         }
         LAUNCH_CHECK();
@@ -1614,10 +1623,11 @@ void StructBatch::pm_launch(int mode, int l, const T *b, const T *xin, T *xout, 
     lay.oB = take(pm_region(f2 ? L.pm.halo : L.pm.slab, es));
     lay.oD = (f2 || first) ? -1 : take(pm_region(L.pm.slab, es));
     lay.oG = f2 ? take(pm_region(L.pm.halo, es)) : -1;
-    lay.oCX = take(pm_region(L.pm.slab, es));
-    lay.oCY = take(pm_region(L.pm.cy, es));
-    lay.oCZ = take(pm_region(L.pm.slab, es));
-    lay.oLK = take(pm_region(L.pm.slab, es));
+    const int ec = (int)sizeof(coef_t<T>);
+    lay.oCX = take(pm_region(L.pm.slab, ec));
+    lay.oCY = take(pm_region(L.pm.cy, ec));
+    lay.oCZ = take(pm_region(L.pm.slab, ec));
+    lay.oLK = take(pm_region(L.pm.slab, ec));
     lay.oDIR = prol ? take(pm_region(L.pm.halo, 1)) : -1;
     lay.oE = prol ? take(pm_region(L.pm.coarse, es)) : -1;
     lay.slot_bytes = (off + 127) & ~127;
@@ -1672,10 +1682,11 @@ void StructBatch::pm_restrict(int l, const T *b, const T *x, T *bc) {
     auto take = [&](int bytes) { int o = off; off += bytes; return o; };
     lay.oX = take(pm_region(L.pm.halo, es));
     lay.oB = take(pm_region(L.pm.slab, es));
-    lay.oCX = take(pm_region(L.pm.slab, es));
-    lay.oCY = take(pm_region(L.pm.cy, es));
-    lay.oCZ = take(pm_region(L.pm.slab, es));
-    lay.oLK = take(pm_region(L.pm.slab, es));
+    const int ec = (int)sizeof(coef_t<T>);
+    lay.oCX = take(pm_region(L.pm.slab, ec));
+    lay.oCY = take(pm_region(L.pm.cy, ec));
+    lay.oCZ = take(pm_region(L.pm.slab, ec));
+    lay.oLK = take(pm_region(L.pm.slab, ec));
     lay.oD = lay.oG = lay.oDIR = lay.oE = -1;
     lay.slot_bytes = (off + 127) & ~127;
     const size_t smem = (size_t)kPlaneStages * lay.slot_bytes;

@@ -82,7 +82,7 @@ public:
         uint8_t *dir = nullptr;        // identity (Dirichlet) rows
         double *c64[4] = {nullptr, nullptr, nullptr, nullptr};  // cx, cy, cz, leak
         double *idg64 = nullptr;       // inverse diagonal (FP64 solves)
-        float *c32[4] = {nullptr, nullptr, nullptr, nullptr};
+        __nv_bfloat16 *c16[4] = {nullptr, nullptr, nullptr, nullptr};  // FP32 V-cycle (bf16)
         float *idg32 = nullptr;        // inverse diagonal (FP32 V-cycle)
         void *work[4] = {nullptr, nullptr, nullptr, nullptr};   // xa, xb, b, d (V-cycle precision)
     };

@@ -37,6 +37,11 @@ __device__ __forceinline__ void cell_at(const LevelDesc &L, int li, Cell &c) {
 #endif
 }
 
+// A stored coefficient as the arithmetic type of its level.
+__device__ __forceinline__ float cf(__nv_bfloat16 v) { return __bfloat162float(v); }
+__device__ __forceinline__ float cf(float v) { return v; }
+__device__ __forceinline__ double cf(double v) { return v; }
+
 // Index in the coarse level arrays of the 2x2x2 aggregate that holds fine cell c.
 __device__ __forceinline__ long long agg_index(const LevelDesc &Lc, const Cell &c) {
     const int ax = c.ix >> 1, ay = c.iy >> 1, az = c.iz >> 1;
@@ -213,7 +218,7 @@ __device__ __forceinline__ void apply7(const LevelDesc &L, const Cell &c, const 
                                        T &diag) {
     const long long i = c.i;
     const long long sy = L.nz, sx = (long long)L.ny * L.nz;
-    T lk = C.leak[i];
+    T lk = cf(C.leak[i]);
     T a = lk * xi, d = lk;
 #if DPF_CHECKED
     // every neighbour the flags below admit lies inside the problem's cells
@@ -228,12 +233,12 @@ __device__ __forceinline__ void apply7(const LevelDesc &L, const Cell &c, const 
         return;
     }
 #endif
-    if (c.iz + 1 < L.nz) { T w = C.cz[i];      a += w * (xi - xat(i + 1, c.ix, c.iy, c.iz + 1));   d += w; }
-    if (c.iz > 0)        { T w = C.cz[i - 1];  a += w * (xi - xat(i - 1, c.ix, c.iy, c.iz - 1));   d += w; }
-    if (c.iy + 1 < L.ny) { T w = C.cy[i];      a += w * (xi - xat(i + sy, c.ix, c.iy + 1, c.iz));  d += w; }
-    if (c.iy > 0)        { T w = C.cy[i - sy]; a += w * (xi - xat(i - sy, c.ix, c.iy - 1, c.iz));  d += w; }
-    if (c.ix + 1 < L.nx) { T w = C.cx[i];      a += w * (xi - xat(i + sx, c.ix + 1, c.iy, c.iz));  d += w; }
-    if (c.ix > 0)        { T w = C.cx[i - sx]; a += w * (xi - xat(i - sx, c.ix - 1, c.iy, c.iz));  d += w; }
+    if (c.iz + 1 < L.nz) { T w = cf(C.cz[i]);      a += w * (xi - xat(i + 1, c.ix, c.iy, c.iz + 1));   d += w; }
+    if (c.iz > 0)        { T w = cf(C.cz[i - 1]);  a += w * (xi - xat(i - 1, c.ix, c.iy, c.iz - 1));   d += w; }
+    if (c.iy + 1 < L.ny) { T w = cf(C.cy[i]);      a += w * (xi - xat(i + sy, c.ix, c.iy + 1, c.iz));  d += w; }
+    if (c.iy > 0)        { T w = cf(C.cy[i - sy]); a += w * (xi - xat(i - sy, c.ix, c.iy - 1, c.iz));  d += w; }
+    if (c.ix + 1 < L.nx) { T w = cf(C.cx[i]);      a += w * (xi - xat(i + sx, c.ix + 1, c.iy, c.iz));  d += w; }
+    if (c.ix > 0)        { T w = cf(C.cx[i - sx]); a += w * (xi - xat(i - sx, c.ix - 1, c.iy, c.iz));  d += w; }
     Ax = a;
     diag = d;
 }
@@ -254,13 +259,13 @@ template <typename T>
 __device__ __forceinline__ T diag7(const LevelDesc &L, const Cell &c, const Coeffs<T> &C) {
     const long long i = c.i;
     const long long sy = L.nz, sx = (long long)L.ny * L.nz;
-    T d = C.leak[i];
-    if (c.iz + 1 < L.nz) d += C.cz[i];
-    if (c.iz > 0) d += C.cz[i - 1];
-    if (c.iy + 1 < L.ny) d += C.cy[i];
-    if (c.iy > 0) d += C.cy[i - sy];
-    if (c.ix + 1 < L.nx) d += C.cx[i];
-    if (c.ix > 0) d += C.cx[i - sx];
+    T d = cf(C.leak[i]);
+    if (c.iz + 1 < L.nz) d += cf(C.cz[i]);
+    if (c.iz > 0) d += cf(C.cz[i - 1]);
+    if (c.iy + 1 < L.ny) d += cf(C.cy[i]);
+    if (c.iy > 0) d += cf(C.cy[i - sy]);
+    if (c.ix + 1 < L.nx) d += cf(C.cx[i]);
+    if (c.ix > 0) d += cf(C.cx[i - sx]);
     return d;
 }
 
