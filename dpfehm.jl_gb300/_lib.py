@@ -38,6 +38,7 @@ class Options(ctypes.Structure):
         ("df_plane_cells", ctypes.c_int),
         ("df_plane_blocks_per_sm", ctypes.c_int),
         ("tail_cluster", ctypes.c_int),
+        ("plane_levels", ctypes.c_int),
     ]
 
 

@@ -287,6 +287,7 @@ dpf_options fill_options(const dpf_options *o) {
     if (r.df_plane_blocks_per_sm <= 0) r.df_plane_blocks_per_sm = d.df_plane_blocks_per_sm;
     if (r.tail_cluster <= 0) r.tail_cluster = d.tail_cluster;
     r.tail_cluster = std::min(16, r.tail_cluster);
+    if (r.plane_levels < 0) r.plane_levels = d.plane_levels;
     return r;
 }
 
@@ -339,6 +340,7 @@ void dpf_default_options(dpf_options *o) {
     o->df_plane_cells = -1;
     o->df_plane_blocks_per_sm = 4;
     o->tail_cluster = 1;
+    o->plane_levels = 0;
 }
 
 int dpf_detect_regular3d(int64_t N, int64_t F, const int64_t *a, const int64_t *b, const double *aol, int *dims,

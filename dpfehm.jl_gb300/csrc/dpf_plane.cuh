@@ -30,14 +30,19 @@ constexpr int kPlaneThreads = DPF_PLANE_THREADS;  // consumer threads per block 
 #endif
 constexpr int kPlaneStages = DPF_PLANE_STAGES;  // planes x-1, x, x+1 resident, the rest in flight
 constexpr int kMaxCellsPerThread = 4;  // slab capacity CPT x kPlaneThreads cells, CPT = 1..4 (a template parameter)
-// Rows per slab: as many whole rows as fit `cells`, even (so that slabs align with the
-// 2x2x2 aggregates of the next level) unless one slab holds the whole plane. Host and
-// device both use it, so the work items and the kernels agree.
+// Rows per slab: the fewest slabs of at most `cells` cells of whole rows, with the rows
+// spread evenly over them, and an even count (so that slabs align with the 2x2x2
+// aggregates of the next level) unless one slab holds the whole plane. Host and device
+// both use it, so the work items and the kernels agree.
 __host__ __device__ __forceinline__ int plane_rows(int ny, int nz, int cells) {
     int t = cells / nz;
     if (t >= 2) t &= ~1;
     if (t < 1) t = 1;
-    return t < ny ? t : ny;
+    if (t >= ny) return ny;
+    const int tiles = (ny + t - 1) / t;
+    int u = (ny + tiles - 1) / tiles;  // <= t
+    if (t >= 2) u += u & 1;            // still <= t: t is even
+    return u;
 }
 
 // per-cell flags: inside the slab, and which of the z+/z-/y+/y- neighbours exist
@@ -218,6 +223,7 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
     CgState *st, Coeffs<T> C, const T *__restrict__ b, const T *__restrict__ xin, T *__restrict__ xout,
     T *__restrict__ d, const uint8_t *__restrict__ dir, const T *__restrict__ e, T c1, T c2, T invtheta, T scale,
     PlaneLayout lay, ReduceScratch rs, const int2 *__restrict__ pinfo, int *err) {
+    pdl_enter();
     constexpr bool F2 = (MODE & PM_FIRST2) != 0, FIRST = (MODE & PM_FIRST) != 0,
                    PROL = (MODE & PM_PROLONG) != 0, NOD = (MODE & PM_NOD) != 0, RZ = (MODE & PM_RZ) != 0;
     constexpr int R = kPlaneStages;
@@ -467,6 +473,7 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
     const LevelDesc *__restrict__ desc, const LevelDesc *__restrict__ cdesc, const int4 *__restrict__ items,
     const CgState *st, Coeffs<T> C, const T *__restrict__ b, const T *__restrict__ xin, T *__restrict__ bc,
     PlaneLayout lay, int *err) {
+    pdl_enter();
     constexpr int R = kPlaneStages;
     constexpr int es = (int)sizeof(T);
     using CT = coef_t<T>;
@@ -625,6 +632,7 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_df_spmv(
     const LevelDesc *__restrict__ desc, const int4 *__restrict__ items, CgState *st, int *active_count,
     ReduceScratch rs, const int2 *__restrict__ pinfo, CoeffsDF C, const float2 *__restrict__ pv,
     float2 *__restrict__ qv, PlaneLayout lay, int *err) {
+    pdl_enter();
     constexpr int R = kPlaneStages;
     constexpr int es = 8;
     constexpr int kConsumerWarps = kPlaneThreads / 32;

@@ -53,6 +53,7 @@ __global__ void k_assemble(const LevelDesc *__restrict__ desc, const int4 *__res
                            __nv_bfloat16 *fx, __nv_bfloat16 *fy, __nv_bfloat16 *fz, __nv_bfloat16 *fleak,
                            float2 *dfx, float2 *dfy, float2 *dfz,
                            float2 *dfleak, double *b, double *x, int init_x) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     LevelDesc L = desc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -119,6 +120,7 @@ __global__ void k_coarsen(const LevelDesc *__restrict__ fdesc, const LevelDesc *
                           const double *__restrict__ fleak, const uint8_t *__restrict__ fdir, double *ccx,
                           double *ccy, double *ccz, double *cleak, uint8_t *cdir, __nv_bfloat16 *gx,
                           __nv_bfloat16 *gy, __nv_bfloat16 *gz, __nv_bfloat16 *gleak) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     LevelDesc Lc = cdesc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)Lc.n; li_ += bm.z * kBlock) {
@@ -159,6 +161,7 @@ __global__ void k_coarse_factor(const LevelDesc *__restrict__ desc, const int *_
                                 const double *__restrict__ cx, const double *__restrict__ cy,
                                 const double *__restrict__ cz, const double *__restrict__ leak, double *Inv,
                                 int *status) {
+    pdl_enter();
     __shared__ double A[kMaxCoarse][kMaxCoarse + 1];
     __shared__ double col[kMaxCoarse];
     __shared__ int bad;
@@ -293,6 +296,7 @@ template <typename T>
 __global__ void k_cheb_first(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                              Coeffs<T> C, const T *__restrict__ b, T *__restrict__ x, T *__restrict__ d,
                              T invtheta) {
+    pdl_enter();
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
         Cell c;
@@ -309,6 +313,7 @@ template <typename T>
 __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 8 : 5) k_cheb_first2(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                               Coeffs<T> C, const T *__restrict__ b, T *__restrict__ xout, T *__restrict__ d,
                               T invtheta, T c1, T c2) {
+    pdl_enter();
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
         Cell c;
@@ -326,6 +331,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 8 : 6)
 k_cheb_step(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st, Coeffs<T> C,
             const T *__restrict__ b, const T *__restrict__ xin, T *__restrict__ xout, T *__restrict__ d, T c1, T c2,
             ReduceScratch rs, const int2 *__restrict__ pinfo) {
+    pdl_enter();
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     Acc<T> part;
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -352,6 +358,7 @@ template <typename T>
 __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 8 : 5) k_restrict(const LevelDesc *__restrict__ fdesc, const LevelDesc *__restrict__ cdesc,
                            const int4 *__restrict__ bmap, CgState *st, Coeffs<T> C, const T *__restrict__ b,
                            const T *__restrict__ x, T *__restrict__ bc) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const int p = bm.x;
     if (st && !st[p].active) return;
@@ -371,6 +378,7 @@ template <typename T>
 __global__ void k_prolong_add(const LevelDesc *__restrict__ desc, const LevelDesc *__restrict__ cdesc,
               const int4 *__restrict__ bmap, CgState *st, const uint8_t *__restrict__ dir, T *__restrict__ x,
               const T *__restrict__ e, T scale) {
+    pdl_enter();
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     const LevelDesc Lc = cdesc[p];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -387,6 +395,7 @@ __global__ void k_prolong_add(const LevelDesc *__restrict__ desc, const LevelDes
 template <typename T, bool FUSE_RZ>
 __global__ void k_coarse_solve(const LevelDesc *__restrict__ desc, const int *__restrict__ plist, CgState *st,
                                const double *__restrict__ Inv, const T *__restrict__ b, T *__restrict__ x) {
+    pdl_enter();
     const int p = plist[blockIdx.x];
     if (st && !st[p].active) return;
     const LevelDesc L = desc[p];
@@ -432,6 +441,7 @@ template <typename T, bool CLUSTER>
 __global__ void __launch_bounds__(kTailThreads) k_tail_cycle(const TailLevel<T> *__restrict__ tl,
                                                              const int4 *__restrict__ tails, const CgState *st,
                                                              const double *__restrict__ Inv, TailParams<T> tp) {
+    pdl_enter();
     // one problem per block, or (CLUSTER) per thread-block cluster: its blocks share every
     // step's cells and meet at hardware cluster barriers
     unsigned rank = 0, nranks = 1;
@@ -540,6 +550,7 @@ template <typename T>
 __global__ void k_cg_start(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                            int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, Coeffs<T> C,
                            const T *__restrict__ b, const T *__restrict__ x, T *__restrict__ r, double tol2) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const int p = bm.x;
     const LevelDesc L = desc[p];
@@ -578,6 +589,7 @@ template <typename T>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_spmv_pq(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                           int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, Coeffs<T> C,
                           const T *__restrict__ pv, T *__restrict__ q) {
+    pdl_enter();
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     Acc<T> part;
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -603,6 +615,7 @@ template <typename T>
 __global__ void k_update_xr(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                             int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, T *__restrict__ x,
                             T *__restrict__ r, const T *__restrict__ pv, const T *__restrict__ q, int maxiter) {
+    pdl_enter();
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     const double alpha = st[p].alpha;
     Acc<T> part;
@@ -631,6 +644,7 @@ __global__ void k_update_xr(const LevelDesc *__restrict__ desc, const int4 *__re
 template <typename T>
 __global__ void k_update_p(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                            const T *__restrict__ z, T *__restrict__ pv) {
+    pdl_enter();
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     const T beta = (T)st[p].beta;
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -662,6 +676,7 @@ __global__ void k_update_p(const LevelDesc *__restrict__ desc, const int4 *__res
 __global__ void __launch_bounds__(kBlock, DPF_DF_SPMV_MINB) k_df_spmv_pq(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                              int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, CoeffsDF C,
                              const float2 *__restrict__ pv, float2 *__restrict__ q) {
+    pdl_enter();
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     Acc<float> part;
     const long long sy = L.nz, sx = (long long)L.ny * L.nz;
@@ -693,6 +708,7 @@ __global__ void k_df_update_xr(const LevelDesc *__restrict__ desc, const int4 *_
                                int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo,
                                double *__restrict__ x64, float2 *__restrict__ r, float *__restrict__ r32,
                                const float2 *__restrict__ pv, const float2 *__restrict__ q, int maxiter) {
+    pdl_enter();
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     const float2 a = df_from_double(st[p].alpha);
     const double as = st[p].alpha * st[p].scale;
@@ -721,6 +737,7 @@ __global__ void k_df_update_xr(const LevelDesc *__restrict__ desc, const int4 *_
 // p = z + beta p (double-float; z is the FP32 preconditioned residual)
 __global__ void k_df_update_p(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                               const float *__restrict__ z, float2 *__restrict__ pv) {
+    pdl_enter();
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     const double beta = st[p].beta;
     const float2 b = df_from_double(beta);
@@ -741,6 +758,7 @@ __global__ void k_df_residual(const LevelDesc *__restrict__ desc, const int4 *__
                               Coeffs<double> C, const uint8_t *__restrict__ dir, const double *__restrict__ b,
                               const double *__restrict__ x, double *__restrict__ r, double tol2, int maxiter,
                               int max_rounds) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const int p = bm.x;
     if (!FIRST && st[p].ru_flag == 0) return;  // finished in an earlier round
@@ -824,6 +842,7 @@ __global__ void k_df_residual(const LevelDesc *__restrict__ desc, const int4 *__
 // start of a round: r = r64 / scale (double-float and its leading float)
 __global__ void k_df_begin(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, const CgState *st,
                            const double *__restrict__ r64, float2 *__restrict__ r, float *__restrict__ r32) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const int p = bm.x;
     if (!st[p].ru_flag) return;
@@ -839,6 +858,7 @@ __global__ void k_df_begin(const LevelDesc *__restrict__ desc, const int4 *__res
 
 // ------------------------------------------------------------ misc vector kernels
 __global__ void k_state_init(CgState *st, int nprob) {
+    pdl_enter();
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nprob) return;
     CgState s;
@@ -851,6 +871,7 @@ __global__ void k_state_init(CgState *st, int nprob) {
 __global__ void k_adjoint_rhs(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                               const uint8_t *__restrict__ dir, const double *__restrict__ delta,
                               double *__restrict__ rhs, double *__restrict__ x) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -864,6 +885,7 @@ __global__ void k_adjoint_rhs(const LevelDesc *__restrict__ desc, const int4 *__
 // delta = 2 h at observation cells (J = sum h[obs]^2), 0 elsewhere (delta zeroed before)
 __global__ void k_obs_delta(const long long *__restrict__ obs_global, long long nobs, const double *__restrict__ h,
                             double *__restrict__ delta) {
+    pdl_enter();
     long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nobs) return;
     long long i = obs_global[k];
@@ -874,6 +896,7 @@ __global__ void k_obs_delta(const long long *__restrict__ obs_global, long long 
 __global__ void k_shift(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                         const ProbParam *__restrict__ prm, const double *__restrict__ Ss, double inv_dt,
                         double *__restrict__ shift) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -888,6 +911,7 @@ __global__ void k_axpy_rhs(const LevelDesc *__restrict__ desc, const int4 *__res
                            const uint8_t *__restrict__ dir, const double *__restrict__ b0,
                            const double *__restrict__ shift, const double *__restrict__ hprev,
                            double *__restrict__ b) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -903,6 +927,7 @@ __global__ void k_axpy_rhs(const LevelDesc *__restrict__ desc, const int4 *__res
 __global__ void k_grad_faces(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                              const ProbParam *__restrict__ prm, const double *__restrict__ h,
                              const double *__restrict__ lam, double *__restrict__ dKs, int accumulate) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -930,6 +955,7 @@ __global__ void k_grad_faces(const LevelDesc *__restrict__ desc, const int4 *__r
 __global__ void k_grad_logk(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                             const ProbParam *__restrict__ prm, const double *__restrict__ kc, int kind,
                             const double *__restrict__ h, const double *__restrict__ lam, double *__restrict__ g) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -979,6 +1005,7 @@ __global__ void k_grad_logk(const LevelDesc *__restrict__ desc, const int4 *__re
 // per-cell values for the face means: exp(logK / 2) (geometric) or exp(logK) (harmonic)
 __global__ void k_cell_k(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                          const double *__restrict__ logK, int kind, double *__restrict__ kc) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -993,6 +1020,7 @@ __global__ void k_cell_k(const LevelDesc *__restrict__ desc, const int4 *__restr
 // instead of dividing); written in FP64 and/or FP32
 __global__ void k_invdiag(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, Coeffs<double> C,
                           Coeffs<float> C16, double *__restrict__ idg, float *__restrict__ idg32) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -1015,6 +1043,7 @@ __global__ void k_grad_dh_q(const LevelDesc *__restrict__ desc, const int4 *__re
                             const ProbParam *__restrict__ prm, FaceK fk, const uint8_t *__restrict__ dir,
                             const double *__restrict__ delta, const double *__restrict__ lam, double *ddh,
                             double *dQs, int accumulate) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -1050,6 +1079,7 @@ __global__ void k_grad_dh_q(const LevelDesc *__restrict__ desc, const int4 *__re
 __global__ void k_logk_to_faces(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                                 const ProbParam *__restrict__ prm, const double *__restrict__ kc, int kind,
                                 double *__restrict__ Ks) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -1070,6 +1100,7 @@ __global__ void k_logk_to_faces(const LevelDesc *__restrict__ desc, const int4 *
 __global__ void k_logk_vjp(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                            const ProbParam *__restrict__ prm, const double *__restrict__ kc, int kind,
                            const double *__restrict__ dKs, double *__restrict__ g) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -1099,6 +1130,7 @@ __global__ void k_logk_vjp(const LevelDesc *__restrict__ desc, const int4 *__res
 // y = A x (FP64 fine operator; Dirichlet rows identity)
 __global__ void k_apply(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, Coeffs<double> C,
                         const double *__restrict__ x, double *__restrict__ y) {
+    pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const LevelDesc L = desc[bm.x];
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
@@ -1116,6 +1148,26 @@ static void ck(cudaError_t e, const char *what) {
 }
 #define CK(x) ck((x), #x)
 #define LAUNCH_CHECK() ck(cudaGetLastError(), "kernel launch")
+
+// Launch with programmatic stream serialization: the launch is prepared while the previous
+// kernel on the stream runs and its blocks start as that kernel's blocks exit; each solver
+// kernel's pdl_enter() waits for the previous kernel's completion and memory before it
+// touches memory, so the order is that of plain launches (also inside captured graphs).
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                       Args &&...args) {
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    ck(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...), "kernel launch");
+}
 
 template <typename T>
 static T *dalloc(size_t n, DevList &owned) {
@@ -1307,7 +1359,8 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         L.all = build_map(L.h_desc, has, owned, nprob, target_blocks);
         L.smooth = build_map(L.h_desc, smooth, owned, nprob, target_blocks);
         L.restr = build_map(L.h_desc, restr, owned, nprob, target_blocks);
-        build_plane_items(L.pm, L, smooth, sms, opt.plane > 0 ? opt.plane_cells : 0, opt.plane_blocks_per_sm, &shapes,
+        const bool plane_here = opt.plane > 0 && (opt.plane_levels <= 0 || l < opt.plane_levels);
+        build_plane_items(L.pm, L, smooth, sms, plane_here ? opt.plane_cells : 0, opt.plane_blocks_per_sm, &shapes,
                           l);
         if (l == 0) build_plane_items(L.pa, L, has, sms, opt.df_plane_cells, opt.df_plane_blocks_per_sm, nullptr, l);
         for (int p = 0; p < nprob; p++) {
@@ -1580,7 +1633,7 @@ static void pm_kernel(unsigned nblocks, size_t smem, cudaStream_t stream, const 
         CK(cudaFuncSetAttribute(k_pm_cheb<T, MODE, CPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = smem;
     }
-    k_pm_cheb<T, MODE, CPT><<<nblocks, kPlaneThreads + 32, smem, stream>>>(desc, cdesc, items, st, C, b, xin, xout, d,
+    launch_pdl(k_pm_cheb<T, MODE, CPT>, nblocks, kPlaneThreads + 32, smem, stream, desc, cdesc, items, st, C, b, xin, xout, d,
                                                                        dir, e, c1, c2, invth, sc, lay, rs, pinfo, err);
 }
 
@@ -1667,7 +1720,7 @@ static void pm_restrict_kernel(unsigned nblocks, size_t smem, cudaStream_t strea
         CK(cudaFuncSetAttribute(k_pm_restrict<T, CPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = smem;
     }
-    k_pm_restrict<T, CPT><<<nblocks, kPlaneThreads + 32, smem, stream>>>(desc, cdesc, items, st, C, b, x, bc, lay, err);
+    launch_pdl(k_pm_restrict<T, CPT>, nblocks, kPlaneThreads + 32, smem, stream, desc, cdesc, items, st, C, b, x, bc, lay, err);
 }
 
 template <typename T>
@@ -1731,7 +1784,7 @@ void StructBatch::launch_tail(const TailParams<T> &tp) {
         tail_cs = cs;
     }
     if (tail_cs <= 1) {
-        k_tail_cycle<T, false><<<nt, kTailThreads, 0, stream>>>((const TailLevel<T> *)d_tail_lv, d_tails, d_state,
+        launch_pdl(k_tail_cycle<T, false>, nt, kTailThreads, 0, stream, (const TailLevel<T> *)d_tail_lv, d_tails, d_state,
                                                                d_coarseL, tp);
         return;
     }
@@ -1794,7 +1847,7 @@ void StructBatch::vcycle(const T *r, T *z) {
                 // steps 0 and 1 fused; the iterate lands where step 1 would leave it (xb)
                 {
                     KTimer _kt(this, kname("k_cheb_first2", l, sizeof(T) == 4), L.smooth_cells);
-                    k_cheb_first2<T><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, L.smooth.d_map, d_state, C, b,
+                    launch_pdl(k_cheb_first2<T>, nb_of(L.smooth), kBlock, 0, stream, L.d_desc, L.smooth.d_map, d_state, C, b,
                                                                              xb, d, invth, (T)cheb_c1[1],
                                                                              (T)cheb_c2[1]);
                 }
@@ -1805,7 +1858,7 @@ void StructBatch::vcycle(const T *r, T *z) {
             } else {
                 {
                     KTimer _kt(this, kname("k_cheb_first", l, sizeof(T) == 4), L.smooth_cells);
-                    k_cheb_first<T><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, L.smooth.d_map, d_state, C, b,
+                    launch_pdl(k_cheb_first<T>, nb_of(L.smooth), kBlock, 0, stream, L.d_desc, L.smooth.d_map, d_state, C, b,
                                                                             xa, d, invth);
                 }
                 LAUNCH_CHECK();
@@ -1813,7 +1866,7 @@ void StructBatch::vcycle(const T *r, T *z) {
             for (int k = k0; k < deg; k++) {
                 {
                     KTimer _kt(this, kname("k_cheb_step", l, sizeof(T) == 4), L.smooth_cells);
-                    k_cheb_step<T, false><<<nb_of(L.smooth), kBlock, 0, stream>>>(
+                    launch_pdl(k_cheb_step<T, false>, nb_of(L.smooth), kBlock, 0, stream, 
                         L.d_desc, L.smooth.d_map, d_state, C, b, cur, oth, d, (T)cheb_c1[k], (T)cheb_c2[k], rs,
                         L.smooth.d_pinfo);
                 }
@@ -1824,7 +1877,7 @@ void StructBatch::vcycle(const T *r, T *z) {
             Level &Cn = lv[l + 1];
             {
                 KTimer _kt(this, kname("k_restrict", l + 1, sizeof(T) == 4), Cn.restr_cells);
-                k_restrict<T><<<nb_of(Cn.restr), kBlock, 0, stream>>>(L.d_desc, Cn.d_desc, Cn.restr.d_map, d_state, C, b,
+                launch_pdl(k_restrict<T>, nb_of(Cn.restr), kBlock, 0, stream, L.d_desc, Cn.d_desc, Cn.restr.d_map, d_state, C, b,
                                                                    cur, (T *)Cn.work[2]);
             }
             LAUNCH_CHECK();
@@ -1836,13 +1889,13 @@ void StructBatch::vcycle(const T *r, T *z) {
             if (l == 0)
                 {
                     KTimer _kt(this, kname("k_coarse_solve", l, sizeof(T) == 4), L.csolve_cells);
-                    k_coarse_solve<T, true><<<(unsigned)L.csolve_list.size(), kMaxCoarse, 0, stream>>>(
+                    launch_pdl(k_coarse_solve<T, true>, (unsigned)L.csolve_list.size(), kMaxCoarse, 0, stream, 
                         L.d_desc, L.d_csolve, d_state, d_coarseL, b, out);
                 }
             else
                 {
                     KTimer _kt(this, kname("k_coarse_solve", l, sizeof(T) == 4), L.csolve_cells);
-                    k_coarse_solve<T, false><<<(unsigned)L.csolve_list.size(), kMaxCoarse, 0, stream>>>(
+                    launch_pdl(k_coarse_solve<T, false>, (unsigned)L.csolve_list.size(), kMaxCoarse, 0, stream, 
                         L.d_desc, L.d_csolve, d_state, d_coarseL, b, out);
                 }
             LAUNCH_CHECK();
@@ -1908,7 +1961,7 @@ void StructBatch::vcycle(const T *r, T *z) {
         }
         {
             KTimer _kt(this, kname("k_prolong_add", l, sizeof(T) == 4), L.smooth_cells);
-            k_prolong_add<T><<<nb_of(L.smooth), kBlock, 0, stream>>>(L.d_desc, Cn.d_desc, L.smooth.d_map, d_state,
+            launch_pdl(k_prolong_add<T>, nb_of(L.smooth), kBlock, 0, stream, L.d_desc, Cn.d_desc, L.smooth.d_map, d_state,
                                                                      L.dir, cur, e, sc);
         }
         LAUNCH_CHECK();
@@ -1920,17 +1973,17 @@ void StructBatch::vcycle(const T *r, T *z) {
                 KTimer _kt(this, kname(k == 0 ? "k_cheb_step0" : "k_cheb_step", l, sizeof(T) == 4), L.smooth_cells);
                 if (l == 0 && last) {
                     if (k == 0)
-                        k_cheb_step<T, true, true><<<nb_of(L.smooth), kBlock, 0, stream>>>(
+                        launch_pdl(k_cheb_step<T, true, true>, nb_of(L.smooth), kBlock, 0, stream, 
                             L.d_desc, L.smooth.d_map, d_state, C, b, cur, o, d, c1, c2, rs, L.smooth.d_pinfo);
                     else
-                        k_cheb_step<T, true, false><<<nb_of(L.smooth), kBlock, 0, stream>>>(
+                        launch_pdl(k_cheb_step<T, true, false>, nb_of(L.smooth), kBlock, 0, stream, 
                             L.d_desc, L.smooth.d_map, d_state, C, b, cur, o, d, c1, c2, rs, L.smooth.d_pinfo);
                 } else {
                     if (k == 0)
-                        k_cheb_step<T, false, true><<<nb_of(L.smooth), kBlock, 0, stream>>>(
+                        launch_pdl(k_cheb_step<T, false, true>, nb_of(L.smooth), kBlock, 0, stream, 
                             L.d_desc, L.smooth.d_map, d_state, C, b, cur, o, d, c1, c2, rs, L.smooth.d_pinfo);
                     else
-                        k_cheb_step<T, false, false><<<nb_of(L.smooth), kBlock, 0, stream>>>(
+                        launch_pdl(k_cheb_step<T, false, false>, nb_of(L.smooth), kBlock, 0, stream, 
                             L.d_desc, L.smooth.d_map, d_state, C, b, cur, o, d, c1, c2, rs, L.smooth.d_pinfo);
                 }
             }
@@ -1956,20 +2009,20 @@ void StructBatch::pcg_iteration(T *x) {
     const unsigned nb = nb_of(L0.all);
     {
         KTimer _kt(this, kname("k_spmv_pq", 0, sizeof(T) == 4), L0.all_cells);
-        k_spmv_pq<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C,
+        launch_pdl(k_spmv_pq<T>, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C,
                                                 pv, q);
     }
     LAUNCH_CHECK();
     {
         KTimer _kt(this, kname("k_update_xr", 0, sizeof(T) == 4), L0.all_cells);
-        k_update_xr<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, x, r,
+        launch_pdl(k_update_xr<T>, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, x, r,
                                                   pv, q, opt.maxiter);
     }
     LAUNCH_CHECK();
     vcycle<T>(r, z);
     {
         KTimer _kt(this, kname("k_update_p", 0, sizeof(T) == 4), L0.all_cells);
-        k_update_p<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z, pv);
+        launch_pdl(k_update_p<T>, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, z, pv);
     }
     LAUNCH_CHECK();
 }
@@ -1986,7 +2039,7 @@ static void pm_df_kernel(unsigned nblocks, size_t smem, cudaStream_t stream, con
         CK(cudaFuncSetAttribute(k_pm_df_spmv<CPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = smem;
     }
-    k_pm_df_spmv<CPT><<<nblocks, kPlaneThreads + 32, smem, stream>>>(desc, items, st, count, rs, pinfo, C, pv, q, lay,
+    launch_pdl(k_pm_df_spmv<CPT>, nblocks, kPlaneThreads + 32, smem, stream, desc, items, st, count, rs, pinfo, C, pv, q, lay,
                                                                      err);
 }
 
@@ -2023,26 +2076,27 @@ void StructBatch::df_iteration(double *x64) {
         pm_df_spmv(C);
     } else {
         KTimer _kt(this, kname("k_df_spmv_pq", 0, true), L0.all_cells);
-        k_df_spmv_pq<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C,
+        launch_pdl(k_df_spmv_pq, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C,
                                                 dfv[2], dfv[3]);
     }
     LAUNCH_CHECK();
     {
         KTimer _kt(this, kname("k_df_update_xr", 0, true), L0.all_cells);
-        k_df_update_xr<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo,
+        launch_pdl(k_df_update_xr, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo,
                                                   x64, dfv[1], r32, dfv[2], dfv[3], opt.maxiter);
     }
     LAUNCH_CHECK();
     vcycle<float>(r32, z32);
     {
         KTimer _kt(this, kname("k_df_update_p", 0, true), L0.all_cells);
-        k_df_update_p<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z32, dfv[2]);
+        launch_pdl(k_df_update_p, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, z32, dfv[2]);
     }
     LAUNCH_CHECK();
 }
 
 // Keeps iterating while any problem is active (bounded by maxiter + 2 passes).
 __global__ void k_loop_cond(cudaGraphConditionalHandle h, const int *count, int *iters, int maxiter) {
+    pdl_enter();
     int it = ++(*iters);
     cudaGraphSetConditional(h, (*count > 0 && it < maxiter + 2) ? 1u : 0u);
 }
@@ -2077,7 +2131,7 @@ cudaGraphExec_t StructBatch::loop_graph(int kind, void *x) {
     try {
         if (kind == 0) pcg_iteration<double>((double *)x);
         else df_iteration((double *)x);
-        k_loop_cond<<<1, 1, 0, stream>>>(cond, d_count, d_count + 2, opt.maxiter);
+        launch_pdl(k_loop_cond, 1, 1, 0, stream, cond, d_count, d_count + 2, opt.maxiter);
         launches++;
         LAUNCH_CHECK();
     } catch (...) {
@@ -2126,14 +2180,14 @@ void StructBatch::pcg(const T *b, T *x, double tol2) {
     CK(cudaMemsetAsync(d_count, 0, 4 * sizeof(int), stream));  // active problems, -, loop passes, -
     {
         KTimer _kt(this, kname("k_cg_start", 0, sizeof(T) == 4), L0.all_cells);
-        k_cg_start<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C, b, x,
+        launch_pdl(k_cg_start<T>, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C, b, x,
                                                  r, tol2);
     }
     LAUNCH_CHECK();
     vcycle<T>(r, z);
     {
         KTimer _kt(this, kname("k_update_p", 0, sizeof(T) == 4), L0.all_cells);
-        k_update_p<T><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z, pv);
+        launch_pdl(k_update_p<T>, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, z, pv);
     }
     LAUNCH_CHECK();
     run_loop(0, (void *)x);
@@ -2149,11 +2203,11 @@ void StructBatch::df_pcg(const double *b64, double *x64, double tol2) {
     {
         KTimer _kt(this, kname(zero_guess ? "k_df_residual0" : "k_df_residual", 0, false), L0.all_cells);
         if (zero_guess)
-            k_df_residual<true, true><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs,
+            launch_pdl(k_df_residual<true, true>, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, d_count, rs,
                                                                  L0.all.d_pinfo, coeffs_of<double>(L0, true), L0.dir,
                                                                  b64, x64, r64, tol2, opt.maxiter, opt.max_outer);
         else
-            k_df_residual<true><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs,
+            launch_pdl(k_df_residual<true>, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, d_count, rs,
                                                            L0.all.d_pinfo, coeffs_of<double>(L0, true), L0.dir, b64,
                                                            x64, r64, tol2, opt.maxiter, opt.max_outer);
     }
@@ -2161,20 +2215,20 @@ void StructBatch::df_pcg(const double *b64, double *x64, double tol2) {
     for (int round = 0; round < opt.max_outer && read_count(0) > 0; round++) {
         {
             KTimer _kt(this, kname("k_df_begin", 0, false), L0.all_cells);
-            k_df_begin<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, r64, dfv[1], r32);
+            launch_pdl(k_df_begin, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, r64, dfv[1], r32);
         }
         LAUNCH_CHECK();
         vcycle<float>(r32, z32);
         {
             KTimer _kt(this, kname("k_df_update_p", 0, true), L0.all_cells);
-            k_df_update_p<<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, z32, dfv[2]);
+            launch_pdl(k_df_update_p, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, z32, dfv[2]);
         }
         LAUNCH_CHECK();
         run_loop(1, x64);
         CK(cudaMemsetAsync(d_count, 0, sizeof(int), stream));
         {
             KTimer _kt(this, kname("k_df_residual", 0, false), L0.all_cells);
-            k_df_residual<false><<<nb, kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_state, d_count, rs,
+            launch_pdl(k_df_residual<false>, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, d_count, rs,
                                                             L0.all.d_pinfo, coeffs_of<double>(L0, true), L0.dir, b64,
                                                             x64, r64, tol2, opt.maxiter, opt.max_outer);
         }
@@ -2192,7 +2246,7 @@ void StructBatch::solve(const double *b, double *x, double reltol) {
     } zg{zero_guess};
     {
         KTimer _kt(this, kname("k_state_init", 0, false), 0);
-        k_state_init<<<(nprob + 127) / 128, 128, 0, stream>>>(d_state, nprob);
+        launch_pdl(k_state_init, (nprob + 127) / 128, 128, 0, stream, d_state, nprob);
     }
     LAUNCH_CHECK();
     CK(cudaMemsetAsync(d_factor_status + 1, 0, sizeof(int), stream));  // expired-wait word of this solve

@@ -19,6 +19,15 @@ struct Cell {
 
 __device__ __forceinline__ unsigned fast_div(unsigned n, unsigned m, int l) { return (__umulhi(n, m) + n) >> l; }
 
+// Programmatic dependent launch. Every solver kernel begins by waiting for the kernels it
+// follows on its stream (griddepcontrol.wait returns once they have completed and their
+// writes are visible, at once when the launch carried no such dependency), so launches with
+// the programmatic serialization attribute run in stream order while the next launch is
+// prepared during the previous kernel. Kernels do not signal their dependents early
+// (griddepcontrol.launch_dependents at block start): on the benchmark solve that made the
+// graphs 10 % slower, as waiting blocks of the next kernel took SM slots.
+__device__ __forceinline__ void pdl_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Coordinates of the li-th cell of a grid (li < n), without integer division.
 __device__ __forceinline__ void cell_at(const LevelDesc &L, int li, Cell &c) {
     unsigned u = (unsigned)li;

@@ -115,6 +115,7 @@ extern "C" int dpf_batch_autotune(int nprob, const int *dims, const double *mins
             {&cur.blocks_per_sm, {8, 16, 24}, true},
             {&cur.df_plane_cells, {-1, 512}, mixed},
             {&cur.tail_cluster, {1, 8}, true},
+            {&cur.plane_levels, {0, 1, 2}, mixed},
         };
         for (const Knob &k : knobs) {
             if (!k.active) continue;

@@ -91,6 +91,9 @@ typedef struct dpf_options {
     int df_plane_blocks_per_sm; /* its work items per SM (default 4) */
     int tail_cluster;    /* blocks (a thread-block cluster, 2..16) per problem for the fused tail
                             (default 1: one block) */
+    int plane_levels;    /* regular grids, MIXED: the plane-marching kernels run on this many of the
+                            finest levels, grid-stride kernels below (default 0: every level whose
+                            rows fit a slab) */
 } dpf_options;
 
 typedef struct dpf_problem dpf_problem;

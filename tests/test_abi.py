@@ -52,6 +52,7 @@ def test_default_options(pkg, lib):
     assert o.cheb_degree == 0 and o.coarse_scale == 0.0 and o.max_coarse == 64 and o.blocks_per_sm == 16 and o.tail_cells == 4096 and o.plane == 1 and o.plane_cells == 1024
     assert o.plane_blocks_per_sm == 2 and o.df_plane_cells == -1 and o.df_plane_blocks_per_sm == 4
     assert o.tail_cluster == 1
+    assert o.plane_levels == 0
 
 
 @pytest.mark.parametrize("ns", [(4, 3, 2), (7, 1, 5), (1, 6, 3), (5, 4, 1), (9, 1, 1), (1, 1, 8), (3, 3, 3)])
