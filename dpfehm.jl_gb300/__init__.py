@@ -218,6 +218,12 @@ class GroundwaterProblem:
     def launch_count(self):
         return int(self._lib.dpf_launch_count(self._h))
 
+    def set_stream(self, stream):
+        """Issue this handle's work on `stream` (a torch.cuda.Stream, a raw cudaStream_t as an
+        int, or None for the legacy default stream)."""
+        raw = getattr(stream, "cuda_stream", stream)
+        _check(self._lib, self._h, self._lib.dpf_set_stream(self._h, ctypes.c_void_p(raw or None)))
+
     # ---- steady state
     def forward(self, Ks, dirichleths, Qs):
         K = _Buf(Ks, n=self.F)
@@ -363,7 +369,7 @@ class GroundwaterBatch(GroundwaterProblem):
 
 
 _TUNED = ("cheb_degree", "plane_cells", "plane_blocks_per_sm", "tail_cells", "blocks_per_sm", "df_plane_cells",
-          "tail_cluster", "plane_levels")
+          "tail_cluster", "plane_levels", "streams")
 
 
 def autotune_batch(dims, mins, maxs, dirichletnodes, logK, dirichleths, Qs, obs_per_problem, mean="geometric",

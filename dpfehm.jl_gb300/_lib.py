@@ -39,6 +39,7 @@ class Options(ctypes.Structure):
         ("df_plane_blocks_per_sm", ctypes.c_int),
         ("tail_cluster", ctypes.c_int),
         ("plane_levels", ctypes.c_int),
+        ("streams", ctypes.c_int),
     ]
 
 
@@ -84,6 +85,7 @@ SIGNATURES = {
                                           ctypes.POINTER(ctypes.c_longlong), _f64p,
                                           ctypes.POINTER(ctypes.c_longlong)]),
     "dpf_launch_count": (ctypes.c_longlong, [_vp]),
+    "dpf_set_stream": (ctypes.c_int, [_vp, _vp]),
     "dpf_logk_to_faces_regular_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_int,
                                                          _vp]),
     "dpf_debug_fail_alloc": (None, [ctypes.c_int64]),

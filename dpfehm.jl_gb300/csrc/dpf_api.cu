@@ -9,9 +9,13 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <functional>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "dpf_check.cuh"
@@ -20,9 +24,73 @@
 
 using namespace dpf;
 
+namespace {
+
+// Persistent workers of a batch handle split into concurrent parts: run(f) calls f(i) for
+// every part i, f(0) on the calling thread and f(1..n-1) on the workers, and returns when
+// all have returned. Each worker has made the handle's device current.
+class PartPool {
+public:
+    PartPool(int n, int device) : n_(n) {
+        for (int i = 1; i < n; i++)
+            th_.emplace_back([this, i, device]() {
+                cudaSetDevice(device);
+                unsigned long long seen = 0;
+                for (;;) {
+                    std::function<void(int)> job;
+                    {
+                        std::unique_lock<std::mutex> lk(m_);
+                        cv_.wait(lk, [&]() { return stop_ || gen_ != seen; });
+                        if (stop_) return;
+                        seen = gen_;
+                        job = job_;
+                    }
+                    job(i);
+                    {
+                        std::lock_guard<std::mutex> lk(m_);
+                        if (--pending_ == 0) done_.notify_all();
+                    }
+                }
+            });
+    }
+    ~PartPool() {
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : th_) t.join();
+    }
+    void run(const std::function<void(int)> &f) {
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            job_ = f;
+            pending_ = n_ - 1;
+            gen_++;
+        }
+        cv_.notify_all();
+        f(0);
+        std::unique_lock<std::mutex> lk(m_);
+        done_.wait(lk, [&]() { return pending_ == 0; });
+    }
+
+private:
+    int n_;
+    std::vector<std::thread> th_;
+    std::mutex m_;
+    std::condition_variable cv_, done_;
+    std::function<void(int)> job_;
+    unsigned long long gen_ = 0;
+    int pending_ = 0;
+    bool stop_ = false;
+};
+
+}  // namespace
+
 struct dpf_problem {
     int device = 0;
     cudaStream_t stream = 0;
+    bool own_stream = false;           // a part's stream, created and destroyed with it
     dpf_options opt;
     std::unique_ptr<StructBatch> sb;   // structured path (one problem or a batch)
     std::unique_ptr<GeneralSolver> gs; // CSR path
@@ -32,8 +100,24 @@ struct dpf_problem {
     double *tr_b0 = nullptr, *tr_ck_states = nullptr, *tr_seg = nullptr, *tr_Ss = nullptr;
     double tr_dt = 0;
     std::vector<void *> scratch;       // device scratch owned by the handle
+    // a batch split into concurrent parts (options.streams): each part is a complete batch
+    // handle over consecutive problems, on its own stream, driven by its own host thread;
+    // `stream` then only orders the parts' work with the caller's stream
+    std::vector<dpf_problem *> parts;
+    std::vector<int> part_first;       // first problem of each part, and the problem count last
+    std::vector<cudaEvent_t> part_events;
+    std::unique_ptr<PartPool> pool;
     ~dpf_problem() {
+        pool.reset();
+        for (dpf_problem *q : parts) delete q;
+        for (cudaEvent_t e : part_events) cudaEventDestroy(e);
+        sb.reset();
+        gs.reset();
         for (void *p : scratch) dev_free(p);
+        if (own_stream && stream) {
+            cudaStreamSynchronize(stream);
+            cudaStreamDestroy(stream);
+        }
     }
 };
 
@@ -208,6 +292,11 @@ int check_device() {
 template <typename F>
 int guarded(dpf_problem *P, const char *name, F &&f) {
     if (!P) return DPF_BAD_INPUT;
+    if (!P->parts.empty()) {
+        P->err = std::string(name) + " is not available on a batch handle split into concurrent parts "
+                                     "(create it with streams = 1)";
+        return DPF_UNSUPPORTED;
+    }
     NvtxRange range(name);
     DeviceGuard g(P->device);
     try {
@@ -288,7 +377,18 @@ dpf_options fill_options(const dpf_options *o) {
     if (r.tail_cluster <= 0) r.tail_cluster = d.tail_cluster;
     r.tail_cluster = std::min(16, r.tail_cluster);
     if (r.plane_levels < 0) r.plane_levels = d.plane_levels;
+    if (r.streams < 0) r.streams = d.streams;
     return r;
+}
+
+// The number of concurrent parts of a batch: the largest k <= the requested count (0: 4)
+// that divides the problem count, so that the parts are equal in size (a batch of identical
+// problems then gives bitwise identical results in every part).
+int batch_parts(int nprob, int streams) {
+    int want = streams > 0 ? streams : 4;
+    want = std::max(1, std::min(want, nprob));
+    while (nprob % want) want--;
+    return want;
 }
 
 int make_struct(const std::vector<GridSpec> &grids, const std::vector<std::vector<int64_t>> &dn,
@@ -302,7 +402,35 @@ int make_struct(const std::vector<GridSpec> &grids, const std::vector<std::vecto
     try {
         ck(cudaGetDevice(&P->device), "cudaGetDevice");
         P->opt = fill_options(opts);
-        P->sb.reset(new StructBatch(grids, dn, P->opt, P->stream));
+        const int nprob = (int)grids.size();
+        const int k = batch_parts(nprob, P->opt.streams);
+        if (k > 1) {
+            // concurrent parts: equal runs of consecutive problems, each its own handle and stream
+            const int per = nprob / k;
+            dpf_options po = P->opt;
+            po.streams = 1;
+            for (int i = 0; i < k; i++) {
+                auto Q = new dpf_problem();
+                P->parts.push_back(Q);  // owned by P from here on (deleted with it on any error)
+                Q->device = P->device;
+                Q->opt = po;
+                ck(cudaStreamCreateWithFlags(&Q->stream, cudaStreamNonBlocking), "part stream");
+                Q->own_stream = true;
+                std::vector<GridSpec> g(grids.begin() + i * per, grids.begin() + (i + 1) * per);
+                std::vector<std::vector<int64_t>> d(dn.begin() + i * per, dn.begin() + (i + 1) * per);
+                Q->sb.reset(new StructBatch(g, d, Q->opt, Q->stream));
+                P->part_first.push_back(i * per);
+            }
+            P->part_first.push_back(nprob);
+            for (int i = 0; i <= k; i++) {
+                cudaEvent_t e;
+                ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "part event");
+                P->part_events.push_back(e);
+            }
+            P->pool.reset(new PartPool(k, P->device));
+        } else {
+            P->sb.reset(new StructBatch(grids, dn, P->opt, P->stream));
+        }
     } catch (const DpfError &e) {
         g_create_error = e.what();
         delete P;
@@ -341,6 +469,7 @@ void dpf_default_options(dpf_options *o) {
     o->df_plane_blocks_per_sm = 4;
     o->tail_cluster = 1;
     o->plane_levels = 0;
+    o->streams = 0;
 }
 
 int dpf_detect_regular3d(int64_t N, int64_t F, const int64_t *a, const int64_t *b, const double *aol, int *dims,
@@ -498,6 +627,22 @@ const char *dpf_last_error(const dpf_problem *P) {
 
 int dpf_info(const dpf_problem *P, int64_t *N, int64_t *F, int64_t *nfree, int *structured, int *levels) {
     if (!P) return DPF_BAD_INPUT;
+    if (!P->parts.empty()) {
+        int64_t n = 0, f = 0, nf = 0;
+        int lv = 0;
+        for (const dpf_problem *Q : P->parts) {
+            n += Q->sb->N;
+            f += Q->sb->F;
+            nf += Q->sb->nfree_total;
+            lv = std::max(lv, Q->sb->nlev_max);
+        }
+        if (N) *N = n;
+        if (F) *F = f;
+        if (nfree) *nfree = nf;
+        if (structured) *structured = 1;
+        if (levels) *levels = lv;
+        return DPF_OK;
+    }
     if (P->sb) {
         if (N) *N = P->sb->N;
         if (F) *F = P->sb->F;
@@ -516,6 +661,19 @@ int dpf_info(const dpf_problem *P, int64_t *N, int64_t *F, int64_t *nfree, int *
 
 int dpf_last_stats(const dpf_problem *P, int *iterations, int *outer, double *relres) {
     if (!P) return DPF_BAD_INPUT;
+    if (!P->parts.empty()) {
+        int it = 0, ou = 0;
+        double rr = 0.0;
+        for (const dpf_problem *Q : P->parts) {
+            it = std::max(it, Q->sb->stats_iters);
+            ou = std::max(ou, Q->sb->stats_outer);
+            rr = std::max(rr, Q->sb->stats_relres);
+        }
+        if (iterations) *iterations = it;
+        if (outer) *outer = ou;
+        if (relres) *relres = rr;
+        return DPF_OK;
+    }
     if (P->sb) {
         if (iterations) *iterations = P->sb->stats_iters;
         if (outer) *outer = P->sb->stats_outer;
@@ -700,15 +858,86 @@ int dpf_solve_grad_logk(dpf_problem *P, const double *logK, int kind, const doub
     });
 }
 
+// cells and faces of the problems before part i of a split batch
+static void part_base(const dpf_problem *P, int i, int64_t &c0, int64_t &f0) {
+    c0 = f0 = 0;
+    for (int j = 0; j < i; j++) {
+        c0 += P->parts[j]->sb->N;
+        f0 += P->parts[j]->sb->F;
+    }
+}
+
 int dpf_batch_offsets(const dpf_problem *P, int p, int64_t *cell_offset, int64_t *face_offset) {
+    if (P && !P->parts.empty()) {
+        const int k = (int)P->parts.size();
+        if (p < 0 || p > P->part_first[k]) return DPF_BAD_INPUT;
+        int i = 0;
+        while (i + 1 < k && p >= P->part_first[i + 1]) i++;
+        int64_t c0, f0;
+        part_base(P, i, c0, f0);
+        const StructBatch &S = *P->parts[i]->sb;
+        if (cell_offset) *cell_offset = c0 + S.cell_off[p - P->part_first[i]];
+        if (face_offset) *face_offset = f0 + S.face_off[p - P->part_first[i]];
+        return DPF_OK;
+    }
     if (!P || !P->sb || p < 0 || p > P->sb->nprob) return DPF_BAD_INPUT;
     if (cell_offset) *cell_offset = P->sb->cell_off[p];
     if (face_offset) *face_offset = P->sb->face_off[p];
     return DPF_OK;
 }
 
+// A split batch: every part solves its problems on its own stream from its own host thread.
+// The parts start after the work already on the handle's stream and that stream continues
+// after all of them; the status is the most severe of the parts' (its part's message).
+static int split_solve_grad_logk(dpf_problem *P, const double *logK, int kind, const double *dh, const double *Qs,
+                                 const int64_t *obs_offsets, const int64_t *obs, double *h_out, double *dlogK) {
+    NvtxRange range("dpf_batch_solve_grad_logk (concurrent parts)");
+    DeviceGuard g(P->device);
+    const int k = (int)P->parts.size();
+    const int nprob = P->part_first[k];
+    if (!logK || !dh || !Qs || !obs_offsets) { P->err = "invalid arguments"; return DPF_BAD_INPUT; }
+    for (int p = 0; p < nprob; p++)
+        if (obs_offsets[p] < 0 || obs_offsets[p + 1] < obs_offsets[p]) {
+            P->err = "obs_offsets must be non-decreasing";
+            return DPF_BAD_INPUT;
+        }
+    if (cudaEventRecord(P->part_events[k], P->stream) != cudaSuccess) {
+        P->err = std::string("event record: ") + cudaGetErrorString(cudaGetLastError());
+        return DPF_CUDA;
+    }
+    std::vector<int> rcs(k, DPF_OK);
+    std::vector<std::vector<int64_t>> offs(k);
+    P->pool->run([&](int i) {
+        dpf_problem *Q = P->parts[i];
+        const int p0 = P->part_first[i], p1 = P->part_first[i + 1];
+        int64_t c0, f0;
+        part_base(P, i, c0, f0);
+        offs[i].resize(p1 - p0 + 1);
+        for (int p = p0; p <= p1; p++) offs[i][p - p0] = obs_offsets[p] - obs_offsets[p0];
+        if (cudaStreamWaitEvent(Q->stream, P->part_events[k], 0) != cudaSuccess) {
+            Q->err = std::string("stream wait: ") + cudaGetErrorString(cudaGetLastError());
+            rcs[i] = DPF_CUDA;
+            return;
+        }
+        rcs[i] = dpf_batch_solve_grad_logk(Q, logK + c0, kind, dh + c0, Qs + c0, offs[i].data(),
+                                           obs ? obs + obs_offsets[p0] : nullptr, h_out ? h_out + c0 : nullptr,
+                                           dlogK ? dlogK + c0 : nullptr);
+        cudaEventRecord(P->part_events[i], Q->stream);
+    });
+    int rc = DPF_OK;
+    for (int i = 0; i < k; i++) {
+        cudaStreamWaitEvent(P->stream, P->part_events[i], 0);
+        if (rcs[i] != DPF_OK && (rc == DPF_OK || rc == DPF_NOT_CONVERGED)) {
+            rc = rcs[i];
+            P->err = P->parts[i]->err;
+        }
+    }
+    return rc;
+}
+
 int dpf_batch_solve_grad_logk(dpf_problem *P, const double *logK, int kind, const double *dh, const double *Qs,
                               const int64_t *obs_offsets, const int64_t *obs, double *h_out, double *dlogK) {
+    if (P && !P->parts.empty()) return split_solve_grad_logk(P, logK, kind, dh, Qs, obs_offsets, obs, h_out, dlogK);
     return guarded(P, __func__, [&]() -> int {
         if (!P->sb) throw BadInput("not a batch handle");
         if (!logK || !dh || !Qs || !obs_offsets) throw BadInput("invalid arguments");
@@ -895,6 +1124,8 @@ int dpf_transient_adjoint(dpf_problem *P, int64_t nobs, const int64_t *obs, cons
 int dpf_profile(dpf_problem *P, int enable) {
     if (!P) return DPF_BAD_INPUT;
     DeviceGuard g(P->device);
+    for (dpf_problem *Q : P->parts) Q->sb->profile(enable != 0);
+    if (!P->parts.empty()) return DPF_OK;
     if (P->sb) P->sb->profile(enable != 0);
     else return DPF_UNSUPPORTED;
     return DPF_OK;
@@ -905,6 +1136,34 @@ int dpf_profile_report(dpf_problem *P, int cap, const char **names, long long *l
     if (!P) return -DPF_BAD_INPUT;
     DeviceGuard g(P->device);
     try {
+        if (!P->parts.empty()) {
+            // the parts' reports merged by kernel name
+            std::vector<const char *> nm;
+            std::vector<long long> cnt, cl;
+            std::vector<double> tot;
+            for (dpf_problem *Q : P->parts) {
+                const int n = Q->sb->profile_report(0, nullptr, nullptr, nullptr, nullptr);
+                std::vector<const char *> qn(n);
+                std::vector<long long> qc(n), qcl(n);
+                std::vector<double> qm(n);
+                Q->sb->profile_report(n, qn.data(), qc.data(), qm.data(), qcl.data());
+                for (int j = 0; j < n; j++) {
+                    size_t t = 0;
+                    while (t < nm.size() && std::strcmp(nm[t], qn[j]) != 0) t++;
+                    if (t == nm.size()) { nm.push_back(qn[j]); cnt.push_back(0); tot.push_back(0.0); cl.push_back(0); }
+                    cnt[t] += qc[j];
+                    tot[t] += qm[j];
+                    cl[t] += qcl[j];
+                }
+            }
+            for (size_t t = 0; t < nm.size() && (int)t < cap; t++) {
+                if (names) names[t] = nm[t];
+                if (launches) launches[t] = cnt[t];
+                if (ms) ms[t] = tot[t];
+                if (cells) cells[t] = cl[t];
+            }
+            return (int)nm.size();
+        }
         if (P->sb) return P->sb->profile_report(cap, names, launches, ms, cells);
         return 0;
     } catch (const DpfError &e) {
@@ -913,8 +1172,26 @@ int dpf_profile_report(dpf_problem *P, int cap, const char **names, long long *l
     }
 }
 
+int dpf_set_stream(dpf_problem *P, void *stream) {
+    if (!P) return DPF_BAD_INPUT;
+    DeviceGuard g(P->device);
+    if (cudaStreamSynchronize(P->stream) != cudaSuccess) {
+        P->err = std::string("stream synchronize: ") + cudaGetErrorString(cudaGetLastError());
+        return DPF_CUDA;
+    }
+    P->stream = (cudaStream_t)stream;
+    if (P->sb) P->sb->stream = P->stream;
+    if (P->gs) P->gs->set_stream(P->stream);
+    return DPF_OK;
+}
+
 long long dpf_launch_count(const dpf_problem *P) {
     if (!P) return -1;
+    if (!P->parts.empty()) {
+        long long n = 0;
+        for (const dpf_problem *Q : P->parts) n += Q->sb->launches;
+        return n;
+    }
     if (P->sb) return P->sb->launches;
     return P->gs ? P->gs->launches : 0;
 }

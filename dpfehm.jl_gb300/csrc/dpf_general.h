@@ -38,6 +38,7 @@ public:
     GeneralSolver &operator=(const GeneralSolver &) = delete;
 
     int forward(const double *Ks, const double *logK, int kind, const double *dh, const double *Qs, double *h_out);
+    void set_stream(cudaStream_t s) { stream = s; }
     int adjoint(const double *delta, double *dKs, double *dlogK, double *ddh, double *dQs);
     int logk_to_faces(const double *logK, int kind, double *Ks);
     int logk_vjp(const double *logK, int kind, const double *dKs, double *dlogK);

@@ -116,6 +116,7 @@ extern "C" int dpf_batch_autotune(int nprob, const int *dims, const double *mins
             {&cur.df_plane_cells, {-1, 512}, mixed},
             {&cur.tail_cluster, {1, 8}, true},
             {&cur.plane_levels, {0, 1, 2}, mixed},
+            {&cur.streams, {1, 2, 4}, true},
         };
         for (const Knob &k : knobs) {
             if (!k.active) continue;

@@ -94,6 +94,12 @@ typedef struct dpf_options {
     int plane_levels;    /* regular grids, MIXED: the plane-marching kernels run on this many of the
                             finest levels, grid-stride kernels below (default 0: every level whose
                             rows fit a slab) */
+    int streams;         /* batches: the problems run as this many equal concurrent parts, each on its
+                            own stream and host thread, so that one part's bandwidth-bound kernels
+                            overlap another's latency-bound small levels (default 0: up to 4; the
+                            largest count not above the request that divides the problem count).
+                            A split batch handle serves dpf_batch_solve_grad_logk and the query,
+                            profiling and stream entry points; others return DPF_UNSUPPORTED. */
 } dpf_options;
 
 typedef struct dpf_problem dpf_problem;
@@ -232,6 +238,12 @@ int dpf_profile_report(dpf_problem *h, int cap, const char **names, long long *l
 
 /* Kernel launches issued by the handle since it was created. */
 long long dpf_launch_count(const dpf_problem *h);
+
+/* No counterpart in the reference. Issue the handle's work on `stream`, a cudaStream_t of
+ * the handle's device (NULL: the legacy default stream, the default). Work already issued
+ * is completed first. Every entry point still returns when its results are complete;
+ * handles on different streams, driven from different host threads, run concurrently. */
+int dpf_set_stream(dpf_problem *h, void *stream);
 
 /* ------------------------------------------------------ allocation-free path */
 

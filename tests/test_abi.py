@@ -53,6 +53,7 @@ def test_default_options(pkg, lib):
     assert o.plane_blocks_per_sm == 2 and o.df_plane_cells == -1 and o.df_plane_blocks_per_sm == 4
     assert o.tail_cluster == 1
     assert o.plane_levels == 0
+    assert o.streams == 0
 
 
 @pytest.mark.parametrize("ns", [(4, 3, 2), (7, 1, 5), (1, 6, 3), (5, 4, 1), (9, 1, 1), (1, 1, 8), (3, 3, 3)])
