@@ -302,9 +302,11 @@ def profile_pass(pkg, torch, dev, B, N, prec, args, tuned=None):
     dh = np.zeros(B * N)
     obs = [np.arange(0, N, N // NOBS)[:NOBS]] * B
     # per-kernel events need a saturated stream: convergence is read back every 4
-    # iterations here so the host stays ahead of the GPU (graphs are off while profiling)
+    # iterations here so the host stays ahead of the GPU (graphs are off while profiling);
+    # the whole batch runs on one stream, so no other part's kernels overlap a timed launch
+    opts = dict(tuned or {}, streams=1)
     b = pkg.GroundwaterBatch([GRID] * B, [MINS] * B, [MAXS] * B, [[N - 1]] * B, reltol=RELTOL, precision=prec,
-                             check_every=4, **(tuned or {}))
+                             check_every=4, **opts)
     d = [torch.tensor(x, device=dev) for x in (logK, dh, Qs)]
     b.solve_grad_logk(*d, obs)
     b.profile(True)
@@ -342,7 +344,7 @@ def profile_pass(pkg, torch, dev, B, N, prec, args, tuned=None):
         "top": [{"kernel": k, "launches": v[0], "ms": round(v[1], 3),
                  "GBps": round(BYTES_PER_CELL[k.split("<")[0]](4 if "<f32>" in k else 8) * v[2] / (v[1] / 1e3) / 1e9, 1)
                  if k.split("<")[0] in BYTES_PER_CELL and v[1] > 0 else None} for k, v in top[:8]],
-        "measured": "per-kernel CUDA events on the solver stream over %d forward+adjoint steps of the same workload"
+        "measured": "per-kernel CUDA events on the solver stream over %d forward+adjoint steps of the same workload (the batch on one stream)"
                     % max(1, min(args.steps, 3)),
     }
 

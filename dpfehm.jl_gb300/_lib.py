@@ -9,7 +9,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libdpfehm_gpu.so")
 
-DPF_OK, DPF_BAD_INPUT, DPF_NOT_CONVERGED, DPF_NAN, DPF_OOM, DPF_CUDA, DPF_NO_DEVICE, DPF_STATE, DPF_UNSUPPORTED = range(9)
+DPF_OK, DPF_BAD_INPUT, DPF_NOT_CONVERGED, DPF_NAN, DPF_OOM, DPF_CUDA, DPF_NO_DEVICE, DPF_STATE, DPF_UNSUPPORTED, DPF_TIMEOUT = range(10)
 STATUS_NAMES = {
     0: "DPF_OK", 1: "DPF_BAD_INPUT", 2: "DPF_NOT_CONVERGED", 3: "DPF_NAN", 4: "DPF_OOM", 5: "DPF_CUDA",
     6: "DPF_NO_DEVICE", 7: "DPF_STATE", 8: "DPF_UNSUPPORTED", 9: "DPF_TIMEOUT",

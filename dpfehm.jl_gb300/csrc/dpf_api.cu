@@ -922,11 +922,17 @@ static int split_solve_grad_logk(dpf_problem *P, const double *logK, int kind, c
         rcs[i] = dpf_batch_solve_grad_logk(Q, logK + c0, kind, dh + c0, Qs + c0, offs[i].data(),
                                            obs ? obs + obs_offsets[p0] : nullptr, h_out ? h_out + c0 : nullptr,
                                            dlogK ? dlogK + c0 : nullptr);
-        cudaEventRecord(P->part_events[i], Q->stream);
+        if (cudaEventRecord(P->part_events[i], Q->stream) != cudaSuccess) {
+            Q->err = std::string("event record: ") + cudaGetErrorString(cudaGetLastError());
+            if (rcs[i] == DPF_OK || rcs[i] == DPF_NOT_CONVERGED) rcs[i] = DPF_CUDA;
+        }
     });
     int rc = DPF_OK;
     for (int i = 0; i < k; i++) {
-        cudaStreamWaitEvent(P->stream, P->part_events[i], 0);
+        if (cudaStreamWaitEvent(P->stream, P->part_events[i], 0) != cudaSuccess) {
+            P->err = std::string("stream wait: ") + cudaGetErrorString(cudaGetLastError());
+            rc = DPF_CUDA;
+        }
         if (rcs[i] != DPF_OK && (rc == DPF_OK || rc == DPF_NOT_CONVERGED)) {
             rc = rcs[i];
             P->err = P->parts[i]->err;

@@ -12,7 +12,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
+#include <mutex>
 #include <set>
 #include <stdexcept>
 
@@ -1149,6 +1151,8 @@ static void ck(cudaError_t e, const char *what) {
 #define CK(x) ck((x), #x)
 #define LAUNCH_CHECK() ck(cudaGetLastError(), "kernel launch")
 
+static void configure_plane_kernels();
+
 // Launch with programmatic stream serialization: the launch is prepared while the previous
 // kernel on the stream runs and its blocks start as that kernel's blocks exit; each solver
 // kernel's pdl_enter() waits for the previous kernel's completion and memory before it
@@ -1165,8 +1169,23 @@ static void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cfg.attrs = at;
-    cfg.numAttrs = 1;
-    ck(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...), "kernel launch");
+#ifndef DPF_PDL
+#define DPF_PDL 1
+#endif
+    cfg.numAttrs = DPF_PDL;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        const char *name = nullptr;
+        if (cudaFuncGetName(&name, (const void *)kernel) != cudaSuccess) {
+            cudaGetLastError();
+            name = "?";
+        }
+        throw CudaError(std::string("kernel launch (") + name + ", grid " + std::to_string(grid.x) + ", block " +
+                            std::to_string(block.x) + ", dynamic shared " + std::to_string(smem) +
+                            " B): " + cudaGetErrorString(e),
+                        e);
+    }
 }
 
 template <typename T>
@@ -1360,6 +1379,7 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         L.smooth = build_map(L.h_desc, smooth, owned, nprob, target_blocks);
         L.restr = build_map(L.h_desc, restr, owned, nprob, target_blocks);
         const bool plane_here = opt.plane > 0 && (opt.plane_levels <= 0 || l < opt.plane_levels);
+        if (mixed && l == 0) configure_plane_kernels();
         build_plane_items(L.pm, L, smooth, sms, plane_here ? opt.plane_cells : 0, opt.plane_blocks_per_sm, &shapes,
                           l);
         if (l == 0) build_plane_items(L.pa, L, has, sms, opt.df_plane_cells, opt.df_plane_blocks_per_sm, nullptr, l);
@@ -1489,10 +1509,14 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
     CK(cudaDeviceSynchronize());
 }
 
-// Stable names "kernel<f64|f32>/L<level>" for the per-kernel timing report.
+// Stable names "kernel<f64|f32>/L<level>" for the per-kernel timing report. Every launch asks
+// for its name, from the host threads of all the handles (and of a batch's concurrent parts)
+// at once, so the shared set is guarded.
 const char *kname(const char *base, int level, bool fp32) {
+    static std::mutex mu;
     static std::set<std::string> names;
     std::string n = std::string(base) + (fp32 ? "<f32>" : "<f64>") + "/L" + std::to_string(level);
+    std::lock_guard<std::mutex> lk(mu);
     return names.insert(n).first->c_str();
 }
 
@@ -1623,16 +1647,56 @@ void StructBatch::assemble(const double *Ks, const double *kc, int kind, const d
 // ---- plane-marching launches
 static int pm_region(int count, int es) { return ((count * es + 32) + 15) & ~15; }
 
+// The plane kernels' dynamic shared memory limit is raised once per device, before any of
+// them is launched, to all that a block may hold beside its static shared memory. The
+// attribute is then never changed while kernels of another handle, or of another part of a
+// split batch on another host thread, run or are being captured into a graph.
+template <int MODE>
+static void raise_pm_cheb(const std::function<void(const void *)> &raise) {
+    raise((const void *)k_pm_cheb<float, MODE, 1>);
+    raise((const void *)k_pm_cheb<float, MODE, 2>);
+    raise((const void *)k_pm_cheb<float, MODE, 3>);
+    raise((const void *)k_pm_cheb<float, MODE, 4>);
+}
+
+static void configure_plane_kernels() {
+    static std::mutex mu;
+    static std::set<int> done;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count(dev)) return;
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const std::function<void(const void *)> raise = [&](const void *f) {
+        cudaFuncAttributes a;
+        CK(cudaFuncGetAttributes(&a, f));
+        CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)a.sharedSizeBytes));
+    };
+    raise_pm_cheb<PM_FIRST2>(raise);
+    raise_pm_cheb<PM_FIRST2 | PM_NOD>(raise);
+    raise_pm_cheb<0>(raise);
+    raise_pm_cheb<PM_NOD>(raise);
+    raise_pm_cheb<PM_PROLONG | PM_FIRST>(raise);
+    raise_pm_cheb<PM_PROLONG | PM_FIRST | PM_NOD>(raise);
+    raise_pm_cheb<PM_PROLONG | PM_FIRST | PM_NOD | PM_RZ>(raise);
+    raise_pm_cheb<PM_NOD | PM_RZ>(raise);
+    raise((const void *)k_pm_restrict<float, 1>);
+    raise((const void *)k_pm_restrict<float, 2>);
+    raise((const void *)k_pm_restrict<float, 3>);
+    raise((const void *)k_pm_restrict<float, 4>);
+    raise((const void *)k_pm_df_spmv<1>);
+    raise((const void *)k_pm_df_spmv<2>);
+    raise((const void *)k_pm_df_spmv<3>);
+    raise((const void *)k_pm_df_spmv<4>);
+    done.insert(dev);
+}
+
 template <typename T, int MODE, int CPT>
 static void pm_kernel(unsigned nblocks, size_t smem, cudaStream_t stream, const LevelDesc *desc,
                       const LevelDesc *cdesc, const int4 *items, CgState *st, Coeffs<T> C, const T *b,
                       const T *xin, T *xout, T *d, const uint8_t *dir, const T *e, T c1, T c2, T invth, T sc,
                       PlaneLayout lay, ReduceScratch rs, const int2 *pinfo, int *err) {
-    static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        CK(cudaFuncSetAttribute(k_pm_cheb<T, MODE, CPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = smem;
-    }
     launch_pdl(k_pm_cheb<T, MODE, CPT>, nblocks, kPlaneThreads + 32, smem, stream, desc, cdesc, items, st, C, b, xin, xout, d,
                                                                        dir, e, c1, c2, invth, sc, lay, rs, pinfo, err);
 }
@@ -1715,11 +1779,6 @@ template <typename T, int CPT>
 static void pm_restrict_kernel(unsigned nblocks, size_t smem, cudaStream_t stream, const LevelDesc *desc,
                                const LevelDesc *cdesc, const int4 *items, const CgState *st, Coeffs<T> C, const T *b,
                                const T *x, T *bc, PlaneLayout lay, int *err) {
-    static size_t configured = 0;
-    if (smem > 48 * 1024 - 2 * CPT * kPlaneThreads * sizeof(T) && smem > configured) {
-        CK(cudaFuncSetAttribute(k_pm_restrict<T, CPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = smem;
-    }
     launch_pdl(k_pm_restrict<T, CPT>, nblocks, kPlaneThreads + 32, smem, stream, desc, cdesc, items, st, C, b, x, bc, lay, err);
 }
 
@@ -2034,11 +2093,6 @@ template <int CPT>
 static void pm_df_kernel(unsigned nblocks, size_t smem, cudaStream_t stream, const LevelDesc *desc, const int4 *items,
                          CgState *st, int *count, ReduceScratch rs, const int2 *pinfo, CoeffsDF C, const float2 *pv,
                          float2 *q, PlaneLayout lay, int *err) {
-    static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        CK(cudaFuncSetAttribute(k_pm_df_spmv<CPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = smem;
-    }
     launch_pdl(k_pm_df_spmv<CPT>, nblocks, kPlaneThreads + 32, smem, stream, desc, items, st, count, rs, pinfo, C, pv, q, lay,
                                                                      err);
 }

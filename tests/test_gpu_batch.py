@@ -167,3 +167,49 @@ def test_cluster_tail_agrees(gpu_lib, precision):
         res.append(B.solve_grad_logk(cat("logK"), cat("dh"), cat("Qs"), [p["obs"] for p in probs]))
     for h, g in res[1:]:
         assert rel(h, res[0][0]) < 1e-11 and rel(g, res[0][1]) < 1e-9
+
+
+def test_concurrent_parts_agree_with_one_stream(gpu_lib):
+    """A batch split into concurrent parts (each on its own stream and host thread) gives the
+    single-stream solution, the same offsets and merged statistics and profiles."""
+    pkg = gpu_lib
+    shapes = [(20, 16, 5), (9, 9, 9), (40, 30, 6), (17, 5, 11)]
+    probs = [_problem(pkg, ns, 81 + k) for k, ns in enumerate(shapes)]
+    cat = lambda k: np.concatenate([p[k] for p in probs])
+    args = ([p["ns"] for p in probs], [p["mins"] for p in probs], [p["maxs"] for p in probs],
+            [p["dn"] for p in probs])
+    res = {}
+    for streams in (1, 2, 4):
+        B = pkg.GroundwaterBatch(*args, reltol=1e-12, precision="mixed", streams=streams)
+        n0 = B.launch_count
+        B.profile(True)
+        res[streams] = B.solve_grad_logk(cat("logK"), cat("dh"), cat("Qs"), [p["obs"] for p in probs])
+        rep = B.profile_report()
+        B.profile(False)
+        assert sum(v[0] for v in rep.values()) == B.launch_count - n0 > 0
+        assert B.N == sum(p["N"] for p in probs)
+        assert list(B.cell_offsets) == list(np.cumsum([0] + [p["N"] for p in probs]))
+        assert B.stats["iterations"] > 0
+        if streams > 1:
+            with pytest.raises(pkg.DPFError) as e:
+                B.forward_logk(cat("logK"), cat("dh"), cat("Qs"))
+            assert e.value.code == pkg._lib.DPF_UNSUPPORTED
+        B.close()
+    h1, g1 = res[1]
+    for s in (2, 4):
+        h, g = res[s]
+        assert rel(h, h1) < 1e-11 and rel(g, g1) < 1e-9, s
+
+
+def test_set_stream(gpu_lib):
+    """Work issued on a caller's stream gives the default stream's results."""
+    import torch
+    pkg = gpu_lib
+    c = _problem(pkg, (18, 14, 6), 31)
+    P = pkg.GroundwaterProblem.regular3d(c["mins"], c["maxs"], c["ns"], c["dn"], reltol=1e-11, precision="mixed")
+    h0, g0 = P.solve_grad_logk(c["logK"], c["dh"], c["Qs"], c["obs"])
+    s = torch.cuda.Stream()
+    P.set_stream(s)
+    h1, g1 = P.solve_grad_logk(c["logK"], c["dh"], c["Qs"], c["obs"])
+    P.set_stream(None)
+    assert np.array_equal(h0, h1) and np.array_equal(g0, g1)
