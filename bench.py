@@ -188,8 +188,11 @@ def run_ours(args, dist, rank, ws):
         tuned, tune_ms = pkg.autotune_batch([GRID] * B, [MINS] * B, [MAXS] * B, [[N - 1]] * B, logK, dh, Qs, obs,
                                             repeats=2, reltol=RELTOL, precision=prec)
         tune_s = time.perf_counter() - t0
+    opts = dict(tuned)
+    if args.streams > 0:
+        opts["streams"] = args.streams
     batch = pkg.GroundwaterBatch([GRID] * B, [MINS] * B, [MAXS] * B, [[N - 1]] * B, reltol=RELTOL, precision=prec,
-                                 use_graphs=0 if args.no_graphs else 1, **tuned)
+                                 use_graphs=0 if args.no_graphs else 1, **opts)
     d_logK = torch.tensor(logK, device=dev)
     d_dh = torch.tensor(dh, device=dev)
     d_Qs = torch.tensor(Qs, device=dev)
@@ -458,6 +461,9 @@ def main():
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch the CG loop from the host (ncu cannot profile kernels inside conditional graphs)")
     ap.add_argument("--main-only", action="store_true", help="only the timed region (for profiling runs)")
+    ap.add_argument("--streams", type=int, default=0,
+                    help="concurrent parts of the batch (0: the library's choice; 1: one stream, e.g. for ncu captures "
+                         "of the batched launches)")
     ap.add_argument("--workload", default="steady_1m", choices=["steady_1m", "steady_100k", "uneven_batch", "transient", "general_1m"],
                     help="steady_1m is the headline; the others are the remaining configurations (bench_workloads.py)")
     args = ap.parse_args()
