@@ -30,7 +30,7 @@ __all__ = [
     "GroundwaterBatch", "DPFError", "NoTangent", "getfreenodes", "addboundaryconditions", "regulargrid1d",
     "regulargrid2d", "regulargrid3d", "load_uge", "fields", "grid", "load", "default_options", "MEAN_GEOMETRIC",
     "MEAN_HARMONIC", "PREC_FP64", "PREC_MIXED", "solvepressure", "rrule_solvepressure", "amg_solver",
-    "cholesky_solver", "autotune_batch",
+    "cholesky_solver", "autotune_batch", "richards_steadystate", "rrule_richards_steadystate",
 ]
 
 
@@ -134,7 +134,7 @@ class GroundwaterProblem:
     """
 
     def __init__(self, neighbors=None, areasoverlengths=None, dirichletnodes=(), N=None, volumes=None, _handle=None,
-                 **options):
+                 general=False, **options):
         self._lib = load()
         if _handle is not None:
             self._h = _handle
@@ -150,9 +150,10 @@ class GroundwaterProblem:
             vol = None if volumes is None else np.ascontiguousarray(volumes, dtype=np.float64)
             h = ctypes.c_void_p()
             o = _options(**options)
-            rc = self._lib.dpf_create(int(N), F, a.ctypes.data, b.ctypes.data, aol.ctypes.data,
-                                      None if vol is None else vol.ctypes.data, dn.size, dn.ctypes.data,
-                                      ctypes.byref(o), ctypes.byref(h))
+            create = self._lib.dpf_create_general if general else self._lib.dpf_create
+            rc = create(int(N), F, a.ctypes.data, b.ctypes.data, aol.ctypes.data,
+                        None if vol is None else vol.ctypes.data, dn.size, dn.ctypes.data, ctypes.byref(o),
+                        ctypes.byref(h))
             if rc != _lib.DPF_OK:
                 raise DPFError(rc, self._lib.dpf_last_error(None).decode())
             self._h = h
@@ -217,6 +218,35 @@ class GroundwaterProblem:
     @property
     def launch_count(self):
         return int(self._lib.dpf_launch_count(self._h))
+
+    # ---- Richards (face-list handles: GroundwaterProblem(..., general=True))
+    def richards_steady(self, psi0, Ks, dirichletpsis, z, alphas, Ns, Qs, tol=1e-10, maxiter=200):
+        """The steady Richards solution psi (N) for the handle's faces (src/richards.jl:148-167);
+        z are the cell elevations (the reference's coords[3, :])."""
+        p0, K, dp, zz = _Buf(psi0, n=self.N), _Buf(Ks, n=self.F), _Buf(dirichletpsis, n=self.N), _Buf(z, n=self.N)
+        al, n_, q = _Buf(alphas, n=self.F), _Buf(Ns, n=self.F), _Buf(Qs, n=self.N)
+        psi, pp = _out(p0, self.N)
+        _check(self._lib, self._h, self._lib.dpf_richards_steady(self._h, p0.ptr, K.ptr, dp.ptr, zz.ptr, al.ptr, n_.ptr,
+                                                                 q.ptr, float(tol), int(maxiter), pp))
+        return psi
+
+    def richards_adjoint(self, delta, tol=1e-10, maxiter=200):
+        """(dKs, ddirichletpsis, dalphas, dNs, dQs) of the rrule at the last Richards solve."""
+        dl = _Buf(delta, n=self.N)
+        dK, dKp = _out(dl, self.F)
+        ddp, ddpp = _out(dl, self.N)
+        dal, dalp = _out(dl, self.F)
+        dN, dNp = _out(dl, self.F)
+        dQ, dQp = _out(dl, self.N)
+        _check(self._lib, self._h, self._lib.dpf_richards_adjoint(self._h, dl.ptr, float(tol), int(maxiter), dKp,
+                                                                  ddpp, dalp, dNp, dQp))
+        return dK, ddp, dal, dN, dQ
+
+    @property
+    def richards_stats(self):
+        it, ai, rr = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        self._lib.dpf_richards_stats(self._h, ctypes.byref(it), ctypes.byref(ai), ctypes.byref(rr))
+        return {"iterations": it.value, "adjoint_iterations": ai.value, "relres": rr.value}
 
     def set_stream(self, stream):
         """Issue this handle's work on `stream` (a torch.cuda.Stream, a raw cudaStream_t as an
@@ -514,6 +544,45 @@ def rrule_solvepressure(Ks_neighbors, neighbors, areasoverlengths, dirichletnode
 
     pullback.problem = pb.problem
     return h, pullback
+
+
+def _z_of(coords):
+    """The cell elevations: row 3 of a (3, N) coords array (src/richards.jl:105-111 use coords[3, node])."""
+    if _is_torch(coords):
+        return coords[2].contiguous()
+    c = np.asarray(coords, dtype=np.float64)
+    return np.ascontiguousarray(c[2] if c.ndim == 2 else c)
+
+
+def richards_steadystate(psi0, Ks, neighbors, areasoverlengths, dirichletnodes, dirichletpsis, coords, alphas, Ns,
+                         Qs, *, tol=1e-10, maxiter=200, **options):
+    """Drop-in for DPFEHM.richards_steadystate (src/richards.jl:148-167): the steady unsaturated
+    head psi (N) with van Genuchten kr per face (alphas, Ns), harmonic face means and gravity."""
+    N = _len(Qs)
+    P = GroundwaterProblem(neighbors, areasoverlengths, dirichletnodes, N=N, general=True, **options)
+    return P.richards_steady(psi0, Ks, dirichletpsis, _z_of(coords), alphas, Ns, Qs, tol, maxiter)
+
+
+def rrule_richards_steadystate(psi0, Ks, neighbors, areasoverlengths, dirichletnodes, dirichletpsis, coords, alphas,
+                               Ns, Qs, *, tol=1e-10, maxiter=200, **options):
+    """(psi, pullback) as ChainRulesCore.rrule(richards_steadystate, ...) (src/richards.jl:168-190):
+    pullback(delta) returns (NoTangent, dpsi0 = 0, dKs, NoTangent x3, ddirichletpsis, NoTangent,
+    dalphas, dNs, dQs)."""
+    N = _len(Qs)
+    P = GroundwaterProblem(neighbors, areasoverlengths, dirichletnodes, N=N, general=True, **options)
+    psi = P.richards_steady(psi0, Ks, dirichletpsis, _z_of(coords), alphas, Ns, Qs, tol, maxiter)
+
+    def pullback(delta):
+        dK, ddp, dal, dN, dQ = P.richards_adjoint(delta, tol, maxiter)
+        zero = dQ * 0
+        return (NoTangent, zero, dK, NoTangent, NoTangent, NoTangent, ddp, NoTangent, dal, dN, dQ)
+
+    pullback.problem = P
+    return psi, pullback
+
+
+def _len(x):
+    return x.numel() if _is_torch(x) else len(x)
 
 
 def logKs2Ks_neighbors(logKs, neighbors, mean="geometric", N=None):

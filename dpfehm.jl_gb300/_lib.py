@@ -86,6 +86,12 @@ SIGNATURES = {
                                           ctypes.POINTER(ctypes.c_longlong)]),
     "dpf_launch_count": (ctypes.c_longlong, [_vp]),
     "dpf_set_stream": (ctypes.c_int, [_vp, _vp]),
+    "dpf_create_general": (ctypes.c_int, [_i64, _i64, _vp, _vp, _vp, _vp, _i64, _vp, ctypes.POINTER(Options),
+                                          ctypes.POINTER(_vp)]),
+    "dpf_richards_steady": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int,
+                                           _vp]),
+    "dpf_richards_adjoint": (ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
+    "dpf_richards_stats": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _f64p]),
     "dpf_logk_to_faces_regular_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_int,
                                                          _vp]),
     "dpf_debug_fail_alloc": (None, [ctypes.c_int64]),

@@ -523,8 +523,24 @@ int dpf_detect_regular3d(int64_t N, int64_t F, const int64_t *a, const int64_t *
     return 0;
 }
 
+static int create_faces(int64_t N, int64_t F, const int64_t *nbr_a, const int64_t *nbr_b, const double *aol,
+                        const double *volumes, int64_t nd, const int64_t *dn, const dpf_options *opts,
+                        dpf_problem **out, bool detect_regular);
+
 int dpf_create(int64_t N, int64_t F, const int64_t *nbr_a, const int64_t *nbr_b, const double *aol,
                const double *volumes, int64_t nd, const int64_t *dn, const dpf_options *opts, dpf_problem **out) {
+    return create_faces(N, F, nbr_a, nbr_b, aol, volumes, nd, dn, opts, out, true);
+}
+
+int dpf_create_general(int64_t N, int64_t F, const int64_t *nbr_a, const int64_t *nbr_b, const double *aol,
+                       const double *volumes, int64_t nd, const int64_t *dn, const dpf_options *opts,
+                       dpf_problem **out) {
+    return create_faces(N, F, nbr_a, nbr_b, aol, volumes, nd, dn, opts, out, false);
+}
+
+static int create_faces(int64_t N, int64_t F, const int64_t *nbr_a, const int64_t *nbr_b, const double *aol,
+                        const double *volumes, int64_t nd, const int64_t *dn, const dpf_options *opts,
+                        dpf_problem **out, bool detect_regular) {
     if (!out || N <= 0 || F < 0 || nd < 0 || (F > 0 && (!nbr_a || !nbr_b || !aol)) || (nd > 0 && !dn)) {
         g_create_error = "invalid arguments";
         return DPF_BAD_INPUT;
@@ -544,7 +560,7 @@ int dpf_create(int64_t N, int64_t F, const int64_t *nbr_a, const int64_t *nbr_b,
     bool uniform_vol = true;
     if (volumes)
         for (int64_t i = 1; i < N; i++) if (volumes[i] != volumes[0]) { uniform_vol = false; break; }
-    if (uniform_vol && dpf_detect_regular3d(N, F, nbr_a, nbr_b, aol, dims, aol3)) {
+    if (detect_regular && uniform_vol && dpf_detect_regular3d(N, F, nbr_a, nbr_b, aol, dims, aol3)) {
         GridSpec g;
         for (int k = 0; k < 3; k++) { g.n[k] = dims[k]; g.mins[k] = 0; g.maxs[k] = dims[k] - 1; g.aol[k] = aol3[k]; }
         g.aol_override = true;
@@ -1176,6 +1192,44 @@ int dpf_profile_report(dpf_problem *P, int cap, const char **names, long long *l
         P->err = e.what();
         return -e.code;
     }
+}
+
+// ------------------------------------------------------------- Richards (face-list handles)
+int dpf_richards_steady(dpf_problem *P, const double *psi0, const double *Ks, const double *dirichletpsis,
+                        const double *z, const double *alphas, const double *Ns, const double *Qs, double tol,
+                        int maxiter, double *psi_out) {
+    return guarded(P, __func__, [&]() -> int {
+        if (!P->gs) {
+            P->err = "the Richards solver runs on face-list handles (dpf_create_general)";
+            return DPF_UNSUPPORTED;
+        }
+        if (!psi0 || !Ks || !dirichletpsis || !z || !alphas || !Ns || !Qs || !psi_out) throw BadInput("invalid arguments");
+        if (!(tol > 0)) tol = 1e-10;
+        if (maxiter <= 0) maxiter = 200;
+        return gs_status(P, P->gs->richards_steady(psi0, Ks, dirichletpsis, z, alphas, Ns, Qs, tol, maxiter, psi_out));
+    });
+}
+
+int dpf_richards_adjoint(dpf_problem *P, const double *delta, double tol, int maxiter, double *dKs, double *ddpsi,
+                         double *dalphas, double *dNs, double *dQs) {
+    return guarded(P, __func__, [&]() -> int {
+        if (!P->gs) {
+            P->err = "the Richards solver runs on face-list handles (dpf_create_general)";
+            return DPF_UNSUPPORTED;
+        }
+        if (!delta) throw BadInput("delta is required");
+        if (!(tol > 0)) tol = 1e-10;
+        if (maxiter <= 0) maxiter = 200;
+        return gs_status(P, P->gs->richards_adjoint(delta, tol, maxiter, dKs, ddpsi, dalphas, dNs, dQs));
+    });
+}
+
+int dpf_richards_stats(const dpf_problem *P, int *iterations, int *adjoint_iterations, double *relres) {
+    if (!P || !P->gs) return DPF_BAD_INPUT;
+    if (iterations) *iterations = P->gs->rich_iters;
+    if (adjoint_iterations) *adjoint_iterations = P->gs->rich_adj_iters;
+    if (relres) *relres = P->gs->rich_relres;
+    return DPF_OK;
 }
 
 int dpf_set_stream(dpf_problem *P, void *stream) {

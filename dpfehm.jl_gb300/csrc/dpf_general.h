@@ -50,6 +50,15 @@ public:
     int transient_adjoint(long long nobs, const int64_t *obs, const double *w, const double *gT, double *dKs,
                           double *ddh, double *dQs, double *dh0);
     int nlevels() const { return (int)lv.size(); }
+    // steady Richards equation (dpf_richards.cu): Picard iteration to `tol` (relative residual),
+    // and the adjoint fixed point for the reference rrule's tangents
+    int richards_steady(const double *psi0, const double *Ks, const double *dpsi, const double *z,
+                        const double *alphas, const double *Ns, const double *Qs, double tol, int maxit,
+                        double *psi_out);
+    int richards_adjoint(const double *delta, double tol, int maxit, double *dKs, double *ddpsi, double *dalphas,
+                         double *dNs, double *dQs);
+    int rich_iters = 0, rich_adj_iters = 0;
+    double rich_relres = 0.0;
 
     long long N = 0, F = 0, nfree = 0;
     int stats_iters = 0, stats_outer = 0;
@@ -77,6 +86,8 @@ private:
     void to_dev(void *dst, const void *src, size_t bytes);
     void from_dev(void *dst, const void *src, size_t bytes);
     const double *stage(const double *src, size_t n, double *dst);
+    void richards_buffers();
+    int richards_spd_solve(const double *rhs_dev, double *x_dev);
 
     dpf_options opt;
     cudaStream_t stream;
@@ -112,6 +123,15 @@ private:
     std::vector<double> cheb_c1, cheb_c2;
     std::vector<double> cheb8_c1, cheb8_c2;  // degree-8 sweep standing in for a coarsest solve
     std::vector<int> hrp_, hci_;             // finest couplings on the host (hierarchy set-up)
+    // Richards: psi, residual, step, adjoint mu, z, Dirichlet psi, zeros, sources, delta (N);
+    // Ks, alphas, Ns, Picard conductances, Jacobian parts, gradients (F); reduction partials
+    double *rc_psi = nullptr, *rc_R = nullptr, *rc_d = nullptr, *rc_mu = nullptr, *rc_z = nullptr;
+    double *rc_dpsi = nullptr, *rc_zero = nullptr, *rc_Q = nullptr, *rc_delta = nullptr;
+    double *rc_Ks = nullptr, *rc_al = nullptr, *rc_N = nullptr, *rc_Kh = nullptr, *rc_na = nullptr, *rc_nb = nullptr;
+    double *rc_gK = nullptr, *rc_ga = nullptr, *rc_gN = nullptr;
+    double2 *rc_part = nullptr;
+    std::vector<double *> rc_V;    // GMRES basis of the Richards adjoint
+    bool have_richards = false;
     // bookkeeping
     bool have_forward = false;
     int fwd_kind = 0, mean_kind = 0;

@@ -156,4 +156,63 @@ function ChainRulesCore.rrule(::typeof(groundwater_steadystate), Ks, neighbors, 
     return h, pullback
 end
 
+"""A face-list handle on the CSR path (the Richards solver needs one)."""
+function GeneralProblem(neighbors, areasoverlengths, dirichletnodes, N; volumes=nothing, kwargs...)
+    F = length(neighbors)
+    a = Int64[p[1] - 1 for p in neighbors]
+    b = Int64[p[2] - 1 for p in neighbors]
+    aol = Vector{Float64}(areasoverlengths[1:F])
+    dn = Int64[d - 1 for d in dirichletnodes]
+    vol = volumes === nothing ? Ptr{Float64}(C_NULL) : Vector{Float64}(volumes)
+    opts = default_options(; kwargs...)
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    rc = ccall((:dpf_create_general, libdpf), Cint,
+        (Int64, Int64, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Int64}, Ref{Options},
+         Ref{Ptr{Cvoid}}), N, F, a, b, aol, vol, length(dn), dn, opts, out)
+    rc == DPF_OK || error("dpf_create_general failed ($rc): $(lasterror(C_NULL))")
+    p = Problem(out[], N, F)
+    finalizer(p) do q
+        q.ptr == C_NULL || ccall((:dpf_destroy, libdpf), Cvoid, (Ptr{Cvoid},), q.ptr)
+        q.ptr = C_NULL
+    end
+    return p
+end
+
+function richards_forward(p::Problem, psi0, Ks, dirichletpsis, coords, alphas, Ns, Qs; tol=1e-10, maxiter=200)
+    psi = Vector{Float64}(undef, p.N)
+    z = Vector{Float64}(coords[3, :])
+    rc = ccall((:dpf_richards_steady, libdpf), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+         Cdouble, Cint, Ptr{Float64}), p.ptr, Vector{Float64}(psi0), Vector{Float64}(Ks),
+        Vector{Float64}(dirichletpsis), z, Vector{Float64}(alphas), Vector{Float64}(Ns), Vector{Float64}(Qs), tol, maxiter,
+        psi)
+    check(p.ptr, rc)
+    return psi
+end
+
+"""Drop-in for `DPFEHM.richards_steadystate` (src/richards.jl:148-167)."""
+richards_steadystate(psi0, Ks, neighbors, areasoverlengths, dirichletnodes, dirichletpsis, coords, alphas, Ns, Qs;
+                     tol=1e-10, maxiter=200, kwargs...) =
+    richards_forward(GeneralProblem(neighbors, areasoverlengths, dirichletnodes, length(Qs); kwargs...), psi0, Ks,
+                     dirichletpsis, coords, alphas, Ns, Qs; tol=tol, maxiter=maxiter)
+
+function ChainRulesCore.rrule(::typeof(richards_steadystate), psi0, Ks, neighbors, areasoverlengths, dirichletnodes,
+                              dirichletpsis, coords, alphas, Ns, Qs; tol=1e-10, maxiter=200, kwargs...)
+    p = GeneralProblem(neighbors, areasoverlengths, dirichletnodes, length(Qs); kwargs...)
+    psi = richards_forward(p, psi0, Ks, dirichletpsis, coords, alphas, Ns, Qs; tol=tol, maxiter=maxiter)
+    function pullback(delta)
+        dKs = Vector{Float64}(undef, p.F); dal = Vector{Float64}(undef, p.F); dN = Vector{Float64}(undef, p.F)
+        ddp = Vector{Float64}(undef, p.N); dQs = Vector{Float64}(undef, p.N)
+        rc = ccall((:dpf_richards_adjoint, libdpf), Cint,
+            (Ptr{Cvoid}, Ptr{Float64}, Cdouble, Cint, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+             Ptr{Float64}), p.ptr, Vector{Float64}(delta), tol, maxiter, dKs, ddp, dal, dN, dQs)
+        check(p.ptr, rc)
+        return (ChainRulesCore.NoTangent(), ChainRulesCore.@thunk(zeros(length(psi0))), ChainRulesCore.@thunk(dKs),
+                ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(),
+                ChainRulesCore.@thunk(ddp), ChainRulesCore.NoTangent(), ChainRulesCore.@thunk(dal),
+                ChainRulesCore.@thunk(dN), ChainRulesCore.@thunk(dQs))
+    end
+    return psi, pullback
+end
+
 end # module

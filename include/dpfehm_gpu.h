@@ -260,6 +260,36 @@ int dpf_set_stream(dpf_problem *h, void *stream);
  * dpf_last_error(NULL). */
 int dpf_logk_to_faces_regular_noalloc(int nx, int ny, int nz, const double *logK, int mean_kind, double *Ks);
 
+/* --------------------------------------------------------------- Richards */
+
+/* dpf_create on the CSR path even when the face list is a regular grid (the Richards solver
+ * and any caller that wants the general path). Same arguments and errors as dpf_create. */
+int dpf_create_general(int64_t N, int64_t F, const int64_t *nbr_a, const int64_t *nbr_b,
+                       const double *areasoverlengths, const double *volumes_or_null, int64_t nd,
+                       const int64_t *dirichletnodes, const dpf_options *opts, dpf_problem **out);
+
+/* DPFEHM.richards_steadystate (src/richards.jl:148-167) on a dpf_create_general handle: the
+ * steady Richards equation with van Genuchten relative permeability (per-face alphas[F] and
+ * Ns[F]), harmonic face means of kr and gravity through the cell elevations z[N] (the
+ * reference's coords[3, :]). psi0[N] is the initial guess; psi_out[N] carries dirichletpsis at
+ * Dirichlet cells. Solved by a Picard iteration with the handle's CG + AMG until the residual is
+ * tol (default 1e-10 when <= 0) times max(|R(psi0)|, |Qs|) or maxiter (default 200) steps
+ * (DPF_NOT_CONVERGED then). Any argument may be a host or a device pointer. */
+int dpf_richards_steady(dpf_problem *h, const double *psi0, const double *Ks, const double *dirichletpsis,
+                        const double *z, const double *alphas, const double *Ns, const double *Qs, double tol,
+                        int maxiter, double *psi_out);
+
+/* The rrule pullback of richards_steadystate (src/richards.jl:168-190) at the last solve:
+ * lambda = J^-T delta by a fixed-point iteration on the Picard operator (to relative change tol,
+ * at most maxiter steps), then dKs[F], ddirichletpsis[N], dalphas[F], dNs[F], dQs[N] (any
+ * output may be NULL; the psi0 tangent is zero). */
+int dpf_richards_adjoint(dpf_problem *h, const double *delta, double tol, int maxiter, double *dKs,
+                         double *ddirichletpsis, double *dalphas, double *dNs, double *dQs);
+
+/* Picard steps of the last Richards solve, fixed-point steps of the last adjoint, and the final
+ * relative residual. */
+int dpf_richards_stats(const dpf_problem *h, int *iterations, int *adjoint_iterations, double *relres);
+
 /* ------------------------------------------------------------ test hooks */
 
 /* No counterpart in the reference. Every device and pinned-host allocation of the

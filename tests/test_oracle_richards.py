@@ -1,0 +1,70 @@
+"""The Richards oracle (a restatement of DPFEHM src/richards.jl) pinned by finite differences:
+kr's derivatives, the Jacobian of the residual, the Newton solve and the rrule's tangents."""
+import numpy as np
+import pytest
+
+import richards_oracle as ro
+from richards_cases import oracle_args, richards_case
+
+
+def test_kr_derivatives_match_finite_differences():
+    rng = np.random.default_rng(1)
+    psi = -rng.uniform(0.05, 3.0, 50)
+    al = rng.uniform(0.2, 1.5, 50)
+    n = rng.uniform(1.1, 2.5, 50)
+    v, dp, da, dn = ro.kr(psi, al, n)
+    h = 1e-6
+    for d, args in ((dp, lambda e: (psi + e, al, n)), (da, lambda e: (psi, al + e, n)), (dn, lambda e: (psi, al, n + e))):
+        fd = (ro.kr(*args(h))[0] - ro.kr(*args(-h))[0]) / (2 * h)
+        assert np.allclose(d, fd, rtol=1e-6, atol=1e-10)
+    # saturated: kr = 1, no derivatives
+    v, dp, da, dn = ro.kr(np.array([0.0, 1.0]), 0.5, 1.5)
+    assert np.all(v == 1) and np.all(dp == 0) and np.all(da == 0) and np.all(dn == 0)
+
+
+def test_jacobian_matches_finite_differences(pkg):
+    c = richards_case(pkg, ns=(5, 4, 3))
+    psi = np.where(np.isin(np.arange(c["N"]), c["dn"]), c["dpsi"], -0.3 - 0.2 * np.random.default_rng(2).uniform(size=c["N"]))
+    args = oracle_args(c)
+    J = ro.jacobian(psi, *args).toarray()
+    free = np.setdiff1d(np.arange(c["N"]), c["dn"])
+    h = 1e-7
+    for col, k in enumerate(free[:12]):
+        e = np.zeros(c["N"]); e[k] = h
+        fd = (ro.residual(psi + e, *args) - ro.residual(psi - e, *args)) / (2 * h)
+        assert np.allclose(J[:, col], fd, rtol=1e-5, atol=1e-14 * np.abs(fd).max() + 1e-20)
+
+
+def test_newton_solve_reaches_the_root(pkg):
+    c = richards_case(pkg)
+    psi = ro.steady(c["psi0"], c["Ks"], c["nb"], c["aol"], c["dn"], c["dpsi"], c["z"], c["alphas"], c["Ns"], c["Qs"])
+    R = ro.residual(psi, *oracle_args(c))
+    assert np.linalg.norm(R) <= 1e-12 * np.linalg.norm(c["Qs"])
+    assert np.all(psi[c["dn"]] == c["dpsi"][c["dn"]])
+    assert (psi < 0).sum() > c["N"] // 4          # the unsaturated regime is exercised
+
+
+@pytest.mark.parametrize("which", ["Ks", "alphas", "Ns", "Qs", "dpsi"])
+def test_pullback_matches_finite_differences(pkg, which):
+    c = richards_case(pkg, ns=(5, 4, 4), seed=3)
+    rng = np.random.default_rng(7)
+    w = rng.standard_normal(c["N"])
+
+    def J(cc):
+        psi = ro.steady(cc["psi0"], cc["Ks"], cc["nb"], cc["aol"], cc["dn"], cc["dpsi"], cc["z"], cc["alphas"],
+                        cc["Ns"], cc["Qs"], tol=1e-14)
+        return float(w @ psi), psi
+
+    _, psi = J(c)
+    dK, ddp, dal, dN, dQ = ro.pullback(psi, w, *oracle_args(c))
+    grad = {"Ks": dK, "alphas": dal, "Ns": dN, "Qs": dQ, "dpsi": ddp}[which]
+    d = rng.standard_normal(len(c[which]))
+    if which == "dpsi":
+        d = np.where(np.isin(np.arange(c["N"]), c["dn"]), d, 0.0)
+    scale = {"Ks": 1e-3 * c["Ks"], "alphas": 1e-4 * c["alphas"], "Ns": 1e-5, "Qs": 1e-9, "dpsi": 1e-5}[which]
+    step = d * scale
+    cp, cm = dict(c), dict(c)
+    cp[which] = c[which] + step
+    cm[which] = c[which] - step
+    fd = (J(cp)[0] - J(cm)[0]) / 2
+    assert fd == pytest.approx(float(grad @ step), rel=2e-4)
