@@ -464,7 +464,8 @@ def main():
     ap.add_argument("--streams", type=int, default=0,
                     help="concurrent parts of the batch (0: the library's choice; 1: one stream, e.g. for ncu captures "
                          "of the batched launches)")
-    ap.add_argument("--workload", default="steady_1m", choices=["steady_1m", "steady_100k", "uneven_batch", "transient", "general_1m"],
+    ap.add_argument("--workload", default="steady_1m", choices=["steady_1m", "steady_100k", "uneven_batch", "transient", "general_1m",
+                                                                "richards"],
                     help="steady_1m is the headline; the others are the remaining configurations (bench_workloads.py)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

@@ -8,6 +8,7 @@ steps, L2 flushed between steps, a plain FP64 GPU run of the same workload besid
     python bench.py --workload transient       # 200x200x20, 100 backward-Euler steps of 3600 s,
                                                # Dirichlet x = max face, J = sum_t sum_50obs h^2
     python bench.py --workload general_1m      # the 1M-cell grid as a shuffled face list: CSR path
+    python bench.py --workload richards        # steady Richards, 100x100x20 unsaturated column, rrule
 
 All inputs are seeded synthetic data. One "solve" is a forward + adjoint (for the transient
 workload: the whole 100-step forward run and its adjoint).
@@ -280,9 +281,80 @@ def run_general(args, dist, rank, ws, METRIC_NAME):
     }
 
 
+def run_richards(args, dist, rank, ws, METRIC_NAME):
+    """The steady Richards equation and its rrule (DPFEHM src/richards.jl:148-190) on a
+    100x100x20 grid over 50x50x10 m: a Dirichlet top layer at psi = -2 m (an unsaturated zone above
+    the water table), a 1e-6 m^3/s source at depth (as in examples/richards_steadystate_3d),
+    Matern(l = 15 m, sigma = 1) logK, van Genuchten alpha ~ 0.375 and N ~ 1.25 per face;
+    J = sum psi^2 at 100 cells. One "solve" is the forward solve and its pullback."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    ge._load_build_module().build()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    grid, mins, maxs = (100, 100, 20), (0.0, 0.0, 0.0), (50.0, 50.0, 10.0)
+    coords, nb, aol, _ = pkg.regulargrid3d(mins, maxs, grid)
+    N, F = coords.shape[1], len(aol)
+    lk = pkg.fields.volume_logk(grid, mins, maxs, 15.0, 1.0, -9.0, 21)
+    Ks = np.exp(0.5 * (lk[nb[:, 0]] + lk[nb[:, 1]]))
+    z = coords[2]
+    dn = np.nonzero(np.isclose(z, maxs[2]))[0]
+    dpsi = np.zeros(N)
+    dpsi[dn] = -2.0
+    Qs = np.zeros(N)
+    Qs[0] = 1e-6
+    rng = np.random.default_rng(22)
+    alphas = 0.375 * np.exp(0.1 * rng.standard_normal(F))
+    Ns = 1.25 + 0.05 * rng.uniform(0, 1, F)
+    obs = rng.choice(np.setdiff1d(np.arange(N), dn), 100, replace=False)
+    delta = np.zeros(N)
+    flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float64, device=dev)
+    d = {k: torch.tensor(v, device=dev) for k, v in (("Ks", Ks), ("dpsi", dpsi), ("z", z), ("al", alphas),
+                                                   ("N", Ns), ("Q", Qs), ("psi0", np.full(N, -2.0)))}
+    import warnings
+    warnings.simplefilter("error", RuntimeWarning)
+
+    def make(prec):
+        return pkg.GroundwaterProblem(nb, aol, dn, N=N, general=True, reltol=1e-10, precision=prec)
+
+    def step(P):
+        psi = P.richards_steady(d["psi0"], d["Ks"], d["dpsi"], d["z"], d["al"], d["N"], d["Q"], 1e-10, 300)
+        dl = torch.zeros(N, dtype=torch.float64, device=dev)
+        dl[obs] = 2 * psi[obs]
+        return psi, P.richards_adjoint(dl, 1e-8, 300)
+
+    P = make(args.precision)
+    steps = max(1, args.steps // 2)
+    t = _events(torch, lambda: step(P), steps, 1, flush)
+    psi, grads = step(P)
+    st = P.richards_stats
+    P64 = make("fp64")
+    t64 = _events(torch, lambda: step(P64), 1, 1, flush)
+    psi64, g64 = step(P64)
+    return {
+        "metric": METRIC_NAME, "value": round(steps / t, 3), "unit": "solves/s", "n_gpus": ws, "steps": steps,
+        "warmup": 1, "ms_per_step": round(1e3 * t / steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64 residuals and kr; inner CG: f32 V-cycle + double-float CG" if args.precision == "mixed" else "f64",
+        "data": "synthetic (seeded Matern logK field, seeded van Genuchten parameters)",
+        "config": {"workload": "richards_steady_fwd_adj_100x100x20_unsaturated", "cells": N, "faces": F,
+                   "dirichlet": "top layer, psi = -2 m", "precision": args.precision, "tol": 1e-10,
+                   "path": "CSR (dpf_create_general)"},
+        "picard_iterations": st["iterations"], "adjoint_gmres_iterations": st["adjoint_iterations"],
+        "unsaturated_fraction": float((psi < 0).double().mean()),
+        "plain_fp64_gpu": {"value": round(1.0 / t64, 3), "unit": "solves/s"},
+        "speedup_vs_plain_fp64": round(t64 / (t / steps), 3),
+        "accuracy": {"rel_psi_err_vs_fp64": _rel(psi.cpu().numpy(), psi64.cpu().numpy()),
+                     "rel_dKs_err_vs_fp64": _rel(grads[0].cpu().numpy(), g64[0].cpu().numpy())},
+    }
+
+
 def run(name, args, dist, rank, ws):
     if rank != 0:
         return None
+    if name == "richards":
+        return run_richards(args, dist, rank, ws, "Richards steady forward+adjoint solves/sec, 200k cells")
     if name == "general_1m":
         return run_general(args, dist, rank, ws, "forward+adjoint solves/sec at 1M cells, general (CSR) path")
     if name == "transient":

@@ -74,8 +74,9 @@ __global__ void kr_faces(int F, const int *__restrict__ fa, const int *__restric
         const int a = fa[f], b = fb[f];
         const Kr ka = kr_vg(psi[a], alphas[f], Ns[f]), kb = kr_vg(psi[b], alphas[f], Ns[f]);
         const double s = ka.v + kb.v;
-        const double H = 2.0 * ka.v * kb.v / s;
-        const double dHa = 2.0 * kb.v * kb.v / (s * s) * ka.dpsi, dHb = 2.0 * ka.v * ka.v / (s * s) * kb.dpsi;
+        const double is = s > 0.0 ? 1.0 / s : 0.0;  // both kr zero: no conductance
+        const double H = 2.0 * ka.v * kb.v * is;
+        const double dHa = 2.0 * kb.v * kb.v * is * is * ka.dpsi, dHb = 2.0 * ka.v * ka.v * is * is * kb.dpsi;
         const double D = psi[b] + z[b] - psi[a] - z[a];
         const double Ka = Ks[f] * aol[f];
         Kh[f] = Ks[f] * H;
@@ -218,8 +219,9 @@ __global__ void richards_face_grads(int F, const int *__restrict__ fa, const int
         const int a = fa[f], b = fb[f];
         const Kr ka = kr_vg(psi[a], alphas[f], Ns[f]), kb = kr_vg(psi[b], alphas[f], Ns[f]);
         const double s = ka.v + kb.v;
-        const double H = 2.0 * ka.v * kb.v / s;
-        const double wa = 2.0 * kb.v * kb.v / (s * s), wb = 2.0 * ka.v * ka.v / (s * s);
+        const double is = s > 0.0 ? 1.0 / s : 0.0;
+        const double H = 2.0 * ka.v * kb.v * is;
+        const double wa = 2.0 * kb.v * kb.v * is * is, wb = 2.0 * ka.v * ka.v * is * is;
         const double D = psi[b] + z[b] - psi[a] - z[a];
         const double dm = (dir[a] ? 0.0 : mu[a]) - (dir[b] ? 0.0 : mu[b]);
         if (dK) dK[f] = H * aol[f] * D * dm;
@@ -253,8 +255,9 @@ __global__ void richards_cell_grads(int n, const int *__restrict__ irp, const in
             if (dir[j]) continue;
             const Kr kk = kr_vg(psi[k], alphas[f], Ns[f]), kj = kr_vg(psi[j], alphas[f], Ns[f]);
             const double s = kk.v + kj.v;
-            const double H = 2.0 * kk.v * kj.v / s;
-            const double dHk = 2.0 * kj.v * kj.v / (s * s) * kk.dpsi;
+            const double is = s > 0.0 ? 1.0 / s : 0.0;
+            const double H = 2.0 * kk.v * kj.v * is;
+            const double dHk = 2.0 * kj.v * kj.v * is * is * kk.dpsi;
             const double Djk = psi[k] + z[k] - psi[j] - z[j];
             g += mu[j] * Ks[f] * aol[f] * (dHk * Djk + H);
         }
