@@ -242,6 +242,38 @@ class GroundwaterProblem:
                                                                   ddpp, dalp, dNp, dQp))
         return dK, ddp, dal, dN, dQ
 
+    def richards_transient_forward(self, psi0, Ks, dirichletpsis, z, alphas, Ns, Qs, specificstorage, dt, nsteps,
+                                   tol=1e-10, maxiter=200, return_states=False):
+        """Fixed-step backward Euler of S V dpsi/dt = R(psi): psi at the final step (and all steps,
+        (nsteps, N), with return_states)."""
+        p0, K, dp, zz = _Buf(psi0, n=self.N), _Buf(Ks, n=self.F), _Buf(dirichletpsis, n=self.N), _Buf(z, n=self.N)
+        al, n_, q, ss = _Buf(alphas, n=self.F), _Buf(Ns, n=self.F), _Buf(Qs, n=self.N), _Buf(specificstorage, n=self.N)
+        psiT, pp = _out(p0, self.N)
+        states, sp = _out(p0, int(nsteps) * self.N) if return_states else (None, None)
+        _check(self._lib, self._h, self._lib.dpf_richards_transient_forward(
+            self._h, p0.ptr, K.ptr, dp.ptr, zz.ptr, al.ptr, n_.ptr, q.ptr, ss.ptr, float(dt), int(nsteps), float(tol),
+            int(maxiter), sp, pp))
+        if return_states:
+            return psiT, states.reshape(int(nsteps), self.N)
+        return psiT
+
+    def richards_transient_adjoint(self, obs, weights=None, gT=None, tol=1e-10, maxiter=200):
+        """(dKs, ddirichletpsis, dalphas, dNs, dQs, dpsi0) of J = sum_n sum_k w_k psi^n[obs_k]^2 + gT . psi^T."""
+        ob = np.ascontiguousarray(np.asarray(obs, dtype=np.int64))
+        w = None if weights is None else np.ascontiguousarray(np.asarray(weights, dtype=np.float64))
+        g = None if gT is None else _Buf(gT, n=self.N)
+        like = g
+        dK, dKp = _out(like, self.F)
+        ddp, ddpp = _out(like, self.N)
+        dal, dalp = _out(like, self.F)
+        dN, dNp = _out(like, self.F)
+        dQ, dQp = _out(like, self.N)
+        d0, d0p = _out(like, self.N)
+        _check(self._lib, self._h, self._lib.dpf_richards_transient_adjoint(
+            self._h, ob.size, ob.ctypes.data, None if w is None else w.ctypes.data, None if g is None else g.ptr,
+            float(tol), int(maxiter), dKp, ddpp, dalp, dNp, dQp, d0p))
+        return dK, ddp, dal, dN, dQ, d0
+
     @property
     def richards_stats(self):
         it, ai, rr = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()

@@ -92,6 +92,10 @@ SIGNATURES = {
                                            _vp]),
     "dpf_richards_adjoint": (ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
     "dpf_richards_stats": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _f64p]),
+    "dpf_richards_transient_forward": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_double,
+                                                      ctypes.c_int, ctypes.c_double, ctypes.c_int, _vp, _vp]),
+    "dpf_richards_transient_adjoint": (ctypes.c_int, [_vp, _i64, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int, _vp,
+                                                      _vp, _vp, _vp, _vp, _vp]),
     "dpf_logk_to_faces_regular_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_int,
                                                          _vp]),
     "dpf_debug_fail_alloc": (None, [ctypes.c_int64]),

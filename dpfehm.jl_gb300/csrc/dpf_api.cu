@@ -1224,6 +1224,41 @@ int dpf_richards_adjoint(dpf_problem *P, const double *delta, double tol, int ma
     });
 }
 
+int dpf_richards_transient_forward(dpf_problem *P, const double *psi0, const double *Ks, const double *dirichletpsis,
+                                   const double *z, const double *alphas, const double *Ns, const double *Qs,
+                                   const double *specificstorage, double dt, int nsteps, double tol, int maxiter,
+                                   double *states, double *psiT) {
+    return guarded(P, __func__, [&]() -> int {
+        if (!P->gs) {
+            P->err = "the Richards solver runs on face-list handles (dpf_create_general)";
+            return DPF_UNSUPPORTED;
+        }
+        if (!psi0 || !Ks || !dirichletpsis || !z || !alphas || !Ns || !Qs || !specificstorage)
+            throw BadInput("invalid arguments");
+        if (!(tol > 0)) tol = 1e-10;
+        if (maxiter <= 0) maxiter = 200;
+        return gs_status(P, P->gs->richards_transient_forward(psi0, Ks, dirichletpsis, z, alphas, Ns, Qs,
+                                                              specificstorage, dt, nsteps, tol, maxiter, states,
+                                                              psiT));
+    });
+}
+
+int dpf_richards_transient_adjoint(dpf_problem *P, int64_t nobs, const int64_t *obs, const double *w,
+                                   const double *gT, double tol, int maxiter, double *dKs, double *ddpsi,
+                                   double *dalphas, double *dNs, double *dQs, double *dpsi0) {
+    return guarded(P, __func__, [&]() -> int {
+        if (!P->gs) {
+            P->err = "the Richards solver runs on face-list handles (dpf_create_general)";
+            return DPF_UNSUPPORTED;
+        }
+        if (nobs < 0 || (nobs > 0 && !obs)) throw BadInput("invalid observations");
+        if (!(tol > 0)) tol = 1e-10;
+        if (maxiter <= 0) maxiter = 200;
+        return gs_status(P, P->gs->richards_transient_adjoint(nobs, obs, w, gT, tol, maxiter, dKs, ddpsi, dalphas,
+                                                              dNs, dQs, dpsi0));
+    });
+}
+
 int dpf_richards_stats(const dpf_problem *P, int *iterations, int *adjoint_iterations, double *relres) {
     if (!P || !P->gs) return DPF_BAD_INPUT;
     if (iterations) *iterations = P->gs->rich_iters;

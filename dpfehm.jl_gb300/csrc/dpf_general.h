@@ -57,6 +57,12 @@ public:
                         double *psi_out);
     int richards_adjoint(const double *delta, double tol, int maxit, double *dKs, double *ddpsi, double *dalphas,
                          double *dNs, double *dQs);
+    int richards_transient_forward(const double *psi0, const double *Ks, const double *dpsi, const double *z,
+                                   const double *alphas, const double *Ns, const double *Qs, const double *Ss,
+                                   double dt, int nsteps, double tol, int maxit, double *states, double *psiT);
+    int richards_transient_adjoint(long long nobs, const int64_t *obs, const double *w, const double *gT, double tol,
+                                   int maxit, double *dKs, double *ddpsi, double *dalphas, double *dNs, double *dQs,
+                                   double *dpsi0);
     int rich_iters = 0, rich_adj_iters = 0;
     double rich_relres = 0.0;
 
@@ -87,7 +93,13 @@ private:
     void from_dev(void *dst, const void *src, size_t bytes);
     const double *stage(const double *src, size_t n, double *dst);
     void richards_buffers();
-    int richards_spd_solve(const double *rhs_dev, double *x_dev);
+    void richards_stage(const double *Ks, const double *dpsi, const double *z, const double *alphas,
+                        const double *Ns, const double *Qs, const double *psi0);
+    int richards_spd_solve(const double *rhs_dev, double *x_dev, const double *shift_dev);
+    int richards_nonlinear(const double *shift_dev, const double *psi_old, double tol, int maxit, int &iters,
+                           double &relres);
+    int richards_gmres(const double *rhs_dev, double *x_dev, const double *shift_dev, double tol, int maxit,
+                       int &iters, double &rel);
 
     dpf_options opt;
     cudaStream_t stream;
@@ -131,6 +143,10 @@ private:
     double *rc_gK = nullptr, *rc_ga = nullptr, *rc_gN = nullptr;
     double2 *rc_part = nullptr;
     std::vector<double *> rc_V;    // GMRES basis of the Richards adjoint
+    double *rc_c = nullptr;        // its preconditioned right-hand side
+    // transient Richards: states psi^0..psi^n, storage shift S V / dt, adjoint buffers
+    double *rt_states = nullptr, *rt_shift = nullptr, *rt_gQ = nullptr, *rt_gD = nullptr, *rt_lam = nullptr;
+    int rt_cap = 0, rt_nsteps = 0;
     bool have_richards = false;
     // bookkeeping
     bool have_forward = false;

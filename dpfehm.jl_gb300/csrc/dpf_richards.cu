@@ -88,18 +88,21 @@ __global__ void kr_faces(int F, const int *__restrict__ fa, const int *__restric
 }
 
 // R_j = Q_j + sum_f Kh_f aol_f (psi_k + z_k - psi_j - z_j) at free cells, 0 at Dirichlet
-// cells; per-block partial sums of R^2 and Q^2 (fixed order: deterministic)
+// cells, minus shift_j (psi_j - psi_old_j) in a backward-Euler step (shift = S V / dt, null
+// when steady); per-block partial sums of R^2 and Q^2 (fixed order: deterministic)
 __global__ void richards_residual(int n, const int *__restrict__ irp, const int *__restrict__ ifc,
                                   const int *__restrict__ fa, const int *__restrict__ fb,
                                   const double *__restrict__ aol, const double *__restrict__ Kh,
                                   const uint8_t *__restrict__ dir, const double *__restrict__ psi,
-                                  const double *__restrict__ z, const double *__restrict__ Qs, double *__restrict__ R,
-                                  double2 *__restrict__ part) {
+                                  const double *__restrict__ z, const double *__restrict__ Qs,
+                                  const double *__restrict__ shift, const double *__restrict__ psi_old,
+                                  double *__restrict__ R, double2 *__restrict__ part) {
     double rr = 0.0, qq = 0.0;
     RSTRIDE(i, n) {
         double r = 0.0;
         if (!dir[i]) {
             r = Qs[i];
+            if (shift) r -= shift[i] * (psi[i] - psi_old[i]);
             const double hi = psi[i] + z[i];
             for (int k = irp[i]; k < irp[i + 1]; k++) {
                 const int f = ifc[k];
@@ -214,7 +217,8 @@ __global__ void richards_face_grads(int F, const int *__restrict__ fa, const int
                                     const double *__restrict__ alphas, const double *__restrict__ Ns,
                                     const double *__restrict__ psi, const double *__restrict__ z,
                                     const uint8_t *__restrict__ dir, const double *__restrict__ mu,
-                                    double *__restrict__ dK, double *__restrict__ dal, double *__restrict__ dN) {
+                                    double *__restrict__ dK, double *__restrict__ dal, double *__restrict__ dN,
+                                    int accumulate) {
     RSTRIDE(f, F) {
         const int a = fa[f], b = fb[f];
         const Kr ka = kr_vg(psi[a], alphas[f], Ns[f]), kb = kr_vg(psi[b], alphas[f], Ns[f]);
@@ -224,10 +228,10 @@ __global__ void richards_face_grads(int F, const int *__restrict__ fa, const int
         const double wa = 2.0 * kb.v * kb.v * is * is, wb = 2.0 * ka.v * ka.v * is * is;
         const double D = psi[b] + z[b] - psi[a] - z[a];
         const double dm = (dir[a] ? 0.0 : mu[a]) - (dir[b] ? 0.0 : mu[b]);
-        if (dK) dK[f] = H * aol[f] * D * dm;
         const double c = Ks[f] * aol[f] * D * dm;
-        if (dal) dal[f] = c * (wa * ka.dalpha + wb * kb.dalpha);
-        if (dN) dN[f] = c * (wa * ka.dN + wb * kb.dN);
+        if (dK) dK[f] = (accumulate ? dK[f] : 0.0) + H * aol[f] * D * dm;
+        if (dal) dal[f] = (accumulate ? dal[f] : 0.0) + c * (wa * ka.dalpha + wb * kb.dalpha);
+        if (dN) dN[f] = (accumulate ? dN[f] : 0.0) + c * (wa * ka.dN + wb * kb.dN);
     }
 }
 
@@ -240,15 +244,15 @@ __global__ void richards_cell_grads(int n, const int *__restrict__ irp, const in
                                     const double *__restrict__ psi, const double *__restrict__ z,
                                     const uint8_t *__restrict__ dir, const double *__restrict__ mu,
                                     const double *__restrict__ delta, double *__restrict__ dQ,
-                                    double *__restrict__ ddp) {
+                                    double *__restrict__ ddp, int accumulate) {
     RSTRIDE(k, n) {
-        if (dQ) dQ[k] = dir[k] ? 0.0 : mu[k];
+        if (dQ) dQ[k] = (accumulate ? dQ[k] : 0.0) + (dir[k] ? 0.0 : mu[k]);
         if (!ddp) continue;
         if (!dir[k]) {
-            ddp[k] = 0.0;
+            if (!accumulate) ddp[k] = 0.0;
             continue;
         }
-        double g = delta[k];
+        double g = (accumulate ? ddp[k] : 0.0) + delta[k];
         for (int e = irp[k]; e < irp[k + 1]; e++) {
             const int f = ifc[e];
             const int j = fa[f] == k ? fb[f] : fa[f];
@@ -263,6 +267,28 @@ __global__ void richards_cell_grads(int n, const int *__restrict__ irp, const in
         }
         ddp[k] = g;
     }
+}
+
+// shift = S V / dt per cell (the backward-Euler storage term)
+__global__ void richards_shift(int n, const double *__restrict__ Ss, const double *__restrict__ vol, double rdt,
+                               double *__restrict__ shift) {
+    RSTRIDE(i, n) shift[i] = Ss[i] * vol[i] * rdt;
+}
+
+// transient adjoint seed: s_i = 2 w_k psi_i at observation cells (+ gT_i at the last step)
+__global__ void richards_seed(int nobs, const long long *__restrict__ obs, const double *__restrict__ w,
+                              const double *__restrict__ psi, double *__restrict__ seed) {
+    RSTRIDE(k, nobs) {
+        const long long i = obs[k];
+        atomicAdd(&seed[i], 2.0 * (w ? w[k] : 1.0) * psi[i]);  // a cell observed twice gets both terms
+    }
+}
+
+// rhs = seed + shift lam_next at free cells, 0 at Dirichlet cells
+__global__ void richards_trans_rhs(int n, const uint8_t *__restrict__ dir, const double *__restrict__ seed,
+                                   const double *__restrict__ shift, const double *__restrict__ lam_next,
+                                   double *__restrict__ rhs) {
+    RSTRIDE(i, n) rhs[i] = dir[i] ? 0.0 : seed[i] + shift[i] * lam_next[i];
 }
 
 // per-block partial sums of x . y
@@ -360,58 +386,47 @@ void GeneralSolver::richards_buffers() {
     rck(cudaMemsetAsync(rc_zero, 0, N * sizeof(double), stream), "zero");
 }
 
-// One SPD solve A(Kh) x = rhs (x = 0 at Dirichlet cells) with the handle's CG + AMG.
-int GeneralSolver::richards_spd_solve(const double *rhs_dev, double *x_dev) {
+// One SPD solve (shift + A(Kh)) x = rhs (x = 0 at Dirichlet cells) with the handle's CG + AMG;
+// shift = S V / dt in a backward-Euler step, null when steady.
+int GeneralSolver::richards_spd_solve(const double *rhs_dev, double *x_dev, const double *shift_dev) {
     rck(cudaMemcpyAsync(in_Q, rhs_dev, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "rhs");
     rck(cudaMemcpyAsync(in_dh, rc_zero, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "dh");
-    assemble(rc_Kh, nullptr, 0, nullptr, true);
+    assemble(rc_Kh, nullptr, 0, shift_dev, true);
     solve(b64, h);
     rck(cudaMemcpyAsync(x_dev, h, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "solution");
     rck(cudaStreamSynchronize(stream), "sync");
     return finish_status();
 }
 
-int GeneralSolver::richards_steady(const double *psi0, const double *Ks, const double *dpsi, const double *z,
-                                   const double *alphas, const double *Ns, const double *Qs, double tol, int maxit,
-                                   double *psi_out) {
-    if (nfree == N) throw BadInput("the problem has no Dirichlet cell: the steady-state operator is singular");
-    richards_buffers();
-    stage(Ks, F, rc_Ks);
-    stage(alphas, F, rc_al);
-    stage(Ns, F, rc_N);
-    stage(z, N, rc_z);
-    stage(dpsi, N, rc_dpsi);
-    stage(Qs, N, rc_Q);
-    const double *Qd = rc_Q;
-    stage(psi0, N, rc_d);
+// Nonlinear solve of one steady or backward-Euler Richards system from the current rc_psi:
+// Picard steps (shift + A(psi)) d = G(psi), G = R(psi) - shift (psi - psi_old), halved while the
+// residual does not drop, until |G| <= tol max(|G(psi_0)|, |Q|) or maxit steps. Leaves the
+// Picard conductances and the Jacobian parts at the result in rc_Kh, rc_na, rc_nb.
+int GeneralSolver::richards_nonlinear(const double *shift_dev, const double *psi_old, double tol, int maxit,
+                                      int &iters, double &relres) {
     const unsigned nbF = rblocks(F, nblocks), nbN = rblocks(N, nblocks);
-    richards_init<<<nbN, kRBlock, 0, stream>>>((int)N, lv[0].dir, rc_d, rc_dpsi, rc_psi);
-    GLAUNCH_CHECK();
     auto residual = [&]() -> double2 {
         kr_faces<<<nbF, kRBlock, 0, stream>>>((int)F, fa, fb, faol, rc_Ks, rc_al, rc_N, rc_psi, rc_z, rc_Kh,
                                               nullptr, nullptr);
         GLAUNCH_CHECK();
         richards_residual<<<nbN, kRBlock, 0, stream>>>((int)N, irp, ifc, fa, fb, faol, rc_Kh, lv[0].dir, rc_psi,
-                                                       rc_z, Qd, rc_R, rc_part);
+                                                       rc_z, rc_Q, shift_dev, psi_old, rc_R, rc_part);
         GLAUNCH_CHECK();
         return sum_parts(rc_part, (int)nbN, stream);
     };
-    double2 rq = residual();
+    const double2 rq = residual();
     const double r0 = std::sqrt(rq.x), scale = std::max(r0, std::sqrt(rq.y));
     double rn = r0;
-    int it = 0, rc = DPF_OK;
-    rich_iters = 0;
+    int it = 0;
     while (rn > tol * scale && it < maxit) {
-        // Picard step d = A(psi)^-1 R(psi), halved while it does not reduce the residual
-        const int src = richards_spd_solve(rc_R, rc_d);
+        const int src = richards_spd_solve(rc_R, rc_d, shift_dev);
         if (src != DPF_OK && src != DPF_NOT_CONVERGED) return src;
         double w = 1.0, applied = 0.0;
         for (int k = 0; k < 6; k++) {
             richards_update<<<nbN, kRBlock, 0, stream>>>((int)N, lv[0].dir, w - applied, rc_d, rc_psi, rc_part);
             GLAUNCH_CHECK();
             applied = w;
-            const double2 r = residual();
-            const double rnew = std::sqrt(r.x);
+            const double rnew = std::sqrt(residual().x);
             if (rnew < rn || k == 5) {
                 rn = rnew;
                 break;
@@ -420,33 +435,26 @@ int GeneralSolver::richards_steady(const double *psi0, const double *Ks, const d
         }
         it++;
     }
-    rich_iters = it;
-    rich_relres = scale > 0 ? rn / scale : 0.0;
-    if (!std::isfinite(rn)) rc = DPF_NAN;
-    else if (rn > tol * scale) rc = DPF_NOT_CONVERGED;
-    // the solution (Dirichlet values included) and the face terms at it, for the adjoint
-    rcopy_out(psi_out, rc_psi, N, stream);
+    iters = it;
+    relres = scale > 0 ? rn / scale : 0.0;
     kr_faces<<<nbF, kRBlock, 0, stream>>>((int)F, fa, fb, faol, rc_Ks, rc_al, rc_N, rc_psi, rc_z, rc_Kh, rc_na,
                                           rc_nb);
     GLAUNCH_CHECK();
     rck(cudaStreamSynchronize(stream), "sync");
-    have_richards = rc == DPF_OK || rc == DPF_NOT_CONVERGED;
-    if (rc == DPF_NOT_CONVERGED) last_message = "the Richards iteration did not reach its tolerance";
-    else if (rc == DPF_NAN) last_message = "non-finite Richards residual";
-    return rc;
+    if (!std::isfinite(rn)) return DPF_NAN;
+    return rn > tol * scale ? DPF_NOT_CONVERGED : DPF_OK;
 }
 
-int GeneralSolver::richards_adjoint(const double *delta_in, double tol, int maxit, double *dKs, double *ddpsi,
-                                    double *dalphas, double *dNs, double *dQs) {
-    if (!have_richards) throw DpfError("richards adjoint called before a Richards solve", DPF_STATE);
-    double *dl = rc_delta;
-    stage(delta_in, N, dl);
-    const unsigned nbF = rblocks(F, nblocks), nbN = rblocks(N, nblocks);
-    // (I - A^-1 N^T) mu = A^-1 delta by restarted GMRES (the Picard operator A preconditions the
-    // transposed Jacobian -J^T = A - N^T); mu = 0 at Dirichlet cells throughout
+// (shift + A - N^T) x = rhs at the Jacobian parts in rc_Kh, rc_na, rc_nb: with M = shift + A
+// (the Picard operator, solved by CG + AMG), (I - M^-1 N^T) x = M^-1 rhs by restarted GMRES(30).
+// x = 0 at Dirichlet cells; iters and the final relative residual are returned.
+int GeneralSolver::richards_gmres(const double *rhs_dev, double *x_dev, const double *shift_dev, double tol,
+                                  int maxit, int &iters, double &rel) {
+    const unsigned nbN = rblocks(N, nblocks);
     const int m = 30;
     if (rc_V.empty()) {
         for (int k = 0; k <= m; k++) rc_V.push_back(dev<double>(N));
+        rc_c = dev<double>(N);
     }
     auto dot = [&](const double *x, const double *y) {
         vec_dot<<<nbN, kRBlock, 0, stream>>>((int)N, x, y, rc_part);
@@ -457,33 +465,27 @@ int GeneralSolver::richards_adjoint(const double *delta_in, double tol, int maxi
         vec_axpby<<<nbN, kRBlock, 0, stream>>>((int)N, a, x, b, y);
         GLAUNCH_CHECK();
     };
-    int rc = DPF_OK;
-    auto apply = [&](const double *v, double *out) -> int {  // out = v - A^-1 N^T v
+    auto apply = [&](const double *v, double *out) -> int {  // out = v - M^-1 N^T v
         richards_adjoint_rhs<<<nbN, kRBlock, 0, stream>>>((int)N, irp, ifc, fa, fb, rc_na, rc_nb, lv[0].dir, rc_zero,
                                                           v, rc_R);
         GLAUNCH_CHECK();
-        const int src = richards_spd_solve(rc_R, out);
+        const int src = richards_spd_solve(rc_R, out, shift_dev);
         if (src != DPF_OK && src != DPF_NOT_CONVERGED) return src;
         axpby(1.0, v, -1.0, out);
         return DPF_OK;
     };
-    // c = A^-1 delta (free cells)
-    richards_adjoint_rhs<<<nbN, kRBlock, 0, stream>>>((int)N, irp, ifc, fa, fb, rc_na, rc_nb, lv[0].dir, dl, nullptr,
-                                                      rc_R);
-    GLAUNCH_CHECK();
-    rc = richards_spd_solve(rc_R, rc_d);
+    int rc = richards_spd_solve(rhs_dev, rc_c, shift_dev);  // c = M^-1 rhs
     if (rc != DPF_OK && rc != DPF_NOT_CONVERGED) return rc;
-    const double cnorm = std::sqrt(dot(rc_d, rc_d));
-    rck(cudaMemsetAsync(rc_mu, 0, N * sizeof(double), stream), "zero");
+    const double cnorm = std::sqrt(dot(rc_c, rc_c));
+    rck(cudaMemsetAsync(x_dev, 0, N * sizeof(double), stream), "zero");
     int it = 0;
-    double rel = cnorm > 0 ? 1.0 : 0.0;
+    rel = cnorm > 0 ? 1.0 : 0.0;
     std::vector<double> Hm((m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
     while (rel > tol && it < maxit) {
-        // r = c - M mu into V0
-        int r2 = apply(rc_mu, rc_V[0]);
+        int r2 = apply(x_dev, rc_V[0]);  // r = c - (I - M^-1 N^T) x
         if (r2 != DPF_OK) return r2;
-        axpby(1.0, rc_d, -1.0, rc_V[0]);
-        double beta = std::sqrt(dot(rc_V[0], rc_V[0]));
+        axpby(1.0, rc_c, -1.0, rc_V[0]);
+        const double beta = std::sqrt(dot(rc_V[0], rc_V[0]));
         if (!std::isfinite(beta)) return DPF_NAN;
         rel = cnorm > 0 ? beta / cnorm : 0.0;
         if (rel <= tol) break;
@@ -502,7 +504,7 @@ int GeneralSolver::richards_adjoint(const double *delta_in, double tol, int maxi
             const double hn = std::sqrt(dot(rc_V[k + 1], rc_V[k + 1]));
             Hm[(k + 1) * m + k] = hn;
             if (hn > 0) axpby(0.0, rc_V[k + 1], 1.0 / hn, rc_V[k + 1]);
-            for (int i2 = 0; i2 < k; i2++) {  // earlier Givens rotations
+            for (int i2 = 0; i2 < k; i2++) {  // the earlier Givens rotations
                 const double a = Hm[i2 * m + k], b = Hm[(i2 + 1) * m + k];
                 Hm[i2 * m + k] = cs[i2] * a + sn[i2] * b;
                 Hm[(i2 + 1) * m + k] = -sn[i2] * a + cs[i2] * b;
@@ -523,38 +525,212 @@ int GeneralSolver::richards_adjoint(const double *delta_in, double tol, int maxi
                 break;
             }
         }
-        // mu += V y, H y = g
-        for (int i2 = k - 1; i2 >= 0; i2--) {
+        for (int i2 = k - 1; i2 >= 0; i2--) {  // x += V y with H y = g
             double s2 = g[i2];
             for (int j2 = i2 + 1; j2 < k; j2++) s2 -= Hm[i2 * m + j2] * y[j2];
             y[i2] = s2 / Hm[i2 * m + i2];
         }
-        for (int i2 = 0; i2 < k; i2++) axpby(y[i2], rc_V[i2], 1.0, rc_mu);
+        for (int i2 = 0; i2 < k; i2++) axpby(y[i2], rc_V[i2], 1.0, x_dev);
     }
-    rich_adj_iters = it;
-    // gradients at the solution
-    double *gK = dKs ? rc_gK : nullptr;
-    double *ga = dalphas ? rc_ga : nullptr;
-    double *gN = dNs ? rc_gN : nullptr;
+    iters = it;
+    return rc;
+}
+
+void GeneralSolver::richards_stage(const double *Ks, const double *dpsi, const double *z, const double *alphas,
+                                   const double *Ns, const double *Qs, const double *psi0) {
+    richards_buffers();
+    stage(Ks, F, rc_Ks);
+    stage(alphas, F, rc_al);
+    stage(Ns, F, rc_N);
+    stage(z, N, rc_z);
+    stage(dpsi, N, rc_dpsi);
+    stage(Qs, N, rc_Q);
+    stage(psi0, N, rc_d);
+    richards_init<<<rblocks(N, nblocks), kRBlock, 0, stream>>>((int)N, lv[0].dir, rc_d, rc_dpsi, rc_psi);
+    GLAUNCH_CHECK();
+}
+
+int GeneralSolver::richards_steady(const double *psi0, const double *Ks, const double *dpsi, const double *z,
+                                   const double *alphas, const double *Ns, const double *Qs, double tol, int maxit,
+                                   double *psi_out) {
+    if (nfree == N) throw BadInput("the problem has no Dirichlet cell: the steady-state operator is singular");
+    richards_stage(Ks, dpsi, z, alphas, Ns, Qs, psi0);
+    have_richards = false;
+    const int rc = richards_nonlinear(nullptr, nullptr, tol, maxit, rich_iters, rich_relres);
+    rcopy_out(psi_out, rc_psi, N, stream);
+    rck(cudaStreamSynchronize(stream), "sync");
+    have_richards = rc == DPF_OK || rc == DPF_NOT_CONVERGED;
+    if (rc == DPF_NOT_CONVERGED) last_message = "the Richards iteration did not reach its tolerance";
+    else if (rc == DPF_NAN) last_message = "non-finite Richards residual";
+    return rc;
+}
+
+int GeneralSolver::richards_adjoint(const double *delta_in, double tol, int maxit, double *dKs, double *ddpsi,
+                                    double *dalphas, double *dNs, double *dQs) {
+    if (!have_richards) throw DpfError("richards adjoint called before a Richards solve", DPF_STATE);
+    stage(delta_in, N, rc_delta);
+    const unsigned nbF = rblocks(F, nblocks), nbN = rblocks(N, nblocks);
+    // mu = -lambda: (A - N^T) mu = delta at the free cells
+    richards_adjoint_rhs<<<nbN, kRBlock, 0, stream>>>((int)N, irp, ifc, fa, fb, rc_na, rc_nb, lv[0].dir, rc_delta,
+                                                      nullptr, rc_d);
+    GLAUNCH_CHECK();
+    double rel = 0.0;
+    const int rc = richards_gmres(rc_d, rc_mu, nullptr, tol, maxit, rich_adj_iters, rel);
+    if (rc != DPF_OK && rc != DPF_NOT_CONVERGED) return rc;
     richards_face_grads<<<nbF, kRBlock, 0, stream>>>((int)F, fa, fb, faol, rc_Ks, rc_al, rc_N, rc_psi, rc_z,
-                                                     lv[0].dir, rc_mu, gK, ga, gN);
+                                                     lv[0].dir, rc_mu, dKs ? rc_gK : nullptr,
+                                                     dalphas ? rc_ga : nullptr, dNs ? rc_gN : nullptr, 0);
     GLAUNCH_CHECK();
-    double *gQ = dQs ? rc_d : nullptr;
-    double *gD = ddpsi ? rc_R : nullptr;
     richards_cell_grads<<<nbN, kRBlock, 0, stream>>>((int)N, irp, ifc, fa, fb, faol, rc_Ks, rc_al, rc_N, rc_psi,
-                                                     rc_z, lv[0].dir, rc_mu, dl, gQ, gD);
+                                                     rc_z, lv[0].dir, rc_mu, rc_delta, dQs ? rc_d : nullptr,
+                                                     ddpsi ? rc_R : nullptr, 0);
     GLAUNCH_CHECK();
-    if (dKs) rcopy_out(dKs, gK, F, stream);
-    if (dalphas) rcopy_out(dalphas, ga, F, stream);
-    if (dNs) rcopy_out(dNs, gN, F, stream);
-    if (dQs) rcopy_out(dQs, gQ, N, stream);
-    if (ddpsi) rcopy_out(ddpsi, gD, N, stream);
+    rcopy_out(dKs, rc_gK, F, stream);
+    rcopy_out(dalphas, rc_ga, F, stream);
+    rcopy_out(dNs, rc_gN, F, stream);
+    rcopy_out(dQs, rc_d, N, stream);
+    rcopy_out(ddpsi, rc_R, N, stream);
     rck(cudaStreamSynchronize(stream), "sync");
     if (rel > tol) {
         last_message = "the Richards adjoint iteration did not reach its tolerance";
         return DPF_NOT_CONVERGED;
     }
-    return rc;
+    return DPF_OK;
+}
+
+// ---- transient: fixed-step backward Euler of S_i V_i dpsi_i/dt = R_i(psi) (the reference's
+// richards_residuals with specific storage and volumes, stepped by an external integrator)
+int GeneralSolver::richards_transient_forward(const double *psi0, const double *Ks, const double *dpsi,
+                                              const double *z, const double *alphas, const double *Ns,
+                                              const double *Qs, const double *Ss, double dt, int nsteps, double tol,
+                                              int maxit, double *states, double *psiT) {
+    if (!(dt > 0) || nsteps < 1) throw BadInput("dt must be positive and nsteps at least 1");
+    richards_stage(Ks, dpsi, z, alphas, Ns, Qs, psi0);
+    have_richards = false;
+    rt_nsteps = 0;
+    if (!rt_shift) rt_shift = dev<double>(N);
+    if (rt_cap < nsteps) {
+        drop(rt_states);
+        rt_states = dev<double>((size_t)(nsteps + 1) * N);  // psi^0 .. psi^nsteps
+        rt_cap = nsteps;
+    }
+    stage(Ss, N, rc_d);
+    richards_shift<<<rblocks(N, nblocks), kRBlock, 0, stream>>>((int)N, rc_d, vol, 1.0 / dt, rt_shift);
+    GLAUNCH_CHECK();
+    rck(cudaMemcpyAsync(rt_states, rc_psi, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "state");
+    int worst = DPF_OK, total = 0;
+    double rr = 0.0;
+    for (int n = 1; n <= nsteps; n++) {
+        int it = 0;
+        double rel = 0.0;
+        const int rc = richards_nonlinear(rt_shift, rt_states + (size_t)(n - 1) * N, tol, maxit, it, rel);
+        if (rc != DPF_OK && rc != DPF_NOT_CONVERGED) {
+            last_message = rc == DPF_NAN ? "non-finite Richards residual" : last_message;
+            return rc;
+        }
+        if (rc == DPF_NOT_CONVERGED) worst = rc;
+        total += it;
+        rr = std::max(rr, rel);
+        rck(cudaMemcpyAsync(rt_states + (size_t)n * N, rc_psi, N * sizeof(double), cudaMemcpyDeviceToDevice, stream),
+            "state");
+        if (states)
+            rck(cudaMemcpyAsync(states + (size_t)(n - 1) * N, rc_psi, N * sizeof(double),
+                                r_is_device(states) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, stream),
+                "states");
+    }
+    rcopy_out(psiT, rc_psi, N, stream);
+    rck(cudaStreamSynchronize(stream), "sync");
+    rich_iters = total;
+    rich_relres = rr;
+    rt_nsteps = nsteps;
+    if (worst == DPF_NOT_CONVERGED) last_message = "a Richards step did not reach its tolerance";
+    return worst;
+}
+
+// Adjoint of the last transient run for J = sum_{n=1..nsteps} sum_k w_k psi^n[obs_k]^2 + gT . psi^nsteps:
+// backward in time (shift + A - N^T)(psi^n) lam^n = dJ/dpsi^n + shift lam^(n+1), the tangents
+// sum_n (dR(psi^n)/dp)^T lam^n, and dpsi0 = shift lam^1.
+int GeneralSolver::richards_transient_adjoint(long long nobs, const int64_t *obs, const double *w, const double *gT,
+                                              double tol, int maxit, double *dKs, double *ddpsi, double *dalphas,
+                                              double *dNs, double *dQs, double *dpsi0) {
+    if (rt_nsteps < 1) throw DpfError("transient Richards adjoint called before a transient Richards run", DPF_STATE);
+    const unsigned nbF = rblocks(F, nblocks), nbN = rblocks(N, nblocks);
+    std::vector<long long> ho(nobs);
+    for (long long k = 0; k < nobs; k++) {
+        long long v = 0;
+        if (r_is_device(obs)) rck(cudaMemcpy(&v, obs + k, sizeof(int64_t), cudaMemcpyDeviceToHost), "obs");
+        else v = obs[k];
+        if (v < 0 || v >= N) throw BadInput("observation index out of range");
+        ho[k] = v;
+    }
+    long long *d_obs = dev<long long>(std::max(nobs, 1LL));
+    double *d_w = w ? dev<double>(std::max(nobs, 1LL)) : nullptr;
+    double *d_gT = gT ? dev<double>(N) : nullptr;
+    if (nobs) rck(cudaMemcpyAsync(d_obs, ho.data(), nobs * sizeof(long long), cudaMemcpyHostToDevice, stream), "obs");
+    if (w) stage(w, nobs, d_w);
+    if (gT) stage(gT, N, d_gT);
+    if (!rt_gQ) {
+        rt_gQ = dev<double>(N);
+        rt_gD = dev<double>(N);
+        rt_lam = dev<double>(N);
+    }
+    double *lam = rc_mu, *seed = rc_delta, *lam_hold = rt_lam;
+    rck(cudaMemsetAsync(lam_hold, 0, N * sizeof(double), stream), "zero");  // lam^(nsteps+1) = 0
+    int worst = DPF_OK, total = 0;
+    const int nsteps = rt_nsteps;
+    for (int n = nsteps; n >= 1; n--) {
+        const double *psi_n = rt_states + (size_t)n * N;
+        rck(cudaMemcpyAsync(rc_psi, psi_n, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "state");
+        kr_faces<<<nbF, kRBlock, 0, stream>>>((int)F, fa, fb, faol, rc_Ks, rc_al, rc_N, rc_psi, rc_z, rc_Kh, rc_na,
+                                              rc_nb);
+        GLAUNCH_CHECK();
+        // seed = dJ/dpsi^n
+        if (n == nsteps && d_gT)
+            rck(cudaMemcpyAsync(seed, d_gT, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "gT");
+        else
+            rck(cudaMemsetAsync(seed, 0, N * sizeof(double), stream), "seed");
+        if (nobs) {
+            richards_seed<<<rblocks(nobs, nblocks), kRBlock, 0, stream>>>((int)nobs, d_obs, d_w, rc_psi, seed);
+            GLAUNCH_CHECK();
+        }
+        richards_trans_rhs<<<nbN, kRBlock, 0, stream>>>((int)N, lv[0].dir, seed, rt_shift, lam_hold, rc_R);
+        GLAUNCH_CHECK();
+        rck(cudaMemcpyAsync(rc_d, rc_R, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "rhs");
+        int it = 0;
+        double rel = 0.0;
+        const int rc = richards_gmres(rc_d, lam, rt_shift, tol, maxit, it, rel);
+        if (rc != DPF_OK && rc != DPF_NOT_CONVERGED) return rc;
+        if (rel > tol) worst = DPF_NOT_CONVERGED;
+        total += it;
+        const int acc = n == nsteps ? 0 : 1;
+        richards_face_grads<<<nbF, kRBlock, 0, stream>>>((int)F, fa, fb, faol, rc_Ks, rc_al, rc_N, rc_psi, rc_z,
+                                                         lv[0].dir, lam, dKs ? rc_gK : nullptr,
+                                                         dalphas ? rc_ga : nullptr, dNs ? rc_gN : nullptr, acc);
+        GLAUNCH_CHECK();
+        richards_cell_grads<<<nbN, kRBlock, 0, stream>>>((int)N, irp, ifc, fa, fb, faol, rc_Ks, rc_al, rc_N, rc_psi,
+                                                         rc_z, lv[0].dir, lam, seed, dQs ? rt_gQ : nullptr,
+                                                         ddpsi ? rt_gD : nullptr, acc);
+        GLAUNCH_CHECK();
+        rck(cudaMemcpyAsync(lam_hold, lam, N * sizeof(double), cudaMemcpyDeviceToDevice, stream), "lam");
+    }
+    // dpsi0 = shift lam^1 at the free cells
+    if (dpsi0) {
+        richards_trans_rhs<<<nbN, kRBlock, 0, stream>>>((int)N, lv[0].dir, rc_zero, rt_shift, lam_hold, rc_R);
+        GLAUNCH_CHECK();
+    }
+    rcopy_out(dKs, rc_gK, F, stream);
+    rcopy_out(dalphas, rc_ga, F, stream);
+    rcopy_out(dNs, rc_gN, F, stream);
+    rcopy_out(dQs, rt_gQ, N, stream);
+    rcopy_out(ddpsi, rt_gD, N, stream);
+    rcopy_out(dpsi0, rc_R, N, stream);
+    rck(cudaStreamSynchronize(stream), "sync");
+    drop(d_obs);
+    drop(d_w);
+    drop(d_gT);
+    rich_adj_iters = total;
+    if (worst == DPF_NOT_CONVERGED) last_message = "a Richards adjoint step did not reach its tolerance";
+    return worst;
 }
 
 }  // namespace dpf

@@ -286,8 +286,28 @@ int dpf_richards_steady(dpf_problem *h, const double *psi0, const double *Ks, co
 int dpf_richards_adjoint(dpf_problem *h, const double *delta, double tol, int maxiter, double *dKs,
                          double *ddirichletpsis, double *dalphas, double *dNs, double *dQs);
 
-/* Picard steps of the last Richards solve, fixed-point steps of the last adjoint, and the final
- * relative residual. */
+/* Fixed-step backward Euler of S_i V_i dpsi_i/dt = R_i(psi), R the steady Richards residual
+ * above (the reference's richards_residuals with specificstorage and volumes, stepped by
+ * DifferentiableBackwardEuler in examples/richards_transient_3d/inputdeck.jl): nsteps steps of dt
+ * from psi0[N], each a Picard iteration on S V/dt + A(psi) to tol. Writes psi at the final step
+ * to psiT[N] and, if states != NULL, every step to states[nsteps*N]. */
+int dpf_richards_transient_forward(dpf_problem *h, const double *psi0, const double *Ks,
+                                   const double *dirichletpsis, const double *z, const double *alphas,
+                                   const double *Ns, const double *Qs, const double *specificstorage, double dt,
+                                   int nsteps, double tol, int maxiter, double *states, double *psiT);
+
+/* Adjoint of the last transient Richards run for
+ *   J = sum_{n=1..nsteps} sum_k w_k psi^n[obs_k]^2  +  gT . psi^nsteps
+ * (w may be NULL for unit weights, gT may be NULL): backward in time, each step one GMRES solve
+ * with the transposed Jacobian (tolerance tol, at most maxiter steps). Outputs dKs[F],
+ * ddirichletpsis[N], dalphas[F], dNs[F], dQs[N], dpsi0[N] (any may be NULL). */
+int dpf_richards_transient_adjoint(dpf_problem *h, int64_t nobs, const int64_t *obs, const double *w,
+                                   const double *gT, double tol, int maxiter, double *dKs,
+                                   double *ddirichletpsis, double *dalphas, double *dNs, double *dQs,
+                                   double *dpsi0);
+
+/* Picard steps of the last Richards solve (summed over the steps of a transient run), GMRES
+ * steps of the last adjoint, and the final relative residual (the largest over the steps). */
 int dpf_richards_stats(const dpf_problem *h, int *iterations, int *adjoint_iterations, double *relres);
 
 /* ------------------------------------------------------------ test hooks */

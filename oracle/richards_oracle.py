@@ -137,6 +137,29 @@ def steady(psi0, Ks, neighbors, aol, dirichletnodes, dirichletpsis, z, alphas, N
     return psi
 
 
+def r_transpose(psi, lfull, Ks, neighbors, aol, dirichletnodes, z, alphas, Ns, Qs):
+    """(dR/dp)^T lambda at psi for lambda (N, zero at Dirichlet cells): the Ks, dirichletpsis,
+    alphas, Ns and Qs parts (the dirichletpsis part only at Dirichlet cells)."""
+    N = len(Qs)
+    nb, isfree, free, fmap = _setup(N, neighbors, dirichletnodes)
+    t = _faces(psi, Ks, nb, aol, z, alphas, Ns)
+    a, b, D, H, KA = t["a"], t["b"], t["D"], t["H"], t["KA"]
+    dl = lfull[a] - lfull[b]
+    aolv = np.asarray(aol, float)
+    gK = H * aolv * D * dl
+    gal = KA * D * t["dHal"] * dl
+    gN = KA * D * t["dHN"] * dl
+    gQ = np.where(isfree, lfull, 0.0)
+    gD = np.zeros(N)
+    dFa = KA * (t["dHa"] * D - H)       # d flux_into_a / d psi_a
+    dFb = KA * (t["dHb"] * D + H)       # d flux_into_a / d psi_b
+    m = isfree[a] & ~isfree[b]          # k = b Dirichlet, j = a free: dR_a/dpsi_b = dFb
+    np.add.at(gD, b[m], lfull[a[m]] * dFb[m])
+    m = ~isfree[a] & isfree[b]          # k = a Dirichlet, j = b free: dR_b/dpsi_a = -dFa
+    np.add.at(gD, a[m], -lfull[b[m]] * dFa[m])
+    return gK, gD, gal, gN, gQ
+
+
 def pullback(psi, delta, Ks, neighbors, aol, dirichletnodes, z, alphas, Ns, Qs):
     """The reference rrule's tangents at the solution psi (N): dKs, ddirichletpsis, dalphas, dNs, dQs."""
     N = len(Qs)
@@ -146,20 +169,73 @@ def pullback(psi, delta, Ks, neighbors, aol, dirichletnodes, z, alphas, Ns, Qs):
     lam = spla.spsolve(J.T.tocsc(), np.asarray(delta, float)[free])
     lfull = np.zeros(N)
     lfull[free] = lam
-    t = _faces(psi, Ks, nb, aol, z, alphas, Ns)
-    a, b, D, H, KA = t["a"], t["b"], t["D"], t["H"], t["KA"]
-    dl = lfull[a] - lfull[b]            # lambda_a - lambda_b (0 at Dirichlet cells)
-    aolv = np.asarray(aol, float)
-    dKs = -(H * aolv * D * dl)
-    dal = -(KA * D * t["dHal"] * dl)
-    dN = -(KA * D * t["dHN"] * dl)
-    dQs = np.where(isfree, -lfull, 0.0)
-    ddp = np.where(isfree, 0.0, np.asarray(delta, float))
-    # dR_j / d psi_k for a Dirichlet neighbour k of a free cell j
-    dFa = KA * (t["dHa"] * D - H)       # d flux_into_a / d psi_a
-    dFb = KA * (t["dHb"] * D + H)       # d flux_into_a / d psi_b
-    m = isfree[a] & ~isfree[b]          # k = b Dirichlet, j = a free: dR_a/dpsi_b = dFb
-    np.add.at(ddp, b[m], -lfull[a[m]] * dFb[m])
-    m = ~isfree[a] & isfree[b]          # k = a Dirichlet, j = b free: dR_b/dpsi_a = -dFa
-    np.add.at(ddp, a[m], -lfull[b[m]] * (-dFa[m]))
-    return dKs, ddp, dal, dN, dQs
+    gK, gD, gal, gN, gQ = r_transpose(psi, lfull, *args)
+    ddp = np.where(isfree, 0.0, np.asarray(delta, float)) - gD
+    return -gK, ddp, -gal, -gN, -gQ
+
+
+def transient(psi0, Ks, neighbors, aol, dirichletnodes, dirichletpsis, z, alphas, Ns, Qs, Ss, vol, dt, nsteps,
+              tol=1e-13, maxiter=100):
+    """Fixed-step backward Euler of S V dpsi/dt = R(psi): each step the root of
+    S V/dt (psi - psi_old) - R(psi) by Newton with the exact Jacobian; returns the states (nsteps, N)."""
+    N = len(Qs)
+    nb, isfree, free, fmap = _setup(N, neighbors, dirichletnodes)
+    args = (Ks, neighbors, aol, dirichletnodes, z, alphas, Ns, Qs)
+    shift = (np.asarray(Ss, float) * np.asarray(vol, float) / dt)[free]
+    psi = np.where(isfree, np.asarray(psi0, float), np.asarray(dirichletpsis, float))
+    out = []
+    for _ in range(nsteps):
+        old = psi.copy()
+
+        def G(p):
+            return shift * (p[free] - old[free]) - residual(p, *args)
+
+        g = G(psi)
+        scale = max(np.linalg.norm(g), np.linalg.norm(np.asarray(Qs)[free]))
+        for _ in range(maxiter):
+            gn = np.linalg.norm(g)
+            if gn <= tol * scale:
+                break
+            Jg = sp.diags(shift) - jacobian(psi, *args)
+            d = spla.spsolve(Jg.tocsc(), -g)
+            w = 1.0
+            for _ in range(30):
+                trial = psi.copy()
+                trial[free] += w * d
+                gt = G(trial)
+                if np.linalg.norm(gt) < gn:
+                    break
+                w *= 0.5
+            psi, g = trial, gt
+        out.append(psi.copy())
+    return np.array(out)
+
+
+def transient_pullback(states, obs, w, gT, Ks, neighbors, aol, dirichletnodes, z, alphas, Ns, Qs, Ss, vol, dt):
+    """Discrete adjoint of `transient` for J = sum_n sum_k w_k psi^n[obs_k]^2 + gT . psi^nsteps:
+    (dKs, ddirichletpsis, dalphas, dNs, dQs, dpsi0)."""
+    N = len(Qs)
+    nb, isfree, free, fmap = _setup(N, neighbors, dirichletnodes)
+    args = (Ks, neighbors, aol, dirichletnodes, z, alphas, Ns, Qs)
+    shift = np.asarray(Ss, float) * np.asarray(vol, float) / dt
+    obs = np.asarray(obs, np.int64)
+    w = np.ones(len(obs)) if w is None else np.asarray(w, float)
+    nsteps = len(states)
+    tot = None
+    lam_next = np.zeros(N)
+    for n in range(nsteps, 0, -1):
+        psi = states[n - 1]
+        seed = np.zeros(N)
+        np.add.at(seed, obs, 2 * w * psi[obs])
+        if n == nsteps and gT is not None:
+            seed += np.asarray(gT, float)
+        rhs = (seed + shift * lam_next)[free]
+        Jg = sp.diags(shift[free]) - jacobian(psi, *args)
+        lam = np.zeros(N)
+        lam[free] = spla.spsolve(Jg.T.tocsc(), rhs)
+        g = r_transpose(psi, lam, *args)
+        g = (g[0], g[1] + np.where(isfree, 0.0, seed), g[2], g[3], g[4])
+        tot = g if tot is None else tuple(x + y for x, y in zip(tot, g))
+        lam_next = lam
+    dpsi0 = np.where(isfree, shift * lam_next, 0.0)
+    return tot + (dpsi0,)

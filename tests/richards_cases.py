@@ -29,3 +29,16 @@ def richards_case(pkg, ns=(8, 6, 4), seed=0, psi_top=-4.0, alpha=0.375, nvg=1.25
 
 def oracle_args(c):
     return (c["Ks"], c["nb"], c["aol"], c["dn"], c["z"], c["alphas"], c["Ns"], c["Qs"])
+
+
+def transient_case(pkg, ns=(5, 4, 4), seed=4):
+    c = richards_case(pkg, ns=ns, seed=seed, psi_top=-1.0)
+    mins, maxs = (0.0, 0.0, 0.0), (7.0, 5.0, 3.0)
+    _, _, _, vol = pkg.regulargrid3d(mins, maxs, ns)
+    c.update(vol=vol, Ss=np.full(c["N"], 0.2), dt=20000.0, nsteps=5,
+             psi0=np.where(np.isin(np.arange(c["N"]), c["dn"]), c["dpsi"], -2.0))
+    rng = np.random.default_rng(seed + 50)
+    c["obs"] = rng.choice(np.setdiff1d(np.arange(c["N"]), c["dn"]), 6, replace=False)
+    c["w"] = rng.uniform(0.5, 1.5, 6)
+    c["gT"] = rng.standard_normal(c["N"]) * 0.1
+    return c

@@ -59,3 +59,22 @@ def test_structured_handle_is_refused(gpu_lib):
     with pytest.raises(pkg.DPFError) as e:
         P.richards_steady(c["psi0"], c["Ks"], c["dpsi"], c["z"], c["alphas"], c["Ns"], c["Qs"])
     assert e.value.code == pkg._lib.DPF_UNSUPPORTED
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_transient_richards_vs_oracle(gpu_lib, precision):
+    from richards_cases import transient_case
+    pkg = gpu_lib
+    c = transient_case(pkg, ns=(8, 6, 4))
+    st_or = ro.transient(c["psi0"], c["Ks"], c["nb"], c["aol"], c["dn"], c["dpsi"], c["z"], c["alphas"], c["Ns"],
+                         c["Qs"], c["Ss"], c["vol"], c["dt"], c["nsteps"], tol=1e-14)
+    g_or = ro.transient_pullback(st_or, c["obs"], c["w"], c["gT"], c["Ks"], c["nb"], c["aol"], c["dn"], c["z"],
+                                 c["alphas"], c["Ns"], c["Qs"], c["Ss"], c["vol"], c["dt"])
+    P = pkg.GroundwaterProblem(c["nb"], c["aol"], c["dn"], N=c["N"], volumes=c["vol"], general=True,
+                               precision=precision, reltol=1e-12)
+    psiT, st = P.richards_transient_forward(c["psi0"], c["Ks"], c["dpsi"], c["z"], c["alphas"], c["Ns"], c["Qs"],
+                                            c["Ss"], c["dt"], c["nsteps"], tol=1e-12, return_states=True)
+    assert rel(st, st_or) < 1e-9 and rel(psiT, st_or[-1]) < 1e-9
+    g = P.richards_transient_adjoint(c["obs"], c["w"], c["gT"], tol=1e-11)
+    for got, want, name in zip(g, g_or, ("dKs", "ddirichletpsis", "dalphas", "dNs", "dQs", "dpsi0")):
+        assert rel(got, want) < 1e-7, name

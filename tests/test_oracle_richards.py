@@ -68,3 +68,37 @@ def test_pullback_matches_finite_differences(pkg, which):
     cm[which] = c[which] - step
     fd = (J(cp)[0] - J(cm)[0]) / 2
     assert fd == pytest.approx(float(grad @ step), rel=2e-4)
+
+
+@pytest.mark.parametrize("which", ["Ks", "alphas", "Qs", "dpsi", "psi0"])
+def test_transient_pullback_matches_finite_differences(pkg, which):
+    from richards_cases import transient_case
+    c = transient_case(pkg)
+
+    def J(cc):
+        st = ro.transient(cc["psi0"], cc["Ks"], cc["nb"], cc["aol"], cc["dn"], cc["dpsi"], cc["z"], cc["alphas"],
+                          cc["Ns"], cc["Qs"], cc["Ss"], cc["vol"], cc["dt"], cc["nsteps"], tol=1e-14)
+        j = sum(float(np.sum(c["w"] * s[c["obs"]] ** 2)) for s in st) + float(c["gT"] @ st[-1])
+        return j, st
+
+    _, st = J(c)
+    g = ro.transient_pullback(st, c["obs"], c["w"], c["gT"], c["Ks"], c["nb"], c["aol"], c["dn"], c["z"], c["alphas"],
+                              c["Ns"], c["Qs"], c["Ss"], c["vol"], c["dt"])
+    grad = {"Ks": g[0], "dpsi": g[1], "alphas": g[2], "Qs": g[4], "psi0": g[5]}[which]
+    rng = np.random.default_rng(9)
+    d = rng.standard_normal(len(c[which]))
+    isd = np.isin(np.arange(c["N"]), c["dn"])
+    if which == "dpsi":
+        d = np.where(isd, d, 0.0)
+    if which == "psi0":
+        d = np.where(isd, 0.0, d)
+    scale = {"Ks": 1e-3 * c["Ks"], "alphas": 1e-4 * c["alphas"], "Qs": 1e-9, "dpsi": 1e-5, "psi0": 1e-5}[which]
+    step = d * scale
+    cp, cm = dict(c), dict(c)
+    cp[which] = c[which] + step
+    cm[which] = c[which] - step
+    if which == "dpsi":   # the initial state carries the Dirichlet values too
+        cp["psi0"] = np.where(isd, cp["dpsi"], c["psi0"])
+        cm["psi0"] = np.where(isd, cm["dpsi"], c["psi0"])
+    fd = (J(cp)[0] - J(cm)[0]) / 2
+    assert fd == pytest.approx(float(grad @ step), rel=2e-4)
