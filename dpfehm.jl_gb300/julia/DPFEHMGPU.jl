@@ -190,6 +190,38 @@ function richards_forward(p::Problem, psi0, Ks, dirichletpsis, coords, alphas, N
     return psi
 end
 
+"""Fixed-step backward Euler of S V dpsi/dt = richards_residuals(psi) on a `GeneralProblem`:
+psi at the final step and the (N, nsteps) states."""
+function richards_transient(p::Problem, psi0, Ks, dirichletpsis, coords, alphas, Ns, Qs, specificstorage, dt, nsteps;
+                            tol=1e-10, maxiter=200)
+    psiT = Vector{Float64}(undef, p.N)
+    states = Matrix{Float64}(undef, p.N, nsteps)
+    z = Vector{Float64}(coords[3, :])
+    rc = ccall((:dpf_richards_transient_forward, libdpf), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+         Ptr{Float64}, Cdouble, Cint, Cdouble, Cint, Ptr{Float64}, Ptr{Float64}), p.ptr, Vector{Float64}(psi0),
+        Vector{Float64}(Ks), Vector{Float64}(dirichletpsis), z, Vector{Float64}(alphas), Vector{Float64}(Ns),
+        Vector{Float64}(Qs), Vector{Float64}(specificstorage), dt, nsteps, tol, maxiter, states, psiT)
+    check(p.ptr, rc)
+    return psiT, states
+end
+
+"""Tangents (dKs, ddirichletpsis, dalphas, dNs, dQs, dpsi0) of the last `richards_transient` run for
+J = sum_n sum_k w_k psi^n[obs_k]^2 + gT . psi^T (obs 1-based; gT may be `nothing`)."""
+function richards_transient_adjoint(p::Problem, obs, w=nothing, gT=nothing; tol=1e-10, maxiter=200)
+    o = Int64[k - 1 for k in obs]
+    ww = w === nothing ? Ptr{Float64}(C_NULL) : Vector{Float64}(w)
+    gg = gT === nothing ? Ptr{Float64}(C_NULL) : Vector{Float64}(gT)
+    dKs = Vector{Float64}(undef, p.F); dal = Vector{Float64}(undef, p.F); dN = Vector{Float64}(undef, p.F)
+    ddp = Vector{Float64}(undef, p.N); dQs = Vector{Float64}(undef, p.N); d0 = Vector{Float64}(undef, p.N)
+    rc = ccall((:dpf_richards_transient_adjoint, libdpf), Cint,
+        (Ptr{Cvoid}, Int64, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Cdouble, Cint, Ptr{Float64}, Ptr{Float64},
+         Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}), p.ptr, length(o), o, ww, gg, tol, maxiter, dKs, ddp,
+        dal, dN, dQs, d0)
+    check(p.ptr, rc)
+    return dKs, ddp, dal, dN, dQs, d0
+end
+
 """Drop-in for `DPFEHM.richards_steadystate` (src/richards.jl:148-167)."""
 richards_steadystate(psi0, Ks, neighbors, areasoverlengths, dirichletnodes, dirichletpsis, coords, alphas, Ns, Qs;
                      tol=1e-10, maxiter=200, kwargs...) =
