@@ -107,6 +107,7 @@ __global__ void richards_residual(int n, const int *__restrict__ irp, const int 
             for (int k = irp[i]; k < irp[i + 1]; k++) {
                 const int f = ifc[k];
                 const int j = fa[f] == i ? fb[f] : fa[f];
+                if (!DPF_INSIDE(CK_NEIGHBOUR, j, 0, n)) continue;
                 r += Kh[f] * aol[f] * (psi[j] + z[j] - hi);
             }
             qq += Qs[i] * Qs[i];
@@ -177,6 +178,7 @@ __global__ void richards_adjoint_rhs(int n, const int *__restrict__ irp, const i
                     const int f = ifc[k];
                     const bool isa = fa[f] == i;
                     const int j = isa ? fb[f] : fa[f];
+                    if (!DPF_INSIDE(CK_NEIGHBOUR, j, 0, n)) continue;
                     const double mj = dir[j] ? 0.0 : mu[j];
                     r += (isa ? na[f] : nb[f]) * (mi - mj);
                 }
@@ -256,6 +258,7 @@ __global__ void richards_cell_grads(int n, const int *__restrict__ irp, const in
         for (int e = irp[k]; e < irp[k + 1]; e++) {
             const int f = ifc[e];
             const int j = fa[f] == k ? fb[f] : fa[f];
+            if (!DPF_INSIDE(CK_NEIGHBOUR, j, 0, n)) continue;
             if (dir[j]) continue;
             const Kr kk = kr_vg(psi[k], alphas[f], Ns[f]), kj = kr_vg(psi[j], alphas[f], Ns[f]);
             const double s = kk.v + kj.v;

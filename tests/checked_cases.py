@@ -21,7 +21,9 @@ sys.path.insert(0, HERE)
 
 import __graft_entry__ as g  # noqa: E402
 import oracle as orc  # noqa: E402
+import richards_oracle as ro  # noqa: E402
 from helpers import rel, steady_case  # noqa: E402
+from richards_cases import oracle_args, richards_case, transient_case  # noqa: E402
 
 SHAPES = [(2, 2, 2), (3, 3, 3), (1, 5, 4), (4, 1, 3), (5, 4, 1), (7, 5, 3), (8, 8, 8), (17, 9, 6), (33, 20, 11)]
 
@@ -37,7 +39,8 @@ def main():
     pkg = g.load_package()
     lib = pkg.load()
     orc.build()
-    err = {"steady": 0.0, "adjoint": 0.0, "batch": 0.0, "csr": 0.0, "transient": 0.0}
+    err = {"steady": 0.0, "adjoint": 0.0, "batch": 0.0, "csr": 0.0, "transient": 0.0, "richards": 0.0,
+           "richards_adjoint": 0.0}
     for k, ns in enumerate(SHAPES):
         c = steady_case(pkg, ns, sigma=1.0, seed=40 + k, ndir=1 if k % 2 == 0 else 3, nq=1)
         delta = np.random.default_rng(k).standard_normal(c["N"])
@@ -88,6 +91,26 @@ def main():
     P = pkg.GroundwaterProblem(c["nb"], c["aol"], c["dn"], N=N, volumes=c["vol"], reltol=1e-12)
     _, states = P.transient_forward(c["Ks"], c["dh"], c["Qs"], Ss, 3600.0, 4, np.zeros(N), return_states=True)
     err["transient"] = rel(states[:, isf], st_or)
+    P.close()
+
+    # Richards: a steady solve with its pullback and a short transient run, on the CSR handle
+    c = richards_case(pkg, ns=(7, 5, 4), seed=12)
+    psi_or = ro.steady(c["psi0"], c["Ks"], c["nb"], c["aol"], c["dn"], c["dpsi"], c["z"], c["alphas"], c["Ns"],
+                       c["Qs"], tol=1e-14)
+    w = np.random.default_rng(6).standard_normal(c["N"])
+    g_or = ro.pullback(psi_or, w, *oracle_args(c))
+    psi, pb = pkg.rrule_richards_steadystate(c["psi0"], c["Ks"], c["nb"], c["aol"], c["dn"], c["dpsi"], c["coords"],
+                                             c["alphas"], c["Ns"], c["Qs"], tol=1e-12, reltol=1e-12)
+    err["richards"] = rel(psi, psi_or)
+    t = pb(w)
+    err["richards_adjoint"] = max(rel(t[2], g_or[0]), rel(t[10], g_or[4]))
+    c = transient_case(pkg, ns=(6, 5, 4))
+    st_or = ro.transient(c["psi0"], c["Ks"], c["nb"], c["aol"], c["dn"], c["dpsi"], c["z"], c["alphas"], c["Ns"],
+                         c["Qs"], c["Ss"], c["vol"], c["dt"], c["nsteps"], tol=1e-14)
+    P = pkg.GroundwaterProblem(c["nb"], c["aol"], c["dn"], N=c["N"], volumes=c["vol"], general=True, reltol=1e-12)
+    _, st = P.richards_transient_forward(c["psi0"], c["Ks"], c["dpsi"], c["z"], c["alphas"], c["Ns"], c["Qs"],
+                                         c["Ss"], c["dt"], c["nsteps"], tol=1e-12, return_states=True)
+    err["richards"] = max(err["richards"], rel(st, st_or))
     P.close()
 
     import ctypes

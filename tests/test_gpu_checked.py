@@ -28,6 +28,7 @@ def test_checked_build_runs_clean(gpu_lib):
     e = out["errors"]
     assert e["steady"] < 1e-8 and e["batch"] < 1e-8 and e["csr"] < 1e-8 and e["transient"] < 1e-8, e
     assert e["adjoint"] < 1e-6, e
+    assert e["richards"] < 1e-8 and e["richards_adjoint"] < 1e-6, e
 
 
 def test_regular_build_has_no_checks(gpu_lib):
