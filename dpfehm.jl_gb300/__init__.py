@@ -460,7 +460,8 @@ def autotune_batch(dims, mins, maxs, dirichletnodes, logK, dirichleths, Qs, obs_
                                 dn.ctypes.data, ctypes.byref(base), lk.ptr, _MEANS[mean], d.ptr, q.ptr,
                                 offs.ctypes.data, ob.ctypes.data, int(repeats), ctypes.byref(best), ctypes.byref(ms))
     if rc != _lib.DPF_OK:
-        raise DPFError(rc, "autotuning failed (the starting options do not give a converged solve)")
+        msg = lib.dpf_last_error(None).decode() if rc == _lib.DPF_CUDA else ""
+        raise DPFError(rc, msg or "autotuning failed (the starting options do not give a converged solve)")
     return {k: getattr(best, k) for k in _TUNED}, ms.value
 
 

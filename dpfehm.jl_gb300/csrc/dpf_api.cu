@@ -108,16 +108,15 @@ struct dpf_problem {
     std::vector<cudaEvent_t> part_events;
     std::unique_ptr<PartPool> pool;
     ~dpf_problem() {
+        // a part's own stream is drained before anything its work may still use is released
+        if (own_stream && stream) cudaStreamSynchronize(stream);
         pool.reset();
         for (dpf_problem *q : parts) delete q;
         for (cudaEvent_t e : part_events) cudaEventDestroy(e);
         sb.reset();
         gs.reset();
         for (void *p : scratch) dev_free(p);
-        if (own_stream && stream) {
-            cudaStreamSynchronize(stream);
-            cudaStreamDestroy(stream);
-        }
+        if (own_stream && stream) cudaStreamDestroy(stream);
     }
 };
 

@@ -13,10 +13,15 @@
 
 #include <cstdint>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "dpfehm_gpu.h"
 #include "dpf_internal.h"
+
+namespace dpf {
+void set_global_error(const std::string &msg);
+}
 
 namespace {
 
@@ -103,30 +108,39 @@ extern "C" int dpf_batch_autotune(int nprob, const int *dims, const double *mins
     if (rc == DPF_OK) {
         const bool mixed = cur.precision == DPF_PREC_MIXED && cur.plane > 0;
         struct Knob {
+            const char *name;
             int *field;
             std::vector<int> values;
             bool active;
         };
         const Knob knobs[] = {
-            {&cur.cheb_degree, {1, 2, 3}, true},
-            {&cur.plane_cells, {512, 768, 1024}, mixed},
-            {&cur.plane_blocks_per_sm, {1, 2, 3}, mixed},
-            {&cur.tail_cells, {-1, 1024, 4096, 16384}, true},
-            {&cur.blocks_per_sm, {8, 16, 24}, true},
-            {&cur.df_plane_cells, {-1, 512}, mixed},
-            {&cur.tail_cluster, {1, 8}, true},
-            {&cur.plane_levels, {0, 1, 2}, mixed},
-            {&cur.streams, {1, 2, 4}, true},
+            {"cheb_degree", &cur.cheb_degree, {1, 2, 3}, true},
+            {"plane_cells", &cur.plane_cells, {512, 768, 1024}, mixed},
+            {"plane_blocks_per_sm", &cur.plane_blocks_per_sm, {1, 2, 3}, mixed},
+            {"tail_cells", &cur.tail_cells, {-1, 1024, 4096, 16384}, true},
+            {"blocks_per_sm", &cur.blocks_per_sm, {8, 16, 24}, true},
+            {"df_plane_cells", &cur.df_plane_cells, {-1, 512}, mixed},
+            {"tail_cluster", &cur.tail_cluster, {1, 8}, true},
+            {"plane_levels", &cur.plane_levels, {0, 1, 2}, mixed},
+            {"streams", &cur.streams, {1, 2, 4}, true},
         };
         for (const Knob &k : knobs) {
-            if (!k.active) continue;
+            if (!k.active || rc != DPF_OK) continue;
             const int keep = *k.field;
             int pick = keep;
             for (int v : k.values) {
                 if (v == keep) continue;
                 *k.field = v;
                 double ms = 0.0;
-                if (evaluate(cur, ms) == DPF_OK && ms < 0.98 * cur_ms) {
+                const int r = evaluate(cur, ms);
+                if (r == DPF_CUDA) {
+                    // a CUDA error is not a slow candidate: stop and name the candidate
+                    dpf::set_global_error(std::string("autotune: candidate ") + k.name + " = " + std::to_string(v) +
+                                          ": " + cudaGetErrorString(cudaGetLastError()));
+                    rc = DPF_CUDA;
+                    break;
+                }
+                if (r == DPF_OK && ms < 0.98 * cur_ms) {
                     cur_ms = ms;
                     pick = v;
                 }
