@@ -672,11 +672,8 @@ __global__ void k_update_p(const LevelDesc *__restrict__ desc, const int4 *__res
 
 // q = A p in double-float (flux form); alpha = rz / (p . q) (hi parts: q is accurate, so
 // its leading float is too)
-// 4 resident blocks (64 registers): the packed stencil spills at 32-48 registers, and the
-// spill traffic cost more than the occupancy gained (8 blocks: 3728 GB/s, 4 blocks: 4407 GB/s
-// on the 8 x 1M-cell solve)
 #ifndef DPF_DF_SPMV_MINB
-#define DPF_DF_SPMV_MINB 4
+#define DPF_DF_SPMV_MINB 8
 #endif
 __global__ void __launch_bounds__(kBlock, DPF_DF_SPMV_MINB) k_df_spmv_pq(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                              int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, CoeffsDF C,
@@ -684,29 +681,19 @@ __global__ void __launch_bounds__(kBlock, DPF_DF_SPMV_MINB) k_df_spmv_pq(const L
     pdl_enter();
     DPF_BLOCK_PROLOGUE(desc, bmap, st)
     Acc<float> part;
-    const int sy = L.nz, sx = L.ny * L.nz;  // one plane of one problem: far below 2^31 cells
+    const long long sy = L.nz, sx = (long long)L.ny * L.nz;
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
         Cell c;
         cell_at(L, li_, c);
         const long long i = c.i;
         const float2 pi = pv[i];
-        // The two faces of an axis go through the f32x2 lanes together. A face outside the
-        // grid takes the cell itself as its neighbour: the difference is then exactly zero,
-        // and so is its term (a missing upper face also has a stored coefficient of zero).
-        const DFx2 pp = dfx2_of(pi, pi);
-        const float2 *__restrict__ P = pv + i;
-        auto axis = [&](const float2 *__restrict__ cd, int up, int down) {
-#if DPF_CHECKED
-            if (!DPF_INSIDE(CK_NEIGHBOUR, i + up, L.off, L.off + L.n)) up = 0;
-            if (!DPF_INSIDE(CK_NEIGHBOUR, i + down, L.off, L.off + L.n)) down = 0;
-#endif
-            return dfx2_mul(dfx2_of(cd[i], cd[i + down]), dfx2_sub(pp, dfx2_of(P[up], P[down])));
-        };
-        DFx2 acc = axis(C.cz, c.iz + 1 < L.nz ? 1 : 0, c.iz > 0 ? -1 : 0);
-        acc = dfx2_add(acc, axis(C.cy, c.iy + 1 < L.ny ? sy : 0, c.iy > 0 ? -sy : 0));
-        acc = dfx2_add(acc, axis(C.cx, c.ix + 1 < L.nx ? sx : 0, c.ix > 0 ? -sx : 0));
-        const float2 h = x2_unpack(acc.hi), l = x2_unpack(acc.lo);
-        const float2 a = df_add(df_mul(C.leak[i], pi), df_add(make_float2(h.x, l.x), make_float2(h.y, l.y)));
+        float2 a = df_mul(C.leak[i], pi);
+        if (c.iz + 1 < L.nz) a = df_add(a, df_mul(C.cz[i], df_sub(pi, pv[i + 1])));
+        if (c.iz > 0) a = df_add(a, df_mul(C.cz[i - 1], df_sub(pi, pv[i - 1])));
+        if (c.iy + 1 < L.ny) a = df_add(a, df_mul(C.cy[i], df_sub(pi, pv[i + sy])));
+        if (c.iy > 0) a = df_add(a, df_mul(C.cy[i - sy], df_sub(pi, pv[i - sy])));
+        if (c.ix + 1 < L.nx) a = df_add(a, df_mul(C.cx[i], df_sub(pi, pv[i + sx])));
+        if (c.ix > 0) a = df_add(a, df_mul(C.cx[i - sx], df_sub(pi, pv[i - sx])));
         q[i] = a;
         part = part + Acc<float>::prod(pi.x, a.x);
     }

@@ -316,81 +316,6 @@ __device__ __forceinline__ float2 df_from_double(double v) {
 }
 __device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + (double)a.y; }
 
-// Packed float pairs: two FP32 lanes in one 64-bit register, operated on by the f32x2 add,
-// sub, mul and fma instructions of sm_100-class GPUs (one issue slot for both lanes, each
-// lane rounded to nearest exactly like its scalar form; inline PTX is never contracted).
-typedef unsigned long long f32x2;
-__device__ __forceinline__ f32x2 x2_pack(float a, float b) {
-    f32x2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ float2 x2_unpack(f32x2 r) {
-    float2 v;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
-    return v;
-}
-__device__ __forceinline__ f32x2 x2_add(f32x2 a, f32x2 b) {
-    f32x2 r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 x2_sub(f32x2 a, f32x2 b) {
-    f32x2 r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 x2_mul(f32x2 a, f32x2 b) {
-    f32x2 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 x2_fma(f32x2 a, f32x2 b, f32x2 c) {
-    f32x2 r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-
-// Two double-float numbers, lane by lane: hi holds both leading words, lo both trailing
-// words. Each operation performs the scalar df_* steps above in the same order, so every
-// lane's result equals the scalar form's (up to the sign of a zero).
-struct DFx2 {
-    f32x2 hi, lo;
-};
-__device__ __forceinline__ DFx2 dfx2_of(float2 a, float2 b) { return {x2_pack(a.x, b.x), x2_pack(a.y, b.y)}; }
-__device__ __forceinline__ DFx2 dfx2_quick(f32x2 s, f32x2 e) {
-    const f32x2 h = x2_add(s, e);
-    return {h, x2_sub(e, x2_sub(h, s))};
-}
-__device__ __forceinline__ DFx2 dfx2_add(DFx2 a, DFx2 b) {
-    const f32x2 s = x2_add(a.hi, b.hi);
-    const f32x2 bb = x2_sub(s, a.hi);
-    f32x2 e = x2_add(x2_sub(a.hi, x2_sub(s, bb)), x2_sub(b.hi, bb));
-    e = x2_add(e, x2_add(a.lo, b.lo));
-    return dfx2_quick(s, e);
-}
-// a - b as df_add(a, -b): two-sum with the negated operand, written with subtractions
-// (-b - bb == -(b + bb) and x + (-y) == x - y exactly under round-to-nearest)
-__device__ __forceinline__ DFx2 dfx2_sub(DFx2 a, DFx2 b) {
-    const f32x2 s = x2_sub(a.hi, b.hi);
-    const f32x2 bb = x2_sub(s, a.hi);
-    f32x2 e = x2_sub(x2_sub(a.hi, x2_sub(s, bb)), x2_add(b.hi, bb));
-    e = x2_add(e, x2_sub(a.lo, b.lo));
-    return dfx2_quick(s, e);
-}
-__device__ __forceinline__ DFx2 dfx2_mul(DFx2 a, DFx2 b) {
-    // The rounding error of the leading product is taken lane by lane with scalar fmaf: the
-    // packed form fma.rn.f32x2(a, b, -(a*b)) gave inexact error terms inside the double-float
-    // CG product (CG then stalled near 1e-7), although the same instruction sequence matched
-    // fmaf bit for bit in an isolated test. The cross terms below only need to be small.
-    const f32x2 p = x2_mul(a.hi, b.hi);
-    const float2 ah = x2_unpack(a.hi), bh = x2_unpack(b.hi), ph = x2_unpack(p);
-    f32x2 e = x2_pack(fmaf(ah.x, bh.x, -ph.x), fmaf(ah.y, bh.y, -ph.y));
-    e = x2_fma(a.hi, b.lo, e);
-    e = x2_fma(a.lo, b.hi, e);
-    return dfx2_quick(p, e);
-}
-
 // Face conductances from cell values kc, computed once per cell by k_cell_k
 // (GB300 has little FP64 throughput, so exp runs once per cell, not once per face):
 //   geometric  kc = exp(logK / 2):  K_f = exp((logK_a + logK_b)/2) = kc_a kc_b
