@@ -9,12 +9,17 @@
 //
 // Here the nonlinear solve is a Picard iteration: A(psi) d = R(psi), psi += d, where A(psi) is the
 // groundwater operator with face conductances K_f hm(kr_j, kr_k) (symmetric positive definite,
-// solved by the handle's CG + AMG). Writing the Jacobian as J = -A + N (N: the terms of the
-// derivatives of kr), the adjoint J^T lambda = delta becomes, with mu = -lambda, the fixed point
-// mu = A^-1 (delta + N^T mu); its contraction factor is that of the Picard iteration at the
-// solution, so it converges wherever the forward iteration does. Both reach the roots of the
-// reference's equations; only the iteration differs.
+// solved by the handle's CG + AMG), with step halving while the residual does not drop. Writing
+// the Jacobian as J = -A + N (N: the terms of the derivatives of kr), the adjoint
+// J^T lambda = delta becomes, with mu = -lambda, (I - A^-1 N^T) mu = A^-1 delta, solved by
+// restarted GMRES(30) whose every step is one N^T product and one CG + AMG solve (the plain
+// fixed point mu = A^-1 (delta + N^T mu) can diverge: an eigenvalue of A^-1 N^T below -1 is what
+// the forward iteration's step halving damps). Both reach the roots of the reference's
+// equations; only the iteration differs. Transient runs take fixed backward-Euler steps of
+// S V dpsi/dt = R(psi) on the shifted operator S V / dt + A(psi), and the adjoint runs backward
+// in time over the stored states.
 #include <algorithm>
+#include <cstring>
 #include <cmath>
 #include <vector>
 
@@ -659,13 +664,10 @@ int GeneralSolver::richards_transient_adjoint(long long nobs, const int64_t *obs
     if (rt_nsteps < 1) throw DpfError("transient Richards adjoint called before a transient Richards run", DPF_STATE);
     const unsigned nbF = rblocks(F, nblocks), nbN = rblocks(N, nblocks);
     std::vector<long long> ho(nobs);
-    for (long long k = 0; k < nobs; k++) {
-        long long v = 0;
-        if (r_is_device(obs)) rck(cudaMemcpy(&v, obs + k, sizeof(int64_t), cudaMemcpyDeviceToHost), "obs");
-        else v = obs[k];
-        if (v < 0 || v >= N) throw BadInput("observation index out of range");
-        ho[k] = v;
-    }
+    if (nobs && r_is_device(obs)) rck(cudaMemcpy(ho.data(), obs, nobs * sizeof(int64_t), cudaMemcpyDeviceToHost), "obs");
+    else if (nobs) std::memcpy(ho.data(), obs, nobs * sizeof(int64_t));
+    for (long long k = 0; k < nobs; k++)
+        if (ho[k] < 0 || ho[k] >= N) throw BadInput("observation index out of range");
     long long *d_obs = dev<long long>(std::max(nobs, 1LL));
     double *d_w = w ? dev<double>(std::max(nobs, 1LL)) : nullptr;
     double *d_gT = gT ? dev<double>(N) : nullptr;
