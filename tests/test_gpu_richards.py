@@ -78,3 +78,19 @@ def test_transient_richards_vs_oracle(gpu_lib, precision):
     g = P.richards_transient_adjoint(c["obs"], c["w"], c["gT"], tol=1e-11)
     for got, want, name in zip(g, g_or, ("dKs", "ddirichletpsis", "dalphas", "dNs", "dQs", "dpsi0")):
         assert rel(got, want) < 1e-7, name
+
+
+def test_thiem_richards_matches_groundwater(gpu_lib):
+    """The reference's Richards-against-groundwater check (test/thiem.jl:72-98) on the GPU: the
+    saturated Richards solve and the groundwater solve of the Thiem setup agree to the solvers'
+    tolerance (the reference asks 1e-4), and both give the Thiem drawdowns within 1e-1."""
+    from test_oracle_richards import _thiem_setup
+    pkg = gpu_lib
+    t = _thiem_setup(pkg)
+    h_gw = pkg.groundwater_steadystate(t["Ks"], t["nb"], t["aol"], t["dn"], t["dh"], t["Qs"], reltol=1e-12)
+    psi = pkg.richards_steadystate(np.full(t["N"], t["steadyhead"]), t["Ks"], t["nb"], t["aol"], t["dn"], t["dh"],
+                                   t["coords3"], t["alphas"], t["Ns"], t["Qs"], tol=1e-12, reltol=1e-12)
+    dd_gw = t["steadyhead"] - h_gw[t["good"]]
+    dd_r = t["steadyhead"] - psi[t["good"]]
+    assert np.linalg.norm(dd_r - dd_gw) <= 1e-8 * np.linalg.norm(dd_gw)
+    assert np.linalg.norm(t["thiem"] - dd_r) <= 1e-1 * max(np.linalg.norm(t["thiem"]), np.linalg.norm(dd_r))

@@ -102,3 +102,38 @@ def test_transient_pullback_matches_finite_differences(pkg, which):
         cm["psi0"] = np.where(isd, cm["dpsi"], c["psi0"])
     fd = (J(cp)[0] - J(cm)[0]) / 2
     assert fd == pytest.approx(float(grad @ step), rel=2e-4)
+
+
+def _thiem_setup(pkg):
+    """The reference's Thiem configuration (test/thiem.jl:27-47): a 101 x 101 grid, a sink at the
+    centre, head 1000 m on the ring r >= 50 m (saturated everywhere, so kr = 1)."""
+    steadyhead, sidelength, thickness, n = 1e3, 50.0, 10.0, 101
+    coords, nb, aol, _ = pkg.regulargrid2d([-sidelength, -sidelength], [sidelength, sidelength], [n, n], thickness)
+    N = coords.shape[1]
+    k, Q = 1e-5, 1e-3
+    Qs = np.zeros(N)
+    Qs[n * ((n + 1) // 2 - 1) + (n + 1) // 2 - 1] = -Q
+    r = np.sqrt(coords[0] ** 2 + coords[1] ** 2)
+    dn = np.nonzero(r >= sidelength)[0]
+    dh = np.zeros(N)
+    dh[dn] = steadyhead
+    coords3 = np.vstack([coords, np.zeros(N)])        # z = 0, as the reference's vcat(coords, zeros)
+    good = np.nonzero((coords[1] == 0) & (coords[0] > 0.1))[0]
+    thiem = Q * np.log(sidelength / coords[0, good]) / (2 * np.pi * thickness * k)
+    return dict(N=N, nb=nb, aol=aol, Ks=np.full(len(nb), k), Qs=Qs, dn=dn, dh=dh, coords3=coords3, good=good,
+                thiem=thiem, steadyhead=steadyhead, alphas=np.full(len(nb), 0.5), Ns=np.full(len(nb), 1.25))
+
+
+def test_richards_thiem_matches_groundwater(orc, pkg):
+    """The reference's Richards-against-groundwater check (test/thiem.jl:72-98): the saturated
+    Richards solution on the Thiem setup gives the groundwater drawdowns (rtol 1e-4 there; the
+    equations coincide when kr = 1, so here to the solvers' tolerance) and the Thiem drawdowns
+    (rtol 1e-1)."""
+    t = _thiem_setup(pkg)
+    h_gw = orc.Problem(t["N"], t["nb"], t["aol"], t["dn"]).steady(t["Ks"], t["dh"], t["Qs"], reltol=1e-13)
+    psi = ro.steady(np.full(t["N"], t["steadyhead"]), t["Ks"], t["nb"], t["aol"], t["dn"], t["dh"], t["coords3"][2],
+                    t["alphas"], t["Ns"], t["Qs"], tol=1e-13)
+    dd_gw = t["steadyhead"] - h_gw[t["good"]]
+    dd_r = t["steadyhead"] - psi[t["good"]]
+    assert np.linalg.norm(dd_r - dd_gw) <= 1e-8 * np.linalg.norm(dd_gw)
+    assert np.linalg.norm(t["thiem"] - dd_r) <= 1e-1 * max(np.linalg.norm(t["thiem"]), np.linalg.norm(dd_r))
