@@ -322,16 +322,18 @@ __global__ void kg_coarse_solve(int n, CgState *st, const double *__restrict__ I
 }
 
 // ------------------------------------------------------------ CG kernels (FP64)
+// |b| over the free rows only (identity rows hold their Dirichlet values exactly; the
+// reference measures reltol against the free cells' right-hand side)
 __global__ void kg_cg_start(int n, CgState *st, int *active_count, ReduceScratch rs, GOp<double> A,
-                            const double *__restrict__ b, const double *__restrict__ x, double *__restrict__ r,
-                            double tol2) {
+                            const uint8_t *__restrict__ dir, const double *__restrict__ b,
+                            const double *__restrict__ x, double *__restrict__ r, double tol2) {
     Acc<double> rr, bb;
     GSTRIDE(i, n) {
         double dg;
         double ri = b[i] - g_apply<double>(i, A, x[i], [&](int j) { return x[j]; }, dg);
         r[i] = ri;
         rr.v += ri * ri;
-        bb.v += b[i] * b[i];
+        if (!dir[i]) bb.v += b[i] * b[i];
     }
     double2 tot;
     if (reduce_last<double, 2>(rr, bb, rs, make_int2(0, gridDim.x), 0, tot) && threadIdx.x == 0) {
@@ -467,8 +469,9 @@ __global__ void kg_df_update_p(int n, const CgState *st, const float *__restrict
 // true FP64 residual; decides whether a (further) double-float round is needed
 template <bool FIRST>
 __global__ void kg_df_residual(int n, CgState *st, int *active_count, ReduceScratch rs, GOp<double> A,
-                               const double *__restrict__ b, const double *__restrict__ x, double *__restrict__ r,
-                               double tol2, int maxiter, int max_rounds) {
+                               const uint8_t *__restrict__ dir, const double *__restrict__ b,
+                               const double *__restrict__ x, double *__restrict__ r, double tol2, int maxiter,
+                               int max_rounds) {
     if (!FIRST && !st[0].ru_flag) return;
     Acc<double> rr, bb;  // FIRST: |r|^2, |b|^2; otherwise |r|^2 and the FP64 rounding floor
     GSTRIDE(i, n) {
@@ -477,7 +480,9 @@ __global__ void kg_df_residual(int n, CgState *st, int *active_count, ReduceScra
         double ri = b[i] - g_apply<double>(i, A, xi, [&](int j) { return x[j]; }, dg);
         r[i] = ri;
         rr.v += ri * ri;
-        if (FIRST) {
+        if (dir[i]) {
+            // identity row: in neither |b| nor the rounding floor
+        } else if (FIRST) {
             bb.v += b[i] * b[i];
         } else {
             const double f = 0x1p-53 * fma(2.0 * dg, fabs(xi), fabs(b[i]));
@@ -1110,7 +1115,7 @@ void GeneralSolver::pcg(const T *b, T *x, double tol2) {
     T *r = (T *)cgv[0], *z = (T *)cgv[1], *pv = (T *)cgv[2], *q = (T *)cgv[3];
     GOp<double> A = gop<double>(L0);
     GCK(cudaMemsetAsync(d_count, 0, sizeof(int), stream));
-    kg_cg_start<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, A, b, x, r, tol2);
+    kg_cg_start<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, A, L0.dir, b, x, r, tol2);
     GLAUNCH();
     vcycle<T>(r, z);
     kg_update_p<<<nblocks, kBlock, 0, stream>>>(n, d_state, z, pv);
@@ -1134,8 +1139,8 @@ void GeneralSolver::df_pcg(const double *b, double *x, double tol2) {
     float *r32 = (float *)cgv[0], *z32 = (float *)cgv[1];
     GOp<double> A = gop<double>(L0);
     GCK(cudaMemsetAsync(d_count, 0, sizeof(int), stream));
-    kg_df_residual<true><<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, A, b, x, r64, tol2, opt.maxiter,
-                                                         opt.max_outer);
+    kg_df_residual<true><<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, A, L0.dir, b, x, r64, tol2,
+                                                         opt.maxiter, opt.max_outer);
     GLAUNCH();
     const int check = std::max(1, opt.check_every);
     for (int round = 0; round < opt.max_outer && read_active() > 0; round++) {
@@ -1157,7 +1162,7 @@ void GeneralSolver::df_pcg(const double *b, double *x, double tol2) {
             GLAUNCH();
         }
         GCK(cudaMemsetAsync(d_count, 0, sizeof(int), stream));
-        kg_df_residual<false><<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, A, b, x, r64, tol2,
+        kg_df_residual<false><<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, A, L0.dir, b, x, r64, tol2,
                                                               opt.maxiter, opt.max_outer);
         GLAUNCH();
     }

@@ -547,11 +547,15 @@ __global__ void __launch_bounds__(kTailThreads) k_tail_cycle(const TailLevel<T> 
 }
 
 // ---------------------------------------------------------------- CG kernels
-// r = b - A x; reduce (r.r, b.b); activate the problem unless already converged.
+// r = b - A x; reduce (r.r, b.b); activate the problem unless already converged. b.b runs over
+// the free rows only: an identity row holds its Dirichlet value exactly, and the reference's
+// solve (src/groundwater.jl:45-49, 78) measures reltol against the right-hand side of the free
+// cells, so large Dirichlet heads must not loosen the test.
 template <typename T>
 __global__ void k_cg_start(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                            int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo, Coeffs<T> C,
-                           const T *__restrict__ b, const T *__restrict__ x, T *__restrict__ r, double tol2) {
+                           const uint8_t *__restrict__ dir, const T *__restrict__ b, const T *__restrict__ x,
+                           T *__restrict__ r, double tol2) {
     pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const int p = bm.x;
@@ -566,7 +570,7 @@ __global__ void k_cg_start(const LevelDesc *__restrict__ desc, const int4 *__res
         T ri = bi - Ax;
         r[c.i] = ri;
         rr = rr + Acc<T>::prod(ri, ri);
-        bb = bb + Acc<T>::prod(bi, bi);
+        if (!dir[c.i]) bb = bb + Acc<T>::prod(bi, bi);
     }
     double2 tot;
     if (reduce_last<T, 2>(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
@@ -783,7 +787,9 @@ __global__ void k_df_residual(const LevelDesc *__restrict__ desc, const int4 *__
         }
         r[c.i] = ri;
         rr.v += ri * ri;
-        if (FIRST) {
+        if (dir[c.i]) {
+            // identity row: holds its Dirichlet value exactly; in neither |b| nor the floor
+        } else if (FIRST) {
             bb.v += bi * bi;
         } else {
             // rounding bound of b_i - (A x)_i in FP64, and of storing x itself:
@@ -2234,8 +2240,8 @@ void StructBatch::pcg(const T *b, T *x, double tol2) {
     CK(cudaMemsetAsync(d_count, 0, 4 * sizeof(int), stream));  // active problems, -, loop passes, -
     {
         KTimer _kt(this, kname("k_cg_start", 0, sizeof(T) == 4), L0.all_cells);
-        launch_pdl(k_cg_start<T>, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C, b, x,
-                                                 r, tol2);
+        launch_pdl(k_cg_start<T>, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, d_count, rs, L0.all.d_pinfo, C,
+                   (const uint8_t *)L0.dir, b, x, r, tol2);
     }
     LAUNCH_CHECK();
     vcycle<T>(r, z);
