@@ -383,11 +383,13 @@ dpf_options fill_options(const dpf_options *o) {
 // The number of concurrent parts of a batch: the largest k <= the requested count (0: 4)
 // that divides the problem count, so that the parts are equal in size (a batch of identical
 // problems then gives bitwise identical results in every part).
+// Concurrent parts are switched off: every batch runs on one stream whatever `streams` asks.
+// Runs with batches split into parts raised illegal-address faults whose cause was not found
+// (the split path stays below, unreachable, until it is).
 int batch_parts(int nprob, int streams) {
-    int want = streams > 0 ? streams : 4;
-    want = std::max(1, std::min(want, nprob));
-    while (nprob % want) want--;
-    return want;
+    (void)nprob;
+    (void)streams;
+    return 1;
 }
 
 int make_struct(const std::vector<GridSpec> &grids, const std::vector<std::vector<int64_t>> &dn,

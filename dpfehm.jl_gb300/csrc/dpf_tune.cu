@@ -107,7 +107,6 @@ extern "C" int dpf_batch_autotune(int nprob, const int *dims, const double *mins
     rc = evaluate(cur, cur_ms);
     if (rc == DPF_OK) {
         const bool mixed = cur.precision == DPF_PREC_MIXED && cur.plane > 0;
-        const int fixed_streams = cur.streams;
         struct Knob {
             const char *name;
             int *field;
@@ -123,7 +122,6 @@ extern "C" int dpf_batch_autotune(int nprob, const int *dims, const double *mins
             {"df_plane_cells", &cur.df_plane_cells, {-1, 512}, mixed},
             {"tail_cluster", &cur.tail_cluster, {1, 8}, true},
             {"plane_levels", &cur.plane_levels, {0, 1, 2}, mixed},
-            {"streams", &cur.streams, {1, 2, 4}, fixed_streams == 0},  // a caller's value is kept
         };
         for (const Knob &k : knobs) {
             if (!k.active || rc != DPF_OK) continue;

@@ -94,12 +94,8 @@ typedef struct dpf_options {
     int plane_levels;    /* regular grids, MIXED: the plane-marching kernels run on this many of the
                             finest levels, grid-stride kernels below (default 0: every level whose
                             rows fit a slab) */
-    int streams;         /* batches: the problems run as this many equal concurrent parts, each on its
-                            own stream and host thread, so that one part's bandwidth-bound kernels
-                            overlap another's latency-bound small levels (default 0: up to 4; the
-                            largest count not above the request that divides the problem count).
-                            A split batch handle serves dpf_batch_solve_grad_logk and the query,
-                            profiling and stream entry points; others return DPF_UNSUPPORTED. */
+    int streams;         /* batches: accepted and ignored; every batch runs on one stream (splitting
+                            a batch into concurrent parts is switched off) */
 } dpf_options;
 
 typedef struct dpf_problem dpf_problem;
