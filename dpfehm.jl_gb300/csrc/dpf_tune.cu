@@ -105,6 +105,9 @@ extern "C" int dpf_batch_autotune(int nprob, const int *dims, const double *mins
 
     double cur_ms = 0.0;
     rc = evaluate(cur, cur_ms);
+    if (rc == DPF_CUDA)
+        dpf::set_global_error(std::string("autotune: the starting options: ") +
+                              cudaGetErrorString(cudaGetLastError()));
     if (rc == DPF_OK) {
         const bool mixed = cur.precision == DPF_PREC_MIXED && cur.plane > 0;
         struct Knob {
