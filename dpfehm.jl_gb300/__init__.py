@@ -259,8 +259,10 @@ class GroundwaterProblem:
 
     def richards_transient_adjoint(self, obs, weights=None, gT=None, tol=1e-10, maxiter=200):
         """(dKs, ddirichletpsis, dalphas, dNs, dQs, dpsi0) of J = sum_n sum_k w_k psi^n[obs_k]^2 + gT . psi^T."""
-        ob = np.ascontiguousarray(np.asarray(obs, dtype=np.int64))
-        w = None if weights is None else np.ascontiguousarray(np.asarray(weights, dtype=np.float64))
+        ob = np.ascontiguousarray(np.asarray(obs, dtype=np.int64).ravel())
+        w = None if weights is None else np.ascontiguousarray(np.asarray(weights, dtype=np.float64).ravel())
+        if w is not None and w.size != ob.size:
+            raise ValueError("weights must have one entry per observation (%d), got %d" % (ob.size, w.size))
         g = None if gT is None else _Buf(gT, n=self.N)
         like = g
         dK, dKp = _out(like, self.F)
@@ -419,6 +421,9 @@ class GroundwaterBatch(GroundwaterProblem):
         lk = _Buf(logK, n=self.N)
         d = _Buf(dirichleths, n=self.N)
         q = _Buf(Qs, n=self.N)
+        if len(obs_per_problem) != self.nprob:
+            raise ValueError("obs_per_problem needs one index list per problem (%d), got %d"
+                             % (self.nprob, len(obs_per_problem)))
         offs = np.zeros(self.nprob + 1, np.int64)
         offs[1:] = np.cumsum([len(o) for o in obs_per_problem])
         ob = np.ascontiguousarray(np.concatenate([np.asarray(o, np.int64) for o in obs_per_problem])
@@ -449,6 +454,8 @@ def autotune_batch(dims, mins, maxs, dirichletnodes, logK, dirichleths, Qs, obs_
                               if nd.sum() else np.zeros(0, np.int64))
     N = int(np.prod(dims, axis=1).sum())
     lk, d, q = _Buf(logK, n=N), _Buf(dirichleths, n=N), _Buf(Qs, n=N)
+    if len(obs_per_problem) != nprob or len(dirichletnodes) != nprob:
+        raise ValueError("obs_per_problem and dirichletnodes need one list per problem (%d)" % nprob)
     offs = np.zeros(nprob + 1, np.int64)
     offs[1:] = np.cumsum([len(o) for o in obs_per_problem])
     ob = np.ascontiguousarray(np.concatenate([np.asarray(o, np.int64) for o in obs_per_problem])
