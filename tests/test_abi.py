@@ -119,3 +119,16 @@ def test_create_without_device_reports_no_device(pkg, lib):
     with pytest.raises(pkg.DPFError) as e:
         pkg.GroundwaterProblem.regular3d((0, 0, 0), (1, 1, 1), (3, 3, 3), [26])
     assert e.value.code == 6
+
+
+def test_autotune_rejects_mismatched_lists(lib, pkg):
+    """The per-problem lists are checked against the problem count on the host, before any
+    device call: a single observation list for a batch of two is an error, not a list
+    that silently goes to the first problem."""
+    dims = [(4, 4, 4), (4, 4, 4)]
+    N = 128
+    z = np.zeros(N)
+    with pytest.raises(ValueError):
+        pkg.autotune_batch(dims, [(0, 0, 0)] * 2, [(3, 3, 3)] * 2, [[63], [63]], z, z, z, [np.array([1, 2])])
+    with pytest.raises(ValueError):
+        pkg.autotune_batch(dims, [(0, 0, 0)] * 2, [(3, 3, 3)] * 2, [[63]], z, z, z, [np.array([1]), np.array([2])])
