@@ -307,13 +307,8 @@ def profile_pass(pkg, torch, dev, B, N, prec, args, tuned=None):
     obs = [np.arange(0, N, N // NOBS)[:NOBS]] * B
     # per-kernel events need a saturated stream: convergence is read back every 4
     # iterations here so the host stays ahead of the GPU (graphs are off while profiling);
-    # the whole batch runs on one stream, so no other part's kernels overlap a timed launch,
-    # with the launch shapes the autotuner picks for one stream (shapes chosen for concurrent
-    # parts, e.g. one plane block per SM, leave a kernel running alone short of bandwidth)
-    opts = dict(tuned or {}, streams=1)
-    if tuned:
-        opts, _ = pkg.autotune_batch([GRID] * B, [MINS] * B, [MAXS] * B, [[N - 1]] * B, logK, dh, Qs, obs,
-                                     repeats=2, reltol=RELTOL, precision=prec, streams=1)
+    # the launch shapes are the timed run's
+    opts = dict(tuned or {})
     b = pkg.GroundwaterBatch([GRID] * B, [MINS] * B, [MAXS] * B, [[N - 1]] * B, reltol=RELTOL, precision=prec,
                              check_every=4, **opts)
     d = [torch.tensor(x, device=dev) for x in (logK, dh, Qs)]
@@ -354,7 +349,7 @@ def profile_pass(pkg, torch, dev, B, N, prec, args, tuned=None):
         "top": [{"kernel": k, "launches": v[0], "ms": round(v[1], 3),
                  "GBps": round(BYTES_PER_CELL[k.split("<")[0]](4 if "<f32>" in k else 8) * v[2] / (v[1] / 1e3) / 1e9, 1)
                  if k.split("<")[0] in BYTES_PER_CELL and v[1] > 0 else None} for k, v in top[:8]],
-        "measured": "per-kernel CUDA events on the solver stream over %d forward+adjoint steps of the same workload (the batch on one stream, launch shapes tuned for one stream)"
+        "measured": "per-kernel CUDA events on the solver stream over %d forward+adjoint steps of the same workload (the batch on one stream)"
                     % max(1, min(args.steps, 3)),
         "profile_options": {k: v for k, v in opts.items()},
     }

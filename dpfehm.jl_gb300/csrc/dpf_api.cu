@@ -380,12 +380,10 @@ dpf_options fill_options(const dpf_options *o) {
     return r;
 }
 
-// The number of concurrent parts of a batch: the largest k <= the requested count (0: 4)
-// that divides the problem count, so that the parts are equal in size (a batch of identical
-// problems then gives bitwise identical results in every part).
-// Concurrent parts are switched off: every batch runs on one stream whatever `streams` asks.
-// Runs with batches split into parts raised illegal-address faults whose cause was not found
-// (the split path stays below, unreachable, until it is).
+// The number of concurrent parts of a batch. Splitting is switched off: every batch runs on
+// one stream whatever `streams` asks, because runs with batches split into equal parts on
+// separate streams raised illegal-address faults whose cause was not found (the split path
+// stays below, unreachable, until it is).
 int batch_parts(int nprob, int streams) {
     (void)nprob;
     (void)streams;
