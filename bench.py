@@ -285,6 +285,7 @@ def run_ours(args, dist, rank, ws):
         "roofline": rep,
     }
     out["accuracy"] = accuracy_check(pkg, torch, dev, N, logK[:N], dh[:N], Qs[:N], obs[0], h[:N], g[:N])
+    out["accuracy"].update(oracle_accuracy(pkg, N, logK[:N], dh[:N], Qs[:N], obs[0], h[:N], g[:N]))
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(pkg, N, logK[:N], dh[:N], Qs[:N], obs[0], args.cpu_steps)
     return out
@@ -384,6 +385,26 @@ def accuracy_check(pkg, torch, dev, N, logK, dh, Qs, obs, h, g):
     g = g.cpu().numpy() if hasattr(g, "cpu") else g
     return {"rel_head_err_vs_fp64_1e-13": float(np.linalg.norm(h - h64) / np.linalg.norm(h64)),
             "rel_grad_err_vs_fp64_1e-13": float(np.linalg.norm(g - g64) / np.linalg.norm(g64))}
+
+
+def oracle_accuracy(pkg, N, logK, dh, Qs, obs, h, g):
+    """Relative L2 errors of the timed run's realization 0 (head, dJ/dlogK) against the oracle
+    (the C restatement of the reference's solve and rrule) solved to reltol 1e-14 on the host."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    orc.build()
+    orc.set_threads(os.cpu_count() or 1)
+    _, nb, aol, _ = pkg.regulargrid3d(MINS, MAXS, GRID)
+    O = orc.Problem(N, nb, aol, [N - 1])
+    h_or = O.steady(orc.logk_to_faces(nb, logK), dh, Qs, reltol=1e-14)
+    delta = np.zeros(N)
+    np.add.at(delta, obs, 2 * h_or[obs])
+    dKs, _, _ = O.adjoint(dh, delta, reltol=1e-14)
+    g_or = orc.logk_to_faces_vjp(nb, logK, dKs)
+    h = h.cpu().numpy() if hasattr(h, "cpu") else h
+    g = g.cpu().numpy() if hasattr(g, "cpu") else g
+    return {"rel_head_err_vs_oracle_1e-14": float(np.linalg.norm(h - h_or) / np.linalg.norm(h_or)),
+            "rel_grad_err_vs_oracle_1e-14": float(np.linalg.norm(g - g_or) / np.linalg.norm(g_or))}
 
 
 def cpu_oracle_step(orc, nb, aol, N, logK, dh, Qs, obs):

@@ -94,7 +94,9 @@ def uneven_batch(pkg, torch, dev, args):
     res = {"workload": "gw_steady_fwd_adj_uneven_batch_256", "cells": cells, "batch_per_gpu": B, "problems": B,
            "sizes": "uniform over 50x50x5, 100x100x10, 150x150x10, 200x200x20 (0.5 m spacing)"}
     off = np.concatenate([[0], np.cumsum([np.prod(g) for g in grids])]).astype(np.int64)
-    check = [(grids[p], mins[p], maxs[p], dns[p], slice(off[p], off[p + 1])) for p in range(min(B, 4))]
+    # checked members: the first problem of each grid size (the 200x200x20 one included)
+    firsts = sorted({tuple(g): p for p, g in reversed(list(enumerate(grids)))}.values())
+    check = [(grids[p], mins[p], maxs[p], dns[p], slice(off[p], off[p + 1])) for p in firsts]
     return res, make, [logK, dh, Qs], obs, B, check
 
 
@@ -146,6 +148,28 @@ def run_steady(name, args, dist, rank, ws, METRIC_NAME):
         "iterations_last_adjoint": mixed.stats["iterations"],
     }
     out["speedup_vs_plain_fp64"] = round(out["value"] / out["plain_fp64_gpu"]["value"], 3)
+    if name == "uneven_batch":
+        # the checked members against the oracle (reltol 1e-14 on the host)
+        import sys
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+        orc.build()
+        orc.set_threads(os.cpu_count() or 1)
+        oe = []
+        for grid, mn, mx, dn, s in check:
+            p = int(np.searchsorted(mixed.cell_offsets, s.start))  # the member's problem index
+            n = s.stop - s.start
+            _, nb, aol, _ = pkg.regulargrid3d(mn, mx, grid)
+            lk = d[0][s].cpu().numpy()
+            O = orc.Problem(n, nb, aol, np.asarray(dn, np.int64))
+            ho = O.steady(orc.logk_to_faces(nb, lk), np.zeros(n), d[2][s].cpu().numpy(), reltol=1e-14)
+            delta = np.zeros(n)
+            np.add.at(delta, obs[p], 2 * ho[obs[p]])
+            dKs, _, _ = O.adjoint(np.zeros(n), delta, reltol=1e-14)
+            oe.append((_rel(h[s], ho), _rel(g[s], orc.logk_to_faces_vjp(nb, lk, dKs))))
+        out["accuracy"]["max_rel_head_err_vs_oracle_1e-14"] = max(e[0] for e in oe)
+        out["accuracy"]["max_rel_grad_err_vs_oracle_1e-14"] = max(e[1] for e in oe)
+        out["accuracy"]["oracle_grids"] = [list(c[0]) for c in check]
     if name == "steady_100k" and not args.no_cpu_baseline:
         # the oracle on realization 0: parity and the CPU rate at this size
         import sys
@@ -216,6 +240,8 @@ def run_transient(args, dist, rank, ws, METRIC_NAME):
     t64 = _events(torch, lambda: run(plain), 1, 1, flush)
     warnings.simplefilter("ignore", RuntimeWarning)
     dK64 = run(make("fp64", 1e-13))[0]
+    acc = {"rel_dKs_err_vs_fp64_1e-13": _rel(dK.cpu().numpy(), dK64.cpu().numpy())}
+    acc.update(_transient_vs_oracle(pkg, torch, mixed, lk, dn, Qs, Ss, dt, obs, vol=maxs, grid=grid, mins=mins))
     return {
         "metric": METRIC_NAME, "value": round(steps / t, 4), "unit": "runs/s", "n_gpus": ws, "steps": steps,
         "warmup": max(1, args.warmup - 1), "ms_per_step": round(1e3 * t / steps, 3), "higher_is_better": True,
@@ -226,8 +252,30 @@ def run_transient(args, dist, rank, ws, METRIC_NAME):
                    "precision": args.precision, "reltol": 1e-10},
         "plain_fp64_gpu": {"value": round(1.0 / t64, 4), "unit": "runs/s"},
         "speedup_vs_plain_fp64": round(t64 / (t / steps), 3),
-        "accuracy": {"rel_dKs_err_vs_fp64_1e-13": _rel(dK.cpu().numpy(), dK64.cpu().numpy())},
+        "accuracy": acc,
     }
+
+
+def _transient_vs_oracle(pkg, torch, P, lk, dn, Qs, Ss, dt, obs, vol, grid, mins, nsteps=10, ck=5):
+    """The first `nsteps` steps of the timed configuration (checkpoint every `ck`) on the timed
+    handle against the oracle's backward Euler and its discrete adjoint (reltol 1e-14)."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    orc.build()
+    orc.set_threads(os.cpu_count() or 1)
+    N = int(np.prod(grid))
+    _, nb, aol, V = pkg.regulargrid3d(mins, vol, grid)
+    Ks = orc.logk_to_faces(nb, lk)
+    dh = np.zeros(N)
+    O = orc.Problem(N, nb, aol, dn)
+    st_or = O.transient(Ks, dh, Qs, Ss, V, dt, nsteps, np.zeros(O.nfree), reltol=1e-14)
+    dK_or = O.transient_adjoint(dh, obs, reltol=1e-14)[0]
+    _, st = P.transient_forward(Ks, dh, Qs, Ss, dt, nsteps, np.zeros(N), checkpoint_every=ck, return_states=True)
+    dK = P.transient_adjoint(obs)[0]
+    isf, _, _ = pkg.getfreenodes(N, dn)
+    return {"rel_state_err_vs_oracle_1e-14": _rel(st[:, isf], st_or), "rel_dKs_err_vs_oracle_1e-14": _rel(dK, dK_or),
+            "oracle_steps": nsteps, "oracle_checkpoint_every": ck}
 
 
 # ---------------------------------------------------------------- general (CSR) path, 1M cells

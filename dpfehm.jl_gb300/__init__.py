@@ -99,13 +99,13 @@ def _out_into(given, like, n):
     return given, b.ptr
 
 
-def _check(lib, h, rc, allow_not_converged=True):
+def _check(lib, h, rc, allow_not_converged=True, what="groundwater solve"):
     if rc == _lib.DPF_OK:
         return
     msg = lib.dpf_last_error(h)
     msg = msg.decode() if msg else ""
     if rc == _lib.DPF_NOT_CONVERGED and allow_not_converged:
-        warnings.warn("groundwater solve did not reach reltol: " + msg, RuntimeWarning, stacklevel=3)
+        warnings.warn("%s did not reach its tolerance: %s" % (what, msg), RuntimeWarning, stacklevel=3)
         return
     raise DPFError(rc, msg)
 
@@ -227,7 +227,8 @@ class GroundwaterProblem:
         al, n_, q = _Buf(alphas, n=self.F), _Buf(Ns, n=self.F), _Buf(Qs, n=self.N)
         psi, pp = _out(p0, self.N)
         _check(self._lib, self._h, self._lib.dpf_richards_steady(self._h, p0.ptr, K.ptr, dp.ptr, zz.ptr, al.ptr, n_.ptr,
-                                                                 q.ptr, float(tol), int(maxiter), pp))
+                                                                 q.ptr, float(tol), int(maxiter), pp),
+               what="Richards solve")
         return psi
 
     def richards_adjoint(self, delta, tol=1e-10, maxiter=200):
@@ -239,7 +240,8 @@ class GroundwaterProblem:
         dN, dNp = _out(dl, self.F)
         dQ, dQp = _out(dl, self.N)
         _check(self._lib, self._h, self._lib.dpf_richards_adjoint(self._h, dl.ptr, float(tol), int(maxiter), dKp,
-                                                                  ddpp, dalp, dNp, dQp))
+                                                                  ddpp, dalp, dNp, dQp),
+               what="Richards adjoint solve")
         return dK, ddp, dal, dN, dQ
 
     def richards_transient_forward(self, psi0, Ks, dirichletpsis, z, alphas, Ns, Qs, specificstorage, dt, nsteps,
@@ -252,7 +254,7 @@ class GroundwaterProblem:
         states, sp = _out(p0, int(nsteps) * self.N) if return_states else (None, None)
         _check(self._lib, self._h, self._lib.dpf_richards_transient_forward(
             self._h, p0.ptr, K.ptr, dp.ptr, zz.ptr, al.ptr, n_.ptr, q.ptr, ss.ptr, float(dt), int(nsteps), float(tol),
-            int(maxiter), sp, pp))
+            int(maxiter), sp, pp), what="transient Richards solve")
         if return_states:
             return psiT, states.reshape(int(nsteps), self.N)
         return psiT
@@ -273,7 +275,7 @@ class GroundwaterProblem:
         d0, d0p = _out(like, self.N)
         _check(self._lib, self._h, self._lib.dpf_richards_transient_adjoint(
             self._h, ob.size, ob.ctypes.data, None if w is None else w.ctypes.data, None if g is None else g.ptr,
-            float(tol), int(maxiter), dKp, ddpp, dalp, dNp, dQp, d0p))
+            float(tol), int(maxiter), dKp, ddpp, dalp, dNp, dQp, d0p), what="transient Richards adjoint solve")
         return dK, ddp, dal, dN, dQ, d0
 
     @property
@@ -505,7 +507,9 @@ def amg_solver(*_a, **_k):
 def cholesky_solver(*_a, **_k):
     """Selector for ``linear_solver=`` (src/groundwater.jl:56-60): a solve to direct-solve
     accuracy. On the GPU this is the AMG-preconditioned CG run to the FP64 rounding floor of
-    the system (the mixed solver with reltol 0 stops there), not a sparse factorisation."""
+    the system, not a sparse factorisation: the mixed-precision solver with a tolerance below
+    any FP64 floor, whose rounds each end after a 1e-12 drop of their recursive residual and
+    whose FP64 check accepts (status OK) once the true residual is at the floor."""
     raise TypeError("cholesky_solver selects the solver; pass it as linear_solver=cholesky_solver")
 
 
@@ -514,7 +518,7 @@ def _solver_options(linear_solver, kwargs):
         return kwargs
     if linear_solver is cholesky_solver or linear_solver == "cholesky":
         o = dict(kwargs)
-        o.setdefault("precision", "mixed")
+        o["precision"] = "mixed"  # the solver with the FP64 floor check
         o["reltol"] = 1e-30  # below any FP64 floor: the solve ends at the floor (status OK)
         o.setdefault("max_outer", 12)
         return o

@@ -260,6 +260,20 @@ void stage_out(dpf_problem *P, T *dst, const T *src, size_t n) {
        "copy out");
 }
 
+// n indices from a host or device array; a device array is read with one copy on the handle's
+// stream, so it is ordered after the work the caller issued there
+std::vector<int64_t> read_indices(dpf_problem *P, const int64_t *idx, int64_t n) {
+    std::vector<int64_t> out(n > 0 ? n : 0);
+    if (n <= 0) return out;
+    if (is_device_ptr(idx)) {
+        ck(cudaMemcpyAsync(out.data(), idx, n * sizeof(int64_t), cudaMemcpyDeviceToHost, P->stream), "indices");
+        ck(cudaStreamSynchronize(P->stream), "indices");
+    } else {
+        std::memcpy(out.data(), idx, n * sizeof(int64_t));
+    }
+    return out;
+}
+
 template <typename T>
 T *scratch(dpf_problem *P, size_t n) {
     void *p = nullptr;
@@ -860,11 +874,7 @@ int dpf_solve_grad_logk(dpf_problem *P, const double *logK, int kind, const doub
         StructBatch &S = *P->sb;
         if (S.nprob != 1) throw BadInput("use dpf_batch_solve_grad_logk for a batch");
         std::vector<long long> og(nobs);
-        std::vector<int64_t> ho(nobs);
-        if (nobs) {
-            if (is_device_ptr(obs)) ck(cudaMemcpy(ho.data(), obs, nobs * sizeof(int64_t), cudaMemcpyDeviceToHost), "obs");
-            else std::memcpy(ho.data(), obs, nobs * sizeof(int64_t));
-        }
+        const std::vector<int64_t> ho = read_indices(P, obs, nobs);
         for (int64_t k = 0; k < nobs; k++) {
             if (ho[k] < 0 || ho[k] >= S.N) throw BadInput("observation index out of range");
             og[k] = ho[k];
@@ -1079,12 +1089,10 @@ int dpf_transient_adjoint(dpf_problem *P, int64_t nobs, const int64_t *obs, cons
         const long long N = S.N;
         const int nsteps = P->tr_nsteps, ck_every = P->tr_ck;
         std::vector<long long> ho(nobs);
+        const std::vector<int64_t> hv = read_indices(P, obs, nobs);
         for (int64_t k = 0; k < nobs; k++) {
-            int64_t v;
-            if (is_device_ptr(obs)) ck(cudaMemcpy(&v, obs + k, sizeof(int64_t), cudaMemcpyDeviceToHost), "obs");
-            else v = obs[k];
-            if (v < 0 || v >= N) throw BadInput("observation index out of range");
-            ho[k] = v;
+            if (hv[k] < 0 || hv[k] >= N) throw BadInput("observation index out of range");
+            ho[k] = hv[k];
         }
         long long *d_obs = scratch<long long>(P, nobs);
         if (nobs) ck(cudaMemcpyAsync(d_obs, ho.data(), nobs * sizeof(long long), cudaMemcpyHostToDevice, P->stream), "obs");

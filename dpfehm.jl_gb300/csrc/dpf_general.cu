@@ -451,7 +451,7 @@ __global__ void kg_df_update_xr(int n, CgState *st, int *active_count, ReduceScr
         s.iters++;
         s.total_iters++;
         if (!isfinite(s.rr)) { s.status = DPF_NAN; deactivate(s, active_count); }
-        else if (s.rr * s.scale * s.scale <= s.tol2 * s.obb) deactivate(s, active_count);
+        else if (s.rr * s.scale * s.scale <= s.tol2 * s.obb || s.rr <= kRoundDrop2) deactivate(s, active_count);
         else if (s.total_iters >= maxiter) { s.status = DPF_NOT_CONVERGED; deactivate(s, active_count); }
     }
 }
@@ -693,6 +693,26 @@ void GeneralSolver::from_dev(void *dst, const void *src, size_t bytes) {
     if (bytes) GCK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream));
 }
 
+static bool g_is_device(const void *p);
+
+// Observation indices (host or device array) read to the host and range-checked against N.
+// A device array is read with one copy on the solver's stream, so it is ordered after the work
+// the caller issued there.
+std::vector<long long> GeneralSolver::read_indices(const int64_t *idx, long long n) {
+    std::vector<long long> out(n);
+    if (n <= 0) return out;
+    static_assert(sizeof(long long) == sizeof(int64_t), "index width");
+    if (g_is_device(idx)) {
+        GCK(cudaMemcpyAsync(out.data(), idx, n * sizeof(int64_t), cudaMemcpyDeviceToHost, stream));
+        GCK(cudaStreamSynchronize(stream));
+    } else {
+        std::memcpy(out.data(), idx, n * sizeof(int64_t));
+    }
+    for (long long v : out)
+        if (v < 0 || v >= N) throw BadInput("observation index out of range");
+    return out;
+}
+
 static bool g_is_device(const void *p) {
     if (!p) return false;
     cudaPointerAttributes a;
@@ -759,7 +779,7 @@ GeneralSolver::GeneralSolver(long long N_, long long F_, const int64_t *a, const
     rs.partials = dev<double2>(nblocks);
     rs.tickets = dev<unsigned>(1);
     rs.capacity = nblocks;
-    GCK(cudaMemset(rs.tickets, 0, sizeof(unsigned)));
+    GCK(cudaMemsetAsync(rs.tickets, 0, sizeof(unsigned), stream));
     dense_inv = dev<double>(kMaxCoarse * kMaxCoarse);
     h_count = (int *)pinned.alloc(4 * sizeof(int));
     h_state = (CgState *)pinned.alloc(sizeof(CgState));
@@ -1291,14 +1311,7 @@ int GeneralSolver::solve_grad_logk(const double *logK, int kind, const double *d
                                    const int64_t *obs, double *h_out, double *dlogK) {
     int rc = forward(nullptr, logK, kind, dh, Qs, h_out);
     if (rc != DPF_OK && rc != DPF_NOT_CONVERGED) return rc;
-    std::vector<long long> ho(nobs);
-    for (long long k = 0; k < nobs; k++) {
-        int64_t v;
-        if (g_is_device(obs)) GCK(cudaMemcpy(&v, obs + k, sizeof(int64_t), cudaMemcpyDeviceToHost));
-        else v = obs[k];
-        if (v < 0 || v >= N) throw BadInput("observation index out of range");
-        ho[k] = v;
-    }
+    const std::vector<long long> ho = read_indices(obs, nobs);
     long long *d_obs = dev<long long>(nobs);
     to_dev(d_obs, ho.data(), nobs * sizeof(long long));
     GCK(cudaMemsetAsync(delta, 0, N * sizeof(double), stream));
@@ -1370,14 +1383,7 @@ int GeneralSolver::transient_adjoint(long long nobs, const int64_t *obs, const d
         return DPF_STATE;
     }
     const int n = (int)N;
-    std::vector<long long> ho(nobs);
-    for (long long k = 0; k < nobs; k++) {
-        int64_t v;
-        if (g_is_device(obs)) GCK(cudaMemcpy(&v, obs + k, sizeof(int64_t), cudaMemcpyDeviceToHost));
-        else v = obs[k];
-        if (v < 0 || v >= N) throw BadInput("observation index out of range");
-        ho[k] = v;
-    }
+    const std::vector<long long> ho = read_indices(obs, nobs);
     long long *d_obs = dev<long long>(std::max(nobs, 1LL));
     to_dev(d_obs, ho.data(), nobs * sizeof(long long));
     double *d_w = nullptr, *d_gT = nullptr;

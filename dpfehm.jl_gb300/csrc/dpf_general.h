@@ -91,6 +91,7 @@ private:
     void drop(void *p);            // free an allocation made by dev() (nullptr: nothing)
     void to_dev(void *dst, const void *src, size_t bytes);
     void from_dev(void *dst, const void *src, size_t bytes);
+    std::vector<long long> read_indices(const int64_t *idx, long long n);
     const double *stage(const double *src, size_t n, double *dst);
     void richards_buffers();
     void richards_stage(const double *Ks, const double *dpsi, const double *z, const double *alphas,

@@ -27,6 +27,13 @@ namespace dpf {
 constexpr int kBlock = 256;        // threads per block of every cell-parallel kernel
 constexpr int kMaxCoarse = 64;     // largest dense coarsest level (cells)
 constexpr int kMinBlocks = 6;      // resident blocks per SM the CG stencils are compiled for
+// Mixed precision: a round of double-float CG also ends once its recursive residual has dropped
+// by 1e-12 from the round's start (|r|^2 <= 1e-24 in the round's units, where |r| starts at 1).
+// A double-float recurrence carries about 48 bits, so a deeper drop within one round would not
+// be reflected in the true residual; the FP64 check that follows then continues from the true
+// residual or, at the system's FP64 rounding floor, accepts. This lets a tolerance below that
+// floor (reltol 0) end at the floor with status OK instead of at the iteration cap.
+constexpr double kRoundDrop2 = 1e-24;
 
 struct LevelDesc {                 // one problem at one level
     int nx, ny, nz, pad;

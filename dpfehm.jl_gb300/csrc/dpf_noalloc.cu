@@ -80,13 +80,21 @@ __global__ void k_na_faces(int nx, int ny, int nz, unsigned mag_nz, int sh_nz, u
     }
 }
 
+// device (or managed) memory of the current device: the kernels read and write it without
+// peer access, so a pointer into another GPU's memory is rejected here, on the host
 bool on_device(const void *p) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type == cudaMemoryTypeDevice) return a.device == cur;
+    return a.type == cudaMemoryTypeManaged;
 }
 
 // device address of the scratch array on the current device (looked up once per device)
@@ -139,7 +147,7 @@ extern "C" int dpf_logk_to_faces_regular_noalloc(int nx, int ny, int nz, const d
         return DPF_BAD_INPUT;
     }
     if (!on_device(logK) || !on_device(Ks)) {
-        dpf::set_global_error("the allocation-free path needs device pointers for logK and Ks");
+        dpf::set_global_error("the allocation-free path needs device pointers of the current device for logK and Ks");
         return DPF_BAD_INPUT;
     }
     std::string err;

@@ -11,8 +11,8 @@
 //
 // The arithmetic is that of the per-cell bodies in dpf_struct.cu in the same order
 // (apply7: z+, z-, y+, y-, x+, x-), so results are bitwise identical to the grid-stride
-// kernels. Every mbarrier wait is bounded; on expiry the kernel records an error in *err,
-// and the producer drains its copies (bounded) before the block returns.
+// kernels. Every mbarrier wait is bounded (one second); on expiry the kernel records an error in
+// *err, and the producer drains its copies (bounded, an expiry recorded too) before the block returns.
 #pragma once
 #include <cstdint>
 
@@ -47,8 +47,8 @@ __host__ __device__ __forceinline__ int plane_rows(int ny, int nz, int cells) {
 
 // per-cell flags: inside the slab, and which of the z+/z-/y+/y- neighbours exist
 constexpr unsigned CF_VALID = 1u, CF_ZP = 2u, CF_ZM = 4u, CF_YP = 8u, CF_YM = 16u;
-constexpr uint32_t kWaitTries = 1u << 20;         // bounded mbarrier polling ...
-constexpr uint64_t kWaitNs = 1000000000ull;       // ... and at most one second of it
+constexpr uint64_t kWaitNs = 1000000000ull;       // a bounded mbarrier wait ends after one second ...
+constexpr uint32_t kWaitTries = 1u << 28;         // ... or, should the global timer stall, 2^28 polls
 
 enum : int { PM_FIRST2 = 1, PM_FIRST = 2, PM_PROLONG = 4, PM_NOD = 8, PM_RZ = 16 };
 
@@ -83,8 +83,10 @@ __device__ __forceinline__ uint64_t global_ns() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
-// bounded wait for the phase with the given parity (kWaitTries polls or kWaitNs, whichever
-// ends first); false (and *err set) on expiry
+// bounded wait for the phase with the given parity: one second by the global timer (a poll
+// count far above what a second of polling takes is only a backstop); false and *err set on
+// expiry. The bound is by time so that a block descheduled or slowed by other work on the GPU
+// does not see a wait expire that would have completed.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = global_ns();
@@ -92,7 +94,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *e
         if (mbar_try_wait(bar, parity)) return true;
         if ((k & 63) == 63 && global_ns() - t0 > kWaitNs) break;
     }
-    if (err) atomicExch(err, 1);
+    atomicExch(err, 1);
     return false;
 }
 // barrier 1 over the `count` consumer threads only (the producer warp does not take part),
@@ -185,7 +187,9 @@ __device__ __forceinline__ int div_nz(const LevelDesc &L, int k) { return (int)f
 // (mbarrier expect_tx) and issues the copies of plane q; the one pending arrival made here
 // afterwards keeps the phase open until every copy has been announced. Before the block
 // may end, the last phase of every filled slot is waited for (bounded), so no copy is
-// still in flight into the block's shared memory.
+// still in flight into the block's shared memory. Should one of those waits expire, copies
+// may still land after the block ends: the error word is set, the solve reports DPF_TIMEOUT
+// and the host treats the device's results as suspect.
 template <int R, typename F>
 __device__ __forceinline__ void pm_produce(int pl_lo, int pl_hi, uint64_t *full, uint64_t *empty, unsigned char *sm,
                                            int slot_bytes, int *err, F stage_plane) {
@@ -200,7 +204,7 @@ __device__ __forceinline__ void pm_produce(int pl_lo, int pl_hi, uint64_t *full,
     }
     for (int q = max(pl_lo, issued_hi - R + 1); q <= issued_hi; q++) {
         const int u = q - pl_lo;
-        mbar_wait(&full[u % R], (uint32_t)((u / R) & 1), nullptr);
+        mbar_wait(&full[u % R], (uint32_t)((u / R) & 1), err);
     }
 }
 

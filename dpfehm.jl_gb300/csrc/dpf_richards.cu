@@ -102,36 +102,52 @@ __global__ void richards_residual(int n, const int *__restrict__ irp, const int 
                                   const double *__restrict__ z, const double *__restrict__ Qs,
                                   const double *__restrict__ shift, const double *__restrict__ psi_old,
                                   double *__restrict__ R, double2 *__restrict__ part) {
-    double rr = 0.0, qq = 0.0;
+    // part[b] = (|R|^2, |Q|^2) and part[gridDim.x + b] = (floor^2, 0) of this block's cells, where
+    // the floor of a cell is twice the FP64 rounding bound of its residual: u (|Q| + the storage
+    // term's operands + per face K aol (|psi_j + z_j| + |h_i| + |flux difference|)), u = 2^-53
+    double rr = 0.0, qq = 0.0, ff = 0.0;
     RSTRIDE(i, n) {
         double r = 0.0;
         if (!dir[i]) {
             r = Qs[i];
-            if (shift) r -= shift[i] * (psi[i] - psi_old[i]);
+            double fl = fabs(Qs[i]);
+            if (shift) {
+                r -= shift[i] * (psi[i] - psi_old[i]);
+                fl += shift[i] * (fabs(psi[i]) + fabs(psi_old[i]));
+            }
             const double hi = psi[i] + z[i];
             for (int k = irp[i]; k < irp[i + 1]; k++) {
                 const int f = ifc[k];
                 const int j = fa[f] == i ? fb[f] : fa[f];
                 if (!DPF_INSIDE(CK_NEIGHBOUR, j, 0, n)) continue;
-                r += Kh[f] * aol[f] * (psi[j] + z[j] - hi);
+                const double hj = psi[j] + z[j], c = Kh[f] * aol[f];
+                r += c * (hj - hi);
+                fl += c * (fabs(hj) + fabs(hi) + fabs(hj - hi));
             }
             qq += Qs[i] * Qs[i];
+            const double f2 = 0x1p-52 * fl;
+            ff += f2 * f2;
         }
         R[i] = r;
         rr += r * r;
     }
-    __shared__ double sr[kRBlock], sq[kRBlock];
+    __shared__ double sr[kRBlock], sq[kRBlock], sf[kRBlock];
     sr[threadIdx.x] = rr;
     sq[threadIdx.x] = qq;
+    sf[threadIdx.x] = ff;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
         if ((int)threadIdx.x < s) {
             sr[threadIdx.x] += sr[threadIdx.x + s];
             sq[threadIdx.x] += sq[threadIdx.x + s];
+            sf[threadIdx.x] += sf[threadIdx.x + s];
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) part[blockIdx.x] = make_double2(sr[0], sq[0]);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = make_double2(sr[0], sq[0]);
+        part[gridDim.x + blockIdx.x] = make_double2(sf[0], 0.0);
+    }
 }
 
 // psi += w d at free cells; per-block sums of (w d)^2 and psi^2
@@ -390,7 +406,7 @@ void GeneralSolver::richards_buffers() {
     rc_gK = dev<double>(F);
     rc_ga = dev<double>(F);
     rc_gN = dev<double>(F);
-    rc_part = dev<double2>(nblocks);
+    rc_part = dev<double2>(2 * (size_t)nblocks);  // the residual kernel's sums and rounding floors
     rck(cudaMemsetAsync(rc_zero, 0, N * sizeof(double), stream), "zero");
 }
 
@@ -408,11 +424,16 @@ int GeneralSolver::richards_spd_solve(const double *rhs_dev, double *x_dev, cons
 
 // Nonlinear solve of one steady or backward-Euler Richards system from the current rc_psi:
 // Picard steps (shift + A(psi)) d = G(psi), G = R(psi) - shift (psi - psi_old), halved while the
-// residual does not drop, until |G| <= tol max(|G(psi_0)|, |Q|) or maxit steps. Leaves the
-// Picard conductances and the Jacobian parts at the result in rc_Kh, rc_na, rc_nb.
+// residual does not drop, until |G| <= tol max(|G(psi_0)|, |Q|) or maxit steps. The iteration
+// also ends, converged, at the FP64 rounding floor of G: when |G| is within the floor's bound,
+// or when a step (with all its halvings) no longer lowers |G| and |G| is within 100 times the
+// bound. No further accuracy exists in FP64 there (heads of 1000 m leave a floor above a
+// tolerance of 1e-12 times |Q|). Leaves the Picard conductances and the Jacobian parts at the
+// result in rc_Kh, rc_na, rc_nb.
 int GeneralSolver::richards_nonlinear(const double *shift_dev, const double *psi_old, double tol, int maxit,
                                       int &iters, double &relres) {
     const unsigned nbF = rblocks(F, nblocks), nbN = rblocks(N, nblocks);
+    double floor2 = 0.0;  // squared rounding floor of the last residual evaluated
     auto residual = [&]() -> double2 {
         kr_faces<<<nbF, kRBlock, 0, stream>>>((int)F, fa, fb, faol, rc_Ks, rc_al, rc_N, rc_psi, rc_z, rc_Kh,
                                               nullptr, nullptr);
@@ -420,13 +441,15 @@ int GeneralSolver::richards_nonlinear(const double *shift_dev, const double *psi
         richards_residual<<<nbN, kRBlock, 0, stream>>>((int)N, irp, ifc, fa, fb, faol, rc_Kh, lv[0].dir, rc_psi,
                                                        rc_z, rc_Q, shift_dev, psi_old, rc_R, rc_part);
         GLAUNCH_CHECK();
+        floor2 = sum_parts(rc_part + nbN, (int)nbN, stream).x;
         return sum_parts(rc_part, (int)nbN, stream);
     };
     const double2 rq = residual();
     const double r0 = std::sqrt(rq.x), scale = std::max(r0, std::sqrt(rq.y));
     double rn = r0;
     int it = 0;
-    while (rn > tol * scale && it < maxit) {
+    bool at_floor = rn * rn <= floor2;
+    while (rn > tol * scale && !at_floor && it < maxit) {
         const int src = richards_spd_solve(rc_R, rc_d, shift_dev);
         if (src != DPF_OK && src != DPF_NOT_CONVERGED) return src;
         double w = 1.0, applied = 0.0;
@@ -436,11 +459,13 @@ int GeneralSolver::richards_nonlinear(const double *shift_dev, const double *psi
             applied = w;
             const double rnew = std::sqrt(residual().x);
             if (rnew < rn || k == 5) {
+                if (rnew >= rn && rnew * rnew <= 1e4 * floor2) at_floor = true;  // stalled at the floor
                 rn = rnew;
                 break;
             }
             w *= 0.5;
         }
+        if (rn * rn <= floor2) at_floor = true;
         it++;
     }
     iters = it;
@@ -450,7 +475,7 @@ int GeneralSolver::richards_nonlinear(const double *shift_dev, const double *psi
     GLAUNCH_CHECK();
     rck(cudaStreamSynchronize(stream), "sync");
     if (!std::isfinite(rn)) return DPF_NAN;
-    return rn > tol * scale ? DPF_NOT_CONVERGED : DPF_OK;
+    return (rn > tol * scale && !at_floor) ? DPF_NOT_CONVERGED : DPF_OK;
 }
 
 // (shift + A - N^T) x = rhs at the Jacobian parts in rc_Kh, rc_na, rc_nb: with M = shift + A
@@ -664,8 +689,12 @@ int GeneralSolver::richards_transient_adjoint(long long nobs, const int64_t *obs
     if (rt_nsteps < 1) throw DpfError("transient Richards adjoint called before a transient Richards run", DPF_STATE);
     const unsigned nbF = rblocks(F, nblocks), nbN = rblocks(N, nblocks);
     std::vector<long long> ho(nobs);
-    if (nobs && r_is_device(obs)) rck(cudaMemcpy(ho.data(), obs, nobs * sizeof(int64_t), cudaMemcpyDeviceToHost), "obs");
-    else if (nobs) std::memcpy(ho.data(), obs, nobs * sizeof(int64_t));
+    if (nobs && r_is_device(obs)) {
+        rck(cudaMemcpyAsync(ho.data(), obs, nobs * sizeof(int64_t), cudaMemcpyDeviceToHost, stream), "obs");
+        rck(cudaStreamSynchronize(stream), "obs");
+    } else if (nobs) {
+        std::memcpy(ho.data(), obs, nobs * sizeof(int64_t));
+    }
     for (long long k = 0; k < nobs; k++)
         if (ho[k] < 0 || ho[k] >= N) throw BadInput("observation index out of range");
     long long *d_obs = dev<long long>(std::max(nobs, 1LL));

@@ -735,7 +735,7 @@ __global__ void k_df_update_xr(const LevelDesc *__restrict__ desc, const int4 *_
         s.iters++;
         s.total_iters++;
         if (!isfinite(s.rr)) { s.status = DPF_NAN; deactivate(s, active_count); }
-        else if (s.rr * s.scale * s.scale <= s.tol2 * s.obb) deactivate(s, active_count);
+        else if (s.rr * s.scale * s.scale <= s.tol2 * s.obb || s.rr <= kRoundDrop2) deactivate(s, active_count);
         else if (s.total_iters >= maxiter) { s.status = DPF_NOT_CONVERGED; deactivate(s, active_count); }
     }
 }
@@ -1157,7 +1157,7 @@ static void ck(cudaError_t e, const char *what) {
 #define CK(x) ck((x), #x)
 #define LAUNCH_CHECK() ck(cudaGetLastError(), "kernel launch")
 
-static void configure_plane_kernels();
+static void configure_kernels();
 
 // Launch with programmatic stream serialization: the launch is prepared while the previous
 // kernel on the stream runs and its blocks start as that kernel's blocks exit; each solver
@@ -1327,6 +1327,8 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         nlev[p] = (int)shapes[p].size();
         nlev_max = std::max(nlev_max, nlev[p]);
     }
+    // function attributes of this device's kernels, set once before any launch
+    configure_kernels();
     // launch shape: grids sized to the resident capacity of the device
     int dev = 0, sms = 152;
     CK(cudaGetDevice(&dev));
@@ -1385,7 +1387,6 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         L.smooth = build_map(L.h_desc, smooth, owned, nprob, target_blocks);
         L.restr = build_map(L.h_desc, restr, owned, nprob, target_blocks);
         const bool plane_here = opt.plane > 0 && (opt.plane_levels <= 0 || l < opt.plane_levels);
-        if (mixed && l == 0) configure_plane_kernels();
         build_plane_items(L.pm, L, smooth, sms, plane_here ? opt.plane_cells : 0, opt.plane_blocks_per_sm, &shapes,
                           l);
         if (l == 0) build_plane_items(L.pa, L, has, sms, opt.df_plane_cells, opt.df_plane_blocks_per_sm, nullptr, l);
@@ -1512,6 +1513,10 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         cheb_c2[k] = 2.0 * rn / delt;
         rho = rn;
     }
+    if (!tails.empty()) write_tail_table();
+    // the uploads above are synchronous copies on the legacy stream, some from pageable memory
+    // (which may return before the DMA lands): the device is drained before the handle is used
+    // from any stream
     CK(cudaDeviceSynchronize());
 }
 
@@ -1598,6 +1603,31 @@ Coeffs<float> coeffs_of<float>(StructBatch::Level &L, bool) {
     return Coeffs<float>{L.c16[0], L.c16[1], L.c16[2], L.c16[3], L.idg32};
 }
 
+// The fused tail's per-level pointer table, written once at construction: staged in pinned
+// memory, copied on the handle's stream and waited for, so no kernel on any stream can read
+// the table before its copy has landed. (A pageable cudaMemcpy may return before its DMA
+// completes, and the legacy stream it runs on is not ordered with non-blocking streams.)
+template <typename T>
+static void fill_tail_table(StructBatch &S, void *host) {
+    TailLevel<T> *tab = (TailLevel<T> *)host;
+    for (int l = 0; l < S.nlev_max; l++) {
+        StructBatch::Level &L = S.lv[l];
+        tab[l] = TailLevel<T>{L.d_desc, coeffs_of<T>(L, S.mixed), (T *)L.work[0], (T *)L.work[1],
+                              (T *)L.work[2], (T *)L.work[3], L.dir};
+    }
+}
+
+void StructBatch::write_tail_table() {
+    const size_t bytes = (size_t)nlev_max * (mixed ? sizeof(TailLevel<float>) : sizeof(TailLevel<double>));
+    void *host = pinned.alloc(bytes);
+    if (!host) throw OomError("pinned host allocation failed");
+    if (mixed) fill_tail_table<float>(*this, host);
+    else fill_tail_table<double>(*this, host);
+    d_tail_lv = dalloc<char>(bytes, owned);
+    CK(cudaMemcpyAsync(d_tail_lv, host, bytes, cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+}
+
 void StructBatch::assemble(const double *Ks, const double *kc, int kind, const double *shift, bool init_x) {
     NvtxRange range("assemble operator and hierarchy");
     Level &L0 = lv[0];
@@ -1653,10 +1683,11 @@ void StructBatch::assemble(const double *Ks, const double *kc, int kind, const d
 // ---- plane-marching launches
 static int pm_region(int count, int es) { return ((count * es + 32) + 15) & ~15; }
 
-// The plane kernels' dynamic shared memory limit is raised once per device, before any of
-// them is launched, to all that a block may hold beside its static shared memory. The
-// attribute is then never changed while kernels of another handle, or of another part of a
-// split batch on another host thread, run or are being captured into a graph.
+// Function attributes are set once per device, at the first handle's construction and before
+// any launch: the plane kernels' dynamic shared memory limit (all that a block may hold beside
+// its static shared memory) and the fused tail's permission for non-portable cluster sizes (up
+// to 16 blocks). An attribute is then never changed while kernels of another handle, or of
+// another part of a split batch on another host thread, run or are being captured into a graph.
 template <int MODE>
 static void raise_pm_cheb(const std::function<void(const void *)> &raise) {
     raise((const void *)k_pm_cheb<float, MODE, 1>);
@@ -1665,7 +1696,7 @@ static void raise_pm_cheb(const std::function<void(const void *)> &raise) {
     raise((const void *)k_pm_cheb<float, MODE, 4>);
 }
 
-static void configure_plane_kernels() {
+static void configure_kernels() {
     static std::mutex mu;
     static std::set<int> done;
     int dev = 0;
@@ -1695,6 +1726,8 @@ static void configure_plane_kernels() {
     raise((const void *)k_pm_df_spmv<2>);
     raise((const void *)k_pm_df_spmv<3>);
     raise((const void *)k_pm_df_spmv<4>);
+    CK(cudaFuncSetAttribute(k_tail_cycle<float, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    CK(cudaFuncSetAttribute(k_tail_cycle<double, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     done.insert(dev);
 }
 
@@ -1828,8 +1861,6 @@ void StructBatch::launch_tail(const TailParams<T> &tp) {
     if (tail_cs == 0) {
         int cs = std::max(1, std::min(16, opt.tail_cluster));
         while (cs > 1) {
-            if (cs > 8)
-                CK(cudaFuncSetAttribute(k_tail_cycle<T, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(nt * cs);
             cfg.blockDim = dim3(kTailThreads);
@@ -1968,16 +1999,8 @@ void StructBatch::vcycle(const T *r, T *z) {
     }
     // the small levels: one fused block per problem
     if (!tails.empty()) {
-        if (!d_tail_lv) {
-            std::vector<TailLevel<T>> tab(nlev_max);
-            for (int l = 0; l < nlev_max; l++) {
-                Level &L = lv[l];
-                tab[l] = TailLevel<T>{L.d_desc, coeffs_of<T>(L, mixed), (T *)L.work[0], (T *)L.work[1],
-                                      (T *)L.work[2], (T *)L.work[3], L.dir};
-            }
-            d_tail_lv = dalloc<TailLevel<T>>(nlev_max, owned);
-            CK(cudaMemcpy(d_tail_lv, tab.data(), nlev_max * sizeof(TailLevel<T>), cudaMemcpyHostToDevice));
-        }
+        // the level table is written once, at construction, for the V-cycle precision in use
+        if (!d_tail_lv || (sizeof(T) == 4) != mixed) throw std::logic_error("fused-tail level table missing");
         TailParams<T> tp{};
         for (int k = 0; k < deg && k < 8; k++) {
             tp.c1[k] = (T)cheb_c1[k];

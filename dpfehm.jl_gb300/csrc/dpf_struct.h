@@ -115,6 +115,7 @@ public:
                            int blocks_per_sm, const std::vector<std::vector<std::array<int, 3>>> *shapes, int l);
     template <typename T>
     void launch_tail(const TailParams<T> &tp);
+    void write_tail_table();
     template <typename T>
     void pm_restrict(int l, const T *b, const T *x, T *bc);
     void pm_df_spmv(const CoeffsDF &C);
@@ -157,7 +158,8 @@ public:
     int *d_factor_status = nullptr;  // [0] coarsest factorisation failed, [1] an async-copy wait expired
     ReduceScratch rs;
     double *d_coarseL = nullptr;
-    // fused tail: per problem {p, first tail level, coarsest level, 0}; level table built on first use
+    // fused tail: per problem {p, first tail level, coarsest level, 0}; per-level pointer table
+    // (TailLevel of the V-cycle precision) written at construction by write_tail_table
     bool zero_guess = false;  // the next solve starts from 0 (Dirichlet values on identity rows)
     // device buffer for observation indices, kept between calls (no allocation per call)
     long long *obs_buffer(size_t n);

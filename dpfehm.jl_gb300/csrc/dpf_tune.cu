@@ -73,6 +73,12 @@ extern "C" int dpf_batch_autotune(int nprob, const int *dims, const double *mins
     DevCopy dlk, ddh, dq;
     int rc;
     if ((rc = to_device(logK, N, dlk)) || (rc = to_device(dh, N, ddh)) || (rc = to_device(Qs, N, dq))) return rc;
+    // a copy from pageable memory may return before its DMA lands: complete it before any
+    // candidate's stream reads the inputs
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        cudaGetLastError();
+        return DPF_CUDA;
+    }
     double *hout = nullptr, *gout = nullptr;
     if (dpf::dev_malloc((void **)&hout, N * sizeof(double)) != cudaSuccess ||
         dpf::dev_malloc((void **)&gout, N * sizeof(double)) != cudaSuccess) {

@@ -59,7 +59,7 @@ lasterror(h) = unsafe_string(ccall((:dpf_last_error, libdpf), Cstring, (Ptr{Cvoi
 
 function check(h, rc)
     rc == DPF_OK && return nothing
-    rc == DPF_NOT_CONVERGED && (@warn "groundwater solve did not reach reltol: $(lasterror(h))"; return nothing)
+    rc == DPF_NOT_CONVERGED && (@warn "solve did not reach its tolerance: $(lasterror(h))"; return nothing)
     error("libdpfehm_gpu status $rc: $(lasterror(h))")
 end
 
@@ -91,22 +91,36 @@ function Problem(neighbors, areasoverlengths, dirichletnodes, N; volumes=nothing
     return p
 end
 
+# Array arguments. A host Vector{Float64} is passed as is and any other host vector as a
+# Float64 copy. A device array (CUDA.jl's CuArray{Float64}, whose `pointer` is a CuPtr) is
+# passed by its device address: the library recognises device pointers and reads and writes
+# them in place, so a CuArray never goes through host memory. Outputs are allocated with
+# `similar`, on the side (host or device) of the input they follow.
+isdevice(x) = nameof(typeof(x)) === :CuArray
+floatbuf(x::Vector{Float64}) = x
+floatbuf(x) = isdevice(x) && eltype(x) === Float64 ? x : Vector{Float64}(x)
+rawptr(x::Array{Float64}) = pointer(x)
+rawptr(x) = Ptr{Float64}(reinterpret(UInt, pointer(x)))   # a device array's address
+outbuf(like, n) = isdevice(like) ? similar(like, Float64, n) : Vector{Float64}(undef, n)
+
 function forward(p::Problem, Ks, dirichleths, Qs)
-    h = Vector{Float64}(undef, p.N)
-    K = Vector{Float64}(Ks); d = Vector{Float64}(dirichleths); q = Vector{Float64}(Qs)
-    rc = ccall((:dpf_steady_forward, libdpf), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
-               Ptr{Float64}), p.ptr, K, d, q, h)
+    K = floatbuf(Ks); d = floatbuf(dirichleths); q = floatbuf(Qs)
+    h = outbuf(K, p.N)
+    rc = GC.@preserve K d q h ccall((:dpf_steady_forward, libdpf), Cint,
+                                    (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                                    p.ptr, rawptr(K), rawptr(d), rawptr(q), rawptr(h))
     check(p.ptr, rc)
     return h
 end
 
 function adjoint(p::Problem, delta)
-    dKs = Vector{Float64}(undef, p.F)
-    ddh = Vector{Float64}(undef, p.N)
-    dQs = Vector{Float64}(undef, p.N)
-    dl = Vector{Float64}(delta)
-    rc = ccall((:dpf_steady_adjoint, libdpf), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
-               Ptr{Float64}), p.ptr, dl, dKs, ddh, dQs)
+    dl = floatbuf(delta)
+    dKs = outbuf(dl, p.F)
+    ddh = outbuf(dl, p.N)
+    dQs = outbuf(dl, p.N)
+    rc = GC.@preserve dl dKs ddh dQs ccall((:dpf_steady_adjoint, libdpf), Cint,
+                                           (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                                           p.ptr, rawptr(dl), rawptr(dKs), rawptr(ddh), rawptr(dQs))
     check(p.ptr, rc)
     return dKs, ddh, dQs
 end
@@ -116,7 +130,7 @@ and `cholesky_solver` (the same GPU solver run to the FP64 rounding floor of the
 function amg_solver end
 function cholesky_solver end
 
-solver_kwargs(ls, kwargs) = ls === cholesky_solver ? merge((; precision=:mixed, max_outer=12), kwargs, (; reltol=1e-30)) : kwargs
+solver_kwargs(ls, kwargs) = ls === cholesky_solver ? merge((; max_outer=12), kwargs, (; precision=:mixed, reltol=1e-30)) : kwargs
 
 """Drop-in for `DPFEHM.groundwater_steadystate`."""
 function groundwater_steadystate(Ks, neighbors, areasoverlengths, dirichletnodes, dirichleths, Qs;

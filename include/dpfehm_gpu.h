@@ -276,9 +276,10 @@ int dpf_richards_steady(dpf_problem *h, const double *psi0, const double *Ks, co
                         int maxiter, double *psi_out);
 
 /* The rrule pullback of richards_steadystate (src/richards.jl:168-190) at the last solve:
- * lambda = J^-T delta by a fixed-point iteration on the Picard operator (to relative change tol,
- * at most maxiter steps), then dKs[F], ddirichletpsis[N], dalphas[F], dNs[F], dQs[N] (any
- * output may be NULL; the psi0 tangent is zero). */
+ * lambda = J^-T delta by restarted GMRES(30) preconditioned with the Picard operator (each step
+ * one CG + AMG solve; to relative residual tol, at most maxiter steps), then dKs[F],
+ * ddirichletpsis[N], dalphas[F], dNs[F], dQs[N] (any output may be NULL; the psi0 tangent is
+ * zero). */
 int dpf_richards_adjoint(dpf_problem *h, const double *delta, double tol, int maxiter, double *dKs,
                          double *ddirichletpsis, double *dalphas, double *dNs, double *dQs);
 
@@ -319,7 +320,7 @@ void dpf_debug_alloc_stats(int64_t *made, int64_t *live);
 
 /* No counterpart in the reference. Runs one block whose threads wait on a
  * shared-memory barrier that nothing arrives on, through the bounded wait every
- * staging kernel uses (at most 2^20 polls or one second). Returns DPF_TIMEOUT when
+ * staging kernel uses (one second by the device's global timer). Returns DPF_TIMEOUT when
  * the bound ended the wait as designed, with the milliseconds it took in
  * *waited_ms (may be NULL); any other status is a defect. The device stays usable. */
 int dpf_debug_expired_wait(double *waited_ms);

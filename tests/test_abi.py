@@ -46,6 +46,36 @@ def test_bindings_cover_header(pkg):
     assert set(_declared_symbols()) <= set(_lib.SIGNATURES)
 
 
+def _c_options_fields():
+    """(name, type) of struct dpf_options in include/dpfehm_gpu.h, in declaration order."""
+    src = open(os.path.join(ROOT, "include", "dpfehm_gpu.h")).read()
+    body = re.search(r"typedef struct dpf_options \{(.*?)\} dpf_options;", src, flags=re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    return [(m.group(2), m.group(1)) for m in re.finditer(r"\b(double|int)\s+([a-z0-9_]+)\s*;", body)]
+
+
+def test_options_layout_matches_bindings(pkg):
+    """The options struct is passed by pointer from Python (ctypes) and Julia (ccall with
+    Ref{Options}): both mirrors must list the C fields in the same order with the same types,
+    or every option after a mismatch would be read from the wrong bytes."""
+    from importlib import import_module
+    c_fields = _c_options_fields()
+    assert len(c_fields) >= 20
+    ct = {ctypes.c_double: "double", ctypes.c_int: "int"}
+    _lib = import_module(pkg.__name__ + "._lib")
+    py_fields = [(n, ct[t]) for n, t in _lib.Options._fields_]
+    assert py_fields == c_fields
+    jl = open(os.path.join(ROOT, "dpfehm.jl_gb300", "julia", "DPFEHMGPU.jl")).read()
+    body = re.search(r"mutable struct Options\n(.*?)\nend", jl, flags=re.S).group(1)
+    jt = {"Cdouble": "double", "Cint": "int"}
+    jl_fields = [(m.group(1), jt[m.group(2)]) for m in re.finditer(r"^\s*([a-z0-9_]+)::(Cdouble|Cint)\s*$", body,
+                                                                    flags=re.M)]
+    assert jl_fields == c_fields
+    # the Julia constructor call that default_options fills must pass one value per field
+    ctor = re.search(r"o = Options\(([^)]*)\)", jl).group(1)
+    assert len(ctor.split(",")) == len(c_fields)
+
+
 def test_default_options(pkg, lib):
     o = pkg.default_options()
     assert o.reltol == 1e-10 and o.maxiter == 500 and o.precision == pkg.PREC_FP64

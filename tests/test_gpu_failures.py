@@ -143,7 +143,7 @@ def test_expired_wait_reports_timeout(gpu_lib, lib):
     ms = ctypes.c_double(-1.0)
     rc = lib.dpf_debug_expired_wait(ctypes.byref(ms))
     assert rc == DPF_TIMEOUT, pkg._lib.STATUS_NAMES.get(rc, rc)
-    assert 0.0 < ms.value <= 1100.0              # 2^20 polls or one second, whichever ends first
+    assert 900.0 <= ms.value <= 1100.0           # the wait is bounded by one second of device time
     # the device and the library stay usable
     shapes, mins, maxs, dn, logK, dh, Qs, obs = _case(pkg)
     B = pkg.GroundwaterBatch(shapes, mins, maxs, dn, precision="mixed", reltol=1e-11)

@@ -58,12 +58,19 @@ def test_golden_twophase_pressure(gpu_lib):
 
 
 def test_cholesky_solver_selector(gpu_lib):
-    """linear_solver=cholesky_solver solves to the FP64 rounding floor (direct-solve accuracy)."""
+    """linear_solver=cholesky_solver solves to the FP64 rounding floor (direct-solve accuracy),
+    ends there with status OK (RuntimeWarnings are errors in the GPU tests) and needs only a
+    few rounds to get there."""
     pkg = gpu_lib
     g = dict(np.load(os.path.join(GOLD, "steady_harmonic_multidir.npz")))
     h = pkg.groundwater_steadystate(g["Ks"], g["nb"], g["aol"], g["dn"], g["dh"], g["Qs"],
                                     linear_solver=pkg.cholesky_solver)
     assert rel(h, g["h"]) < 1e-12
+    h1, back = pkg.rrule_groundwater_steadystate(g["Ks"], g["nb"], g["aol"], g["dn"], g["dh"], g["Qs"],
+                                                 linear_solver=pkg.cholesky_solver)
+    st = back.problem.stats
+    assert rel(h1, g["h"]) < 1e-12
+    assert st["relres"] < 1e-11 and st["outer"] <= 6 and st["iterations"] <= 120, st
     h2 = pkg.groundwater_steadystate(g["Ks"], g["nb"], g["aol"], g["dn"], g["dh"], g["Qs"],
                                      linear_solver=pkg.amg_solver, reltol=1e-10)
     assert rel(h2, g["h"]) < HEAD_TOL
