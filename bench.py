@@ -486,7 +486,7 @@ def main():
                     help="launch the CG loop from the host (ncu cannot profile kernels inside conditional graphs)")
     ap.add_argument("--main-only", action="store_true", help="only the timed region (for profiling runs)")
     ap.add_argument("--streams", type=int, default=0,
-                    help="the library's streams option (accepted and ignored: every batch runs on one stream)")
+                    help="split the batch into this many concurrent parts (0: the autotuner's choice)")
     ap.add_argument("--workload", default="steady_1m", choices=["steady_1m", "steady_100k", "uneven_batch", "transient", "general_1m",
                                                                 "richards"],
                     help="steady_1m is the headline; the others are the remaining configurations (bench_workloads.py)")

@@ -394,14 +394,13 @@ dpf_options fill_options(const dpf_options *o) {
     return r;
 }
 
-// The number of concurrent parts of a batch. Splitting is switched off: every batch runs on
-// one stream whatever `streams` asks, because runs with batches split into equal parts on
-// separate streams raised illegal-address faults whose cause was not found (the split path
-// stays below, unreachable, until it is).
+// The number of concurrent parts of a batch: `streams` parts (at most one per problem) when
+// streams > 1, else one. Each part is a complete batch handle on its own non-blocking stream,
+// driven by its own host thread, so one part's bandwidth-bound finest-level kernels run while
+// another part is in its latency-bound small levels.
 int batch_parts(int nprob, int streams) {
-    (void)nprob;
-    (void)streams;
-    return 1;
+    if (streams <= 1) return 1;
+    return std::min(streams, nprob);
 }
 
 int make_struct(const std::vector<GridSpec> &grids, const std::vector<std::vector<int64_t>> &dn,
@@ -418,21 +417,24 @@ int make_struct(const std::vector<GridSpec> &grids, const std::vector<std::vecto
         const int nprob = (int)grids.size();
         const int k = batch_parts(nprob, P->opt.streams);
         if (k > 1) {
-            // concurrent parts: equal runs of consecutive problems, each its own handle and stream
-            const int per = nprob / k;
+            // concurrent parts: runs of consecutive problems (sizes differing by at most one),
+            // each its own handle and stream
             dpf_options po = P->opt;
             po.streams = 1;
+            int first = 0;
             for (int i = 0; i < k; i++) {
+                const int cnt = nprob / k + (i < nprob % k ? 1 : 0);
                 auto Q = new dpf_problem();
                 P->parts.push_back(Q);  // owned by P from here on (deleted with it on any error)
                 Q->device = P->device;
                 Q->opt = po;
                 ck(cudaStreamCreateWithFlags(&Q->stream, cudaStreamNonBlocking), "part stream");
                 Q->own_stream = true;
-                std::vector<GridSpec> g(grids.begin() + i * per, grids.begin() + (i + 1) * per);
-                std::vector<std::vector<int64_t>> d(dn.begin() + i * per, dn.begin() + (i + 1) * per);
+                std::vector<GridSpec> g(grids.begin() + first, grids.begin() + first + cnt);
+                std::vector<std::vector<int64_t>> d(dn.begin() + first, dn.begin() + first + cnt);
                 Q->sb.reset(new StructBatch(g, d, Q->opt, Q->stream));
-                P->part_first.push_back(i * per);
+                P->part_first.push_back(first);
+                first += cnt;
             }
             P->part_first.push_back(nprob);
             for (int i = 0; i <= k; i++) {

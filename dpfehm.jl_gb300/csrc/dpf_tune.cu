@@ -131,6 +131,7 @@ extern "C" int dpf_batch_autotune(int nprob, const int *dims, const double *mins
             {"df_plane_cells", &cur.df_plane_cells, {-1, 512}, mixed},
             {"tail_cluster", &cur.tail_cluster, {1, 8}, true},
             {"plane_levels", &cur.plane_levels, {0, 1, 2}, mixed},
+            {"streams", &cur.streams, {1, 2, 4}, nprob >= 2},
         };
         for (const Knob &k : knobs) {
             if (!k.active || rc != DPF_OK) continue;

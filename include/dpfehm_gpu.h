@@ -94,8 +94,10 @@ typedef struct dpf_options {
     int plane_levels;    /* regular grids, MIXED: the plane-marching kernels run on this many of the
                             finest levels, grid-stride kernels below (default 0: every level whose
                             rows fit a slab) */
-    int streams;         /* batches: accepted and ignored; every batch runs on one stream (splitting
-                            a batch into concurrent parts is switched off) */
+    int streams;         /* batches: split into this many concurrent parts (consecutive problems, each
+                            on its own non-blocking stream and host thread), so that one part's
+                            finest-level kernels overlap another's small levels (default 0: one
+                            stream; an autotuner choice) */
 } dpf_options;
 
 typedef struct dpf_problem dpf_problem;

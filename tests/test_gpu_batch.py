@@ -169,25 +169,38 @@ def test_cluster_tail_agrees(gpu_lib, precision):
         assert rel(h, res[0][0]) < 1e-11 and rel(g, res[0][1]) < 1e-9
 
 
-def test_streams_option_runs_one_stream(gpu_lib):
-    """The streams option is accepted and ignored: every value gives the same single-stream
-    solve (bit for bit), and the handle serves every entry point."""
+def test_batch_split_into_concurrent_parts(gpu_lib, orc):
+    """streams = k splits a batch into k parts of consecutive problems (sizes differing by one
+    when k does not divide the batch), each on its own stream and host thread. Every part is a
+    smaller batch of the same solver, whose per-problem reductions run over a different number
+    of blocks, so the results equal the single-stream ones to rounding and the oracle's to the
+    usual tolerances. Entry points other than the batched solve are refused on a split handle."""
     pkg = gpu_lib
-    shapes = [(20, 16, 5), (9, 9, 9), (40, 30, 6), (17, 5, 11)]
+    shapes = [(20, 16, 5), (9, 9, 9), (40, 30, 6), (17, 5, 11), (24, 20, 8)]
     probs = [_problem(pkg, ns, 81 + k) for k, ns in enumerate(shapes)]
     cat = lambda k: np.concatenate([p[k] for p in probs])
     args = ([p["ns"] for p in probs], [p["mins"] for p in probs], [p["maxs"] for p in probs],
             [p["dn"] for p in probs])
     res = {}
-    for streams in (0, 1, 2, 4):
+    for streams in (1, 2, 3, 4):
         B = pkg.GroundwaterBatch(*args, reltol=1e-12, precision="mixed", streams=streams)
-        res[streams] = B.solve_grad_logk(cat("logK"), cat("dh"), cat("Qs"), [p["obs"] for p in probs])
+        for _ in range(2):  # the first solve of fresh parts, then a repeat on the same handles
+            res[streams] = B.solve_grad_logk(cat("logK"), cat("dh"), cat("Qs"), [p["obs"] for p in probs])
         assert list(B.cell_offsets) == list(np.cumsum([0] + [p["N"] for p in probs]))
-        B.forward_logk(cat("logK"), cat("dh"), cat("Qs"))
+        if streams > 1:
+            with pytest.raises(pkg.DPFError) as e:
+                B.forward_logk(cat("logK"), cat("dh"), cat("Qs"))
+            assert e.value.code == pkg._lib.DPF_UNSUPPORTED
+        else:
+            B.forward_logk(cat("logK"), cat("dh"), cat("Qs"))
         B.close()
     h1, g1 = res[1]
-    for s in (0, 2, 4):
-        assert np.array_equal(res[s][0], h1) and np.array_equal(res[s][1], g1), s
+    for s in (2, 3, 4):
+        assert rel(res[s][0], h1) < 1e-11 and rel(res[s][1], g1) < 1e-9, s
+    for k, p in enumerate(probs):
+        a, b = int(np.sum([q["N"] for q in probs[:k]])), int(np.sum([q["N"] for q in probs[:k + 1]]))
+        h_or, g_or = _oracle(orc, pkg, p)
+        assert rel(res[4][0][a:b], h_or) < 1e-8 and rel(res[4][1][a:b], g_or) < 1e-6, k
 
 
 def test_set_stream(gpu_lib):

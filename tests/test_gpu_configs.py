@@ -12,8 +12,10 @@
     steps of h^2 at 50 cells) on its full grid, cut from 100 to 12 steps with a checkpoint every
     5 steps (so the last segment is partial) to keep the oracle's 24 solves within a minute.
 
-The oracle solves to reltol 1e-14; the GPU to the configurations' 1e-10. Tolerances (relative L2):
-heads 1e-8, gradients 1e-6.
+The oracle solves to reltol 1e-14; the GPU to the configurations' 1e-10, except the transient run,
+whose every step is solved to 1e-11: the states of 12 steps at 1e-10 per step were 2.8e-8 from the
+oracle's (both precisions alike), above the 1e-8 head bar. Tolerances (relative L2): heads 1e-8,
+gradients 1e-6.
 """
 import numpy as np
 import pytest
@@ -139,7 +141,7 @@ def test_transient_800k_cells_vs_oracle(gpu_lib, orc, precision):
     O = orc.Problem(N, nb, aol, dn)
     st_or = O.transient(Ks, dh, Qs, Ss, vol, dt, nsteps, np.zeros(O.nfree), reltol=1e-14)
     dK_or, ddh_or, dQ_or, dh0_or = O.transient_adjoint(dh, obs, reltol=1e-14)
-    P = pkg.GroundwaterProblem.regular3d(mins, maxs, grid, dn, reltol=1e-10, precision=precision)
+    P = pkg.GroundwaterProblem.regular3d(mins, maxs, grid, dn, reltol=1e-11, precision=precision)
     hT, states = P.transient_forward(Ks, dh, Qs, Ss, dt, nsteps, np.zeros(N), checkpoint_every=ck,
                                      return_states=True)
     isf, _, _ = pkg.getfreenodes(N, dn)
