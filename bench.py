@@ -309,7 +309,10 @@ def profile_pass(pkg, torch, dev, B, N, prec, args, tuned=None):
     # per-kernel events need a saturated stream: convergence is read back every 4
     # iterations here so the host stays ahead of the GPU (graphs are off while profiling);
     # the launch shapes are the timed run's
+    # one stream: with the batch split into concurrent parts, a kernel's events would also span
+    # the other parts' kernels running beside it, so each kernel is timed alone here
     opts = dict(tuned or {})
+    opts["streams"] = 1
     b = pkg.GroundwaterBatch([GRID] * B, [MINS] * B, [MAXS] * B, [[N - 1]] * B, reltol=RELTOL, precision=prec,
                              check_every=4, **opts)
     d = [torch.tensor(x, device=dev) for x in (logK, dh, Qs)]
@@ -350,8 +353,10 @@ def profile_pass(pkg, torch, dev, B, N, prec, args, tuned=None):
         "top": [{"kernel": k, "launches": v[0], "ms": round(v[1], 3),
                  "GBps": round(BYTES_PER_CELL[k.split("<")[0]](4 if "<f32>" in k else 8) * v[2] / (v[1] / 1e3) / 1e9, 1)
                  if k.split("<")[0] in BYTES_PER_CELL and v[1] > 0 else None} for k, v in top[:8]],
-        "measured": "per-kernel CUDA events on the solver stream over %d forward+adjoint steps of the same workload (the batch on one stream)"
-                    % max(1, min(args.steps, 3)),
+        "measured": "per-kernel CUDA events on the solver stream over %d forward+adjoint steps of a profiling pass: the "
+                    "timed run's launch shapes and batch size, the batch on one stream (each kernel alone), %d identical "
+                    "realizations of a different seed (every scheduled cell active in every launch), convergence read "
+                    "every 4 iterations with graphs off" % (max(1, min(args.steps, 3)), B),
         "profile_options": {k: v for k, v in opts.items()},
     }
 
