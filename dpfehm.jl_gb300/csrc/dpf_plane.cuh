@@ -182,30 +182,42 @@ __device__ __forceinline__ void stage_range(uint64_t *bar, const void *base, int
 // Fast division of k (< 2^31) by nz with the level's invariant-integer constants.
 __device__ __forceinline__ int div_nz(const LevelDesc &L, int k) { return (int)fast_div((unsigned)k, L.mag_nz, L.sh_nz); }
 
-// Producer loop, run by lane 0 of the producer warp: stages planes pl_lo..pl_hi into the
-// ring of R slots as the consumer warps release them. stage_plane(q, slot, bar) announces
-// (mbarrier expect_tx) and issues the copies of plane q; the one pending arrival made here
-// afterwards keeps the phase open until every copy has been announced. Before the block
-// may end, the last phase of every filled slot is waited for (bounded), so no copy is
-// still in flight into the block's shared memory. Should one of those waits expire, copies
-// may still land after the block ends: the error word is set, the solve reports DPF_TIMEOUT
-// and the host treats the device's results as suspect.
+// Work of a plane-marching launch: items {p, y0, x0, x1} (a slab of rows y0.. of problem p,
+// planes x0..x1-1; x0 even, x1 even or the grid's last plane), and per block the contiguous
+// range of items it marches through, first[b] .. first[b+1]-1. The host cuts the items so that
+// every block gets about the same number of cells. A block's planes are numbered across its
+// items (g = 0, 1, ...): ring slot g % R, phase (g / R) & 1, so the ring runs on from one item to
+// the next.
+struct PlaneWork {
+    const int4 *items;
+    const int *first;
+};
+
+// Producer of one item, run by lane 0 of the producer warp: stages planes pl_lo..pl_hi (block
+// plane numbers g0, g0 + 1, ...) into the ring as the consumer warps release slots.
+// stage_plane(q, slot, bar) announces (mbarrier expect_tx) and issues the copies of plane q;
+// the one pending arrival made here afterwards keeps the phase open until every copy has been
+// announced. Returns the planes issued (fewer than the item's when a bounded wait expired).
 template <int R, typename F>
-__device__ __forceinline__ void pm_produce(int pl_lo, int pl_hi, uint64_t *full, uint64_t *empty, unsigned char *sm,
-                                           int slot_bytes, int *err, F stage_plane) {
-    int issued_hi = pl_lo - 1;
+__device__ __forceinline__ int pm_produce(int pl_lo, int pl_hi, int g0, uint64_t *full, uint64_t *empty,
+                                          unsigned char *sm, int slot_bytes, int *err, F stage_plane) {
     for (int q = pl_lo; q <= pl_hi; q++) {
-        const int u = q - pl_lo, s = u % R;
-        if (u >= R && !mbar_wait(&empty[s], (uint32_t)((u / R - 1) & 1), err)) break;
+        const int g = g0 + (q - pl_lo), s = g % R;
+        if (g >= R && !mbar_wait(&empty[s], (uint32_t)((g / R - 1) & 1), err)) return q - pl_lo;
         fence_proxy_async_smem();
         stage_plane(q, (char *)sm + s * slot_bytes, &full[s]);
         mbar_arrive(&full[s]);
-        issued_hi = q;
     }
-    for (int q = max(pl_lo, issued_hi - R + 1); q <= issued_hi; q++) {
-        const int u = q - pl_lo;
-        mbar_wait(&full[u % R], (uint32_t)((u / R) & 1), err);
-    }
+    return pl_hi - pl_lo + 1;
+}
+
+// Before the block may end, the last phase of every filled slot (the last min(R, issued) planes)
+// is waited for (bounded), so no copy is still in flight into the block's shared memory. Should
+// one of those waits expire, copies may still land after the block ends: the error word is set,
+// the solve reports DPF_TIMEOUT and the host treats the device's results as suspect.
+template <int R>
+__device__ __forceinline__ void pm_drain(int issued, uint64_t *full, int *err) {
+    for (int g = max(0, issued - R); g < issued; g++) mbar_wait(&full[g % R], (uint32_t)((g / R) & 1), err);
 }
 
 // Chebyshev step family on the plane ring. MODE bits:
@@ -220,10 +232,13 @@ __device__ __forceinline__ void pm_produce(int pl_lo, int pl_hi, uint64_t *full,
 // Warp-specialised pipeline: warp kPlaneThreads/32 is the producer (its lane 0 stages
 // plane after plane as ring slots free up), warps 0..7 consume. Per slot three mbarriers:
 // full (copies landed), empty (all consumer warps are done with the plane), ready (with
-// PM_PROLONG: every consumer thread has applied its share of the correction).
+// PM_PROLONG: every consumer thread has applied its share of the correction). A block marches
+// through its items one after another; at the end of each item every thread meets (a block
+// barrier that also carries the error flag, and with PM_RZ the item's partial of b . xout in its
+// own reduction slot, so the sum per problem is formed in a fixed order).
 template <typename T, int MODE, int CPT>
 __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
-    const LevelDesc *__restrict__ desc, const LevelDesc *__restrict__ cdesc, const int4 *__restrict__ items,
+    const LevelDesc *__restrict__ desc, const LevelDesc *__restrict__ cdesc, PlaneWork work,
     CgState *st, Coeffs<T> C, const T *__restrict__ b, const T *__restrict__ xin, T *__restrict__ xout,
     T *__restrict__ d, const uint8_t *__restrict__ dir, const T *__restrict__ e, T c1, T c2, T invtheta, T scale,
     PlaneLayout lay, ReduceScratch rs, const int2 *__restrict__ pinfo, int *err) {
@@ -238,25 +253,9 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
     extern __shared__ __align__(128) unsigned char sm[];
     __shared__ uint64_t full[R], empty[R], ready[R];
 
-    const int4 it = items[blockIdx.x];
-    const int p = it.x, y0 = it.y, xa = it.z, xe = it.w;
-    if (st && !st[p].active) return;
-    const LevelDesc L = desc[p];
-    const int nz = L.nz, ny = L.ny, nx = L.nx;
-    const long long sx = (long long)ny * nz;
-    const int Ty = plane_rows(ny, nz, CPT * kPlaneThreads);
-    const int rows = min(Ty, ny - y0);
-    const int ncell = rows * nz;
     const int t = threadIdx.x;
     const int warp = t >> 5, lane = t & 31;
-    const int pl_lo = max(xa - 1, 0), pl_hi = min(xe, nx - 1);
-    const int h0 = max(y0 - 1, 0), h1 = min(y0 + rows + 1, ny);
-    LevelDesc Lc{};
-    if (PROL) Lc = cdesc[p];
-    const long long csx = PROL ? (long long)Lc.ny * Lc.nz : 0;
-    const int cr_lo = (y0 - 1) >> 1;  // logical first coarse row of the halo (may be -1)
-    auto slot_of = [&](int q) { return (char *)sm + ((unsigned)(q - pl_lo) % (unsigned)R) * lay.slot_bytes; };
-
+    auto slot_of = [&](int g) { return (char *)sm + ((unsigned)g % (unsigned)R) * lay.slot_bytes; };
     if (t == 0) {
         for (int s = 0; s < R; s++) {
             mbar_init(&full[s], 1);
@@ -266,198 +265,231 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
         fence_mbarrier_init();
     }
     __syncthreads();
-    Acc<T> part;
+    int g0 = 0;      // block plane number of the current item's first plane
+    int issued = 0;  // planes the producer has staged (producer lane 0)
+    for (int w = work.first[blockIdx.x]; w < work.first[blockIdx.x + 1]; w++) {
+        const int4 it = work.items[w];
+        const int p = it.x, y0 = it.y, xa = it.z, xe = it.w;
+        if (st && !st[p].active) continue;  // uniform over the block
+        const LevelDesc L = desc[p];
+        const int nz = L.nz, ny = L.ny, nx = L.nx;
+        const long long sx = (long long)ny * nz;
+        const int Ty = plane_rows(ny, nz, CPT * kPlaneThreads);
+        const int rows = min(Ty, ny - y0);
+        const int ncell = rows * nz;
+        const int pl_lo = max(xa - 1, 0), pl_hi = min(xe, nx - 1);
+        const int h0 = max(y0 - 1, 0), h1 = min(y0 + rows + 1, ny);
+        LevelDesc Lc{};
+        if (PROL) Lc = cdesc[p];
+        const long long csx = PROL ? (long long)Lc.ny * Lc.nz : 0;
+        const int cr_lo = (y0 - 1) >> 1;  // logical first coarse row of the halo (may be -1)
+        auto gof = [&](int q) { return g0 + (q - pl_lo); };
+        Acc<T> part;
+        bool bad = false;
 
-    if (warp == kConsumerWarps) {
-        // ---------------- producer
-        if (lane == 0) {
-            pm_produce<R>(pl_lo, pl_hi, full, empty, sm, lay.slot_bytes, err, [&](int q, char *slot, uint64_t *bar) {
-                const long long pb = L.off + (long long)q * sx;
-                const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
-                const long long hA = pb + (long long)h0 * nz, hB = pb + (long long)h1 * nz, pE = lp + ncell;
-                auto stage = [&](const void *base, int esz, long long l0, long long a0, long long a1, int off) {
-                    stage_range(bar, base, esz, l0, a0, a1, slot + off, L.off, L.off + L.n, slot, lay.slot_bytes);
-                };
-                if (F2) {
-                    stage(b, es, lh, hA, hB, lay.oB);
-                    stage(C.idg, es, lh, hA, hB, lay.oG);
-                } else {
-                    stage(xin, es, lh, hA, hB, lay.oX);
-                    stage(b, es, lp, lp, pE, lay.oB);
-                    if (!FIRST) stage(d, es, lp, lp, pE, lay.oD);
-                }
-                stage(C.cx, ec, lp, lp, pE, lay.oCX);
-                stage(C.cy, ec, lh, hA, pE, lay.oCY);
-                stage(C.cz, ec, lp, lp, pE, lay.oCZ);
-                stage(C.leak, ec, lp, lp, pE, lay.oLK);
-                if (PROL) {
-                    stage(dir, 1, lh, hA, hB, lay.oDIR);
-                    const long long cb = Lc.off + (long long)(q >> 1) * csx;
-                    const int c0 = max(cr_lo, 0), c1r = min((y0 + rows) >> 1, Lc.ny - 1) + 1;
-                    stage_range(bar, e, es, cb + (long long)cr_lo * Lc.nz, cb + (long long)c0 * Lc.nz,
-                                cb + (long long)c1r * Lc.nz, slot + lay.oE, Lc.off, Lc.off + Lc.n, slot,
-                                lay.slot_bytes);
-                }
-            });
-        }
-        __syncwarp();
-    } else {
-        // ---------------- consumers
-        // this thread's cells of the slab (the same in every plane) and their y/z neighbours
-        unsigned cfl[CPT];
-#pragma unroll
-        for (int k = 0; k < CPT; k++) {
-            const int tc = t + k * kPlaneThreads;
-            unsigned f = 0;
-            if (tc < ncell) {
-                const int ty = div_nz(L, tc), z = tc - ty * nz, y = y0 + ty;
-                f = CF_VALID | (z + 1 < nz ? CF_ZP : 0u) | (z > 0 ? CF_ZM : 0u) | (y + 1 < ny ? CF_YP : 0u) |
-                    (y > 0 ? CF_YM : 0u);
-            }
-            cfl[k] = f;
-        }
-        int waited = pl_lo - 1;
-        bool ok = true;
-        for (int x = xa; x < xe && ok; x++) {
-            const int need = min(x + 1, pl_hi);
-            const int first_new = waited + 1;
-            while (waited < need) {
-                const int q = waited + 1, u = q - pl_lo;
-                if (!mbar_wait(&full[u % R], (uint32_t)((u / R) & 1), err)) {
-                    ok = false;
-                    break;
-                }
-                waited = q;
-                if (PROL) {
-                    // prolongation on arrival: this thread's share of the slab and its halo rows
-                    char *sl = slot_of(q);
+        if (warp == kConsumerWarps) {
+            // ---------------- producer
+            if (lane == 0) {
+                const int n = pm_produce<R>(pl_lo, pl_hi, g0, full, empty, sm, lay.slot_bytes, err,
+                                            [&](int q, char *slot, uint64_t *bar) {
                     const long long pb = L.off + (long long)q * sx;
-                    const long long lh = pb + (long long)(y0 - 1) * nz;
-                    T *X = (T *)(sl + lay.oX) + stage_delta(lh, es);
-                    const uint8_t *DR = (const uint8_t *)(sl + lay.oDIR) + stage_delta(lh, 1);
-                    const long long cb = Lc.off + (long long)(q >> 1) * csx;
-                    const T *E = (const T *)(sl + lay.oE) + stage_delta(cb + (long long)cr_lo * Lc.nz, es);
-                    const int nh = (rows + 2) * nz;
-                    for (int k = t; k < nh; k += kPlaneThreads) {
-                        const int rr = div_nz(L, k);
-                        const int row = y0 - 1 + rr;
-                        if (row < 0 || row >= ny || DR[k]) continue;
-                        const int zz = k - rr * nz;
-                        X[k] += scale * E[((row >> 1) - cr_lo) * Lc.nz + (zz >> 1)];
+                    const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
+                    const long long hA = pb + (long long)h0 * nz, hB = pb + (long long)h1 * nz, pE = lp + ncell;
+                    auto stage = [&](const void *base, int esz, long long l0, long long a0, long long a1, int off) {
+                        stage_range(bar, base, esz, l0, a0, a1, slot + off, L.off, L.off + L.n, slot, lay.slot_bytes);
+                    };
+                    if (F2) {
+                        stage(b, es, lh, hA, hB, lay.oB);
+                        stage(C.idg, es, lh, hA, hB, lay.oG);
+                    } else {
+                        stage(xin, es, lh, hA, hB, lay.oX);
+                        stage(b, es, lp, lp, pE, lay.oB);
+                        if (!FIRST) stage(d, es, lp, lp, pE, lay.oD);
                     }
-                    mbar_arrive(&ready[u % R]);
-                }
+                    stage(C.cx, ec, lp, lp, pE, lay.oCX);
+                    stage(C.cy, ec, lh, hA, pE, lay.oCY);
+                    stage(C.cz, ec, lp, lp, pE, lay.oCZ);
+                    stage(C.leak, ec, lp, lp, pE, lay.oLK);
+                    if (PROL) {
+                        stage(dir, 1, lh, hA, hB, lay.oDIR);
+                        const long long cb = Lc.off + (long long)(q >> 1) * csx;
+                        const int c0 = max(cr_lo, 0), c1r = min((y0 + rows) >> 1, Lc.ny - 1) + 1;
+                        stage_range(bar, e, es, cb + (long long)cr_lo * Lc.nz, cb + (long long)c0 * Lc.nz,
+                                    cb + (long long)c1r * Lc.nz, slot + lay.oE, Lc.off, Lc.off + Lc.n, slot,
+                                    lay.slot_bytes);
+                    }
+                });
+                issued += n;
+                bad = n != pl_hi - pl_lo + 1;
             }
-            if (!ok) break;
-            if (PROL) {
-                for (int q = first_new; q <= waited; q++) {
-                    const int u = q - pl_lo;
-                    if (!mbar_wait(&ready[u % R], (uint32_t)((u / R) & 1), err)) {
-                        ok = false;
+            __syncwarp();
+        } else {
+            // ---------------- consumers
+            // this thread's cells of the slab (the same in every plane) and their y/z neighbours
+            unsigned cfl[CPT];
+#pragma unroll
+            for (int k = 0; k < CPT; k++) {
+                const int tc = t + k * kPlaneThreads;
+                unsigned f = 0;
+                if (tc < ncell) {
+                    const int ty = div_nz(L, tc), z = tc - ty * nz, y = y0 + ty;
+                    f = CF_VALID | (z + 1 < nz ? CF_ZP : 0u) | (z > 0 ? CF_ZM : 0u) | (y + 1 < ny ? CF_YP : 0u) |
+                        (y > 0 ? CF_YM : 0u);
+                }
+                cfl[k] = f;
+            }
+            int waited = pl_lo - 1, released = pl_lo;
+            for (int x = xa; x < xe && !bad; x++) {
+                const int need = min(x + 1, pl_hi);
+                const int first_new = waited + 1;
+                while (waited < need) {
+                    const int q = waited + 1, g = gof(q);
+                    if (!mbar_wait(&full[g % R], (uint32_t)((g / R) & 1), err)) {
+                        bad = true;
                         break;
                     }
-                }
-                if (!ok) break;
-            }
-            {
-                // per-plane addresses, shared by this thread's cells
-                const long long pb = L.off + (long long)x * sx;
-                const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
-                const int dh = stage_delta(lh, es), dp = stage_delta(lp, es);
-                char *sc = slot_of(x);
-                const bool xp = x + 1 < nx, xm = x > 0;
-                char *sn = xp ? slot_of(x + 1) : sc;
-                char *sq = xm ? slot_of(x - 1) : sc;
-                const int dn_ = xp ? stage_delta(lh + sx, es) : dh;
-                const int dq = xm ? stage_delta(lh - sx, es) : dh;
-                const int ch = stage_delta(lh, ec), cp = stage_delta(lp, ec);
-                const int cqp = xm ? stage_delta(lp - sx, ec) : cp;
-                const CT *CX = (const CT *)(sc + lay.oCX) + cp;
-                const CT *CXq = (const CT *)(sq + lay.oCX) + cqp;
-                const CT *CY = (const CT *)(sc + lay.oCY) + ch;  // logical row 0 = y0 - 1
-                const CT *CZ = (const CT *)(sc + lay.oCZ) + cp;
-                const CT *LK = (const CT *)(sc + lay.oLK) + cp;
-#pragma unroll
-                for (int k = 0; k < CPT; k++) {
-                    const unsigned f = cfl[k];
-                    if (!(f & CF_VALID)) continue;
-                    const int tc = t + k * kPlaneThreads;
-                    const long long i = lp + tc;
-                    const int c = nz + tc;  // own cell in halo coordinates
-                    if (F2) {
-                        // x1 = invtheta b g at a cell; neighbours from the staged b and g halos
-                        const T *B = (const T *)(sc + lay.oB) + dh;
-                        const T *G = (const T *)(sc + lay.oG) + dh;
-                        const T bi = B[c], gi = G[c];
-                        const T x1 = invtheta * bi * gi;
-                        T a = cf(LK[tc]) * x1;
-                        if (f & CF_ZP) a += cf(CZ[tc]) * (x1 - invtheta * B[c + 1] * G[c + 1]);
-                        if (f & CF_ZM) a += cf(CZ[tc - 1]) * (x1 - invtheta * B[c - 1] * G[c - 1]);
-                        if (f & CF_YP) a += cf(CY[c]) * (x1 - invtheta * B[c + nz] * G[c + nz]);
-                        if (f & CF_YM) a += cf(CY[tc]) * (x1 - invtheta * B[c - nz] * G[c - nz]);
-                        if (xp) {
-                            const T *Bn = (const T *)(sn + lay.oB) + dn_;
-                            const T *Gn = (const T *)(sn + lay.oG) + dn_;
-                            a += cf(CX[tc]) * (x1 - invtheta * Bn[c] * Gn[c]);
+                    waited = q;
+                    if (PROL) {
+                        // prolongation on arrival: this thread's share of the slab and its halo rows
+                        char *sl = slot_of(g);
+                        const long long pb = L.off + (long long)q * sx;
+                        const long long lh = pb + (long long)(y0 - 1) * nz;
+                        T *X = (T *)(sl + lay.oX) + stage_delta(lh, es);
+                        const uint8_t *DR = (const uint8_t *)(sl + lay.oDIR) + stage_delta(lh, 1);
+                        const long long cb = Lc.off + (long long)(q >> 1) * csx;
+                        const T *E = (const T *)(sl + lay.oE) + stage_delta(cb + (long long)cr_lo * Lc.nz, es);
+                        const int nh = (rows + 2) * nz;
+                        for (int k = t; k < nh; k += kPlaneThreads) {
+                            const int rr = div_nz(L, k);
+                            const int row = y0 - 1 + rr;
+                            if (row < 0 || row >= ny || DR[k]) continue;
+                            const int zz = k - rr * nz;
+                            X[k] += scale * E[((row >> 1) - cr_lo) * Lc.nz + (zz >> 1)];
                         }
-                        if (xm) {
-                            const T *Bq = (const T *)(sq + lay.oB) + dq;
-                            const T *Gq = (const T *)(sq + lay.oG) + dq;
-                            a += cf(CXq[tc]) * (x1 - invtheta * Bq[c] * Gq[c]);
-                        }
-                        const T dn = c1 * x1 + c2 * (bi - a) * gi;
-                        if (!NOD) d[i] = dn;
-                        xout[i] = x1 + dn;
-                    } else {
-                        const T *X = (const T *)(sc + lay.oX) + dh;
-                        const T xi = X[c];
-                        const T lk = cf(LK[tc]);
-                        T a = lk * xi, dg = lk;
-                        if (f & CF_ZP) { T w = cf(CZ[tc]);     a += w * (xi - X[c + 1]);  dg += w; }
-                        if (f & CF_ZM) { T w = cf(CZ[tc - 1]); a += w * (xi - X[c - 1]);  dg += w; }
-                        if (f & CF_YP) { T w = cf(CY[c]);      a += w * (xi - X[c + nz]); dg += w; }
-                        if (f & CF_YM) { T w = cf(CY[tc]);     a += w * (xi - X[c - nz]); dg += w; }
-                        if (xp) {
-                            const T *Xn = (const T *)(sn + lay.oX) + dn_;
-                            T w = cf(CX[tc]);
-                            a += w * (xi - Xn[c]);
-                            dg += w;
-                        }
-                        if (xm) {
-                            const T *Xq = (const T *)(sq + lay.oX) + dq;
-                            T w = cf(CXq[tc]);
-                            a += w * (xi - Xq[c]);
-                            dg += w;
-                        }
-                        const T bi = ((const T *)(sc + lay.oB) + dp)[tc];
-                        T r;
-                        if constexpr (sizeof(T) == 8) r = (bi - a) * C.idg[i];
-                        else r = __fdividef(bi - a, dg);
-                        T dn;
-                        if (FIRST) dn = c2 * r;
-                        else dn = c1 * ((const T *)(sc + lay.oD) + dp)[tc] + c2 * r;
-                        const T xo = xi + dn;
-                        if (!NOD) d[i] = dn;
-                        xout[i] = xo;
-                        if (RZ) part = part + Acc<T>::prod(bi, xo);
+                        mbar_arrive(&ready[g % R]);
                     }
                 }
+                if (bad) break;
+                if (PROL) {
+                    for (int q = first_new; q <= waited; q++) {
+                        const int g = gof(q);
+                        if (!mbar_wait(&ready[g % R], (uint32_t)((g / R) & 1), err)) {
+                            bad = true;
+                            break;
+                        }
+                    }
+                    if (bad) break;
+                }
+                {
+                    // per-plane addresses, shared by this thread's cells
+                    const long long pb = L.off + (long long)x * sx;
+                    const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
+                    const int dh = stage_delta(lh, es), dp = stage_delta(lp, es);
+                    char *sc = slot_of(gof(x));
+                    const bool xp = x + 1 < nx, xm = x > 0;
+                    char *sn = xp ? slot_of(gof(x + 1)) : sc;
+                    char *sq = xm ? slot_of(gof(x - 1)) : sc;
+                    const int dn_ = xp ? stage_delta(lh + sx, es) : dh;
+                    const int dq = xm ? stage_delta(lh - sx, es) : dh;
+                    const int ch = stage_delta(lh, ec), cp = stage_delta(lp, ec);
+                    const int cqp = xm ? stage_delta(lp - sx, ec) : cp;
+                    const CT *CX = (const CT *)(sc + lay.oCX) + cp;
+                    const CT *CXq = (const CT *)(sq + lay.oCX) + cqp;
+                    const CT *CY = (const CT *)(sc + lay.oCY) + ch;  // logical row 0 = y0 - 1
+                    const CT *CZ = (const CT *)(sc + lay.oCZ) + cp;
+                    const CT *LK = (const CT *)(sc + lay.oLK) + cp;
+#pragma unroll
+                    for (int k = 0; k < CPT; k++) {
+                        const unsigned f = cfl[k];
+                        if (!(f & CF_VALID)) continue;
+                        const int tc = t + k * kPlaneThreads;
+                        const long long i = lp + tc;
+                        const int c = nz + tc;  // own cell in halo coordinates
+                        if (F2) {
+                            // x1 = invtheta b g at a cell; neighbours from the staged b and g halos
+                            const T *B = (const T *)(sc + lay.oB) + dh;
+                            const T *G = (const T *)(sc + lay.oG) + dh;
+                            const T bi = B[c], gi = G[c];
+                            const T x1 = invtheta * bi * gi;
+                            T a = cf(LK[tc]) * x1;
+                            if (f & CF_ZP) a += cf(CZ[tc]) * (x1 - invtheta * B[c + 1] * G[c + 1]);
+                            if (f & CF_ZM) a += cf(CZ[tc - 1]) * (x1 - invtheta * B[c - 1] * G[c - 1]);
+                            if (f & CF_YP) a += cf(CY[c]) * (x1 - invtheta * B[c + nz] * G[c + nz]);
+                            if (f & CF_YM) a += cf(CY[tc]) * (x1 - invtheta * B[c - nz] * G[c - nz]);
+                            if (xp) {
+                                const T *Bn = (const T *)(sn + lay.oB) + dn_;
+                                const T *Gn = (const T *)(sn + lay.oG) + dn_;
+                                a += cf(CX[tc]) * (x1 - invtheta * Bn[c] * Gn[c]);
+                            }
+                            if (xm) {
+                                const T *Bq = (const T *)(sq + lay.oB) + dq;
+                                const T *Gq = (const T *)(sq + lay.oG) + dq;
+                                a += cf(CXq[tc]) * (x1 - invtheta * Bq[c] * Gq[c]);
+                            }
+                            const T dn = c1 * x1 + c2 * (bi - a) * gi;
+                            if (!NOD) d[i] = dn;
+                            xout[i] = x1 + dn;
+                        } else {
+                            const T *X = (const T *)(sc + lay.oX) + dh;
+                            const T xi = X[c];
+                            const T lk = cf(LK[tc]);
+                            T a = lk * xi, dg = lk;
+                            if (f & CF_ZP) { T w_ = cf(CZ[tc]);     a += w_ * (xi - X[c + 1]);  dg += w_; }
+                            if (f & CF_ZM) { T w_ = cf(CZ[tc - 1]); a += w_ * (xi - X[c - 1]);  dg += w_; }
+                            if (f & CF_YP) { T w_ = cf(CY[c]);      a += w_ * (xi - X[c + nz]); dg += w_; }
+                            if (f & CF_YM) { T w_ = cf(CY[tc]);     a += w_ * (xi - X[c - nz]); dg += w_; }
+                            if (xp) {
+                                const T *Xn = (const T *)(sn + lay.oX) + dn_;
+                                T w_ = cf(CX[tc]);
+                                a += w_ * (xi - Xn[c]);
+                                dg += w_;
+                            }
+                            if (xm) {
+                                const T *Xq = (const T *)(sq + lay.oX) + dq;
+                                T w_ = cf(CXq[tc]);
+                                a += w_ * (xi - Xq[c]);
+                                dg += w_;
+                            }
+                            const T bi = ((const T *)(sc + lay.oB) + dp)[tc];
+                            T r;
+                            if constexpr (sizeof(T) == 8) r = (bi - a) * C.idg[i];
+                            else r = __fdividef(bi - a, dg);
+                            T dn;
+                            if (FIRST) dn = c2 * r;
+                            else dn = c1 * ((const T *)(sc + lay.oD) + dp)[tc] + c2 * r;
+                            const T xo = xi + dn;
+                            if (!NOD) d[i] = dn;
+                            xout[i] = xo;
+                            if (RZ) part = part + Acc<T>::prod(bi, xo);
+                        }
+                    }
+                }
+                // this warp is done with plane x-1
+                __syncwarp();
+                if (lane == 0 && x - 1 >= released) mbar_arrive(&empty[gof(x - 1) % R]);
+                released = max(released, x);
             }
-            // this warp is done with plane x-1
-            __syncwarp();
-            if (lane == 0 && x - 1 >= pl_lo) mbar_arrive(&empty[(x - 1 - pl_lo) % R]);
+            // the item's remaining planes go back to the producer
+            if (!bad) {
+                __syncwarp();
+                for (int q = released; q <= waited; q++)
+                    if (lane == 0) mbar_arrive(&empty[gof(q) % R]);
+            }
         }
-    }
-    if (RZ) {
-        double2 tot;
-        if (reduce_last<T>(part, Acc<T>(), rs, pinfo[p], p, tot) && threadIdx.x == 0) {
-            CgState &s = st[p];
-            s.rz_old = s.rz;
-            s.rz = tot.x;
-            s.beta = (s.iters == 0 || s.rz_old == 0.0) ? 0.0 : s.rz / s.rz_old * s.cont;
-            s.cont = 1.0;
+        g0 += pl_hi - pl_lo + 1;
+        if (RZ) {
+            double2 tot;
+            if (reduce_last_slot<T>(part, rs, pinfo[p], p, w, tot) && threadIdx.x == 0) {
+                CgState &s = st[p];
+                s.rz_old = s.rz;
+                s.rz = tot.x;
+                s.beta = (s.iters == 0 || s.rz_old == 0.0) ? 0.0 : s.rz / s.rz_old * s.cont;
+                s.cont = 1.0;
+            }
         }
+        if (__syncthreads_or(bad)) break;  // every thread leaves together after an expired wait
     }
+    if (warp == kConsumerWarps && lane == 0) pm_drain<R>(issued, full, err);
 }
 
 __device__ __forceinline__ void finish_pq(CgState &s, double pq, int *active_count) {
@@ -471,10 +503,11 @@ __device__ __forceinline__ void finish_pq(CgState &s, double pq, int *active_cou
 // shared buffer (two planes), and after every odd plane (or the grid's last) the coarse
 // cells of the slab sum their children in the order of cell_restrict (x, then y, then z),
 // so the coarse right-hand side is bitwise that of k_restrict. Slabs start on even rows and
-// chunks on even planes. Streams per plane: x with halo rows, b, cx, cy (+ row below), cz, leak.
+// items on even planes (and end on one, or on the grid's last plane). Streams per plane: x with
+// halo rows, b, cx, cy (+ row below), cz, leak. A block marches through its items like k_pm_cheb.
 template <typename T, int CPT>
 __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
-    const LevelDesc *__restrict__ desc, const LevelDesc *__restrict__ cdesc, const int4 *__restrict__ items,
+    const LevelDesc *__restrict__ desc, const LevelDesc *__restrict__ cdesc, PlaneWork work,
     const CgState *st, Coeffs<T> C, const T *__restrict__ b, const T *__restrict__ xin, T *__restrict__ bc,
     PlaneLayout lay, int *err) {
     pdl_enter();
@@ -487,25 +520,9 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
     __shared__ uint64_t full[R], empty[R];
     __shared__ T res[2][CPT * kPlaneThreads];
 
-    const int4 it = items[blockIdx.x];
-    const int p = it.x, y0 = it.y, xa = it.z, xe = it.w;
-    if (st && !st[p].active) return;
-    const LevelDesc L = desc[p];
-    const LevelDesc Lc = cdesc[p];
-    const int nz = L.nz, ny = L.ny, nx = L.nx;
-    const long long sx = (long long)ny * nz;
-    const int Ty = plane_rows(ny, nz, CPT * kPlaneThreads);
-    const int rows = min(Ty, ny - y0);
-    const int ncell = rows * nz;
     const int t = threadIdx.x;
     const int warp = t >> 5, lane = t & 31;
-    const int pl_lo = max(xa - 1, 0), pl_hi = min(xe, nx - 1);
-    const int h0 = max(y0 - 1, 0), h1 = min(y0 + rows + 1, ny);
-    auto slot_of = [&](int q) { return (char *)sm + ((unsigned)(q - pl_lo) % (unsigned)R) * lay.slot_bytes; };
-    // coarse cells of the slab: rows y0/2 .. (y0+rows-1)/2, all coarse z
-    const int cy0 = y0 >> 1, crows = ((y0 + rows - 1) >> 1) - cy0 + 1;
-    const int ncc = crows * Lc.nz;
-
+    auto slot_of = [&](int g) { return (char *)sm + ((unsigned)g % (unsigned)R) * lay.slot_bytes; };
     if (t == 0) {
         for (int s = 0; s < R; s++) {
             mbar_init(&full[s], 1);
@@ -514,126 +531,164 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
         fence_mbarrier_init();
     }
     __syncthreads();
+    int g0 = 0, issued = 0;
+    for (int w = work.first[blockIdx.x]; w < work.first[blockIdx.x + 1]; w++) {
+        const int4 it = work.items[w];
+        const int p = it.x, y0 = it.y, xa = it.z, xe = it.w;
+        if (st && !st[p].active) continue;  // uniform over the block
+        const LevelDesc L = desc[p];
+        const LevelDesc Lc = cdesc[p];
+        const int nz = L.nz, ny = L.ny, nx = L.nx;
+        const long long sx = (long long)ny * nz;
+        const int Ty = plane_rows(ny, nz, CPT * kPlaneThreads);
+        const int rows = min(Ty, ny - y0);
+        const int ncell = rows * nz;
+        const int pl_lo = max(xa - 1, 0), pl_hi = min(xe, nx - 1);
+        const int h0 = max(y0 - 1, 0), h1 = min(y0 + rows + 1, ny);
+        auto gof = [&](int q) { return g0 + (q - pl_lo); };
+        // coarse cells of the slab: rows y0/2 .. (y0+rows-1)/2, all coarse z
+        const int cy0 = y0 >> 1, crows = ((y0 + rows - 1) >> 1) - cy0 + 1;
+        const int ncc = crows * Lc.nz;
+        bool bad = false;
 
-    if (warp == kConsumerWarps) {
-        if (lane == 0) {
-            pm_produce<R>(pl_lo, pl_hi, full, empty, sm, lay.slot_bytes, err, [&](int q, char *slot, uint64_t *bar) {
-                const long long pb = L.off + (long long)q * sx;
-                const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
-                const long long hA = pb + (long long)h0 * nz, hB = pb + (long long)h1 * nz, pE = lp + ncell;
-                auto stage = [&](const void *base, int esz, long long l0, long long a0, long long a1, int off) {
-                    stage_range(bar, base, esz, l0, a0, a1, slot + off, L.off, L.off + L.n, slot, lay.slot_bytes);
-                };
-                stage(xin, es, lh, hA, hB, lay.oX);
-                stage(b, es, lp, lp, pE, lay.oB);
-                stage(C.cx, ec, lp, lp, pE, lay.oCX);
-                stage(C.cy, ec, lh, hA, pE, lay.oCY);
-                stage(C.cz, ec, lp, lp, pE, lay.oCZ);
-                stage(C.leak, ec, lp, lp, pE, lay.oLK);
-            });
-        }
-        __syncwarp();
-        return;
-    }
-    // ---------------- consumers
-    unsigned cfl[CPT];
-#pragma unroll
-    for (int k = 0; k < CPT; k++) {
-        const int tc = t + k * kPlaneThreads;
-        unsigned f = 0;
-        if (tc < ncell) {
-            const int ty = div_nz(L, tc), z = tc - ty * nz, y = y0 + ty;
-            f = CF_VALID | (z + 1 < nz ? CF_ZP : 0u) | (z > 0 ? CF_ZM : 0u) | (y + 1 < ny ? CF_YP : 0u) |
-                (y > 0 ? CF_YM : 0u);
-        }
-        cfl[k] = f;
-    }
-    int waited = pl_lo - 1;
-    bool bad = false;
-    for (int x = xa; x < xe; x++) {
-        const int need = min(x + 1, pl_hi);
-        while (!bad && waited < need) {
-            const int u = waited + 1 - pl_lo;
-            if (!mbar_wait(&full[u % R], (uint32_t)((u / R) & 1), err)) bad = true;
-            else waited++;
-        }
-        if (!bad) {
-            const long long pb = L.off + (long long)x * sx;
-            const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
-            const int dh = stage_delta(lh, es), dp = stage_delta(lp, es);
-            char *sc = slot_of(x);
-            const bool xp = x + 1 < nx, xm = x > 0;
-            char *sn = xp ? slot_of(x + 1) : sc;
-            char *sq = xm ? slot_of(x - 1) : sc;
-            const int dn_ = xp ? stage_delta(lh + sx, es) : dh;
-            const int dq = xm ? stage_delta(lh - sx, es) : dh;
-            const int dqp = xm ? stage_delta(lp - sx, es) : dp;
-            const T *X = (const T *)(sc + lay.oX) + dh;
-            const T *B = (const T *)(sc + lay.oB) + dp;
-            const int ch = stage_delta(lh, ec), cp = stage_delta(lp, ec);
-            const int cqp = xm ? stage_delta(lp - sx, ec) : cp;
-            const CT *CX = (const CT *)(sc + lay.oCX) + cp;
-            const CT *CXq = (const CT *)(sq + lay.oCX) + cqp;
-            const CT *CY = (const CT *)(sc + lay.oCY) + ch;
-            const CT *CZ = (const CT *)(sc + lay.oCZ) + cp;
-            const CT *LK = (const CT *)(sc + lay.oLK) + cp;
-            const T *Xn = (const T *)(sn + lay.oX) + dn_;
-            const T *Xq = (const T *)(sq + lay.oX) + dq;
-            T *rs = res[x & 1];
+        if (warp == kConsumerWarps) {
+            if (lane == 0) {
+                const int n = pm_produce<R>(pl_lo, pl_hi, g0, full, empty, sm, lay.slot_bytes, err,
+                                            [&](int q, char *slot, uint64_t *bar) {
+                    const long long pb = L.off + (long long)q * sx;
+                    const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
+                    const long long hA = pb + (long long)h0 * nz, hB = pb + (long long)h1 * nz, pE = lp + ncell;
+                    auto stage = [&](const void *base, int esz, long long l0, long long a0, long long a1, int off) {
+                        stage_range(bar, base, esz, l0, a0, a1, slot + off, L.off, L.off + L.n, slot, lay.slot_bytes);
+                    };
+                    stage(xin, es, lh, hA, hB, lay.oX);
+                    stage(b, es, lp, lp, pE, lay.oB);
+                    stage(C.cx, ec, lp, lp, pE, lay.oCX);
+                    stage(C.cy, ec, lh, hA, pE, lay.oCY);
+                    stage(C.cz, ec, lp, lp, pE, lay.oCZ);
+                    stage(C.leak, ec, lp, lp, pE, lay.oLK);
+                });
+                issued += n;
+                bad = n != pl_hi - pl_lo + 1;
+            }
+            __syncwarp();
+        } else {
+            // ---------------- consumers
+            unsigned cfl[CPT];
 #pragma unroll
             for (int k = 0; k < CPT; k++) {
-                const unsigned f = cfl[k];
-                if (!(f & CF_VALID)) continue;
                 const int tc = t + k * kPlaneThreads;
-                const int c = nz + tc;
-                const T xi = X[c];
-                T a = cf(LK[tc]) * xi;
-                if (f & CF_ZP) a += cf(CZ[tc]) * (xi - X[c + 1]);
-                if (f & CF_ZM) a += cf(CZ[tc - 1]) * (xi - X[c - 1]);
-                if (f & CF_YP) a += cf(CY[c]) * (xi - X[c + nz]);
-                if (f & CF_YM) a += cf(CY[tc]) * (xi - X[c - nz]);
-                if (xp) a += cf(CX[tc]) * (xi - Xn[c]);
-                if (xm) a += cf(CXq[tc]) * (xi - Xq[c]);
-                rs[tc] = B[tc] - a;
+                unsigned f = 0;
+                if (tc < ncell) {
+                    const int ty = div_nz(L, tc), z = tc - ty * nz, y = y0 + ty;
+                    f = CF_VALID | (z + 1 < nz ? CF_ZP : 0u) | (z > 0 ? CF_ZM : 0u) | (y + 1 < ny ? CF_YP : 0u) |
+                        (y > 0 ? CF_YM : 0u);
+                }
+                cfl[k] = f;
             }
-        }
-        // planes x-1 is no longer needed by this warp
-        __syncwarp();
-        if (lane == 0 && x - 1 >= pl_lo) mbar_arrive(&empty[(x - 1 - pl_lo) % R]);
-        const bool pair_done = (x & 1) || x + 1 == nx;
-        if (!pair_done) continue;
-        if (consumer_sync_or(bad, kPlaneThreads)) break;  // residuals of the pair are in res[]
-        const int X0 = x & ~1;
-        const int cx = X0 >> 1;
-        const bool two = X0 + 1 < nx;
-        const long long cb = Lc.off + (long long)cx * Lc.ny * Lc.nz + (long long)cy0 * Lc.nz;
-        for (int tcc = t; tcc < ncc; tcc += kPlaneThreads) {
-            const int cr = div_nz(Lc, tcc), czz = tcc - cr * Lc.nz;
-            const int fy0 = 2 * (cy0 + cr) - y0, fz0 = 2 * czz;
-            const bool y2 = 2 * (cy0 + cr) + 1 < ny, z2 = fz0 + 1 < nz;
-            T acc = 0;
-            for (int ix = 0; ix < (two ? 2 : 1); ix++) {
-                const T *r = res[(X0 + ix) & 1];
-                acc += r[fy0 * nz + fz0];
-                if (z2) acc += r[fy0 * nz + fz0 + 1];
-                if (y2) {
-                    acc += r[(fy0 + 1) * nz + fz0];
-                    if (z2) acc += r[(fy0 + 1) * nz + fz0 + 1];
+            int waited = pl_lo - 1, released = pl_lo;
+            for (int x = xa; x < xe; x++) {
+                const int need = min(x + 1, pl_hi);
+                while (!bad && waited < need) {
+                    const int g = gof(waited + 1);
+                    if (!mbar_wait(&full[g % R], (uint32_t)((g / R) & 1), err)) bad = true;
+                    else waited++;
+                }
+                if (!bad) {
+                    const long long pb = L.off + (long long)x * sx;
+                    const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
+                    const int dh = stage_delta(lh, es), dp = stage_delta(lp, es);
+                    char *sc = slot_of(gof(x));
+                    const bool xp = x + 1 < nx, xm = x > 0;
+                    char *sn = xp ? slot_of(gof(x + 1)) : sc;
+                    char *sq = xm ? slot_of(gof(x - 1)) : sc;
+                    const int dn_ = xp ? stage_delta(lh + sx, es) : dh;
+                    const int dq = xm ? stage_delta(lh - sx, es) : dh;
+                    const T *X = (const T *)(sc + lay.oX) + dh;
+                    const T *B = (const T *)(sc + lay.oB) + dp;
+                    const int ch = stage_delta(lh, ec), cp = stage_delta(lp, ec);
+                    const int cqp = xm ? stage_delta(lp - sx, ec) : cp;
+                    const CT *CX = (const CT *)(sc + lay.oCX) + cp;
+                    const CT *CXq = (const CT *)(sq + lay.oCX) + cqp;
+                    const CT *CY = (const CT *)(sc + lay.oCY) + ch;
+                    const CT *CZ = (const CT *)(sc + lay.oCZ) + cp;
+                    const CT *LK = (const CT *)(sc + lay.oLK) + cp;
+                    const T *Xn = (const T *)(sn + lay.oX) + dn_;
+                    const T *Xq = (const T *)(sq + lay.oX) + dq;
+                    T *rsd = res[x & 1];
+#pragma unroll
+                    for (int k = 0; k < CPT; k++) {
+                        const unsigned f = cfl[k];
+                        if (!(f & CF_VALID)) continue;
+                        const int tc = t + k * kPlaneThreads;
+                        const int c = nz + tc;
+                        const T xi = X[c];
+                        T a = cf(LK[tc]) * xi;
+                        if (f & CF_ZP) a += cf(CZ[tc]) * (xi - X[c + 1]);
+                        if (f & CF_ZM) a += cf(CZ[tc - 1]) * (xi - X[c - 1]);
+                        if (f & CF_YP) a += cf(CY[c]) * (xi - X[c + nz]);
+                        if (f & CF_YM) a += cf(CY[tc]) * (xi - X[c - nz]);
+                        if (xp) a += cf(CX[tc]) * (xi - Xn[c]);
+                        if (xm) a += cf(CXq[tc]) * (xi - Xq[c]);
+                        rsd[tc] = B[tc] - a;
+                    }
+                }
+                // plane x-1 is no longer needed by this warp
+                __syncwarp();
+                if (!bad && lane == 0 && x - 1 >= released) mbar_arrive(&empty[gof(x - 1) % R]);
+                released = max(released, x);
+                const bool pair_done = (x & 1) || x + 1 == nx;
+                if (!pair_done) continue;
+                if (consumer_sync_or(bad, kPlaneThreads)) {  // residuals of the pair are in res[]
+                    bad = true;
+                    break;
+                }
+                const int X0 = x & ~1;
+                const int cx = X0 >> 1;
+                const bool two = X0 + 1 < nx;
+                const long long cb = Lc.off + (long long)cx * Lc.ny * Lc.nz + (long long)cy0 * Lc.nz;
+                for (int tcc = t; tcc < ncc; tcc += kPlaneThreads) {
+                    const int cr = div_nz(Lc, tcc), czz = tcc - cr * Lc.nz;
+                    const int fy0 = 2 * (cy0 + cr) - y0, fz0 = 2 * czz;
+                    const bool y2 = 2 * (cy0 + cr) + 1 < ny, z2 = fz0 + 1 < nz;
+                    T acc = 0;
+                    for (int ix = 0; ix < (two ? 2 : 1); ix++) {
+                        const T *r = res[(X0 + ix) & 1];
+                        acc += r[fy0 * nz + fz0];
+                        if (z2) acc += r[fy0 * nz + fz0 + 1];
+                        if (y2) {
+                            acc += r[(fy0 + 1) * nz + fz0];
+                            if (z2) acc += r[(fy0 + 1) * nz + fz0 + 1];
+                        }
+                    }
+                    bc[cb + tcc] = acc;
+                }
+                if (consumer_sync_or(bad, kPlaneThreads)) {  // res[] may be overwritten
+                    bad = true;
+                    break;
                 }
             }
-            bc[cb + tcc] = acc;
+            // the item's remaining planes go back to the producer
+            if (!bad) {
+                __syncwarp();
+                for (int q = released; q <= waited; q++)
+                    if (lane == 0) mbar_arrive(&empty[gof(q) % R]);
+            }
         }
-        if (consumer_sync_or(bad, kPlaneThreads)) break;  // res[] may be overwritten
+        g0 += pl_hi - pl_lo + 1;
+        if (__syncthreads_or(bad)) break;  // every thread leaves together after an expired wait
     }
+    if (warp == kConsumerWarps && lane == 0) pm_drain<R>(issued, full, err);
 }
 
 // Double-float CG product q = A p (flux form, double-float coefficients) and the problem's
 // p . q (leading floats) on the plane ring; the arithmetic and its order are those of the
 // grid-stride k_df_spmv_pq. Streams per plane: p with halo rows, cx, cy (+ the row
-// below), cz, leak, all 8-byte double-float values.
+// below), cz, leak, all 8-byte double-float values. A block marches through its items like
+// k_pm_cheb; each item's partial of p . q has its own reduction slot.
 template <int CPT>
 __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_df_spmv(
-    const LevelDesc *__restrict__ desc, const int4 *__restrict__ items, CgState *st, int *active_count,
+    const LevelDesc *__restrict__ desc, PlaneWork work, CgState *st, int *active_count,
     ReduceScratch rs, const int2 *__restrict__ pinfo, CoeffsDF C, const float2 *__restrict__ pv,
     float2 *__restrict__ qv, PlaneLayout lay, int *err) {
     pdl_enter();
@@ -643,21 +698,9 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_df_spmv(
     extern __shared__ __align__(128) unsigned char sm[];
     __shared__ uint64_t full[R], empty[R];
 
-    const int4 it = items[blockIdx.x];
-    const int p = it.x, y0 = it.y, xa = it.z, xe = it.w;
-    if (!st[p].active) return;
-    const LevelDesc L = desc[p];
-    const int nz = L.nz, ny = L.ny, nx = L.nx;
-    const long long sx = (long long)ny * nz;
-    const int Ty = plane_rows(ny, nz, CPT * kPlaneThreads);
-    const int rows = min(Ty, ny - y0);
-    const int ncell = rows * nz;
     const int t = threadIdx.x;
     const int warp = t >> 5, lane = t & 31;
-    const int pl_lo = max(xa - 1, 0), pl_hi = min(xe, nx - 1);
-    const int h0 = max(y0 - 1, 0), h1 = min(y0 + rows + 1, ny);
-    auto slot_of = [&](int q) { return (char *)sm + ((unsigned)(q - pl_lo) % (unsigned)R) * lay.slot_bytes; };
-
+    auto slot_of = [&](int g) { return (char *)sm + ((unsigned)g % (unsigned)R) * lay.slot_bytes; };
     if (t == 0) {
         for (int s = 0; s < R; s++) {
             mbar_init(&full[s], 1);
@@ -666,90 +709,117 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_df_spmv(
         fence_mbarrier_init();
     }
     __syncthreads();
-    Acc<float> part;
+    int g0 = 0, issued = 0;
+    for (int w = work.first[blockIdx.x]; w < work.first[blockIdx.x + 1]; w++) {
+        const int4 it = work.items[w];
+        const int p = it.x, y0 = it.y, xa = it.z, xe = it.w;
+        if (!st[p].active) continue;  // uniform over the block
+        const LevelDesc L = desc[p];
+        const int nz = L.nz, ny = L.ny, nx = L.nx;
+        const long long sx = (long long)ny * nz;
+        const int Ty = plane_rows(ny, nz, CPT * kPlaneThreads);
+        const int rows = min(Ty, ny - y0);
+        const int ncell = rows * nz;
+        const int pl_lo = max(xa - 1, 0), pl_hi = min(xe, nx - 1);
+        const int h0 = max(y0 - 1, 0), h1 = min(y0 + rows + 1, ny);
+        auto gof = [&](int q) { return g0 + (q - pl_lo); };
+        Acc<float> part;
+        bool bad = false;
 
-    if (warp == kConsumerWarps) {
-        if (lane == 0) {
-            pm_produce<R>(pl_lo, pl_hi, full, empty, sm, lay.slot_bytes, err, [&](int q, char *slot, uint64_t *bar) {
-                const long long pb = L.off + (long long)q * sx;
-                const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
-                const long long hA = pb + (long long)h0 * nz, hB = pb + (long long)h1 * nz, pE = lp + ncell;
-                auto stage = [&](const void *base, long long l0, long long a0, long long a1, int off) {
-                    stage_range(bar, base, es, l0, a0, a1, slot + off, L.off, L.off + L.n, slot, lay.slot_bytes);
-                };
-                stage(pv, lh, hA, hB, lay.oX);
-                stage(C.cx, lp, lp, pE, lay.oCX);
-                stage(C.cy, lh, hA, pE, lay.oCY);
-                stage(C.cz, lp, lp, pE, lay.oCZ);
-                stage(C.leak, lp, lp, pE, lay.oLK);
-            });
-        }
-        __syncwarp();
-    } else {
-        unsigned cfl[CPT];
-#pragma unroll
-        for (int k = 0; k < CPT; k++) {
-            const int tc = t + k * kPlaneThreads;
-            unsigned f = 0;
-            if (tc < ncell) {
-                const int ty = div_nz(L, tc), z = tc - ty * nz, y = y0 + ty;
-                f = CF_VALID | (z + 1 < nz ? CF_ZP : 0u) | (z > 0 ? CF_ZM : 0u) | (y + 1 < ny ? CF_YP : 0u) |
-                    (y > 0 ? CF_YM : 0u);
-            }
-            cfl[k] = f;
-        }
-        int waited = pl_lo - 1;
-        bool ok = true;
-        for (int x = xa; x < xe && ok; x++) {
-            const int need = min(x + 1, pl_hi);
-            while (waited < need) {
-                const int u = waited + 1 - pl_lo;
-                if (!mbar_wait(&full[u % R], (uint32_t)((u / R) & 1), err)) {
-                    ok = false;
-                    break;
-                }
-                waited++;
-            }
-            if (!ok) break;
-            const long long pb = L.off + (long long)x * sx;
-            const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
-            const int dh = stage_delta(lh, es), dp = stage_delta(lp, es);
-            char *sc = slot_of(x);
-            const bool xp = x + 1 < nx, xm = x > 0;
-            char *sn = xp ? slot_of(x + 1) : sc;
-            char *sq = xm ? slot_of(x - 1) : sc;
-            const float2 *P = (const float2 *)(sc + lay.oX) + dh;
-            const float2 *CX = (const float2 *)(sc + lay.oCX) + dp;
-            const float2 *CY = (const float2 *)(sc + lay.oCY) + dh;
-            const float2 *CZ = (const float2 *)(sc + lay.oCZ) + dp;
-            const float2 *LK = (const float2 *)(sc + lay.oLK) + dp;
-            const float2 *Pn = (const float2 *)(sn + lay.oX) + (xp ? stage_delta(lh + sx, es) : dh);
-            const float2 *Pq = (const float2 *)(sq + lay.oX) + (xm ? stage_delta(lh - sx, es) : dh);
-            const float2 *CXq = (const float2 *)(sq + lay.oCX) + (xm ? stage_delta(lp - sx, es) : dp);
-#pragma unroll
-            for (int k = 0; k < CPT; k++) {
-                const unsigned f = cfl[k];
-                if (!(f & CF_VALID)) continue;
-                const int tc = t + k * kPlaneThreads;
-                const int c = nz + tc;
-                const float2 pi = P[c];
-                float2 a = df_mul(LK[tc], pi);
-                if (f & CF_ZP) a = df_add(a, df_mul(CZ[tc], df_sub(pi, P[c + 1])));
-                if (f & CF_ZM) a = df_add(a, df_mul(CZ[tc - 1], df_sub(pi, P[c - 1])));
-                if (f & CF_YP) a = df_add(a, df_mul(CY[c], df_sub(pi, P[c + nz])));
-                if (f & CF_YM) a = df_add(a, df_mul(CY[tc], df_sub(pi, P[c - nz])));
-                if (xp) a = df_add(a, df_mul(CX[tc], df_sub(pi, Pn[c])));
-                if (xm) a = df_add(a, df_mul(CXq[tc], df_sub(pi, Pq[c])));
-                qv[lp + tc] = a;
-                part = part + Acc<float>::prod(pi.x, a.x);
+        if (warp == kConsumerWarps) {
+            if (lane == 0) {
+                const int n = pm_produce<R>(pl_lo, pl_hi, g0, full, empty, sm, lay.slot_bytes, err,
+                                            [&](int q, char *slot, uint64_t *bar) {
+                    const long long pb = L.off + (long long)q * sx;
+                    const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
+                    const long long hA = pb + (long long)h0 * nz, hB = pb + (long long)h1 * nz, pE = lp + ncell;
+                    auto stage = [&](const void *base, long long l0, long long a0, long long a1, int off) {
+                        stage_range(bar, base, es, l0, a0, a1, slot + off, L.off, L.off + L.n, slot, lay.slot_bytes);
+                    };
+                    stage(pv, lh, hA, hB, lay.oX);
+                    stage(C.cx, lp, lp, pE, lay.oCX);
+                    stage(C.cy, lh, hA, pE, lay.oCY);
+                    stage(C.cz, lp, lp, pE, lay.oCZ);
+                    stage(C.leak, lp, lp, pE, lay.oLK);
+                });
+                issued += n;
+                bad = n != pl_hi - pl_lo + 1;
             }
             __syncwarp();
-            if (lane == 0 && x - 1 >= pl_lo) mbar_arrive(&empty[(x - 1 - pl_lo) % R]);
+        } else {
+            unsigned cfl[CPT];
+#pragma unroll
+            for (int k = 0; k < CPT; k++) {
+                const int tc = t + k * kPlaneThreads;
+                unsigned f = 0;
+                if (tc < ncell) {
+                    const int ty = div_nz(L, tc), z = tc - ty * nz, y = y0 + ty;
+                    f = CF_VALID | (z + 1 < nz ? CF_ZP : 0u) | (z > 0 ? CF_ZM : 0u) | (y + 1 < ny ? CF_YP : 0u) |
+                        (y > 0 ? CF_YM : 0u);
+                }
+                cfl[k] = f;
+            }
+            int waited = pl_lo - 1, released = pl_lo;
+            for (int x = xa; x < xe && !bad; x++) {
+                const int need = min(x + 1, pl_hi);
+                while (waited < need) {
+                    const int g = gof(waited + 1);
+                    if (!mbar_wait(&full[g % R], (uint32_t)((g / R) & 1), err)) {
+                        bad = true;
+                        break;
+                    }
+                    waited++;
+                }
+                if (bad) break;
+                const long long pb = L.off + (long long)x * sx;
+                const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
+                const int dh = stage_delta(lh, es), dp = stage_delta(lp, es);
+                char *sc = slot_of(gof(x));
+                const bool xp = x + 1 < nx, xm = x > 0;
+                char *sn = xp ? slot_of(gof(x + 1)) : sc;
+                char *sq = xm ? slot_of(gof(x - 1)) : sc;
+                const float2 *P = (const float2 *)(sc + lay.oX) + dh;
+                const float2 *CX = (const float2 *)(sc + lay.oCX) + dp;
+                const float2 *CY = (const float2 *)(sc + lay.oCY) + dh;
+                const float2 *CZ = (const float2 *)(sc + lay.oCZ) + dp;
+                const float2 *LK = (const float2 *)(sc + lay.oLK) + dp;
+                const float2 *Pn = (const float2 *)(sn + lay.oX) + (xp ? stage_delta(lh + sx, es) : dh);
+                const float2 *Pq = (const float2 *)(sq + lay.oX) + (xm ? stage_delta(lh - sx, es) : dh);
+                const float2 *CXq = (const float2 *)(sq + lay.oCX) + (xm ? stage_delta(lp - sx, es) : dp);
+#pragma unroll
+                for (int k = 0; k < CPT; k++) {
+                    const unsigned f = cfl[k];
+                    if (!(f & CF_VALID)) continue;
+                    const int tc = t + k * kPlaneThreads;
+                    const int c = nz + tc;
+                    const float2 pi = P[c];
+                    float2 a = df_mul(LK[tc], pi);
+                    if (f & CF_ZP) a = df_add(a, df_mul(CZ[tc], df_sub(pi, P[c + 1])));
+                    if (f & CF_ZM) a = df_add(a, df_mul(CZ[tc - 1], df_sub(pi, P[c - 1])));
+                    if (f & CF_YP) a = df_add(a, df_mul(CY[c], df_sub(pi, P[c + nz])));
+                    if (f & CF_YM) a = df_add(a, df_mul(CY[tc], df_sub(pi, P[c - nz])));
+                    if (xp) a = df_add(a, df_mul(CX[tc], df_sub(pi, Pn[c])));
+                    if (xm) a = df_add(a, df_mul(CXq[tc], df_sub(pi, Pq[c])));
+                    qv[lp + tc] = a;
+                    part = part + Acc<float>::prod(pi.x, a.x);
+                }
+                __syncwarp();
+                if (lane == 0 && x - 1 >= released) mbar_arrive(&empty[gof(x - 1) % R]);
+                released = max(released, x);
+            }
+            if (!bad) {
+                __syncwarp();
+                for (int q = released; q <= waited; q++)
+                    if (lane == 0) mbar_arrive(&empty[gof(q) % R]);
+            }
         }
+        g0 += pl_hi - pl_lo + 1;
+        double2 tot;
+        if (reduce_last_slot<float>(part, rs, pinfo[p], p, w, tot) && threadIdx.x == 0)
+            finish_pq(st[p], tot.x, active_count);
+        if (__syncthreads_or(bad)) break;  // every thread leaves together after an expired wait
     }
-    double2 tot;
-    if (reduce_last<float>(part, Acc<float>(), rs, pinfo[p], p, tot) && threadIdx.x == 0)
-        finish_pq(st[p], tot.x, active_count);
+    if (warp == kConsumerWarps && lane == 0) pm_drain<R>(issued, full, err);
 }
 
 }  // namespace dpf

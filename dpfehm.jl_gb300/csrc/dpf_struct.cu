@@ -1246,9 +1246,14 @@ static BlockMap build_map(const std::vector<LevelDesc> &desc, const std::vector<
     return m;
 }
 
-// Plane-marching work items of a level: per smoothed problem, slabs of Ty = 256 / nz rows
-// (whole rows, so a slab is contiguous in every array) times chunks of x-planes, with the
-// chunk length chosen so that all items fill the device about once.
+// Plane-marching work of a level. Per smoothed problem the grid is cut into slabs of whole
+// rows (plane_rows: up to `cells` cells, so a slab is contiguous in every array), and the
+// planes of all slabs of all problems form one sequence of plane pairs (the restriction sums
+// pairs of planes) weighted by their cells. The sequence is cut into contiguous runs of about
+// equal weight, one per block (SMs x blocks_per_sm blocks, fewer on small levels), so
+// every block of a launch gets the same work whatever the batch's sizes; a run that crosses a
+// slab boundary becomes several items, which the block marches through one after another.
+// Items start on even planes and end on one, or on the grid's last plane.
 void StructBatch::build_plane_items(PlaneItems &P, const Level &L, const std::vector<int> &take, int sms,
                                     int cells, int blocks_per_sm,
                                     const std::vector<std::vector<std::array<int, 3>>> *shapes, int l) {
@@ -1265,23 +1270,23 @@ void StructBatch::build_plane_items(PlaneItems &P, const Level &L, const std::ve
         total += D.n;
     }
     if (total == 0) return;
-    const long long target = (long long)sms * std::max(1, blocks_per_sm);
-    std::vector<int4> items;
-    std::vector<int2> pinfo(nprob, make_int2(0, 0));
+    // the units: plane pairs of every slab, in problem, slab, plane order
+    struct Unit {
+        int p, y0, x0, x1;
+        long long w;
+    };
+    std::vector<Unit> units;
     for (int p = 0; p < nprob; p++) {
         if (!take[p]) continue;
         const LevelDesc &D = L.h_desc[p];
         const int Ty = plane_rows(D.ny, D.nz, cells);
-        const int ytiles = (D.ny + Ty - 1) / Ty;
-        long long chunks = (long long)((double)target * (double)D.n / (double)total / ytiles);
-        chunks = std::max(1LL, std::min(chunks, (long long)D.nx));
-        int xc = (int)((D.nx + chunks - 1) / chunks);
-        xc = std::max(xc, std::min(2, D.nx));
-        xc += xc & 1;  // chunks start on even planes (restriction pairs planes)
-        pinfo[p].x = (int)items.size();
-        for (int y0 = 0; y0 < D.ny; y0 += Ty)
-            for (int x0 = 0; x0 < D.nx; x0 += xc) items.push_back(make_int4(p, y0, x0, std::min(x0 + xc, D.nx)));
-        pinfo[p].y = (int)items.size() - pinfo[p].x;
+        for (int y0 = 0; y0 < D.ny; y0 += Ty) {
+            const long long rc = (long long)std::min(Ty, D.ny - y0) * D.nz;
+            for (int x0 = 0; x0 < D.nx; x0 += 2) {
+                const int x1 = std::min(x0 + 2, D.nx);
+                units.push_back(Unit{p, y0, x0, x1, rc * (x1 - x0)});
+            }
+        }
         P.halo = std::max(P.halo, (Ty + 2) * D.nz);
         P.cy = std::max(P.cy, (Ty + 1) * D.nz);
         P.slab = std::max(P.slab, Ty * D.nz);
@@ -1290,10 +1295,50 @@ void StructBatch::build_plane_items(PlaneItems &P, const Level &L, const std::ve
             P.coarse = std::max(P.coarse, ((Ty + 2) / 2 + 2) * cnz);
         }
     }
+    // on the finest level at least 4 plane pairs per block where the level allows: every run also
+    // stages the plane on each side of it, which for shorter runs costs more bandwidth than the
+    // parallelism gains; the coarser levels are latency-bound and take as many blocks as they can
+    const long long target = (long long)sms * std::max(1, blocks_per_sm);
+    const long long min_pairs = l == 0 ? 4 : 1;
+    const int nb = (int)std::max(1LL, std::min<long long>(target, ((long long)units.size() + min_pairs - 1) / min_pairs));
+    std::vector<int4> items;
+    std::vector<int> first(nb + 1, 0);
+    std::vector<int2> pinfo(nprob, make_int2(0, 0));
+    long long acc = 0;
+    size_t u = 0;
+    for (int blk = 0; blk < nb; blk++) {
+        first[blk] = (int)items.size();
+        // units up to the block's share of the cumulative weight (at least one; the last block
+        // takes what is left)
+        const long long end = blk + 1 == nb ? -1 : (long long)((double)total * (blk + 1) / nb + 0.5);
+        bool took = false;
+        while (u < units.size() && (!took || end < 0 || acc + units[u].w / 2 <= end) &&
+               (units.size() - u) > (size_t)(nb - 1 - blk)) {
+            const Unit &U = units[u];
+            if (!items.empty() && (int)items.size() > first[blk] && items.back().x == U.p && items.back().y == U.y0 &&
+                items.back().w == U.x0)
+                items.back().w = U.x1;  // extend the block's current item
+            else
+                items.push_back(make_int4(U.p, U.y0, U.x0, U.x1));
+            acc += U.w;
+            took = true;
+            u++;
+        }
+    }
+    first[nb] = (int)items.size();
+    if (u != units.size()) throw std::logic_error("plane work partition left units unassigned");
+    for (int w = 0; w < (int)items.size(); w++) {
+        const int p = items[w].x;
+        if (pinfo[p].y == 0) pinfo[p].x = w;
+        pinfo[p].y++;
+    }
     P.n = (int)items.size();
+    P.nb = nb;
     P.items = dalloc<int4>(items.size(), owned);
+    P.first = dalloc<int>(first.size(), owned);
     P.pinfo = dalloc<int2>(nprob, owned);
     CK(cudaMemcpy(P.items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(P.first, first.data(), first.size() * sizeof(int), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(P.pinfo, pinfo.data(), nprob * sizeof(int2), cudaMemcpyHostToDevice));
     P.ok = true;
 }
@@ -1733,7 +1778,7 @@ static void configure_kernels() {
 
 template <typename T, int MODE, int CPT>
 static void pm_kernel(unsigned nblocks, size_t smem, cudaStream_t stream, const LevelDesc *desc,
-                      const LevelDesc *cdesc, const int4 *items, CgState *st, Coeffs<T> C, const T *b,
+                      const LevelDesc *cdesc, PlaneWork items, CgState *st, Coeffs<T> C, const T *b,
                       const T *xin, T *xout, T *d, const uint8_t *dir, const T *e, T c1, T c2, T invth, T sc,
                       PlaneLayout lay, ReduceScratch rs, const int2 *pinfo, int *err) {
     launch_pdl(k_pm_cheb<T, MODE, CPT>, nblocks, kPlaneThreads + 32, smem, stream, desc, cdesc, items, st, C, b, xin, xout, d,
@@ -1742,7 +1787,7 @@ static void pm_kernel(unsigned nblocks, size_t smem, cudaStream_t stream, const 
 
 template <typename T, int MODE>
 static void pm_kernel_cpt(int cpt, unsigned nblocks, size_t smem, cudaStream_t stream, const LevelDesc *desc,
-                          const LevelDesc *cdesc, const int4 *items, CgState *st, Coeffs<T> C, const T *b,
+                          const LevelDesc *cdesc, PlaneWork items, CgState *st, Coeffs<T> C, const T *b,
                           const T *xin, T *xout, T *d, const uint8_t *dir, const T *e, T c1, T c2, T invth, T sc,
                           PlaneLayout lay, ReduceScratch rs, const int2 *pinfo, int *err) {
 #define DPF_PM_CPT(N)                                                                                              \
@@ -1790,11 +1835,12 @@ void StructBatch::pm_launch(int mode, int l, const T *b, const T *xin, T *xout, 
     const size_t smem = (size_t)kPlaneStages * lay.slot_bytes;
     Coeffs<T> C = coeffs_of<T>(L, mixed);
     const LevelDesc *cd = l + 1 < nlev_max ? lv[l + 1].d_desc : nullptr;
-    const unsigned nb = (unsigned)L.pm.n;
+    const unsigned nb = (unsigned)L.pm.nb;
+    const PlaneWork wk{L.pm.items, L.pm.first};
     int *err = d_factor_status + 1;
 #define DPF_PM_CASE(M)                                                                                           \
     case M:                                                                                                      \
-        pm_kernel_cpt<T, M>(cpt, nb, smem, stream, L.d_desc, cd, L.pm.items, d_state, C, b, xin, xout, d, L.dir, e, \
+        pm_kernel_cpt<T, M>(cpt, nb, smem, stream, L.d_desc, cd, wk, d_state, C, b, xin, xout, d, L.dir, e, \
                             c1, c2, invth, sc, lay, rs, L.pm.pinfo, err);                                         \
         break;
     switch (mode) {
@@ -1816,7 +1862,7 @@ void StructBatch::pm_launch(int mode, int l, const T *b, const T *xin, T *xout, 
 // Plane-marching restriction of level l's residual into level l+1 (the smoothed problems).
 template <typename T, int CPT>
 static void pm_restrict_kernel(unsigned nblocks, size_t smem, cudaStream_t stream, const LevelDesc *desc,
-                               const LevelDesc *cdesc, const int4 *items, const CgState *st, Coeffs<T> C, const T *b,
+                               const LevelDesc *cdesc, PlaneWork items, const CgState *st, Coeffs<T> C, const T *b,
                                const T *x, T *bc, PlaneLayout lay, int *err) {
     launch_pdl(k_pm_restrict<T, CPT>, nblocks, kPlaneThreads + 32, smem, stream, desc, cdesc, items, st, C, b, x, bc, lay, err);
 }
@@ -1841,13 +1887,14 @@ void StructBatch::pm_restrict(int l, const T *b, const T *x, T *bc) {
     lay.oD = lay.oG = lay.oDIR = lay.oE = -1;
     lay.slot_bytes = (off + 127) & ~127;
     const size_t smem = (size_t)kPlaneStages * lay.slot_bytes;
-    const unsigned nb = (unsigned)L.pm.n;
+    const unsigned nb = (unsigned)L.pm.nb;
+    const PlaneWork wk{L.pm.items, L.pm.first};
     const Coeffs<T> C = coeffs_of<T>(L, mixed);
     switch (L.pm.cells / kPlaneThreads) {
-        case 1: pm_restrict_kernel<T, 1>(nb, smem, stream, L.d_desc, lv[l + 1].d_desc, L.pm.items, d_state, C, b, x, bc, lay, d_factor_status + 1); break;
-        case 2: pm_restrict_kernel<T, 2>(nb, smem, stream, L.d_desc, lv[l + 1].d_desc, L.pm.items, d_state, C, b, x, bc, lay, d_factor_status + 1); break;
-        case 3: pm_restrict_kernel<T, 3>(nb, smem, stream, L.d_desc, lv[l + 1].d_desc, L.pm.items, d_state, C, b, x, bc, lay, d_factor_status + 1); break;
-        case 4: pm_restrict_kernel<T, 4>(nb, smem, stream, L.d_desc, lv[l + 1].d_desc, L.pm.items, d_state, C, b, x, bc, lay, d_factor_status + 1); break;
+        case 1: pm_restrict_kernel<T, 1>(nb, smem, stream, L.d_desc, lv[l + 1].d_desc, wk, d_state, C, b, x, bc, lay, d_factor_status + 1); break;
+        case 2: pm_restrict_kernel<T, 2>(nb, smem, stream, L.d_desc, lv[l + 1].d_desc, wk, d_state, C, b, x, bc, lay, d_factor_status + 1); break;
+        case 3: pm_restrict_kernel<T, 3>(nb, smem, stream, L.d_desc, lv[l + 1].d_desc, wk, d_state, C, b, x, bc, lay, d_factor_status + 1); break;
+        case 4: pm_restrict_kernel<T, 4>(nb, smem, stream, L.d_desc, lv[l + 1].d_desc, wk, d_state, C, b, x, bc, lay, d_factor_status + 1); break;
         default: throw std::logic_error("plane slab must hold 1..4 cells per thread");
     }
     }
@@ -2119,7 +2166,7 @@ void StructBatch::pcg_iteration(T *x) {
 // FP32 V-cycle on the rounded residual, double-float p update.
 // Plane-marching double-float CG product over all problems of the finest level.
 template <int CPT>
-static void pm_df_kernel(unsigned nblocks, size_t smem, cudaStream_t stream, const LevelDesc *desc, const int4 *items,
+static void pm_df_kernel(unsigned nblocks, size_t smem, cudaStream_t stream, const LevelDesc *desc, PlaneWork items,
                          CgState *st, int *count, ReduceScratch rs, const int2 *pinfo, CoeffsDF C, const float2 *pv,
                          float2 *q, PlaneLayout lay, int *err) {
     launch_pdl(k_pm_df_spmv<CPT>, nblocks, kPlaneThreads + 32, smem, stream, desc, items, st, count, rs, pinfo, C, pv, q, lay,
@@ -2139,12 +2186,13 @@ void StructBatch::pm_df_spmv(const CoeffsDF &C) {
     lay.oB = lay.oD = lay.oG = lay.oDIR = lay.oE = -1;
     lay.slot_bytes = (off + 127) & ~127;
     const size_t smem = (size_t)kPlaneStages * lay.slot_bytes;
-    const unsigned nb = (unsigned)L0.pa.n;
+    const unsigned nb = (unsigned)L0.pa.nb;
+    const PlaneWork wk{L0.pa.items, L0.pa.first};
     switch (L0.pa.cells / kPlaneThreads) {
-        case 1: pm_df_kernel<1>(nb, smem, stream, L0.d_desc, L0.pa.items, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2], dfv[3], lay, d_factor_status + 1); break;
-        case 2: pm_df_kernel<2>(nb, smem, stream, L0.d_desc, L0.pa.items, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2], dfv[3], lay, d_factor_status + 1); break;
-        case 3: pm_df_kernel<3>(nb, smem, stream, L0.d_desc, L0.pa.items, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2], dfv[3], lay, d_factor_status + 1); break;
-        case 4: pm_df_kernel<4>(nb, smem, stream, L0.d_desc, L0.pa.items, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2], dfv[3], lay, d_factor_status + 1); break;
+        case 1: pm_df_kernel<1>(nb, smem, stream, L0.d_desc, wk, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2], dfv[3], lay, d_factor_status + 1); break;
+        case 2: pm_df_kernel<2>(nb, smem, stream, L0.d_desc, wk, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2], dfv[3], lay, d_factor_status + 1); break;
+        case 3: pm_df_kernel<3>(nb, smem, stream, L0.d_desc, wk, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2], dfv[3], lay, d_factor_status + 1); break;
+        case 4: pm_df_kernel<4>(nb, smem, stream, L0.d_desc, wk, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2], dfv[3], lay, d_factor_status + 1); break;
         default: throw std::logic_error("plane slab must hold 1..4 cells per thread");
     }
 }

@@ -54,12 +54,15 @@ const char *kname(const char *base, int level, bool fp32);
 
 class StructBatch {
 public:
-    // Plane-marching work items {p, y0, x0, x1} (slab of rows y0.. of planes x0..x1-1),
-    // per-problem item ranges, and the largest stage regions (elements)
+    // Plane-marching work items {p, y0, x0, x1} (slab of rows y0.. of planes x0..x1-1), each
+    // block's contiguous range of items (first[b] .. first[b+1]-1), per-problem item ranges (an
+    // item's reduction slot is its index), and the largest stage regions (elements)
     struct PlaneItems {
         int4 *items = nullptr;
+        int *first = nullptr;
         int2 *pinfo = nullptr;
-        int n = 0;
+        int n = 0;   // items
+        int nb = 0;  // blocks of a launch
         bool ok = false;
         int cells = 0;  // slab capacity: Ty = cells / nz whole rows
         int halo = 0, cy = 0, slab = 0, coarse = 0;

@@ -191,12 +191,13 @@ __device__ __forceinline__ double2 block_sum(Acc<T> a, Acc<T> b) {
 // per launch (kernels loop over their cells), so this runs about once per resident
 // block rather than once per 256 cells.
 template <typename T, int NV = 1>
-__device__ __forceinline__ bool reduce_last(Acc<T> a, Acc<T> b, ReduceScratch rs, int2 pinfo, int p, double2 &tot) {
+__device__ __forceinline__ bool reduce_last(Acc<T> a, Acc<T> b, ReduceScratch rs, int2 pinfo, int p, double2 &tot,
+                                            int slot = -1) {
     __shared__ int amlast;
     __shared__ double2 total;
     double2 s = block_sum<T, NV>(a, b);
     if (threadIdx.x == 0) {
-        rs.partials[blockIdx.x] = s;
+        rs.partials[slot >= 0 ? slot : (int)blockIdx.x] = s;
         __threadfence();
         unsigned t = atomicAdd(&rs.tickets[p], 1u);
         amlast = (t == (unsigned)(pinfo.y - 1));
@@ -218,6 +219,15 @@ __device__ __forceinline__ bool reduce_last(Acc<T> a, Acc<T> b, ReduceScratch rs
     __syncthreads();
     tot = total;
     return true;
+}
+
+// reduce_last for launches whose blocks each contribute one partial per work item (the
+// plane-marching kernels): the partial goes to the item's slot, and pinfo = {first slot, slots}
+// of problem p.
+template <typename T>
+__device__ __forceinline__ bool reduce_last_slot(Acc<T> a, ReduceScratch rs, int2 pinfo, int p, int slot,
+                                                 double2 &tot) {
+    return reduce_last<T, 1>(a, Acc<T>(), rs, pinfo, p, tot, slot);
 }
 
 // Flux-form 7-point operator at one cell: Ax = leak x_i + sum_f c_f (x_i - x_j) and
