@@ -438,7 +438,7 @@ class GroundwaterBatch(GroundwaterProblem):
 
 
 _TUNED = ("cheb_degree", "plane_cells", "plane_blocks_per_sm", "tail_cells", "blocks_per_sm", "df_plane_cells",
-          "tail_cluster", "plane_levels", "streams")
+          "tail_cluster", "plane_levels", "streams", "fuse")
 
 
 def autotune_batch(dims, mins, maxs, dirichletnodes, logK, dirichleths, Qs, obs_per_problem, mean="geometric",

@@ -40,6 +40,7 @@ class Options(ctypes.Structure):
         ("tail_cluster", ctypes.c_int),
         ("plane_levels", ctypes.c_int),
         ("streams", ctypes.c_int),
+        ("fuse", ctypes.c_int),
     ]
 
 

@@ -391,6 +391,7 @@ dpf_options fill_options(const dpf_options *o) {
     r.tail_cluster = std::min(16, r.tail_cluster);
     if (r.plane_levels < 0) r.plane_levels = d.plane_levels;
     if (r.streams < 0) r.streams = d.streams;
+    if (r.fuse == 0) r.fuse = d.fuse;
     return r;
 }
 
@@ -485,6 +486,7 @@ void dpf_default_options(dpf_options *o) {
     o->tail_cluster = 1;
     o->plane_levels = 0;
     o->streams = 0;
+    o->fuse = 1;
 }
 
 int dpf_detect_regular3d(int64_t N, int64_t F, const int64_t *a, const int64_t *b, const double *aol, int *dims,

@@ -23,6 +23,7 @@
 #include "dpf_struct.h"
 #include "dpf_struct_kernels.cuh"
 #include "dpf_plane.cuh"
+#include "dpf_plane2.cuh"
 
 namespace dpf {
 namespace cg = cooperative_groups;
@@ -1290,9 +1291,12 @@ void StructBatch::build_plane_items(PlaneItems &P, const Level &L, const std::ve
         P.halo = std::max(P.halo, (Ty + 2) * D.nz);
         P.cy = std::max(P.cy, (Ty + 1) * D.nz);
         P.slab = std::max(P.slab, Ty * D.nz);
+        P.halo2 = std::max(P.halo2, (Ty + 4) * D.nz);
+        P.cy2 = std::max(P.cy2, (Ty + 3) * D.nz);
         if (shapes && l + 1 < (int)(*shapes)[p].size()) {
             const int cnz = (*shapes)[p][l + 1][2];
             P.coarse = std::max(P.coarse, ((Ty + 2) / 2 + 2) * cnz);
+            P.coarse2 = std::max(P.coarse2, ((Ty + 4) / 2 + 2) * cnz);
         }
     }
     // on the finest level at least 4 plane pairs per block where the level allows: every run also
@@ -1771,6 +1775,9 @@ static void configure_kernels() {
     raise((const void *)k_pm_df_spmv<2>);
     raise((const void *)k_pm_df_spmv<3>);
     raise((const void *)k_pm_df_spmv<4>);
+    raise((const void *)k_pm_post2<float, false>);
+    raise((const void *)k_pm_post2<float, true>);
+    raise((const void *)k_pm_pre2r<float>);
     CK(cudaFuncSetAttribute(k_tail_cycle<float, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     CK(cudaFuncSetAttribute(k_tail_cycle<double, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     done.insert(dev);
@@ -1900,6 +1907,76 @@ void StructBatch::pm_restrict(int l, const T *b, const T *x, T *bc) {
     }
 }
 
+// Layout of the fused kernels' shared memory for level l: the staged regions of one plane (kFusedStages
+// of them), then the rings of first-step results, directions and residual pairs.
+static FusedLayout fused_layout(const StructBatch::PlaneItems &P, bool post, int es, int ec) {
+    FusedLayout lay{};
+    int off = 0;
+    auto take = [&](int bytes) { int o = off; off += bytes; return o; };
+    lay.oX = lay.oDIR = lay.oE = lay.oB = lay.oG = lay.oCX = lay.oCY = lay.oCZ = lay.oLK = -1;
+    if (post) {
+        lay.oX = take(pm_region(P.halo2, es));
+        lay.oDIR = take(pm_region(P.halo2, 1));
+        lay.oE = take(pm_region(P.coarse2, es));
+        lay.oB = take(pm_region(P.halo, es));
+    } else {
+        lay.oB = take(pm_region(P.halo2, es));
+        lay.oG = take(pm_region(P.halo2, es));
+    }
+    lay.oCX = take(pm_region(P.halo, ec));
+    lay.oCY = take(pm_region(P.cy2, ec));
+    lay.oCZ = take(pm_region(P.halo, ec));
+    lay.oLK = take(pm_region(P.halo, ec));
+    lay.slot_bytes = (off + 127) & ~127;
+    int ring = kFusedStages * lay.slot_bytes;
+    lay.v_stride = (P.halo * es + 127) & ~127;
+    lay.oV = ring;
+    ring += 4 * lay.v_stride;
+    lay.d_stride = lay.r_stride = (P.slab * es + 127) & ~127;
+    lay.oD = lay.oR = ring;  // the post-smoothing's directions or the pre-smoothing's residual pairs
+    ring += 2 * lay.d_stride;
+    lay.slot_bytes = lay.slot_bytes;
+    return lay;
+}
+static size_t fused_smem(const FusedLayout &lay) { return (size_t)lay.oD + 2 * (size_t)lay.d_stride; }
+
+// Fused pre-smoothing (two Chebyshev steps from zero) and restriction of level l into level l+1.
+template <typename T>
+void StructBatch::pm_pre2r(int l, const T *b, T *xout, T *bc, T c1, T c2, T invth) {
+    if constexpr (sizeof(T) != 4) {
+        throw std::logic_error("plane-marching kernels run FP32 V-cycles only");
+    } else {
+        Level &L = lv[l];
+        const FusedLayout lay = fused_layout(L.pm, false, (int)sizeof(T), (int)sizeof(coef_t<T>));
+        launch_pdl(k_pm_pre2r<T>, (unsigned)L.pm.nb, kFusedThreads + 32, fused_smem(lay), stream, L.d_desc,
+                   lv[l + 1].d_desc, PlaneWork{L.pm.items, L.pm.first}, L.pm.cells, (const CgState *)d_state,
+                   coeffs_of<T>(L, mixed), b, xout, bc, c1, c2, invth, lay, d_factor_status + 1);
+    }
+}
+
+// Fused prolongation and post-smoothing (two Chebyshev steps) of level l; on the finest level it
+// also forms r . z and beta.
+template <typename T>
+void StructBatch::pm_post2(int l, const T *b, const T *xin, T *xout, const T *e, T c2a, T c1b, T c2b, T sc) {
+    if constexpr (sizeof(T) != 4) {
+        throw std::logic_error("plane-marching kernels run FP32 V-cycles only");
+    } else {
+        Level &L = lv[l];
+        const FusedLayout lay = fused_layout(L.pm, true, (int)sizeof(T), (int)sizeof(coef_t<T>));
+        const PlaneWork wk{L.pm.items, L.pm.first};
+        if (l == 0)
+            launch_pdl(k_pm_post2<T, true>, (unsigned)L.pm.nb, kFusedThreads + 32, fused_smem(lay), stream, L.d_desc,
+                       lv[l + 1].d_desc, wk, L.pm.cells, d_state, coeffs_of<T>(L, mixed), b, xin, xout,
+                       (const uint8_t *)L.dir, e, c2a, c1b, c2b, sc, lay, rs, (const int2 *)L.pm.pinfo,
+                       d_factor_status + 1);
+        else
+            launch_pdl(k_pm_post2<T, false>, (unsigned)L.pm.nb, kFusedThreads + 32, fused_smem(lay), stream, L.d_desc,
+                       lv[l + 1].d_desc, wk, L.pm.cells, d_state, coeffs_of<T>(L, mixed), b, xin, xout,
+                       (const uint8_t *)L.dir, e, c2a, c1b, c2b, sc, lay, rs, (const int2 *)L.pm.pinfo,
+                       d_factor_status + 1);
+    }
+}
+
 // The fused tail: one block per problem, or a cluster of tail_cs blocks per problem when
 // the device can co-schedule that many 1024-thread blocks (halved until it can).
 template <typename T>
@@ -1952,13 +2029,27 @@ void StructBatch::vcycle(const T *r, T *z) {
     const int deg = opt.cheb_degree;
     const T invth = (T)inv_theta, sc = (T)opt.coarse_scale;
     std::vector<T *> pre(nlev_max, nullptr);
+    // where each level's final iterate lands (the coarse correction of the next finer level):
+    // work[1] (xb), except after the fused post-smoothing, which cannot write in place
+    std::vector<T *> fin(nlev_max, nullptr);
+    for (int l = 0; l < nlev_max; l++) fin[l] = (T *)lv[l].work[1];
+    const bool fused = opt.fuse > 0 && deg == 2;
     // descend
     for (int l = 0; l < nlev_max; l++) {
         Level &L = lv[l];
         Coeffs<T> C = coeffs_of<T>(L, mixed);
         const T *b = l == 0 ? r : (const T *)L.work[2];
         T *xa = (T *)L.work[0], *xb = (T *)L.work[1], *d = (T *)L.work[3];
-        if (nb_of(L.smooth) && L.pm.ok && deg >= 2) {
+        if (nb_of(L.smooth) && L.pm.ok && fused) {
+            // one pass: two pre-smoothing steps from zero and the restriction of their residual
+            Level &Cn = lv[l + 1];
+            {
+                KTimer _kt(this, kname("k_pm_pre2r", l, sizeof(T) == 4), L.smooth_cells);
+                pm_pre2r<T>(l, b, xb, (T *)Cn.work[2], (T)cheb_c1[1], (T)cheb_c2[1], invth);
+            }
+            LAUNCH_CHECK();
+            pre[l] = xb;
+        } else if (nb_of(L.smooth) && L.pm.ok && deg >= 2) {
             // plane-marching pre-smoothing: two fused first steps, then the rest
             {
                 KTimer _kt(this, kname("k_pm_first2", l, sizeof(T) == 4), L.smooth_cells);
@@ -2074,7 +2165,18 @@ void StructBatch::vcycle(const T *r, T *z) {
         const T *b = l == 0 ? r : (const T *)L.work[2];
         T *xa = (T *)L.work[0], *xb = (T *)L.work[1], *d = (T *)L.work[3];
         T *cur = pre[l];
-        const T *e = (const T *)Cn.work[1];
+        const T *e = fin[l + 1];
+        if (L.pm.ok && fused) {
+            // one pass: prolongation and both post-smoothing steps (the finest level also forms r . z)
+            T *o = l == 0 ? z : xa;
+            {
+                KTimer _kt(this, kname("k_pm_post2", l, sizeof(T) == 4), L.smooth_cells);
+                pm_post2<T>(l, b, cur, o, e, invth, (T)cheb_c1[1], (T)cheb_c2[1], sc);
+            }
+            LAUNCH_CHECK();
+            fin[l] = o;
+            continue;
+        }
         if (L.pm.ok && deg >= 2) {
             // plane-marching post-smoothing: prolongation fused into the first step; the
             // last step writes no direction (and on the finest level also forms r . z)

@@ -66,6 +66,7 @@ public:
         bool ok = false;
         int cells = 0;  // slab capacity: Ty = cells / nz whole rows
         int halo = 0, cy = 0, slab = 0, coarse = 0;
+        int halo2 = 0, cy2 = 0, coarse2 = 0;  // regions of the fused kernels (two halo rows)
     };
     struct Level {
         long long ntot = 0;
@@ -121,6 +122,10 @@ public:
     void write_tail_table();
     template <typename T>
     void pm_restrict(int l, const T *b, const T *x, T *bc);
+    template <typename T>
+    void pm_pre2r(int l, const T *b, T *xout, T *bc, T c1, T c2, T invth);
+    template <typename T>
+    void pm_post2(int l, const T *b, const T *xin, T *xout, const T *e, T c2a, T c1b, T c2b, T sc);
     void pm_df_spmv(const CoeffsDF &C);
     template <typename T>
     void pm_launch(int mode, int l, const T *b, const T *xin, T *xout, T *d, const T *e, T c1, T c2, T invth, T sc);

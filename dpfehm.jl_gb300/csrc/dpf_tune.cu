@@ -132,6 +132,7 @@ extern "C" int dpf_batch_autotune(int nprob, const int *dims, const double *mins
             {"tail_cluster", &cur.tail_cluster, {1, 8}, true},
             {"plane_levels", &cur.plane_levels, {0, 1, 2}, mixed},
             {"streams", &cur.streams, {1, 2, 4}, nprob >= 2},
+            {"fuse", &cur.fuse, {-1, 1}, mixed},
         };
         for (const Knob &k : knobs) {
             if (!k.active || rc != DPF_OK) continue;

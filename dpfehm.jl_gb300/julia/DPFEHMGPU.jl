@@ -38,12 +38,13 @@ mutable struct Options
     tail_cluster::Cint
     plane_levels::Cint
     streams::Cint
+    fuse::Cint
 end
 
 """The library defaults with any `dpf_options` field overridden by keyword (`precision` as
 `:fp64` or `:mixed`)."""
 function default_options(; kwargs...)
-    o = Options(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
+    o = Options(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
     ccall((:dpf_default_options, libdpf), Cvoid, (Ref{Options},), o)
     for (k, v) in pairs(kwargs)
         if k === :precision

@@ -98,6 +98,10 @@ typedef struct dpf_options {
                             on its own non-blocking stream and host thread), so that one part's
                             finest-level kernels overlap another's small levels (default 0: one
                             stream; an autotuner choice) */
+    int fuse;            /* regular grids, MIXED, Chebyshev degree 2: the plane-marching pre-smoothing and
+                            restriction of a level run as one pass, and so do the prolongation and
+                            post-smoothing (the intermediate iterate stays in shared memory)
+                            (default 1; negative: separate passes) */
 } dpf_options;
 
 typedef struct dpf_problem dpf_problem;
