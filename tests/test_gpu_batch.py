@@ -88,7 +88,7 @@ def test_profile_report_and_launch_count(gpu_lib):
     rep = P.profile_report()
     P.profile(False)
     assert P.launch_count > n0
-    assert any(k.startswith(("k_pm_step<f32>/L0", "k_cheb_step<f32>/L0")) for k in rep)
+    assert any(k.startswith(("k_pm_post2<f32>/L0", "k_pm_step<f32>/L0", "k_cheb_step<f32>/L0")) for k in rep)
     assert all(v[0] > 0 and v[1] >= 0 for v in rep.values())
     assert sum(v[0] for v in rep.values()) == P.launch_count - n0
 
