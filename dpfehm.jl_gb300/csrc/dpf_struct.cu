@@ -2029,10 +2029,11 @@ void StructBatch::vcycle(const T *r, T *z) {
     const int deg = opt.cheb_degree;
     const T invth = (T)inv_theta, sc = (T)opt.coarse_scale;
     std::vector<T *> pre(nlev_max, nullptr);
-    // where each level's final iterate lands (the coarse correction of the next finer level):
-    // work[1] (xb), except after the fused post-smoothing, which cannot write in place
-    std::vector<T *> fin(nlev_max, nullptr);
-    for (int l = 0; l < nlev_max; l++) fin[l] = (T *)lv[l].work[1];
+    // Every level leaves its final iterate (the coarse correction of the next finer level) in
+    // work[1] (xb), whichever kernels ran it for a problem: per-level passes, the fused tail or the
+    // coarsest solve. Problems of an uneven batch reach the tail at different levels, so this must
+    // hold for every problem. The fused passes keep it: the pre-smoothed iterate goes to work[0]
+    // and the post-smoothing (which cannot run in place) reads it there and writes work[1].
     const bool fused = opt.fuse > 0 && deg == 2;
     // descend
     for (int l = 0; l < nlev_max; l++) {
@@ -2045,10 +2046,10 @@ void StructBatch::vcycle(const T *r, T *z) {
             Level &Cn = lv[l + 1];
             {
                 KTimer _kt(this, kname("k_pm_pre2r", l, sizeof(T) == 4), L.smooth_cells);
-                pm_pre2r<T>(l, b, xb, (T *)Cn.work[2], (T)cheb_c1[1], (T)cheb_c2[1], invth);
+                pm_pre2r<T>(l, b, xa, (T *)Cn.work[2], (T)cheb_c1[1], (T)cheb_c2[1], invth);
             }
             LAUNCH_CHECK();
-            pre[l] = xb;
+            pre[l] = xa;
         } else if (nb_of(L.smooth) && L.pm.ok && deg >= 2) {
             // plane-marching pre-smoothing: two fused first steps, then the rest
             {
@@ -2165,16 +2166,14 @@ void StructBatch::vcycle(const T *r, T *z) {
         const T *b = l == 0 ? r : (const T *)L.work[2];
         T *xa = (T *)L.work[0], *xb = (T *)L.work[1], *d = (T *)L.work[3];
         T *cur = pre[l];
-        const T *e = fin[l + 1];
+        const T *e = (const T *)Cn.work[1];
         if (L.pm.ok && fused) {
             // one pass: prolongation and both post-smoothing steps (the finest level also forms r . z)
-            T *o = l == 0 ? z : xa;
             {
                 KTimer _kt(this, kname("k_pm_post2", l, sizeof(T) == 4), L.smooth_cells);
-                pm_post2<T>(l, b, cur, o, e, invth, (T)cheb_c1[1], (T)cheb_c2[1], sc);
+                pm_post2<T>(l, b, cur, l == 0 ? z : xb, e, invth, (T)cheb_c1[1], (T)cheb_c2[1], sc);
             }
             LAUNCH_CHECK();
-            fin[l] = o;
             continue;
         }
         if (L.pm.ok && deg >= 2) {

@@ -93,6 +93,28 @@ def test_profile_report_and_launch_count(gpu_lib):
     assert sum(v[0] for v in rep.values()) == P.launch_count - n0
 
 
+def test_fused_and_separate_plane_passes_agree(gpu_lib, orc):
+    """The fused plane passes (pre-smoothing + restriction, prolongation + post-smoothing in one
+    pass each) give the separate passes' solve to rounding and the oracle's, on an uneven batch
+    whose problems reach the fused small-level tail at different levels (so a level is
+    smoothed by per-level kernels for some problems and inside the tail for others)."""
+    pkg = gpu_lib
+    shapes = [(50, 50, 5), (66, 60, 10), (31, 29, 7), (24, 20, 8), (9, 9, 9)]
+    probs = [_problem(pkg, ns, 141 + k) for k, ns in enumerate(shapes)]
+    cat = lambda k: np.concatenate([p[k] for p in probs])
+    out = {}
+    for fuse in (1, -1):
+        B = pkg.GroundwaterBatch([p["ns"] for p in probs], [p["mins"] for p in probs], [p["maxs"] for p in probs],
+                                 [p["dn"] for p in probs], reltol=1e-11, precision="mixed", fuse=fuse)
+        out[fuse] = B.solve_grad_logk(cat("logK"), cat("dh"), cat("Qs"), [p["obs"] for p in probs])
+    assert rel(out[1][0], out[-1][0]) < 1e-9 and rel(out[1][1], out[-1][1]) < 1e-7
+    off = np.cumsum([0] + [p["N"] for p in probs])
+    for k, p in enumerate(probs):
+        h_or, g_or = _oracle(orc, pkg, p)
+        assert rel(out[1][0][off[k]:off[k + 1]], h_or) < 1e-8, k
+        assert rel(out[1][1][off[k]:off[k + 1]], g_or) < 1e-6, k
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_plane_and_grid_stride_smoothers_agree(gpu_lib, precision):
     """The plane-marching smoothers (shared-memory staged, prolongation fused) and the
