@@ -486,7 +486,7 @@ void dpf_default_options(dpf_options *o) {
     o->tail_cluster = 1;
     o->plane_levels = 0;
     o->streams = 0;
-    o->fuse = 1;
+    o->fuse = -1;
 }
 
 int dpf_detect_regular3d(int64_t N, int64_t F, const int64_t *a, const int64_t *b, const double *aol, int *dims,

@@ -485,7 +485,8 @@ __global__ void kg_df_residual(int n, CgState *st, int *active_count, ReduceScra
         } else if (FIRST) {
             bb.v += b[i] * b[i];
         } else {
-            const double f = 0x1p-53 * fma(2.0 * dg, fabs(xi), fabs(b[i]));
+            // the rounding bound of the double-float recurrence (u = 2^-48), as on the structured path
+            const double f = 0x1p-48 * fma(2.0 * dg, fabs(xi), fabs(b[i]));
             bb.v += f * f;
         }
     }

@@ -793,9 +793,12 @@ __global__ void k_df_residual(const LevelDesc *__restrict__ desc, const int4 *__
         } else if (FIRST) {
             bb.v += bi * bi;
         } else {
-            // rounding bound of b_i - (A x)_i in FP64, and of storing x itself:
-            // u (|b_i| + 2 diag_i |x_i|), u = 2^-53 (neighbours of x_i taken as |x_i|)
-            const double f = 0x1p-53 * fma(2.0 * dg, fabs(xi), fabs(bi));
+            // rounding bound of b_i - (A x)_i and of x itself, u (|b_i| + 2 diag_i |x_i|) (neighbours
+            // of x_i taken as |x_i|), with the unit roundoff of the double-float recurrence that
+            // produced x, u = 2^-48: its search directions and residuals carry about 48 bits, so the
+            // true residual of a converged round settles near this bound, about 32 times the FP64
+            // one; a round that reaches it is accepted without a further round that cannot improve it
+            const double f = 0x1p-48 * fma(2.0 * dg, fabs(xi), fabs(bi));
             bb.v += f * f;
         }
     }

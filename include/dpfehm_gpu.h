@@ -100,8 +100,9 @@ typedef struct dpf_options {
                             stream; an autotuner choice) */
     int fuse;            /* regular grids, MIXED, Chebyshev degree 2: the plane-marching pre-smoothing and
                             restriction of a level run as one pass, and so do the prolongation and
-                            post-smoothing (the intermediate iterate stays in shared memory)
-                            (default 1; negative: separate passes) */
+                            post-smoothing (the intermediate iterate stays in shared memory); half
+                            the bytes, but more instructions per cell, and slower on GB300 at the
+                            benchmark sizes (default -1: separate passes; an autotuner choice) */
 } dpf_options;
 
 typedef struct dpf_problem dpf_problem;
