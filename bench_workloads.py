@@ -400,9 +400,126 @@ def run_richards(args, dist, rank, ws, METRIC_NAME):
     }
 
 
+def run_dfn(args, dist, rank, ws, METRIC_NAME):
+    """A synthetic fracture network mesh (grid.fracture_network: 3000 square fractures with power-law
+    sizes from 4 to 50 m in a 100 m cube, cells of 0.25 m, about 5M cells after keeping the largest
+    connected component; degrees 2-9) through dpf_create, so the CSR path solves it: h = 1 within
+    5 m of x = 0, h = 0 within 5 m of x = 100, two 1e-6 m^3/s injections, one log-conductivity per
+    fracture (N(-9, 1)), J = sum of h^2 at 100 cells. Host setup (topology, aggregation hierarchy)
+    is timed separately from the solves."""
+    import sys
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    ge._load_build_module().build()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    t0 = time.perf_counter()
+    c, vol, nb, areas, lengths, fr = pkg.grid.fracture_network(3000, 100.0, 0.25, 3, smin=4.0)
+    gen_s = time.perf_counter() - t0
+    N, F = c.shape[1], len(nb)
+    aol = areas / lengths
+    rng = np.random.default_rng(4)
+    logK = rng.normal(-9.0, 1.0, fr.max() + 1)[fr]
+    x = c[0]
+    dn = np.nonzero((x < 5.0) | (x > 95.0))[0]
+    dh = np.zeros(N)
+    dh[x < 5.0] = 1.0
+    Qs = np.zeros(N)
+    Qs[rng.choice(np.nonzero((x > 30) & (x < 70))[0], 2, replace=False)] = 1e-6
+    obs = rng.choice(np.setdiff1d(np.arange(N), dn), 100, replace=False)
+    d = [torch.tensor(v, device=dev) for v in (logK, dh, Qs)]
+    flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float64, device=dev)
+    import warnings
+    warnings.simplefilter("error", RuntimeWarning)
+    t0 = time.perf_counter()
+    G = pkg.GroundwaterProblem(nb, aol, dn, N=N, volumes=vol, reltol=1e-10, precision=args.precision)
+    setup_s = time.perf_counter() - t0
+    assert not G.structured
+    steps = max(1, args.steps // 2)
+    t = _events(torch, lambda: G.solve_grad_logk(*d, obs), steps, 2, flush)
+    h, g = G.solve_grad_logk(*d, obs)
+    iters = G.stats["iterations"]
+    # per-kernel CUDA events over one more forward + adjoint: the dominant kernel against the roofline
+    G.profile(True)
+    G.solve_grad_logk(*d, obs)
+    rep = G.profile_report()
+    G.profile(False)
+    total = sum(v[1] for v in rep.values())
+    top = sorted(rep.items(), key=lambda kv: -kv[1][1])
+    name, (cnt, ms, cells) = top[0]
+    nnz = 2 * int(np.sum(~(np.isin(nb[:, 0], dn) | np.isin(nb[:, 1], dn))))  # couplings between free cells
+    # kg_df_spmv_pq: column index (4 B) and double-float value (8 B) per coupling, row pointer (4 B),
+    # p, leak and q as double-float pairs (8 B each) per row
+    spmv_bytes = 12 * nnz + 4 * (N + 1) + 24 * N
+    sp = rep.get("kg_df_spmv_pq<f32>/L0")
+    peaks = {}
+    try:
+        import json as _json
+        peaks = _json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    roof = None
+    if sp:
+        ach = spmv_bytes * sp[0] / (sp[1] / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": "kg_df_spmv_pq<f32>/L0", "achieved": round(ach, 1), "peak": peak,
+                "unit": "GB/s", "frac": round(ach / peak, 4),
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "traffic": None,
+                "bytes_per_launch": int(spmv_bytes), "avg_launch_us": round(1e3 * sp[1] / sp[0], 3),
+                "share": round(sp[1] / total, 4) if total else None,
+                "measured": "per-kernel CUDA events on the solver stream over one forward+adjoint of this workload"}
+    G64 = pkg.GroundwaterProblem(nb, aol, dn, N=N, volumes=vol, reltol=1e-10, precision="fp64")
+    t64 = _events(torch, lambda: G64.solve_grad_logk(*d, obs), 1, 1, flush)
+    h, g = h.cpu().numpy(), g.cpu().numpy()
+    # the oracle: timed at the run's reltol (the CPU baseline), then at 1e-13 for the errors
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    orc.build()
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    Ks = orc.logk_to_faces(nb, logK)
+
+    def oracle_step(tol):
+        O = orc.Problem(N, nb, aol, dn)
+        ho = O.steady(Ks, dh, Qs, reltol=tol)
+        delta = np.zeros(N)
+        np.add.at(delta, obs, 2 * ho[obs])
+        dKs, _, _ = O.adjoint(dh, delta, reltol=tol)
+        return ho, orc.logk_to_faces_vjp(nb, logK, dKs)
+
+    t0 = time.perf_counter()
+    oracle_step(1e-10)
+    tc = time.perf_counter() - t0
+    ho, go = oracle_step(1e-13)
+    return {
+        "metric": METRIC_NAME, "value": round(steps / t, 3), "unit": "solves/s", "n_gpus": ws, "steps": steps,
+        "warmup": 2, "ms_per_step": round(1e3 * t / steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 V-cycle + double-float CG (f32 ops), f64 residual"
+        if args.precision == "mixed" else "f64",
+        "data": "synthetic (seeded fracture network, one log-conductivity per fracture)",
+        "config": {"workload": "gw_steady_fwd_adj_dfn_5M", "cells": N, "faces": F,
+                   "fractures": int(len(np.unique(fr))), "max_degree": int(np.bincount(nb.ravel()).max()),
+                   "dirichlet_cells": int(len(dn)), "path": "CSR (dpf_create on a face list)",
+                   "generate_seconds": round(gen_s, 2), "setup_seconds": round(setup_s, 2),
+                   "precision": args.precision, "reltol": 1e-10},
+        "iterations_last_adjoint": iters,
+        "plain_fp64_gpu": {"value": round(1.0 / t64, 3), "unit": "solves/s"},
+        "speedup_vs_plain_fp64": round(t64 / (t / steps), 3),
+        "roofline": roof,
+        "top": [{"kernel": k, "launches": v[0], "ms": round(v[1], 3)} for k, v in top[:8]],
+        "accuracy": {"rel_head_err_vs_oracle_1e-13": _rel(h, ho), "rel_grad_err_vs_oracle_1e-13": _rel(g, go)},
+        "cpu_baseline": {"value": round(1.0 / tc, 4), "unit": "solves/s", "cores": cores, "kind": "port",
+                         "sample": "one forward+adjoint of this workload (oracle: Ruge-Stueben AMG + CG, FP64, "
+                                   "reltol 1e-10, setup included)"},
+    }
+
+
 def run(name, args, dist, rank, ws):
     if rank != 0:
         return None
+    if name == "dfn":
+        return run_dfn(args, dist, rank, ws, "forward+adjoint solves/sec, 5M-cell fracture network, CSR path")
     if name == "richards":
         return run_richards(args, dist, rank, ws, "Richards steady forward+adjoint solves/sec, 200k cells")
     if name == "general_1m":

@@ -1160,7 +1160,7 @@ int dpf_profile(dpf_problem *P, int enable) {
     for (dpf_problem *Q : P->parts) Q->sb->profile(enable != 0);
     if (!P->parts.empty()) return DPF_OK;
     if (P->sb) P->sb->profile(enable != 0);
-    else return DPF_UNSUPPORTED;
+    else P->gs->profile(enable != 0);
     return DPF_OK;
 }
 
@@ -1198,7 +1198,7 @@ int dpf_profile_report(dpf_problem *P, int cap, const char **names, long long *l
             return (int)nm.size();
         }
         if (P->sb) return P->sb->profile_report(cap, names, launches, ms, cells);
-        return 0;
+        return P->gs->profile_report(cap, names, launches, ms, cells);
     } catch (const DpfError &e) {
         P->err = e.what();
         return -e.code;

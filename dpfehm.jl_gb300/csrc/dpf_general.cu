@@ -667,6 +667,58 @@ static void gck(cudaError_t e, const char *what) {
         gck(cudaGetLastError(), "kernel launch"); \
     } while (0)
 
+// Brackets one kernel launch with a pair of CUDA events on the solver's stream while profiling is
+// on (per-kernel device time for dpf_profile_report; launches are counted by GLAUNCH).
+struct GTimer {
+    GeneralSolver *S;
+    int slot = -1;
+    GTimer(GeneralSolver *s, const char *name, long long cells) : S(s) {
+        if (!S->prof_on || S->prof_recs.size() >= (1u << 20)) return;
+        const int e = (int)(2 * S->prof_recs.size());
+        while ((int)S->ev_pool.size() < e + 2) {
+            cudaEvent_t ev;
+            if (cudaEventCreate(&ev) != cudaSuccess) { cudaGetLastError(); return; }
+            S->ev_pool.push_back(ev);
+        }
+        S->prof_recs.push_back(ProfRec{name, e, cells});
+        cudaEventRecord(S->ev_pool[e], S->stream);
+        slot = e;
+    }
+    ~GTimer() {
+        if (slot >= 0) cudaEventRecord(S->ev_pool[slot + 1], S->stream);
+    }
+};
+
+void GeneralSolver::profile(bool on) {
+    cudaStreamSynchronize(stream);
+    prof_recs.clear();
+    prof_on = on;
+}
+
+int GeneralSolver::profile_report(int cap, const char **names, long long *counts, double *ms, long long *cells) {
+    GCK(cudaStreamSynchronize(stream));
+    std::vector<const char *> nm;
+    std::vector<long long> cnt, cl;
+    std::vector<double> tot;
+    for (auto &r : prof_recs) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, ev_pool[r.ev], ev_pool[r.ev + 1]) != cudaSuccess) { cudaGetLastError(); continue; }
+        size_t k = 0;
+        while (k < nm.size() && std::strcmp(nm[k], r.name) != 0) k++;
+        if (k == nm.size()) { nm.push_back(r.name); cnt.push_back(0); tot.push_back(0.0); cl.push_back(0); }
+        cnt[k]++;
+        tot[k] += t;
+        cl[k] += r.cells;
+    }
+    for (size_t k = 0; k < nm.size() && (int)k < cap; k++) {
+        if (names) names[k] = nm[k];
+        if (counts) counts[k] = cnt[k];
+        if (ms) ms[k] = tot[k];
+        if (cells) cells[k] = cl[k];
+    }
+    return (int)nm.size();
+}
+
 template <typename T>
 T *GeneralSolver::dev(size_t n) {
     void *p = nullptr;
@@ -809,6 +861,7 @@ GeneralSolver::GeneralSolver(long long N_, long long F_, const int64_t *a, const
 
 GeneralSolver::~GeneralSolver() {
     cudaStreamSynchronize(stream);  // then `owned` and `pinned` free the buffers
+    for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
 }
 
 // Host-side topology: the Dirichlet mask, the cell -> face incidence, the CSR of the
@@ -918,26 +971,48 @@ void GeneralSolver::build_hierarchy() {
         for (int I = 0; I < nc; I++) mrp[I + 1] += mrp[I];
         std::vector<int> mci(mrp[nc]), pos(mrp.begin(), mrp.end() - 1);
         for (int i = 0; i < n; i++) if (agg[i] >= 0) mci[pos[agg[i]]++] = i;
-        // coarse couplings: each fine coupling between different aggregates, merged per pair
-        std::vector<std::vector<std::pair<int, int>>> rows(nc);  // (coarse col, fine entry)
+        // coarse couplings: each fine coupling between different aggregates, merged per pair. The
+        // fine entries are bucketed by coarse row with a counting sort into one flat array of
+        // (coarse column, fine entry) keys, and each row's short run is sorted by key, so the
+        // setup is linear in the couplings up to the sort of a row's few entries.
+        std::vector<long long> rstart(nc + 1, 0);
         for (int i = 0; i < n; i++) {
-            int I = agg[i];
+            const int I = agg[i];
             if (I < 0) continue;
             for (int e = rp[i]; e < rp[i + 1]; e++) {
-                int J = agg[ci[e]];
-                if (J >= 0 && J != I) rows[I].push_back({J, e});
+                const int J = agg[ci[e]];
+                if (J >= 0 && J != I) rstart[I + 1]++;
+            }
+        }
+        for (int I = 0; I < nc; I++) rstart[I + 1] += rstart[I];
+        std::vector<unsigned long long> keys(rstart[nc]);
+        {
+            std::vector<long long> fill(rstart.begin(), rstart.end() - 1);
+            for (int i = 0; i < n; i++) {
+                const int I = agg[i];
+                if (I < 0) continue;
+                for (int e = rp[i]; e < rp[i + 1]; e++) {
+                    const int J = agg[ci[e]];
+                    if (J >= 0 && J != I) keys[fill[I]++] = ((unsigned long long)(unsigned)J << 32) | (unsigned)e;
+                }
             }
         }
         std::vector<int> crp_c(nc + 1, 0), cci_c;     // coarse CSR
         std::vector<int> mrp_e, mci_e;                // coarse entry -> fine entries
+        cci_c.reserve(keys.size());
+        mci_e.reserve(keys.size());
+        mrp_e.reserve(keys.size() + 1);
         mrp_e.push_back(0);
         for (int I = 0; I < nc; I++) {
-            auto &r = rows[I];
-            std::sort(r.begin(), r.end());
-            for (size_t k = 0; k < r.size();) {
-                size_t k2 = k;
-                while (k2 < r.size() && r[k2].first == r[k].first) { mci_e.push_back(r[k2].second); k2++; }
-                cci_c.push_back(r[k].first);
+            std::sort(keys.begin() + rstart[I], keys.begin() + rstart[I + 1]);
+            for (long long k = rstart[I]; k < rstart[I + 1];) {
+                const unsigned J = (unsigned)(keys[k] >> 32);
+                long long k2 = k;
+                while (k2 < rstart[I + 1] && (unsigned)(keys[k2] >> 32) == J) {
+                    mci_e.push_back((int)(keys[k2] & 0xffffffffu));
+                    k2++;
+                }
+                cci_c.push_back((int)J);
                 mrp_e.push_back((int)mci_e.size());
                 k = k2;
             }
@@ -1055,19 +1130,19 @@ void GeneralSolver::vcycle(const T *r, T *z) {
         if (l == nl - 1) {
             T *out = l == 0 ? z : xb;
             if (L.dense) {
-                if (l == 0) kg_coarse_solve<T, true><<<1, kMaxCoarse, 0, stream>>>(L.n, d_state, dense_inv, b, out);
-                else kg_coarse_solve<T, false><<<1, kMaxCoarse, 0, stream>>>(L.n, d_state, dense_inv, b, out);
+                if (l == 0) { GTimer _gt(this, kname("kg_coarse_solve", l, sizeof(T) == 4), L.n); kg_coarse_solve<T, true><<<1, kMaxCoarse, 0, stream>>>(L.n, d_state, dense_inv, b, out); }
+                else { GTimer _gt(this, kname("kg_coarse_solve", l, sizeof(T) == 4), L.n); kg_coarse_solve<T, false><<<1, kMaxCoarse, 0, stream>>>(L.n, d_state, dense_inv, b, out); }
                 GLAUNCH();
             } else {
                 // no useful coarsening left: a long Chebyshev sweep stands in for the solve
-                kg_cheb_first<T><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, xa, d, invth);
+                { GTimer _gt(this, kname("kg_cheb_first", l, sizeof(T) == 4), L.n); kg_cheb_first<T><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, xa, d, invth); }
                 GLAUNCH();
                 T *cur = xa;
                 for (int k = 1; k < 8; k++) {
                     T *o = (k == 7) ? out : (cur == xa ? xb : xa);
                     if (o == cur) o = cur == xa ? xb : xa;
-                    kg_cheb_step<T, false, false><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d,
-                                                                           (T)cheb8_c1[k], (T)cheb8_c2[k], rs);
+                    { GTimer _gt(this, kname("kg_cheb_step", l, sizeof(T) == 4), L.n); kg_cheb_step<T, false, false><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d,
+                                                                           (T)cheb8_c1[k], (T)cheb8_c2[k], rs); }
                     GLAUNCH();
                     cur = o;
                 }
@@ -1077,24 +1152,24 @@ void GeneralSolver::vcycle(const T *r, T *z) {
         }
         T *cur = xa;
         if (deg >= 2) {
-            kg_cheb_first2<T><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, xb, d, invth, (T)cheb_c1[1], (T)cheb_c2[1]);
+            { GTimer _gt(this, kname("kg_cheb_first2", l, sizeof(T) == 4), L.n); kg_cheb_first2<T><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, xb, d, invth, (T)cheb_c1[1], (T)cheb_c2[1]); }
             GLAUNCH();
             cur = xb;
             for (int k = 2; k < deg; k++) {
                 T *o = cur == xa ? xb : xa;
-                kg_cheb_step<T, false, false><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d, (T)cheb_c1[k],
-                                                                       (T)cheb_c2[k], rs);
+                { GTimer _gt(this, kname("kg_cheb_step", l, sizeof(T) == 4), L.n); kg_cheb_step<T, false, false><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d, (T)cheb_c1[k],
+                                                                       (T)cheb_c2[k], rs); }
                 GLAUNCH();
                 cur = o;
             }
         } else {
-            kg_cheb_first<T><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, xa, d, invth);
+            { GTimer _gt(this, kname("kg_cheb_first", l, sizeof(T) == 4), L.n); kg_cheb_first<T><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, xa, d, invth); }
             GLAUNCH();
         }
         pre[l] = cur;
         GLevel &C = lv[l + 1];
-        kg_restrict<T><<<gblocks(C.n, nblocks), kBlock, 0, stream>>>(C.n, d_state, A, L.mrp, L.mci, b, cur,
-                                                                    (T *)C.work[2]);
+        { GTimer _gt(this, kname("kg_restrict", l, sizeof(T) == 4), C.n); kg_restrict<T><<<gblocks(C.n, nblocks), kBlock, 0, stream>>>(C.n, d_state, A, L.mrp, L.mci, b, cur,
+                                                                    (T *)C.work[2]); }
         GLAUNCH();
     }
     for (int l = nl - 2; l >= 0; l--) {
@@ -1104,7 +1179,7 @@ void GeneralSolver::vcycle(const T *r, T *z) {
         T *xa = (T *)L.work[0], *xb = (T *)L.work[1], *d = (T *)L.work[3];
         const unsigned g = gblocks(L.n, nblocks);
         T *cur = pre[l];
-        kg_prolong_add<T><<<g, kBlock, 0, stream>>>(L.n, d_state, L.agg, L.dir, cur, (const T *)C.work[1], sc);
+        { GTimer _gt(this, kname("kg_prolong_add", l, sizeof(T) == 4), L.n); kg_prolong_add<T><<<g, kBlock, 0, stream>>>(L.n, d_state, L.agg, L.dir, cur, (const T *)C.work[1], sc); }
         GLAUNCH();
         for (int k = 0; k < deg; k++) {
             const bool last = k == deg - 1;
@@ -1113,15 +1188,15 @@ void GeneralSolver::vcycle(const T *r, T *z) {
             if (l == 0 && last) {
                 // the fused reduction needs the level-0 grid used by every other reduction
                 if (k == 0)
-                    kg_cheb_step<T, true, true><<<nblocks, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d, c1, c2, rs);
+                    { GTimer _gt(this, kname("kg_cheb_step", l, sizeof(T) == 4), L.n); kg_cheb_step<T, true, true><<<nblocks, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d, c1, c2, rs); }
                 else
-                    kg_cheb_step<T, true, false><<<nblocks, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d, c1, c2,
-                                                                                rs);
+                    { GTimer _gt(this, kname("kg_cheb_step", l, sizeof(T) == 4), L.n); kg_cheb_step<T, true, false><<<nblocks, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d, c1, c2,
+                                                                                rs); }
             } else {
                 if (k == 0)
-                    kg_cheb_step<T, false, true><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d, c1, c2, rs);
+                    { GTimer _gt(this, kname("kg_cheb_step", l, sizeof(T) == 4), L.n); kg_cheb_step<T, false, true><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d, c1, c2, rs); }
                 else
-                    kg_cheb_step<T, false, false><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d, c1, c2, rs);
+                    { GTimer _gt(this, kname("kg_cheb_step", l, sizeof(T) == 4), L.n); kg_cheb_step<T, false, false><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d, c1, c2, rs); }
             }
             GLAUNCH();
             cur = o;
@@ -1136,20 +1211,20 @@ void GeneralSolver::pcg(const T *b, T *x, double tol2) {
     T *r = (T *)cgv[0], *z = (T *)cgv[1], *pv = (T *)cgv[2], *q = (T *)cgv[3];
     GOp<double> A = gop<double>(L0);
     GCK(cudaMemsetAsync(d_count, 0, sizeof(int), stream));
-    kg_cg_start<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, A, L0.dir, b, x, r, tol2);
+    { GTimer _gt(this, kname("kg_cg_start", 0, sizeof(T) == 4), n); kg_cg_start<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, A, L0.dir, b, x, r, tol2); }
     GLAUNCH();
     vcycle<T>(r, z);
-    kg_update_p<<<nblocks, kBlock, 0, stream>>>(n, d_state, z, pv);
+    { GTimer _gt(this, kname("kg_update_p", 0, sizeof(T) == 4), n); kg_update_p<<<nblocks, kBlock, 0, stream>>>(n, d_state, z, pv); }
     GLAUNCH();
     const int check = std::max(1, opt.check_every);
     for (int it = 1; it <= opt.maxiter + 1; it++) {
-        kg_spmv_pq<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, A, pv, q);
+        { GTimer _gt(this, kname("kg_spmv_pq", 0, sizeof(T) == 4), n); kg_spmv_pq<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, A, pv, q); }
         GLAUNCH();
-        kg_update_xr<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, x, r, pv, q, opt.maxiter);
+        { GTimer _gt(this, kname("kg_update_xr", 0, sizeof(T) == 4), n); kg_update_xr<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, x, r, pv, q, opt.maxiter); }
         GLAUNCH();
         if (it % check == 0 && read_active() <= 0) return;
         vcycle<T>(r, z);
-        kg_update_p<<<nblocks, kBlock, 0, stream>>>(n, d_state, z, pv);
+        { GTimer _gt(this, kname("kg_update_p", 0, sizeof(T) == 4), n); kg_update_p<<<nblocks, kBlock, 0, stream>>>(n, d_state, z, pv); }
         GLAUNCH();
     }
 }
@@ -1160,31 +1235,31 @@ void GeneralSolver::df_pcg(const double *b, double *x, double tol2) {
     float *r32 = (float *)cgv[0], *z32 = (float *)cgv[1];
     GOp<double> A = gop<double>(L0);
     GCK(cudaMemsetAsync(d_count, 0, sizeof(int), stream));
-    kg_df_residual<true><<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, A, L0.dir, b, x, r64, tol2,
-                                                         opt.maxiter, opt.max_outer);
+    { GTimer _gt(this, kname("kg_df_residual", 0, false), n); kg_df_residual<true><<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, A, L0.dir, b, x, r64, tol2,
+                                                         opt.maxiter, opt.max_outer); }
     GLAUNCH();
     const int check = std::max(1, opt.check_every);
     for (int round = 0; round < opt.max_outer && read_active() > 0; round++) {
-        kg_df_begin<<<nblocks, kBlock, 0, stream>>>(n, d_state, r64, dfv[1], r32);
+        { GTimer _gt(this, kname("kg_df_begin", 0, false), n); kg_df_begin<<<nblocks, kBlock, 0, stream>>>(n, d_state, r64, dfv[1], r32); }
         GLAUNCH();
         vcycle<float>(r32, z32);
-        kg_df_update_p<<<nblocks, kBlock, 0, stream>>>(n, d_state, z32, dfv[2]);
+        { GTimer _gt(this, kname("kg_df_update_p", 0, true), n); kg_df_update_p<<<nblocks, kBlock, 0, stream>>>(n, d_state, z32, dfv[2]); }
         GLAUNCH();
         for (int it = 1; it <= opt.maxiter + 1; it++) {
-            kg_df_spmv_pq<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, L0.rp, L0.ci, vdf, leakdf, dfv[2],
-                                                          dfv[3]);
+            { GTimer _gt(this, kname("kg_df_spmv_pq", 0, true), n); kg_df_spmv_pq<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, L0.rp, L0.ci, vdf, leakdf, dfv[2],
+                                                          dfv[3]); }
             GLAUNCH();
-            kg_df_update_xr<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, x, dfv[1], r32, dfv[2],
-                                                            dfv[3], opt.maxiter);
+            { GTimer _gt(this, kname("kg_df_update_xr", 0, true), n); kg_df_update_xr<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, x, dfv[1], r32, dfv[2],
+                                                            dfv[3], opt.maxiter); }
             GLAUNCH();
             if (it % check == 0 && read_active() <= 0) break;
             vcycle<float>(r32, z32);
-            kg_df_update_p<<<nblocks, kBlock, 0, stream>>>(n, d_state, z32, dfv[2]);
+            { GTimer _gt(this, kname("kg_df_update_p", 0, true), n); kg_df_update_p<<<nblocks, kBlock, 0, stream>>>(n, d_state, z32, dfv[2]); }
             GLAUNCH();
         }
         GCK(cudaMemsetAsync(d_count, 0, sizeof(int), stream));
-        kg_df_residual<false><<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, A, L0.dir, b, x, r64, tol2,
-                                                              opt.maxiter, opt.max_outer);
+        { GTimer _gt(this, kname("kg_df_residual", 0, false), n); kg_df_residual<false><<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, A, L0.dir, b, x, r64, tol2,
+                                                              opt.maxiter, opt.max_outer); }
         GLAUNCH();
     }
 }

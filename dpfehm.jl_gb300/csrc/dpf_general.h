@@ -70,9 +70,16 @@ public:
     int stats_iters = 0, stats_outer = 0;
     double stats_relres = 0.0;
     long long launches = 0;
+    // per-kernel timing (dpf_profile): event pairs around the iteration kernels while on
+    bool prof_on = false;
+    std::vector<ProfRec> prof_recs;
+    std::vector<cudaEvent_t> ev_pool;
+    void profile(bool on);
+    int profile_report(int cap, const char **names, long long *counts, double *ms, long long *cells);
     std::string last_message;
 
 private:
+    friend struct GTimer;
     void setup_topology(const int64_t *a, const int64_t *b, const double *aol, const double *volumes, long long nd,
                         const int64_t *dn);
     void build_hierarchy();

@@ -132,3 +132,87 @@ def addboundaryconditions(hfree, dirichletnodes, dirichleths, isfreenode, nodei2
     h = np.array(dirichleths, dtype=np.float64, copy=True)
     h[isfreenode] = np.asarray(hfree)[nodei2freenodei[isfreenode]]
     return h
+
+
+def fracture_network(nfrac, L, h, seed, smin=None, smax=None, alpha=2.6, aperture=1e-3):
+    """A seeded synthetic discrete fracture network mesh, a stand-in for the dfnWorks meshes that
+    DPFEHM reads with load_uge (examples/fracture_network_solver_scaling): square planar fractures
+    with power-law side lengths (density s^-alpha on [smin, smax]), uniform centres in [0, L]^3 and
+    uniformly random orientations, each meshed as a 2-D grid of cells of spacing h. Cells of one
+    fracture are joined to their four in-plane neighbours (area h * aperture, length h); where two
+    fractures cross, every cell of one that lies within h / 2 of the other's plane and inside it is
+    joined to the nearest cell of the other (area h * aperture over the distance between the two
+    centres, at least h / 2). Only the largest connected component is kept.
+
+    Returns coords (3, N), volumes (N), neighbors (F, 2; 0-based), areas (F) and lengths (F) as
+    load_uge does (areasoverlengths = areas / lengths), and the fracture of every cell (N). Degrees
+    run from 2 at fracture corners to far above the in-plane four on cells that many fractures cross.
+    """
+    rng = np.random.default_rng(seed)
+    smin = 4.0 * h if smin is None else smin
+    smax = 0.5 * L if smax is None else smax
+    a1 = 1.0 - alpha
+    s = (smin ** a1 + rng.uniform(size=nfrac) * (smax ** a1 - smin ** a1)) ** (1.0 / a1)
+    cen = rng.uniform(0.0, L, (nfrac, 3))
+    nrm = rng.standard_normal((nfrac, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    ref = np.where(np.abs(nrm[:, :1]) < 0.9, np.array([[1.0, 0.0, 0.0]]), np.array([[0.0, 1.0, 0.0]]))
+    u = np.cross(nrm, ref)
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    v = np.cross(nrm, u)
+    th = rng.uniform(0, 2 * np.pi, nfrac)[:, None]
+    u, v = np.cos(th) * u + np.sin(th) * v, -np.sin(th) * u + np.cos(th) * v
+    m = np.maximum(2, np.round(s / h).astype(np.int64))  # cells per side
+    off = np.concatenate([[0], np.cumsum(m * m)])
+    N0 = int(off[-1])
+    frac = np.repeat(np.arange(nfrac), m * m)
+    loc = np.arange(N0) - off[frac]
+    ii, jj = loc // m[frac], loc % m[frac]
+    half = 0.5 * m[frac]
+    coords = (cen[frac] + ((ii + 0.5 - half) * h)[:, None] * u[frac] + ((jj + 0.5 - half) * h)[:, None] * v[frac])
+    # in-plane neighbours
+    ex, ey = np.nonzero(ii < m[frac] - 1)[0], np.nonzero(jj < m[frac] - 1)[0]
+    a_list, b_list, kind = [ex, ey], [ex + m[frac[ex]], ey + 1], [np.zeros(len(ex), bool), np.zeros(len(ey), bool)]
+    # crossings: candidate pairs whose bounding spheres overlap
+    rad = 0.5 * np.sqrt(2.0) * m * h
+    for A in range(nfrac):
+        d = np.linalg.norm(cen - cen[A], axis=1)
+        cand = np.nonzero((d < rad + rad[A]) & (np.arange(nfrac) != A))[0]
+        if len(cand) == 0:
+            continue
+        cells = np.arange(off[A], off[A + 1])
+        for B in cand:
+            rel = coords[cells] - cen[B]
+            dist = rel @ nrm[B]
+            pu, pv = rel @ u[B], rel @ v[B]
+            hb = 0.5 * m[B] * h
+            near = (np.abs(dist) < 0.5 * h) & (np.abs(pu) < hb) & (np.abs(pv) < hb)
+            if not near.any():
+                continue
+            ib = np.clip(np.floor(pu[near] / h + 0.5 * m[B]).astype(np.int64), 0, m[B] - 1)
+            jb = np.clip(np.floor(pv[near] / h + 0.5 * m[B]).astype(np.int64), 0, m[B] - 1)
+            a_list.append(cells[near])
+            b_list.append(off[B] + ib * m[B] + jb)
+            kind.append(np.ones(int(near.sum()), bool))
+    a, b, cross = np.concatenate(a_list), np.concatenate(b_list), np.concatenate(kind)
+    # one face per unordered pair
+    lo, hi = np.minimum(a, b), np.maximum(a, b)
+    _, first = np.unique(lo * N0 + hi, return_index=True)
+    lo, hi, cross = lo[first], hi[first], cross[first]
+    # the largest connected component
+    import scipy.sparse as sp
+    from scipy.sparse.csgraph import connected_components
+    G = sp.coo_matrix((np.ones(len(lo)), (lo, hi)), shape=(N0, N0))
+    _, lab = connected_components(G, directed=False)
+    keep = lab == np.argmax(np.bincount(lab))
+    newid = np.full(N0, -1, np.int64)
+    newid[keep] = np.arange(int(keep.sum()))
+    ek = keep[lo] & keep[hi]
+    nb = np.stack([newid[lo[ek]], newid[hi[ek]]], axis=1)
+    coords = np.ascontiguousarray(coords[keep].T)
+    lengths = np.sqrt(((coords[:, nb[:, 0]] - coords[:, nb[:, 1]]) ** 2).sum(axis=0))
+    lengths = np.where(cross[ek], np.maximum(lengths, 1e-9 * h), h)
+    # crossings: area over length = h aperture / max(length, h / 2)
+    areas = np.where(cross[ek], h * aperture * lengths / np.maximum(lengths, 0.5 * h), h * aperture)
+    volumes = np.full(coords.shape[1], h * h * aperture)
+    return coords, volumes, nb, areas, lengths, frac[keep]

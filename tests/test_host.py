@@ -71,6 +71,34 @@ def test_uge_roundtrip(pkg, tmp_path):
     assert np.allclose(l2, np.sqrt(((coords[:, nb[:, 0]] - coords[:, nb[:, 1]]) ** 2).sum(0)))
 
 
+def test_fracture_network_mesh(pkg, tmp_path):
+    """The synthetic fracture network: seeded (same seed, same mesh), one connected component,
+    irregular degrees (cells that several fractures cross have more than four neighbours), every
+    face between two fractures' cells or two in-plane neighbours, and a .uge round trip that
+    reproduces the areas over lengths the solver uses."""
+    import scipy.sparse as sp
+    from scipy.sparse.csgraph import connected_components
+    c, vol, nb, ar, ln, fr = pkg.grid.fracture_network(1000, 100.0, 1.0, 3)
+    c2, _, nb2, ar2, _, _ = pkg.grid.fracture_network(1000, 100.0, 1.0, 3)
+    assert np.array_equal(nb, nb2) and np.array_equal(ar, ar2) and np.array_equal(c, c2)
+    N = c.shape[1]
+    assert N > 50000 and len(np.unique(fr)) > 100
+    G = sp.coo_matrix((np.ones(len(nb)), (nb[:, 0], nb[:, 1])), shape=(N, N))
+    assert connected_components(G, directed=False)[0] == 1
+    deg = np.bincount(nb.ravel(), minlength=N)
+    assert deg.min() >= 1 and deg.max() >= 7 and (deg > 4).sum() > 1000
+    assert np.all(nb[:, 0] < nb[:, 1]) and len(np.unique(nb[:, 0] * N + nb[:, 1])) == len(nb)
+    cross = fr[nb[:, 0]] != fr[nb[:, 1]]
+    assert cross.any() and np.allclose(ln[~cross], 1.0) and np.all(ar / ln > 0)
+    sub = np.nonzero((nb < 3000).all(axis=1))[0]  # a small piece for the file round trip
+    keep = np.unique(nb[sub])
+    f = tmp_path / "dfn.uge"
+    pkg.grid.write_uge(str(f), c[:, :3000], vol[:3000], nb[sub], ar[sub])
+    c3, v3, nb3, a3, l3 = pkg.load_uge(str(f))
+    assert np.array_equal(nb3, nb[sub]) and np.allclose(a3 / l3, ar[sub] / ln[sub], rtol=1e-12)
+    assert keep.size > 0
+
+
 def test_matern_field_statistics(pkg):
     f = pkg.fields.matern_field((200, 200), (0.5, 0.5), 5.0, 2.0, -9.0, seed=3)
     assert f.shape == (200, 200)
