@@ -1188,13 +1188,13 @@ void GeneralSolver::vcycle(const T *r, T *z) {
             if (l == 0 && last) {
                 // the fused reduction needs the level-0 grid used by every other reduction
                 if (k == 0)
-                    { GTimer _gt(this, kname("kg_cheb_step", l, sizeof(T) == 4), L.n); kg_cheb_step<T, true, true><<<nblocks, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d, c1, c2, rs); }
+                    { GTimer _gt(this, kname("kg_cheb_step0", l, sizeof(T) == 4), L.n); kg_cheb_step<T, true, true><<<nblocks, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d, c1, c2, rs); }
                 else
                     { GTimer _gt(this, kname("kg_cheb_step", l, sizeof(T) == 4), L.n); kg_cheb_step<T, true, false><<<nblocks, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d, c1, c2,
                                                                                 rs); }
             } else {
                 if (k == 0)
-                    { GTimer _gt(this, kname("kg_cheb_step", l, sizeof(T) == 4), L.n); kg_cheb_step<T, false, true><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d, c1, c2, rs); }
+                    { GTimer _gt(this, kname("kg_cheb_step0", l, sizeof(T) == 4), L.n); kg_cheb_step<T, false, true><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d, c1, c2, rs); }
                 else
                     { GTimer _gt(this, kname("kg_cheb_step", l, sizeof(T) == 4), L.n); kg_cheb_step<T, false, false><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, o, d, c1, c2, rs); }
             }
