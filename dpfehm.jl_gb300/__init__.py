@@ -417,10 +417,42 @@ class GroundwaterBatch(GroundwaterProblem):
             lib.dpf_batch_offsets(self._h, p, ctypes.byref(co), ctypes.byref(fo))
             self.cell_offsets[p], self.face_offsets[p] = co.value, fo.value
 
+    def sample_logk(self, seeds, ell, sigma, mean=-9.0, nmodes=512, out=None):
+        """Seeded Matern(nu = 1) log-conductivity fields for every problem, drawn on the GPU
+        (dpf_batch_sample_logk): one seed, correlation length, sigma and mean per problem (scalars
+        are broadcast). With out=None the fields stay in the handle for solve_grad_logk(None, ...);
+        out may be "cuda" (a new torch CUDA tensor), "host" (a new numpy array) or a float64 buffer."""
+        lib = self._lib
+        sd = np.ascontiguousarray(np.broadcast_to(np.asarray(seeds, dtype=np.uint64), (self.nprob,)))
+        el, sg, mu = (np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.float64), (self.nprob,)))
+                      for v in (ell, sigma, mean))
+        res, ptr = None, None
+        if isinstance(out, str):
+            if out == "cuda":
+                import torch
+                res = torch.empty(self.N, dtype=torch.float64, device="cuda")
+                ptr = res.data_ptr()
+            elif out == "host":
+                res = np.empty(self.N)
+                ptr = res.ctypes.data
+            else:
+                raise ValueError("out must be None, 'cuda', 'host' or a float64 buffer")
+        elif out is not None:
+            res, ptr = _out_into(out, None, self.N)
+        _check(lib, self._h, lib.dpf_batch_sample_logk(self._h, int(nmodes), sd.ctypes.data, el.ctypes.data,
+                                                       sg.ctypes.data, mu.ctypes.data, ptr))
+        return res
+
     def solve_grad_logk(self, logK, dirichleths, Qs, obs_per_problem, mean="geometric", out=None):
         """Forward solves, J_p = sum(h_p[obs_p]^2), adjoints for every problem; returns the
-        concatenated (h, dJ/dlogK). `out` = (h, g) writes into the caller's buffers."""
-        lk = _Buf(logK, n=self.N)
+        concatenated (h, dJ/dlogK). `out` = (h, g) writes into the caller's buffers. logK=None
+        solves on the fields last drawn into the handle by sample_logk (outputs on the device)."""
+        if logK is None:
+            import torch
+            lk = _Buf(torch.empty(0, dtype=torch.float64, device="cuda"))
+            lk.ptr, lk.size = None, self.N
+        else:
+            lk = _Buf(logK, n=self.N)
         d = _Buf(dirichleths, n=self.N)
         q = _Buf(Qs, n=self.N)
         if len(obs_per_problem) != self.nprob:

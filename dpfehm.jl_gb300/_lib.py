@@ -79,6 +79,7 @@ SIGNATURES = {
                                         ctypes.POINTER(_vp)]),
     "dpf_batch_offsets": (ctypes.c_int, [_vp, ctypes.c_int, _i64p, _i64p]),
     "dpf_batch_solve_grad_logk": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "dpf_batch_sample_logk": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
     "dpf_solve_grad_logk": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, _vp, _i64, _vp, _vp, _vp]),
     "dpf_apply_operator": (ctypes.c_int, [_vp, _vp, _vp]),
     "dpf_profile": (ctypes.c_int, [_vp, ctypes.c_int]),

@@ -924,7 +924,7 @@ static int split_solve_grad_logk(dpf_problem *P, const double *logK, int kind, c
     DeviceGuard g(P->device);
     const int k = (int)P->parts.size();
     const int nprob = P->part_first[k];
-    if (!logK || !dh || !Qs || !obs_offsets) { P->err = "invalid arguments"; return DPF_BAD_INPUT; }
+    if (!dh || !Qs || !obs_offsets) { P->err = "invalid arguments"; return DPF_BAD_INPUT; }
     for (int p = 0; p < nprob; p++)
         if (obs_offsets[p] < 0 || obs_offsets[p + 1] < obs_offsets[p]) {
             P->err = "obs_offsets must be non-decreasing";
@@ -948,7 +948,7 @@ static int split_solve_grad_logk(dpf_problem *P, const double *logK, int kind, c
             rcs[i] = DPF_CUDA;
             return;
         }
-        rcs[i] = dpf_batch_solve_grad_logk(Q, logK + c0, kind, dh + c0, Qs + c0, offs[i].data(),
+        rcs[i] = dpf_batch_solve_grad_logk(Q, logK ? logK + c0 : nullptr, kind, dh + c0, Qs + c0, offs[i].data(),
                                            obs ? obs + obs_offsets[p0] : nullptr, h_out ? h_out + c0 : nullptr,
                                            dlogK ? dlogK + c0 : nullptr);
         if (cudaEventRecord(P->part_events[i], Q->stream) != cudaSuccess) {
@@ -970,14 +970,66 @@ static int split_solve_grad_logk(dpf_problem *P, const double *logK, int kind, c
     return rc;
 }
 
+// Draws into part or handle Q's own field buffer, and copies to out (host or device) when given.
+static int sample_into(dpf_problem *Q, int nmodes, const uint64_t *seeds, const double *ell, const double *sigma,
+                       const double *mean, double *out) {
+    return guarded(Q, "dpf_batch_sample_logk", [&]() -> int {
+        StructBatch &S = *Q->sb;
+        static_assert(sizeof(uint64_t) == sizeof(unsigned long long), "seed width");
+        const bool direct = out && is_device_ptr(out);
+        S.have_sampled = false;
+        S.sample_logk(nmodes, (const unsigned long long *)seeds, ell, sigma, mean, direct ? out : S.in_logK);
+        if (!direct) {
+            S.have_sampled = true;
+            if (out) stage_out(Q, out, S.in_logK, S.N);
+        }
+        return DPF_OK;
+    });
+}
+
+int dpf_batch_sample_logk(dpf_problem *P, int nmodes, const uint64_t *seeds, const double *ell, const double *sigma,
+                          const double *mean, double *logK) {
+    if (!P) return DPF_BAD_INPUT;
+    if (!seeds || !ell || !sigma || !mean) {
+        P->err = "seeds, ell, sigma and mean are required (one per problem)";
+        return DPF_BAD_INPUT;
+    }
+    if (P->gs) {
+        P->err = "the sampler needs a regular-grid handle";
+        return DPF_UNSUPPORTED;
+    }
+    if (P->parts.empty()) return sample_into(P, nmodes, seeds, ell, sigma, mean, logK);
+    DeviceGuard g(P->device);
+    for (size_t i = 0; i < P->parts.size(); i++) {
+        const int p0 = P->part_first[i];
+        int64_t c0, f0;
+        part_base(P, (int)i, c0, f0);
+        const int rc = sample_into(P->parts[i], nmodes, seeds + p0, ell + p0, sigma + p0, mean + p0,
+                                   logK ? logK + c0 : nullptr);
+        if (rc != DPF_OK) {
+            P->err = P->parts[i]->err;
+            return rc;
+        }
+    }
+    return DPF_OK;
+}
+
 int dpf_batch_solve_grad_logk(dpf_problem *P, const double *logK, int kind, const double *dh, const double *Qs,
                               const int64_t *obs_offsets, const int64_t *obs, double *h_out, double *dlogK) {
     if (P && !P->parts.empty()) return split_solve_grad_logk(P, logK, kind, dh, Qs, obs_offsets, obs, h_out, dlogK);
     return guarded(P, __func__, [&]() -> int {
         if (!P->sb) throw BadInput("not a batch handle");
-        if (!logK || !dh || !Qs || !obs_offsets) throw BadInput("invalid arguments");
+        if (!dh || !Qs || !obs_offsets) throw BadInput("invalid arguments");
         if (kind != DPF_MEAN_GEOMETRIC && kind != DPF_MEAN_HARMONIC) throw BadInput("unknown mean kind");
         StructBatch &S = *P->sb;
+        if (!logK) {
+            // the fields last drawn into the handle by dpf_batch_sample_logk
+            if (!S.have_sampled) {
+                P->err = "logK is NULL but no fields were drawn into the handle (dpf_batch_sample_logk)";
+                return DPF_STATE;
+            }
+            logK = S.in_logK;
+        }
         std::vector<long long> og;
         for (int p = 0; p < S.nprob; p++) {
             int64_t a = obs_offsets[p], b = obs_offsets[p + 1];

@@ -90,6 +90,7 @@ struct ProbParam {                 // per-problem constants of a regular grid
     double vol;                    // cell volume (transient storage term)
     long long face_off;            // offset of the problem's faces in concatenated face arrays
     long long F;                   // faces of the problem
+    double x0[3], dx[3];           // node coordinates: x0 + i dx per axis (regulargrid3d's)
 };
 
 // Storage type of the operator coefficients of a level whose vectors are T. FP64 levels

@@ -1487,6 +1487,10 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         P.aol[2] = dxyz[0] * dxyz[1] / dxyz[2];
         if (g.aol_override) for (int k = 0; k < 3; k++) P.aol[k] = g.aol[k];
         P.vol = g.vol_override ? g.vol : dxyz[0] * dxyz[1] * dxyz[2];
+        for (int k = 0; k < 3; k++) {
+            P.x0[k] = g.mins[k];
+            P.dx[k] = dxyz[k];
+        }
         long long Fp = 3LL * nx * ny * nz - (long long)nx * ny - (long long)nx * nz - (long long)ny * nz;
         P.face_off = foff;
         P.F = Fp;
@@ -2548,6 +2552,8 @@ void StructBatch::adjoint_solve() {
     zero_guess = true;
     solve(arhs, lam, opt.reltol);
 }
+
+void *StructBatch::dalloc_bytes(size_t bytes) { return (void *)dalloc<char>(bytes, owned); }
 
 long long *StructBatch::obs_buffer(size_t n) {
     if (n > obs_cap || !d_obs_buf) {

@@ -120,6 +120,10 @@ public:
     template <typename T>
     void launch_tail(const TailParams<T> &tp);
     void write_tail_table();
+    // Matern(nu = 1) log-conductivity fields of every problem, drawn on the device (dpf_sampler.cu)
+    void sample_logk(int nmodes, const unsigned long long *seeds, const double *ell, const double *sigma,
+                     const double *mean, double *out);
+    void *dalloc_bytes(size_t bytes);  // a device allocation owned by the batch
     template <typename T>
     void pm_restrict(int l, const T *b, const T *x, T *bc);
     template <typename T>
@@ -169,6 +173,10 @@ public:
     // fused tail: per problem {p, first tail level, coarsest level, 0}; per-level pointer table
     // (TailLevel of the V-cycle precision) written at construction by write_tail_table
     bool zero_guess = false;  // the next solve starts from 0 (Dirichlet values on identity rows)
+    // sampler state: per-problem parameters (device and pinned staging) and the modes of the last draw
+    void *d_sample = nullptr, *h_sample = nullptr, *d_modes = nullptr;
+    long long modes_cap = 0;
+    bool have_sampled = false;  // in_logK holds fields drawn by sample_logk
     // device buffer for observation indices, kept between calls (no allocation per call)
     long long *obs_buffer(size_t n);
     long long *d_obs_buf = nullptr;

@@ -198,10 +198,25 @@ int dpf_batch_offsets(const dpf_problem *h, int p, int64_t *cell_offset, int64_t
 /* Forward + adjoint of every problem from concatenated logK; delta for the
  * adjoint is J_p = sum_k h_p[obs]^2 over each problem's observation cells
  * (obs_offsets[nprob+1] into obs, local indices). Outputs h[N_total] and
- * dlogK[N_total] (either may be NULL). */
+ * dlogK[N_total] (either may be NULL). logK NULL: the fields last drawn into the
+ * handle by dpf_batch_sample_logk (DPF_STATE if there are none). */
 int dpf_batch_solve_grad_logk(dpf_problem *h, const double *logK, int mean_kind, const double *dirichleths,
                               const double *Qs, const int64_t *obs_offsets, const int64_t *obs, double *h_out,
                               double *dlogK);
+
+/* Seeded Gaussian log-conductivity fields with Matern (nu = 1) covariance for every problem of a
+ * regular-grid batch, drawn on the GPU (the inverse and uncertainty-quantification drivers' field
+ * step, examples/gw_multigrid_inverse/inputdeck.jl:58-105, where the reference samples on the host):
+ * logK_p(x) = mean[p] + sigma[p] sqrt(2/M) sum_k cos(w_k . x + phi_k) over M = nmodes modes, with the
+ * frequencies drawn from the Matern spectral density for correlation length ell[p] (the convention
+ * (2/ell^2 + |w|^2)^-(5/2) of the package's FFT sampler) and the phases uniform, from the
+ * counter-based Philox4x32-10 generator keyed by seeds[p]: a field depends only on its seed, grid
+ * and nmodes (1..65536), and repeats bit for bit. Cells sit at the grid's node coordinates (integer
+ * indices for a grid detected from a face list). logK[N_total] (host or device) receives the
+ * fields; with logK NULL they stay in the handle, and dpf_batch_solve_grad_logk with a NULL logK
+ * solves on them, so a draw-solve-differentiate loop has no host step for the fields. */
+int dpf_batch_sample_logk(dpf_problem *h, int nmodes, const uint64_t *seeds, const double *ell, const double *sigma,
+                          const double *mean, double *logK);
 
 /* Autotuner for a batch (same arguments as dpf_batch_create and dpf_batch_solve_grad_logk):
  * coordinate descent over the Chebyshev degree, plane_cells, plane_blocks_per_sm,

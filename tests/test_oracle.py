@@ -218,3 +218,40 @@ def test_oracle_1m_accuracy_floor(orc, pkg):
     finally:
         orc.set_threads(1)
     assert rel(h1, h2) < 1e-9
+
+
+def test_philox_known_answers():
+    """The sampler checker's Philox4x32-10 against the generator's published known-answer vectors."""
+    import matern_oracle as mo
+    kat = [((0, 0, 0, 0), (0, 0), (0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8)),
+           ((0xffffffff,) * 4, (0xffffffff,) * 2, (0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd)),
+           ((0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344), (0xa4093822, 0x299f31d0),
+            (0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1))]
+    for ctr, key, want in kat:
+        got = mo.philox4x32_10(*ctr, *key)
+        assert tuple(int(x) for x in got) == want
+
+
+def test_matern_sampler_restatement_statistics():
+    """The spectral-synthesis method (the GPU sampler's, restated in float64): mean, variance and
+    the Matern (nu = 1) correlation at several lags, over an ensemble of seeds."""
+    import matern_oracle as mo
+    ell, sigma, mu, M = 4.0, 1.5, -9.0, 512
+    lags = np.array([1.0, 2.0, 4.0, 8.0])
+    vals, pairs = [], {lag: [] for lag in lags}
+    for seed in range(40):
+        w, phi = mo.modes(seed, ell, M)
+        pts = np.array([[0.0, 0.0, 0.0]] + [[lag, 0.0, 0.0] for lag in lags])
+        f = mu + sigma * np.sqrt(2.0 / M) * np.cos(pts @ w.T + phi).sum(axis=1)
+        vals.append(f[0])
+        for j, lag in enumerate(lags):
+            pairs[lag].append((f[0] - mu) * (f[1 + j] - mu))
+    vals = np.array(vals)
+    assert abs(vals.mean() - mu) < 4 * sigma / np.sqrt(len(vals))
+    # exact second moments of the method (expectation over modes): E[f^2] - mu^2 = sigma^2 and
+    # E[(f(0)-mu)(f(r)-mu)] = sigma^2 E[cos(w . r)]; the characteristic function of the scale mixture
+    # is the Matern correlation, checked here by the mode average over all seeds
+    allw = np.concatenate([mo.modes(s, ell, M)[0] for s in range(40)])
+    for lag in lags:
+        emp = np.mean(np.cos(allw[:, 0] * lag))
+        assert abs(emp - mo.matern_correlation(lag, ell)) < 0.02, lag
