@@ -68,7 +68,7 @@ BYTES_PER_CELL = {
     "k_pm_step": lambda T: 4 * T + 4 * _coef(T),     # x, b, d, cx, cy, cz, leak in; x out (last step)
     "k_pm_prolong_step": lambda T: 4 * T + T / 8 + 1 + 4 * _coef(T),  # x, e/8, dir, b, 4 coeffs in; x, d out
     "k_df_residual0": lambda T: 17,            # b, dir in; r out
-    "k_pm_df_spmv": lambda T: 48,              # plane-marching form of k_df_spmv_pq
+    "k_pm_df_flux": lambda T: 48,              # plane-marching form of k_df_spmv_pq (each face flux once)
 }
 
 

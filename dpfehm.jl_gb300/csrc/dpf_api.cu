@@ -385,7 +385,7 @@ dpf_options fill_options(const dpf_options *o) {
     r.plane_cells = std::min(4, std::max(1, (r.plane_cells + 255) / 256)) * 256;
     if (r.plane_blocks_per_sm <= 0) r.plane_blocks_per_sm = d.plane_blocks_per_sm;
     if (r.df_plane_cells == 0) r.df_plane_cells = d.df_plane_cells;
-    if (r.df_plane_cells > 0) r.df_plane_cells = std::min(4, std::max(1, (r.df_plane_cells + 255) / 256)) * 256;
+    if (r.df_plane_cells > 0) r.df_plane_cells = 256;  // one cell per thread: the product's only slab size
     if (r.df_plane_blocks_per_sm <= 0) r.df_plane_blocks_per_sm = d.df_plane_blocks_per_sm;
     if (r.tail_cluster <= 0) r.tail_cluster = d.tail_cluster;
     r.tail_cluster = std::min(16, r.tail_cluster);
@@ -481,8 +481,8 @@ void dpf_default_options(dpf_options *o) {
     o->plane = 1;
     o->plane_cells = 1024;
     o->plane_blocks_per_sm = 2;
-    o->df_plane_cells = -1;
-    o->df_plane_blocks_per_sm = 4;
+    o->df_plane_cells = 256;
+    o->df_plane_blocks_per_sm = 8;
     o->tail_cluster = 1;
     o->plane_levels = 0;
     o->streams = 0;

@@ -681,35 +681,39 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_restrict(
     if (warp == kConsumerWarps && lane == 0) pm_drain<R>(issued, full, err);
 }
 
-// Double-float CG product q = A p (flux form, double-float coefficients) and the problem's
-// p . q (leading floats) on the plane ring; the arithmetic and its order are those of the
-// grid-stride k_df_spmv_pq. Streams per plane: p with halo rows, cx, cy (+ the row
-// below), cz, leak, all 8-byte double-float values. A block marches through its items like
-// k_pm_cheb; each item's partial of p . q has its own reduction slot.
+// Double-float CG product q = A p (flux form, double-float coefficients) and the problem's p . q
+// (leading floats), marching along x through the plane work items with every face flux computed
+// once. A cell computes the fluxes c_f (p_i - p_j) through its z+, y+ and x+ faces; the cell
+// above takes the z+ and y+ fluxes of the cell below it from shared memory (two buffers by plane
+// parity, so one block barrier per plane), and the x+ flux is carried in a register to the next
+// plane, where it is that cell's x- flux. A slab's first row computes its y- flux itself (the cell
+// below is in the slab underneath), and so does an item's first plane its x- flux.
+// The double-float difference and product are odd functions of their arguments (round to nearest
+// is symmetric and the two-sum error is exact), so the negated flux of a neighbour equals the
+// term the cell would compute itself, up to the sign of a zero: q is the six-face product of
+// k_df_spmv_pq term for term, with the terms summed in its order (z+, z-, y+, y-, x+, x-). The
+// leading-float p . q is summed per thread along x, so its rounding differs from k_df_spmv_pq's.
+// Global reads per cell: p of the next plane (once from HBM) and of the z+ and y+ neighbours
+// (loaded by those cells' threads a plane earlier, mostly cache hits), and the four coefficients.
+// Every value a plane needs is loaded into registers one plane ahead, so the loads of plane x + 1
+// are in flight while plane x is computed.
+#ifndef DPF_DF_FLUX_MINB
+#define DPF_DF_FLUX_MINB 4
+#endif
+struct FluxPlane {  // one cell's operands of one plane
+    float2 pz, py, pym, pn;  // p at z+1, y+1, y-1 (slab's first row only), x+1
+    float2 cz, cy, cym, cx, lk;
+};
 template <int CPT>
-__global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_df_spmv(
-    const LevelDesc *__restrict__ desc, PlaneWork work, CgState *st, int *active_count,
-    ReduceScratch rs, const int2 *__restrict__ pinfo, CoeffsDF C, const float2 *__restrict__ pv,
-    float2 *__restrict__ qv, PlaneLayout lay, int *err) {
+__global__ void __launch_bounds__(kPlaneThreads, (DPF_DF_FLUX_MINB / CPT > 0 ? DPF_DF_FLUX_MINB / CPT : 1))
+    k_pm_df_flux(const LevelDesc *__restrict__ desc, PlaneWork work, CgState *st, int *active_count,
+                 ReduceScratch rs, const int2 *__restrict__ pinfo, CoeffsDF C, const float2 *__restrict__ pv,
+                 float2 *__restrict__ qv) {
     pdl_enter();
-    constexpr int R = kPlaneStages;
-    constexpr int es = 8;
-    constexpr int kConsumerWarps = kPlaneThreads / 32;
-    extern __shared__ __align__(128) unsigned char sm[];
-    __shared__ uint64_t full[R], empty[R];
-
+    constexpr unsigned CF_YIN = 32u;  // the y- neighbour is inside the slab
+    __shared__ float2 fz_s[2][CPT * kPlaneThreads], fy_s[2][CPT * kPlaneThreads];
     const int t = threadIdx.x;
-    const int warp = t >> 5, lane = t & 31;
-    auto slot_of = [&](int g) { return (char *)sm + ((unsigned)g % (unsigned)R) * lay.slot_bytes; };
-    if (t == 0) {
-        for (int s = 0; s < R; s++) {
-            mbar_init(&full[s], 1);
-            mbar_init(&empty[s], kConsumerWarps);
-        }
-        fence_mbarrier_init();
-    }
-    __syncthreads();
-    int g0 = 0, issued = 0;
+    const float2 zero = make_float2(0.f, 0.f);
     for (int w = work.first[blockIdx.x]; w < work.first[blockIdx.x + 1]; w++) {
         const int4 it = work.items[w];
         const int p = it.x, y0 = it.y, xa = it.z, xe = it.w;
@@ -718,108 +722,103 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_df_spmv(
         const int nz = L.nz, ny = L.ny, nx = L.nx;
         const long long sx = (long long)ny * nz;
         const int Ty = plane_rows(ny, nz, CPT * kPlaneThreads);
-        const int rows = min(Ty, ny - y0);
-        const int ncell = rows * nz;
-        const int pl_lo = max(xa - 1, 0), pl_hi = min(xe, nx - 1);
-        const int h0 = max(y0 - 1, 0), h1 = min(y0 + rows + 1, ny);
-        auto gof = [&](int q) { return g0 + (q - pl_lo); };
-        Acc<float> part;
-        bool bad = false;
-
-        if (warp == kConsumerWarps) {
-            if (lane == 0) {
-                const int n = pm_produce<R>(pl_lo, pl_hi, g0, full, empty, sm, lay.slot_bytes, err,
-                                            [&](int q, char *slot, uint64_t *bar) {
-                    const long long pb = L.off + (long long)q * sx;
-                    const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
-                    const long long hA = pb + (long long)h0 * nz, hB = pb + (long long)h1 * nz, pE = lp + ncell;
-                    auto stage = [&](const void *base, long long l0, long long a0, long long a1, int off) {
-                        stage_range(bar, base, es, l0, a0, a1, slot + off, L.off, L.off + L.n, slot, lay.slot_bytes);
-                    };
-                    stage(pv, lh, hA, hB, lay.oX);
-                    stage(C.cx, lp, lp, pE, lay.oCX);
-                    stage(C.cy, lh, hA, pE, lay.oCY);
-                    stage(C.cz, lp, lp, pE, lay.oCZ);
-                    stage(C.leak, lp, lp, pE, lay.oLK);
-                });
-                issued += n;
-                bad = n != pl_hi - pl_lo + 1;
-            }
-            __syncwarp();
-        } else {
-            unsigned cfl[CPT];
+        const int ncell = min(Ty, ny - y0) * nz;
+        unsigned cfl[CPT];
+        long long ic[CPT];
+        float2 pi[CPT], fxm[CPT];
+        FluxPlane cur[CPT];
+        // the operands of the plane at ic (x < nx, so the x+1 load is guarded by x + 1 < nx)
+        auto fetch = [&](FluxPlane &o, unsigned f, long long i, int x) {
+            o.pz = (f & CF_ZP) ? pv[i + 1] : zero;
+            o.py = (f & CF_YP) ? pv[i + nz] : zero;
+            const bool ylo = (f & CF_YM) && !(f & CF_YIN);
+            o.pym = ylo ? pv[i - nz] : zero;
+            o.pn = x + 1 < nx ? pv[i + sx] : zero;
+            o.cz = (f & CF_ZP) ? C.cz[i] : zero;
+            o.cy = (f & CF_YP) ? C.cy[i] : zero;
+            o.cym = ylo ? C.cy[i - nz] : zero;
+            o.cx = x + 1 < nx ? C.cx[i] : zero;
+            o.lk = C.leak[i];
+        };
 #pragma unroll
-            for (int k = 0; k < CPT; k++) {
-                const int tc = t + k * kPlaneThreads;
-                unsigned f = 0;
-                if (tc < ncell) {
-                    const int ty = div_nz(L, tc), z = tc - ty * nz, y = y0 + ty;
-                    f = CF_VALID | (z + 1 < nz ? CF_ZP : 0u) | (z > 0 ? CF_ZM : 0u) | (y + 1 < ny ? CF_YP : 0u) |
-                        (y > 0 ? CF_YM : 0u);
+        for (int k = 0; k < CPT; k++) {
+            const int tc = t + k * kPlaneThreads;
+            unsigned f = 0;
+            ic[k] = L.off + (long long)xa * sx + (long long)y0 * nz + tc;
+            pi[k] = fxm[k] = zero;
+            if (tc < ncell) {
+                const int ty = div_nz(L, tc), z = tc - ty * nz, y = y0 + ty;
+                f = CF_VALID | (z + 1 < nz ? CF_ZP : 0u) | (z > 0 ? CF_ZM : 0u) | (y + 1 < ny ? CF_YP : 0u) |
+                    (y > 0 ? CF_YM : 0u) | (ty > 0 ? CF_YIN : 0u);
+#if DPF_CHECKED
+                // every neighbour the flags admit, on the item's first and last planes
+                for (int e = 0; e < 2 && f; e++) {
+                    const long long i = ic[k] + (e ? (long long)(xe - 1 - xa) * sx : 0);
+                    const int x = e ? xe - 1 : xa;
+                    if (!(DPF_INSIDE(CK_NEIGHBOUR, i, L.off, L.off + L.n) &&
+                          DPF_INSIDE(CK_NEIGHBOUR, (f & CF_ZP) ? i + 1 : i, L.off, L.off + L.n) &&
+                          DPF_INSIDE(CK_NEIGHBOUR, (f & CF_YP) ? i + nz : i, L.off, L.off + L.n) &&
+                          DPF_INSIDE(CK_NEIGHBOUR, (f & CF_YM) ? i - nz : i, L.off, L.off + L.n) &&
+                          DPF_INSIDE(CK_NEIGHBOUR, x + 1 < nx ? i + sx : i, L.off, L.off + L.n) &&
+                          DPF_INSIDE(CK_NEIGHBOUR, x > 0 ? i - sx : i, L.off, L.off + L.n)))
+                        f = 0;
                 }
-                cfl[k] = f;
+#endif
             }
-            int waited = pl_lo - 1, released = pl_lo;
-            for (int x = xa; x < xe && !bad; x++) {
-                const int need = min(x + 1, pl_hi);
-                while (waited < need) {
-                    const int g = gof(waited + 1);
-                    if (!mbar_wait(&full[g % R], (uint32_t)((g / R) & 1), err)) {
-                        bad = true;
-                        break;
-                    }
-                    waited++;
-                }
-                if (bad) break;
-                const long long pb = L.off + (long long)x * sx;
-                const long long lh = pb + (long long)(y0 - 1) * nz, lp = pb + (long long)y0 * nz;
-                const int dh = stage_delta(lh, es), dp = stage_delta(lp, es);
-                char *sc = slot_of(gof(x));
-                const bool xp = x + 1 < nx, xm = x > 0;
-                char *sn = xp ? slot_of(gof(x + 1)) : sc;
-                char *sq = xm ? slot_of(gof(x - 1)) : sc;
-                const float2 *P = (const float2 *)(sc + lay.oX) + dh;
-                const float2 *CX = (const float2 *)(sc + lay.oCX) + dp;
-                const float2 *CY = (const float2 *)(sc + lay.oCY) + dh;
-                const float2 *CZ = (const float2 *)(sc + lay.oCZ) + dp;
-                const float2 *LK = (const float2 *)(sc + lay.oLK) + dp;
-                const float2 *Pn = (const float2 *)(sn + lay.oX) + (xp ? stage_delta(lh + sx, es) : dh);
-                const float2 *Pq = (const float2 *)(sq + lay.oX) + (xm ? stage_delta(lh - sx, es) : dh);
-                const float2 *CXq = (const float2 *)(sq + lay.oCX) + (xm ? stage_delta(lp - sx, es) : dp);
-#pragma unroll
-                for (int k = 0; k < CPT; k++) {
-                    const unsigned f = cfl[k];
-                    if (!(f & CF_VALID)) continue;
-                    const int tc = t + k * kPlaneThreads;
-                    const int c = nz + tc;
-                    const float2 pi = P[c];
-                    float2 a = df_mul(LK[tc], pi);
-                    if (f & CF_ZP) a = df_add(a, df_mul(CZ[tc], df_sub(pi, P[c + 1])));
-                    if (f & CF_ZM) a = df_add(a, df_mul(CZ[tc - 1], df_sub(pi, P[c - 1])));
-                    if (f & CF_YP) a = df_add(a, df_mul(CY[c], df_sub(pi, P[c + nz])));
-                    if (f & CF_YM) a = df_add(a, df_mul(CY[tc], df_sub(pi, P[c - nz])));
-                    if (xp) a = df_add(a, df_mul(CX[tc], df_sub(pi, Pn[c])));
-                    if (xm) a = df_add(a, df_mul(CXq[tc], df_sub(pi, Pq[c])));
-                    qv[lp + tc] = a;
-                    part = part + Acc<float>::prod(pi.x, a.x);
-                }
-                __syncwarp();
-                if (lane == 0 && x - 1 >= released) mbar_arrive(&empty[gof(x - 1) % R]);
-                released = max(released, x);
-            }
-            if (!bad) {
-                __syncwarp();
-                for (int q = released; q <= waited; q++)
-                    if (lane == 0) mbar_arrive(&empty[gof(q) % R]);
+            cfl[k] = f;
+            if (f) {
+                pi[k] = pv[ic[k]];
+                fetch(cur[k], f, ic[k], xa);
+                if (xa > 0) fxm[k] = df_mul(C.cx[ic[k] - sx], df_sub(pv[ic[k] - sx], pi[k]));
             }
         }
-        g0 += pl_hi - pl_lo + 1;
+        Acc<float> part;
+        for (int x = xa; x < xe; x++) {
+            const bool xp = x + 1 < nx, xm = x > 0;
+            float2 *fzb = fz_s[x & 1], *fyb = fy_s[x & 1];
+            float2 fz[CPT], fy[CPT], fx[CPT];
+            FluxPlane nxt[CPT];
+#pragma unroll
+            for (int k = 0; k < CPT; k++) {
+                const unsigned f = cfl[k];
+                const int tc = t + k * kPlaneThreads;
+                fz[k] = fy[k] = fx[k] = zero;
+                if (!f) continue;
+                if (x + 1 < xe) fetch(nxt[k], f, ic[k] + sx, x + 1);
+                const FluxPlane &o = cur[k];
+                if (f & CF_ZP) fz[k] = df_mul(o.cz, df_sub(pi[k], o.pz));
+                if (f & CF_YP) fy[k] = df_mul(o.cy, df_sub(pi[k], o.py));
+                if (xp) fx[k] = df_mul(o.cx, df_sub(pi[k], o.pn));
+                fzb[tc] = fz[k];
+                fyb[tc] = fy[k];
+            }
+            __syncthreads();
+#pragma unroll
+            for (int k = 0; k < CPT; k++) {
+                const unsigned f = cfl[k];
+                const int tc = t + k * kPlaneThreads;
+                if (!f) continue;
+                const FluxPlane &o = cur[k];
+                float2 a = df_mul(o.lk, pi[k]);
+                if (f & CF_ZP) a = df_add(a, fz[k]);
+                if (f & CF_ZM) a = df_sub(a, fzb[tc - 1]);
+                if (f & CF_YP) a = df_add(a, fy[k]);
+                if (f & CF_YM) a = (f & CF_YIN) ? df_sub(a, fyb[tc - nz]) : df_add(a, df_mul(o.cym, df_sub(pi[k], o.pym)));
+                if (xp) a = df_add(a, fx[k]);
+                if (xm) a = df_sub(a, fxm[k]);
+                qv[ic[k]] = a;
+                part = part + Acc<float>::prod(pi[k].x, a.x);
+                fxm[k] = fx[k];
+                pi[k] = o.pn;
+                ic[k] += sx;
+                cur[k] = nxt[k];
+            }
+        }
+        // reduce_last_slot's block barriers also keep the next item's first flux writes
+        // behind this item's last reads
         double2 tot;
-        if (reduce_last_slot<float>(part, rs, pinfo[p], p, w, tot) && threadIdx.x == 0)
-            finish_pq(st[p], tot.x, active_count);
-        if (__syncthreads_or(bad)) break;  // every thread leaves together after an expired wait
+        if (reduce_last_slot<float>(part, rs, pinfo[p], p, w, tot) && t == 0) finish_pq(st[p], tot.x, active_count);
     }
-    if (warp == kConsumerWarps && lane == 0) pm_drain<R>(issued, full, err);
 }
 
 }  // namespace dpf

@@ -1441,7 +1441,9 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         const bool plane_here = opt.plane > 0 && (opt.plane_levels <= 0 || l < opt.plane_levels);
         build_plane_items(L.pm, L, smooth, sms, plane_here ? opt.plane_cells : 0, opt.plane_blocks_per_sm, &shapes,
                           l);
-        if (l == 0) build_plane_items(L.pa, L, has, sms, opt.df_plane_cells, opt.df_plane_blocks_per_sm, nullptr, l);
+        if (l == 0)
+            build_plane_items(L.pa, L, has, sms, opt.df_plane_cells > 0 ? kPlaneThreads : 0, opt.df_plane_blocks_per_sm,
+                              nullptr, l);
         for (int p = 0; p < nprob; p++) {
             if (has[p]) L.all_cells += L.h_desc[p].n;
             if (smooth[p]) L.smooth_cells += L.h_desc[p].n;
@@ -1778,10 +1780,6 @@ static void configure_kernels() {
     raise((const void *)k_pm_restrict<float, 2>);
     raise((const void *)k_pm_restrict<float, 3>);
     raise((const void *)k_pm_restrict<float, 4>);
-    raise((const void *)k_pm_df_spmv<1>);
-    raise((const void *)k_pm_df_spmv<2>);
-    raise((const void *)k_pm_df_spmv<3>);
-    raise((const void *)k_pm_df_spmv<4>);
     raise((const void *)k_pm_post2<float, false>);
     raise((const void *)k_pm_post2<float, true>);
     raise((const void *)k_pm_pre2r<float>);
@@ -2270,48 +2268,26 @@ void StructBatch::pcg_iteration(T *x) {
     LAUNCH_CHECK();
 }
 
-// One iteration of the mixed-precision CG: double-float q = A p, alpha, x/r update,
-// FP32 V-cycle on the rounded residual, double-float p update.
-// Plane-marching double-float CG product over all problems of the finest level.
-template <int CPT>
-static void pm_df_kernel(unsigned nblocks, size_t smem, cudaStream_t stream, const LevelDesc *desc, PlaneWork items,
-                         CgState *st, int *count, ReduceScratch rs, const int2 *pinfo, CoeffsDF C, const float2 *pv,
-                         float2 *q, PlaneLayout lay, int *err) {
-    launch_pdl(k_pm_df_spmv<CPT>, nblocks, kPlaneThreads + 32, smem, stream, desc, items, st, count, rs, pinfo, C, pv, q, lay,
-                                                                     err);
-}
-
+// Plane-marching double-float CG product over all problems of the finest level (each face flux
+// computed once; slabs of at most 256 cells, one per thread).
 void StructBatch::pm_df_spmv(const CoeffsDF &C) {
     Level &L0 = lv[0];
-    PlaneLayout lay{};
-    int off = 0;
-    auto take = [&](int bytes) { int o = off; off += bytes; return o; };
-    lay.oX = take(pm_region(L0.pa.halo, 8));
-    lay.oCX = take(pm_region(L0.pa.slab, 8));
-    lay.oCY = take(pm_region(L0.pa.cy, 8));
-    lay.oCZ = take(pm_region(L0.pa.slab, 8));
-    lay.oLK = take(pm_region(L0.pa.slab, 8));
-    lay.oB = lay.oD = lay.oG = lay.oDIR = lay.oE = -1;
-    lay.slot_bytes = (off + 127) & ~127;
-    const size_t smem = (size_t)kPlaneStages * lay.slot_bytes;
     const unsigned nb = (unsigned)L0.pa.nb;
     const PlaneWork wk{L0.pa.items, L0.pa.first};
-    switch (L0.pa.cells / kPlaneThreads) {
-        case 1: pm_df_kernel<1>(nb, smem, stream, L0.d_desc, wk, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2], dfv[3], lay, d_factor_status + 1); break;
-        case 2: pm_df_kernel<2>(nb, smem, stream, L0.d_desc, wk, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2], dfv[3], lay, d_factor_status + 1); break;
-        case 3: pm_df_kernel<3>(nb, smem, stream, L0.d_desc, wk, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2], dfv[3], lay, d_factor_status + 1); break;
-        case 4: pm_df_kernel<4>(nb, smem, stream, L0.d_desc, wk, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2], dfv[3], lay, d_factor_status + 1); break;
-        default: throw std::logic_error("plane slab must hold 1..4 cells per thread");
-    }
+    if (L0.pa.cells != kPlaneThreads) throw std::logic_error("the marching product holds one cell per thread");
+    launch_pdl(k_pm_df_flux<1>, nb, kPlaneThreads, 0, stream, L0.d_desc, wk, d_state, d_count, rs, L0.pa.pinfo, C, dfv[2],
+               dfv[3]);
 }
 
+// One iteration of the mixed-precision CG: double-float q = A p, alpha, x/r update,
+// FP32 V-cycle on the rounded residual, double-float p update.
 void StructBatch::df_iteration(double *x64) {
     Level &L0 = lv[0];
     const unsigned nb = nb_of(L0.all);
     float *r32 = (float *)cgv[0], *z32 = (float *)cgv[1];
     CoeffsDF C{cdf[0], cdf[1], cdf[2], cdf[3]};
     if (L0.pa.ok) {
-        KTimer _kt(this, kname("k_pm_df_spmv", 0, true), L0.all_cells);
+        KTimer _kt(this, kname("k_pm_df_flux", 0, true), L0.all_cells);
         pm_df_spmv(C);
     } else {
         KTimer _kt(this, kname("k_df_spmv_pq", 0, true), L0.all_cells);

@@ -128,7 +128,7 @@ extern "C" int dpf_batch_autotune(int nprob, const int *dims, const double *mins
             {"plane_blocks_per_sm", &cur.plane_blocks_per_sm, {1, 2, 3}, mixed},
             {"tail_cells", &cur.tail_cells, {-1, 1024, 4096, 16384}, true},
             {"blocks_per_sm", &cur.blocks_per_sm, {8, 16, 24}, true},
-            {"df_plane_cells", &cur.df_plane_cells, {-1, 512}, mixed},
+            {"df_plane_cells", &cur.df_plane_cells, {-1, 256}, mixed},
             {"tail_cluster", &cur.tail_cluster, {1, 8}, true},
             {"plane_levels", &cur.plane_levels, {0, 1, 2}, mixed},
             {"streams", &cur.streams, {1, 2, 4}, nprob >= 2},

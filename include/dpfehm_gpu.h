@@ -86,9 +86,10 @@ typedef struct dpf_options {
                             staging (default 1; negative: grid-stride kernels) */
     int plane_cells;     /* plane-marching slab capacity in cells: 256, 512, 768 or 1024 (default 1024) */
     int plane_blocks_per_sm; /* plane-marching work items per SM (default 2) */
-    int df_plane_cells;  /* MIXED: slab capacity of a plane-marching double-float CG product, 256..1024
-                            (default -1: the grid-stride product, as fast on GB300; an autotuner choice) */
-    int df_plane_blocks_per_sm; /* its work items per SM (default 4) */
+    int df_plane_cells;  /* MIXED: positive: the double-float CG product marches along x over slabs of
+                            whole rows of at most 256 cells, every face flux computed once (default
+                            256); negative: the grid-stride product; an autotuner choice */
+    int df_plane_blocks_per_sm; /* the marching product's work runs per SM (default 8) */
     int tail_cluster;    /* blocks (a thread-block cluster, 2..16) per problem for the fused tail
                             (default 1: one block) */
     int plane_levels;    /* regular grids, MIXED: the plane-marching kernels run on this many of the

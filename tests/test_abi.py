@@ -80,7 +80,7 @@ def test_default_options(pkg, lib):
     o = pkg.default_options()
     assert o.reltol == 1e-10 and o.maxiter == 500 and o.precision == pkg.PREC_FP64
     assert o.cheb_degree == 0 and o.coarse_scale == 0.0 and o.max_coarse == 64 and o.blocks_per_sm == 16 and o.tail_cells == 4096 and o.plane == 1 and o.plane_cells == 1024
-    assert o.plane_blocks_per_sm == 2 and o.df_plane_cells == -1 and o.df_plane_blocks_per_sm == 4
+    assert o.plane_blocks_per_sm == 2 and o.df_plane_cells == 256 and o.df_plane_blocks_per_sm == 8
     assert o.tail_cluster == 1
     assert o.plane_levels == 0
     assert o.streams == 0

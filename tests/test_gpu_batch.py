@@ -129,7 +129,7 @@ def test_plane_and_grid_stride_smoothers_agree(gpu_lib, precision):
             B = pkg.GroundwaterBatch([p["ns"] for p in probs], [p["mins"] for p in probs],
                                      [p["maxs"] for p in probs], [p["dn"] for p in probs], reltol=1e-12,
                                      precision=precision, plane=plane, tail_cells=tail,
-                                     df_plane_cells=512 if plane > 0 else -1)
+                                     df_plane_cells=256 if plane > 0 else -1)
             out[(plane, tail)] = B.solve_grad_logk(cat("logK"), cat("dh"), cat("Qs"), [p["obs"] for p in probs])
     h0, g0 = out[(-1, -1)]
     for key, (h, g) in out.items():
@@ -164,7 +164,7 @@ def test_autotune_batch(gpu_lib):
     assert ms > 0
     assert tuned["cheb_degree"] in (1, 2, 3) and tuned["plane_cells"] in (512, 768, 1024)
     assert tuned["plane_blocks_per_sm"] in (1, 2, 3) and tuned["tail_cells"] in (-1, 1024, 4096, 16384)
-    assert tuned["blocks_per_sm"] in (8, 16, 24) and tuned["df_plane_cells"] in (-1, 512)
+    assert tuned["blocks_per_sm"] in (8, 16, 24) and tuned["df_plane_cells"] in (-1, 256)
     assert tuned["tail_cluster"] in (1, 8)
     B0 = pkg.GroundwaterBatch(*args, reltol=1e-11, precision="mixed")
     B1 = pkg.GroundwaterBatch(*args, reltol=1e-11, precision="mixed", **tuned)
