@@ -106,13 +106,22 @@ struct dpf_problem {
     std::vector<dpf_problem *> parts;
     std::vector<int> part_first;       // first problem of each part, and the problem count last
     std::vector<cudaEvent_t> part_events;
+    std::vector<cudaEvent_t> input_events;  // a part's host inputs have landed (split batches)
     std::unique_ptr<PartPool> pool;
+    // the copy of the heads to a host buffer runs on its own stream during the adjoint solve
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_events[2] = {nullptr, nullptr};
     ~dpf_problem() {
         // a part's own stream is drained before anything its work may still use is released
         if (own_stream && stream) cudaStreamSynchronize(stream);
+        if (copy_stream) cudaStreamSynchronize(copy_stream);
         pool.reset();
         for (dpf_problem *q : parts) delete q;
         for (cudaEvent_t e : part_events) cudaEventDestroy(e);
+        for (cudaEvent_t e : input_events) cudaEventDestroy(e);
+        for (cudaEvent_t e : copy_events)
+            if (e) cudaEventDestroy(e);
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         sb.reset();
         gs.reset();
         for (void *p : scratch) dev_free(p);
@@ -442,6 +451,11 @@ int make_struct(const std::vector<GridSpec> &grids, const std::vector<std::vecto
                 cudaEvent_t e;
                 ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "part event");
                 P->part_events.push_back(e);
+            }
+            for (int i = 0; i < k; i++) {
+                cudaEvent_t e;
+                ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "part event");
+                P->input_events.push_back(e);
             }
             P->pool.reset(new PartPool(k, P->device));
         } else {
@@ -857,13 +871,39 @@ static int solve_grad_common(dpf_problem *P, const double *logK, int kind, const
                            P->stream),
            "obs");
     S.obs_delta(d_obs, (long long)obs_global.size());
-    stage_out(P, h_out, S.h, S.N);
+    // heads to a host buffer: copied on the handle's copy stream while the adjoint runs (the
+    // adjoint and the gradient only read S.h); the handle's stream waits for the copy before
+    // anything after this call can overwrite S.h, and the copy is complete when this returns
+    struct CopyJoin {
+        dpf_problem *P;
+        bool pending = false;
+        ~CopyJoin() {
+            if (pending) cudaStreamSynchronize(P->copy_stream);  // an error path: the caller's buffer is settled
+        }
+    } join{P};
+    if (h_out && !is_device_ptr(h_out)) {
+        if (!P->copy_stream) {
+            ck(cudaStreamCreateWithFlags(&P->copy_stream, cudaStreamNonBlocking), "copy stream");
+            for (cudaEvent_t &e : P->copy_events) ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "copy event");
+        }
+        ck(cudaEventRecord(P->copy_events[0], P->stream), "event record");
+        ck(cudaStreamWaitEvent(P->copy_stream, P->copy_events[0], 0), "stream wait");
+        join.pending = true;
+        ck(cudaMemcpyAsync(h_out, S.h, S.N * sizeof(double), cudaMemcpyDeviceToHost, P->copy_stream), "copy out");
+        ck(cudaEventRecord(P->copy_events[1], P->copy_stream), "event record");
+    } else {
+        stage_out(P, h_out, S.h, S.N);
+    }
     S.adjoint_solve();
     int rc2 = solver_status(P, S);
     if (dlogK) {
         double *tmp = is_device_ptr(dlogK) ? dlogK : S.r64;
         S.grad_logk(tmp);
         if (tmp != dlogK) stage_out(P, dlogK, tmp, S.N);
+    }
+    if (join.pending) {
+        ck(cudaStreamWaitEvent(P->stream, P->copy_events[1], 0), "stream wait");
+        join.pending = false;
     }
     ck(cudaStreamSynchronize(P->stream), "sync");
     return rc != DPF_OK ? rc : rc2;
@@ -936,6 +976,39 @@ static int split_solve_grad_logk(dpf_problem *P, const double *logK, int kind, c
     }
     std::vector<int> rcs(k, DPF_OK);
     std::vector<std::vector<int64_t>> offs(k);
+    // Inputs in host memory are copied here, part after part (each part's copies wait for the
+    // previous part's), so the first part computes while the later parts' inputs are still in
+    // flight instead of every part waiting for the whole batch's copies.
+    std::vector<const double *> in_lk(k), in_dh(k), in_q(k);
+    const bool lk_host = logK && !is_device_ptr(logK), dh_host = !is_device_ptr(dh), q_host = !is_device_ptr(Qs);
+    for (int i = 0; i < k; i++) {
+        dpf_problem *Q = P->parts[i];
+        StructBatch &S = *Q->sb;
+        int64_t c0, f0;
+        part_base(P, i, c0, f0);
+        in_lk[i] = logK ? (lk_host ? S.in_logK : logK + c0) : nullptr;
+        if (lk_host) S.have_sampled = false;  // the input is staged over the drawn fields
+        in_dh[i] = dh_host ? S.in_dh : dh + c0;
+        in_q[i] = q_host ? S.in_Q : Qs + c0;
+        cudaError_t e = cudaStreamWaitEvent(Q->stream, P->part_events[k], 0);
+        if (e == cudaSuccess && (lk_host || dh_host || q_host)) {
+            if (i > 0) e = cudaStreamWaitEvent(Q->stream, P->input_events[i - 1], 0);
+            if (e == cudaSuccess && lk_host)
+                e = cudaMemcpyAsync(S.in_logK, logK + c0, S.N * sizeof(double), cudaMemcpyHostToDevice, Q->stream);
+            if (e == cudaSuccess && dh_host)
+                e = cudaMemcpyAsync(S.in_dh, dh + c0, S.N * sizeof(double), cudaMemcpyHostToDevice, Q->stream);
+            if (e == cudaSuccess && q_host)
+                e = cudaMemcpyAsync(S.in_Q, Qs + c0, S.N * sizeof(double), cudaMemcpyHostToDevice, Q->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(P->input_events[i], Q->stream);
+        }
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            P->err = std::string("part inputs: ") + cudaGetErrorString(e);
+            // parts already started are drained before the caller may reuse its buffers
+            for (int j = 0; j <= i; j++) cudaStreamSynchronize(P->parts[j]->stream);
+            return DPF_CUDA;
+        }
+    }
     P->pool->run([&](int i) {
         dpf_problem *Q = P->parts[i];
         const int p0 = P->part_first[i], p1 = P->part_first[i + 1];
@@ -943,12 +1016,7 @@ static int split_solve_grad_logk(dpf_problem *P, const double *logK, int kind, c
         part_base(P, i, c0, f0);
         offs[i].resize(p1 - p0 + 1);
         for (int p = p0; p <= p1; p++) offs[i][p - p0] = obs_offsets[p] - obs_offsets[p0];
-        if (cudaStreamWaitEvent(Q->stream, P->part_events[k], 0) != cudaSuccess) {
-            Q->err = std::string("stream wait: ") + cudaGetErrorString(cudaGetLastError());
-            rcs[i] = DPF_CUDA;
-            return;
-        }
-        rcs[i] = dpf_batch_solve_grad_logk(Q, logK ? logK + c0 : nullptr, kind, dh + c0, Qs + c0, offs[i].data(),
+        rcs[i] = dpf_batch_solve_grad_logk(Q, in_lk[i], kind, in_dh[i], in_q[i], offs[i].data(),
                                            obs ? obs + obs_offsets[p0] : nullptr, h_out ? h_out + c0 : nullptr,
                                            dlogK ? dlogK + c0 : nullptr);
         if (cudaEventRecord(P->part_events[i], Q->stream) != cudaSuccess) {
@@ -1029,6 +1097,8 @@ int dpf_batch_solve_grad_logk(dpf_problem *P, const double *logK, int kind, cons
                 return DPF_STATE;
             }
             logK = S.in_logK;
+        } else if (logK != S.in_logK) {
+            S.have_sampled = false;  // the input is staged over the drawn fields
         }
         std::vector<long long> og;
         for (int p = 0; p < S.nprob; p++) {

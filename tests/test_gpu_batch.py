@@ -137,6 +137,33 @@ def test_plane_and_grid_stride_smoothers_agree(gpu_lib, precision):
         assert rel(g, g0) < 1e-9, key
 
 
+@pytest.mark.parametrize("streams", [1, 3])
+def test_host_buffers_match_device_buffers(gpu_lib, streams):
+    """Host (page-locked) inputs and outputs give the device-resident results bit for bit, also
+    when the batch runs as concurrent parts whose host inputs are copied part after part and
+    whose heads are copied out during the adjoint solve."""
+    import torch
+    pkg = gpu_lib
+    shapes = [(20, 16, 5), (9, 9, 9), (40, 30, 6), (12, 3, 70)]
+    probs = [_problem(pkg, ns, 51 + k) for k, ns in enumerate(shapes)]
+    cat = lambda k: np.concatenate([p[k] for p in probs])
+    B = pkg.GroundwaterBatch([p["ns"] for p in probs], [p["mins"] for p in probs], [p["maxs"] for p in probs],
+                             [p["dn"] for p in probs], reltol=1e-11, precision="mixed", streams=streams)
+    obs = [p["obs"] for p in probs]
+    dev = [torch.tensor(cat(k), device="cuda") for k in ("logK", "dh", "Qs")]
+    hd, gd = B.solve_grad_logk(*dev, obs)
+    hd, gd = hd.cpu().numpy(), gd.cpu().numpy()
+    host = [torch.from_numpy(cat(k)).pin_memory() for k in ("logK", "dh", "Qs")]
+    outs = [torch.full((B.N,), np.nan, dtype=torch.float64).pin_memory() for _ in range(2)]
+    for _ in range(2):  # twice: the second call reuses the copy stream and the staged inputs
+        h, g = B.solve_grad_logk(*[x.numpy() for x in host], obs, out=tuple(x.numpy() for x in outs))
+        assert np.array_equal(h, hd) and np.array_equal(g, gd)
+    # pageable host arrays as well
+    h, g = B.solve_grad_logk(cat("logK"), cat("dh"), cat("Qs"), obs)
+    assert np.array_equal(h, hd) and np.array_equal(g, gd)
+    B.close()
+
+
 def test_caller_output_buffers(gpu_lib):
     """solve_grad_logk(out=(h, g)) fills the caller's host buffers with the same values."""
     pkg = gpu_lib

@@ -84,6 +84,10 @@ def test_fused_sample_and_solve(gpu_lib, orc, streams):
     h2, g2 = B.solve_grad_logk(field, dh, Qs, obs)
     h1, g1 = h1.cpu().numpy(), g1.cpu().numpy()
     assert np.array_equal(h1, h2) and np.array_equal(g1, g2)
+    # the explicit field was staged over the drawn ones: a NULL logK is refused again
+    with pytest.raises(pkg.DPFError) as e:
+        B.solve_grad_logk(None, dh, Qs, obs)
+    assert e.value.code == pkg._lib.DPF_STATE
     for p, g in enumerate(grids):
         _, nb, aol, _ = pkg.regulargrid3d(mins[p], maxs[p], g)
         a, b = B.cell_offsets[p], B.cell_offsets[p + 1]
