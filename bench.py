@@ -244,9 +244,12 @@ def run_ours(args, dist, rank, ws):
     _barrier(dist)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    e2e_steps = []
     for k in range(args.steps):
+        t1 = time.perf_counter()
         h_e2e, g_e2e = batch.solve_grad_logk(h_logK.numpy(), h_dh.numpy(), h_Qs.numpy(), obs,
                                              out=(h_h.numpy(), h_g.numpy()))
+        e2e_steps.append(time.perf_counter() - t1)  # each call returns with its outputs in host memory
     torch.cuda.synchronize()
     t_e2e = _max_over_ranks(dist, time.perf_counter() - t0)
     # ---- roofline of the dominant kernel (profiling pass on identical realizations so every
@@ -278,7 +281,8 @@ def run_ours(args, dist, rank, ws):
                    "autotuned": tuned or None,
                    "autotune_seconds": round(tune_s, 2) if tune_s else None},
         "e2e": {"value": round(solves / t_e2e, 3), "unit": "solves/s",
-                "h2d_bytes_per_step": int(3 * 8 * B * N), "d2h_bytes_per_step": int(2 * 8 * B * N)},
+                "h2d_bytes_per_step": int(3 * 8 * B * N), "d2h_bytes_per_step": int(2 * 8 * B * N),
+                "step_ms": [round(1e3 * t, 2) for t in e2e_steps]},
         "gpu_launches": int(launches),
         "clocks": clk,
         "iterations_last_adjoint": stats["iterations"],

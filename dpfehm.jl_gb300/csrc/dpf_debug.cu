@@ -1,4 +1,5 @@
-// dpf_debug.cu -- test hook for the bounded waits of the staging kernels.
+// dpf_debug.cu -- test hooks: the bounded waits of the staging kernels, and the integer-only
+// 48-bit split of doubles that the assembly and the round start use.
 //
 // dpf_debug_expired_wait runs one block whose threads wait on a shared-memory mbarrier
 // that nothing arrives on, through the same bounded wait (mbar_wait) that every staging
@@ -27,7 +28,32 @@ __global__ void k_expired_wait(int *err, unsigned long long *waited_ns) {
     }
 }
 
+__global__ void k_split48(long long n, const double *v, float *hi, float *lo, double *v48, int *ok) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float h = 0.f, l = 0.f;
+    double w = 0.0;
+    ok[i] = split48(v[i], h, l, w) ? 1 : 0;
+    hi[i] = h;
+    lo[i] = l;
+    v48[i] = w;
+}
+
 }  // namespace dpf
+
+extern "C" int dpf_debug_split48(int64_t n, const double *v, float *hi, float *lo, double *v48, int *ok) {
+    if (n < 0 || (n > 0 && (!v || !hi || !lo || !v48 || !ok))) return DPF_BAD_INPUT;
+    if (n == 0) return DPF_OK;
+    dpf::k_split48<<<(unsigned)((n + 255) / 256), 256>>>((long long)n, v, hi, lo, v48, ok);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        dpf::set_global_error(std::string("split probe: ") + cudaGetErrorString(e));
+        return DPF_CUDA;
+    }
+    return DPF_OK;
+}
 
 extern "C" int dpf_debug_expired_wait(double *waited_ms) {
     int ndev = 0;

@@ -92,20 +92,31 @@ __global__ void k_assemble(const LevelDesc *__restrict__ desc, const int4 *__res
         } else {
             lk = 1.0;
         }
+        double *cv[4] = {&cp[0], &cp[1], &cp[2], &lk};
         if (dfx) {
             // mixed precision: the FP64 operator is the exact value of its double-float copy
-            // (48 of 53 bits), so the double-float CG and the FP64 residual check see the
-            // same operator (a relative change of at most 2^-49 in every coefficient)
-            const float2 qx = df_from_double(cp[0]), qy = df_from_double(cp[1]);
-            const float2 qz = df_from_double(cp[2]), ql = df_from_double(lk);
-            dfx[i] = qx; dfy[i] = qy; dfz[i] = qz; dfleak[i] = ql;
-            cp[0] = df_to_double(qx); cp[1] = df_to_double(qy); cp[2] = df_to_double(qz); lk = df_to_double(ql);
-        }
-        cx[i] = cp[0]; cy[i] = cp[1]; cz[i] = cp[2]; leak[i] = lk;
-        if (fx) {
+            // (each coefficient rounded to 48 of its 53 bits: a relative change of at most 2^-48),
+            // so the double-float CG and the FP64 residual check see the same operator; the bf16
+            // copies of the FP32 V-cycle are rounded from the leading floats
+            float2 *dv[4] = {dfx, dfy, dfz, dfleak};
+            __nv_bfloat16 *bv[4] = {fx, fy, fz, fleak};
+    #pragma unroll
+            for (int k = 0; k < 4; k++) {
+                float2 q;
+                double v48;
+                if (!split48(*cv[k], q.x, q.y, v48)) {
+                    q = df_from_double(*cv[k]);
+                    v48 = df_to_double(q);
+                }
+                dv[k][i] = q;
+                *cv[k] = v48;
+                if (fx) bv[k][i] = __float2bfloat16(q.x);
+            }
+        } else if (fx) {
             fx[i] = __double2bfloat16(cp[0]); fy[i] = __double2bfloat16(cp[1]);
             fz[i] = __double2bfloat16(cp[2]); fleak[i] = __double2bfloat16(lk);
         }
+        cx[i] = cp[0]; cy[i] = cp[1]; cz[i] = cp[2]; leak[i] = lk;
         b[i] = rhs;
         if (init_x) x[i] = fi ? 0.0 : dh[i];
         else if (!fi) x[i] = dh[i];
@@ -762,18 +773,19 @@ __global__ void k_df_update_p(const LevelDesc *__restrict__ desc, const int4 *__
 template <bool FIRST, bool ZERO = false>
 __global__ void k_df_residual(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, CgState *st,
                               int *active_count, ReduceScratch rs, const int2 *__restrict__ pinfo,
-                              Coeffs<double> C, const uint8_t *__restrict__ dir, const double *__restrict__ b,
-                              const double *__restrict__ x, double *__restrict__ r, double tol2, int maxiter,
-                              int max_rounds) {
+                              Coeffs<double> C, Coeffs<float> C16, const uint8_t *__restrict__ dir,
+                              const double *__restrict__ b, const double *__restrict__ x, double *__restrict__ r,
+                              double tol2, int maxiter, int max_rounds) {
     pdl_enter();
     int4 bm = bmap[blockIdx.x];
     const int p = bm.x;
     if (!FIRST && st[p].ru_flag == 0) return;  // finished in an earlier round
     const LevelDesc L = desc[p];
-    Acc<double> rr, bb;  // FIRST: |r|^2, |b|^2; otherwise |r|^2 and the rounding floor
+    Acc<double> rr, bb;  // FIRST: |r|^2, |b|^2; otherwise |r|^2 and the rounding floor / 2^-96
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
         Cell c;
-        double ri, bi, xi = 0.0, dg = 0.0;
+        double ri, bi, xi = 0.0;
+        float dg = 0.0f;
         if (ZERO) {
             c.i = L.off + li_;
             bi = b[c.i];
@@ -782,7 +794,7 @@ __global__ void k_df_residual(const LevelDesc *__restrict__ desc, const int4 *__
             cell_at(L, li_, c);
             xi = x[c.i];
             double Ax;
-            apply7(L, c, C, xi, [&](long long j, int, int, int) { return x[j]; }, Ax, dg);
+            apply7_f32diag(L, c, C, C16, xi, x, Ax, dg);
             bi = b[c.i];
             ri = bi - Ax;
         }
@@ -797,11 +809,13 @@ __global__ void k_df_residual(const LevelDesc *__restrict__ desc, const int4 *__
             // of x_i taken as |x_i|), with the unit roundoff of the double-float recurrence that
             // produced x, u = 2^-48: its search directions and residuals carry about 48 bits, so the
             // true residual of a converged round settles near this bound, about 32 times the FP64
-            // one; a round that reaches it is accepted without a further round that cannot improve it
-            const double f = 0x1p-48 * fma(2.0 * dg, fabs(xi), fabs(bi));
-            bb.v += f * f;
+            // one; a round that reaches it is accepted without a further round that cannot improve it.
+            // An estimate: formed in FP32 (u applied to the sum), squared and summed in FP64.
+            const double f = (double)fmaf(2.0f * dg, abs_float_trunc(xi), abs_float_trunc(bi));
+            bb.v = fma(f, f, bb.v);
         }
     }
+    if (!FIRST) bb.v *= 0x1p-96;
     double2 tot;
     if (reduce_last<double, 2>(rr, bb, rs, pinfo[p], p, tot) && threadIdx.x == 0) {
         CgState &s = st[p];
@@ -862,7 +876,10 @@ __global__ void k_df_begin(const LevelDesc *__restrict__ desc, const int4 *__res
     const double inv = 1.0 / st[p].scale;
     for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
         const long long i = L.off + li_;
-        const float2 v = df_from_double(r64[i] * inv);
+        const double w = r64[i] * inv;
+        float2 v;
+        double w48;
+        if (!split48(w, v.x, v.y, w48)) v = df_from_double(w);  // 48 bits either way
         r[i] = v;
         r32[i] = v.x;
     }
@@ -2419,12 +2436,14 @@ void StructBatch::df_pcg(const double *b64, double *x64, double tol2) {
         KTimer _kt(this, kname(zero_guess ? "k_df_residual0" : "k_df_residual", 0, false), L0.all_cells);
         if (zero_guess)
             launch_pdl(k_df_residual<true, true>, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, d_count, rs,
-                                                                 L0.all.d_pinfo, coeffs_of<double>(L0, true), L0.dir,
-                                                                 b64, x64, r64, tol2, opt.maxiter, opt.max_outer);
+                                                                 L0.all.d_pinfo, coeffs_of<double>(L0, true),
+                                                                 coeffs_of<float>(L0, true), L0.dir, b64, x64, r64, tol2,
+                                                                 opt.maxiter, opt.max_outer);
         else
             launch_pdl(k_df_residual<true>, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, d_count, rs,
-                                                           L0.all.d_pinfo, coeffs_of<double>(L0, true), L0.dir, b64,
-                                                           x64, r64, tol2, opt.maxiter, opt.max_outer);
+                                                           L0.all.d_pinfo, coeffs_of<double>(L0, true),
+                                                           coeffs_of<float>(L0, true), L0.dir, b64, x64, r64, tol2,
+                                                           opt.maxiter, opt.max_outer);
     }
     LAUNCH_CHECK();
     for (int round = 0; round < opt.max_outer && read_count(0) > 0; round++) {
@@ -2444,8 +2463,9 @@ void StructBatch::df_pcg(const double *b64, double *x64, double tol2) {
         {
             KTimer _kt(this, kname("k_df_residual", 0, false), L0.all_cells);
             launch_pdl(k_df_residual<false>, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, d_count, rs,
-                                                            L0.all.d_pinfo, coeffs_of<double>(L0, true), L0.dir, b64,
-                                                            x64, r64, tol2, opt.maxiter, opt.max_outer);
+                                                            L0.all.d_pinfo, coeffs_of<double>(L0, true),
+                                                            coeffs_of<float>(L0, true), L0.dir, b64, x64, r64, tol2,
+                                                            opt.maxiter, opt.max_outer);
         }
         LAUNCH_CHECK();
     }

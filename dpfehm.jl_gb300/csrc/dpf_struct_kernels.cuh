@@ -262,6 +262,50 @@ __device__ __forceinline__ void apply7(const LevelDesc &L, const Cell &c, const 
     diag = d;
 }
 
+// |v| as a float, truncated, from v's bits (integer operations only): 0 below 2^-126, 3e38 at or
+// above 2^128 (Inf and NaN included). For rounding-floor estimates, where a relative error of
+// 2^-23 is immaterial and an FP64-to-FP32 conversion would occupy GB300's FP64 pipe.
+__device__ __forceinline__ float abs_float_trunc(double v) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+    const int e = (int)(u >> 52);
+    if (e >= 1023 + 128) return 3.0e38f;
+    if (e <= 1023 - 127) return 0.0f;
+    return __uint_as_float(((unsigned)(e - 1023 + 127) << 23) | ((unsigned)(u >> 29) & 0x7FFFFFu));
+}
+
+// apply7 in FP64 (the same arithmetic in the same order: A x is bitwise apply7's) with the
+// diagonal summed in FP32 from the level's bf16 coefficients: the diagonal only scales a
+// rounding-floor estimate, where bf16 precision is ample, and FP64 additions cost as much as
+// the flux terms on GB300's FP64 pipe.
+__device__ __forceinline__ void apply7_f32diag(const LevelDesc &L, const Cell &c, const Coeffs<double> &C,
+                                               const Coeffs<float> &C16, double xi, const double *__restrict__ x,
+                                               double &Ax, float &diag) {
+    const long long i = c.i;
+    const long long sy = L.nz, sx = (long long)L.ny * L.nz;
+    double a = C.leak[i] * xi;
+    float d = cf(C16.leak[i]);
+#if DPF_CHECKED
+    if (!(DPF_INSIDE(CK_NEIGHBOUR, c.iz + 1 < L.nz ? i + 1 : i, L.off, L.off + L.n) &&
+          DPF_INSIDE(CK_NEIGHBOUR, c.iz > 0 ? i - 1 : i, L.off, L.off + L.n) &&
+          DPF_INSIDE(CK_NEIGHBOUR, c.iy + 1 < L.ny ? i + sy : i, L.off, L.off + L.n) &&
+          DPF_INSIDE(CK_NEIGHBOUR, c.iy > 0 ? i - sy : i, L.off, L.off + L.n) &&
+          DPF_INSIDE(CK_NEIGHBOUR, c.ix + 1 < L.nx ? i + sx : i, L.off, L.off + L.n) &&
+          DPF_INSIDE(CK_NEIGHBOUR, c.ix > 0 ? i - sx : i, L.off, L.off + L.n))) {
+        Ax = a;
+        diag = d;
+        return;
+    }
+#endif
+    if (c.iz + 1 < L.nz) { a += C.cz[i] * (xi - x[i + 1]);       d += cf(C16.cz[i]); }
+    if (c.iz > 0)        { a += C.cz[i - 1] * (xi - x[i - 1]);   d += cf(C16.cz[i - 1]); }
+    if (c.iy + 1 < L.ny) { a += C.cy[i] * (xi - x[i + sy]);      d += cf(C16.cy[i]); }
+    if (c.iy > 0)        { a += C.cy[i - sy] * (xi - x[i - sy]); d += cf(C16.cy[i - sy]); }
+    if (c.ix + 1 < L.nx) { a += C.cx[i] * (xi - x[i + sx]);      d += cf(C16.cx[i]); }
+    if (c.ix > 0)        { a += C.cx[i - sx] * (xi - x[i - sx]); d += cf(C16.cx[i - sx]); }
+    Ax = a;
+    diag = d;
+}
+
 // v / diag for the smoothers: FP64 levels multiply by the stored inverse diagonal
 // (a DP division per cell per sweep is expensive on GB300), FP32 levels use the fast
 // approximate division (about 2 ulp, ample for a smoother).
@@ -325,6 +369,35 @@ __device__ __forceinline__ float2 df_from_double(double v) {
     return make_float2(h, (float)(v - (double)h));
 }
 __device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + (double)a.y; }
+// v rounded to 48 significant bits (to nearest, ties away from zero), v48, and its exact split
+// v48 = hi + lo into two floats, formed from v's bits with integer operations only: conversions
+// between FP64 and FP32 run on GB300's FP64 pipe, a small fraction of its FP32 rate, and the
+// split is needed per cell. hi is v48 with its low 29 fraction bits cleared (exactly a float), lo
+// the next 24 bits (a 24-bit integer times a power of two: exact). Handles zero and
+// 2^-79 <= |v48| < 2^128; returns false for anything else (subnormals, tiny or huge values, Inf,
+// NaN), where the caller takes the FP64 route.
+__device__ __forceinline__ bool split48(double v, float &hi, float &lo, double &v48) {
+    const unsigned long long u0 = (unsigned long long)__double_as_longlong(v);
+    const unsigned sign = (unsigned)(u0 >> 32) & 0x80000000u;
+    if ((u0 << 1) == 0ull) {  // +0 or -0
+        hi = lo = __uint_as_float(sign);
+        v48 = v;
+        return true;
+    }
+    if (((u0 >> 52) & 0x7FFull) == 0x7FFull) return false;  // Inf, NaN
+    // add half of the 5 dropped bits, then drop them (a carry runs into the exponent correctly)
+    const unsigned long long u = (u0 + 0x10ull) & ~0x1Full;
+    const int e = (int)((u >> 52) & 0x7FFull);
+    const int E = e - 1023;
+    if (e == 0 || E < -79 || E > 127) return false;
+    const unsigned long long m = u & 0xFFFFFFFFFFFFFull;
+    hi = __uint_as_float(sign | ((unsigned)(E + 127) << 23) | (unsigned)(m >> 29));
+    const unsigned r24 = (unsigned)(m >> 5) & 0xFFFFFFu;
+    const float lo_mag = __uint2float_rn(r24) * __uint_as_float((unsigned)(E - 47 + 127) << 23);
+    lo = __uint_as_float(__float_as_uint(lo_mag) | sign);
+    v48 = __longlong_as_double((long long)u);
+    return true;
+}
 
 // Face conductances from cell values kc, computed once per cell by k_cell_k
 // (GB300 has little FP64 throughput, so exp runs once per cell, not once per face):

@@ -348,6 +348,14 @@ void dpf_debug_alloc_stats(int64_t *made, int64_t *live);
  * *waited_ms (may be NULL); any other status is a defect. The device stays usable. */
 int dpf_debug_expired_wait(double *waited_ms);
 
+/* No counterpart in the reference. For n doubles v (device memory) the split that the
+ * mixed-precision assembly and round start use: v48 = v rounded to 48 significant bits
+ * (to nearest, ties away from zero), hi + lo = v48 exactly (two floats), formed with integer
+ * operations only; ok[i] = 1 where the split applies (zero, 2^-79 <= |v48| < 2^128), 0 where
+ * the FP64 route is taken
+ * (outputs then unspecified). All outputs are device arrays of n entries. */
+int dpf_debug_split48(int64_t n, const double *v, float *hi, float *lo, double *v48, int *ok);
+
 /* No counterpart in the reference. In a library built with DPF_CHECK defined
  * (device-side bounds and alignment checks on cell decodes, stencil neighbours,
  * aggregates, staged copies and CSR columns; a violating access is clamped or

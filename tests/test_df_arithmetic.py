@@ -107,3 +107,53 @@ def test_double_float_flux_product_keeps_48_bits_on_a_smooth_direction():
         c32 = c[ax].astype(F32)
         q32 = (q32 + c32 * (p32 - p32[up]) + c32[dn] * (p32 - p32[dn])).astype(F32)
     assert np.linalg.norm(q32[m].astype(F64) - e[m]) >= 0.5 * nrm     # emulated: 1.0
+
+
+def test_face_flux_is_antisymmetric_bit_for_bit():
+    """The marching product computes each face flux c (p_i - p_j) once and hands its negation to
+    the neighbour. That equals the neighbour's own term c (p_j - p_i) bit for bit (up to the sign
+    of a zero) because the double-float difference and product are odd: round to nearest is
+    symmetric and the two-sum error is exact."""
+    rng = np.random.default_rng(11)
+    n = 200000
+    base = rng.normal(0.0, 1.0, n) * 10.0 ** rng.integers(-6, 3, n)
+    a64 = base + rng.normal(0.0, 1.0, n) * 10.0 ** rng.integers(-16, 0, n) * np.abs(base)
+    b64 = base.copy()
+    a, b = _split(a64), _split(b64)
+    c = _split(np.exp(rng.normal(-9.0, 2.0, n)))
+    ab, ba = df_sub(a, b), df_sub(b, a)
+    f_ab, f_ba = df_mul(c, ab), df_mul(c, ba)
+    for k in range(2):
+        assert np.array_equal(ab[k], -ba[k])
+        assert np.array_equal(f_ab[k], -f_ba[k])
+
+
+def split48_reference(v):
+    """The bits of the library's split48 (integer-only 48-bit split), in numpy: v48 is v rounded to
+    48 significant bits (half of the 5 dropped bits added, then dropped: to nearest, ties away from
+    zero), hi its top 24 (exactly a float), lo = v48 - hi (exactly a float, a zero carrying v's
+    sign); ok where v is zero or 2^-79 <= |v48| < 2^128."""
+    v = np.asarray(v, dtype=F64)
+    u0 = v.view(np.uint64)
+    zero = (u0 << np.uint64(1)) == 0
+    special = ((u0 >> np.uint64(52)) & np.uint64(0x7FF)) == np.uint64(0x7FF)
+    u = np.where(zero, u0, (u0 + np.uint64(0x10)) & ~np.uint64(0x1F))
+    e = ((u >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int64)
+    ok = zero | (~special & (e != 0) & (e - 1023 >= -79) & (e - 1023 <= 127))
+    v48 = np.where(ok, u.view(F64), 0.0)
+    hi64 = np.where(ok, (u & ~np.uint64((1 << 29) - 1)).view(F64), 0.0)
+    hi = hi64.astype(F32)
+    lo = (v48 - hi64).astype(F32)
+    lo = np.where(lo == 0, np.copysign(F32(0.0), v).astype(F32), lo)  # a zero lo carries v's sign
+    return hi, lo, v48, ok
+
+
+def test_split48_reference_is_exact():
+    rng = np.random.default_rng(5)
+    v = rng.normal(0.0, 1.0, 100000) * 10.0 ** rng.integers(-15, 20, 100000)
+    hi, lo, v48, ok = split48_reference(v)
+    assert ok.all()
+    assert np.array_equal(hi.astype(F64) + lo.astype(F64), v48)     # exact in float64
+    assert np.all(np.abs(v48 - v) <= np.abs(v) * 2.0 ** -48)          # rounded to nearest
+    # nearly unbiased: only the ties (1 in 32) round away from zero, 1.1e-16 on average (truncation: 3.6e-15)
+    assert abs(np.mean((v48 - v) / v)) < 2e-16
