@@ -500,7 +500,7 @@ def main():
     ap.add_argument("--streams", type=int, default=0,
                     help="split the batch into this many concurrent parts (0: the autotuner's choice)")
     ap.add_argument("--workload", default="steady_1m", choices=["steady_1m", "steady_100k", "uneven_batch", "transient", "general_1m",
-                                                                "richards", "dfn"],
+                                                                "richards", "dfn", "cholesky"],
                     help="steady_1m is the headline; the others are the remaining configurations (bench_workloads.py)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

@@ -405,6 +405,80 @@ def run_richards(args, dist, rank, ws, METRIC_NAME):
     }
 
 
+def run_cholesky(args, dist, rank, ws, METRIC_NAME):
+    """The direct solver (linear_solver = cholesky_solver, DPFEHM src/groundwater.jl:56-60): a
+    banded Cholesky factorisation of the FP64 operator on the GPU, for the grid classes the
+    reference's own Cholesky-versus-CG comparison covers (examples/fracture_network_solver_scaling/
+    porous_media_comparison.jl: unit conductivity, Dirichlet h = 1 and 0 on the x = min and x = max
+    faces). Here: a 2-D grid of 500 x 500 cells and a 3-D grid of 48^3, each with a Matern
+    (l = 20 cells, sigma = 1) logK. One "solve" is a forward solve (factorisation included) and its
+    adjoint; the same on the AMG-preconditioned CG in FP64 for comparison; heads against the
+    oracle (its CG to 1e-14) on the host."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    ge._load_build_module().build()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    import warnings
+    warnings.simplefilter("error", RuntimeWarning)
+    cases = []
+    for grid in ((500, 500, 1), (48, 48, 48)):
+        mins = (0.0, 0.0, 0.0)
+        maxs = tuple(float(n - 1) for n in grid)
+        coords, nb, aol, vol = pkg.regulargrid3d(mins, maxs, grid)
+        N = coords.shape[1]
+        lk = pkg.fields.volume_logk(grid, mins, maxs, 20.0, 1.0, -9.0, 31)
+        Ks = np.exp(0.5 * (lk[nb[:, 0]] + lk[nb[:, 1]]))
+        x = coords[0]
+        dn = np.nonzero((x == mins[0]) | (x == maxs[0]))[0]
+        dh = np.where(x == mins[0], 1.0, 0.0)
+        Qs = np.zeros(N)
+        rng = np.random.default_rng(32)
+        delta = np.zeros(N)
+        delta[rng.choice(np.setdiff1d(np.arange(N), dn), 100, replace=False)] = 1.0
+        row = {"grid": list(grid), "cells": N, "band": int(grid[1] * grid[2]) if grid[2] > 1 else int(grid[1])}
+        for solver, prec, tol in (("cholesky", "fp64", 1e-10), ("cg", "fp64", 1e-10)):
+            P = pkg.GroundwaterProblem(nb, aol, dn, N=N, solver=solver, precision=prec, reltol=tol)
+            P.forward(Ks, dh, Qs)  # warm-up (and the band set-up)
+            P.adjoint(delta)
+            torch.cuda.synchronize()
+            reps = 2
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                h = P.forward(Ks, dh, Qs)
+                g = P.adjoint(delta)
+            torch.cuda.synchronize()
+            row[solver + "_ms_per_solve"] = round(1e3 * (time.perf_counter() - t0) / reps, 2)
+            row[solver + "_relres"] = P.stats["relres"]
+            row[solver + "_iterations"] = P.stats["iterations"]
+            row[solver + "_h"] = np.asarray(h)
+        cases.append((grid, nb, aol, dn, Ks, dh, Qs, row))
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    orc.build()
+    orc.set_threads(os.cpu_count() or 1)
+    out_rows = []
+    for grid, nb, aol, dn, Ks, dh, Qs, row in cases:
+        O = orc.Problem(row["cells"], nb, aol, np.asarray(dn, np.int64))
+        t0 = time.perf_counter()
+        ho = O.steady(Ks, dh, Qs, reltol=1e-14)
+        row["oracle_forward_s"] = round(time.perf_counter() - t0, 3)
+        row["rel_head_err_vs_oracle"] = _rel(row.pop("cholesky_h"), ho)
+        row["cg_rel_head_err_vs_oracle"] = _rel(row.pop("cg_h"), ho)
+        out_rows.append(row)
+    t_main = out_rows[0]["cholesky_ms_per_solve"] / 1e3
+    return {
+        "metric": METRIC_NAME, "value": round(1.0 / t_main, 3), "unit": "solves/s", "n_gpus": ws, "steps": 2,
+        "warmup": 1, "ms_per_step": out_rows[0]["cholesky_ms_per_solve"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Matern logK fields)",
+        "config": {"workload": "gw_steady_fwd_adj_direct_cholesky", "precision": "fp64", "solver": "cholesky",
+                   "value_case": "2-D 500 x 500", "cases": out_rows},
+    }
+
+
 def run_dfn(args, dist, rank, ws, METRIC_NAME):
     """A synthetic fracture network mesh (grid.fracture_network: 3000 square fractures with power-law
     sizes from 4 to 50 m in a 100 m cube, cells of 0.25 m, about 5M cells after keeping the largest
@@ -535,6 +609,8 @@ def run(name, args, dist, rank, ws):
         return None
     if name == "dfn":
         return run_dfn(args, dist, rank, ws, "forward+adjoint solves/sec, 5M-cell fracture network, CSR path")
+    if name == "cholesky":
+        return run_cholesky(args, dist, rank, ws, "forward+adjoint solves/sec, direct (banded Cholesky) solver")
     if name == "richards":
         return run_richards(args, dist, rank, ws, "Richards steady forward+adjoint solves/sec, 200k cells")
     if name == "general_1m":

@@ -22,14 +22,15 @@ import numpy as np
 
 from . import _lib
 from . import fields, grid
-from ._lib import MEAN_GEOMETRIC, MEAN_HARMONIC, PREC_FP64, PREC_MIXED, default_options, load
+from ._lib import (MEAN_GEOMETRIC, MEAN_HARMONIC, PREC_FP64, PREC_MIXED, SOLVER_CG, SOLVER_CHOLESKY,
+                   default_options, load)
 from .grid import addboundaryconditions, getfreenodes, load_uge, regulargrid1d, regulargrid2d, regulargrid3d
 
 __all__ = [
     "groundwater_steadystate", "rrule_groundwater_steadystate", "logKs2Ks_neighbors", "GroundwaterProblem",
     "GroundwaterBatch", "DPFError", "NoTangent", "getfreenodes", "addboundaryconditions", "regulargrid1d",
     "regulargrid2d", "regulargrid3d", "load_uge", "fields", "grid", "load", "default_options", "MEAN_GEOMETRIC",
-    "MEAN_HARMONIC", "PREC_FP64", "PREC_MIXED", "solvepressure", "rrule_solvepressure", "amg_solver",
+    "MEAN_HARMONIC", "PREC_FP64", "PREC_MIXED", "SOLVER_CG", "SOLVER_CHOLESKY", "solvepressure", "rrule_solvepressure", "amg_solver",
     "cholesky_solver", "autotune_batch", "richards_steadystate", "rrule_richards_steadystate",
 ]
 
@@ -52,6 +53,7 @@ NoTangent = _NoTangent()
 _MEANS = {"geometric": MEAN_GEOMETRIC, "harmonic": MEAN_HARMONIC, MEAN_GEOMETRIC: MEAN_GEOMETRIC,
           MEAN_HARMONIC: MEAN_HARMONIC}
 _PRECS = {"fp64": PREC_FP64, "mixed": PREC_MIXED, PREC_FP64: PREC_FP64, PREC_MIXED: PREC_MIXED}
+_SOLVERS = {"cg": SOLVER_CG, "cholesky": SOLVER_CHOLESKY}
 
 
 def _is_torch(x):
@@ -118,6 +120,8 @@ def _options(reltol=None, maxiter=None, precision=None, **kw):
         o.maxiter = int(maxiter)
     if precision is not None:
         o.precision = _PRECS[precision]
+    if isinstance(kw.get("solver"), str):
+        kw = dict(kw, solver=_SOLVERS[kw["solver"]])
     for k, v in kw.items():
         if not hasattr(o, k):
             raise TypeError("unknown solver option %r" % k)
@@ -537,11 +541,13 @@ def amg_solver(*_a, **_k):
 
 
 def cholesky_solver(*_a, **_k):
-    """Selector for ``linear_solver=`` (src/groundwater.jl:56-60): a solve to direct-solve
-    accuracy. On the GPU this is the AMG-preconditioned CG run to the FP64 rounding floor of
-    the system, not a sparse factorisation: the mixed-precision solver with a tolerance below
-    any FP64 floor, whose rounds each end after a 1e-12 drop of their recursive residual and
-    whose FP64 check accepts (status OK) once the true residual is at the floor."""
+    """Selector for ``linear_solver=`` (src/groundwater.jl:56-60): a direct solve. The GPU
+    factors the operator as L L^T in a narrow band (rows renumbered: regular grids with their two
+    shortest axes fastest, other meshes in reverse Cuthill-McKee order) once per assembly and
+    answers each solve with two triangular solves (options ``solver="cholesky"``). A band too wide
+    for the device falls back to the AMG-preconditioned CG run to the FP64 rounding floor of the
+    system (the mixed-precision solver with a tolerance below any floor, whose FP64 check accepts
+    with status OK once the true residual is at the floor)."""
     raise TypeError("cholesky_solver selects the solver; pass it as linear_solver=cholesky_solver")
 
 
@@ -550,8 +556,11 @@ def _solver_options(linear_solver, kwargs):
         return kwargs
     if linear_solver is cholesky_solver or linear_solver == "cholesky":
         o = dict(kwargs)
-        o["precision"] = "mixed"  # the solver with the FP64 floor check
-        o["reltol"] = 1e-30  # below any FP64 floor: the solve ends at the floor (status OK)
+        o["solver"] = SOLVER_CHOLESKY
+        # the fallback for bands too wide for the device: the solver with the FP64 floor check,
+        # at a tolerance below any FP64 floor (the solve ends at the floor, status OK)
+        o["precision"] = "mixed"
+        o["reltol"] = 1e-30
         o.setdefault("max_outer", 12)
         return o
     raise ValueError("linear_solver must be amg_solver or cholesky_solver")
@@ -562,8 +571,8 @@ def groundwater_steadystate(Ks, neighbors, areasoverlengths, dirichletnodes, dir
     """Steady-state heads over all cells (src/groundwater.jl:75-83).
 
     ``linear_solver``: ``amg_solver`` (default; CG + AMG to ``reltol``) or ``cholesky_solver``
-    (the same solver run to the FP64 rounding floor, i.e. direct-solve accuracy). ``kwargs``
-    are solver options (reltol, maxiter, precision='fp64'|'mixed', ...).
+    (a banded Cholesky factorisation on the GPU). ``kwargs`` are solver options (reltol, maxiter,
+    precision='fp64'|'mixed', solver='cg'|'cholesky', ...).
     """
     N = len(Qs) if not _is_torch(Qs) else Qs.numel()
     P = _problem_for(neighbors, areasoverlengths, dirichletnodes, N, _solver_options(linear_solver, kwargs))

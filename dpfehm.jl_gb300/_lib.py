@@ -16,6 +16,7 @@ STATUS_NAMES = {
 }
 MEAN_GEOMETRIC, MEAN_HARMONIC = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
+SOLVER_CG, SOLVER_CHOLESKY = 0, 1
 
 
 class Options(ctypes.Structure):
@@ -41,6 +42,7 @@ class Options(ctypes.Structure):
         ("plane_levels", ctypes.c_int),
         ("streams", ctypes.c_int),
         ("fuse", ctypes.c_int),
+        ("solver", ctypes.c_int),
     ]
 
 

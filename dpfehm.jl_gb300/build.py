@@ -12,7 +12,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libdpfehm_gpu.so")
 SOURCES = ["dpf_struct.cu", "dpf_general.cu", "dpf_api.cu", "dpf_noalloc.cu", "dpf_tune.cu", "dpf_debug.cu",
-           "dpf_richards.cu", "dpf_sampler.cu"]
+           "dpf_richards.cu", "dpf_sampler.cu", "dpf_direct.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "--extended-lambda", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
               "-I" + os.path.join(HERE, "..", "include")]

@@ -401,6 +401,7 @@ dpf_options fill_options(const dpf_options *o) {
     if (r.plane_levels < 0) r.plane_levels = d.plane_levels;
     if (r.streams < 0) r.streams = d.streams;
     if (r.fuse == 0) r.fuse = d.fuse;
+    if (r.solver != DPF_SOLVER_CHOLESKY) r.solver = DPF_SOLVER_CG;
     return r;
 }
 
@@ -501,6 +502,7 @@ void dpf_default_options(dpf_options *o) {
     o->plane_levels = 0;
     o->streams = 0;
     o->fuse = -1;
+    o->solver = DPF_SOLVER_CG;
 }
 
 int dpf_detect_regular3d(int64_t N, int64_t F, const int64_t *a, const int64_t *b, const double *aol, int *dims,

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <numeric>
 
+#include "dpf_direct.h"
 #include "dpf_general.h"
 #include "dpf_struct_kernels.cuh"
 
@@ -1070,6 +1071,7 @@ static unsigned gblocks(long long n, int cap) { return (unsigned)std::max(1LL, s
 
 void GeneralSolver::assemble(const double *Ks, const double *kc, int kind, const double *shift_, bool init_x) {
     GLevel &L0 = lv[0];
+    direct_stale = true;  // a direct factor of the previous operator is out of date
     const int n = (int)N;
     kg_assemble<<<gblocks(n, nblocks), kBlock, 0, stream>>>(n, irp, ifc, fa, fb, faol, Ks, kc, kind, L0.dir, in_dh, in_Q,
                                                            shift_, L0.leak64, b64, h, init_x ? 1 : 0);
@@ -1264,7 +1266,71 @@ void GeneralSolver::df_pcg(const double *b, double *x, double tol2) {
     }
 }
 
+// The FP64 operator in the banded Cholesky's storage: per row its diagonal leak + the sum of
+// its couplings, and from the row with the smaller index of each coupling -c at (max, min) of the
+// two band rows (added: a pair of cells joined by several faces has several couplings).
+__global__ void kg_band_fill(int n, GOp<double> A, const long long *__restrict__ iperm, long long w,
+                             double *__restrict__ band) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const long long k = iperm[i];
+        double d = A.leak[i];
+        for (int e = A.rp[i]; e < A.rp[i + 1]; e++) {
+            const int j = A.ci[e];
+            d += A.v[e];
+            if (j > i) {
+                const long long kj = iperm[j];
+                const long long r = max(k, kj), q = min(k, kj);
+                if (r - q <= w) atomicAdd(&band[q * (w + 1) + (r - q)], -A.v[e]);
+            }
+        }
+        band[k * (w + 1)] = d;
+    }
+}
+
+bool GeneralSolver::direct_solve(const double *b, double *x) {
+    GLevel &L0 = lv[0];
+    if (!direct_tried) {
+        direct_tried = true;
+        const BandOrder ord = band_order_rcm(N, hrp_, hci_);
+        size_t free_b = 0, total_b = 0;
+        GCK(cudaMemGetInfo(&free_b, &total_b));
+        if (BandCholesky::fits(N, ord.w, free_b / 2)) direct.reset(new BandCholesky(ord, stream));
+    }
+    if (!direct) return false;
+    NvtxRange range("direct solve (banded Cholesky, CSR)");
+    BandCholesky &D = *direct;
+    D.set_stream(stream);
+    const long long l0 = D.launches;
+    if (direct_stale) {
+        D.clear();
+        kg_band_fill<<<gblocks(N, nblocks), kBlock, 0, stream>>>((int)N, gop<double>(L0), D.iperm(), D.w, D.band());
+        GLAUNCH();
+        direct_ok = D.factor();
+        direct_stale = false;
+    }
+    stats_iters = 0;
+    stats_outer = 0;
+    stats_relres = 0.0;
+    h_state->total_iters = 0;
+    h_state->outer = 0;
+    if (!direct_ok) {
+        h_state->status = DPF_BAD_INPUT;
+        last_message = "the operator is not positive definite (is there a Dirichlet cell?)";
+        launches += D.launches - l0;
+        return true;
+    }
+    D.solve(b, x);
+    kg_apply<<<gblocks(N, nblocks), kBlock, 0, stream>>>((int)N, gop<double>(L0), x, r64);
+    GLAUNCH();
+    if (!d_direct_acc) d_direct_acc = dev<double>(2);
+    stats_relres = BandCholesky::relres(stream, N, L0.dir, b, r64, d_direct_acc);
+    h_state->status = std::isfinite(stats_relres) ? DPF_OK : DPF_NAN;
+    launches += D.launches - l0 + 2;
+    return true;
+}
+
 void GeneralSolver::solve(const double *b, double *x) {
+    if (opt.solver == DPF_SOLVER_CHOLESKY && direct_solve(b, x)) return;
     NvtxRange range("CG + AMG solve (CSR)");
     kg_state_init<<<1, 1, 0, stream>>>(d_state);
     GLAUNCH();

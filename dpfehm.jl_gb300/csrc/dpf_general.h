@@ -8,6 +8,7 @@
 // once per topology on the host; the numeric Galerkin rebuild each forward is a
 // deterministic gather on the device).
 #pragma once
+#include <memory>
 #include <vector>
 
 #include "dpf_struct.h"
@@ -85,6 +86,13 @@ private:
     void build_hierarchy();
     void assemble(const double *Ks, const double *kc, int kind, const double *shift, bool init_x);
     void solve(const double *b, double *x);
+    // options.solver = DPF_SOLVER_CHOLESKY: x = A^-1 b by the banded Cholesky factor of the FP64
+    // operator in reverse Cuthill-McKee order (factored again after each assembly); false when the
+    // band is too wide for the device (the iterative solve then runs instead)
+    bool direct_solve(const double *b, double *x);
+    std::unique_ptr<BandCholesky> direct;
+    bool direct_tried = false, direct_stale = true, direct_ok = false;
+    double *d_direct_acc = nullptr;
     template <typename T>
     void vcycle(const T *r, T *z);
     template <typename T>

@@ -20,6 +20,7 @@
 
 #include <cooperative_groups.h>
 
+#include "dpf_direct.h"
 #include "dpf_struct.h"
 #include "dpf_struct_kernels.cuh"
 #include "dpf_plane.cuh"
@@ -1171,6 +1172,40 @@ __global__ void k_apply(const LevelDesc *__restrict__ desc, const int4 *__restri
     }
 }
 
+// The FP64 operator in the banded Cholesky's storage (dpf_direct.h): per cell its diagonal
+// leak + the sum of its face coefficients, and, from the cell on the lower side of each face,
+// the coupling -c at (max, min) of the two cells' band rows. Dirichlet rows are identity rows.
+__global__ void k_band_fill(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap, Coeffs<double> C,
+                            const long long *__restrict__ iperm, long long w, double *__restrict__ band) {
+    int4 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    const long long sy = L.nz, sx = (long long)L.ny * L.nz;
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        const long long i = c.i, k = iperm[i];
+        double d = C.leak[i];
+        const bool up[3] = {c.iz + 1 < L.nz, c.iy + 1 < L.ny, c.ix + 1 < L.nx};
+        const long long st[3] = {1, sy, sx};
+        const double *cf[3] = {C.cz, C.cy, C.cx};
+        if (c.iz > 0) d += C.cz[i - 1];
+        if (c.iy > 0) d += C.cy[i - sy];
+        if (c.ix > 0) d += C.cx[i - sx];
+    #pragma unroll
+        for (int a = 0; a < 3; a++) {
+            if (!up[a]) continue;
+            const double v = cf[a][i];
+            d += v;
+            if (v != 0.0) {
+                const long long kj = iperm[i + st[a]];
+                const long long r = max(k, kj), q = min(k, kj);
+                if (r - q <= w) band[q * (w + 1) + (r - q)] = -v;
+            }
+        }
+        band[k * (w + 1)] = d;
+    }
+}
+
 // ================================================================ host side
 static void ck(cudaError_t e, const char *what) {
     if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e), e);
@@ -1705,6 +1740,7 @@ void StructBatch::write_tail_table() {
 
 void StructBatch::assemble(const double *Ks, const double *kc, int kind, const double *shift, bool init_x) {
     NvtxRange range("assemble operator and hierarchy");
+    direct_stale = true;  // a direct factor of the previous operator is out of date
     Level &L0 = lv[0];
     FaceK fk{Ks, kc, kind};
     if (nb_of(L0.all))
@@ -2473,6 +2509,7 @@ void StructBatch::df_pcg(const double *b64, double *x64, double tol2) {
 
 // ---- full solve of A x = b for every problem (x holds the initial guess)
 void StructBatch::solve(const double *b, double *x, double reltol) {
+    if (opt.solver == DPF_SOLVER_CHOLESKY && direct_solve(b, x)) return;
     NvtxRange range("CG + AMG solve");
     const double tol2 = reltol * reltol;
     struct ZeroGuessReset {
@@ -2640,6 +2677,55 @@ void StructBatch::apply(const double *x, double *y) {
         k_apply<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, coeffs_of<double>(L0, true), x, y);
     }
     LAUNCH_CHECK();
+}
+
+bool StructBatch::direct_solve(const double *b, double *x) {
+    Level &L0 = lv[0];
+    if (!direct_tried) {
+        direct_tried = true;
+        std::vector<std::array<int, 3>> dims;
+        std::vector<long long> off;
+        for (int p = 0; p < nprob; p++) {
+            const LevelDesc &D = L0.h_desc[p];
+            dims.push_back({D.nx, D.ny, D.nz});
+            off.push_back(D.off);
+        }
+        const BandOrder ord = band_order_regular(dims, off);
+        size_t free_b = 0, total_b = 0;
+        CK(cudaMemGetInfo(&free_b, &total_b));
+        if (BandCholesky::fits(N, ord.w, free_b / 2)) direct.reset(new BandCholesky(ord, stream));
+    }
+    if (!direct) return false;
+    NvtxRange range("direct solve (banded Cholesky)");
+    BandCholesky &D = *direct;
+    D.set_stream(stream);
+    const long long l0 = D.launches;
+    if (direct_stale) {
+        D.clear();
+        k_band_fill<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, coeffs_of<double>(L0, true),
+                                                         D.iperm(), D.w, D.band());
+        LAUNCH_CHECK();
+        direct_ok = D.factor();
+        direct_stale = false;
+    }
+    stats_iters = 0;
+    stats_outer = 0;
+    stats_relres = 0.0;
+    if (!direct_ok) {
+        last_status = DPF_BAD_INPUT;
+        last_message = "the operator is not positive definite (does every problem have a Dirichlet cell?)";
+        launches += D.launches - l0;
+        return true;
+    }
+    D.solve(b, x);
+    // the relative residual over the free cells, for the statistics
+    apply(x, r64);
+    if (!d_direct_acc) d_direct_acc = (double *)dalloc_bytes(2 * sizeof(double));
+    stats_relres = BandCholesky::relres(stream, N, L0.dir, b, r64, d_direct_acc);
+    last_status = std::isfinite(stats_relres) ? DPF_OK : DPF_NAN;
+    if (last_status != DPF_OK) last_message = "non-finite residual after the direct solve";
+    launches += D.launches - l0 + 2;
+    return true;
 }
 
 // ---- transient backward Euler with checkpointed adjoint

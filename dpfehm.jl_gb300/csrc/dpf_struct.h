@@ -2,6 +2,7 @@
 #pragma once
 #include <array>
 #include <map>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -34,6 +35,7 @@ struct GridSpec {
 };
 
 class StructBatch;
+class BandCholesky;
 
 // Counts every kernel launch and, while profiling is on, brackets it with a pair
 // of CUDA events on the launching stream (per-kernel device time).
@@ -139,6 +141,13 @@ public:
     template <typename T>
     void pcg_iteration(T *x);
     void df_iteration(double *x64);
+    // options.solver = DPF_SOLVER_CHOLESKY: x = A^-1 b by the banded Cholesky factor of the FP64
+    // operator (factored again after each assembly); false when the band is too wide for the device
+    // (the iterative solve then runs instead)
+    bool direct_solve(const double *b, double *x);
+    std::unique_ptr<BandCholesky> direct;
+    bool direct_tried = false, direct_stale = true, direct_ok = false;
+    double *d_direct_acc = nullptr;  // the direct solve's residual sums
     cudaGraphExec_t loop_graph(int kind, void *x);
     void run_loop(int kind, void *x);
     int read_count(int which);

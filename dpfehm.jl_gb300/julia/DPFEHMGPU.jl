@@ -39,12 +39,13 @@ mutable struct Options
     plane_levels::Cint
     streams::Cint
     fuse::Cint
+    solver::Cint
 end
 
 """The library defaults with any `dpf_options` field overridden by keyword (`precision` as
 `:fp64` or `:mixed`)."""
 function default_options(; kwargs...)
-    o = Options(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
+    o = Options(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0)
     ccall((:dpf_default_options, libdpf), Cvoid, (Ref{Options},), o)
     for (k, v) in pairs(kwargs)
         if k === :precision
@@ -127,11 +128,13 @@ function adjoint(p::Problem, delta)
 end
 
 """Selectors for the `linear_solver` keyword: `amg_solver` (CG + AMG to reltol, the default)
-and `cholesky_solver` (the same GPU solver run to the FP64 rounding floor of the system)."""
+and `cholesky_solver` (a banded Cholesky factorisation of the operator on the GPU; a band too
+wide for the device falls back to the CG solver run to the FP64 rounding floor)."""
 function amg_solver end
 function cholesky_solver end
 
-solver_kwargs(ls, kwargs) = ls === cholesky_solver ? merge((; max_outer=12), kwargs, (; precision=:mixed, reltol=1e-30)) : kwargs
+solver_kwargs(ls, kwargs) = ls === cholesky_solver ?
+    merge((; max_outer=12), kwargs, (; solver=1, precision=:mixed, reltol=1e-30)) : kwargs
 
 """Drop-in for `DPFEHM.groundwater_steadystate`."""
 function groundwater_steadystate(Ks, neighbors, areasoverlengths, dirichletnodes, dirichleths, Qs;

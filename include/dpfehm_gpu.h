@@ -66,6 +66,16 @@ typedef enum {
                            FP64 CG scalars */
 } dpf_precision;
 
+typedef enum {
+    DPF_SOLVER_CG = 0,       /* AMG-preconditioned CG to reltol (the reference's amg_solver) */
+    DPF_SOLVER_CHOLESKY = 1  /* banded Cholesky factorisation of the FP64 operator (the reference's
+                                cholesky_solver, src/groundwater.jl:56-60): the rows renumbered into a
+                                narrow band (regular grids: the two shortest axes fastest; other meshes:
+                                reverse Cuthill-McKee), factored once per assembly, two triangular solves
+                                per solve; a band too wide for the device (more than half its free memory,
+                                or above about 2e13 multiply-adds) falls back to the CG solve */
+} dpf_solver;
+
 typedef struct dpf_options {
     double reltol;       /* stop when ||b - A h|| <= reltol * ||b||            (default 1e-10) */
     int maxiter;         /* CG iteration cap per solve                        (default 500)   */
@@ -104,6 +114,8 @@ typedef struct dpf_options {
                             post-smoothing (the intermediate iterate stays in shared memory); half
                             the bytes, but more instructions per cell, and slower on GB300 at the
                             benchmark sizes (default -1: separate passes; an autotuner choice) */
+    int solver;          /* dpf_solver: steady and transient solves of single problems and batches
+                            (default DPF_SOLVER_CG) */
 } dpf_options;
 
 typedef struct dpf_problem dpf_problem;

@@ -85,6 +85,7 @@ def test_default_options(pkg, lib):
     assert o.plane_levels == 0
     assert o.streams == 0
     assert o.fuse == -1
+    assert o.solver == pkg.SOLVER_CG
 
 
 @pytest.mark.parametrize("ns", [(4, 3, 2), (7, 1, 5), (1, 6, 3), (5, 4, 1), (9, 1, 1), (1, 1, 8), (3, 3, 3)])
