@@ -1,10 +1,9 @@
 // dpf_direct.cu -- banded Cholesky factorisation and solves (see dpf_direct.h).
 //
-// Factorisation: right-looking, in blocks of kNB = 32 columns. Per block three launches: the
-// 32 x 32 diagonal block factored by one CTA (a thread per entry, in shared memory); the panel
-// below it, up to w rows, solved against that block (a thread per row); and the symmetric
-// update of the trailing window, at most (w + 32)^2 / 2 entries inside the band, in 32 x 32
-// tiles. Triangular solves: one CTA that walks the blocks in order (forward) and in reverse
+// Factorisation: right-looking, in blocks of kNB = 32 columns. Per block two launches: the
+// 32 x 32 diagonal block factored in shared memory by every CTA of the panel solve, which then
+// solves the panel below it (up to w rows, a thread per row); and the symmetric update of the
+// trailing window, at most (w + 32)^2 / 2 entries inside the band, in 32 x 32 tiles. Triangular solves: one CTA that walks the blocks in order (forward) and in reverse
 // (backward); per block one warp solves the 32 x 32 triangle and the CTA applies the block's
 // columns to the up to w rows (forward) or columns (backward) that depend on it.
 // All arithmetic is FP64.
@@ -26,46 +25,49 @@ constexpr int kSolveThreads = 1024;
 
 __device__ __forceinline__ long long bidx(long long r, long long c, long long w) { return c * (w + 1) + (r - c); }
 
-// factor the diagonal block [j0, j0 + jb): thread (tx, ty) owns entry (ty, tx), tx <= ty
-__global__ void __launch_bounds__(kNB * kNB) k_band_potrf(double *__restrict__ B, long long w, long long j0, int jb,
-                                                          int *err) {
-    __shared__ double a[kNB][kNB + 1];
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const bool own = tx <= ty && ty < jb && (long long)(ty - tx) <= w;
-    a[ty][tx] = own ? B[bidx(j0 + ty, j0 + tx, w)] : 0.0;
-    for (int k = 0; k < jb; k++) {
-        __syncthreads();
-        if (tx == k && ty == k) {
-            double d = a[k][k];
-            if (!(d > 0.0)) {  // not positive definite: recorded; a unit pivot keeps the rest finite
-                atomicExch(err, 1);
-                d = 1.0;
-            }
-            a[k][k] = sqrt(d);
-        }
-        __syncthreads();
-        if (tx == k && ty > k && ty < jb) a[ty][k] /= a[k][k];
-        __syncthreads();
-        if (tx > k && tx <= ty && ty < jb) a[ty][tx] -= a[ty][k] * a[tx][k];
-    }
-    __syncthreads();
-    if (own) B[bidx(j0 + ty, j0 + tx, w)] = a[ty][tx];
-}
-
-// the panel rows r in [j0 + jb, r_end) of the block's columns: L[r, c] = (A[r, c] - sum_{k < c}
-// L[r, k] L[c, k]) / L[c, c]; columns c < r - w are outside the band and stay zero
-__global__ void __launch_bounds__(256) k_band_trsm(double *__restrict__ B, long long w, long long j0, int jb,
-                                                   long long r_end) {
+// One block step's diagonal factorisation and panel solve, in one launch: every CTA factors the
+// 32 x 32 diagonal block [j0, j0 + jb) in shared memory (the same arithmetic in every CTA, so the
+// same result; CTA 0 stores it and reports a non-positive pivot), then solves its 256 rows of the
+// panel r in [j0 + jb, r_end): L[r, c] = (A[r, c] - sum_{k < c} L[r, k] L[c, k]) / L[c, c];
+// columns c < r - w are outside the band and stay zero.
+constexpr int kPanelThreads = 256;
+__global__ void __launch_bounds__(kPanelThreads) k_band_panel(double *__restrict__ B, long long w, long long j0,
+                                                              int jb, long long r_end, int *err) {
     __shared__ double d[kNB][kNB + 1];
     __shared__ double inv[kNB];
-    for (int e = threadIdx.x; e < kNB * kNB; e += blockDim.x) {
-        const int i = e / kNB, j = e % kNB;
+    const int t = threadIdx.x;
+    for (int e = t; e < kNB * kNB; e += kPanelThreads) {
+        const int j = e / kNB, i = e % kNB;  // consecutive threads: consecutive rows of column j
         d[i][j] = (j <= i && i < jb && (long long)(i - j) <= w) ? B[bidx(j0 + i, j0 + j, w)] : 0.0;
     }
+    for (int k = 0; k < jb; k++) {
+        __syncthreads();
+        if (t == 0) {
+            double v = d[k][k];
+            if (!(v > 0.0)) {  // not positive definite: recorded; a unit pivot keeps the rest finite
+                if (blockIdx.x == 0) atomicExch(err, 1);
+                v = 1.0;
+            }
+            d[k][k] = sqrt(v);
+            inv[k] = 1.0 / d[k][k];
+        }
+        __syncthreads();
+        if (t > k && t < jb) d[t][k] *= inv[k];
+        __syncthreads();
+        // trailing entries (i, j), k < j <= i < jb (zero outside the band stays zero: a factor of
+        // each product is zero there)
+        for (int e = t; e < kNB * kNB; e += kPanelThreads) {
+            const int i = e / kNB, j = e % kNB;
+            if (j > k && j <= i && i < jb) d[i][j] -= d[i][k] * d[j][k];
+        }
+    }
     __syncthreads();
-    if (threadIdx.x < kNB) inv[threadIdx.x] = threadIdx.x < jb ? 1.0 / d[threadIdx.x][threadIdx.x] : 0.0;
-    __syncthreads();
-    const long long r = j0 + jb + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (blockIdx.x == 0)
+        for (int e = t; e < kNB * kNB; e += kPanelThreads) {
+            const int j = e / kNB, i = e % kNB;
+            if (j <= i && i < jb && (long long)(i - j) <= w) B[bidx(j0 + i, j0 + j, w)] = d[i][j];
+        }
+    const long long r = j0 + jb + (long long)blockIdx.x * kPanelThreads + t;
     if (r >= r_end) return;
     const int cmin = (int)max(0LL, r - w - j0);
     double x[kNB];
@@ -117,30 +119,50 @@ __global__ void k_scatter(long long n, const long long *__restrict__ perm, const
         x[perm[k]] = y[k];
 }
 
+// the lower triangle of diagonal block [j0, j0 + jb) into d (zeros elsewhere), by all threads
+// (consecutive threads read consecutive rows of one column: consecutive in the band), with the
+// reciprocals of its diagonal on the diagonal (one FP64 division per entry, in parallel, instead
+// of 32 in the sequential solve)
+__device__ __forceinline__ void load_diag(const double *__restrict__ B, long long w, long long j0, int jb,
+                                          double (*d)[kNB + 1]) {
+    for (int e = threadIdx.x; e < kNB * kNB; e += blockDim.x) {
+        const int j = e / kNB, i = e % kNB;
+        double v = (j <= i && i < jb && (long long)(i - j) <= w) ? B[bidx(j0 + i, j0 + j, w)] : 0.0;
+        if (i == j) v = i < jb ? 1.0 / v : 0.0;
+        d[i][j] = v;
+    }
+}
+
 // L z = y, then L^T x = z, in place in y, by one CTA walking the blocks. Forward, per block: warp
-// 0 solves the 32 x 32 triangle (lane i holds row j0 + i), then every thread applies the block's
-// columns to its rows below (up to w rows, consecutive rows consecutive in the band). Backward,
+// 0 solves the 32 x 32 triangle (lane i holds row j0 + i) from the block's entries staged in
+// shared memory, then every thread applies the block's columns to its rows below (up to w rows,
+// consecutive rows consecutive in the band), while the next block's triangle is staged. Backward,
 // per block from the last: warp 0 solves the transposed triangle, then the CTA applies the
 // block's rows to the columns above it that reach them (each thread one column, its entries in
 // the block's rows contiguous in the band).
 __global__ void __launch_bounds__(kSolveThreads) k_band_solve(const double *__restrict__ B, long long n, long long w,
                                                                double *__restrict__ y) {
+    __shared__ double d[2][kNB][kNB + 1];
     const int t = threadIdx.x, lane = t & 31;
     const long long nblk = (n + kNB - 1) / kNB;
+    load_diag(B, w, 0, (int)min((long long)kNB, n), d[0]);
+    __syncthreads();
     for (long long b = 0; b < nblk; b++) {
         const long long j0 = b * kNB;
         const int jb = (int)min((long long)kNB, n - j0);
+        double(*D)[kNB + 1] = d[b & 1];
         if (t < 32) {
             double v = lane < jb ? y[j0 + lane] : 0.0;
             for (int k = 0; k < jb; k++) {
-                double z = v / B[bidx(j0 + k, j0 + k, w)];  // meaningful in lane k
+                double z = v * D[k][k];  // meaningful in lane k (D[k][k] holds 1 / L[k][k])
                 z = __shfl_sync(0xffffffffu, z, k);
                 if (lane == k) v = z;
-                else if (lane > k && lane < jb && (long long)(lane - k) <= w) v -= B[bidx(j0 + lane, j0 + k, w)] * z;
+                else if (lane > k) v -= D[lane][k] * z;  // zero outside the band and past jb
             }
             if (lane < jb) y[j0 + lane] = v;
         }
         __syncthreads();
+        if (b + 1 < nblk) load_diag(B, w, j0 + kNB, (int)min((long long)kNB, n - j0 - kNB), d[(b + 1) & 1]);
         const long long r_end = min(n, j0 + jb + w);
         for (long long r = j0 + jb + t; r < r_end; r += kSolveThreads) {
             double s = 0.0;
@@ -150,20 +172,25 @@ __global__ void __launch_bounds__(kSolveThreads) k_band_solve(const double *__re
         }
         __syncthreads();
     }
+    // backward step s = nblk - 1 - b uses d[s & 1] and stages the next block into d[(s + 1) & 1]
+    load_diag(B, w, (nblk - 1) * kNB, (int)(n - (nblk - 1) * kNB), d[0]);
+    __syncthreads();
     for (long long b = nblk - 1; b >= 0; b--) {
         const long long j0 = b * kNB;
         const int jb = (int)min((long long)kNB, n - j0);
+        double(*D)[kNB + 1] = d[(nblk - 1 - b) & 1];
         if (t < 32) {
             double v = lane < jb ? y[j0 + lane] : 0.0;
             for (int k = jb - 1; k >= 0; k--) {
-                double x = v / B[bidx(j0 + k, j0 + k, w)];
+                double x = v * D[k][k];
                 x = __shfl_sync(0xffffffffu, x, k);
                 if (lane == k) v = x;
-                else if (lane < k && (long long)(k - lane) <= w) v -= B[bidx(j0 + k, j0 + lane, w)] * x;
+                else if (lane < k) v -= D[k][lane] * x;
             }
             if (lane < jb) y[j0 + lane] = v;
         }
         __syncthreads();
+        if (b > 0) load_diag(B, w, j0 - kNB, kNB, d[(nblk - b) & 1]);
         const long long c_lo = max(0LL, j0 - w);
         for (long long c = c_lo + t; c < j0; c += kSolveThreads) {
             double s = 0.0;
@@ -340,15 +367,15 @@ bool BandCholesky::factor() {
     dck(cudaMemsetAsync(d_err, 0, sizeof(int), stream), "factor");
     for (long long j0 = 0; j0 < n; j0 += kNB) {
         const int jb = (int)std::min<long long>(kNB, n - j0);
-        k_band_potrf<<<1, dim3(kNB, kNB), 0, stream>>>(B, w, j0, jb, d_err);
-        launches++;
         const long long r_end = std::min(n, j0 + jb + w);
         const long long m = r_end - (j0 + jb);
+        k_band_panel<<<(unsigned)std::max(1LL, (m + kPanelThreads - 1) / kPanelThreads), kPanelThreads, 0, stream>>>(
+            B, w, j0, jb, r_end, d_err);
+        launches++;
         if (m > 0) {
-            k_band_trsm<<<(unsigned)((m + 255) / 256), 256, 0, stream>>>(B, w, j0, jb, r_end);
             const unsigned nt = (unsigned)((m + kNB - 1) / kNB);
             k_band_syrk<<<dim3(nt, nt), dim3(kNB, kNB), 0, stream>>>(B, w, j0, jb, j0 + jb, r_end);
-            launches += 2;
+            launches++;
         }
     }
     dck(cudaGetLastError(), "factor launch");
