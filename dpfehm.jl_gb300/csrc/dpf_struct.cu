@@ -1032,6 +1032,64 @@ __global__ void k_grad_logk(const LevelDesc *__restrict__ desc, const int4 *__re
     }
 }
 
+// Mixed handles, geometric means: d/dlogK of k_grad_logk in double-float arithmetic on the FP32
+// pipe (the FP64 form is bound by GB300's FP64 rate). A pre-pass splits h, lambda and the cell
+// factors kc into double-floats (integer operations, 48 bits); the differences h_i - h_j and
+// lambda_i - lambda_j are then formed from those, which keeps about 48 bits of each difference
+// relative to |h| (a relative error of 2^-48 |h| / |h_i - h_j|, far inside the gradient's 1e-6).
+__global__ void k_grad_split(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
+                             const double *__restrict__ h, const double *__restrict__ lam,
+                             const double *__restrict__ kc, float2 *__restrict__ hd, float2 *__restrict__ ld,
+                             float2 *__restrict__ kd) {
+    int4 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    auto split = [](double v) {
+        float2 q;
+        double v48;
+        if (!split48(v, q.x, q.y, v48)) q = df_from_double(v);
+        return q;
+    };
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        const long long i = L.off + li_;
+        hd[i] = split(h[i]);
+        ld[i] = split(lam[i]);
+        kd[i] = split(kc[i]);
+    }
+}
+
+__global__ void k_grad_logk_df(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
+                               const ProbParam *__restrict__ prm, const float2 *__restrict__ kd,
+                               const float2 *__restrict__ hd, const float2 *__restrict__ ld, double *__restrict__ g) {
+    int4 bm = bmap[blockIdx.x];
+    const LevelDesc L = desc[bm.x];
+    const ProbParam P = prm[bm.x];
+    const float2 w3[3] = {df_from_double(-0.5 * P.aol[0]), df_from_double(-0.5 * P.aol[1]),
+                          df_from_double(-0.5 * P.aol[2])};
+    const long long st3[3] = {(long long)L.ny * L.nz, (long long)L.nz, 1};
+    for (int li_ = bm.y * kBlock + (int)threadIdx.x; li_ < (int)L.n; li_ += bm.z * kBlock) {
+        Cell c;
+        cell_at(L, li_, c);
+        const int co[3] = {c.ix, c.iy, c.iz};
+        const int nn[3] = {L.nx, L.ny, L.nz};
+        const float2 hi = hd[c.i], li = ld[c.i], ki = kd[c.i];
+        float2 acc = make_float2(0.f, 0.f);
+    #pragma unroll
+        for (int d = 0; d < 3; d++) {
+            float2 sd = make_float2(0.f, 0.f);
+            if (co[d] + 1 < nn[d]) {
+                const long long j = c.i + st3[d];
+                sd = df_add(sd, df_mul(kd[j], df_mul(df_sub(hi, hd[j]), df_sub(li, ld[j]))));
+            }
+            if (co[d] > 0) {
+                const long long j = c.i - st3[d];
+                sd = df_add(sd, df_mul(kd[j], df_mul(df_sub(hi, hd[j]), df_sub(li, ld[j]))));
+            }
+            acc = df_add(acc, df_mul(df_mul(w3[d], ki), sd));
+        }
+        g[c.i] = df_to_double(acc);
+    }
+}
+
 // per-cell values for the face means: exp(logK / 2) (geometric) or exp(logK) (harmonic)
 __global__ void k_cell_k(const LevelDesc *__restrict__ desc, const int4 *__restrict__ bmap,
                          const double *__restrict__ logK, int kind, double *__restrict__ kc) {
@@ -2621,6 +2679,22 @@ void StructBatch::grad_faces(const double *hv, const double *lv_, double *dKs, b
 
 void StructBatch::grad_logk(double *g) {
     Level &L0 = lv[0];
+    if (mixed && mean_kind == DPF_MEAN_GEOMETRIC) {
+        // the CG's double-float vectors are free once the solves are done
+        {
+            KTimer _kt(this, kname("k_grad_split", 0, false), L0.all_cells);
+            k_grad_split<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, h, lam, in_kc, dfv[2],
+                                                               dfv[3], dfv[1]);
+        }
+        LAUNCH_CHECK();
+        {
+            KTimer _kt(this, kname("k_grad_logk", 0, true), L0.all_cells);
+            k_grad_logk_df<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_prm, dfv[1], dfv[2],
+                                                                 dfv[3], g);
+        }
+        LAUNCH_CHECK();
+        return;
+    }
     {
         KTimer _kt(this, kname("k_grad_logk", 0, false), L0.all_cells);
         k_grad_logk<<<nb_of(L0.all), kBlock, 0, stream>>>(L0.d_desc, L0.all.d_map, d_prm, in_kc, mean_kind, h, lam,
