@@ -11,7 +11,9 @@
 //
 // The arithmetic is that of the per-cell bodies in dpf_struct.cu in the same order
 // (apply7: z+, z-, y+, y-, x+, x-), so results are bitwise identical to the grid-stride
-// kernels. Every mbarrier wait is bounded (one second); on expiry the kernel records an error in
+// kernels, except in the two fused pre-smoothing steps from zero (PM_FIRST2), which stage the
+// first step's iterate in place of b and recover the cell's own b from it (a few ulps of FP32).
+// Every mbarrier wait is bounded (one second); on expiry the kernel records an error in
 // *err, and the producer drains its copies (bounded, an expiry recorded too) before the block returns.
 #pragma once
 #include <cstdint>
@@ -220,9 +222,15 @@ __device__ __forceinline__ void pm_drain(int issued, uint64_t *full, int *err) {
     for (int g = max(0, issued - R); g < issued; g++) mbar_wait(&full[g % R], (uint32_t)((g / R) & 1), err);
 }
 
+// x / y for the plane smoothers: FP32 takes the fast approximate division (about 2 ulp, ample in
+// a smoother), FP64 the exact one
+__device__ __forceinline__ float pm_div(float x, float y) { return __fdividef(x, y); }
+__device__ __forceinline__ double pm_div(double x, double y) { return x / y; }
+
 // Chebyshev step family on the plane ring. MODE bits:
 //   PM_FIRST2  the first two steps from a zero guess (reads b and the inverse diagonal
-//              with halos instead of an iterate)
+//              with halos instead of an iterate; the first step's iterate invtheta b g is
+//              formed once per staged plane, in place of b, before the plane is used)
 //   PM_FIRST   d = c2 r (d not read)
 //   PM_PROLONG the iterate is corrected on arrival: x += scale * e[aggregate] (not at
 //              identity rows), i.e. the prolongation fused into the first post-step
@@ -232,7 +240,8 @@ __device__ __forceinline__ void pm_drain(int issued, uint64_t *full, int *err) {
 // Warp-specialised pipeline: warp kPlaneThreads/32 is the producer (its lane 0 stages
 // plane after plane as ring slots free up), warps 0..7 consume. Per slot three mbarriers:
 // full (copies landed), empty (all consumer warps are done with the plane), ready (with
-// PM_PROLONG: every consumer thread has applied its share of the correction). A block marches
+// PM_PROLONG or PM_FIRST2: every consumer thread has applied its share of the correction or of
+// the first step). A block marches
 // through its items one after another; at the end of each item every thread meets (a block
 // barrier that also carries the error flag, and with PM_RZ the item's partial of b . xout in its
 // own reduction slot, so the sum per problem is formed in a fixed order).
@@ -349,6 +358,17 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
                         break;
                     }
                     waited = q;
+                    if (F2) {
+                        // the first step's iterate x1 = invtheta b g of every staged cell, once per
+                        // plane, in place of b (the cell's own b is recovered as x1 / (invtheta g))
+                        char *sl = slot_of(g);
+                        const long long lh = L.off + (long long)q * sx + (long long)(y0 - 1) * nz;
+                        T *Bq_ = (T *)(sl + lay.oB) + stage_delta(lh, es);
+                        const T *Gq_ = (const T *)(sl + lay.oG) + stage_delta(lh, es);
+                        const int nh = (rows + 2) * nz;
+                        for (int k = t; k < nh; k += kPlaneThreads) Bq_[k] = invtheta * Bq_[k] * Gq_[k];
+                        mbar_arrive(&ready[g % R]);
+                    }
                     if (PROL) {
                         // prolongation on arrival: this thread's share of the slab and its halo rows
                         char *sl = slot_of(g);
@@ -370,7 +390,7 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
                     }
                 }
                 if (bad) break;
-                if (PROL) {
+                if (PROL || F2) {
                     for (int q = first_new; q <= waited; q++) {
                         const int g = gof(q);
                         if (!mbar_wait(&ready[g % R], (uint32_t)((g / R) & 1), err)) {
@@ -406,26 +426,20 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
                         const long long i = lp + tc;
                         const int c = nz + tc;  // own cell in halo coordinates
                         if (F2) {
-                            // x1 = invtheta b g at a cell; neighbours from the staged b and g halos
-                            const T *B = (const T *)(sc + lay.oB) + dh;
+                            // x1 = invtheta b g, staged in place of b for every cell of the plane
+                            // and its halo; the cell's own b is x1 / (invtheta g) (g > 0)
+                            const T *X1 = (const T *)(sc + lay.oB) + dh;
                             const T *G = (const T *)(sc + lay.oG) + dh;
-                            const T bi = B[c], gi = G[c];
-                            const T x1 = invtheta * bi * gi;
+                            const T gi = G[c];
+                            const T x1 = X1[c];
+                            const T bi = pm_div(x1, invtheta * gi);
                             T a = cf(LK[tc]) * x1;
-                            if (f & CF_ZP) a += cf(CZ[tc]) * (x1 - invtheta * B[c + 1] * G[c + 1]);
-                            if (f & CF_ZM) a += cf(CZ[tc - 1]) * (x1 - invtheta * B[c - 1] * G[c - 1]);
-                            if (f & CF_YP) a += cf(CY[c]) * (x1 - invtheta * B[c + nz] * G[c + nz]);
-                            if (f & CF_YM) a += cf(CY[tc]) * (x1 - invtheta * B[c - nz] * G[c - nz]);
-                            if (xp) {
-                                const T *Bn = (const T *)(sn + lay.oB) + dn_;
-                                const T *Gn = (const T *)(sn + lay.oG) + dn_;
-                                a += cf(CX[tc]) * (x1 - invtheta * Bn[c] * Gn[c]);
-                            }
-                            if (xm) {
-                                const T *Bq = (const T *)(sq + lay.oB) + dq;
-                                const T *Gq = (const T *)(sq + lay.oG) + dq;
-                                a += cf(CXq[tc]) * (x1 - invtheta * Bq[c] * Gq[c]);
-                            }
+                            if (f & CF_ZP) a += cf(CZ[tc]) * (x1 - X1[c + 1]);
+                            if (f & CF_ZM) a += cf(CZ[tc - 1]) * (x1 - X1[c - 1]);
+                            if (f & CF_YP) a += cf(CY[c]) * (x1 - X1[c + nz]);
+                            if (f & CF_YM) a += cf(CY[tc]) * (x1 - X1[c - nz]);
+                            if (xp) a += cf(CX[tc]) * (x1 - ((const T *)(sn + lay.oB) + dn_)[c]);
+                            if (xm) a += cf(CXq[tc]) * (x1 - ((const T *)(sq + lay.oB) + dq)[c]);
                             const T dn = c1 * x1 + c2 * (bi - a) * gi;
                             if (!NOD) d[i] = dn;
                             xout[i] = x1 + dn;
