@@ -347,6 +347,21 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
                 }
                 cfl[k] = f;
             }
+            // PM_PROLONG: this thread's first kHaloSlots elements k = t + m kPlaneThreads of a staged
+            // plane and its halo rows, and the offset of each one's aggregate in the staged coarse
+            // plane (-1: past the halo, or a row outside the grid); the same in every plane
+            constexpr int kHaloSlots = PROL ? CPT + 2 : 1;
+            int eoff[kHaloSlots];
+#pragma unroll
+            for (int m = 0; m < kHaloSlots; m++) {
+                const int k = t + m * kPlaneThreads;
+                eoff[m] = -1;
+                if (PROL && k < (rows + 2) * nz) {
+                    const int rr = div_nz(L, k);
+                    const int row = y0 - 1 + rr;
+                    if (row >= 0 && row < ny) eoff[m] = ((row >> 1) - cr_lo) * Lc.nz + ((k - rr * nz) >> 1);
+                }
+            }
             int waited = pl_lo - 1, released = pl_lo;
             for (int x = xa; x < xe && !bad; x++) {
                 const int need = min(x + 1, pl_hi);
@@ -379,7 +394,10 @@ __global__ void __launch_bounds__(kPlaneThreads + 32) k_pm_cheb(
                         const long long cb = Lc.off + (long long)(q >> 1) * csx;
                         const T *E = (const T *)(sl + lay.oE) + stage_delta(cb + (long long)cr_lo * Lc.nz, es);
                         const int nh = (rows + 2) * nz;
-                        for (int k = t; k < nh; k += kPlaneThreads) {
+#pragma unroll
+                        for (int m = 0; m < kHaloSlots; m++)  // offsets worked out once per item
+                            if (eoff[m] >= 0 && !DR[t + m * kPlaneThreads]) X[t + m * kPlaneThreads] += scale * E[eoff[m]];
+                        for (int k = t + kHaloSlots * kPlaneThreads; k < nh; k += kPlaneThreads) {
                             const int rr = div_nz(L, k);
                             const int row = y0 - 1 + rr;
                             if (row < 0 || row >= ny || DR[k]) continue;
