@@ -743,9 +743,11 @@ __global__ void __launch_bounds__(kPlaneThreads, (DPF_DF_FLUX_MINB / CPT > 0 ? D
                  float2 *__restrict__ qv) {
     pdl_enter();
     constexpr unsigned CF_YIN = 32u;  // the y- neighbour is inside the slab
-    __shared__ float2 fz_s[2][CPT * kPlaneThreads], fy_s[2][CPT * kPlaneThreads];
+    // z fluxes with one leading zero entry (the z- flux of the slab's first cell, z = 0), y fluxes
+    __shared__ float2 fz_s[2][CPT * kPlaneThreads + 1], fy_s[2][CPT * kPlaneThreads];
     const int t = threadIdx.x;
     const float2 zero = make_float2(0.f, 0.f);
+    if (t < 2) fz_s[t][0] = zero;  // written before the first block barrier of the first item
     for (int w = work.first[blockIdx.x]; w < work.first[blockIdx.x + 1]; w++) {
         const int4 it = work.items[w];
         const int p = it.x, y0 = it.y, xa = it.z, xe = it.w;
@@ -759,15 +761,21 @@ __global__ void __launch_bounds__(kPlaneThreads, (DPF_DF_FLUX_MINB / CPT > 0 ? D
         long long ic[CPT];
         float2 pi[CPT], fxm[CPT];
         FluxPlane cur[CPT];
-        // the operands of the plane at ic (x < nx, so the x+1 load is guarded by x + 1 < nx)
+        // the operands of the plane at ic (x < nx, so the x+1 load is guarded by x + 1 < nx). The
+        // z+ and y+ operands are read unconditionally: the assembly stores a zero coefficient for
+        // a face that does not exist (the grid's last z or y) or that leads to a Dirichlet cell, so
+        // such a flux is exactly zero and adding it leaves the (normalised) double-float sum as it
+        // is; the neighbour index is clamped to the problem's last cell, so the p read there is a
+        // finite value of the same array.
+        const long long ilast = L.off + L.n - 1;
         auto fetch = [&](FluxPlane &o, unsigned f, long long i, int x) {
-            o.pz = (f & CF_ZP) ? pv[i + 1] : zero;
-            o.py = (f & CF_YP) ? pv[i + nz] : zero;
+            o.pz = pv[min(i + 1, ilast)];
+            o.py = pv[min(i + nz, ilast)];
             const bool ylo = (f & CF_YM) && !(f & CF_YIN);
             o.pym = ylo ? pv[i - nz] : zero;
             o.pn = x + 1 < nx ? pv[i + sx] : zero;
-            o.cz = (f & CF_ZP) ? C.cz[i] : zero;
-            o.cy = (f & CF_YP) ? C.cy[i] : zero;
+            o.cz = C.cz[i];
+            o.cy = C.cy[i];
             o.cym = ylo ? C.cy[i - nz] : zero;
             o.cx = x + 1 < nx ? C.cx[i] : zero;
             o.lk = C.leak[i];
@@ -807,7 +815,7 @@ __global__ void __launch_bounds__(kPlaneThreads, (DPF_DF_FLUX_MINB / CPT > 0 ? D
         Acc<float> part;
         for (int x = xa; x < xe; x++) {
             const bool xp = x + 1 < nx, xm = x > 0;
-            float2 *fzb = fz_s[x & 1], *fyb = fy_s[x & 1];
+            float2 *fzb = fz_s[x & 1] + 1, *fyb = fy_s[x & 1];
             float2 fz[CPT], fy[CPT], fx[CPT];
             FluxPlane nxt[CPT];
 #pragma unroll
@@ -818,8 +826,8 @@ __global__ void __launch_bounds__(kPlaneThreads, (DPF_DF_FLUX_MINB / CPT > 0 ? D
                 if (!f) continue;
                 if (x + 1 < xe) fetch(nxt[k], f, ic[k] + sx, x + 1);
                 const FluxPlane &o = cur[k];
-                if (f & CF_ZP) fz[k] = df_mul(o.cz, df_sub(pi[k], o.pz));
-                if (f & CF_YP) fy[k] = df_mul(o.cy, df_sub(pi[k], o.py));
+                fz[k] = df_mul(o.cz, df_sub(pi[k], o.pz));  // zero where no z+ face
+                fy[k] = df_mul(o.cy, df_sub(pi[k], o.py));  // zero where no y+ face
                 if (xp) fx[k] = df_mul(o.cx, df_sub(pi[k], o.pn));
                 fzb[tc] = fz[k];
                 fyb[tc] = fy[k];
@@ -832,9 +840,9 @@ __global__ void __launch_bounds__(kPlaneThreads, (DPF_DF_FLUX_MINB / CPT > 0 ? D
                 if (!f) continue;
                 const FluxPlane &o = cur[k];
                 float2 a = df_mul(o.lk, pi[k]);
-                if (f & CF_ZP) a = df_add(a, fz[k]);
-                if (f & CF_ZM) a = df_sub(a, fzb[tc - 1]);
-                if (f & CF_YP) a = df_add(a, fy[k]);
+                a = df_add(a, fz[k]);
+                a = df_sub(a, fzb[tc - 1]);  // zero at z = 0: the row below ends with a zero z+ flux
+                a = df_add(a, fy[k]);
                 if (f & CF_YM) a = (f & CF_YIN) ? df_sub(a, fyb[tc - nz]) : df_add(a, df_mul(o.cym, df_sub(pi[k], o.pym)));
                 if (xp) a = df_add(a, fx[k]);
                 if (xm) a = df_sub(a, fxm[k]);
