@@ -1548,7 +1548,12 @@ StructBatch::StructBatch(const std::vector<GridSpec> &grids, const std::vector<s
         L.all = build_map(L.h_desc, has, owned, nprob, target_blocks);
         L.smooth = build_map(L.h_desc, smooth, owned, nprob, target_blocks);
         L.restr = build_map(L.h_desc, restr, owned, nprob, target_blocks);
-        const bool plane_here = opt.plane > 0 && (opt.plane_levels <= 0 || l < opt.plane_levels);
+        // plane-marching smoothers where the batch is large enough to fill the GPU with their
+        // work runs: a finest level of 2^21 cells or more (an 800k-cell single problem ran 8 %
+        // faster on the grid-stride kernels), or at any size with plane >= 2
+        const long long fine_cells = l == 0 ? off : lv[0].ntot;
+        const bool plane_on = opt.plane >= 2 || (opt.plane > 0 && fine_cells >= (1LL << 21));
+        const bool plane_here = plane_on && (opt.plane_levels <= 0 || l < opt.plane_levels);
         build_plane_items(L.pm, L, smooth, sms, plane_here ? opt.plane_cells : 0, opt.plane_blocks_per_sm, &shapes,
                           l);
         if (l == 0)

@@ -93,7 +93,8 @@ typedef struct dpf_options {
     int tail_cells;      /* regular grids: the multigrid levels of a problem with at most this many cells
                             run as one fused kernel per problem (default 4096; negative: off) */
     int plane;           /* regular grids, MIXED: plane-marching smoother kernels with shared-memory
-                            staging (default 1; negative: grid-stride kernels) */
+                            staging (default 1: where the finest level of the handle holds at least
+                            2^21 cells; 2: at every size; negative: grid-stride kernels) */
     int plane_cells;     /* plane-marching slab capacity in cells: 256, 512, 768 or 1024 (default 1024) */
     int plane_blocks_per_sm; /* plane-marching work items per SM (default 2) */
     int df_plane_cells;  /* MIXED: positive: the double-float CG product marches along x over slabs of

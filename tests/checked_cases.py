@@ -46,7 +46,7 @@ def main():
         delta = np.random.default_rng(k).standard_normal(c["N"])
         h_or, dK_or = oracle_pair(c, delta)
         for opts in ({"precision": "fp64"}, {"precision": "mixed"}, {"precision": "mixed", "tail_cells": -1},
-                     {"precision": "mixed", "plane_cells": 256, "df_plane_cells": 256},
+                     {"precision": "mixed", "plane": 2}, {"precision": "mixed", "plane": 2, "plane_cells": 256},
                      {"precision": "mixed", "tail_cluster": 8}):
             P = pkg.GroundwaterProblem(c["nb"], c["aol"], c["dn"], N=c["N"], reltol=1e-12, **opts)
             h = P.forward(c["Ks"], c["dh"], c["Qs"])

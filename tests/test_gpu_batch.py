@@ -33,13 +33,15 @@ def _oracle(orc, pkg, c):
     return h, orc.logk_to_faces_vjp(nb, c["logK"], dKs)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_uneven_batch_vs_oracle(gpu_lib, orc, precision):
+@pytest.mark.parametrize("precision,plane", [("fp64", 1), ("mixed", 1), ("mixed", 2)])
+def test_uneven_batch_vs_oracle(gpu_lib, orc, precision, plane):
+    """plane=2 forces the plane-marching smoothers at these small sizes (by default a handle this
+    small runs the grid-stride ones)."""
     pkg = gpu_lib
     shapes = [(20, 16, 5), (9, 9, 9), (40, 30, 6), (3, 4, 2), (25, 25, 4), (17, 5, 11)]
     probs = [_problem(pkg, ns, 11 + k) for k, ns in enumerate(shapes)]
     B = pkg.GroundwaterBatch([p["ns"] for p in probs], [p["mins"] for p in probs], [p["maxs"] for p in probs],
-                             [p["dn"] for p in probs], reltol=1e-11, precision=precision)
+                             [p["dn"] for p in probs], reltol=1e-11, precision=precision, plane=plane)
     assert B.nprob == len(probs)
     cat = lambda k: np.concatenate([p[k] for p in probs])
     h, g = B.solve_grad_logk(cat("logK"), cat("dh"), cat("Qs"), [p["obs"] for p in probs])
@@ -105,7 +107,7 @@ def test_fused_and_separate_plane_passes_agree(gpu_lib, orc):
     out = {}
     for fuse in (1, -1):
         B = pkg.GroundwaterBatch([p["ns"] for p in probs], [p["mins"] for p in probs], [p["maxs"] for p in probs],
-                                 [p["dn"] for p in probs], reltol=1e-11, precision="mixed", fuse=fuse)
+                                 [p["dn"] for p in probs], reltol=1e-11, precision="mixed", fuse=fuse, plane=2)
         out[fuse] = B.solve_grad_logk(cat("logK"), cat("dh"), cat("Qs"), [p["obs"] for p in probs])
     assert rel(out[1][0], out[-1][0]) < 1e-9 and rel(out[1][1], out[-1][1]) < 1e-7
     off = np.cumsum([0] + [p["N"] for p in probs])
@@ -124,7 +126,7 @@ def test_plane_and_grid_stride_smoothers_agree(gpu_lib, precision):
     probs = [_problem(pkg, ns, 31 + k) for k, ns in enumerate(shapes)]
     cat = lambda k: np.concatenate([p[k] for p in probs])
     out = {}
-    for plane in (1, -1):
+    for plane in (2, -1):  # 2: the plane kernels also at these small sizes
         for tail in (4096, -1):
             B = pkg.GroundwaterBatch([p["ns"] for p in probs], [p["mins"] for p in probs],
                                      [p["maxs"] for p in probs], [p["dn"] for p in probs], reltol=1e-12,
@@ -232,7 +234,7 @@ def test_batch_split_into_concurrent_parts(gpu_lib, orc):
             [p["dn"] for p in probs])
     res = {}
     for streams in (1, 2, 3, 4):
-        B = pkg.GroundwaterBatch(*args, reltol=1e-12, precision="mixed", streams=streams)
+        B = pkg.GroundwaterBatch(*args, reltol=1e-12, precision="mixed", streams=streams, plane=2)
         for _ in range(2):  # the first solve of fresh parts, then a repeat on the same handles
             res[streams] = B.solve_grad_logk(cat("logK"), cat("dh"), cat("Qs"), [p["obs"] for p in probs])
         assert list(B.cell_offsets) == list(np.cumsum([0] + [p["N"] for p in probs]))
