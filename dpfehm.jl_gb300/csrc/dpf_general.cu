@@ -265,19 +265,27 @@ __global__ void kg_cheb_step(int n, CgState *st, GOp<T> A, const T *__restrict__
     }
 }
 
-// bc[I] = sum over the members i of I of (b - A x)_i
+// Restriction b_c = sum over the aggregate's members of (b - A x), in two passes: the residual of
+// every fine cell (a thread per cell, so the work is spread evenly however uneven the aggregates
+// are), then per coarse cell the sum over its members in member order. A thread per coarse cell
+// applying every member's row in turn was up to 5x slower on coarse levels of fracture networks,
+// whose large or uneven aggregates left most threads waiting on a few.
 template <typename T>
-__global__ void kg_restrict(int nc, const CgState *st, GOp<T> A, const int *__restrict__ mrp,
-                            const int *__restrict__ mci, const T *__restrict__ b, const T *__restrict__ x,
-                            T *__restrict__ bc) {
+__global__ void kg_resid(int n, const CgState *st, GOp<T> A, const T *__restrict__ b, const T *__restrict__ x,
+                         T *__restrict__ r) {
+    if (!g_active(st)) return;
+    GSTRIDE(i, n) {
+        T dg;
+        r[i] = b[i] - g_apply<T>(i, A, x[i], [&](int j) { return x[j]; }, dg);
+    }
+}
+template <typename T>
+__global__ void kg_restrict_sum(int nc, const CgState *st, const int *__restrict__ mrp, const int *__restrict__ mci,
+                                const T *__restrict__ r, T *__restrict__ bc) {
     if (!g_active(st)) return;
     GSTRIDE(I, nc) {
         T acc = 0;
-        for (int k = mrp[I]; k < mrp[I + 1]; k++) {
-            int i = mci[k];
-            T dg;
-            acc += b[i] - g_apply<T>(i, A, x[i], [&](int j) { return x[j]; }, dg);
-        }
+        for (int k = mrp[I]; k < mrp[I + 1]; k++) acc += r[mci[k]];
         bc[I] = acc;
     }
 }
@@ -1170,7 +1178,11 @@ void GeneralSolver::vcycle(const T *r, T *z) {
         }
         pre[l] = cur;
         GLevel &C = lv[l + 1];
-        { GTimer _gt(this, kname("kg_restrict", l, sizeof(T) == 4), C.n); kg_restrict<T><<<gblocks(C.n, nblocks), kBlock, 0, stream>>>(C.n, d_state, A, L.mrp, L.mci, b, cur,
+        // the fine residual in the level's Chebyshev direction buffer (d is written afresh by the
+        // first post-smoothing step), then the sums over the aggregates
+        { GTimer _gt(this, kname("kg_restrict_resid", l, sizeof(T) == 4), L.n); kg_resid<T><<<g, kBlock, 0, stream>>>(L.n, d_state, A, b, cur, d); }
+        GLAUNCH();
+        { GTimer _gt(this, kname("kg_restrict", l, sizeof(T) == 4), C.n); kg_restrict_sum<T><<<gblocks(C.n, nblocks), kBlock, 0, stream>>>(C.n, d_state, L.mrp, L.mci, d,
                                                                     (T *)C.work[2]); }
         GLAUNCH();
     }
