@@ -125,11 +125,15 @@ def run_steady(name, args, dist, rank, ws, METRIC_NAME):
     for _ in range(args.warmup):  # the host-buffer path's own warm-up
         mixed.solve_grad_logk(*[x.numpy() for x in hosts], obs, out=(hh.numpy(), hg.numpy()))
     torch.cuda.synchronize()
+    import gc
+    gc.collect()
+    gc.disable()  # no garbage-collection pass inside the wall-clock region
     t0 = time.perf_counter()
     for _ in range(args.steps):
         mixed.solve_grad_logk(*[x.numpy() for x in hosts], obs, out=(hh.numpy(), hg.numpy()))
     torch.cuda.synchronize()
     t_e2e = time.perf_counter() - t0
+    gc.enable()
     # plain FP64 GPU and accuracy against an FP64 solve at 1e-13
     plain = make("fp64", 1e-10)
     t64 = _events(torch, lambda: plain.solve_grad_logk(*d, obs), max(1, args.steps // 2), 1, flush)
