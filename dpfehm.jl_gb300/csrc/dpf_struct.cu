@@ -2356,6 +2356,15 @@ int StructBatch::read_count(int which) {
     return h_count[which];
 }
 
+int StructBatch::read_stats() {
+    CK(cudaMemcpyAsync(h_state_buf, d_state, nprob * sizeof(CgState), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(h_misc, d_factor_status, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(h_misc + 2, d_count + 2, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(h_count, d_count, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    return h_count[0];
+}
+
 // One PCG iteration (FP64 mode): q = A p, alpha; x, r update and convergence test;
 // z = M r, beta; p update.
 template <typename T>
@@ -2545,7 +2554,15 @@ void StructBatch::df_pcg(const double *b64, double *x64, double tol2) {
                                                            opt.maxiter, opt.max_outer);
     }
     LAUNCH_CHECK();
-    for (int round = 0; round < opt.max_outer && read_count(0) > 0; round++) {
+    for (int round = 0; round < opt.max_outer; round++) {
+        // the last check's outcome, read together with the statistics: when no round follows
+        // (warm-started transient steps often pass the first check), that is the solve's final
+        // synchronisation. Running round 0 without reading the first check was slower: when no
+        // problem needs it, its launches (all skipping) cost more than the synchronisation.
+        if (read_stats() <= 0) {
+            stats_fresh = true;
+            break;
+        }
         {
             KTimer _kt(this, kname("k_df_begin", 0, false), L0.all_cells);
             launch_pdl(k_df_begin, nb, kBlock, 0, stream, L0.d_desc, L0.all.d_map, d_state, r64, dfv[1], r32);
@@ -2586,17 +2603,17 @@ void StructBatch::solve(const double *b, double *x, double reltol) {
     LAUNCH_CHECK();
     CK(cudaMemsetAsync(d_factor_status + 1, 0, sizeof(int), stream));  // expired-wait word of this solve
     graph_body_kernels = 0;
+    stats_fresh = false;
     if (!mixed) {
         pcg<double>(b, x, tol2);
         stats_outer = 0;
     } else {
         df_pcg(b, x, tol2);
     }
-    // statistics, the error words and the graph passes in one synchronisation
-    CK(cudaMemcpyAsync(h_state_buf, d_state, nprob * sizeof(CgState), cudaMemcpyDeviceToHost, stream));
-    CK(cudaMemcpyAsync(h_misc, d_factor_status, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
-    CK(cudaMemcpyAsync(h_misc + 2, d_count + 2, sizeof(int), cudaMemcpyDeviceToHost, stream));
-    CK(cudaStreamSynchronize(stream));
+    // statistics, the error words and the graph passes in one synchronisation (already read when
+    // the rounds ended on reading them)
+    if (!stats_fresh) read_stats();
+    stats_fresh = false;
     if (graph_body_kernels) launches += graph_body_kernels * (long long)h_misc[2];
     CgState *hs = (CgState *)h_state_buf;
     last_status = DPF_OK;

@@ -151,6 +151,10 @@ public:
     cudaGraphExec_t loop_graph(int kind, void *x);
     void run_loop(int kind, void *x);
     int read_count(int which);
+    // the problems' states, the error words, the loop passes and the active count in one
+    // synchronisation; returns the active count
+    int read_stats();
+    bool stats_fresh = false;        // the host copies hold the solve's final statistics
 
     // configuration and sizes
     dpf_options opt;
