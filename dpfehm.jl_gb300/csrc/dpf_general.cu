@@ -1075,6 +1075,12 @@ int GeneralSolver::read_active() {
     return h_count[0];
 }
 
+bool GeneralSolver::check_due(int it) const {
+    const int check = std::max(1, opt.check_every);
+    if (it % check != 0) return false;
+    return it >= loop_hint - 2 || it % 8 == 0;
+}
+
 static unsigned gblocks(long long n, int cap) { return (unsigned)std::max(1LL, std::min((n + kBlock - 1) / kBlock, (long long)cap)); }
 
 void GeneralSolver::assemble(const double *Ks, const double *kc, int kind, const double *shift_, bool init_x) {
@@ -1230,13 +1236,15 @@ void GeneralSolver::pcg(const T *b, T *x, double tol2) {
     vcycle<T>(r, z);
     { GTimer _gt(this, kname("kg_update_p", 0, sizeof(T) == 4), n); kg_update_p<<<nblocks, kBlock, 0, stream>>>(n, d_state, z, pv); }
     GLAUNCH();
-    const int check = std::max(1, opt.check_every);
     for (int it = 1; it <= opt.maxiter + 1; it++) {
         { GTimer _gt(this, kname("kg_spmv_pq", 0, sizeof(T) == 4), n); kg_spmv_pq<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, A, pv, q); }
         GLAUNCH();
         { GTimer _gt(this, kname("kg_update_xr", 0, sizeof(T) == 4), n); kg_update_xr<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, x, r, pv, q, opt.maxiter); }
         GLAUNCH();
-        if (it % check == 0 && read_active() <= 0) return;
+        if (check_due(it) && read_active() <= 0) {
+            loop_hint = it;
+            return;
+        }
         vcycle<T>(r, z);
         { GTimer _gt(this, kname("kg_update_p", 0, sizeof(T) == 4), n); kg_update_p<<<nblocks, kBlock, 0, stream>>>(n, d_state, z, pv); }
         GLAUNCH();
@@ -1266,7 +1274,10 @@ void GeneralSolver::df_pcg(const double *b, double *x, double tol2) {
             { GTimer _gt(this, kname("kg_df_update_xr", 0, true), n); kg_df_update_xr<<<nblocks, kBlock, 0, stream>>>(n, d_state, d_count, rs, x, dfv[1], r32, dfv[2],
                                                             dfv[3], opt.maxiter); }
             GLAUNCH();
-            if (it % check == 0 && read_active() <= 0) break;
+            if ((round == 0 ? check_due(it) : it % check == 0) && read_active() <= 0) {
+                if (round == 0) loop_hint = it;
+                break;
+            }
             vcycle<float>(r32, z32);
             { GTimer _gt(this, kname("kg_df_update_p", 0, true), n); kg_df_update_p<<<nblocks, kBlock, 0, stream>>>(n, d_state, z32, dfv[2]); }
             GLAUNCH();

@@ -101,6 +101,11 @@ private:
     void adjoint_solve(const double *delta_dev);
     int finish_status();
     int read_active();
+    // whether the CG loop reads its convergence after iteration `it`: every check_every
+    // iterations, but up to two iterations before the one at which the previous solve's first
+    // round stopped (loop_hint) only every eighth, since each read is a host synchronisation
+    bool check_due(int it) const;
+    int loop_hint = 0;
     template <typename T>
     T *dev(size_t n);
     void drop(void *p);            // free an allocation made by dev() (nullptr: nothing)
