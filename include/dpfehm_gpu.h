@@ -88,7 +88,10 @@ typedef struct dpf_options {
     int max_coarse;      /* coarsen until a level has at most this many cells (default 64, <= 64) */
     int max_outer;       /* MIXED: cap on rounds, each restarted from the true FP64 residual (default 6) */
     int use_graphs;      /* capture each solve's iteration in a CUDA graph    (default 1)     */
-    int check_every;     /* convergence is read back every this many iterations (default 1)   */
+    int check_every;     /* host-driven CG loops (use_graphs = 0, and the general path): convergence is
+                            read back every this many iterations (default 1); the general path reads
+                            only every eighth until two iterations before the handle's previous solve
+                            stopped */
     int blocks_per_sm;   /* launch shape: grids hold SMs x this many 256-thread blocks (default 16) */
     int tail_cells;      /* regular grids: the multigrid levels of a problem with at most this many cells
                             run as one fused kernel per problem (default 4096; negative: off) */
