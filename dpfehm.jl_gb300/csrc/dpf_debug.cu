@@ -1,5 +1,6 @@
-// dpf_debug.cu -- test hooks: the bounded waits of the staging kernels, and the integer-only
-// 48-bit split of doubles that the assembly and the round start use.
+// dpf_debug.cu -- test hooks: the bounded waits of the staging kernels, the integer-only
+// 48-bit split of doubles that the assembly and the round start use, and the band orderings of
+// the direct solver (host code, callable without a GPU).
 //
 // dpf_debug_expired_wait runs one block whose threads wait on a shared-memory mbarrier
 // that nothing arrives on, through the same bounded wait (mbar_wait) that every staging
@@ -7,8 +8,10 @@
 // device still usable, without any kernel of a solve being made to fail.
 #include <cuda_runtime.h>
 
+#include <new>
 #include <string>
 
+#include "dpf_direct.h"
 #include "dpf_plane.cuh"
 
 namespace dpf {
@@ -92,4 +95,51 @@ extern "C" int dpf_debug_expired_wait(double *waited_ms) {
     }
     dpf::set_global_error("a bounded staging wait expired after " + std::to_string(1e-6 * (double)h_ns) + " ms");
     return DPF_TIMEOUT;
+}
+
+// The direct solver's band orderings, run on the host: perm[k] = the original row of band row k,
+// *w = the half-bandwidth the ordering gives.
+extern "C" int dpf_debug_band_order_graph(int64_t n, const int32_t *rp, const int32_t *ci, int64_t *perm,
+                                          int64_t *w) {
+    if (n < 0 || !rp || !perm || !w || n > (int64_t)1 << 30) return DPF_BAD_INPUT;
+    if (rp[0] != 0) return DPF_BAD_INPUT;
+    for (int64_t i = 0; i < n; i++)
+        if (rp[i + 1] < rp[i]) return DPF_BAD_INPUT;
+    const int64_t nnz = rp[n];
+    if (nnz > 0 && !ci) return DPF_BAD_INPUT;
+    for (int64_t e = 0; e < nnz; e++)
+        if (ci[e] < 0 || ci[e] >= n) return DPF_BAD_INPUT;
+    try {
+        std::vector<int> r(rp, rp + n + 1), c(ci, ci + nnz);
+        const dpf::BandOrder o = dpf::band_order_rcm((long long)n, r, c);
+        for (int64_t k = 0; k < n; k++) perm[k] = o.perm[k];
+        *w = o.w;
+    } catch (const std::bad_alloc &) {
+        return DPF_OOM;
+    }
+    return DPF_OK;
+}
+
+extern "C" int dpf_debug_band_order_grids(int nprob, const int32_t *dims, int64_t *perm, int64_t *w) {
+    if (nprob < 0 || (nprob > 0 && !dims) || !perm || !w) return DPF_BAD_INPUT;
+    try {
+        std::vector<std::array<int, 3>> d(nprob);
+        std::vector<long long> off(nprob);
+        long long n = 0;
+        for (int p = 0; p < nprob; p++) {
+            for (int a = 0; a < 3; a++) {
+                if (dims[3 * p + a] < 1) return DPF_BAD_INPUT;
+                d[p][a] = dims[3 * p + a];
+            }
+            off[p] = n;
+            n += (long long)d[p][0] * d[p][1] * d[p][2];
+            if (n > (1LL << 30)) return DPF_BAD_INPUT;
+        }
+        const dpf::BandOrder o = dpf::band_order_regular(d, off);
+        for (long long k = 0; k < n; k++) perm[k] = o.perm[k];
+        *w = o.w;
+    } catch (const std::bad_alloc &) {
+        return DPF_OOM;
+    }
+    return DPF_OK;
 }

@@ -372,6 +372,15 @@ int dpf_debug_expired_wait(double *waited_ms);
  * (outputs then unspecified). All outputs are device arrays of n entries. */
 int dpf_debug_split48(int64_t n, const double *v, float *hi, float *lo, double *v48, int *ok);
 
+/* No counterpart in the reference. The band orderings of the direct solver, run on the host (no
+ * device needed): for a symmetric graph in CSR form (rp[n + 1], ci, host arrays) the reverse
+ * Cuthill-McKee order; for nprob regular grids (dims[3 p .. 3 p + 2] = nx, ny, nz, cells z fastest,
+ * problems one after another) the order with each grid's two shortest axes fastest. perm[k] (n
+ * entries, host) is the original row of band row k and *w the half-bandwidth the order gives.
+ * DPF_BAD_INPUT for malformed arrays or extents. */
+int dpf_debug_band_order_graph(int64_t n, const int32_t *rp, const int32_t *ci, int64_t *perm, int64_t *w);
+int dpf_debug_band_order_grids(int nprob, const int32_t *dims, int64_t *perm, int64_t *w);
+
 /* No counterpart in the reference. In a library built with DPF_CHECK defined
  * (device-side bounds and alignment checks on cell decodes, stencil neighbours,
  * aggregates, staged copies and CSR columns; a violating access is clamped or

@@ -164,3 +164,78 @@ def test_autotune_rejects_mismatched_lists(lib, pkg):
         pkg.autotune_batch(dims, [(0, 0, 0)] * 2, [(3, 3, 3)] * 2, [[63], [63]], z, z, z, [np.array([1, 2])])
     with pytest.raises(ValueError):
         pkg.autotune_batch(dims, [(0, 0, 0)] * 2, [(3, 3, 3)] * 2, [[63]], z, z, z, [np.array([1]), np.array([2])])
+
+
+def _bandwidth(perm, edges):
+    """Half-bandwidth of the couplings `edges` (pairs of original rows) under the band order perm
+    (perm[k] = original row of band row k)."""
+    pos = np.empty(len(perm), dtype=np.int64)
+    pos[perm] = np.arange(len(perm))
+    return int(np.abs(pos[edges[:, 0]] - pos[edges[:, 1]]).max()) if len(edges) else 0
+
+
+def _grid_edges(nx, ny, nz, off):
+    """The 7-point couplings of an nx x ny x nz grid (cells z fastest) from cell offset off."""
+    idx = off + np.arange(nx * ny * nz).reshape(nx, ny, nz)
+    pairs = [np.stack([idx[1:].ravel(), idx[:-1].ravel()], 1), np.stack([idx[:, 1:].ravel(), idx[:, :-1].ravel()], 1),
+             np.stack([idx[:, :, 1:].ravel(), idx[:, :, :-1].ravel()], 1)]
+    return np.concatenate(pairs)
+
+
+@pytest.mark.parametrize("grids", [[(20, 16, 1), (9, 9, 9), (30, 4, 6)], [(7, 1, 1)], [(1, 1, 1), (3, 50, 2)],
+                                   [(200, 200, 25)]])
+def test_band_order_grids(lib, grids):
+    """The direct solver's band order for a batch of regular grids (host code, no device): a
+    permutation of all cells, each grid's two shortest axes fastest, and the half-bandwidth it
+    reports equal to the largest coupling distance, the largest product of a grid's two shorter
+    extents."""
+    dims = np.array(grids, dtype=np.int32).ravel()
+    n = int(sum(a * b * c for a, b, c in grids))
+    perm = np.empty(n, dtype=np.int64)
+    w = ctypes.c_int64(-1)
+    assert lib.dpf_debug_band_order_grids(len(grids), dims.ctypes.data, perm.ctypes.data, ctypes.byref(w)) == 0
+    assert np.array_equal(np.sort(perm), np.arange(n))
+    off, edges, expect = 0, [], 0
+    for g in grids:
+        edges.append(_grid_edges(*g, off))
+        s = sorted(g)
+        expect = max(expect, s[0] * s[1] if s[2] > 1 else 0)
+        off += g[0] * g[1] * g[2]
+    edges = np.concatenate(edges)
+    assert w.value == _bandwidth(perm, edges) == expect
+    assert lib.dpf_debug_band_order_grids(1, np.array([4, 0, 2], dtype=np.int32).ctypes.data, perm.ctypes.data,
+                                          ctypes.byref(w)) == 1
+
+
+def _csr(n, edges):
+    a = np.concatenate([edges[:, 0], edges[:, 1]])
+    b = np.concatenate([edges[:, 1], edges[:, 0]])
+    order = np.lexsort((b, a))
+    a, b = a[order], b[order]
+    rp = np.zeros(n + 1, dtype=np.int32)
+    np.add.at(rp, a + 1, 1)
+    return np.cumsum(rp).astype(np.int32), b.astype(np.int32)
+
+
+def test_band_order_graph_rcm(lib):
+    """Reverse Cuthill-McKee on a shuffled 40 x 60 grid graph with a second component and isolated
+    vertices (host code, no device): a permutation, the reported half-bandwidth equal to the
+    largest coupling distance, and a band close to the grid's short side (the shuffled labels'
+    band is thousands)."""
+    rng = np.random.default_rng(3)
+    g = _grid_edges(40, 60, 1, 0)
+    tri = np.array([[0, 1], [1, 2], [2, 0]]) + 2400           # a second component
+    n = 2400 + 3 + 5                                           # and five isolated vertices
+    lab = rng.permutation(n)
+    edges = lab[np.concatenate([g, tri])]
+    rp, ci = _csr(n, edges)
+    perm = np.empty(n, dtype=np.int64)
+    w = ctypes.c_int64(-1)
+    assert lib.dpf_debug_band_order_graph(n, rp.ctypes.data, ci.ctypes.data, perm.ctypes.data, ctypes.byref(w)) == 0
+    assert np.array_equal(np.sort(perm), np.arange(n))
+    assert w.value == _bandwidth(perm, edges)
+    assert _bandwidth(np.arange(n), edges) > 1000
+    assert 40 <= w.value <= 80
+    bad = ci.copy()
+    bad[0] = n
+    assert lib.dpf_debug_band_order_graph(n, rp.ctypes.data, bad.ctypes.data, perm.ctypes.data, ctypes.byref(w)) == 1
